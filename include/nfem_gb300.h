@@ -1,0 +1,187 @@
+/*
+ * nfem_gb300.h - C ABI of the GB300 finite-element assembly-and-solve path.
+ *
+ * Every entry point is `extern "C"`, takes plain device pointers, sizes and a
+ * cudaStream_t (passed as void*), never allocates device memory unless its
+ * comment says so, never throws, and returns an nfem_status.  Kernels are
+ * asynchronous on `stream`; conditions detected on the device (a row whose
+ * merged length disagrees with the pattern, a full hash table, a Krylov
+ * breakdown) are written to an optional device `int32_t* dev_status` word
+ * (first nonzero code wins) that the caller reads after synchronising.
+ *
+ * Index conventions: cell-to-vertex, cell-to-DoF, CSR row_ptr and col_idx are
+ * int32 (sizes are checked against 2^31 - 1); point coordinates are FP64
+ * [n_points, 3] row-major like the reference's mesh.points.
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * inside the nfempy project).
+ */
+#ifndef NFEM_GB300_H
+#define NFEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  NFEM_OK = 0,
+  NFEM_ERR_INVALID_ARG = 1,   /* bad pointer / size / enum */
+  NFEM_ERR_CUDA = 2,          /* a CUDA runtime call or launch failed */
+  NFEM_ERR_WORKSPACE = 3,     /* workspace smaller than the query returned */
+  NFEM_ERR_OVERFLOW = 4,      /* a size does not fit the index type */
+  NFEM_ERR_CAPACITY = 5,      /* a per-row buffer or hash table is full */
+  NFEM_ERR_PATTERN = 6,       /* assembled row disagrees with the CSR pattern */
+  NFEM_ERR_UNSUPPORTED = 7,   /* configuration not implemented */
+  NFEM_ERR_NOT_CONVERGED = 8, /* Krylov iteration cap reached */
+  NFEM_ERR_BREAKDOWN = 9,     /* Krylov breakdown (zero or non-finite denominator) */
+  NFEM_ERR_NONFINITE = 10,    /* NaN / Inf detected in an input or residual */
+  NFEM_ERR_DEGENERATE = 11    /* a cell with |det J| == 0 */
+} nfem_status;
+
+typedef enum { NFEM_F64 = 0, NFEM_F32 = 1 } nfem_value_type;
+
+/* Coefficient sampling modes for per-cell data arrays. */
+typedef enum {
+  NFEM_COEF_NONE = 0,      /* absent (treated as zero) */
+  NFEM_COEF_CELL = 1,      /* one value per cell, [n_cells] */
+  NFEM_COEF_QPOINT = 2     /* one value per quadrature point, [n_cells, n_qp] */
+} nfem_coef_mode;
+
+/* ------------------------------------------------------------------ misc */
+int nfem_abi_version(void);
+const char* nfem_status_string(int status);
+
+/* Exclusive prefix sum of n int32 counts into n + 1 int64 offsets. */
+int nfem_scan_workspace_bytes(int64_t n, size_t* bytes);
+int nfem_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offsets,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* --------------------------------------- K0: entity numbering (a1, a2, a8)
+ * Replaces Mesh.build_conformal_mesh + insert_* (src/mesh/mesh.py:125-339),
+ * the first-appearance entity order of MeshTopology
+ * (src/mesh/mesh_topology.py:16-35 via src/mesh/mesh.py:639-681) and the
+ * orientation checks of src/basis/permute_and_transform.py:8-107.
+ *
+ * For every (cell, local sub-entity of dimension entity_dim) occurrence,
+ * writes the rank of its global entity in first-appearance order over the
+ * cells (cells in the given order, sub-entities in the reference's local
+ * order).  entity_dim must be 0, 1 or 2 and < cell_dim.  When entity_dim ==
+ * cell_dim - 1 and `flags` is non-NULL, also writes per occurrence:
+ *   bit0 = reflected  (2-D: local edge order differs from the stored edge
+ *                      order; 3-D: the face's global tags are an odd
+ *                      permutation of sorted order)
+ *   bit1 = tagged     (the facet appears in the boundary facet block)
+ * `facets` [n_facets, cell_dim] are the tagged lower-dimensional cells in file
+ * order; facets_first != 0 means that block precedes the cells in the file
+ * (it then fixes the stored node order of those edges).
+ * n_entities_out is a device int64.
+ */
+int nfem_numbering_workspace_bytes(int64_t n_cells, int cell_dim, int entity_dim,
+                                   int64_t n_points, int64_t n_facets, size_t* bytes);
+int nfem_number_entities(const int32_t* cell_vertices, int64_t n_cells, int cell_dim,
+                         int entity_dim, int64_t n_points, const int32_t* facets,
+                         int64_t n_facets, int facets_first, void* workspace,
+                         size_t workspace_bytes, int32_t* occ_rank, uint8_t* flags,
+                         int64_t* n_entities_out, void* stream);
+
+/* Packs the RT1 orientation sign of each local facet into one byte per cell
+ * (bit i set = basis function i negated), applying the reference rule
+ * (src/basis/permute_and_transform.py:57-107 for 3-D, :8-35 for 2-D). */
+int nfem_rt1_sign_mask(const uint8_t* facet_flags, int64_t n_cells, int cell_dim,
+                       uint8_t* sign_mask, void* stream);
+
+/* ------------------------------------------------------ K0: DoF map (a3, a4)
+ * Replaces DoFMap.build_entity_maps / destination_indices
+ * (src/spaces/dof_map.py:38-146) and ProductSpace.destination_indexes
+ * (src/spaces/product_space.py:147-170).  Blocks are concatenated in order;
+ * block b contributes, for each local entity e < n_ent and j < width, the DoF
+ * base + rank(c, e) * width + j (rank = cell index when occ_rank is NULL). */
+typedef struct {
+  const int32_t* occ_rank; /* [n_cells, n_ent] or NULL for the cell block */
+  int32_t n_ent;           /* local entities of this dimension per cell */
+  int32_t width;           /* e_dofs * n_comp */
+  int64_t base;            /* first global DoF of the block */
+} nfem_dof_block;
+
+#define NFEM_MAX_DOF_BLOCKS 16
+int nfem_compose_cell_dofs(int64_t n_cells, int n_blocks, const nfem_dof_block* blocks,
+                           int32_t* cell_dofs, int ld, void* stream);
+
+/* ------------------------------------------------ K0: CSR pattern (a15)
+ * Replaces the sparsity that PETSc builds from the per-entry setValue calls
+ * of src/assembly/ScatterFormData.py:5-11 ("pattern A": every entry of every
+ * element clique, zeros included, columns sorted per row).
+ *
+ * Step 1 (rows): row incidence lists (cell * n_loc + local, sorted per row)
+ * and row lengths.  inc_ptr [n_rows + 1], inc [n_cells * n_loc] (int32),
+ * row_ptr [n_rows + 1] (int32).  *nnz_host receives the total (the call
+ * synchronises on `stream` to read it back).
+ * Step 2 (cols): col_idx [nnz].
+ * Optional slot map: slots [n_cells, n_loc, n_loc] = position of each element
+ * entry in the CSR value array. */
+int nfem_pattern_workspace_bytes(int64_t n_cells, int n_loc, int64_t n_rows, size_t* bytes);
+int nfem_pattern_rows(const int32_t* cell_dofs, int64_t n_cells, int n_loc, int ld,
+                      int64_t n_rows, void* workspace, size_t workspace_bytes,
+                      int32_t* inc_ptr, int32_t* inc, int32_t* row_ptr,
+                      int64_t* nnz_host, int32_t* dev_status, void* stream);
+int nfem_pattern_cols(const int32_t* cell_dofs, int64_t n_cells, int n_loc, int ld,
+                      int64_t n_rows, const int32_t* inc_ptr, const int32_t* inc,
+                      const int32_t* row_ptr, int32_t* col_idx, int32_t* dev_status,
+                      void* stream);
+int nfem_pattern_slots(const int32_t* cell_dofs, int64_t n_cells, int n_loc, int ld,
+                       const int32_t* row_ptr, const int32_t* col_idx, int32_t* slots,
+                       int32_t* dev_status, void* stream);
+
+/* Compressed slot map for short rows: per incidence entry k of row r (cell c,
+ * local a), codes[k] packs, 4 bits per local column b (n_loc <= 8, rows of at
+ * most 16 entries), the position of cell_dofs[c, b] inside row r relative to
+ * row_ptr[r].  Used by the row-owner assembly kernels. */
+int nfem_pattern_local_codes(const int32_t* cell_dofs, int64_t n_cells, int n_loc, int ld,
+                             int64_t n_rows, const int32_t* inc_ptr, const int32_t* inc,
+                             const int32_t* row_ptr, const int32_t* col_idx, uint32_t* codes,
+                             int32_t* dev_status, void* stream);
+
+/* Splits FP64 points into float hi/lo pairs [n_points, 6] = (hi xyz, lo xyz)
+ * so FP32 kernels form cell edge vectors without FP64 arithmetic. */
+int nfem_points_split(const double* points, int64_t n_points, float* points_split,
+                      void* stream);
+
+/* --------------------------- K1-K4: mixed Darcy RT1 x P0 (a6-a10, a15)
+ * Replaces LaplaceDualWeakForm.evaluate_form
+ * (src/weak_forms/laplace_dual_weak_form.py:10-86) for every cell together
+ * with the scatter of src/assembly/ScatterFormData.py:5-25: writes the CSR
+ * values of the global Jacobian (pattern from nfem_pattern_*) and the global
+ * residual at alpha = 0, r = -int f w on pressure rows, 0 on flux rows.
+ *
+ * Geometry: affine simplices, contravariant Piola with |det J|, orientation
+ * signs from nfem_rt1_sign_mask.  kappa is one value per cell; source is per
+ * cell or per quadrature point of the rule `2*1+1` (collapsed Gauss-Jacobi,
+ * 4 points on triangles, 8 on tetrahedra; ordering as in the reference).
+ * value_type selects FP64 (coordinates `points`) or FP32 (coordinates
+ * `points_split` from nfem_points_split); kappa/source/values/rhs then have
+ * that type.  flux_dofs [n_cells, dim + 1] are the RT1 DoFs, the pressure DoF
+ * of cell c is p_base + c.  qweights (host, n_qp entries) are the reference
+ * quadrature weights, read only when source_mode == NFEM_COEF_QPOINT.
+ * inc_ptr/inc/codes come from nfem_pattern_rows / nfem_pattern_local_codes
+ * with cell_dofs = [flux_dofs | p_base + c].  accumulate == 0 overwrites
+ * values/rhs (the first form of an assembly pass, like a zeroed PETSc Mat
+ * and residual); accumulate != 0 adds to them (setValue(addv=True)).  Each CSR value and residual entry is written once
+ * (row-owner gather; no atomics, deterministic). */
+int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t n_rows,
+                              const double* points, const float* points_split,
+                              const int32_t* cell_vertices, const int32_t* flux_dofs,
+                              int64_t p_base, const uint8_t* sign_mask,
+                              const void* kappa, const void* source, int source_mode,
+                              const double* qweights, int n_qp,
+                              const int32_t* inc_ptr, const int32_t* inc,
+                              const uint32_t* codes, const int32_t* row_ptr,
+                              void* values, void* rhs, int accumulate,
+                              int32_t* dev_status, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NFEM_GB300_H */

@@ -1,0 +1,108 @@
+"""ctypes binding of libnfem_gb300.so (the C ABI declared in include/nfem_gb300.h).
+
+The library is required: every compute entry point of the package goes
+through it, and importing a function from here raises when the library is
+missing.  There is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnfem_gb300.so")
+
+NFEM_OK = 0
+NFEM_F64 = 0
+NFEM_F32 = 1
+COEF_NONE, COEF_CELL, COEF_QPOINT = 0, 1, 2
+
+STATUS_NAMES = {
+    0: "NFEM_OK", 1: "NFEM_ERR_INVALID_ARG", 2: "NFEM_ERR_CUDA", 3: "NFEM_ERR_WORKSPACE",
+    4: "NFEM_ERR_OVERFLOW", 5: "NFEM_ERR_CAPACITY", 6: "NFEM_ERR_PATTERN", 7: "NFEM_ERR_UNSUPPORTED",
+    8: "NFEM_ERR_NOT_CONVERGED", 9: "NFEM_ERR_BREAKDOWN", 10: "NFEM_ERR_NONFINITE",
+    11: "NFEM_ERR_DEGENERATE",
+}
+
+
+class NfemError(RuntimeError):
+    def __init__(self, status, where=""):
+        self.status = int(status)
+        name = STATUS_NAMES.get(self.status, str(status))
+        super().__init__(f"{where}: {name}" if where else name)
+
+
+class DofBlock(C.Structure):
+    _fields_ = [("occ_rank", C.c_void_p), ("n_ent", C.c_int32), ("width", C.c_int32), ("base", C.c_int64)]
+
+
+_P = C.c_void_p
+_I = C.c_int
+_I64 = C.c_int64
+_SZ = C.c_size_t
+
+_SIGS = {
+    "nfem_abi_version": ([], _I),
+    "nfem_status_string": ([_I], C.c_char_p),
+    "nfem_scan_workspace_bytes": ([_I64, C.POINTER(_SZ)], _I),
+    "nfem_exclusive_scan": ([_P, _I64, _P, _P, _SZ, _P], _I),
+    "nfem_numbering_workspace_bytes": ([_I64, _I, _I, _I64, _I64, C.POINTER(_SZ)], _I),
+    "nfem_number_entities": ([_P, _I64, _I, _I, _I64, _P, _I64, _I, _P, _SZ, _P, _P, _P, _P], _I),
+    "nfem_rt1_sign_mask": ([_P, _I64, _I, _P, _P], _I),
+    "nfem_compose_cell_dofs": ([_I64, _I, C.POINTER(DofBlock), _P, _I, _P], _I),
+    "nfem_pattern_workspace_bytes": ([_I64, _I, _I64, C.POINTER(_SZ)], _I),
+    "nfem_pattern_rows": ([_P, _I64, _I, _I, _I64, _P, _SZ, _P, _P, _P, C.POINTER(_I64), _P, _P], _I),
+    "nfem_pattern_cols": ([_P, _I64, _I, _I, _I64, _P, _P, _P, _P, _P, _P], _I),
+    "nfem_pattern_slots": ([_P, _I64, _I, _I, _P, _P, _P, _P, _P], _I),
+    "nfem_pattern_local_codes": ([_P, _I64, _I, _I, _I64, _P, _P, _P, _P, _P, _P, _P], _I),
+    "nfem_points_split": ([_P, _I64, _P, _P], _I),
+    "nfem_darcy_rt1p0_assemble": ([_I, _I, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P, _P, _I,
+                                   _P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P], _I),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library once; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NfemError(-1, f"{LIB_PATH} is missing: run nfempy_gb300.build.build() (nvcc, sm_103a)")
+        h = C.CDLL(LIB_PATH)
+        for name, (args, res) in _SIGS.items():
+            f = getattr(h, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = h
+    return _lib
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def call(name, *args):
+    rc = getattr(lib(), name)(*args)
+    if rc != NFEM_OK:
+        raise NfemError(rc, name)
+    return rc
+
+
+def ptr(t):
+    """Raw device pointer of a tensor (None -> NULL)."""
+    if t is None:
+        return None
+    return C.c_void_p(t.data_ptr())
+
+
+def stream_ptr(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def require_cuda(t, what):
+    if not t.is_cuda:
+        raise ValueError(f"{what} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError(f"{what} must be contiguous")

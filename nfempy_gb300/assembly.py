@@ -1,0 +1,274 @@
+"""Device assembly behind the reference's WeakForm / SequentialAssembler API.
+
+  * CSRMatrix        - stands where the reference passes a PETSc Mat
+                       (setValue(addv=True) target, then assemble()); holds the
+                       element-clique sparsity pattern built on the GPU
+                       (nfem_pattern_rows/cols) and the values on the device.
+  * LaplaceDualWeakForm - mixed Darcy RT1 x P0
+                       (src/weak_forms/laplace_dual_weak_form.py:10-86);
+                       all cells are assembled by one fused kernel
+                       (nfem_darcy_rt1p0_assemble).
+  * SequentialAssembler - same constructor and form_to_input_list /
+                       scatter_forms as src/assembly/SequentialAssembler.py:13-86.
+
+Coefficients: the reference calls Python functions at every quadrature point.
+Here a function is sampled once on the host at the physical quadrature points
+(kappa must then be constant on each cell), or the caller passes per-cell
+arrays directly (numpy or torch, host or device).
+"""
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .elements import lagrange_p1_values
+
+
+class CSRMatrix:
+    """Global sparse matrix on the device with the pattern of a space's element cliques."""
+
+    def __init__(self, space, dtype=torch.float64, codes=True, stream=None):
+        if space.cell_dofs is None:
+            raise ValueError("build_structures() the space first")
+        self.space = space
+        self.dtype = dtype
+        self.n_rows = space.n_dof + space.dof_shift
+        dev = space.device
+        st = _lib.stream_ptr(stream)
+        T, n_loc = space.n_cells, space.n_loc
+        ws_b = _lib.C.c_size_t(0)
+        _lib.call("nfem_pattern_workspace_bytes", T, n_loc, self.n_rows, _lib.C.byref(ws_b))
+        ws = torch.empty(int(ws_b.value), dtype=torch.uint8, device=dev)
+        self.inc_ptr = torch.empty(self.n_rows + 1, dtype=torch.int32, device=dev)
+        self.inc = torch.empty(T * n_loc, dtype=torch.int32, device=dev)
+        self.row_ptr = torch.empty(self.n_rows + 1, dtype=torch.int32, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        nnz = _lib.C.c_int64(0)
+        _lib.call("nfem_pattern_rows", _lib.ptr(space.cell_dofs), T, n_loc, n_loc, self.n_rows, _lib.ptr(ws),
+                  ws.numel(), _lib.ptr(self.inc_ptr), _lib.ptr(self.inc), _lib.ptr(self.row_ptr),
+                  _lib.C.byref(nnz), _lib.ptr(self.status), st)
+        self.nnz = int(nnz.value)
+        self.col_idx = torch.empty(max(self.nnz, 1), dtype=torch.int32, device=dev)
+        _lib.call("nfem_pattern_cols", _lib.ptr(space.cell_dofs), T, n_loc, n_loc, self.n_rows,
+                  _lib.ptr(self.inc_ptr), _lib.ptr(self.inc), _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
+                  _lib.ptr(self.status), st)
+        self.codes = None
+        if codes and n_loc <= 8:
+            self.codes = torch.empty(T * n_loc, dtype=torch.int32, device=dev)
+            _lib.call("nfem_pattern_local_codes", _lib.ptr(space.cell_dofs), T, n_loc, n_loc, self.n_rows,
+                      _lib.ptr(self.inc_ptr), _lib.ptr(self.inc), _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
+                      _lib.ptr(self.codes), _lib.ptr(self.status), st)
+        self.values = torch.zeros(max(self.nnz, 1), dtype=dtype, device=dev)
+        self.fresh = True
+        self.check_status("pattern")
+
+    def check_status(self, where=""):
+        s = int(self.status.item())
+        if s:
+            self.status.zero_()
+            raise _lib.NfemError(s, where)
+
+    # PETSc-like surface used by the drivers
+    def zeroEntries(self):
+        self.fresh = True
+
+    def assemble(self):
+        self.check_status("assemble")
+
+    def getSize(self):
+        return (self.n_rows, self.n_rows)
+
+    def getInfo(self):
+        return {"nz_allocated": self.nnz, "nz_used": self.nnz, "nz_unneeded": 0}
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.values[: self.nnz].double().cpu().numpy(),
+                              self.col_idx[: self.nnz].cpu().numpy(), self.row_ptr.cpu().numpy()),
+                             shape=(self.n_rows, self.n_rows))
+
+
+def _to_device(x, dtype, device, n):
+    t = torch.as_tensor(x)
+    t = t.to(device=device, dtype=dtype).reshape(-1).contiguous()
+    if t.numel() == 1 and n > 1:
+        t = t.expand(n).contiguous()
+    return t
+
+
+class WeakForm:
+    """Base with the reference's attributes (src/weak_forms/weak_from.py:6-29)."""
+
+    def __init__(self, space):
+        self.space = space
+        self._functions = None
+
+    @property
+    def functions(self):
+        return self._functions
+
+    @functions.setter
+    def functions(self, functions):
+        self._functions = functions
+        self._cache = {}
+
+    def quadrature_points(self):
+        """Physical quadrature points [T, Q, 3] (host float64)."""
+        sp = self.space
+        pts, _ = sp.quadrature[sp.dim]
+        lam = lagrange_p1_values(sp.dim, pts)  # [Q, d+1]
+        X = sp.mesh.points[sp.cells_host]  # [T, d+1, 3]
+        return np.einsum("qv,tvg->tqg", lam, X)
+
+
+class LaplaceDualWeakForm(WeakForm):
+    """Mixed Darcy RT1 x P0 on triangles or tetrahedra; fields "u" (RT, k=1) and
+    "p" (Lagrange, k=0, discontinuous), in that order.
+
+    functions: "kappa" - scalar, per-cell array [T], or f(x, y, z) constant per cell;
+               "rhs"   - None, scalar, per-cell array [T], per-quadrature-point
+                         array [T, Q], or f(x, y, z) -> [1, N] (sampled at the
+                         quadrature points).
+    """
+
+    def _check_space(self):
+        sp = self.space
+        if sp is None or self.functions is None:
+            raise ValueError
+        if sp.names[:2] != ["u", "p"] or len(sp.names) != 2:
+            raise NotImplementedError("LaplaceDualWeakForm expects fields ('u', 'p') in that order")
+        u, p = sp.discrete_spaces["u"], sp.discrete_spaces["p"]
+        if not (u.family == "RT" and u.k_order == 1 and u.n_comp == 1 and not u.discontinuous):
+            raise NotImplementedError("flux space must be continuous RT1 with one component")
+        if not (p.family == "Lagrange" and p.k_order == 0 and p.n_comp == 1):
+            raise NotImplementedError("pressure space must be P0 with one component")
+
+    def coefficients(self, dtype):
+        """(kappa [T], source, source_mode) on the device in `dtype`."""
+        key = ("coef", dtype)
+        if key in self._cache:
+            return self._cache[key]
+        sp = self.space
+        T = sp.n_cells
+        dev = sp.device
+        kappa = self.functions["kappa"]
+        xq = None
+        if callable(kappa):
+            xq = self.quadrature_points()
+            kv = np.asarray(kappa(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).reshape(T, -1)
+            if np.abs(kv - kv[:, :1]).max() > 1e-14 * max(1.0, np.abs(kv).max()):
+                raise NotImplementedError("kappa must be constant on each cell")
+            kappa = kv[:, 0]
+        kt = _to_device(kappa, dtype, dev, T)
+        rhs = self.functions.get("rhs")
+        mode = _lib.COEF_NONE
+        st = None
+        if callable(rhs):
+            xq = self.quadrature_points() if xq is None else xq
+            fv = np.asarray(rhs(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64)
+            fv = fv.reshape(-1, T, xq.shape[1])[0]
+            st = _to_device(fv, dtype, dev, T * xq.shape[1])
+            mode = _lib.COEF_QPOINT
+        elif rhs is not None:
+            r = torch.as_tensor(rhs)
+            if r.numel() == 1:
+                st = _to_device(r, dtype, dev, T)
+                mode = _lib.COEF_CELL
+            elif r.numel() == T:
+                st = _to_device(r, dtype, dev, T)
+                mode = _lib.COEF_CELL
+            else:
+                st = _to_device(r, dtype, dev, r.numel())
+                mode = _lib.COEF_QPOINT
+        self._cache[key] = (kt, st, mode)
+        return self._cache[key]
+
+    def assemble(self, jacobian, residual, accumulate=False, stream=None, coefficients=None):
+        """Assemble every cell into `jacobian` (CSRMatrix) and `residual` (device tensor)."""
+        self._check_space()
+        sp = self.space
+        dtype = jacobian.dtype
+        vt = _lib.NFEM_F64 if dtype == torch.float64 else _lib.NFEM_F32
+        if residual.dtype != dtype or not residual.is_cuda:
+            raise ValueError("residual must be a CUDA tensor of the matrix dtype")
+        if jacobian.codes is None:
+            raise NotImplementedError("matrix built without slot codes")
+        kt, st, mode = coefficients if coefficients is not None else self.coefficients(dtype)
+        pts, wts = sp.quadrature[sp.dim]
+        qw = (_lib.C.c_double * len(wts))(*wts.tolist())
+        _lib.call("nfem_darcy_rt1p0_assemble", sp.dim, vt, sp.n_cells, jacobian.n_rows,
+                  _lib.ptr(sp.points), _lib.ptr(sp.points_split), _lib.ptr(sp.cells), None,
+                  sp.field_offsets["p"], _lib.ptr(sp.rt_sign_mask), _lib.ptr(kt), _lib.ptr(st), mode,
+                  _lib.C.cast(qw, _lib.C.c_void_p), len(wts), _lib.ptr(jacobian.inc_ptr), _lib.ptr(jacobian.inc), _lib.ptr(jacobian.codes),
+                  _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate),
+                  _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+
+    def evaluate_form(self, element_index, alpha):
+        raise NotImplementedError(
+            "per-cell evaluation is not offered on the device; assemble with SequentialAssembler")
+
+
+class SequentialAssembler:
+    """Drop-in for src/assembly/SequentialAssembler.py:13-86 with device forms.
+
+    `jacobian` is a CSRMatrix; `residual` a device tensor (or a host numpy
+    array, updated in place with a device->host copy at the end).  A call to
+    scatter_forms() is one assembly pass: the first form overwrites the
+    matrix values and the residual (they are treated as zeroed, as every
+    reference driver creates them), later forms of the pass add to them.
+    """
+
+    def __init__(self, space, jacobian, residual):
+        self.space = space
+        self.jacobian = jacobian
+        self.residual = residual
+        self._form_to_input_list = None
+
+    @property
+    def form_type_to_callable_map(self):
+        return {"form": self._scatter_form}
+
+    @property
+    def form_to_input_list(self):
+        return self._form_to_input_list
+
+    @form_to_input_list.setter
+    def form_to_input_list(self, v):
+        self._form_to_input_list = v
+
+    def _scatter_form(self, form, sequence, alpha, residual, accumulate):
+        n = self.space.n_cells
+        seq = range(n) if sequence is None else sequence
+        if not (isinstance(seq, range) and seq.start == 0 and seq.stop == n and seq.step == 1):
+            if not np.array_equal(np.asarray(list(seq)), np.arange(n)):
+                raise NotImplementedError("device assembly covers all cells of the space in one pass")
+        if alpha is not None and np.any(np.asarray(alpha.cpu() if torch.is_tensor(alpha) else alpha) != 0):
+            raise NotImplementedError("linear forms are assembled at alpha = 0 (one Newton step)")
+        form.assemble(self.jacobian, residual, accumulate=accumulate)
+
+    def scatter_forms(self, measure_time_q=False):
+        host_res = None
+        residual = self.residual
+        if not torch.is_tensor(residual):
+            host_res = residual
+            residual = torch.zeros(self.jacobian.n_rows, dtype=self.jacobian.dtype, device=self.space.device)
+        accumulate = not self.jacobian.fresh
+        first = True
+        for name, input_list in self.form_to_input_list.items():
+            if measure_time_q:
+                torch.cuda.synchronize()
+                st = time.time()
+            form_type = input_list[0]
+            if form_type not in self.form_type_to_callable_map:
+                raise NotImplementedError(f"form type {form_type}")
+            _, sequence, form, alpha = input_list[:4]
+            self._scatter_form(form, sequence, alpha, residual, accumulate or not first)
+            first = False
+            if measure_time_q:
+                torch.cuda.synchronize()
+                print("SequentialAssembler:: Weak form: ", name)
+                print("SequentialAssembler:: Scatter time:", time.time() - st, "seconds")
+        self.jacobian.fresh = False
+        if host_res is not None:
+            host_res += residual.double().cpu().numpy()

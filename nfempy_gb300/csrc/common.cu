@@ -1,0 +1,187 @@
+// ABI helpers, device prefix scan, coordinate split.
+#include "nfem_common.cuh"
+
+namespace nfem {
+
+static int g_num_sms = 0;
+
+int grid_for(int64_t n_items, int block, int blocks_per_sm) {
+  if (g_num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 152;
+  }
+  int64_t need = ceil_div(n_items, block);
+  int64_t cap = int64_t(g_num_sms) * blocks_per_sm;
+  if (need < 1) need = 1;
+  return int(need < cap ? need : cap);
+}
+
+// ---------------------------------------------------------------- scan
+// Three passes over tiles of kScanTile counts: tile sums, a single-block scan
+// of the tile sums, then per-tile scans offset by the scanned sums.
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int64_t block_exclusive_scan(int64_t v, int64_t* smem, int64_t* total) {
+  // warp-level inclusive scan, then scan of warp totals
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    int64_t w = lane < nw ? smem[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int64_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nw) smem[lane] = w;
+  }
+  __syncthreads();
+  int64_t warp_prefix = warp > 0 ? smem[warp - 1] : 0;
+  if (total) *total = smem[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return warp_prefix + x - v;
+}
+
+__global__ void scan_tile_sums(const int32_t* __restrict__ in, int64_t n, int64_t* __restrict__ sums) {
+  __shared__ int64_t smem[32];
+  const int64_t base = int64_t(blockIdx.x) * kScanTile;
+  int64_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = base + int64_t(k) * kScanThreads + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+  int64_t total;
+  block_exclusive_scan(s, smem, &total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void scan_sums_single(int64_t* __restrict__ sums, int64_t n_tiles, int64_t* __restrict__ out_total) {
+  __shared__ int64_t smem[32];
+  int64_t carry = 0;
+  for (int64_t b = 0; b < n_tiles; b += blockDim.x) {
+    int64_t i = b + threadIdx.x;
+    int64_t v = i < n_tiles ? sums[i] : 0;
+    int64_t total;
+    int64_t ex = block_exclusive_scan(v, smem, &total);
+    if (i < n_tiles) sums[i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) *out_total = carry;
+}
+
+__global__ void scan_tiles(const int32_t* __restrict__ in, int64_t n, const int64_t* __restrict__ sums,
+                           int64_t* __restrict__ out) {
+  __shared__ int64_t smem[32];
+  const int64_t base = int64_t(blockIdx.x) * kScanTile;
+  // each thread owns kScanItems consecutive items
+  int32_t v[kScanItems];
+  int64_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = base + int64_t(threadIdx.x) * kScanItems + k;
+    v[k] = i < n ? in[i] : 0;
+    s += v[k];
+  }
+  int64_t ex = block_exclusive_scan(s, smem, nullptr) + sums[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = base + int64_t(threadIdx.x) * kScanItems + k;
+    if (i < n) out[i] = ex;
+    ex += v[k];
+  }
+}
+
+size_t scan_workspace_bytes(int64_t n) {
+  int64_t tiles = ceil_div(n > 0 ? n : 1, kScanTile);
+  return align256(size_t(tiles) * sizeof(int64_t)) + 256;
+}
+
+int exclusive_scan_i32(const int32_t* in, int64_t n, int64_t* out, void* ws, size_t ws_bytes,
+                       cudaStream_t stream) {
+  if (n < 0 || !out) return NFEM_ERR_INVALID_ARG;
+  if (ws_bytes < scan_workspace_bytes(n) || !ws) return NFEM_ERR_WORKSPACE;
+  if (n == 0) {
+    NFEM_TRY_CUDA(cudaMemsetAsync(out, 0, sizeof(int64_t), stream));
+    return NFEM_OK;
+  }
+  int64_t tiles = ceil_div(n, kScanTile);
+  if (tiles > INT32_MAX) return NFEM_ERR_OVERFLOW;
+  int64_t* sums = reinterpret_cast<int64_t*>(ws);
+  scan_tile_sums<<<unsigned(tiles), kScanThreads, 0, stream>>>(in, n, sums);
+  NFEM_CHECK_LAUNCH();
+  scan_sums_single<<<1, 1024, 0, stream>>>(sums, tiles, out + n);
+  NFEM_CHECK_LAUNCH();
+  scan_tiles<<<unsigned(tiles), kScanThreads, 0, stream>>>(in, n, sums, out);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+// ---------------------------------------------------------------- split
+__global__ void split_points_kernel(const double* __restrict__ p, int64_t n, float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double x = p[i * 3 + k];
+      float hi = __double2float_rn(x);
+      float lo = __double2float_rn(x - double(hi));
+      out[i * 6 + k] = hi;
+      out[i * 6 + 3 + k] = lo;
+    }
+  }
+}
+
+}  // namespace nfem
+
+using namespace nfem;
+
+extern "C" int nfem_abi_version(void) { return 1; }
+
+extern "C" const char* nfem_status_string(int s) {
+  switch (s) {
+    case NFEM_OK: return "ok";
+    case NFEM_ERR_INVALID_ARG: return "invalid argument";
+    case NFEM_ERR_CUDA: return "CUDA runtime error";
+    case NFEM_ERR_WORKSPACE: return "workspace too small";
+    case NFEM_ERR_OVERFLOW: return "size does not fit the index type";
+    case NFEM_ERR_CAPACITY: return "per-row buffer or hash table full";
+    case NFEM_ERR_PATTERN: return "assembled row disagrees with the CSR pattern";
+    case NFEM_ERR_UNSUPPORTED: return "unsupported configuration";
+    case NFEM_ERR_NOT_CONVERGED: return "Krylov iteration cap reached";
+    case NFEM_ERR_BREAKDOWN: return "Krylov breakdown";
+    case NFEM_ERR_NONFINITE: return "non-finite value";
+    case NFEM_ERR_DEGENERATE: return "degenerate cell (|det J| == 0)";
+    default: return "unknown status";
+  }
+}
+
+extern "C" int nfem_scan_workspace_bytes(int64_t n, size_t* bytes) {
+  if (!bytes || n < 0) return NFEM_ERR_INVALID_ARG;
+  *bytes = scan_workspace_bytes(n);
+  return NFEM_OK;
+}
+
+extern "C" int nfem_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offsets, void* ws,
+                                   size_t ws_bytes, void* stream) {
+  if (n > 0 && !counts) return NFEM_ERR_INVALID_ARG;
+  return exclusive_scan_i32(counts, n, offsets, ws, ws_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int nfem_points_split(const double* points, int64_t n_points, float* out, void* stream) {
+  if (n_points < 0 || (n_points > 0 && (!points || !out))) return NFEM_ERR_INVALID_ARG;
+  if (n_points == 0) return NFEM_OK;
+  split_points_kernel<<<grid_for(n_points, 256), 256, 0, (cudaStream_t)stream>>>(points, n_points, out);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}

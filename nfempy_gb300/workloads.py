@@ -1,0 +1,41 @@
+"""Benchmark workloads (synthetic inputs with the named sizes).
+
+darcy3d(n): unit cube, n^3 hexahedra x 6 Kuhn tetrahedra, RT1 x P0,
+  log K from a Gaussian random field (correlation length 0.05, sigma 2.0,
+  sampled at cell centroids), source f = 1 per cell.  n = 64 gives
+  1,572,864 tets, 4,743,168 DoF, nnz 36,200,448.
+darcy2d(n): unit square, n x n squares x 2 triangles, RT1 x P0, K = 1,
+  f = 2 pi^2 sin(pi x) sin(pi y) at the quadrature points (n = 32: 2,048
+  triangles, 5,184 DoF).
+Seeds: 20261203 + configuration index.
+"""
+import numpy as np
+
+from . import meshes
+from .spaces import Mesh, ProductSpace
+
+SEED = 20261203
+
+
+def darcy_space(mesh_dict, dof_shift=0, device=None):
+    dim = mesh_dict["dim"]
+    mesh = Mesh(dim, data=mesh_dict)
+    sp = ProductSpace({"u": (dim, 1, "RT", 1, mesh), "p": (dim, 1, "Lagrange", 0, mesh)}, device=device)
+    sp.make_subspaces_discontinuous({"u": False, "p": True})
+    sp.dof_shift = dof_shift
+    sp.build_structures({"u": [1], "p": [1]}, {})
+    return sp
+
+
+def darcy3d_coefficients(mesh_dict, corr_len=0.05, sigma=2.0, seed=SEED + 5):
+    cells = mesh_dict["blocks"][-1][1]
+    centroids = mesh_dict["points"][cells].mean(axis=1)
+    logk = meshes.grf_log_field(centroids, corr_len, sigma, seed)
+    return np.exp(logk), np.ones(cells.shape[0])
+
+
+def darcy3d(n=64, device=None):
+    m = meshes.cube(n)
+    sp = darcy_space(m, device=device)
+    kappa, f = darcy3d_coefficients(m)
+    return m, sp, kappa, f

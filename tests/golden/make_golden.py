@@ -1,0 +1,232 @@
+"""Generate golden fixtures by running the reference's OWN code (this container only).
+
+The reference (nfempy, pure Python) cannot run end to end here: basix,
+auto_diff, petsc4py, gmsh, meshio and matplotlib are absent.  Its mesh,
+topology, DoF-map, assembler, mapping and orientation code is plain
+Python/numpy, so this script runs exactly those files unchanged with small
+stand-ins:
+
+  * meshio   - `read(name)` returns an in-memory mesh from oracle.mesh_gen
+  * basix    - element metadata, tabulation and push-forward from
+               oracle.elements, quadrature from oracle.quadrature
+  * matplotlib - empty module (imported but unused by src/assembly/ScatterFormData.py:2)
+
+What the fixtures pin, from the reference's own code paths:
+  * destination indices of every cell   (ProductSpace.destination_indexes,
+                                          src/spaces/product_space.py:164-170)
+  * the assembled sparsity pattern and per-slot multiplicity (SequentialAssembler
+    + scatter_form_data, src/assembly/*.py, recorded through a Mat stand-in)
+  * orientation flags (src/basis/permute_and_transform.py:8-107)
+  * |det J| and J+ (src/geometry/mapping.py:23-55)
+  * the oriented, pushed-forward RT1 basis (FiniteElement.evaluate_basis,
+    src/basis/finite_element.py:156-186) - its Piola/orientation logic is the
+    reference's, its reference-cell tables come from the basix stand-in.
+
+Run:  python -B tests/golden/make_golden.py   (writes tests/golden/*.npz)
+"""
+import os
+import sys
+import types
+
+sys.dont_write_bytecode = True
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF_SRC = "/root/reference/src"
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+from oracle import elements as oel  # noqa: E402
+from oracle import mesh_gen, quadrature  # noqa: E402
+
+# ---------------------------------------------------------------- stand-ins
+_MESHES = {}
+
+
+class _Block:
+    def __init__(self, typ, data):
+        self.type = typ
+        self.data = np.asarray(data, dtype=np.int64)
+        self.dim = mesh_gen.BLOCK_DIM[typ]
+
+
+class _MeshioMesh:
+    def __init__(self, m):
+        self.points = np.asarray(m["points"], dtype=np.float64)
+        self.cells = [_Block(t, c) for t, c, _ in m["blocks"]]
+        self.cell_data = {"gmsh:physical": [np.asarray(p) for _, _, p in m["blocks"]]}
+
+    def get_cells_type(self, name):
+        n = {"vertex": 1, "line": 2, "triangle": 3, "tetra": 4}[name]
+        blocks = [b.data for b in self.cells if b.type == name]
+        if not blocks:
+            return np.zeros((0, n), dtype=np.int64)
+        return np.concatenate(blocks, axis=0)
+
+
+meshio = types.ModuleType("meshio")
+meshio.read = lambda name: _MeshioMesh(_MESHES[name])
+meshio.Mesh = object
+meshio.write = lambda *a, **k: None
+
+basix = types.ModuleType("basix")
+
+
+class ElementFamily:
+    P = "P"
+    RT = "RT"
+    BDM = "BDM"
+    N1E = "N1E"
+
+
+class LagrangeVariant:
+    gll_centroid = "gll_centroid"
+
+
+class CellType:
+    point = 0
+    interval = 1
+    triangle = 2
+    tetrahedron = 3
+
+
+class QuadratureType:
+    gauss_jacobi = "gauss_jacobi"
+
+
+class _PointElement:
+    entity_dofs = [[[0]]]
+    num_entity_dofs = [[1]]
+    dof_transformations_are_identity = True
+
+    def entity_transformations(self):
+        return {}
+
+    def tabulate(self, n, pts):
+        return np.ones((1, 1, 1, 1))
+
+
+def _create_element(family, celltype, degree, lagrange_variant=None, discontinuous=False):
+    if celltype == 0:
+        return _PointElement()
+    return oel.create_element(family, celltype, degree, discontinuous)
+
+
+basix.ElementFamily = ElementFamily
+basix.LagrangeVariant = LagrangeVariant
+basix.CellType = CellType
+basix.QuadratureType = QuadratureType
+basix.create_element = _create_element
+basix.make_quadrature = lambda cell, degree, rule=None: quadrature.make_quadrature(cell, degree)
+
+matplotlib = types.ModuleType("matplotlib")
+matplotlib.pyplot = types.ModuleType("matplotlib.pyplot")
+
+sys.modules.update({"meshio": meshio, "basix": basix, "matplotlib": matplotlib,
+                    "matplotlib.pyplot": matplotlib.pyplot})
+sys.path.insert(0, REF_SRC)
+
+from mesh.mesh import Mesh  # noqa: E402
+from spaces.product_space import ProductSpace  # noqa: E402
+from assembly.SequentialAssembler import SequentialAssembler  # noqa: E402
+from basis.permute_and_transform import (  # noqa: E402
+    _validate_edge_orientation_2d, _validate_face_orientation_3d)
+
+
+class RecordingMat:
+    """Stands in for a PETSc Mat: records every setValue(addv=True)."""
+
+    def __init__(self):
+        self.entries = {}
+
+    def setValue(self, row, col, value, addv=True):
+        key = (int(row), int(col))
+        self.entries[key] = self.entries.get(key, 0.0) + float(value)
+
+
+class CountingForm:
+    """A weak form whose element Jacobian is all ones (counts contributions)."""
+
+    def __init__(self, space):
+        self.space = space
+
+    def evaluate_form(self, i, alpha):
+        n = len(alpha)
+        return np.zeros(n), np.ones((n, n))
+
+
+def make_case(name, mesh, fields):
+    _MESHES[name] = mesh
+    dim = mesh["dim"]
+    gmesh = Mesh(dimension=dim, file_name=name)
+    gmesh.build_conformal_mesh()
+    data = {}
+    disc = {}
+    for fname, family, degree, nc, dsc in fields:
+        data[fname] = (dim, nc, family, degree, gmesh)
+        disc[fname] = dsc
+    space = ProductSpace(data)
+    space.make_subspaces_discontinuous(disc)
+    space.build_structures({f[0]: [1] for f in fields}, {})
+    first = fields[0][0]
+    n_el = len(space.discrete_spaces[first].elements)
+    dest = np.array([space.destination_indexes(i) for i in range(n_el)], dtype=np.int64)
+
+    mat = RecordingMat()
+    res = np.zeros(space.n_dof)
+    asm = SequentialAssembler(space, mat, res)
+    asm.form_to_input_list = {"count": ["form", range(n_el), CountingForm(space),
+                                        np.zeros(space.n_dof)]}
+    asm.scatter_forms()
+    keys = np.array(sorted(mat.entries.keys()), dtype=np.int64)
+    mult = np.array([mat.entries[tuple(k)] for k in keys])
+
+    out = {"cell_dofs": dest, "n_dof": np.int64(space.n_dof),
+           "pattern_rows": keys[:, 0], "pattern_cols": keys[:, 1], "multiplicity": mult,
+           "points": mesh["points"]}
+    # node tags of the elements (file order of the cells)
+    out["cell_vertices"] = np.array(
+        [space.discrete_spaces[first].elements[i].data.cell.node_tags for i in range(n_el)],
+        dtype=np.int64)
+
+    rt_fields = [f for f in fields if f[1] == "RT"]
+    if rt_fields:
+        fe_list = space.discrete_spaces[rt_fields[0][0]].elements
+        if dim == 2:
+            flags = np.array([_validate_edge_orientation_2d(fe.data) for fe in fe_list])
+            out["edge_oriented"] = flags
+        else:
+            o, rot, ref = zip(*[_validate_face_orientation_3d(fe.data) for fe in fe_list])
+            out["face_oriented"] = np.array(o)
+            out["face_rotations"] = np.array(rot)
+            out["face_reflections"] = np.array(ref)
+            out["bc_entities"] = np.array([fe.data.bc_entities for fe in fe_list])
+        pts, wts = space.quadrature[dim]
+        dets, invs, tabs = [], [], []
+        for fe in fe_list:
+            x, jac, det, inv = fe.evaluate_mapping(pts)
+            dets.append(det)
+            invs.append(inv)
+            tabs.append(fe.evaluate_basis(pts, jac, det, inv))
+        out["det_jac"] = np.array(dets)
+        out["inv_jac"] = np.array(invs)
+        out["rt_basis"] = np.array(tabs)
+        out["quad_points"] = pts
+        out["quad_weights"] = wts
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, "cells", n_el, "n_dof", space.n_dof, "nnz", len(keys))
+
+
+def main():
+    darcy = [("u", "RT", 1, 1, False), ("p", "Lagrange", 0, 1, True)]
+    make_case("darcy2d_n4", mesh_gen.square(4), darcy)
+    make_case("darcy3d_n2", mesh_gen.cube(2), darcy)
+    make_case("elast3d_n2", mesh_gen.cube(2), [("u", "Lagrange", 2, 3, False)])
+    make_case("elast2d_n3", mesh_gen.square(3), [("u", "Lagrange", 2, 2, False)])
+    make_case("cosserat3d_n1", mesh_gen.cube(1),
+              [("s", "RT", 1, 3, False), ("m", "RT", 1, 3, False),
+               ("u", "Lagrange", 0, 3, True), ("t", "Lagrange", 0, 3, True)])
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,88 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares (no GPU calls)."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from nfempy_gb300 import _lib, build, meshes, quadrature
+from oracle import mesh_gen
+from oracle import quadrature as oquad
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    syms = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        txt = open(h).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        syms |= set(re.findall(r"\b(nfem_[a-z0-9_]+)\s*\(", txt))
+    return syms
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    if not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    return _lib.LIB_PATH
+
+
+def test_library_exports_header(lib_path):
+    h = ctypes.CDLL(lib_path)
+    syms = header_symbols()
+    assert len(syms) >= 10
+    missing = [s for s in sorted(syms) if not hasattr(h, s)]
+    assert not missing, missing
+    # every symbol bound in ctypes is declared in the header and vice versa
+    assert set(_lib.exported_symbols()) == syms
+
+
+def test_status_strings(lib_path):
+    lib = _lib.lib()
+    assert lib.nfem_abi_version() >= 1
+    assert lib.nfem_status_string(0) == b"ok"
+    assert lib.nfem_status_string(6).startswith(b"assembled row")
+
+
+def test_workspace_queries(lib_path):
+    lib = _lib.lib()
+    b = ctypes.c_size_t(0)
+    assert lib.nfem_scan_workspace_bytes(1000, ctypes.byref(b)) == 0 and b.value > 0
+    assert lib.nfem_numbering_workspace_bytes(100, 3, 2, 50, 10, ctypes.byref(b)) == 0 and b.value > 0
+    assert lib.nfem_numbering_workspace_bytes(100, 3, 3, 50, 10, ctypes.byref(b)) == 1  # entity_dim == cell_dim
+    assert lib.nfem_pattern_workspace_bytes(100, 5, 300, ctypes.byref(b)) == 0 and b.value > 0
+    assert lib.nfem_pattern_workspace_bytes(-1, 5, 300, ctypes.byref(b)) == 1
+
+
+@pytest.mark.parametrize("dim,order", [(1, 3), (2, 3), (2, 5), (3, 3), (3, 5)])
+def test_product_quadrature_matches_oracle(dim, order):
+    a = quadrature.make_quadrature(dim, order)
+    b = oquad.make_quadrature(dim, order)
+    np.testing.assert_allclose(a[0], b[0], atol=1e-15)
+    np.testing.assert_allclose(a[1], b[1], atol=1e-15)
+
+
+@pytest.mark.parametrize("gen,n", [("square", 3), ("square", 8), ("cube", 2), ("cube", 3)])
+def test_product_meshes_match_oracle(gen, n):
+    a = getattr(meshes, gen)(n)
+    b = getattr(mesh_gen, gen)(n)
+    np.testing.assert_array_equal(a["points"], b["points"])
+    assert len(a["blocks"]) == len(b["blocks"])
+    for (ta, ca, pa), (tb, cb, pb) in zip(a["blocks"], b["blocks"]):
+        assert ta == tb
+        np.testing.assert_array_equal(ca, cb)
+        np.testing.assert_array_equal(pa, pb)
+
+
+def test_grf_is_seeded():
+    x = np.random.default_rng(0).random((100, 3))
+    a = meshes.grf_log_field(x, 0.1, 1.0, 7, device="cpu")
+    b = meshes.grf_log_field(x, 0.1, 1.0, 7, device="cpu")
+    c = meshes.grf_log_field(x, 0.1, 1.0, 8, device="cpu")
+    np.testing.assert_array_equal(a, b)
+    assert np.abs(a - c).max() > 1e-3
+    big = meshes.grf_log_field(np.random.default_rng(1).random((20000, 3)) * 50, 0.1, 2.0, 3, device="cpu")
+    assert abs(big.std() - 2.0) < 0.15

@@ -1,0 +1,63 @@
+"""The oracle against the fixtures produced by the reference's own code."""
+import numpy as np
+import pytest
+
+from oracle import assembly, forms, geometry, quadrature, topology
+from tests.cases import CASES, golden
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_dof_map_and_pattern(name):
+    mk, fields = CASES[name]
+    m = mk()
+    g = golden(name)
+    topo = topology.Topology(m, physical_tags=[1])
+    cd, nd = topology.cell_dofs(topo, [topology.FieldSpec(*f) for f in fields])
+    assert nd == int(g["n_dof"])
+    np.testing.assert_array_equal(cd, g["cell_dofs"])
+    np.testing.assert_array_equal(topo.cells, g["cell_vertices"])
+    ip, ix = assembly.pattern_csr(cd, nd)
+    rows = np.repeat(np.arange(nd), np.diff(ip))
+    np.testing.assert_array_equal(rows, g["pattern_rows"])
+    np.testing.assert_array_equal(ix, g["pattern_cols"])
+    n = cd.shape[1]
+    A, _ = assembly.assemble_csr(cd, np.ones((topo.n_cells, n, n)), np.zeros(cd.shape), nd)
+    np.testing.assert_array_equal(A.data, g["multiplicity"])
+
+
+@pytest.mark.parametrize("name", [n for n in sorted(CASES) if "darcy" in n or "cosserat" in n])
+def test_orientation_mapping_basis(name):
+    mk, fields = CASES[name]
+    m = mk()
+    g = golden(name)
+    dim = m["dim"]
+    topo = topology.Topology(m, physical_tags=[1])
+    if dim == 2:
+        np.testing.assert_array_equal(~topo.facet_reflected, g["edge_oriented"])
+    else:
+        np.testing.assert_array_equal(topo.facet_tagged, g["bc_entities"])
+        np.testing.assert_array_equal(topo.rt1_signs() < 0, g["face_reflections"] % 2 == 1)
+    pts, wts = g["quad_points"], g["quad_weights"]
+    qp, qw = quadrature.make_quadrature(dim, 3)
+    np.testing.assert_allclose(qp, pts, atol=1e-15)
+    np.testing.assert_allclose(qw, wts, atol=1e-15)
+    X = m["points"][topo.cells]
+    s = topo.rt1_signs()
+    for c in range(topo.n_cells):
+        x, J, det, pinv = geometry.evaluate_mapping(dim, pts, X[c])
+        np.testing.assert_array_equal(det, g["det_jac"][c])
+        np.testing.assert_array_equal(pinv, g["inv_jac"][c])
+        tab = forms.tabulate_oriented("RT", dim, 1, pts, J, det, pinv, s[c])
+        np.testing.assert_array_equal(tab, g["rt_basis"][c])
+    _, detb, pinvb = geometry.cell_jacobians(X)
+    np.testing.assert_allclose(np.broadcast_to(detb[:, None], g["det_jac"].shape), g["det_jac"], rtol=1e-14)
+    np.testing.assert_allclose(np.broadcast_to(pinvb[:, None], g["inv_jac"].shape), g["inv_jac"], atol=1e-13)
+
+
+def test_pattern_b_filter():
+    """Driver filter: drops |v| <= 1e-8, keeps row <= col, adds zero diagonals."""
+    cd = np.array([[0, 1, 2]])
+    j = np.array([[[1.0, 1e-9, 2.0], [1e-9, 0.0, 3.0], [2.0, 3.0, 4.0]]])
+    ip, ix = assembly.pattern_b(cd, j, 3)
+    rows = np.repeat(np.arange(3), np.diff(ip))
+    assert list(zip(rows.tolist(), ix.tolist())) == [(0, 0), (0, 2), (1, 1), (1, 2), (2, 2)]
