@@ -144,6 +144,14 @@ int nfem_pattern_local_codes(const int32_t* cell_dofs, int64_t n_cells, int n_lo
                              const int32_t* row_ptr, const int32_t* col_idx, uint32_t* codes,
                              int32_t* dev_status, void* stream);
 
+/* Fixed-stride form of the incidence lists for rows with at most two
+ * incidences (mixed RT1 x P0 spaces): pairs [n_rows, 2] = the (cell * n_loc +
+ * local) occurrences of each row or -1, pair_codes [n_rows, 2] = their slot
+ * codes.  Returns NFEM_ERR_UNSUPPORTED (through dev_status) for longer lists. */
+int nfem_pattern_pairs(const int32_t* inc_ptr, const int32_t* inc, const uint32_t* codes,
+                       int64_t n_rows, int32_t* pairs, uint32_t* pair_codes,
+                       int32_t* dev_status, void* stream);
+
 /* Splits FP64 points into float hi/lo pairs [n_points, 6] = (hi xyz, lo xyz)
  * so FP32 kernels form cell edge vectors without FP64 arithmetic. */
 int nfem_points_split(const double* points, int64_t n_points, float* points_split,
@@ -165,8 +173,8 @@ int nfem_points_split(const double* points, int64_t n_points, float* points_spli
  * that type.  flux_dofs [n_cells, dim + 1] are the RT1 DoFs, the pressure DoF
  * of cell c is p_base + c.  qweights (host, n_qp entries) are the reference
  * quadrature weights, read only when source_mode == NFEM_COEF_QPOINT.
- * inc_ptr/inc/codes come from nfem_pattern_rows / nfem_pattern_local_codes
- * with cell_dofs = [flux_dofs | p_base + c].  accumulate == 0 overwrites
+ * row_pairs/pair_codes come from nfem_pattern_rows, nfem_pattern_local_codes and
+ * nfem_pattern_pairs with cell_dofs = [flux_dofs | p_base + c].  accumulate == 0 overwrites
  * values/rhs (the first form of an assembly pass, like a zeroed PETSc Mat
  * and residual); accumulate != 0 adds to them (setValue(addv=True)).  Each CSR value and residual entry is written once
  * (row-owner gather; no atomics, deterministic). */
@@ -176,10 +184,80 @@ int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t 
                               int64_t p_base, const uint8_t* sign_mask,
                               const void* kappa, const void* source, int source_mode,
                               const double* qweights, int n_qp,
-                              const int32_t* inc_ptr, const int32_t* inc,
-                              const uint32_t* codes, const int32_t* row_ptr,
+                              const int32_t* row_pairs, const uint32_t* pair_codes,
+                              const int32_t* row_ptr,
                               void* values, void* rhs, int accumulate,
                               int32_t* dev_status, void* stream);
+
+/* -------------------------------------------- K5 + K7: Krylov solve (a17)
+ * Replaces the PETSc KSP solves of the drivers
+ * (examples/md_elliptic_scalar/md_elliptic_scalar.py:343-363,
+ * examples/cauchy_elasticity/cg_elasticity_example_1.py:159-170,
+ * examples/cosserat_elasticity/mfe_cosserat_elasticity_example_3.py:256-297):
+ * solves A x = b to ||b - A x||_2 / ||b||_2 <= rtol with the residual always
+ * evaluated in FP64 on the FP64 matrix, inner flexible GMRES(restart) in FP32
+ * on the FP32 copy of the same matrix (iterative refinement). */
+typedef struct {
+  int64_t n_rows;
+  const int32_t* row_ptr;
+  const int32_t* col_idx;
+  const void* values;
+  int value_type; /* nfem_value_type */
+} nfem_csr;
+
+typedef enum {
+  NFEM_PC_NONE = 0,
+  NFEM_PC_JACOBI = 1,     /* point Jacobi: diag_inv [n_rows] */
+  NFEM_PC_CELL_BLOCK = 2  /* cell-patch block Jacobi (weighted additive Schwarz over
+                             the element cliques): cell_dofs [n_cells, n_loc],
+                             block_inv [n_cells, n_loc, n_loc], row incidences */
+} nfem_pc_kind;
+
+typedef struct {
+  int kind;
+  int n_loc;
+  int64_t n_cells;
+  const int32_t* cell_dofs;
+  const int32_t* inc_ptr;
+  const int32_t* inc;
+  float* block_inv;
+  float* diag_inv;
+} nfem_precond;
+
+typedef struct {
+  double rtol;        /* FP64 relative residual target */
+  double inner_rtol;  /* reduction asked of each FP32 inner solve */
+  int restart;        /* GMRES restart length, 1..64 */
+  int max_inner;      /* cap on total inner iterations */
+  int max_outer;      /* cap on refinement steps */
+} nfem_solve_params;
+
+typedef struct {
+  int inner_iterations;
+  int outer_iterations;
+  double initial_relres;
+  double final_relres;
+  int status;
+} nfem_solve_info;
+
+/* y = A x (FP32 or FP64 matrix and vectors) */
+int nfem_spmv(int value_type, int64_t n_rows, const int32_t* row_ptr, const int32_t* col_idx,
+              const void* values, const void* x, void* y, void* stream);
+/* r = b - A x in FP64 */
+int nfem_residual_f64(int64_t n_rows, const int32_t* row_ptr, const int32_t* col_idx,
+                      const double* values, const double* x, const double* b, double* r,
+                      void* stream);
+/* Builds the preconditioner data from the FP64 matrix (block inverses in
+ * FP64 Gauss-Jordan, stored FP32). */
+int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, int32_t* dev_status,
+                       void* stream);
+int nfem_precond_apply(const nfem_precond* pc, int64_t n, const float* v, float* z, void* stream);
+int nfem_solve_workspace_bytes(int64_t n_rows, int restart, size_t* bytes);
+/* Synchronises on `stream` once per GMRES cycle and per refinement step. */
+int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, const nfem_precond* pc,
+                         const double* b, double* x, const nfem_solve_params* params,
+                         void* workspace, size_t workspace_bytes, nfem_solve_info* info,
+                         void* stream);
 
 #ifdef __cplusplus
 }

@@ -36,6 +36,28 @@ class DofBlock(C.Structure):
     _fields_ = [("occ_rank", C.c_void_p), ("n_ent", C.c_int32), ("width", C.c_int32), ("base", C.c_int64)]
 
 
+class Csr(C.Structure):
+    _fields_ = [("n_rows", C.c_int64), ("row_ptr", C.c_void_p), ("col_idx", C.c_void_p), ("values", C.c_void_p),
+                ("value_type", C.c_int)]
+
+
+class Precond(C.Structure):
+    _fields_ = [("kind", C.c_int), ("n_loc", C.c_int), ("n_cells", C.c_int64), ("cell_dofs", C.c_void_p),
+                ("inc_ptr", C.c_void_p), ("inc", C.c_void_p), ("block_inv", C.c_void_p), ("diag_inv", C.c_void_p)]
+
+
+class SolveParams(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("inner_rtol", C.c_double), ("restart", C.c_int), ("max_inner", C.c_int),
+                ("max_outer", C.c_int)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("inner_iterations", C.c_int), ("outer_iterations", C.c_int), ("initial_relres", C.c_double),
+                ("final_relres", C.c_double), ("status", C.c_int)]
+
+
+PC_NONE, PC_JACOBI, PC_CELL_BLOCK = 0, 1, 2
+
 _P = C.c_void_p
 _I = C.c_int
 _I64 = C.c_int64
@@ -56,8 +78,16 @@ _SIGS = {
     "nfem_pattern_slots": ([_P, _I64, _I, _I, _P, _P, _P, _P, _P], _I),
     "nfem_pattern_local_codes": ([_P, _I64, _I, _I, _I64, _P, _P, _P, _P, _P, _P, _P], _I),
     "nfem_points_split": ([_P, _I64, _P, _P], _I),
+    "nfem_pattern_pairs": ([_P, _P, _P, _I64, _P, _P, _P, _P], _I),
     "nfem_darcy_rt1p0_assemble": ([_I, _I, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P, _P, _I,
-                                   _P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P], _I),
+                                   _P, _I, _P, _P, _P, _P, _P, _I, _P, _P], _I),
+    "nfem_spmv": ([_I, _I64, _P, _P, _P, _P, _P, _P], _I),
+    "nfem_residual_f64": ([_I64, _P, _P, _P, _P, _P, _P, _P], _I),
+    "nfem_precond_setup": ([C.POINTER(Precond), C.POINTER(Csr), _P, _P], _I),
+    "nfem_precond_apply": ([C.POINTER(Precond), _I64, _P, _P, _P], _I),
+    "nfem_solve_workspace_bytes": ([_I64, _I, C.POINTER(_SZ)], _I),
+    "nfem_solve_ir_fgmres": ([C.POINTER(Csr), C.POINTER(Csr), C.POINTER(Precond), _P, _P, C.POINTER(SolveParams),
+                              _P, _SZ, C.POINTER(SolveInfo), _P], _I),
 }
 
 _lib = None

@@ -59,6 +59,12 @@ class CSRMatrix:
             _lib.call("nfem_pattern_local_codes", _lib.ptr(space.cell_dofs), T, n_loc, n_loc, self.n_rows,
                       _lib.ptr(self.inc_ptr), _lib.ptr(self.inc), _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
                       _lib.ptr(self.codes), _lib.ptr(self.status), st)
+        self.pairs = None
+        if self.codes is not None and max_incidence(self.inc_ptr) <= 2:
+            self.pairs = torch.empty((self.n_rows, 2), dtype=torch.int32, device=dev)
+            self.pair_codes = torch.empty((self.n_rows, 2), dtype=torch.int32, device=dev)
+            _lib.call("nfem_pattern_pairs", _lib.ptr(self.inc_ptr), _lib.ptr(self.inc), _lib.ptr(self.codes),
+                      self.n_rows, _lib.ptr(self.pairs), _lib.ptr(self.pair_codes), _lib.ptr(self.status), st)
         self.values = torch.zeros(max(self.nnz, 1), dtype=dtype, device=dev)
         self.fresh = True
         self.check_status("pattern")
@@ -87,6 +93,10 @@ class CSRMatrix:
         return sp.csr_matrix((self.values[: self.nnz].double().cpu().numpy(),
                               self.col_idx[: self.nnz].cpu().numpy(), self.row_ptr.cpu().numpy()),
                              shape=(self.n_rows, self.n_rows))
+
+
+def max_incidence(inc_ptr):
+    return int((inc_ptr[1:] - inc_ptr[:-1]).max().item()) if inc_ptr.numel() > 1 else 0
 
 
 def _to_device(x, dtype, device, n):
@@ -192,16 +202,16 @@ class LaplaceDualWeakForm(WeakForm):
         vt = _lib.NFEM_F64 if dtype == torch.float64 else _lib.NFEM_F32
         if residual.dtype != dtype or not residual.is_cuda:
             raise ValueError("residual must be a CUDA tensor of the matrix dtype")
-        if jacobian.codes is None:
-            raise NotImplementedError("matrix built without slot codes")
+        if jacobian.pairs is None:
+            raise NotImplementedError("matrix built without the two-incidence row layout")
         kt, st, mode = coefficients if coefficients is not None else self.coefficients(dtype)
         pts, wts = sp.quadrature[sp.dim]
         qw = (_lib.C.c_double * len(wts))(*wts.tolist())
         _lib.call("nfem_darcy_rt1p0_assemble", sp.dim, vt, sp.n_cells, jacobian.n_rows,
                   _lib.ptr(sp.points), _lib.ptr(sp.points_split), _lib.ptr(sp.cells), None,
                   sp.field_offsets["p"], _lib.ptr(sp.rt_sign_mask), _lib.ptr(kt), _lib.ptr(st), mode,
-                  _lib.C.cast(qw, _lib.C.c_void_p), len(wts), _lib.ptr(jacobian.inc_ptr), _lib.ptr(jacobian.inc), _lib.ptr(jacobian.codes),
-                  _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate),
+                  _lib.C.cast(qw, _lib.C.c_void_p), len(wts), _lib.ptr(jacobian.pairs),
+                  _lib.ptr(jacobian.pair_codes), _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate),
                   _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
 
     def evaluate_form(self, element_index, alpha):

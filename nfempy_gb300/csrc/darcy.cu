@@ -42,9 +42,8 @@ struct DarcyParams {
   const uint8_t* sign;
   const void* kappa;
   const void* source;
-  const int32_t* inc_ptr;
-  const int32_t* inc;
-  const uint32_t* codes;
+  const int32_t* pairs;
+  const uint32_t* pair_codes;
   const int32_t* row_ptr;
   void* values;
   void* rhs;
@@ -147,16 +146,113 @@ __device__ __forceinline__ T abs_det(const T (&J)[DIM][3], const T (&G)[DIM][DIM
   }
 }
 
+// One incidence (cell c, local row a) of a row: everything loaded up front so
+// that the two incidences of a face row overlap their memory latency.
+template <typename T, int DIM>
+struct Incidence {
+  T J[DIM][3];
+  T kap;
+  T src;
+  uint32_t m;
+};
+
+template <typename T, int DIM, int SRC>
+__device__ __forceinline__ void load_incidence(const DarcyParams& p, int32_t c, bool need_geo,
+                                               Incidence<T, DIM>& x) {
+  const T* kappa = static_cast<const T*>(p.kappa);
+  const T* src = static_cast<const T*>(p.source);
+  x.m = __ldg(p.sign + c);
+  x.kap = __ldg(kappa + c);
+  x.src = T(0);
+  if constexpr (SRC == NFEM_COEF_CELL) x.src = __ldg(src + c);
+  if constexpr (SRC == NFEM_COEF_QPOINT) {
+    T acc = T(0);
+#pragma unroll 4
+    for (int q = 0; q < 32; ++q)
+      if (q < p.n_qp) acc += T(p.qw[q]) * __ldg(src + int64_t(c) * p.n_qp + q);
+    x.src = acc;
+  }
+  if (need_geo) {
+    cell_edges<T, DIM>(p, c, x.J);
+  } else {
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) x.J[i][d] = T(0);
+  }
+}
+
+// Row a of the element matrix of the incidence (vals[0..NF) flux columns,
+// vals[NF] pressure column) and, for the pressure row, the residual entry.
+template <typename T, int DIM, int SRC>
+__device__ __forceinline__ void element_row(const DarcyParams& p, const Incidence<T, DIM>& x, int a, bool need_geo,
+                                            T (&vals)[DIM + 2], T& rhs_val) {
+  constexpr int NF = DIM + 1;
+  using C = DarcyConst<T, DIM>;
+  T sg[NF];
+#pragma unroll
+  for (int i = 0; i < NF; ++i) sg[i] = ((x.m >> i) & 1u) ? -C::sigma(i) : C::sigma(i);
+  T G[DIM][DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) G[i][j] = x.J[i][0] * x.J[j][0] + x.J[i][1] * x.J[j][1] + x.J[i][2] * x.J[j][2];
+  T det = T(1);
+  if (need_geo) {
+    det = abs_det<T, DIM>(x.J, G);
+    if (!(det > T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+  }
+  if (a < NF) {
+    T R[DIM];
+    T trG = T(0), sumG = T(0);
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      R[i] = T(0);
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) R[i] += G[i][j];
+      trG += G[i][i];
+      sumG += R[i];
+    }
+    const T tgs = (trG + sumG) * T(C::f2);
+    const T scale = T(C::kappa2) / (x.kap * det);
+    // row a-1 of G and R[a-1] through selects (no local-memory indexing)
+    T Ga[DIM];
+    T Ra = T(0);
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) Ga[j] = T(0);
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      const bool hit = (a == i + 1);
+      Ra = hit ? R[i] : Ra;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) Ga[j] = hit ? G[i][j] : Ga[j];
+    }
+    T sga = sg[0];
+#pragma unroll
+    for (int i = 1; i < NF; ++i) sga = (a == i) ? sg[i] : sga;
+    const T gma = Ra * T(C::f1);
+#pragma unroll
+    for (int b = 0; b < NF; ++b) {
+      const T gmb = b > 0 ? R[b - 1] * T(C::f1) : T(0);
+      const T gv = b > 0 ? Ga[b - 1] * T(C::area) : T(0);
+      vals[b] = scale * sga * sg[b] * (tgs - gma - gmb + gv);
+    }
+    vals[NF] = -sga;
+  } else {
+#pragma unroll
+    for (int b = 0; b < NF; ++b) vals[b] = sg[b];
+    vals[NF] = T(0);
+    if constexpr (SRC == NFEM_COEF_CELL) rhs_val += -det * T(C::area) * x.src;
+    if constexpr (SRC == NFEM_COEF_QPOINT) rhs_val += -det * x.src;
+  }
+}
+
 template <typename T, int DIM, int SRC>
 __global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const DarcyParams p) {
-  constexpr int NF = DIM + 1;
   constexpr int NLOC = DIM + 2;
-  using C = DarcyConst<T, DIM>;
   __shared__ T stage[kDarcyWarps][32 * kDarcyMaxRow];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* st = stage[warp];
-  const T* kappa = static_cast<const T*>(p.kappa);
-  const T* src = static_cast<const T*>(p.source);
   T* values = static_cast<T*>(p.values);
   T* rhs = static_cast<T*>(p.rhs);
 
@@ -164,8 +260,27 @@ __global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const Darc
        r0 += int64_t(gridDim.x) * kDarcyWarps * 32) {
     const int64_t r = r0 + lane;
     const bool valid = r < p.n_rows;
+    // independent loads of the row: extent, incidence pair, slot codes
     const int32_t rb = valid ? __ldg(p.row_ptr + r) : 0;
     const int32_t re = valid ? __ldg(p.row_ptr + r + 1) : 0;
+    const int2 pr = valid ? __ldg(reinterpret_cast<const int2*>(p.pairs) + r) : make_int2(-1, -1);
+    const uint2 cd = valid ? __ldg(reinterpret_cast<const uint2*>(p.pair_codes) + r) : make_uint2(0u, 0u);
+    const int occ[2] = {pr.x, pr.y};
+    const uint32_t code[2] = {cd.x, cd.y};
+    int32_t c[2];
+    int a[2];
+    bool on[2], geo[2];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      on[t] = occ[t] >= 0;
+      c[t] = on[t] ? occ[t] / NLOC : 0;
+      a[t] = on[t] ? occ[t] - c[t] * NLOC : 0;
+      geo[t] = on[t] && ((a[t] < DIM + 1) || (SRC != 0));
+    }
+    Incidence<T, DIM> inc[2];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) load_incidence<T, DIM, SRC>(p, c[t], geo[t], inc[t]);
+
     const int last = int(min(int64_t(31), p.n_rows - 1 - r0));
     const int32_t base = __shfl_sync(0xffffffffu, rb, 0);
     const int32_t end = __shfl_sync(0xffffffffu, re, last);
@@ -177,94 +292,18 @@ __global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const Darc
     for (int i = lane; i < span; i += 32) st[i] = T(0);
     __syncwarp();
     T rhs_val = T(0);
-    if (valid) {
-      const int32_t kb = __ldg(p.inc_ptr + r), ke = __ldg(p.inc_ptr + r + 1);
-      if (ke - kb > 2) set_status(p.status, NFEM_ERR_PATTERN);
-      const int off = rb - base;
+    const int off = rb - base;
 #pragma unroll
-      for (int t = 0; t < 2; ++t) {
-        const int32_t k = kb + t;
-        if (k < ke) {
-          const int32_t occ = __ldg(p.inc + k);
-          const uint32_t code = __ldg(p.codes + k);
-          const int32_t c = occ / NLOC;
-          const int a = occ - c * NLOC;
-          const uint32_t m = __ldg(p.sign + c);
-          T sg[NF];
+    for (int t = 0; t < 2; ++t) {
+      if (on[t]) {
+        T vals[NLOC];
+        element_row<T, DIM, SRC>(p, inc[t], a[t], geo[t], vals, rhs_val);
 #pragma unroll
-          for (int i = 0; i < NF; ++i) sg[i] = ((m >> i) & 1u) ? -C::sigma(i) : C::sigma(i);
-          T vals[NLOC];
-          const bool need_geo = (a < NF) || (SRC != 0);
-          T det = T(1);
-          T G[DIM][DIM];
-          if (need_geo) {
-            T J[DIM][3];
-            cell_edges<T, DIM>(p, c, J);
-#pragma unroll
-            for (int i = 0; i < DIM; ++i)
-#pragma unroll
-              for (int j = 0; j < DIM; ++j) G[i][j] = J[i][0] * J[j][0] + J[i][1] * J[j][1] + J[i][2] * J[j][2];
-            det = abs_det<T, DIM>(J, G);
-            if (!(det > T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
-          }
-          if (a < NF) {
-            // face row a: mass entries and the divergence coupling
-            T R[DIM];
-            T trG = T(0), sumG = T(0);
-#pragma unroll
-            for (int i = 0; i < DIM; ++i) {
-              R[i] = T(0);
-#pragma unroll
-              for (int j = 0; j < DIM; ++j) R[i] += G[i][j];
-              trG += G[i][i];
-              sumG += R[i];
-            }
-            const T tgs = (trG + sumG) * T(C::f2);
-            const T scale = T(C::kappa2) / (__ldg(kappa + c) * det);
-            // row a-1 of G and R[a-1] through selects (no local-memory indexing)
-            T Ga[DIM];
-            T Ra = T(0);
-#pragma unroll
-            for (int j = 0; j < DIM; ++j) Ga[j] = T(0);
-#pragma unroll
-            for (int i = 0; i < DIM; ++i) {
-              const bool hit = (a == i + 1);
-              Ra = hit ? R[i] : Ra;
-#pragma unroll
-              for (int j = 0; j < DIM; ++j) Ga[j] = hit ? G[i][j] : Ga[j];
-            }
-            T sga = sg[0];
-#pragma unroll
-            for (int i = 1; i < NF; ++i) sga = (a == i) ? sg[i] : sga;
-            const T gma = Ra * T(C::f1);
-#pragma unroll
-            for (int b = 0; b < NF; ++b) {
-              const T gmb = b > 0 ? R[b - 1] * T(C::f1) : T(0);
-              const T gv = b > 0 ? Ga[b - 1] * T(C::area) : T(0);
-              vals[b] = scale * sga * sg[b] * (tgs - gma - gmb + gv);
-            }
-            vals[NF] = -sga;
-          } else {
-#pragma unroll
-            for (int b = 0; b < NF; ++b) vals[b] = sg[b];
-            vals[NF] = T(0);
-            if constexpr (SRC == NFEM_COEF_CELL) {
-              rhs_val = -det * T(C::area) * __ldg(src + c);
-            } else if constexpr (SRC == NFEM_COEF_QPOINT) {
-              T acc = T(0);
-#pragma unroll 4
-              for (int q = 0; q < 32; ++q)
-                if (q < p.n_qp) acc += T(p.qw[q]) * __ldg(src + int64_t(c) * p.n_qp + q);
-              rhs_val = -det * acc;
-            }
-          }
-#pragma unroll
-          for (int b = 0; b < NLOC; ++b) {
-            // codes index inside the row (< 16 entries); the clamp keeps a
-            // corrupted code inside this warp's staging buffer
-            const int idx = min(off + int((code >> (4 * b)) & 15u), 32 * kDarcyMaxRow - 1);
-            st[idx] += vals[b];
-          }
+        for (int b = 0; b < NLOC; ++b) {
+          // codes index inside the row (< 16 entries); the clamp keeps a
+          // corrupted code inside this warp's staging buffer
+          const int idx = min(off + int((code[t] >> (4 * b)) & 15u), 32 * kDarcyMaxRow - 1);
+          st[idx] += vals[b];
         }
       }
     }
@@ -303,7 +342,7 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
                                          const int32_t* cell_vertices, const int32_t* flux_dofs, int64_t p_base,
                                          const uint8_t* sign_mask, const void* kappa, const void* source,
                                          int source_mode, const double* qweights, int n_qp,
-                                         const int32_t* inc_ptr, const int32_t* inc, const uint32_t* codes,
+                                         const int32_t* row_pairs, const uint32_t* pair_codes,
                                          const int32_t* row_ptr, void* values, void* rhs, int accumulate,
                                          int32_t* dev_status, void* stream_) {
   (void)flux_dofs;
@@ -313,13 +352,15 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   if ((dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_rows < 0)
     return NFEM_ERR_INVALID_ARG;
   if (n_rows == 0) return NFEM_OK;
-  if (!cell_vertices || !sign_mask || !kappa || !inc_ptr || !inc || !codes || !row_ptr || !values || !rhs)
+  if (!cell_vertices || !sign_mask || !kappa || !row_pairs || !pair_codes || !row_ptr || !values || !rhs)
     return NFEM_ERR_INVALID_ARG;
   if (value_type == NFEM_F64 && !points) return NFEM_ERR_INVALID_ARG;
   if (value_type == NFEM_F32 && !points_split) return NFEM_ERR_INVALID_ARG;
   if (source_mode != NFEM_COEF_NONE && !source) return NFEM_ERR_INVALID_ARG;
   if (source_mode == NFEM_COEF_QPOINT && (!qweights || n_qp < 1 || n_qp > 32)) return NFEM_ERR_INVALID_ARG;
   if (dim == 3 && (reinterpret_cast<uintptr_t>(cell_vertices) & 15)) return NFEM_ERR_INVALID_ARG;
+  if ((reinterpret_cast<uintptr_t>(row_pairs) & 7) || (reinterpret_cast<uintptr_t>(pair_codes) & 7))
+    return NFEM_ERR_INVALID_ARG;
   DarcyParams p;
   p.n_rows = n_rows;
   p.points = points;
@@ -328,9 +369,8 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   p.sign = sign_mask;
   p.kappa = kappa;
   p.source = source;
-  p.inc_ptr = inc_ptr;
-  p.inc = inc;
-  p.codes = codes;
+  p.pairs = row_pairs;
+  p.pair_codes = pair_codes;
   p.row_ptr = row_ptr;
   p.values = values;
   p.rhs = rhs;

@@ -1,0 +1,563 @@
+// K5 + K7: device-resident Krylov solve with FP64 iterative refinement.
+//
+// Reference: the drivers hand the assembled PETSc matrix to a KSP
+// (examples/md_elliptic_scalar/md_elliptic_scalar.py:343-363 MUMPS LU;
+// examples/cauchy_elasticity/cg_elasticity_example_1.py:159-170 ICC-CG;
+// examples/cosserat_elasticity/mfe_cosserat_elasticity_example_3.py:256-297
+// MINRES + fieldsplit) and solve A x = b with b = -r(0).
+//
+// GPU design:
+//  * CSR SpMV in FP32 (inner) and FP64 (outer residual r = b - A x), warp
+//    chunks of 32 rows whose contiguous CSR segment is streamed with
+//    coalesced loads into shared memory, then reduced per row.
+//  * Deterministic reductions: a fixed grid of kRedBlocks blocks writes
+//    partial sums, one block adds them in a fixed order (bitwise
+//    reproducible dots and norms).
+//  * Preconditioners: point Jacobi, and cell-patch block Jacobi (weighted
+//    additive Schwarz over the element cliques: z = sum_c R_c^T D_c A_c^-1 R_c v
+//    with D_c = 1 / multiplicity, applied row-owner, no atomics).
+//  * Flexible GMRES(m) with classical Gram-Schmidt and one
+//    re-orthogonalisation; the Hessenberg matrix, Givens rotations and
+//    residual estimates live on the device, so a restart cycle synchronises
+//    with the host once.
+//  * Mixed precision: inner FGMRES in FP32 on the FP32 matrix, outer
+//    refinement with the FP64 residual of the FP64 matrix until
+//    ||b - A x|| / ||b|| <= rtol (the stopping test is always FP64).
+#include <math.h>
+#include <stdio.h>
+
+#include <vector>
+
+#include "nfem_common.cuh"
+
+namespace nfem {
+
+constexpr int kRedBlocks = 304;  // 2 x 152 SMs
+constexpr int kRedThreads = 256;
+constexpr int kSpmvWarps = 8;
+constexpr int kSpmvCap = 32 * 16;
+constexpr int kMaxRestart = 64;
+
+// ------------------------------------------------------------------ SpMV
+template <typename VT, typename XT, typename AT>
+__global__ void __launch_bounds__(32 * kSpmvWarps)
+    spmv_kernel(int64_t n_rows, const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                const VT* __restrict__ val, const XT* __restrict__ x, XT* __restrict__ y,
+                const XT* __restrict__ b, int residual) {
+  __shared__ AT stage[kSpmvWarps][kSpmvCap];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  AT* st = stage[warp];
+  for (int64_t r0 = (int64_t(blockIdx.x) * kSpmvWarps + warp) * 32; r0 < n_rows;
+       r0 += int64_t(gridDim.x) * kSpmvWarps * 32) {
+    const int64_t r = r0 + lane;
+    const bool valid = r < n_rows;
+    const int32_t rb = valid ? __ldg(row_ptr + r) : 0;
+    const int32_t re = valid ? __ldg(row_ptr + r + 1) : 0;
+    const int last = int(min(int64_t(31), n_rows - 1 - r0));
+    const int32_t base = __shfl_sync(0xffffffffu, rb, 0);
+    const int32_t end = __shfl_sync(0xffffffffu, re, last);
+    const int span = end - base;
+    AT acc = AT(0);
+    if (span <= kSpmvCap) {
+      for (int i = lane; i < span; i += 32) {
+        const int64_t k = int64_t(base) + i;
+        st[i] = AT(__ldg(val + k)) * AT(__ldg(x + __ldg(col + k)));
+      }
+      __syncwarp();
+      if (valid)
+        for (int32_t k = rb - base; k < re - base; ++k) acc += st[k];
+      __syncwarp();
+    } else if (valid) {
+      for (int32_t k = rb; k < re; ++k) acc += AT(__ldg(val + k)) * AT(__ldg(x + __ldg(col + k)));
+    }
+    if (valid) y[r] = residual ? XT(AT(b[r]) - acc) : XT(acc);
+  }
+}
+
+template <typename VT, typename XT, typename AT>
+static int spmv(int64_t n, const int32_t* rp, const int32_t* ci, const VT* v, const XT* x, XT* y, const XT* b,
+                int residual, cudaStream_t s) {
+  if (n == 0) return NFEM_OK;
+  const int grid = grid_for(ceil_div(n, 32 * kSpmvWarps), 1, 8);
+  spmv_kernel<VT, XT, AT><<<grid, 32 * kSpmvWarps, 0, s>>>(n, rp, ci, v, x, y, b, residual);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+// ------------------------------------------------------------------ reductions
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = lane < (blockDim.x >> 5) ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;
+}
+
+// partial[j * kRedBlocks + block] = sum_i X_j[i] * y[i] for j < k (X_j = X + j * ldx)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    multidot_partial(int64_t n, int k, const T* __restrict__ X, int64_t ldx, const T* __restrict__ y,
+                     double* __restrict__ partial) {
+  __shared__ double sh[32];
+  for (int j = 0; j < k; ++j) {
+    const T* xj = X + int64_t(j) * ldx;
+    float accf = 0.f;
+    double acc = 0.0;
+    int cnt = 0;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+      if constexpr (sizeof(T) == 4) {
+        accf = fmaf(float(xj[i]), float(y[i]), accf);
+        if (++cnt == 64) { acc += double(accf); accf = 0.f; cnt = 0; }
+      } else {
+        acc += double(xj[i]) * double(y[i]);
+      }
+    }
+    acc += double(accf);
+    double t = block_sum(acc, sh);
+    if (threadIdx.x == 0) partial[int64_t(j) * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// out[j] = scale * sum_b partial[j][b] (fixed order); mode 1: out = sqrt(sum)
+__global__ void reduce_partials(const double* __restrict__ partial, int nb, int k, double* __restrict__ out,
+                                int mode, double sign) {
+  __shared__ double sh[32];
+  for (int j = 0; j < k; ++j) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) v += partial[int64_t(j) * nb + b];
+    double t = block_sum(v, sh);
+    if (threadIdx.x == 0) out[j] = mode == 1 ? sqrt(t) : sign * t;
+  }
+}
+
+template <typename T>
+static int multidot(int64_t n, int k, const T* X, int64_t ldx, const T* y, double* partial, double* out, int mode,
+                    cudaStream_t s) {
+  multidot_partial<T><<<kRedBlocks, kRedThreads, 0, s>>>(n, k, X, ldx, y, partial);
+  reduce_partials<<<1, 1024, 0, s>>>(partial, kRedBlocks, k, out, mode, 1.0);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+// w -= sum_{j<k} h[j] X_j   (h on the device; FP64 coefficients)
+template <typename T>
+__global__ void multi_axpy(int64_t n, int k, const T* __restrict__ X, int64_t ldx, const double* __restrict__ h,
+                           T* __restrict__ w, double hsign) {
+  __shared__ double hs[kMaxRestart + 1];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = hsign * h[j];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    float acc = 0.f;
+    for (int j = 0; j < k; ++j) acc = fmaf(float(hs[j]), float(X[int64_t(j) * ldx + i]), acc);
+    w[i] = T(float(w[i]) - acc);
+  }
+}
+
+// v = w / nrm (nrm device scalar); zero when nrm is 0
+template <typename T>
+__global__ void scale_by_inv(int64_t n, const T* __restrict__ w, const double* __restrict__ nrm, T* __restrict__ v) {
+  const double d = *nrm;
+  const float inv = d > 0.0 ? float(1.0 / d) : 0.f;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    v[i] = T(float(w[i]) * inv);
+}
+
+__global__ void cast_f64_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    b[i] = float(a[i]);
+}
+
+// x64 += d32
+__global__ void add_f32_to_f64(int64_t n, const float* __restrict__ d, double* __restrict__ x) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    x[i] += double(d[i]);
+}
+
+__global__ void fill_f32(int64_t n, float* __restrict__ x, float v) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    x[i] = v;
+}
+
+// ------------------------------------------------------------------ preconditioners
+__global__ void jacobi_setup(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                             const double* __restrict__ v, float* __restrict__ dinv, int32_t* status) {
+  for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n; r += int64_t(gridDim.x) * blockDim.x) {
+    double d = 0.0;
+    for (int32_t k = rp[r]; k < rp[r + 1]; ++k)
+      if (ci[k] == r) d = v[k];
+    if (d == 0.0) set_status(status, NFEM_ERR_BREAKDOWN);
+    dinv[r] = d != 0.0 ? float(1.0 / d) : 0.f;
+  }
+}
+
+__global__ void jacobi_apply(int64_t n, const float* __restrict__ dinv, const float* __restrict__ v,
+                             float* __restrict__ z) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    z[i] = dinv[i] * v[i];
+}
+
+// Extracts the principal submatrix A[dofs_c, dofs_c] of every cell and
+// inverts it (Gauss-Jordan with partial pivoting, FP64); stores FP32.
+template <int N>
+__global__ void block_extract_invert(int64_t n_cells, const int32_t* __restrict__ cd, const int32_t* __restrict__ rp,
+                                     const int32_t* __restrict__ ci, const double* __restrict__ v,
+                                     float* __restrict__ inv, int32_t* status) {
+  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < n_cells;
+       c += int64_t(gridDim.x) * blockDim.x) {
+    double a[N][2 * N];
+    int32_t d[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) d[i] = cd[c * N + i];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const int32_t b0 = rp[d[i]], b1 = rp[d[i] + 1];
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        int32_t lo = b0, hi = b1;
+        while (lo < hi) {
+          int32_t mid = (lo + hi) >> 1;
+          if (ci[mid] < d[j]) lo = mid + 1; else hi = mid;
+        }
+        a[i][j] = (lo < b1 && ci[lo] == d[j]) ? v[lo] : 0.0;
+        a[i][N + j] = i == j ? 1.0 : 0.0;
+      }
+    }
+    bool singular = false;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      int p = k;
+      double best = fabs(a[k][k]);
+#pragma unroll
+      for (int i = k + 1; i < N; ++i)
+        if (fabs(a[i][k]) > best) { best = fabs(a[i][k]); p = i; }
+      if (best == 0.0) { singular = true; break; }
+      if (p != k) {
+#pragma unroll
+        for (int j = 0; j < 2 * N; ++j) { double t = a[k][j]; a[k][j] = a[p][j]; a[p][j] = t; }
+      }
+      const double ip = 1.0 / a[k][k];
+#pragma unroll
+      for (int j = 0; j < 2 * N; ++j) a[k][j] *= ip;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        if (i == k) continue;
+        const double f = a[i][k];
+#pragma unroll
+        for (int j = 0; j < 2 * N; ++j) a[i][j] -= f * a[k][j];
+      }
+    }
+    if (singular) set_status(status, NFEM_ERR_BREAKDOWN);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = 0; j < N; ++j) inv[(c * N + i) * N + j] = singular ? 0.f : float(a[i][N + j]);
+  }
+}
+
+// z_r = (1 / m_r) sum over the incidences (c, a) of row r of (A_c^-1 v[dofs_c])_a
+template <int N>
+__global__ void block_apply(int64_t n_rows, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                            const int32_t* __restrict__ cd, const float* __restrict__ inv, const float* __restrict__ v,
+                            float* __restrict__ z) {
+  for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n_rows; r += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t kb = inc_ptr[r], ke = inc_ptr[r + 1];
+    float acc = 0.f;
+    for (int32_t k = kb; k < ke; ++k) {
+      const int32_t occ = inc[k];
+      const int32_t c = occ / N;
+      const int a = occ - c * N;
+      const float* row = inv + (int64_t(c) * N + a) * N;
+#pragma unroll
+      for (int b = 0; b < N; ++b) acc = fmaf(__ldg(row + b), __ldg(v + __ldg(cd + int64_t(c) * N + b)), acc);
+    }
+    z[r] = ke > kb ? acc / float(ke - kb) : v[r];
+  }
+}
+
+// ------------------------------------------------------------------ Hessenberg / Givens
+// Column j of H holds h[0..j+1]; rotations cs/sn; g the rotated rhs.
+__global__ void givens_update(double* __restrict__ H, int ldh, double* __restrict__ cs, double* __restrict__ sn,
+                              double* __restrict__ g, int j, double* __restrict__ hist, int32_t* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double* h = H + int64_t(j) * ldh;
+  for (int i = 0; i < j; ++i) {
+    const double t = cs[i] * h[i] + sn[i] * h[i + 1];
+    h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
+    h[i] = t;
+  }
+  const double a = h[j], b = h[j + 1];
+  const double rr = hypot(a, b);
+  if (!(rr > 0.0) || !isfinite(rr)) {
+    set_status(status, NFEM_ERR_BREAKDOWN);
+    cs[j] = 1.0;
+    sn[j] = 0.0;
+    hist[j] = fabs(g[j]);
+    return;
+  }
+  cs[j] = a / rr;
+  sn[j] = b / rr;
+  h[j] = rr;
+  h[j + 1] = 0.0;
+  g[j + 1] = -sn[j] * g[j];
+  g[j] = cs[j] * g[j];
+  hist[j] = fabs(g[j + 1]);
+}
+
+// y = R^-1 g for the leading k x k triangle of H (stored by columns)
+__global__ void upper_solve(const double* __restrict__ H, int ldh, const double* __restrict__ g, int k,
+                            double* __restrict__ y) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int i = k - 1; i >= 0; --i) {
+    double s = g[i];
+    for (int j = i + 1; j < k; ++j) s -= H[int64_t(j) * ldh + i] * y[j];
+    y[i] = s / H[int64_t(i) * ldh + i];
+  }
+}
+
+__global__ void add_small(int k, const double* __restrict__ y, double* __restrict__ h) {
+  for (int i = threadIdx.x; i < k; i += blockDim.x) h[i] += y[i];
+}
+
+__global__ void init_cycle(double* __restrict__ g, int m, const double* __restrict__ beta) {
+  for (int i = threadIdx.x; i <= m; i += blockDim.x) g[i] = i == 0 ? *beta : 0.0;
+}
+
+}  // namespace nfem
+
+using namespace nfem;
+
+// ===================================================================== C ABI
+extern "C" int nfem_spmv(int value_type, int64_t n_rows, const int32_t* row_ptr, const int32_t* col_idx,
+                         const void* values, const void* x, void* y, void* stream) {
+  if (n_rows < 0 || (n_rows > 0 && (!row_ptr || !col_idx || !values || !x || !y))) return NFEM_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (value_type == NFEM_F64)
+    return spmv<double, double, double>(n_rows, row_ptr, col_idx, (const double*)values, (const double*)x,
+                                        (double*)y, nullptr, 0, s);
+  if (value_type == NFEM_F32)
+    return spmv<float, float, float>(n_rows, row_ptr, col_idx, (const float*)values, (const float*)x, (float*)y,
+                                     nullptr, 0, s);
+  return NFEM_ERR_INVALID_ARG;
+}
+
+extern "C" int nfem_residual_f64(int64_t n_rows, const int32_t* row_ptr, const int32_t* col_idx,
+                                 const double* values, const double* x, const double* b, double* r, void* stream) {
+  if (n_rows < 0 || (n_rows > 0 && (!row_ptr || !col_idx || !values || !x || !b || !r))) return NFEM_ERR_INVALID_ARG;
+  return spmv<double, double, double>(n_rows, row_ptr, col_idx, values, x, r, b, 1, (cudaStream_t)stream);
+}
+
+extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, int32_t* dev_status, void* stream) {
+  if (!pc || !A64 || A64->value_type != NFEM_F64) return NFEM_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (pc->kind == NFEM_PC_JACOBI) {
+    if (!pc->diag_inv) return NFEM_ERR_INVALID_ARG;
+    jacobi_setup<<<grid_for(A64->n_rows, 256), 256, 0, s>>>(A64->n_rows, A64->row_ptr, A64->col_idx,
+                                                             (const double*)A64->values, pc->diag_inv, dev_status);
+  } else if (pc->kind == NFEM_PC_CELL_BLOCK) {
+    if (!pc->cell_dofs || !pc->block_inv) return NFEM_ERR_INVALID_ARG;
+    const int g = grid_for(pc->n_cells, 128);
+    switch (pc->n_loc) {
+      case 4: block_extract_invert<4><<<g, 128, 0, s>>>(pc->n_cells, pc->cell_dofs, A64->row_ptr, A64->col_idx,
+                                                        (const double*)A64->values, pc->block_inv, dev_status); break;
+      case 5: block_extract_invert<5><<<g, 128, 0, s>>>(pc->n_cells, pc->cell_dofs, A64->row_ptr, A64->col_idx,
+                                                        (const double*)A64->values, pc->block_inv, dev_status); break;
+      default: return NFEM_ERR_UNSUPPORTED;
+    }
+  } else if (pc->kind != NFEM_PC_NONE) {
+    return NFEM_ERR_UNSUPPORTED;
+  }
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, float* z, cudaStream_t s) {
+  const int B = 256;
+  switch (pc->kind) {
+    case NFEM_PC_NONE:
+      NFEM_TRY_CUDA(cudaMemcpyAsync(z, v, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      return NFEM_OK;
+    case NFEM_PC_JACOBI:
+      jacobi_apply<<<grid_for(n, B), B, 0, s>>>(n, pc->diag_inv, v, z);
+      break;
+    case NFEM_PC_CELL_BLOCK:
+      if (pc->n_loc == 5)
+        block_apply<5><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z);
+      else if (pc->n_loc == 4)
+        block_apply<4><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z);
+      else
+        return NFEM_ERR_UNSUPPORTED;
+      break;
+    default:
+      return NFEM_ERR_UNSUPPORTED;
+  }
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+extern "C" int nfem_precond_apply(const nfem_precond* pc, int64_t n, const float* v, float* z, void* stream) {
+  if (!pc || n < 0 || (n > 0 && (!v || !z))) return NFEM_ERR_INVALID_ARG;
+  if (n == 0) return NFEM_OK;
+  return precond_apply(pc, n, v, z, (cudaStream_t)stream);
+}
+
+// workspace layout of the solver
+struct SolveWs {
+  float *V, *Z, *w, *r32, *d32;
+  double *r64, *partial, *H, *cs, *sn, *g, *hist, *y, *scal;
+  int32_t* status;
+};
+
+static size_t solve_ws_bytes(int64_t n, int m, SolveWs* out, void* base) {
+  Carver c{reinterpret_cast<char*>(base), 0, ~size_t(0)};
+  SolveWs w;
+  w.V = c.take<float>(size_t(m + 1) * n);
+  w.Z = c.take<float>(size_t(m) * n);
+  w.w = c.take<float>(n);
+  w.r32 = c.take<float>(n);
+  w.d32 = c.take<float>(n);
+  w.r64 = c.take<double>(n);
+  w.partial = c.take<double>(size_t(kRedBlocks) * (m + 2));
+  w.H = c.take<double>(size_t(m) * (m + 1));
+  w.cs = c.take<double>(m + 1);
+  w.sn = c.take<double>(m + 1);
+  w.g = c.take<double>(m + 2);
+  w.hist = c.take<double>(m + 1);
+  w.y = c.take<double>(m + 1);
+  w.scal = c.take<double>(8);
+  w.status = c.take<int32_t>(4);
+  if (out) *out = w;
+  return c.off + 256;
+}
+
+extern "C" int nfem_solve_workspace_bytes(int64_t n, int restart, size_t* bytes) {
+  if (!bytes || n < 0 || restart < 1 || restart > kMaxRestart) return NFEM_ERR_INVALID_ARG;
+  *bytes = solve_ws_bytes(n, restart, nullptr, nullptr);
+  return NFEM_OK;
+}
+
+#define NFEM_RC(...)                \
+  do {                              \
+    int _rc = (__VA_ARGS__);        \
+    if (_rc != NFEM_OK) return _rc; \
+  } while (0)
+
+extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, const nfem_precond* pc,
+                                    const double* b, double* x, const nfem_solve_params* prm, void* workspace,
+                                    size_t workspace_bytes, nfem_solve_info* info, void* stream) {
+  if (!A64 || !A32 || !pc || !b || !x || !prm || !info) return NFEM_ERR_INVALID_ARG;
+  if (A64->value_type != NFEM_F64 || A32->value_type != NFEM_F32 || A64->n_rows != A32->n_rows)
+    return NFEM_ERR_INVALID_ARG;
+  const int64_t n = A64->n_rows;
+  const int m = prm->restart;
+  if (m < 1 || m > kMaxRestart) return NFEM_ERR_INVALID_ARG;
+  if (!workspace || workspace_bytes < solve_ws_bytes(n, m, nullptr, nullptr)) return NFEM_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  SolveWs w;
+  solve_ws_bytes(n, m, &w, workspace);
+  const int B = 256;
+  const int gv = grid_for(n, B);
+  const int ldh = m + 1;
+  NFEM_TRY_CUDA(cudaMemsetAsync(w.status, 0, 4 * sizeof(int32_t), s));
+  info->inner_iterations = 0;
+  info->outer_iterations = 0;
+  info->status = NFEM_OK;
+  double hb[2];
+  // ||b||
+  NFEM_RC(multidot<double>(n, 1, b, n, b, w.partial, w.scal + 0, 1, s));
+  NFEM_RC(spmv<double, double, double>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, x, w.r64, b, 1, s));
+  NFEM_RC(multidot<double>(n, 1, w.r64, n, w.r64, w.partial, w.scal + 1, 1, s));
+  NFEM_TRY_CUDA(cudaMemcpyAsync(hb, w.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  NFEM_TRY_CUDA(cudaStreamSynchronize(s));
+  const double nb = hb[0] > 0.0 ? hb[0] : 1.0;
+  double rel = hb[1] / nb;
+  info->initial_relres = rel;
+  std::vector<double> hist(m + 1);
+  while (rel > prm->rtol && info->outer_iterations < prm->max_outer &&
+         info->inner_iterations < prm->max_inner) {
+    info->outer_iterations++;
+    // inner problem A32 d = r32, d0 = 0
+    cast_f64_f32<<<gv, B, 0, s>>>(n, w.r64, w.r32);
+    fill_f32<<<gv, B, 0, s>>>(n, w.d32, 0.f);
+    NFEM_TRY_CUDA(cudaMemcpyAsync(w.V, w.r32, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    double inner0 = rel * nb;
+    double inner_target = fmax(prm->inner_rtol * inner0, 0.5 * prm->rtol * nb);
+    double inner_res = inner0;
+    bool inner_done = false;
+    bool first_cycle = true;
+    while (!inner_done && info->inner_iterations < prm->max_inner) {
+      // V0 = current inner residual (r32 - A32 d32 after the first cycle)
+      if (!first_cycle) {
+        NFEM_RC(spmv<float, float, float>(n, A32->row_ptr, A32->col_idx, (const float*)A32->values, w.d32, w.V,
+                                          w.r32, 1, s));
+      }
+      first_cycle = false;
+      NFEM_RC(multidot<float>(n, 1, w.V, n, w.V, w.partial, w.scal + 2, 1, s));
+      scale_by_inv<float><<<gv, B, 0, s>>>(n, w.V, w.scal + 2, w.V);
+      init_cycle<<<1, 128, 0, s>>>(w.g, m, w.scal + 2);
+      NFEM_CHECK_LAUNCH();
+      int j = 0;
+      for (; j < m; ++j) {
+        float* vj = w.V + int64_t(j) * n;
+        float* zj = w.Z + int64_t(j) * n;
+        NFEM_RC(precond_apply(pc, n, vj, zj, s));
+        NFEM_RC(spmv<float, float, float>(n, A32->row_ptr, A32->col_idx, (const float*)A32->values, zj, w.w,
+                                          nullptr, 0, s));
+        double* hcol = w.H + int64_t(j) * ldh;
+        // classical Gram-Schmidt, twice
+        NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, hcol, 0, s));
+        multi_axpy<float><<<gv, B, 0, s>>>(n, j + 1, w.V, n, hcol, w.w, 1.0);
+        NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, w.y, 0, s));
+        multi_axpy<float><<<gv, B, 0, s>>>(n, j + 1, w.V, n, w.y, w.w, 1.0);
+        add_small<<<1, 64, 0, s>>>(j + 1, w.y, hcol);  // h += second-pass coefficients
+        NFEM_RC(multidot<float>(n, 1, w.w, n, w.w, w.partial, hcol + j + 1, 1, s));
+        scale_by_inv<float><<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * n);
+        givens_update<<<1, 32, 0, s>>>(w.H, ldh, w.cs, w.sn, w.g, j, w.hist, w.status);
+        NFEM_CHECK_LAUNCH();
+      }
+      // one synchronisation per cycle: residual estimates of every step
+      NFEM_TRY_CUDA(cudaMemcpyAsync(hist.data(), w.hist, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+      NFEM_TRY_CUDA(cudaStreamSynchronize(s));
+      int k = m;
+      for (int i = 0; i < m; ++i) {
+        if (hist[i] <= inner_target || !std::isfinite(hist[i])) { k = i + 1; break; }
+      }
+      info->inner_iterations += k;
+      inner_res = hist[k - 1];
+      upper_solve<<<1, 32, 0, s>>>(w.H, ldh, w.g, k, w.y);
+      // d += Z y   (multi_axpy subtracts: pass -1 via hsign)
+      multi_axpy<float><<<gv, B, 0, s>>>(n, k, w.Z, n, w.y, w.d32, -1.0);
+      NFEM_CHECK_LAUNCH();
+      if (!std::isfinite(inner_res)) {
+        info->status = NFEM_ERR_NONFINITE;
+        return NFEM_ERR_NONFINITE;
+      }
+      if (inner_res <= inner_target) inner_done = true;
+    }
+    add_f32_to_f64<<<gv, B, 0, s>>>(n, w.d32, x);
+    NFEM_RC(spmv<double, double, double>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, x, w.r64, b, 1,
+                                         s));
+    NFEM_RC(multidot<double>(n, 1, w.r64, n, w.r64, w.partial, w.scal + 1, 1, s));
+    NFEM_TRY_CUDA(cudaMemcpyAsync(hb + 1, w.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    NFEM_TRY_CUDA(cudaStreamSynchronize(s));
+    rel = hb[1] / nb;
+    if (!std::isfinite(rel)) {
+      info->status = NFEM_ERR_NONFINITE;
+      info->final_relres = rel;
+      return NFEM_ERR_NONFINITE;
+    }
+  }
+  info->final_relres = rel;
+  int32_t st = 0;
+  NFEM_TRY_CUDA(cudaMemcpyAsync(&st, w.status, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  NFEM_TRY_CUDA(cudaStreamSynchronize(s));
+  if (rel > prm->rtol) info->status = st ? st : NFEM_ERR_NOT_CONVERGED;
+  return info->status;
+}

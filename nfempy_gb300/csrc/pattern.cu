@@ -209,6 +209,23 @@ __global__ void local_codes_kernel(const int32_t* __restrict__ cd, int n_loc, in
   }
 }
 
+// Fixed-stride incidence layout for rows with at most two incidences:
+// pairs[r] = (occ0, occ1) with -1 for absent, pair_codes[r] = (code0, code1).
+__global__ void pairs_kernel(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                             const uint32_t* __restrict__ codes, int64_t n_rows, int2* __restrict__ pairs,
+                             uint2* __restrict__ pair_codes, int32_t* status) {
+  for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n_rows; r += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t b = inc_ptr[r], e = inc_ptr[r + 1];
+    if (e - b > 2) set_status(status, NFEM_ERR_UNSUPPORTED);
+    int2 pr = make_int2(-1, -1);
+    uint2 cd = make_uint2(0u, 0u);
+    if (e > b) { pr.x = inc[b]; cd.x = codes[b]; }
+    if (e > b + 1) { pr.y = inc[b + 1]; cd.y = codes[b + 1]; }
+    pairs[r] = pr;
+    pair_codes[r] = cd;
+  }
+}
+
 static size_t pattern_bytes(int64_t n_rows) {
   size_t b = 0;
   b += align256(size_t(n_rows) * 4) * 3;                 // counts, cursor, row_len
@@ -304,6 +321,21 @@ extern "C" int nfem_pattern_local_codes(const int32_t* cd, int64_t n_cells, int 
   if (n_rows == 0) return NFEM_OK;
   local_codes_kernel<<<grid_for(n_rows, 256), 256, 0, stream>>>(cd, n_loc, ld, n_rows, inc_ptr, inc, row_ptr, col_idx,
                                                                 codes, dev_status);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+extern "C" int nfem_pattern_pairs(const int32_t* inc_ptr, const int32_t* inc, const uint32_t* codes,
+                                  int64_t n_rows, int32_t* pairs, uint32_t* pair_codes, int32_t* dev_status,
+                                  void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n_rows < 0 || (n_rows > 0 && (!inc_ptr || !inc || !codes || !pairs || !pair_codes)))
+    return NFEM_ERR_INVALID_ARG;
+  if ((reinterpret_cast<uintptr_t>(pairs) & 7) || (reinterpret_cast<uintptr_t>(pair_codes) & 7))
+    return NFEM_ERR_INVALID_ARG;
+  if (n_rows == 0) return NFEM_OK;
+  pairs_kernel<<<grid_for(n_rows, 256), 256, 0, stream>>>(inc_ptr, inc, codes, n_rows, reinterpret_cast<int2*>(pairs),
+                                                          reinterpret_cast<uint2*>(pair_codes), dev_status);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }

@@ -1,0 +1,117 @@
+"""Device Krylov solve: the step the reference drivers hand to PETSc KSP.
+
+    A = CSRMatrix(space, torch.float64); assemble ...
+    ksp = KrylovSolver(A, pc="cell_block")
+    x, info = ksp.solve(b, rtol=1e-8)
+
+A is the FP64 matrix (the residual is always measured on it, in FP64); the
+solver keeps an FP32 copy with the same pattern for the inner FGMRES
+iterations, refreshed from A (or assembled directly in FP32 by the caller
+and passed as A32).  Preconditioners: "none", "jacobi", "cell_block"
+(cell-patch block Jacobi = weighted additive Schwarz over the element
+cliques, blocks inverted in FP64, applied in FP32).
+Reference call sites: examples/md_elliptic_scalar/md_elliptic_scalar.py:343-363,
+examples/cauchy_elasticity/cg_elasticity_example_1.py:159-170.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+
+
+class SolveResult:
+    def __init__(self, info, seconds=None):
+        self.inner_iterations = info.inner_iterations
+        self.outer_iterations = info.outer_iterations
+        self.initial_relres = info.initial_relres
+        self.final_relres = info.final_relres
+        self.status = info.status
+        self.seconds = seconds
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k in ("inner_iterations", "outer_iterations", "initial_relres",
+                                              "final_relres", "status", "seconds")}
+
+
+def _csr(A, values=None):
+    v = A.values if values is None else values
+    vt = _lib.NFEM_F64 if v.dtype == torch.float64 else _lib.NFEM_F32
+    return _lib.Csr(A.n_rows, _lib.ptr(A.row_ptr).value, _lib.ptr(A.col_idx).value, _lib.ptr(v).value, vt)
+
+
+class KrylovSolver:
+    def __init__(self, A, pc="cell_block", A32_values=None, restart=30):
+        if A.dtype != torch.float64:
+            raise ValueError("A must be the FP64 matrix (the residual is measured in FP64)")
+        self.A = A
+        self.restart = int(restart)
+        self.values32 = A32_values
+        self.pc_kind = pc
+        self._setup_done = False
+        self.status = torch.zeros(1, dtype=torch.int32, device=A.values.device)
+
+    def set_operators(self, A32_values=None):
+        """Refresh the FP32 copy and the preconditioner after A changed."""
+        if A32_values is not None:
+            self.values32 = A32_values
+        self._setup_done = False
+
+    def setup(self, stream=None):
+        A = self.A
+        dev = A.values.device
+        if self.values32 is None or self.values32.data_ptr() == 0:
+            self.values32 = A.values.to(torch.float32)
+        st = _lib.stream_ptr(stream)
+        sp = A.space
+        if self.pc_kind == "none":
+            self.pc = _lib.Precond(_lib.PC_NONE, 0, 0, None, None, None, None, None)
+        elif self.pc_kind == "jacobi":
+            self.diag_inv = torch.empty(A.n_rows, dtype=torch.float32, device=dev)
+            self.pc = _lib.Precond(_lib.PC_JACOBI, 0, 0, None, None, None, None, _lib.ptr(self.diag_inv).value)
+        elif self.pc_kind == "cell_block":
+            n_loc = sp.n_loc
+            if n_loc not in (4, 5):
+                raise NotImplementedError("cell_block preconditioner for 4 or 5 local DoFs")
+            self.block_inv = torch.empty((sp.n_cells, n_loc, n_loc), dtype=torch.float32, device=dev)
+            self.pc = _lib.Precond(_lib.PC_CELL_BLOCK, n_loc, sp.n_cells, _lib.ptr(sp.cell_dofs).value,
+                                   _lib.ptr(A.inc_ptr).value, _lib.ptr(A.inc).value,
+                                   _lib.ptr(self.block_inv).value, None)
+        else:
+            raise ValueError(f"unknown preconditioner {self.pc_kind}")
+        a64 = _csr(A)
+        _lib.call("nfem_precond_setup", _lib.C.byref(self.pc), _lib.C.byref(a64), _lib.ptr(self.status), st)
+        ws_b = _lib.C.c_size_t(0)
+        _lib.call("nfem_solve_workspace_bytes", A.n_rows, self.restart, _lib.C.byref(ws_b))
+        self.ws = torch.empty(int(ws_b.value), dtype=torch.uint8, device=dev)
+        self._setup_done = True
+        if int(self.status.item()):
+            s = int(self.status.item())
+            self.status.zero_()
+            raise _lib.NfemError(s, "preconditioner setup")
+
+    def solve(self, b, x=None, rtol=1e-8, inner_rtol=1e-4, max_inner=100000, max_outer=20, stream=None,
+              raise_on_failure=True):
+        """Solve A x = b (FP64 device tensors) to ||b - A x|| / ||b|| <= rtol."""
+        if not self._setup_done:
+            self.setup(stream)
+        A = self.A
+        if x is None:
+            x = torch.zeros(A.n_rows, dtype=torch.float64, device=b.device)
+        prm = _lib.SolveParams(float(rtol), float(inner_rtol), self.restart, int(max_inner), int(max_outer))
+        info = _lib.SolveInfo()
+        a64 = _csr(A)
+        a32 = _csr(A, self.values32)
+        rc = _lib.lib().nfem_solve_ir_fgmres(_lib.C.byref(a64), _lib.C.byref(a32), _lib.C.byref(self.pc),
+                                              _lib.ptr(b), _lib.ptr(x), _lib.C.byref(prm), _lib.ptr(self.ws),
+                                              self.ws.numel(), _lib.C.byref(info), _lib.stream_ptr(stream))
+        res = SolveResult(info)
+        if rc != 0 and raise_on_failure:
+            raise _lib.NfemError(rc, f"solve ({res.as_dict()})")
+        return x, res
+
+    def residual(self, x, b, stream=None):
+        r = torch.empty_like(b)
+        A = self.A
+        _lib.call("nfem_residual_f64", A.n_rows, _lib.ptr(A.row_ptr), _lib.ptr(A.col_idx), _lib.ptr(A.values),
+                  _lib.ptr(x), _lib.ptr(b), _lib.ptr(r), _lib.stream_ptr(stream))
+        return r
