@@ -41,7 +41,7 @@ typedef enum {
   NFEM_ERR_DEGENERATE = 11    /* a cell with |det J| == 0 */
 } nfem_status;
 
-typedef enum { NFEM_F64 = 0, NFEM_F32 = 1 } nfem_value_type;
+typedef enum { NFEM_F64 = 0, NFEM_F32 = 1, NFEM_BF16 = 2 } nfem_value_type;
 
 /* Coefficient sampling modes for per-cell data arrays. */
 typedef enum {
@@ -207,11 +207,35 @@ typedef struct {
 
 typedef enum {
   NFEM_PC_NONE = 0,
-  NFEM_PC_JACOBI = 1,     /* point Jacobi: diag_inv [n_rows] */
-  NFEM_PC_CELL_BLOCK = 2  /* cell-patch block Jacobi (weighted additive Schwarz over
-                             the element cliques): cell_dofs [n_cells, n_loc],
-                             block_inv [n_cells, n_loc, n_loc], row incidences */
+  NFEM_PC_JACOBI = 1,      /* point Jacobi: diag_inv [n_rows] */
+  NFEM_PC_CELL_BLOCK = 2,  /* cell-patch block Jacobi (weighted additive Schwarz over
+                              the element cliques): cell_dofs [n_cells, n_loc],
+                              block_inv [n_cells, n_loc, n_loc], row incidences */
+  NFEM_PC_LEARNED = 3      /* NFEM_PC_CELL_BLOCK plus a learned coarse correction of
+                              the pressure (P0) DoFs: the network maps the
+                              aggregate sums of the pressure residual (normalised)
+                              and one feature per aggregate to an aggregate
+                              pressure correction (see nfem_learned_coarse) */
 } nfem_pc_kind;
+
+/* Learned coarse correction: M(v) = B(v) + P (s * f([R v / s, feat])) with B
+ * the cell-block Jacobi, R the sum of v's pressure entries over each
+ * aggregate of cells, s = ||R v||_2, f the MLP with dims {2 n_agg, h1, h2,
+ * n_agg}, P the injection of an aggregate value into the pressure DoFs of its
+ * cells scaled by out_scale.  work holds 2 n_agg + h1 + h2 + n_agg + 64 floats. */
+typedef struct {
+  int64_t p_base;            /* pressure DoF of cell c is p_base + c */
+  int32_t n_agg;
+  int32_t mlp_dims[4];
+  const int32_t* agg_ptr;    /* [n_agg + 1] cells of each aggregate (CSR) */
+  const int32_t* agg_cells;  /* [n_cells] */
+  const int32_t* cell_agg;   /* [n_cells] */
+  const float* agg_feat;     /* [n_agg] */
+  const void* params_bf16;   /* network weights (BF16) */
+  const float* params_f32;   /* FP32 master copy (biases read from here) */
+  float* work;
+  float out_scale;
+} nfem_learned_coarse;
 
 typedef struct {
   int kind;
@@ -222,14 +246,28 @@ typedef struct {
   const int32_t* inc;
   float* block_inv;
   float* diag_inv;
+  /* Optional weighted inner product for the flexible GMRES: W^1/2 and W^-1/2
+   * [n_rows] filled by nfem_precond_setup (which then needs setup_scratch,
+   * 2 * n_rows doubles).  W balances the flux and pressure rows of saddle-point
+   * systems: W_i = sqrt(s_i^2 c_i^2), s_i^2 = 1/|a_ii| (or the inverse Schur
+   * diagonal sum_j a_ij^2/|a_jj| where a_ii = 0), c_i^2 = squared column norm
+   * of the preconditioner.  NULL = Euclidean inner product. */
+  float* wsqrt;
+  float* winvsqrt;
+  double* setup_scratch;
+  const nfem_learned_coarse* learned; /* NFEM_PC_LEARNED only (host pointer) */
 } nfem_precond;
 
 typedef struct {
   double rtol;        /* FP64 relative residual target */
   double inner_rtol;  /* reduction asked of each FP32 inner solve */
-  int restart;        /* GMRES restart length, 1..64 */
+  int restart;        /* GMRES restart length, 1..128 */
   int max_inner;      /* cap on total inner iterations */
   int max_outer;      /* cap on refinement steps */
+  float* snapshots;   /* optional [max_snapshots, n_rows] FP32: the iterate after
+                         every restart cycle (training data for the learned
+                         preconditioner); NULL = none */
+  int max_snapshots;
 } nfem_solve_params;
 
 typedef struct {
@@ -238,6 +276,7 @@ typedef struct {
   double initial_relres;
   double final_relres;
   int status;
+  int n_snapshots;
 } nfem_solve_info;
 
 /* y = A x (FP32 or FP64 matrix and vectors) */
@@ -258,6 +297,29 @@ int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, const nfem_pr
                          const double* b, double* x, const nfem_solve_params* params,
                          void* workspace, size_t workspace_bytes, nfem_solve_info* info,
                          void* stream);
+
+/* ----------------------------------- K6: learned preconditioner network
+ * No counterpart in the reference (nfempy has no learned component).
+ * Network x -> relu(W1 x + b1) -> relu(W2 h1 + b2) -> W3 h2 + b3, dims =
+ * {in, h1, h2, out}, parameters flat [W1 | b1 | W2 | b2 | W3 | b3] with
+ * W_l [out, in] row-major; activations batch-major.  weight_type NFEM_BF16
+ * reads BF16 weights (and biases from params_f32), FP32 accumulation. */
+int nfem_mlp_param_count(const int32_t* dims, int64_t* count);
+int nfem_mlp_forward(const int32_t* dims, int weight_type, const void* params,
+                     const float* params_f32, int64_t batch, const float* x, float* h1,
+                     float* h2, float* y, void* stream);
+/* Gradients of loss = 0.5 / batch * sum ||y - target||^2 into grads (flat,
+ * FP32, same layout as the parameters); loss (device double) optional. */
+int nfem_mlp_backward_workspace_bytes(const int32_t* dims, int64_t batch, size_t* bytes);
+int nfem_mlp_backward(const int32_t* dims, int weight_type, const void* params, int64_t batch,
+                      const float* x, const float* h1, const float* h2, const float* y,
+                      const float* target, float* grads, void* workspace,
+                      size_t workspace_bytes, double* loss, void* stream);
+/* Adam on the flat FP32 parameters; refreshes params_bf16 when non-NULL. */
+int nfem_adam_step(int64_t n, float* params, const float* grads, float* m, float* v, float lr,
+                   float beta1, float beta2, float eps, int step, void* params_bf16,
+                   void* stream);
+int nfem_to_bf16(int64_t n, const float* x, void* out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "libnfem_gb300.so")
 NFEM_OK = 0
 NFEM_F64 = 0
 NFEM_F32 = 1
+NFEM_BF16 = 2
 COEF_NONE, COEF_CELL, COEF_QPOINT = 0, 1, 2
 
 STATUS_NAMES = {
@@ -41,22 +42,31 @@ class Csr(C.Structure):
                 ("value_type", C.c_int)]
 
 
+class LearnedCoarse(C.Structure):
+    _fields_ = [("p_base", C.c_int64), ("n_agg", C.c_int32), ("mlp_dims", C.c_int32 * 4), ("agg_ptr", C.c_void_p),
+                ("agg_cells", C.c_void_p), ("cell_agg", C.c_void_p), ("agg_feat", C.c_void_p),
+                ("params_bf16", C.c_void_p), ("params_f32", C.c_void_p), ("work", C.c_void_p),
+                ("out_scale", C.c_float)]
+
+
 class Precond(C.Structure):
     _fields_ = [("kind", C.c_int), ("n_loc", C.c_int), ("n_cells", C.c_int64), ("cell_dofs", C.c_void_p),
-                ("inc_ptr", C.c_void_p), ("inc", C.c_void_p), ("block_inv", C.c_void_p), ("diag_inv", C.c_void_p)]
+                ("inc_ptr", C.c_void_p), ("inc", C.c_void_p), ("block_inv", C.c_void_p), ("diag_inv", C.c_void_p),
+                ("wsqrt", C.c_void_p), ("winvsqrt", C.c_void_p), ("setup_scratch", C.c_void_p),
+                ("learned", C.POINTER(LearnedCoarse))]
 
 
 class SolveParams(C.Structure):
     _fields_ = [("rtol", C.c_double), ("inner_rtol", C.c_double), ("restart", C.c_int), ("max_inner", C.c_int),
-                ("max_outer", C.c_int)]
+                ("max_outer", C.c_int), ("snapshots", C.c_void_p), ("max_snapshots", C.c_int)]
 
 
 class SolveInfo(C.Structure):
     _fields_ = [("inner_iterations", C.c_int), ("outer_iterations", C.c_int), ("initial_relres", C.c_double),
-                ("final_relres", C.c_double), ("status", C.c_int)]
+                ("final_relres", C.c_double), ("status", C.c_int), ("n_snapshots", C.c_int)]
 
 
-PC_NONE, PC_JACOBI, PC_CELL_BLOCK = 0, 1, 2
+PC_NONE, PC_JACOBI, PC_CELL_BLOCK, PC_LEARNED = 0, 1, 2, 3
 
 _P = C.c_void_p
 _I = C.c_int
@@ -88,6 +98,12 @@ _SIGS = {
     "nfem_solve_workspace_bytes": ([_I64, _I, C.POINTER(_SZ)], _I),
     "nfem_solve_ir_fgmres": ([C.POINTER(Csr), C.POINTER(Csr), C.POINTER(Precond), _P, _P, C.POINTER(SolveParams),
                               _P, _SZ, C.POINTER(SolveInfo), _P], _I),
+    "nfem_mlp_param_count": ([_P, C.POINTER(_I64)], _I),
+    "nfem_mlp_forward": ([_P, _I, _P, _P, _I64, _P, _P, _P, _P, _P], _I),
+    "nfem_mlp_backward_workspace_bytes": ([_P, _I64, C.POINTER(_SZ)], _I),
+    "nfem_mlp_backward": ([_P, _I, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _SZ, _P, _P], _I),
+    "nfem_adam_step": ([_I64, _P, _P, _P, _P, C.c_float, C.c_float, C.c_float, C.c_float, _I, _P, _P], _I),
+    "nfem_to_bf16": ([_I64, _P, _P, _P], _I),
 }
 
 _lib = None

@@ -69,6 +69,26 @@ class CSRMatrix:
         self.fresh = True
         self.check_status("pattern")
 
+    def with_dtype(self, dtype):
+        """A matrix with the same pattern (index arrays shared) and its own values."""
+        other = object.__new__(CSRMatrix)
+        other.__dict__.update(self.__dict__)
+        other.dtype = dtype
+        other.values = torch.zeros_like(self.values, dtype=dtype)
+        other.status = torch.zeros_like(self.status)
+        other.fresh = True
+        return other
+
+    def spmv(self, x, y=None, stream=None):
+        """y = A x on the device (x of the matrix dtype)."""
+        if y is None:
+            y = torch.empty(self.n_rows, dtype=self.dtype, device=self.values.device)
+        vt = _lib.NFEM_F64 if self.dtype == torch.float64 else _lib.NFEM_F32
+        x = x.to(self.dtype).contiguous()
+        _lib.call("nfem_spmv", vt, self.n_rows, _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx), _lib.ptr(self.values),
+                  _lib.ptr(x), _lib.ptr(y), _lib.stream_ptr(stream))
+        return y
+
     def check_status(self, where=""):
         s = int(self.status.item())
         if s:

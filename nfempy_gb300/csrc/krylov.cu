@@ -30,20 +30,23 @@
 
 #include "nfem_common.cuh"
 
+extern "C" int nfem_mlp_forward(const int32_t* dims, int weight_type, const void* params, const float* params_f32,
+                                int64_t batch, const float* x, float* h1, float* h2, float* y, void* stream);
+
 namespace nfem {
 
-constexpr int kRedBlocks = 304;  // 2 x 152 SMs
+constexpr int kRedBlocks = 1216;  // 8 x 152 SMs
 constexpr int kRedThreads = 256;
 constexpr int kSpmvWarps = 8;
 constexpr int kSpmvCap = 32 * 16;
-constexpr int kMaxRestart = 64;
+constexpr int kMaxRestart = 128;
 
 // ------------------------------------------------------------------ SpMV
 template <typename VT, typename XT, typename AT>
 __global__ void __launch_bounds__(32 * kSpmvWarps)
     spmv_kernel(int64_t n_rows, const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
                 const VT* __restrict__ val, const XT* __restrict__ x, XT* __restrict__ y,
-                const XT* __restrict__ b, int residual) {
+                const XT* __restrict__ b, int residual, const float* __restrict__ yscale) {
   __shared__ AT stage[kSpmvWarps][kSpmvCap];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   AT* st = stage[warp];
@@ -70,16 +73,20 @@ __global__ void __launch_bounds__(32 * kSpmvWarps)
     } else if (valid) {
       for (int32_t k = rb; k < re; ++k) acc += AT(__ldg(val + k)) * AT(__ldg(x + __ldg(col + k)));
     }
-    if (valid) y[r] = residual ? XT(AT(b[r]) - acc) : XT(acc);
+    if (valid) {
+      AT out = residual ? AT(b[r]) - acc : acc;
+      if (yscale) out *= AT(yscale[r]);
+      y[r] = XT(out);
+    }
   }
 }
 
 template <typename VT, typename XT, typename AT>
 static int spmv(int64_t n, const int32_t* rp, const int32_t* ci, const VT* v, const XT* x, XT* y, const XT* b,
-                int residual, cudaStream_t s) {
+                int residual, cudaStream_t s, const float* yscale = nullptr) {
   if (n == 0) return NFEM_OK;
   const int grid = grid_for(ceil_div(n, 32 * kSpmvWarps), 1, 8);
-  spmv_kernel<VT, XT, AT><<<grid, 32 * kSpmvWarps, 0, s>>>(n, rp, ci, v, x, y, b, residual);
+  spmv_kernel<VT, XT, AT><<<grid, 32 * kSpmvWarps, 0, s>>>(n, rp, ci, v, x, y, b, residual, yscale);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }
@@ -101,48 +108,86 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return t;
 }
 
-// partial[j * kRedBlocks + block] = sum_i X_j[i] * y[i] for j < k (X_j = X + j * ldx)
+// partial[j * gridDim.x + block] = sum_i X_j[i] * y[i] for j < k (X_j = X + j * ldx).
+// Eight basis vectors per pass share one read of y; each thread keeps two
+// elements in flight per vector (memory-level parallelism for HBM).
+constexpr int kDotGroup = 8;
+
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads)
     multidot_partial(int64_t n, int k, const T* __restrict__ X, int64_t ldx, const T* __restrict__ y,
                      double* __restrict__ partial) {
-  __shared__ double sh[32];
-  for (int j = 0; j < k; ++j) {
-    const T* xj = X + int64_t(j) * ldx;
-    float accf = 0.f;
-    double acc = 0.0;
+  __shared__ double sh[kDotGroup][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int j0 = 0; j0 < k; j0 += kDotGroup) {
+    const int g = min(kDotGroup, k - j0);
+    double acc[kDotGroup];
+    float accf[kDotGroup];
+#pragma unroll
+    for (int q = 0; q < kDotGroup; ++q) { acc[q] = 0.0; accf[q] = 0.f; }
     int cnt = 0;
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += 2 * stride) {
+      const int64_t i2 = i + stride;
+      const bool has2 = i2 < n;
+      const float y0 = float(__ldg(y + i));
+      const float y1 = has2 ? float(__ldg(y + i2)) : 0.f;
+#pragma unroll
+      for (int q = 0; q < kDotGroup; ++q) {
+        if (q < g) {
+          const T* xj = X + int64_t(j0 + q) * ldx;
+          const float x0 = float(__ldg(xj + i));
+          const float x1 = has2 ? float(__ldg(xj + i2)) : 0.f;
+          if constexpr (sizeof(T) == 4) {
+            accf[q] = fmaf(x0, y0, fmaf(x1, y1, accf[q]));
+          } else {
+            acc[q] += double(__ldg(xj + i)) * double(__ldg(y + i)) +
+                      (has2 ? double(__ldg(xj + i2)) * double(__ldg(y + i2)) : 0.0);
+          }
+        }
+      }
       if constexpr (sizeof(T) == 4) {
-        accf = fmaf(float(xj[i]), float(y[i]), accf);
-        if (++cnt == 64) { acc += double(accf); accf = 0.f; cnt = 0; }
-      } else {
-        acc += double(xj[i]) * double(y[i]);
+        if (++cnt == 32) {
+#pragma unroll
+          for (int q = 0; q < kDotGroup; ++q) { acc[q] += double(accf[q]); accf[q] = 0.f; }
+          cnt = 0;
+        }
       }
     }
-    acc += double(accf);
-    double t = block_sum(acc, sh);
-    if (threadIdx.x == 0) partial[int64_t(j) * gridDim.x + blockIdx.x] = t;
+#pragma unroll
+    for (int q = 0; q < kDotGroup; ++q) {
+      double v = acc[q] + double(accf[q]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) sh[q][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < g) {
+      double t = 0.0;
+      for (int w = 0; w < (kRedThreads / 32); ++w) t += sh[threadIdx.x][w];
+      partial[int64_t(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+    }
+    __syncthreads();
   }
 }
 
-// out[j] = scale * sum_b partial[j][b] (fixed order); mode 1: out = sqrt(sum)
+// out[j] = sum_b partial[j][b] (fixed order, one block per j); mode 1: sqrt
 __global__ void reduce_partials(const double* __restrict__ partial, int nb, int k, double* __restrict__ out,
                                 int mode, double sign) {
   __shared__ double sh[32];
-  for (int j = 0; j < k; ++j) {
-    double v = 0.0;
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) v += partial[int64_t(j) * nb + b];
-    double t = block_sum(v, sh);
-    if (threadIdx.x == 0) out[j] = mode == 1 ? sqrt(t) : sign * t;
-  }
+  const int j = blockIdx.x;
+  if (j >= k) return;
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) v += partial[int64_t(j) * nb + b];
+  double t = block_sum(v, sh);
+  if (threadIdx.x == 0) out[j] = mode == 1 ? sqrt(t) : sign * t;
 }
 
 template <typename T>
 static int multidot(int64_t n, int k, const T* X, int64_t ldx, const T* y, double* partial, double* out, int mode,
                     cudaStream_t s) {
   multidot_partial<T><<<kRedBlocks, kRedThreads, 0, s>>>(n, k, X, ldx, y, partial);
-  reduce_partials<<<1, 1024, 0, s>>>(partial, kRedBlocks, k, out, mode, 1.0);
+  reduce_partials<<<k, 256, 0, s>>>(partial, kRedBlocks, k, out, mode, 1.0);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }
@@ -154,10 +199,20 @@ __global__ void multi_axpy(int64_t n, int k, const T* __restrict__ X, int64_t ld
   __shared__ double hs[kMaxRestart + 1];
   for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = hsign * h[j];
   __syncthreads();
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
-    float acc = 0.f;
-    for (int j = 0; j < k; ++j) acc = fmaf(float(hs[j]), float(X[int64_t(j) * ldx + i]), acc);
-    w[i] = T(float(w[i]) - acc);
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += 2 * stride) {
+    const int64_t i2 = i + stride;
+    const bool has2 = i2 < n;
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < k; ++j) {
+      const float hj = float(hs[j]);
+      const T* xj = X + int64_t(j) * ldx;
+      a0 = fmaf(hj, float(__ldg(xj + i)), a0);
+      if (has2) a1 = fmaf(hj, float(__ldg(xj + i2)), a1);
+    }
+    w[i] = T(float(w[i]) - a0);
+    if (has2) w[i2] = T(float(w[i2]) - a1);
   }
 }
 
@@ -168,6 +223,114 @@ __global__ void scale_by_inv(int64_t n, const T* __restrict__ w, const double* _
   const float inv = d > 0.0 ? float(1.0 / d) : 0.f;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
     v[i] = T(float(w[i]) * inv);
+}
+
+// y = a (.) x  (elementwise)
+__global__ void scale_vec(int64_t n, const float* __restrict__ a, const float* __restrict__ x, float* __restrict__ y) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    y[i] = a[i] * x[i];
+}
+
+// Weights of the inner product the flexible GMRES minimises in.  s_i^2 is
+// |a_ii|^-1 for rows with a diagonal and (sum_j a_ij^2 / |a_jj|)^-1 for rows
+// without one (the pressure rows of a saddle point, a Schur-complement
+// diagonal); c_i^2 is the squared column norm of the preconditioner (1 when
+// there is none).  W_i = sqrt(s_i^2 c_i^2), stored as W^1/2 and W^-1/2.
+__global__ void weights_rows(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                             const double* __restrict__ v, double* __restrict__ s2) {
+  for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n; r += int64_t(gridDim.x) * blockDim.x) {
+    double d = 0.0;
+    for (int32_t k = rp[r]; k < rp[r + 1]; ++k)
+      if (ci[k] == r) d = fabs(v[k]);
+    if (d > 0.0) {
+      s2[r] = 1.0 / d;
+    } else {
+      double acc = 0.0;
+      for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
+        const int32_t j = ci[k];
+        double dj = 0.0;
+        for (int32_t q = rp[j]; q < rp[j + 1]; ++q)
+          if (ci[q] == j) dj = fabs(v[q]);
+        if (dj > 0.0) acc += v[k] * v[k] / dj;
+      }
+      s2[r] = acc > 0.0 ? 1.0 / acc : 1.0;
+    }
+  }
+}
+
+// c_i^2 = sum over the incidences (c, a) of column i of sum_b (inv[c][b][a] / m_b)^2
+template <int N>
+__global__ void weights_blockcols(int64_t n_rows, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                  const int32_t* __restrict__ cd, const float* __restrict__ inv, double* __restrict__ c2) {
+  for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n_rows; r += int64_t(gridDim.x) * blockDim.x) {
+    double acc = 0.0;
+    for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; ++k) {
+      const int32_t occ = inc[k];
+      const int32_t c = occ / N;
+      const int a = occ - c * N;
+      for (int b = 0; b < N; ++b) {
+        const int32_t db = cd[int64_t(c) * N + b];
+        const double mb = double(inc_ptr[db + 1] - inc_ptr[db]);
+        const double x = double(inv[(int64_t(c) * N + b) * N + a]) / mb;
+        acc += x * x;
+      }
+    }
+    c2[r] = acc > 0.0 ? acc : 1.0;
+  }
+}
+
+__global__ void weights_final(int64_t n, const double* __restrict__ s2, const double* __restrict__ c2,
+                              float* __restrict__ wsqrt, float* __restrict__ winvsqrt) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const double w = sqrt(s2[i] * (c2 ? c2[i] : 1.0));
+    wsqrt[i] = float(sqrt(w));
+    winvsqrt[i] = float(1.0 / sqrt(w));
+  }
+}
+
+// ---- learned coarse correction
+// rc[a] = sum over the cells of aggregate a of v[p_base + c] (cell order)
+__global__ void coarse_restrict(int n_agg, const int32_t* __restrict__ agg_ptr, const int32_t* __restrict__ agg_cells,
+                                int64_t p_base, const float* __restrict__ v, float* __restrict__ rc) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n_agg) return;
+  float acc = 0.f;
+  for (int32_t k = agg_ptr[warp] + lane; k < agg_ptr[warp + 1]; k += 32) acc += v[p_base + agg_cells[k]];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) rc[warp] = acc;
+}
+
+// x_in = [rc / s, feat], s = ||rc|| stored in *s_out (single block)
+__global__ void coarse_input(int n_agg, const float* __restrict__ rc, const float* __restrict__ feat,
+                             float* __restrict__ x_in, float* __restrict__ s_out) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n_agg; i += blockDim.x) acc += double(rc[i]) * double(rc[i]);
+  const double t = block_sum(acc, sh);
+  __shared__ float s;
+  if (threadIdx.x == 0) { s = float(sqrt(t)); *s_out = s; }
+  __syncthreads();
+  const float inv = s > 0.f ? 1.f / s : 0.f;
+  for (int i = threadIdx.x; i < n_agg; i += blockDim.x) {
+    x_in[i] = rc[i] * inv;
+    x_in[n_agg + i] = feat[i];
+  }
+}
+
+// z[p_base + c] += out_scale * s * y[cell_agg[c]]
+__global__ void coarse_prolong(int64_t n_cells, const int32_t* __restrict__ cell_agg, int64_t p_base,
+                               const float* __restrict__ y, const float* __restrict__ s, float out_scale,
+                               float* __restrict__ z) {
+  const float f = out_scale * (*s);
+  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < n_cells; c += int64_t(gridDim.x) * blockDim.x)
+    z[p_base + c] += f * y[cell_agg[c]];
+}
+
+__global__ void snapshot_kernel(int64_t n, const double* __restrict__ x, const float* __restrict__ d,
+                                float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = float(x[i] + double(d[i]));
 }
 
 __global__ void cast_f64_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
@@ -361,8 +524,14 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     if (!pc->diag_inv) return NFEM_ERR_INVALID_ARG;
     jacobi_setup<<<grid_for(A64->n_rows, 256), 256, 0, s>>>(A64->n_rows, A64->row_ptr, A64->col_idx,
                                                              (const double*)A64->values, pc->diag_inv, dev_status);
-  } else if (pc->kind == NFEM_PC_CELL_BLOCK) {
+  } else if (pc->kind == NFEM_PC_CELL_BLOCK || pc->kind == NFEM_PC_LEARNED) {
     if (!pc->cell_dofs || !pc->block_inv) return NFEM_ERR_INVALID_ARG;
+    if (pc->kind == NFEM_PC_LEARNED) {
+      const nfem_learned_coarse* L = pc->learned;
+      if (!L || L->n_agg < 1 || !L->agg_ptr || !L->agg_cells || !L->cell_agg || !L->agg_feat || !L->params_bf16 ||
+          !L->params_f32 || !L->work || L->mlp_dims[0] != 2 * L->n_agg || L->mlp_dims[3] != L->n_agg)
+        return NFEM_ERR_INVALID_ARG;
+    }
     const int g = grid_for(pc->n_cells, 128);
     switch (pc->n_loc) {
       case 4: block_extract_invert<4><<<g, 128, 0, s>>>(pc->n_cells, pc->cell_dofs, A64->row_ptr, A64->col_idx,
@@ -375,6 +544,24 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     return NFEM_ERR_UNSUPPORTED;
   }
   NFEM_CHECK_LAUNCH();
+  if (pc->wsqrt) {
+    if (!pc->winvsqrt || !pc->setup_scratch) return NFEM_ERR_INVALID_ARG;
+    const int64_t n = A64->n_rows;
+    double* s2 = pc->setup_scratch;
+    double* c2 = pc->setup_scratch + n;
+    const int g = grid_for(n, 256);
+    weights_rows<<<g, 256, 0, s>>>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, s2);
+    bool have_c = false;
+    if (pc->kind == NFEM_PC_CELL_BLOCK || pc->kind == NFEM_PC_LEARNED) {
+      have_c = true;
+      if (pc->n_loc == 5)
+        weights_blockcols<5><<<g, 256, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, c2);
+      else
+        weights_blockcols<4><<<g, 256, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, c2);
+    }
+    weights_final<<<g, 256, 0, s>>>(n, s2, have_c ? c2 : nullptr, pc->wsqrt, pc->winvsqrt);
+    NFEM_CHECK_LAUNCH();
+  }
   return NFEM_OK;
 }
 
@@ -387,6 +574,7 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
     case NFEM_PC_JACOBI:
       jacobi_apply<<<grid_for(n, B), B, 0, s>>>(n, pc->diag_inv, v, z);
       break;
+    case NFEM_PC_LEARNED:
     case NFEM_PC_CELL_BLOCK:
       if (pc->n_loc == 5)
         block_apply<5><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z);
@@ -399,6 +587,26 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
       return NFEM_ERR_UNSUPPORTED;
   }
   NFEM_CHECK_LAUNCH();
+  if (pc->kind == NFEM_PC_LEARNED) {
+    const nfem_learned_coarse* L = pc->learned;
+    if (!L) return NFEM_ERR_INVALID_ARG;
+    const int na = L->n_agg;
+    float* x_in = L->work;
+    float* h1 = x_in + 2 * na;
+    float* h2 = h1 + L->mlp_dims[1];
+    float* y = h2 + L->mlp_dims[2];
+    float* rc = y + na;
+    float* sc = rc + na;
+    coarse_restrict<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->agg_ptr, L->agg_cells, L->p_base,
+                                                                              v, rc);
+    coarse_input<<<1, 1024, 0, s>>>(na, rc, L->agg_feat, x_in, sc);
+    NFEM_CHECK_LAUNCH();
+    int rc2 = nfem_mlp_forward(L->mlp_dims, NFEM_BF16, L->params_bf16, L->params_f32, 1, x_in, h1, h2, y, s);
+    if (rc2) return rc2;
+    coarse_prolong<<<grid_for(pc->n_cells, 256), 256, 0, s>>>(pc->n_cells, L->cell_agg, L->p_base, y, sc,
+                                                               L->out_scale, z);
+    NFEM_CHECK_LAUNCH();
+  }
   return NFEM_OK;
 }
 
@@ -410,7 +618,7 @@ extern "C" int nfem_precond_apply(const nfem_precond* pc, int64_t n, const float
 
 // workspace layout of the solver
 struct SolveWs {
-  float *V, *Z, *w, *r32, *d32;
+  float *V, *Z, *w, *t32, *r32, *d32;
   double *r64, *partial, *H, *cs, *sn, *g, *hist, *y, *scal;
   int32_t* status;
 };
@@ -421,6 +629,7 @@ static size_t solve_ws_bytes(int64_t n, int m, SolveWs* out, void* base) {
   w.V = c.take<float>(size_t(m + 1) * n);
   w.Z = c.take<float>(size_t(m) * n);
   w.w = c.take<float>(n);
+  w.t32 = c.take<float>(n);
   w.r32 = c.take<float>(n);
   w.d32 = c.take<float>(n);
   w.r64 = c.take<double>(n);
@@ -462,12 +671,14 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
   cudaStream_t s = (cudaStream_t)stream;
   SolveWs w;
   solve_ws_bytes(n, m, &w, workspace);
+  const bool weighted = pc->wsqrt != nullptr && pc->winvsqrt != nullptr;
   const int B = 256;
   const int gv = grid_for(n, B);
   const int ldh = m + 1;
   NFEM_TRY_CUDA(cudaMemsetAsync(w.status, 0, 4 * sizeof(int32_t), s));
   info->inner_iterations = 0;
   info->outer_iterations = 0;
+  info->n_snapshots = 0;
   info->status = NFEM_OK;
   double hb[2];
   // ||b||
@@ -486,17 +697,25 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
     // inner problem A32 d = r32, d0 = 0
     cast_f64_f32<<<gv, B, 0, s>>>(n, w.r64, w.r32);
     fill_f32<<<gv, B, 0, s>>>(n, w.d32, 0.f);
-    NFEM_TRY_CUDA(cudaMemcpyAsync(w.V, w.r32, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    double inner0 = rel * nb;
-    double inner_target = fmax(prm->inner_rtol * inner0, 0.5 * prm->rtol * nb);
-    double inner_res = inner0;
-    bool inner_done = false;
+    if (weighted)
+      scale_vec<<<gv, B, 0, s>>>(n, pc->wsqrt, w.r32, w.V);
+    else
+      NFEM_TRY_CUDA(cudaMemcpyAsync(w.V, w.r32, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    // the inner solve reduces the W-weighted residual norm by inner_rtol;
+    // the outer loop measures the true FP64 residual
+    NFEM_RC(multidot<float>(n, 1, w.V, n, w.V, w.partial, w.scal + 3, 1, s));
+    double wr0 = 0.0;
+    NFEM_TRY_CUDA(cudaMemcpyAsync(&wr0, w.scal + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
+    NFEM_TRY_CUDA(cudaStreamSynchronize(s));
+    const double inner_target = prm->inner_rtol * wr0;
+    double inner_res = wr0;
+    bool inner_done = wr0 == 0.0;
     bool first_cycle = true;
     while (!inner_done && info->inner_iterations < prm->max_inner) {
-      // V0 = current inner residual (r32 - A32 d32 after the first cycle)
+      // V0 = W^1/2 (r32 - A32 d32) after the first cycle
       if (!first_cycle) {
         NFEM_RC(spmv<float, float, float>(n, A32->row_ptr, A32->col_idx, (const float*)A32->values, w.d32, w.V,
-                                          w.r32, 1, s));
+                                          w.r32, 1, s, weighted ? pc->wsqrt : nullptr));
       }
       first_cycle = false;
       NFEM_RC(multidot<float>(n, 1, w.V, n, w.V, w.partial, w.scal + 2, 1, s));
@@ -507,9 +726,14 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       for (; j < m; ++j) {
         float* vj = w.V + int64_t(j) * n;
         float* zj = w.Z + int64_t(j) * n;
-        NFEM_RC(precond_apply(pc, n, vj, zj, s));
+        if (weighted) {
+          scale_vec<<<gv, B, 0, s>>>(n, pc->winvsqrt, vj, w.t32);
+          NFEM_RC(precond_apply(pc, n, w.t32, zj, s));
+        } else {
+          NFEM_RC(precond_apply(pc, n, vj, zj, s));
+        }
         NFEM_RC(spmv<float, float, float>(n, A32->row_ptr, A32->col_idx, (const float*)A32->values, zj, w.w,
-                                          nullptr, 0, s));
+                                          nullptr, 0, s, weighted ? pc->wsqrt : nullptr));
         double* hcol = w.H + int64_t(j) * ldh;
         // classical Gram-Schmidt, twice
         NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, hcol, 0, s));
@@ -535,6 +759,10 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       // d += Z y   (multi_axpy subtracts: pass -1 via hsign)
       multi_axpy<float><<<gv, B, 0, s>>>(n, k, w.Z, n, w.y, w.d32, -1.0);
       NFEM_CHECK_LAUNCH();
+      if (prm->snapshots && info->n_snapshots < prm->max_snapshots) {
+        snapshot_kernel<<<gv, B, 0, s>>>(n, x, w.d32, prm->snapshots + int64_t(info->n_snapshots) * n);
+        info->n_snapshots++;
+      }
       if (!std::isfinite(inner_res)) {
         info->status = NFEM_ERR_NONFINITE;
         return NFEM_ERR_NONFINITE;

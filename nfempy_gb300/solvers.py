@@ -26,6 +26,7 @@ class SolveResult:
         self.initial_relres = info.initial_relres
         self.final_relres = info.final_relres
         self.status = info.status
+        self.n_snapshots = info.n_snapshots
         self.seconds = seconds
 
     def as_dict(self):
@@ -40,13 +41,15 @@ def _csr(A, values=None):
 
 
 class KrylovSolver:
-    def __init__(self, A, pc="cell_block", A32_values=None, restart=30):
+    def __init__(self, A, pc="cell_block", A32_values=None, restart=30, weighted=True, learned=None):
         if A.dtype != torch.float64:
             raise ValueError("A must be the FP64 matrix (the residual is measured in FP64)")
         self.A = A
         self.restart = int(restart)
         self.values32 = A32_values
         self.pc_kind = pc
+        self.weighted = weighted
+        self.learned = learned
         self._setup_done = False
         self.status = torch.zeros(1, dtype=torch.int32, device=A.values.device)
 
@@ -64,20 +67,33 @@ class KrylovSolver:
         st = _lib.stream_ptr(stream)
         sp = A.space
         if self.pc_kind == "none":
-            self.pc = _lib.Precond(_lib.PC_NONE, 0, 0, None, None, None, None, None)
+            self.pc = _lib.Precond(_lib.PC_NONE, 0, 0, None, None, None, None, None, None, None, None)
         elif self.pc_kind == "jacobi":
             self.diag_inv = torch.empty(A.n_rows, dtype=torch.float32, device=dev)
-            self.pc = _lib.Precond(_lib.PC_JACOBI, 0, 0, None, None, None, None, _lib.ptr(self.diag_inv).value)
-        elif self.pc_kind == "cell_block":
+            self.pc = _lib.Precond(_lib.PC_JACOBI, 0, 0, None, None, None, None, _lib.ptr(self.diag_inv).value,
+                                   None, None, None)
+        elif self.pc_kind in ("cell_block", "learned"):
             n_loc = sp.n_loc
             if n_loc not in (4, 5):
                 raise NotImplementedError("cell_block preconditioner for 4 or 5 local DoFs")
             self.block_inv = torch.empty((sp.n_cells, n_loc, n_loc), dtype=torch.float32, device=dev)
-            self.pc = _lib.Precond(_lib.PC_CELL_BLOCK, n_loc, sp.n_cells, _lib.ptr(sp.cell_dofs).value,
+            kind = _lib.PC_CELL_BLOCK if self.pc_kind == "cell_block" else _lib.PC_LEARNED
+            self.pc = _lib.Precond(kind, n_loc, sp.n_cells, _lib.ptr(sp.cell_dofs).value,
                                    _lib.ptr(A.inc_ptr).value, _lib.ptr(A.inc).value,
-                                   _lib.ptr(self.block_inv).value, None)
+                                   _lib.ptr(self.block_inv).value, None, None, None, None)
+            if self.pc_kind == "learned":
+                if self.learned is None:
+                    raise ValueError("pc='learned' needs learned=LearnedPreconditioner(...)")
+                self.pc.learned = _lib.C.pointer(self.learned.struct)
         else:
             raise ValueError(f"unknown preconditioner {self.pc_kind}")
+        if self.weighted:
+            self.wsqrt = torch.empty(A.n_rows, dtype=torch.float32, device=dev)
+            self.winvsqrt = torch.empty(A.n_rows, dtype=torch.float32, device=dev)
+            scratch = torch.empty(2 * A.n_rows, dtype=torch.float64, device=dev)
+            self.pc.wsqrt = _lib.ptr(self.wsqrt).value
+            self.pc.winvsqrt = _lib.ptr(self.winvsqrt).value
+            self.pc.setup_scratch = _lib.ptr(scratch).value
         a64 = _csr(A)
         _lib.call("nfem_precond_setup", _lib.C.byref(self.pc), _lib.C.byref(a64), _lib.ptr(self.status), st)
         ws_b = _lib.C.c_size_t(0)
@@ -90,14 +106,20 @@ class KrylovSolver:
             raise _lib.NfemError(s, "preconditioner setup")
 
     def solve(self, b, x=None, rtol=1e-8, inner_rtol=1e-4, max_inner=100000, max_outer=20, stream=None,
-              raise_on_failure=True):
-        """Solve A x = b (FP64 device tensors) to ||b - A x|| / ||b|| <= rtol."""
+              raise_on_failure=True, snapshots=None):
+        """Solve A x = b (FP64 device tensors) to ||b - A x|| / ||b|| <= rtol.
+
+        snapshots: optional FP32 tensor [S, n] that receives the iterate after
+        each restart cycle (res.n_snapshots of them)."""
         if not self._setup_done:
             self.setup(stream)
         A = self.A
         if x is None:
             x = torch.zeros(A.n_rows, dtype=torch.float64, device=b.device)
         prm = _lib.SolveParams(float(rtol), float(inner_rtol), self.restart, int(max_inner), int(max_outer))
+        if snapshots is not None:
+            prm.snapshots = _lib.ptr(snapshots).value
+            prm.max_snapshots = int(snapshots.shape[0])
         info = _lib.SolveInfo()
         a64 = _csr(A)
         a32 = _csr(A, self.values32)
