@@ -211,31 +211,37 @@ typedef enum {
   NFEM_PC_CELL_BLOCK = 2,  /* cell-patch block Jacobi (weighted additive Schwarz over
                               the element cliques): cell_dofs [n_cells, n_loc],
                               block_inv [n_cells, n_loc, n_loc], row incidences */
-  NFEM_PC_LEARNED = 3      /* NFEM_PC_CELL_BLOCK plus a learned coarse correction of
-                              the pressure (P0) DoFs: the network maps the
-                              aggregate sums of the pressure residual (normalised)
-                              and one feature per aggregate to an aggregate
-                              pressure correction (see nfem_learned_coarse) */
+  NFEM_PC_TWO_LEVEL = 3    /* NFEM_PC_CELL_BLOCK smoother followed by a Galerkin coarse
+                              correction (see nfem_two_level) */
 } nfem_pc_kind;
 
-/* Learned coarse correction: M(v) = B(v) + P (s * f([R v / s, feat])) with B
- * the cell-block Jacobi, R the sum of v's pressure entries over each
- * aggregate of cells, s = ||R v||_2, f the MLP with dims {2 n_agg, h1, h2,
- * n_agg}, P the injection of an aggregate value into the pressure DoFs of its
- * cells scaled by out_scale.  work holds 2 n_agg + h1 + h2 + n_agg + 64 floats. */
+/* Two-level preconditioner: z = B v, then z += P Ac^-1 P^T (v - A z), with B
+ * the cell-block Jacobi, P the prolongation from n_agg aggregates of cells
+ * (pressure DoF of a cell -> its aggregate with weight 1; flux row f -> the
+ * aggregates of the pressure columns of row f with weight -w_f * sum of the
+ * row's entries in that aggregate's columns, so rows of faces interior to an
+ * aggregate vanish) and Ac = P^T A P formed exactly (Galerkin) and inverted
+ * densely.  w [n_rows] are the flux-extension weights: 1/|a_ff| is the
+ * classical choice; the learned preconditioner predicts them with the network.
+ * All arrays are caller-owned; the coarse correction also needs the FP32
+ * matrix (a32 in nfem_precond). */
 typedef struct {
   int64_t p_base;            /* pressure DoF of cell c is p_base + c */
   int32_t n_agg;
-  int32_t mlp_dims[4];
-  const int32_t* agg_ptr;    /* [n_agg + 1] cells of each aggregate (CSR) */
-  const int32_t* agg_cells;  /* [n_cells] */
-  const int32_t* cell_agg;   /* [n_cells] */
-  const float* agg_feat;     /* [n_agg] */
-  const void* params_bf16;   /* network weights (BF16) */
-  const float* params_f32;   /* FP32 master copy (biases read from here) */
-  float* work;
-  float out_scale;
-} nfem_learned_coarse;
+  const int32_t* cell_agg;   /* [n_cells] aggregate of each cell */
+  const float* w;            /* [n_rows] flux-extension weights */
+  const int32_t* p_agg;      /* [n_rows, 2] aggregates of each row's P entries, -1 = none */
+  float* p_val;              /* [n_rows, 2] filled by nfem_precond_setup */
+  int64_t pt_nnz;
+  const int32_t* pt_ptr;     /* [n_agg + 1] CSR of P^T, rows ascending in each list */
+  const int32_t* pt_row;     /* [pt_nnz] */
+  const int32_t* pt_slot;    /* [pt_nnz] index 2 * row + slot into p_val */
+  float* pt_val;             /* [pt_nnz] filled by nfem_precond_setup */
+  double* ac;                /* [n_agg, n_agg] Galerkin coarse matrix */
+  double* gj;                /* [n_agg, 2 n_agg] Gauss-Jordan scratch */
+  float* ac_inv;             /* [n_agg, n_agg] */
+  float* work;               /* [64 + n_rows + 2 n_agg] */
+} nfem_two_level;
 
 typedef struct {
   int kind;
@@ -255,7 +261,8 @@ typedef struct {
   float* wsqrt;
   float* winvsqrt;
   double* setup_scratch;
-  const nfem_learned_coarse* learned; /* NFEM_PC_LEARNED only (host pointer) */
+  const nfem_two_level* two_level; /* NFEM_PC_TWO_LEVEL only (host pointer) */
+  const nfem_csr* a32;             /* FP32 matrix, NFEM_PC_TWO_LEVEL only (host pointer) */
 } nfem_precond;
 
 typedef struct {

@@ -42,18 +42,18 @@ class Csr(C.Structure):
                 ("value_type", C.c_int)]
 
 
-class LearnedCoarse(C.Structure):
-    _fields_ = [("p_base", C.c_int64), ("n_agg", C.c_int32), ("mlp_dims", C.c_int32 * 4), ("agg_ptr", C.c_void_p),
-                ("agg_cells", C.c_void_p), ("cell_agg", C.c_void_p), ("agg_feat", C.c_void_p),
-                ("params_bf16", C.c_void_p), ("params_f32", C.c_void_p), ("work", C.c_void_p),
-                ("out_scale", C.c_float)]
+class TwoLevel(C.Structure):
+    _fields_ = [("p_base", C.c_int64), ("n_agg", C.c_int32), ("cell_agg", C.c_void_p), ("w", C.c_void_p),
+                ("p_agg", C.c_void_p), ("p_val", C.c_void_p), ("pt_nnz", C.c_int64), ("pt_ptr", C.c_void_p),
+                ("pt_row", C.c_void_p), ("pt_slot", C.c_void_p), ("pt_val", C.c_void_p), ("ac", C.c_void_p),
+                ("gj", C.c_void_p), ("ac_inv", C.c_void_p), ("work", C.c_void_p)]
 
 
 class Precond(C.Structure):
     _fields_ = [("kind", C.c_int), ("n_loc", C.c_int), ("n_cells", C.c_int64), ("cell_dofs", C.c_void_p),
                 ("inc_ptr", C.c_void_p), ("inc", C.c_void_p), ("block_inv", C.c_void_p), ("diag_inv", C.c_void_p),
                 ("wsqrt", C.c_void_p), ("winvsqrt", C.c_void_p), ("setup_scratch", C.c_void_p),
-                ("learned", C.POINTER(LearnedCoarse))]
+                ("two_level", C.POINTER(TwoLevel)), ("a32", C.POINTER(Csr))]
 
 
 class SolveParams(C.Structure):
@@ -66,7 +66,7 @@ class SolveInfo(C.Structure):
                 ("final_relres", C.c_double), ("status", C.c_int), ("n_snapshots", C.c_int)]
 
 
-PC_NONE, PC_JACOBI, PC_CELL_BLOCK, PC_LEARNED = 0, 1, 2, 3
+PC_NONE, PC_JACOBI, PC_CELL_BLOCK, PC_TWO_LEVEL = 0, 1, 2, 3
 
 _P = C.c_void_p
 _I = C.c_int

@@ -89,6 +89,16 @@ class CSRMatrix:
                   _lib.ptr(x), _lib.ptr(y), _lib.stream_ptr(stream))
         return y
 
+    def diagonal(self):
+        """Diagonal of the matrix (device tensor, zeros where the pattern has none)."""
+        rp = self.row_ptr.long()
+        rows = torch.repeat_interleave(torch.arange(self.n_rows, device=rp.device), rp[1:] - rp[:-1])
+        cols = self.col_idx[: self.nnz].long()
+        d = torch.zeros(self.n_rows, dtype=self.dtype, device=rp.device)
+        on = rows == cols
+        d[rows[on]] = self.values[: self.nnz][on]
+        return d
+
     def check_status(self, where=""):
         s = int(self.status.item())
         if s:

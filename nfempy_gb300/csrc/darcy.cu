@@ -247,6 +247,39 @@ __device__ __forceinline__ void element_row(const DarcyParams& p, const Incidenc
   }
 }
 
+struct RowHead {
+  int2 pr;
+  uint2 cd;
+};
+
+__device__ __forceinline__ RowHead load_head(const DarcyParams& p, int64_t r) {
+  RowHead h;
+  if (r < p.n_rows) {
+    h.pr = __ldg(reinterpret_cast<const int2*>(p.pairs) + r);
+    h.cd = __ldg(reinterpret_cast<const uint2*>(p.pair_codes) + r);
+  } else {
+    h.pr = make_int2(-1, -1);
+    h.cd = make_uint2(0u, 0u);
+  }
+  return h;
+}
+
+// Row length from the slot codes: 1 + the largest position any incidence
+// writes (the positions of a row's columns are 0..len-1 and every column is
+// written by some incidence).
+template <int NLOC>
+__device__ __forceinline__ int row_len_from_codes(const RowHead& h) {
+  int len = 0;
+  const int occ[2] = {h.pr.x, h.pr.y};
+  const uint32_t code[2] = {h.cd.x, h.cd.y};
+#pragma unroll
+  for (int t = 0; t < 2; ++t)
+    if (occ[t] >= 0)
+#pragma unroll
+      for (int b = 0; b < NLOC; ++b) len = max(len, int((code[t] >> (4 * b)) & 15u) + 1);
+  return len;
+}
+
 template <typename T, int DIM, int SRC>
 __global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const DarcyParams p) {
   constexpr int NLOC = DIM + 2;
@@ -255,18 +288,22 @@ __global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const Darc
   T* st = stage[warp];
   T* values = static_cast<T*>(p.values);
   T* rhs = static_cast<T*>(p.rhs);
+  const int64_t stride = int64_t(gridDim.x) * kDarcyWarps * 32;
 
-  for (int64_t r0 = (int64_t(blockIdx.x) * kDarcyWarps + warp) * 32; r0 < p.n_rows;
-       r0 += int64_t(gridDim.x) * kDarcyWarps * 32) {
+  int64_t r0 = (int64_t(blockIdx.x) * kDarcyWarps + warp) * 32;
+  RowHead head = load_head(p, r0 + lane);
+  int32_t base_next = r0 < p.n_rows ? __ldg(p.row_ptr + r0) : 0;
+  for (; r0 < p.n_rows; r0 += stride) {
     const int64_t r = r0 + lane;
     const bool valid = r < p.n_rows;
-    // independent loads of the row: extent, incidence pair, slot codes
-    const int32_t rb = valid ? __ldg(p.row_ptr + r) : 0;
-    const int32_t re = valid ? __ldg(p.row_ptr + r + 1) : 0;
-    const int2 pr = valid ? __ldg(reinterpret_cast<const int2*>(p.pairs) + r) : make_int2(-1, -1);
-    const uint2 cd = valid ? __ldg(reinterpret_cast<const uint2*>(p.pair_codes) + r) : make_uint2(0u, 0u);
-    const int occ[2] = {pr.x, pr.y};
-    const uint32_t code[2] = {cd.x, cd.y};
+    const RowHead h = head;
+    const int32_t base = base_next;
+    // prefetch the next chunk of this warp (overlaps its latency with this one)
+    head = load_head(p, r0 + stride + lane);
+    base_next = (r0 + stride < p.n_rows) ? __ldg(p.row_ptr + r0 + stride) : 0;
+
+    const int occ[2] = {h.pr.x, h.pr.y};
+    const uint32_t code[2] = {h.cd.x, h.cd.y};
     int32_t c[2];
     int a[2];
     bool on[2], geo[2];
@@ -281,10 +318,16 @@ __global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const Darc
 #pragma unroll
     for (int t = 0; t < 2; ++t) load_incidence<T, DIM, SRC>(p, c[t], geo[t], inc[t]);
 
-    const int last = int(min(int64_t(31), p.n_rows - 1 - r0));
-    const int32_t base = __shfl_sync(0xffffffffu, rb, 0);
-    const int32_t end = __shfl_sync(0xffffffffu, re, last);
-    const int span = end - base;
+    // row offsets inside the chunk: exclusive warp scan of the row lengths
+    const int len = valid ? row_len_from_codes<NLOC>(h) : 0;
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int off = incl - len;
+    const int span = __shfl_sync(0xffffffffu, incl, 31);
     if (span > 32 * kDarcyMaxRow) {  // cannot happen for codes built with rows <= 16
       if (lane == 0) set_status(p.status, NFEM_ERR_PATTERN);
       continue;
@@ -292,7 +335,6 @@ __global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const Darc
     for (int i = lane; i < span; i += 32) st[i] = T(0);
     __syncwarp();
     T rhs_val = T(0);
-    const int off = rb - base;
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
       if (on[t]) {

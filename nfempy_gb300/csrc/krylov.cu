@@ -30,6 +30,12 @@
 
 #include "nfem_common.cuh"
 
+#define NFEM_RC(...)                \
+  do {                              \
+    int _rc = (__VA_ARGS__);        \
+    if (_rc != NFEM_OK) return _rc; \
+  } while (0)
+
 extern "C" int nfem_mlp_forward(const int32_t* dims, int weight_type, const void* params, const float* params_f32,
                                 int64_t batch, const float* x, float* h1, float* h2, float* y, void* stream);
 
@@ -288,43 +294,181 @@ __global__ void weights_final(int64_t n, const double* __restrict__ s2, const do
   }
 }
 
-// ---- learned coarse correction
-// rc[a] = sum over the cells of aggregate a of v[p_base + c] (cell order)
-__global__ void coarse_restrict(int n_agg, const int32_t* __restrict__ agg_ptr, const int32_t* __restrict__ agg_cells,
-                                int64_t p_base, const float* __restrict__ v, float* __restrict__ rc) {
+// ---- two-level (Galerkin) coarse correction
+// p_val[2i + s]: pressure rows -> 1 for their aggregate; flux rows -> -w_i *
+// (sum of row i's entries in the pressure columns of aggregate p_agg[2i + s]).
+__global__ void twolevel_fill_p(int64_t n_rows, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                const double* __restrict__ v, int64_t p_base, int64_t n_cells,
+                                const int32_t* __restrict__ cell_agg, const float* __restrict__ w,
+                                const int32_t* __restrict__ p_agg, float* __restrict__ p_val) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows; i += int64_t(gridDim.x) * blockDim.x) {
+    const bool prow = i >= p_base && i < p_base + n_cells;
+#pragma unroll
+    for (int sl = 0; sl < 2; ++sl) {
+      const int32_t a = p_agg[2 * i + sl];
+      float val = 0.f;
+      if (a >= 0) {
+        if (prow) {
+          val = 1.f;
+        } else {
+          double acc = 0.0;
+          for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+            const int64_t j = ci[k];
+            if (j >= p_base && j < p_base + n_cells && cell_agg[j - p_base] == a) acc += v[k];
+          }
+          val = float(-double(w[i]) * acc);
+        }
+      }
+      p_val[2 * i + sl] = val;
+    }
+  }
+}
+
+// ac[alpha, beta] += P[i, alpha] A[i, j] P[j, beta] over the nonzeros of A
+__global__ void twolevel_galerkin(int64_t n_rows, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                  const double* __restrict__ v, const int32_t* __restrict__ p_agg,
+                                  const float* __restrict__ p_val, int n_agg, double* __restrict__ ac) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows; i += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t ai0 = p_agg[2 * i], ai1 = p_agg[2 * i + 1];
+    const double pi0 = p_val[2 * i], pi1 = p_val[2 * i + 1];
+    if ((ai0 < 0 || pi0 == 0.0) && (ai1 < 0 || pi1 == 0.0)) continue;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+      const int64_t j = ci[k];
+      const double aij = v[k];
+#pragma unroll
+      for (int sj = 0; sj < 2; ++sj) {
+        const int32_t bj = p_agg[2 * j + sj];
+        const double pj = p_val[2 * j + sj];
+        if (bj < 0 || pj == 0.0) continue;
+        if (ai0 >= 0 && pi0 != 0.0) atomicAdd(ac + int64_t(ai0) * n_agg + bj, pi0 * aij * pj);
+        if (ai1 >= 0 && pi1 != 0.0) atomicAdd(ac + int64_t(ai1) * n_agg + bj, pi1 * aij * pj);
+      }
+    }
+  }
+}
+
+// Gauss-Jordan inversion of the dense [n, 2n] array [Ac | I] (FP64, row-major)
+__global__ void gj_pivot(double* __restrict__ m, int n, int k, int32_t* __restrict__ piv, int32_t* status) {
+  __shared__ double best[1024];
+  __shared__ int besti[1024];
+  double b = -1.0;
+  int bi = k;
+  for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+    const double x = fabs(m[int64_t(i) * 2 * n + k]);
+    if (x > b) { b = x; bi = i; }
+  }
+  best[threadIdx.x] = b;
+  besti[threadIdx.x] = bi;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      const double y = best[threadIdx.x + o];
+      const int yi = besti[threadIdx.x + o];
+      if (y > best[threadIdx.x] || (y == best[threadIdx.x] && yi < besti[threadIdx.x])) {
+        best[threadIdx.x] = y;
+        besti[threadIdx.x] = yi;
+      }
+    }
+    __syncthreads();
+  }
+  const int p = besti[0];
+  if (threadIdx.x == 0) {
+    *piv = p;
+    if (!(best[0] > 0.0)) set_status(status, NFEM_ERR_BREAKDOWN);
+  }
+  // swap rows k and p, then scale row k
+  if (p != k)
+    for (int j = threadIdx.x; j < 2 * n; j += blockDim.x) {
+      const double t = m[int64_t(k) * 2 * n + j];
+      m[int64_t(k) * 2 * n + j] = m[int64_t(p) * 2 * n + j];
+      m[int64_t(p) * 2 * n + j] = t;
+    }
+  __syncthreads();
+  const double d = m[int64_t(k) * 2 * n + k];
+  const double inv = d != 0.0 ? 1.0 / d : 0.0;
+  __syncthreads();
+  for (int j = threadIdx.x; j < 2 * n; j += blockDim.x) m[int64_t(k) * 2 * n + j] *= inv;
+}
+
+// rows i != k: m[i, j] -= m[i, k] m[k, j] for j > k (columns < k of the left
+// half are already unit vectors); column k is cleared afterwards
+__global__ void gj_eliminate(double* __restrict__ m, int n, int k) {
+  const int w = 2 * n - k - 1;
+  const int64_t total = int64_t(n) * w;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+    const int i = int(e / w);
+    const int j = k + 1 + int(e - int64_t(i) * w);
+    if (i == k) continue;
+    const double f = m[int64_t(i) * 2 * n + k];
+    if (f != 0.0) m[int64_t(i) * 2 * n + j] -= f * m[int64_t(k) * 2 * n + j];
+  }
+}
+
+__global__ void gj_clear_col(double* __restrict__ m, int n, int k) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (i != k) m[int64_t(i) * 2 * n + k] = 0.0;
+}
+
+__global__ void gj_extract(const double* __restrict__ m, int n, float* __restrict__ inv) {
+  const int64_t total = int64_t(n) * n;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+    const int i = int(e / n), j = int(e - int64_t(i) * n);
+    inv[e] = float(m[int64_t(i) * 2 * n + n + j]);
+  }
+}
+
+__global__ void gj_init(const double* __restrict__ ac, int n, double* __restrict__ m) {
+  const int64_t total = int64_t(n) * 2 * n;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+    const int i = int(e / (2 * n)), j = int(e - int64_t(i) * 2 * n);
+    m[e] = j < n ? ac[int64_t(i) * n + j] : (j - n == i ? 1.0 : 0.0);
+  }
+}
+
+// rc[alpha] = sum over P^T's list of alpha (rows in ascending order) of p_val * r
+__global__ void twolevel_restrict(int n_agg, const int32_t* __restrict__ pt_ptr, const int32_t* __restrict__ pt_row,
+                                  const float* __restrict__ pt_val, const float* __restrict__ r,
+                                  float* __restrict__ rc) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= n_agg) return;
   float acc = 0.f;
-  for (int32_t k = agg_ptr[warp] + lane; k < agg_ptr[warp + 1]; k += 32) acc += v[p_base + agg_cells[k]];
+  for (int32_t k = pt_ptr[warp] + lane; k < pt_ptr[warp + 1]; k += 32) acc = fmaf(pt_val[k], r[pt_row[k]], acc);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if (lane == 0) rc[warp] = acc;
 }
 
-// x_in = [rc / s, feat], s = ||rc|| stored in *s_out (single block)
-__global__ void coarse_input(int n_agg, const float* __restrict__ rc, const float* __restrict__ feat,
-                             float* __restrict__ x_in, float* __restrict__ s_out) {
-  __shared__ double sh[32];
-  double acc = 0.0;
-  for (int i = threadIdx.x; i < n_agg; i += blockDim.x) acc += double(rc[i]) * double(rc[i]);
-  const double t = block_sum(acc, sh);
-  __shared__ float s;
-  if (threadIdx.x == 0) { s = float(sqrt(t)); *s_out = s; }
-  __syncthreads();
-  const float inv = s > 0.f ? 1.f / s : 0.f;
-  for (int i = threadIdx.x; i < n_agg; i += blockDim.x) {
-    x_in[i] = rc[i] * inv;
-    x_in[n_agg + i] = feat[i];
+// ec = Ainv rc  (one warp per row)
+__global__ void dense_gemv(int n, const float* __restrict__ Ainv, const float* __restrict__ x, float* __restrict__ y) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const float* row = Ainv + int64_t(warp) * n;
+  float acc = 0.f;
+  for (int j = lane; j < n; j += 32) acc = fmaf(row[j], x[j], acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) y[warp] = acc;
+}
+
+// z[i] += sum_s p_val[2i + s] ec[p_agg[2i + s]]
+__global__ void twolevel_prolong(int64_t n_rows, const int32_t* __restrict__ p_agg, const float* __restrict__ p_val,
+                                 const float* __restrict__ ec, float* __restrict__ z) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows; i += int64_t(gridDim.x) * blockDim.x) {
+    float acc = 0.f;
+#pragma unroll
+    for (int sl = 0; sl < 2; ++sl) {
+      const int32_t a = p_agg[2 * i + sl];
+      if (a >= 0) acc = fmaf(p_val[2 * i + sl], ec[a], acc);
+    }
+    z[i] += acc;
   }
 }
 
-// z[p_base + c] += out_scale * s * y[cell_agg[c]]
-__global__ void coarse_prolong(int64_t n_cells, const int32_t* __restrict__ cell_agg, int64_t p_base,
-                               const float* __restrict__ y, const float* __restrict__ s, float out_scale,
-                               float* __restrict__ z) {
-  const float f = out_scale * (*s);
-  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < n_cells; c += int64_t(gridDim.x) * blockDim.x)
-    z[p_base + c] += f * y[cell_agg[c]];
+// pt_val[k] = p_val of the (row, slot) that P^T entry k refers to
+__global__ void twolevel_fill_pt(int64_t nnz, const int32_t* __restrict__ pt_slot, const float* __restrict__ p_val,
+                                 float* __restrict__ pt_val) {
+  for (int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < nnz; k += int64_t(gridDim.x) * blockDim.x)
+    pt_val[k] = p_val[pt_slot[k]];
 }
 
 __global__ void snapshot_kernel(int64_t n, const double* __restrict__ x, const float* __restrict__ d,
@@ -524,12 +668,12 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     if (!pc->diag_inv) return NFEM_ERR_INVALID_ARG;
     jacobi_setup<<<grid_for(A64->n_rows, 256), 256, 0, s>>>(A64->n_rows, A64->row_ptr, A64->col_idx,
                                                              (const double*)A64->values, pc->diag_inv, dev_status);
-  } else if (pc->kind == NFEM_PC_CELL_BLOCK || pc->kind == NFEM_PC_LEARNED) {
+  } else if (pc->kind == NFEM_PC_CELL_BLOCK || pc->kind == NFEM_PC_TWO_LEVEL) {
     if (!pc->cell_dofs || !pc->block_inv) return NFEM_ERR_INVALID_ARG;
-    if (pc->kind == NFEM_PC_LEARNED) {
-      const nfem_learned_coarse* L = pc->learned;
-      if (!L || L->n_agg < 1 || !L->agg_ptr || !L->agg_cells || !L->cell_agg || !L->agg_feat || !L->params_bf16 ||
-          !L->params_f32 || !L->work || L->mlp_dims[0] != 2 * L->n_agg || L->mlp_dims[3] != L->n_agg)
+    if (pc->kind == NFEM_PC_TWO_LEVEL) {
+      const nfem_two_level* L = pc->two_level;
+      if (!L || L->n_agg < 1 || !L->cell_agg || !L->w || !L->p_agg || !L->p_val || !L->pt_ptr || !L->pt_row ||
+          !L->pt_slot || !L->pt_val || !L->ac || !L->ac_inv || !L->gj || !L->work)
         return NFEM_ERR_INVALID_ARG;
     }
     const int g = grid_for(pc->n_cells, 128);
@@ -552,7 +696,7 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     const int g = grid_for(n, 256);
     weights_rows<<<g, 256, 0, s>>>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, s2);
     bool have_c = false;
-    if (pc->kind == NFEM_PC_CELL_BLOCK || pc->kind == NFEM_PC_LEARNED) {
+    if (pc->kind == NFEM_PC_CELL_BLOCK || pc->kind == NFEM_PC_TWO_LEVEL) {
       have_c = true;
       if (pc->n_loc == 5)
         weights_blockcols<5><<<g, 256, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, c2);
@@ -560,6 +704,27 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
         weights_blockcols<4><<<g, 256, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, c2);
     }
     weights_final<<<g, 256, 0, s>>>(n, s2, have_c ? c2 : nullptr, pc->wsqrt, pc->winvsqrt);
+    NFEM_CHECK_LAUNCH();
+  }
+  if (pc->kind == NFEM_PC_TWO_LEVEL) {
+    const nfem_two_level* L = pc->two_level;
+    const int64_t n = A64->n_rows;
+    const int na = L->n_agg;
+    const int g = grid_for(n, 256);
+    twolevel_fill_p<<<g, 256, 0, s>>>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, L->p_base,
+                                      pc->n_cells, L->cell_agg, L->w, L->p_agg, L->p_val);
+    twolevel_fill_pt<<<grid_for(L->pt_nnz, 256), 256, 0, s>>>(L->pt_nnz, L->pt_slot, L->p_val, L->pt_val);
+    NFEM_TRY_CUDA(cudaMemsetAsync(L->ac, 0, size_t(na) * na * sizeof(double), s));
+    twolevel_galerkin<<<g, 256, 0, s>>>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, L->p_agg,
+                                        L->p_val, na, L->ac);
+    gj_init<<<grid_for(int64_t(na) * 2 * na, 256), 256, 0, s>>>(L->ac, na, L->gj);
+    int32_t* piv = reinterpret_cast<int32_t*>(L->work);
+    for (int k = 0; k < na; ++k) {
+      gj_pivot<<<1, 1024, 0, s>>>(L->gj, na, k, piv, dev_status);
+      gj_eliminate<<<grid_for(int64_t(na) * (2 * na - k - 1), 256), 256, 0, s>>>(L->gj, na, k);
+      gj_clear_col<<<grid_for(na, 256), 256, 0, s>>>(L->gj, na, k);
+    }
+    gj_extract<<<grid_for(int64_t(na) * na, 256), 256, 0, s>>>(L->gj, na, L->ac_inv);
     NFEM_CHECK_LAUNCH();
   }
   return NFEM_OK;
@@ -574,7 +739,7 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
     case NFEM_PC_JACOBI:
       jacobi_apply<<<grid_for(n, B), B, 0, s>>>(n, pc->diag_inv, v, z);
       break;
-    case NFEM_PC_LEARNED:
+    case NFEM_PC_TWO_LEVEL:
     case NFEM_PC_CELL_BLOCK:
       if (pc->n_loc == 5)
         block_apply<5><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z);
@@ -587,24 +752,20 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
       return NFEM_ERR_UNSUPPORTED;
   }
   NFEM_CHECK_LAUNCH();
-  if (pc->kind == NFEM_PC_LEARNED) {
-    const nfem_learned_coarse* L = pc->learned;
-    if (!L) return NFEM_ERR_INVALID_ARG;
+  if (pc->kind == NFEM_PC_TWO_LEVEL) {
+    // z += P Ac^-1 P^T (v - A z)
+    const nfem_two_level* L = pc->two_level;
+    if (!L || !pc->a32) return NFEM_ERR_INVALID_ARG;
     const int na = L->n_agg;
-    float* x_in = L->work;
-    float* h1 = x_in + 2 * na;
-    float* h2 = h1 + L->mlp_dims[1];
-    float* y = h2 + L->mlp_dims[2];
-    float* rc = y + na;
-    float* sc = rc + na;
-    coarse_restrict<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->agg_ptr, L->agg_cells, L->p_base,
-                                                                              v, rc);
-    coarse_input<<<1, 1024, 0, s>>>(na, rc, L->agg_feat, x_in, sc);
-    NFEM_CHECK_LAUNCH();
-    int rc2 = nfem_mlp_forward(L->mlp_dims, NFEM_BF16, L->params_bf16, L->params_f32, 1, x_in, h1, h2, y, s);
-    if (rc2) return rc2;
-    coarse_prolong<<<grid_for(pc->n_cells, 256), 256, 0, s>>>(pc->n_cells, L->cell_agg, L->p_base, y, sc,
-                                                               L->out_scale, z);
+    float* r2 = L->work + 64;
+    float* rc = r2 + n;
+    float* ec = rc + na;
+    NFEM_RC(spmv<float, float, float>(n, pc->a32->row_ptr, pc->a32->col_idx, (const float*)pc->a32->values, z, r2, v,
+                                      1, s));
+    twolevel_restrict<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->pt_ptr, L->pt_row, L->pt_val,
+                                                                                r2, rc);
+    dense_gemv<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->ac_inv, rc, ec);
+    twolevel_prolong<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z);
     NFEM_CHECK_LAUNCH();
   }
   return NFEM_OK;
@@ -652,11 +813,6 @@ extern "C" int nfem_solve_workspace_bytes(int64_t n, int restart, size_t* bytes)
   return NFEM_OK;
 }
 
-#define NFEM_RC(...)                \
-  do {                              \
-    int _rc = (__VA_ARGS__);        \
-    if (_rc != NFEM_OK) return _rc; \
-  } while (0)
 
 extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, const nfem_precond* pc,
                                     const double* b, double* x, const nfem_solve_params* prm, void* workspace,

@@ -182,3 +182,71 @@ class LearnedPreconditioner:
             _lib.ptr(grid.agg_cells).value, _lib.ptr(grid.cell_agg).value, _lib.ptr(self.feat).value,
             _lib.ptr(model.params_bf16).value, _lib.ptr(model.params).value, _lib.ptr(self.work).value,
             float(out_scale))
+
+
+class DarcyProblem:
+    """A Darcy RT1 x P0 space on cube(n) with reusable matrices (only K changes)."""
+
+    def __init__(self, n, device="cuda"):
+        from . import meshes, workloads
+        from .assembly import CSRMatrix, LaplaceDualWeakForm
+        self.n = n
+        self.mesh = meshes.cube(n)
+        self.space = workloads.darcy_space(self.mesh, device=device)
+        cells = self.mesh["blocks"][-1][1]
+        self.centroids = self.mesh["points"][cells].mean(axis=1)
+        self.A = CSRMatrix(self.space, dtype=torch.float64)
+        self.A32 = self.A.with_dtype(torch.float32)
+        self.res = torch.empty(self.A.n_rows, dtype=torch.float64, device=device)
+        self.res32 = torch.empty(self.A.n_rows, dtype=torch.float32, device=device)
+        self.form = LaplaceDualWeakForm(self.space)
+
+    def field(self, seed, corr_len=0.05, sigma=2.0):
+        from . import meshes
+        return np.exp(meshes.grf_log_field(self.centroids, corr_len, sigma, seed))
+
+    def assemble(self, kappa, f=1.0):
+        self.form.functions = {"kappa": kappa, "rhs": f}
+        self.form.assemble(self.A, self.res)
+        self.form.assemble(self.A32, self.res32)
+        return -self.res
+
+
+def generate_pairs(problem, grid, seeds, restart=30, max_snapshots=64, max_iters=20000, log=None):
+    """Plain-solver (residual, error) pairs on the permeability fields of `seeds`."""
+    from .solvers import KrylovSolver
+    xs, ts, stats = [], [], []
+    n = problem.A.n_rows
+    snaps = torch.empty((max_snapshots, n), dtype=torch.float32, device=problem.A.values.device)
+    for i, seed in enumerate(seeds):
+        kappa = problem.field(seed)
+        b = problem.assemble(kappa)
+        ksp = KrylovSolver(problem.A, pc="cell_block", A32_values=problem.A32.values, restart=restart)
+        x, info = ksp.solve(b, rtol=1e-8, max_inner=max_iters, raise_on_failure=False, snapshots=snaps)
+        S = info.n_snapshots
+        if S == 0 or info.status != 0:
+            continue
+        feat = grid.features(kappa)
+        xi, ti = make_pairs(grid, problem.A, b, x, snaps[:S], feat)
+        xs.append(xi)
+        ts.append(ti)
+        stats.append(info.inner_iterations)
+        if log and (i % 50 == 0):
+            log(f"field {i}: seed {seed} iters {info.inner_iterations} pairs {xi.shape[0]}")
+    return torch.cat(xs), torch.cat(ts), stats
+
+
+def train(model, X, T, steps=4000, batch=256, lr=1e-3, seed=0, log=None):
+    """Adam on the pairs with the library's kernels; returns the loss history."""
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    N = X.shape[0]
+    hist = []
+    for s in range(steps):
+        idx = torch.randint(0, N, (batch,), generator=g).to(X.device)
+        cur_lr = lr * 0.5 * (1 + np.cos(np.pi * s / steps))
+        loss = model.train_step(X[idx].contiguous(), T[idx].contiguous(), lr=cur_lr)
+        if s % 200 == 0 or s == steps - 1:
+            hist.append((s, float(loss.item())))
+            if log:
+                log(f"step {s} loss {hist[-1][1]:.4e}")
+    return hist

@@ -9,7 +9,9 @@ solver keeps an FP32 copy with the same pattern for the inner FGMRES
 iterations, refreshed from A (or assembled directly in FP32 by the caller
 and passed as A32).  Preconditioners: "none", "jacobi", "cell_block"
 (cell-patch block Jacobi = weighted additive Schwarz over the element
-cliques, blocks inverted in FP64, applied in FP32).
+cliques, blocks inverted in FP64, applied in FP32), "two_level" (that
+smoother plus a Galerkin coarse correction over aggregates of cells, see
+TwoLevelCoarse).
 Reference call sites: examples/md_elliptic_scalar/md_elliptic_scalar.py:343-363,
 examples/cauchy_elasticity/cg_elasticity_example_1.py:159-170.
 """
@@ -41,7 +43,7 @@ def _csr(A, values=None):
 
 
 class KrylovSolver:
-    def __init__(self, A, pc="cell_block", A32_values=None, restart=30, weighted=True, learned=None):
+    def __init__(self, A, pc="cell_block", A32_values=None, restart=30, weighted=True, two_level=None):
         if A.dtype != torch.float64:
             raise ValueError("A must be the FP64 matrix (the residual is measured in FP64)")
         self.A = A
@@ -49,7 +51,7 @@ class KrylovSolver:
         self.values32 = A32_values
         self.pc_kind = pc
         self.weighted = weighted
-        self.learned = learned
+        self.two_level = two_level
         self._setup_done = False
         self.status = torch.zeros(1, dtype=torch.int32, device=A.values.device)
 
@@ -72,19 +74,21 @@ class KrylovSolver:
             self.diag_inv = torch.empty(A.n_rows, dtype=torch.float32, device=dev)
             self.pc = _lib.Precond(_lib.PC_JACOBI, 0, 0, None, None, None, None, _lib.ptr(self.diag_inv).value,
                                    None, None, None)
-        elif self.pc_kind in ("cell_block", "learned"):
+        elif self.pc_kind in ("cell_block", "two_level"):
             n_loc = sp.n_loc
             if n_loc not in (4, 5):
                 raise NotImplementedError("cell_block preconditioner for 4 or 5 local DoFs")
             self.block_inv = torch.empty((sp.n_cells, n_loc, n_loc), dtype=torch.float32, device=dev)
-            kind = _lib.PC_CELL_BLOCK if self.pc_kind == "cell_block" else _lib.PC_LEARNED
+            kind = _lib.PC_CELL_BLOCK if self.pc_kind == "cell_block" else _lib.PC_TWO_LEVEL
             self.pc = _lib.Precond(kind, n_loc, sp.n_cells, _lib.ptr(sp.cell_dofs).value,
                                    _lib.ptr(A.inc_ptr).value, _lib.ptr(A.inc).value,
                                    _lib.ptr(self.block_inv).value, None, None, None, None)
-            if self.pc_kind == "learned":
-                if self.learned is None:
-                    raise ValueError("pc='learned' needs learned=LearnedPreconditioner(...)")
-                self.pc.learned = _lib.C.pointer(self.learned.struct)
+            if self.pc_kind == "two_level":
+                if self.two_level is None:
+                    raise ValueError("pc='two_level' needs two_level=TwoLevelCoarse(...)")
+                self._a32 = _csr(A, self.values32)
+                self.pc.two_level = _lib.C.pointer(self.two_level.struct)
+                self.pc.a32 = _lib.C.pointer(self._a32)
         else:
             raise ValueError(f"unknown preconditioner {self.pc_kind}")
         if self.weighted:
@@ -137,3 +141,96 @@ class KrylovSolver:
         _lib.call("nfem_residual_f64", A.n_rows, _lib.ptr(A.row_ptr), _lib.ptr(A.col_idx), _lib.ptr(A.values),
                   _lib.ptr(x), _lib.ptr(b), _lib.ptr(r), _lib.stream_ptr(stream))
         return r
+
+
+class TwoLevelCoarse:
+    """Aggregates and prolongation structure of the two-level preconditioner.
+
+    Cells are binned by centroid into an n_c^d grid of aggregates.  P maps an
+    aggregate value to the pressure DoFs of its cells (weight 1) and to the
+    flux rows whose cells lie in different aggregates or on the domain
+    boundary (weight -w_f times the row's entries in that aggregate's
+    pressure columns).  w = None gives the classical weights 1/|a_ff|; the
+    learned preconditioner passes the network's prediction."""
+
+    def __init__(self, A, n_c, w=None):
+        sp = A.space
+        self.A = A
+        dim = sp.dim
+        dev = A.values.device
+        X = sp.mesh.points[sp.cells_host]
+        cent = X.mean(axis=1)[:, :dim]
+        lo, hi = cent.min(axis=0), cent.max(axis=0)
+        idx = np.clip(np.floor((cent - lo) / np.maximum(hi - lo, 1e-300) * n_c).astype(np.int64), 0, n_c - 1)
+        agg = np.zeros(sp.n_cells, dtype=np.int64)
+        for d in range(dim):
+            agg = agg * n_c + idx[:, d]
+        self.n_agg = int(n_c ** dim)
+        self.cell_agg_host = agg
+        n = A.n_rows
+        pb = sp.field_offsets["p"]
+        self.p_base = pb
+        cd = sp.all_destination_indexes()
+        nf = sp.dim + 1
+        p_agg = np.full((n, 2), -1, dtype=np.int64)
+        p_agg[pb:pb + sp.n_cells, 0] = agg
+        # flux rows: aggregates of the cells on either side of the face
+        faces = cd[:, :nf].ravel()
+        fagg = np.repeat(agg, nf)
+        order = np.lexsort((fagg, faces))
+        faces, fagg = faces[order], fagg[order]
+        first = np.ones(faces.size, dtype=bool)
+        first[1:] = faces[1:] != faces[:-1]
+        cnt = np.bincount(faces, minlength=n)
+        start = np.flatnonzero(first)
+        f0 = faces[start]
+        a0 = fagg[start]
+        two = cnt[f0] == 2
+        a1 = np.where(two, fagg[np.minimum(start + 1, faces.size - 1)], -1)
+        boundary = cnt[f0] == 1
+        differ = two & (a1 != a0)
+        keep0 = boundary | differ
+        p_agg[f0[keep0], 0] = a0[keep0]
+        p_agg[f0[differ], 1] = a1[differ]
+        self.p_agg_host = p_agg
+        rows = np.repeat(np.arange(n), 2)
+        slots = np.arange(2 * n)
+        aa = p_agg.ravel()
+        m = aa >= 0
+        key = np.lexsort((rows[m], aa[m]))
+        pt_agg = aa[m][key]
+        self.pt_row_host = rows[m][key]
+        pt_slot = slots[m][key]
+        pt_ptr = np.zeros(self.n_agg + 1, dtype=np.int64)
+        np.add.at(pt_ptr, pt_agg + 1, 1)
+        pt_ptr = np.cumsum(pt_ptr)
+        i32 = lambda a: torch.as_tensor(np.ascontiguousarray(a).astype(np.int32), device=dev)
+        self.cell_agg = i32(agg)
+        self.p_agg = i32(p_agg.ravel())
+        self.p_val = torch.zeros(2 * n, dtype=torch.float32, device=dev)
+        self.pt_ptr = i32(pt_ptr)
+        self.pt_row = i32(self.pt_row_host)
+        self.pt_slot = i32(pt_slot)
+        self.pt_val = torch.zeros(max(1, pt_slot.size), dtype=torch.float32, device=dev)
+        na = self.n_agg
+        self.ac = torch.zeros((na, na), dtype=torch.float64, device=dev)
+        self.gj = torch.zeros((na, 2 * na), dtype=torch.float64, device=dev)
+        self.ac_inv = torch.zeros((na, na), dtype=torch.float32, device=dev)
+        self.work = torch.zeros(64 + n + 2 * na, dtype=torch.float32, device=dev)
+        self.set_weights(w)
+        self.struct = _lib.TwoLevel(pb, na, _lib.ptr(self.cell_agg).value, _lib.ptr(self.w).value,
+                                    _lib.ptr(self.p_agg).value, _lib.ptr(self.p_val).value, int(pt_slot.size),
+                                    _lib.ptr(self.pt_ptr).value, _lib.ptr(self.pt_row).value,
+                                    _lib.ptr(self.pt_slot).value, _lib.ptr(self.pt_val).value,
+                                    _lib.ptr(self.ac).value, _lib.ptr(self.gj).value, _lib.ptr(self.ac_inv).value,
+                                    _lib.ptr(self.work).value)
+
+    def classical_weights(self):
+        d = self.A.diagonal().abs()
+        return torch.where(d > 0, 1.0 / d.clamp_min(1e-300), torch.zeros_like(d)).float()
+
+    def set_weights(self, w):
+        self.w = (self.classical_weights() if w is None else torch.as_tensor(w, device=self.A.values.device)
+                  .float()).contiguous()
+        if hasattr(self, "struct"):
+            self.struct.w = _lib.ptr(self.w).value
