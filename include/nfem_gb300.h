@@ -59,6 +59,20 @@ int nfem_scan_workspace_bytes(int64_t n, size_t* bytes);
 int nfem_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offsets,
                         void* workspace, size_t workspace_bytes, void* stream);
 
+/* The same scan for callers that cannot allocate device memory: code that
+ * runs while a CUDA graph is being captured (cudaMalloc is not a capturable
+ * operation), or inside a host framework that owns all device memory through
+ * its own pool allocator and forbids raw allocations.  No counterpart in the
+ * reference.  The scan's scratch (one int64 per 4096 counts) is a fixed
+ * device array inside the library, so n is limited to 67,108,864 counts
+ * (NFEM_ERR_CAPACITY above that).  The first call on a device looks up that
+ * array's device address; make that first call before any stream capture.
+ * All calls on a device share the one array: calls whose kernels overlap on
+ * the GPU (different streams, or different host threads without ordering)
+ * race and must be serialised by the caller.  Allocates nothing. */
+int nfem_exclusive_scan_noalloc(const int32_t* counts, int64_t n, int64_t* offsets,
+                                void* stream);
+
 /* --------------------------------------- K0: entity numbering (a1, a2, a8)
  * Replaces Mesh.build_conformal_mesh + insert_* (src/mesh/mesh.py:125-339),
  * the first-appearance entity order of MeshTopology

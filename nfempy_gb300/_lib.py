@@ -78,6 +78,7 @@ _SIGS = {
     "nfem_status_string": ([_I], C.c_char_p),
     "nfem_scan_workspace_bytes": ([_I64, C.POINTER(_SZ)], _I),
     "nfem_exclusive_scan": ([_P, _I64, _P, _P, _SZ, _P], _I),
+    "nfem_exclusive_scan_noalloc": ([_P, _I64, _P, _P], _I),
     "nfem_numbering_workspace_bytes": ([_I64, _I, _I, _I64, _I64, C.POINTER(_SZ)], _I),
     "nfem_number_entities": ([_P, _I64, _I, _I, _I64, _P, _I64, _I, _P, _SZ, _P, _P, _P, _P], _I),
     "nfem_rt1_sign_mask": ([_P, _I64, _I, _P, _P], _I),

@@ -1,4 +1,6 @@
 // ABI helpers, device prefix scan, coordinate split.
+#include <mutex>
+
 #include "nfem_common.cuh"
 
 namespace nfem {
@@ -128,6 +130,36 @@ int exclusive_scan_i32(const int32_t* in, int64_t n, int64_t* out, void* ws, siz
   return NFEM_OK;
 }
 
+// ------------------------------------------------- scan without allocation
+// Scratch for nfem_exclusive_scan_noalloc: one int64 per tile of kScanTile
+// counts.  A file-scope device array exists once per device that loads the
+// library and stays resident until the process exits.
+constexpr int64_t kNoAllocMaxTiles = 16384;
+constexpr int64_t kNoAllocMaxCounts = kNoAllocMaxTiles * kScanTile;  // 67,108,864
+static __device__ __align__(256) int64_t g_noalloc_scan_scratch[kNoAllocMaxTiles];
+
+// Device address of g_noalloc_scan_scratch, looked up once per device.  In
+// host code the symbol's name is only a host-side stand-in and must never be
+// handed to a kernel; cudaGetSymbolAddress gives the real device address.
+constexpr int kMaxDevices = 64;
+static int64_t* g_noalloc_scratch_ptr[kMaxDevices] = {nullptr};
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch(int64_t** out) {
+  int dev = 0;
+  NFEM_TRY_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return NFEM_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_scratch_ptr[dev]) {
+    int64_t* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scan_scratch);
+    if (e != cudaSuccess || !ptr) return NFEM_ERR_CUDA;
+    g_noalloc_scratch_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_scratch_ptr[dev];
+  return NFEM_OK;
+}
+
 // ---------------------------------------------------------------- split
 __global__ void split_points_kernel(const double* __restrict__ p, int64_t n, float* __restrict__ out) {
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
@@ -182,6 +214,30 @@ extern "C" int nfem_points_split(const double* points, int64_t n_points, float* 
   if (n_points < 0 || (n_points > 0 && (!points || !out))) return NFEM_ERR_INVALID_ARG;
   if (n_points == 0) return NFEM_OK;
   split_points_kernel<<<grid_for(n_points, 256), 256, 0, (cudaStream_t)stream>>>(points, n_points, out);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+extern "C" int nfem_exclusive_scan_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, void* stream) {
+  if (n < 0 || !offsets || (n > 0 && !counts)) return NFEM_ERR_INVALID_ARG;
+  if (n > kNoAllocMaxCounts) return NFEM_ERR_CAPACITY;
+  int64_t* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n == 0) {
+    NFEM_TRY_CUDA(cudaMemsetAsync(offsets, 0, sizeof(int64_t), st));
+    return NFEM_OK;
+  }
+  // The same three passes as nfem_exclusive_scan.  Every tile sum the later
+  // passes read is written by the first pass of the same call, so whatever a
+  // previous call left in the scratch needs no clearing.
+  const int64_t tiles = ceil_div(n, kScanTile);
+  scan_tile_sums<<<unsigned(tiles), kScanThreads, 0, st>>>(counts, n, scratch);
+  NFEM_CHECK_LAUNCH();
+  scan_sums_single<<<1, 1024, 0, st>>>(scratch, tiles, offsets + n);
+  NFEM_CHECK_LAUNCH();
+  scan_tiles<<<unsigned(tiles), kScanThreads, 0, st>>>(counts, n, scratch, offsets);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }
