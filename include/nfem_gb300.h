@@ -203,6 +203,57 @@ int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t 
                               void* values, void* rhs, int accumulate,
                               int32_t* dev_status, void* stream);
 
+/* ------------------------- vector P2 linear elasticity (a12, a13, a15)
+ * Replaces LEPrimalWeakForm.evaluate_form
+ * (src/weak_forms/le_primal_weak_form.py:10-129) for every tetrahedron, with
+ * the scatter of src/assembly/ScatterFormData.py:5-25: the CSR values of the
+ * global Jacobian and the residual at alpha = 0 (r = +int f . phi).  One
+ * field, 3 components, DoF = row0 + 3 * node + component.  lambda and mu are
+ * per cell, force per cell [n_cells, 3] or NULL.  ref_S [10*10*3*3]
+ * (int dhat_k phihat_a dhat_l phihat_b) and ref_m [10] (int phihat_a) are the
+ * exact reference-tetrahedron tables (host arrays).  Row owner, each value
+ * written once, deterministic. */
+int nfem_pattern_node_codes(const int32_t* cell_dofs, int64_t n_cells, int n_loc, int n_comp,
+                            int64_t row0, int64_t n_rows, const int32_t* inc_ptr,
+                            const int32_t* inc, const int32_t* row_ptr, const int32_t* col_idx,
+                            uint8_t* node_codes, int32_t* dev_status, void* stream);
+int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                                const double* points, const float* points_split,
+                                const int32_t* cell_vertices, const void* lambda_,
+                                const void* mu, const void* force, const double* ref_S,
+                                const double* ref_m, const int32_t* inc_ptr, const int32_t* inc,
+                                const uint8_t* node_codes, const int32_t* row_ptr, void* values,
+                                void* rhs, int accumulate, int32_t* dev_status, void* stream);
+/* Replaces LEPrimalWeakFormBCDirichlet.evaluate_form
+ * (src/weak_forms/le_primal_weak_form.py:131-177) with u_D = 0: adds
+ * beta * int_F phi_a phi_b to every component's (a, b) entry of the boundary
+ * facets' rows.  facet_dofs [n_facets, 18] in facet P2 order, facet_vertices
+ * [n_facets, 3]; ref_Mf [6*6] the reference-triangle P2 mass matrix.
+ * Accumulates with atomics (the order of additions into a row may vary). */
+int nfem_elasticity_p2_penalty(int value_type, int64_t n_facets, const int32_t* facet_dofs,
+                               const int32_t* facet_vertices, const double* points, double beta,
+                               const double* ref_S, const double* ref_m, const double* ref_Mf,
+                               const int32_t* row_ptr, const int32_t* col_idx, void* values,
+                               int32_t* dev_status, void* stream);
+
+/* ------------------------------- mixed Cosserat elasticity, 3-D (a14)
+ * Replaces LCEDualWeakForm.evaluate_form_vectorized
+ * (src/weak_forms/lce_dual_weak_form.py:410-648) for every tetrahedron with
+ * the scatter: fields s (RT1 x 3), m (RT1 x 3), u (P0 x 3), t (P0 x 3), DoF =
+ * row0 + 3 * node + component.  params7 = {lambda_s, mu_s, kappa_s,
+ * lambda_o, mu_o, kappa_o, l} (host), force [n_cells, 6] (f_u, f_t) or
+ * NULL; ref_Psi [4*4*3*3] = int psihat_i psihat_j^T, ref_mhat [4*3] =
+ * int psihat_i, ref_divhat [4] = int div psihat_i on the reference
+ * tetrahedron (host).  Row owner over node rows, each value written once. */
+int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                           const double* points, const float* points_split,
+                           const int32_t* cell_vertices, const uint8_t* sign_mask,
+                           const double* params7, const void* force, const double* ref_Psi,
+                           const double* ref_mhat, const double* ref_divhat,
+                           const int32_t* inc_ptr, const int32_t* inc,
+                           const uint8_t* node_codes, const int32_t* row_ptr, void* values,
+                           void* rhs, int accumulate, int32_t* dev_status, void* stream);
+
 /* -------------------------------------------- K5 + K7: Krylov solve (a17)
  * Replaces the PETSc KSP solves of the drivers
  * (examples/md_elliptic_scalar/md_elliptic_scalar.py:343-363,

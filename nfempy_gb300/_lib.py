@@ -105,6 +105,14 @@ _SIGS = {
     "nfem_mlp_backward": ([_P, _I, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _SZ, _P, _P], _I),
     "nfem_adam_step": ([_I64, _P, _P, _P, _P, C.c_float, C.c_float, C.c_float, C.c_float, _I, _P, _P], _I),
     "nfem_to_bf16": ([_I64, _P, _P, _P], _I),
+    "nfem_pattern_node_codes": ([_P, _I64, _I, _I, _I64, _I64, _P, _P, _P, _P, _P, _P, _P], _I),
+    "nfem_elasticity_p2_assemble": ([_I, _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), _P, _P, _P, _P, _P, _P, _I, _P, _P], _I),
+    "nfem_elasticity_p2_penalty": ([_I, _I64, _P, _P, _P, C.c_double, C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double), _P, _P, _P, _P, _P], _I),
+    "nfem_cosserat_assemble": ([_I, _I64, _I64, _I64, _P, _P, _P, _P, C.POINTER(C.c_double), _P,
+                                C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), _P, _P, _P,
+                                _P, _P, _P, _I, _P, _P], _I),
 }
 
 _lib = None

@@ -59,6 +59,16 @@ class CSRMatrix:
             _lib.call("nfem_pattern_local_codes", _lib.ptr(space.cell_dofs), T, n_loc, n_loc, self.n_rows,
                       _lib.ptr(self.inc_ptr), _lib.ptr(self.inc), _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
                       _lib.ptr(self.codes), _lib.ptr(self.status), st)
+        self.node_codes = None
+        vec = [space.discrete_spaces[n] for n in space.names]
+        ncs = {f.n_comp for f in vec}
+        if (self.codes is None and len(ncs) == 1 and vec[0].n_comp > 1 and n_loc % vec[0].n_comp == 0
+                and n_loc // vec[0].n_comp <= 16 and space.dof_shift % vec[0].n_comp == 0):
+            self.n_comp = vec[0].n_comp
+            self.node_codes = torch.empty((T * n_loc, 16), dtype=torch.uint8, device=dev)
+            _lib.call("nfem_pattern_node_codes", _lib.ptr(space.cell_dofs), T, n_loc, self.n_comp, space.dof_shift,
+                      self.n_rows, _lib.ptr(self.inc_ptr), _lib.ptr(self.inc), _lib.ptr(self.row_ptr),
+                      _lib.ptr(self.col_idx), _lib.ptr(self.node_codes), _lib.ptr(self.status), st)
         self.pairs = None
         if self.codes is not None and max_incidence(self.inc_ptr) <= 2:
             self.pairs = torch.empty((self.n_rows, 2), dtype=torch.int32, device=dev)
@@ -312,3 +322,195 @@ class SequentialAssembler:
         self.jacobian.fresh = False
         if host_res is not None:
             host_res += residual.double().cpu().numpy()
+
+
+def _cellwise(v, T, what, sp, form):
+    """Scalar, per-cell array, or callable constant on each cell -> [T] float64."""
+    if callable(v):
+        xq = form.quadrature_points()
+        vals = np.asarray(v(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).reshape(T, -1)
+        if np.abs(vals - vals[:, :1]).max() > 1e-14 * max(1.0, np.abs(vals).max()):
+            raise NotImplementedError(f"{what} must be constant on each cell")
+        return vals[:, 0]
+    a = np.asarray(v, dtype=np.float64).reshape(-1)
+    return np.full(T, a[0]) if a.size == 1 else a
+
+
+class LEPrimalWeakForm(WeakForm):
+    """Vector P2 linear elasticity (src/weak_forms/le_primal_weak_form.py:10-129)
+    on tetrahedra; field "u" (Lagrange, k=2, 3 components).
+
+    functions: "lambda", "mu" - scalar, per-cell array, or f(x, y, z) constant
+               per cell; "rhs" - None, a 3-vector, per-cell array [T, 3], or
+               f(x, y, z) -> [3, N] constant per cell.  r = +int f . phi."""
+
+    def _check_space(self):
+        sp = self.space
+        if sp is None or self.functions is None:
+            raise ValueError
+        u = sp.discrete_spaces.get("u")
+        if (len(sp.names) != 1 or u is None or u.family != "Lagrange" or u.k_order != 2 or u.n_comp != 3
+                or sp.dim != 3 or u.discontinuous):
+            raise NotImplementedError("LEPrimalWeakForm expects one field 'u': continuous vector P2 on tetrahedra")
+
+    def coefficients(self, dtype):
+        key = ("coef", dtype)
+        if key in self._cache:
+            return self._cache[key]
+        sp = self.space
+        T = sp.n_cells
+        lam = _cellwise(self.functions["lambda"], T, "lambda", sp, self)
+        mu = _cellwise(self.functions["mu"], T, "mu", sp, self)
+        f = self.functions.get("rhs")
+        ft = None
+        if f is not None:
+            if callable(f):
+                xq = self.quadrature_points()
+                fv = np.asarray(f(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).reshape(3, T, -1)
+                if np.abs(fv - fv[:, :, :1]).max() > 1e-14 * max(1.0, np.abs(fv).max()):
+                    raise NotImplementedError("rhs must be constant on each cell")
+                fv = fv[:, :, 0].T
+            else:
+                fv = np.asarray(f, dtype=np.float64)
+                fv = np.broadcast_to(fv.reshape(-1, 3) if fv.size != 3 else fv.reshape(1, 3), (T, 3))
+            ft = torch.as_tensor(np.ascontiguousarray(fv), dtype=dtype, device=sp.device)
+        from .elements import p2_reference_tables
+        S, m, Mf = p2_reference_tables(3)
+        out = (torch.as_tensor(lam, dtype=dtype, device=sp.device), torch.as_tensor(mu, dtype=dtype, device=sp.device),
+               ft, np.ascontiguousarray(S.reshape(-1)), np.ascontiguousarray(m), np.ascontiguousarray(Mf.reshape(-1)))
+        self._cache[key] = out
+        return out
+
+    def assemble(self, jacobian, residual, accumulate=False, stream=None, coefficients=None):
+        self._check_space()
+        sp = self.space
+        dtype = jacobian.dtype
+        vt = _lib.NFEM_F64 if dtype == torch.float64 else _lib.NFEM_F32
+        if jacobian.node_codes is None:
+            raise NotImplementedError("matrix built without node codes")
+        lam, mu, f, S, m, _ = coefficients if coefficients is not None else self.coefficients(dtype)
+        dp = _lib.C.POINTER(_lib.C.c_double)
+        _lib.call("nfem_elasticity_p2_assemble", vt, sp.n_cells, sp.n_dof // 3, sp.dof_shift, _lib.ptr(sp.points),
+                  _lib.ptr(sp.points_split), _lib.ptr(sp.cells), _lib.ptr(lam), _lib.ptr(mu), _lib.ptr(f),
+                  S.ctypes.data_as(dp), m.ctypes.data_as(dp), _lib.ptr(jacobian.inc_ptr), _lib.ptr(jacobian.inc),
+                  _lib.ptr(jacobian.node_codes), _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values),
+                  _lib.ptr(residual), int(accumulate), _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+
+
+class LEPrimalWeakFormBCDirichlet(WeakForm):
+    """Penalty Dirichlet condition u = 0 on the boundary facets
+    (src/weak_forms/le_primal_weak_form.py:131-177, beta = 1e12): adds
+    beta int_F phi_a phi_b to every component's (a, b) entry.  Accumulates
+    into the matrix (use it as the second form of an assembly pass)."""
+
+    beta = 1.0e12
+
+    def facet_dofs(self):
+        """[n_facets, 18] DoFs of the boundary facets in the facet's P2 order
+        (vertices in file order, then edges (1,2), (0,2), (0,1))."""
+        if "fdofs" in self._cache:
+            return self._cache["fdofs"]
+        sp = self.space
+        cells = sp.cells_host
+        T = sp.n_cells
+        V = sp.mesh.points.shape[0]
+        r0 = sp.occ_rank[0].cpu().numpy()
+        vrank = np.full(V, -1, dtype=np.int64)
+        vrank[cells.ravel()] = r0.ravel()
+        from .elements import P2_EDGES
+        tet_e = np.array(P2_EDGES[3])
+        ekeys_c = np.sort(cells[:, tet_e], axis=2)
+        ek = (ekeys_c[..., 0] * V + ekeys_c[..., 1]).ravel()
+        r1 = sp.occ_rank[1].cpu().numpy().ravel()
+        order = np.argsort(ek, kind="stable")
+        ek_s, r1_s = ek[order], r1[order]
+        fac = sp.facets.cpu().numpy().astype(np.int64)
+        tri_e = np.array(P2_EDGES[2])
+        fk = np.sort(fac[:, tri_e], axis=2)
+        fkey = fk[..., 0] * V + fk[..., 1]
+        pos = np.searchsorted(ek_s, fkey.ravel())
+        if np.any(pos >= ek_s.size) or np.any(ek_s[np.minimum(pos, ek_s.size - 1)] != fkey.ravel()):
+            raise ValueError("boundary facet edge not found among the cells' edges")
+        erank = r1_s[pos].reshape(-1, 3)
+        base_v = sp.field_offsets["u"]
+        base_e = base_v + 3 * sp.n_entities[0]
+        nodes = np.concatenate([base_v + 3 * vrank[fac], base_e + 3 * erank], axis=1)  # [F, 6]
+        fd = (nodes[:, :, None] + np.arange(3)[None, None, :]).reshape(-1, 18)
+        out = (torch.as_tensor(fd.astype(np.int32), device=sp.device),
+               torch.as_tensor(fac.astype(np.int32), device=sp.device))
+        self._cache["fdofs"] = out
+        return out
+
+    def assemble(self, jacobian, residual=None, accumulate=True, stream=None):
+        sp = self.space
+        fd, fv = self.facet_dofs()
+        vt = _lib.NFEM_F64 if jacobian.dtype == torch.float64 else _lib.NFEM_F32
+        from .elements import p2_reference_tables
+        S, m, Mf = p2_reference_tables(3)
+        S = np.ascontiguousarray(S.reshape(-1))
+        Mf = np.ascontiguousarray(Mf.reshape(-1))
+        dp = _lib.C.POINTER(_lib.C.c_double)
+        _lib.call("nfem_elasticity_p2_penalty", vt, fd.shape[0], _lib.ptr(fd), _lib.ptr(fv), _lib.ptr(sp.points),
+                  float(self.beta), S.ctypes.data_as(dp), m.ctypes.data_as(dp), Mf.ctypes.data_as(dp),
+                  _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.col_idx), _lib.ptr(jacobian.values),
+                  _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+
+
+class LCEDualWeakForm(WeakForm):
+    """Mixed Cosserat elasticity, 3-D (src/weak_forms/lce_dual_weak_form.py:410-648):
+    fields s (RT1, 3 rows), m (RT1, 3 rows), u (P0^3), t (P0^3) in that order.
+
+    functions: lambda_s, mu_s, kappa_s, lambda_o, mu_o, kappa_o, l - scalars
+    (constant material, as the reference drivers use); "rhs" - None, a
+    6-vector (f_u, f_t), or a per-cell array [T, 6]."""
+
+    NAMES = ("lambda_s", "mu_s", "kappa_s", "lambda_o", "mu_o", "kappa_o", "l")
+
+    def _check_space(self):
+        sp = self.space
+        if sp is None or self.functions is None:
+            raise ValueError
+        if sp.names != ["s", "m", "u", "t"] or sp.dim != 3:
+            raise NotImplementedError("LCEDualWeakForm expects fields ('s', 'm', 'u', 't') on tetrahedra")
+        d = sp.discrete_spaces
+        ok = (d["s"].family == "RT" and d["s"].k_order == 1 and d["m"].family == "RT" and d["m"].k_order == 1
+              and d["u"].family == "Lagrange" and d["u"].k_order == 0 and d["t"].family == "Lagrange"
+              and d["t"].k_order == 0 and all(d[n].n_comp == 3 for n in sp.names))
+        if not ok:
+            raise NotImplementedError("LCEDualWeakForm expects RT1^3 x RT1^3 x P0^3 x P0^3")
+
+    def coefficients(self, dtype):
+        key = ("coef", dtype)
+        if key in self._cache:
+            return self._cache[key]
+        sp = self.space
+        T = sp.n_cells
+        par = np.array([float(np.ravel(self.functions[k])[0]) for k in self.NAMES], dtype=np.float64)
+        f = self.functions.get("rhs")
+        ft = None
+        if f is not None:
+            fv = np.asarray(f, dtype=np.float64)
+            fv = np.broadcast_to(fv.reshape(1, 6) if fv.size == 6 else fv.reshape(T, 6), (T, 6))
+            ft = torch.as_tensor(np.ascontiguousarray(fv), dtype=dtype, device=sp.device)
+        from .elements import rt1_tet_tables
+        Psi, mhat, divhat = rt1_tet_tables()
+        out = (par, ft, np.ascontiguousarray(Psi.reshape(-1)), np.ascontiguousarray(mhat.reshape(-1)),
+               np.ascontiguousarray(divhat))
+        self._cache[key] = out
+        return out
+
+    def assemble(self, jacobian, residual, accumulate=False, stream=None, coefficients=None):
+        self._check_space()
+        sp = self.space
+        dtype = jacobian.dtype
+        vt = _lib.NFEM_F64 if dtype == torch.float64 else _lib.NFEM_F32
+        if jacobian.node_codes is None:
+            raise NotImplementedError("matrix built without node codes")
+        par, f, Psi, mhat, divhat = coefficients if coefficients is not None else self.coefficients(dtype)
+        dp = _lib.C.POINTER(_lib.C.c_double)
+        _lib.call("nfem_cosserat_assemble", vt, sp.n_cells, sp.n_dof // 3, sp.dof_shift, _lib.ptr(sp.points),
+                  _lib.ptr(sp.points_split), _lib.ptr(sp.cells), _lib.ptr(sp.rt_sign_mask), par.ctypes.data_as(dp),
+                  _lib.ptr(f), Psi.ctypes.data_as(dp), mhat.ctypes.data_as(dp), divhat.ctypes.data_as(dp),
+                  _lib.ptr(jacobian.inc_ptr), _lib.ptr(jacobian.inc), _lib.ptr(jacobian.node_codes),
+                  _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate),
+                  _lib.ptr(jacobian.status), _lib.stream_ptr(stream))

@@ -1,0 +1,289 @@
+// Mixed Cosserat elasticity (3-D): element integrals + CSR scatter.
+//
+// Reference: LCEDualWeakForm.evaluate_form_vectorized
+// (src/weak_forms/lce_dual_weak_form.py:410-648).  Fields s (RT1, three rows
+// of the stress), m (RT1, three rows of the couple stress), u (P0^3), t (P0^3),
+// local order s, m, u, t, basis-major / component-minor.  With
+// Phi_ij = int psi_i psi_j^T (3 x 3) of the oriented, Piola-mapped RT1
+// functions:
+//   (s,s)[(i,c),(j,d)] = tr(Phi_ij) delta_cd (1/(4 mu) + 1/(4 kappa))
+//                      + Phi_ij[d][c] (1/(4 mu) - 1/(4 kappa)) - vf Phi_ij[c][d],
+//     vf = lambda / (2 mu (2 mu + 3 lambda));  (m,m) the same with the
+//     couple-stress parameters, scaled by 1/l;
+//   (t,s)[c,(j,d)] = M(v_j)[c][d], v_j = int psi_j, M(v) = [[0, vz, -vy],
+//     [-vz, 0, vx], [vy, -vx, 0]]  (the asymmetry coupling, :531-580), and its
+//     transpose in (s,t);
+//   (u,s)[c,(j,d)] = delta_cd int div psi_j, (t,m) likewise, and transposes;
+//   r[u_c] = -int f_c, r[t_c] = -int f_{3+c}  (alpha = 0).
+// Closed forms on affine cells: Phi_ij = sg_i sg_j J Psihat_ij J^T / |det J|,
+// v_j = sg_j J mhat_j, int div psi_j = sg_j divhat_j, sg = orientation signs.
+//
+// GPU design: the node-row owner of the vector P2 kernel (elasticity.cu):
+// the CSR has 3 x 3 blocks (every field has three components), one warp owns
+// a node's three rows, one 10-lane group per incidence, lane b evaluates the
+// 3 x 3 block of local node b; group images summed in a fixed order.
+#include <string.h>
+
+#include <mutex>
+
+#include "nfem_common.cuh"
+
+namespace nfem {
+
+constexpr int kCosDegMax = 32;
+constexpr int kCosWarps = 4;
+
+__constant__ double c_Psi[4 * 4 * 9];
+__constant__ double c_mhat[4 * 3];
+__constant__ double c_divhat[4];
+
+static double h_Psi[144], h_mhat[12], h_divhat[4];
+static bool h_cos_set = false;
+static std::mutex h_cos_mutex;
+
+static int upload_cos_tables(const double* Psi, const double* mhat, const double* divhat, cudaStream_t s) {
+  std::lock_guard<std::mutex> lock(h_cos_mutex);
+  if (h_cos_set && !memcmp(Psi, h_Psi, sizeof(h_Psi)) && !memcmp(mhat, h_mhat, sizeof(h_mhat)) &&
+      !memcmp(divhat, h_divhat, sizeof(h_divhat)))
+    return NFEM_OK;
+  memcpy(h_Psi, Psi, sizeof(h_Psi));
+  memcpy(h_mhat, mhat, sizeof(h_mhat));
+  memcpy(h_divhat, divhat, sizeof(h_divhat));
+  NFEM_TRY_CUDA(cudaMemcpyToSymbolAsync(c_Psi, h_Psi, sizeof(h_Psi), 0, cudaMemcpyHostToDevice, s));
+  NFEM_TRY_CUDA(cudaMemcpyToSymbolAsync(c_mhat, h_mhat, sizeof(h_mhat), 0, cudaMemcpyHostToDevice, s));
+  NFEM_TRY_CUDA(cudaMemcpyToSymbolAsync(c_divhat, h_divhat, sizeof(h_divhat), 0, cudaMemcpyHostToDevice, s));
+  NFEM_TRY_CUDA(cudaStreamSynchronize(s));
+  h_cos_set = true;
+  return NFEM_OK;
+}
+
+struct CosParams {
+  int64_t n_nodes;
+  int64_t row0;
+  const double* points;
+  const float* split;
+  const int32_t* cv;
+  const uint8_t* sign;
+  const double* par;  // host copy in the struct below
+  double mu_s, kappa_s, lam_s, mu_o, kappa_o, lam_o, l;
+  const void* force;  // [n_cells, 6] or NULL
+  const int32_t* inc_ptr;
+  const int32_t* inc;
+  const uint8_t* codes;
+  const int32_t* row_ptr;
+  void* values;
+  void* rhs;
+  int accumulate;
+  int32_t* status;
+};
+
+template <typename T>
+__device__ __forceinline__ void cos_edges(const CosParams& p, int32_t c, T (&J)[3][3]);
+
+template <>
+__device__ __forceinline__ void cos_edges<double>(const CosParams& p, int32_t c, double (&J)[3][3]) {
+  const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+  const int vs[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      J[d][k] = __ldg(p.points + int64_t(vs[k + 1]) * 3 + d) - __ldg(p.points + int64_t(vs[0]) * 3 + d);
+}
+
+template <>
+__device__ __forceinline__ void cos_edges<float>(const CosParams& p, int32_t c, float (&J)[3][3]) {
+  const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+  const int vs[4] = {v.x, v.y, v.z, v.w};
+  const float* s0 = p.split + int64_t(vs[0]) * 6;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float* sk = p.split + int64_t(vs[k + 1]) * 6;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) J[d][k] = (__ldg(sk + d) - __ldg(s0 + d)) + (__ldg(sk + 3 + d) - __ldg(s0 + 3 + d));
+  }
+}
+
+// 3 x 3 block between local nodes a (row) and b (column); node kinds:
+// 0..3 s-faces, 4..7 m-faces, 8 u, 9 t.
+template <typename T>
+__device__ __forceinline__ void cos_block(const CosParams& p, const T (&J)[3][3], T adet, uint32_t m, int a, int b,
+                                          T (&K)[3][3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) K[i][j] = T(0);
+  const bool as = a < 4, am = a >= 4 && a < 8, au = a == 8, at = a == 9;
+  const bool bs = b < 4, bm = b >= 4 && b < 8, bu = b == 8, bt = b == 9;
+  const int fa = a & 3, fb = b & 3;
+  const T sga = ((m >> fa) & 1u) ? T(-1) : T(1);
+  const T sgb = ((m >> fb) & 1u) ? T(-1) : T(1);
+  if ((as && bs) || (am && bm)) {
+    // Phi = sga sgb J Psihat_ab J^T / |det|
+    const double* Ps = c_Psi + (fa * 4 + fb) * 9;
+    T PJ[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        PJ[k][q] = T(Ps[k * 3 + 0]) * J[q][0] + T(Ps[k * 3 + 1]) * J[q][1] + T(Ps[k * 3 + 2]) * J[q][2];
+    T Phi[3][3];
+    const T sc = sga * sgb / adet;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) Phi[c][d] = sc * (J[c][0] * PJ[0][d] + J[c][1] * PJ[1][d] + J[c][2] * PJ[2][d]);
+    const T tr = Phi[0][0] + Phi[1][1] + Phi[2][2];
+    T mu, ka, la, scale;
+    if (as) { mu = T(p.mu_s); ka = T(p.kappa_s); la = T(p.lam_s); scale = T(1); }
+    else { mu = T(p.mu_o); ka = T(p.kappa_o); la = T(p.lam_o); scale = T(1) / T(p.l); }
+    const T cin = T(0.25) / mu + T(0.25) / ka;
+    const T cout = T(0.25) / mu - T(0.25) / ka;
+    const T vf = la / (T(2) * mu * (T(2) * mu + T(3) * la));
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) K[c][d] = scale * ((c == d ? tr * cin : T(0)) + Phi[d][c] * cout - vf * Phi[c][d]);
+  } else if ((at && bs) || (as && bt)) {
+    const int f = at ? fb : fa;
+    const T sg = at ? sgb : sga;
+    T v[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      v[k] = sg * (J[k][0] * T(c_mhat[f * 3 + 0]) + J[k][1] * T(c_mhat[f * 3 + 1]) + J[k][2] * T(c_mhat[f * 3 + 2]));
+    T M[3][3] = {{T(0), v[2], -v[1]}, {-v[2], T(0), v[0]}, {v[1], -v[0], T(0)}};
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) K[c][d] = at ? M[c][d] : M[d][c];
+  } else if ((au && bs) || (as && bu) || (at && bm) || (am && bt)) {
+    const int f = (au || at) ? fb : fa;
+    const T sg = (au || at) ? sgb : sga;
+    const T val = sg * T(c_divhat[f]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) K[c][c] = val;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const CosParams p) {
+  constexpr int IMG = 3 * 3 * kCosDegMax;
+  __shared__ T img[kCosWarps][2][IMG];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane / 10, b = lane - 10 * (lane / 10);
+  const T* force = static_cast<const T*>(p.force);
+  T* values = static_cast<T*>(p.values);
+  T* rhs = static_cast<T*>(p.rhs);
+  for (int64_t v = int64_t(blockIdx.x) * kCosWarps + warp; v < p.n_nodes; v += int64_t(gridDim.x) * kCosWarps) {
+    const int64_t r0 = p.row0 + 3 * v;
+    const int32_t base = __ldg(p.row_ptr + r0);
+    const int len = __ldg(p.row_ptr + r0 + 1) - base;
+    const int32_t kb = __ldg(p.inc_ptr + r0), ke = __ldg(p.inc_ptr + r0 + 1);
+    if (len > 3 * kCosDegMax || len % 3 != 0 || ke - kb > 2) {
+      if (lane == 0) set_status(p.status, NFEM_ERR_UNSUPPORTED);
+      continue;
+    }
+    for (int i = lane; i < 3 * len; i += 32) {
+      img[warp][0][i] = T(0);
+      img[warp][1][i] = T(0);
+    }
+    __syncwarp();
+    T rhs_acc[3] = {T(0), T(0), T(0)};
+    const int32_t k = kb + g;
+    if (lane < 20 && k < ke) {
+      const int32_t occ = __ldg(p.inc + k);
+      const int32_t c = occ / 30;
+      const int a = (occ - c * 30) / 3;
+      const int pos = __ldg(p.codes + int64_t(k) * 16 + b);
+      T J[3][3];
+      cos_edges<T>(p, c, J);
+      const T det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                    J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      if (!(det != T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+      const T adet = det < T(0) ? -det : det;
+      const uint32_t m = __ldg(p.sign + c);
+      T K[3][3];
+      cos_block<T>(p, J, adet, m, a, b, K);
+      T* im = img[warp][g];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) im[min(i * len + 3 * pos + j, IMG - 1)] += K[i][j];
+      if (b == 0 && force && (a == 8 || a == 9)) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+          rhs_acc[i] = -adet * T(1.0 / 6.0) * __ldg(force + int64_t(c) * 6 + (a == 8 ? 0 : 3) + i);
+      }
+    }
+    __syncwarp();
+    for (int i = lane; i < len * 3; i += 32) {
+      const T s = img[warp][0][i] + img[warp][1][i];
+      if (p.accumulate) values[int64_t(base) + i] += s; else values[int64_t(base) + i] = s;
+    }
+    T r[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) r[i] = __shfl_sync(0xffffffffu, rhs_acc[i], 0) + __shfl_sync(0xffffffffu, rhs_acc[i], 10);
+    if (lane < 3) {
+      const T rv = lane == 0 ? r[0] : (lane == 1 ? r[1] : r[2]);
+      if (p.accumulate) rhs[r0 + lane] += rv; else rhs[r0 + lane] = rv;
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace nfem
+
+using namespace nfem;
+
+extern "C" int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                                      const double* points, const float* points_split, const int32_t* cell_vertices,
+                                      const uint8_t* sign_mask, const double* params7, const void* force,
+                                      const double* ref_Psi, const double* ref_mhat, const double* ref_divhat,
+                                      const int32_t* inc_ptr, const int32_t* inc, const uint8_t* node_codes,
+                                      const int32_t* row_ptr, void* values, void* rhs, int accumulate,
+                                      int32_t* dev_status, void* stream_) {
+  (void)n_cells;
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n_nodes < 0 || row0 < 0 || !params7)
+    return NFEM_ERR_INVALID_ARG;
+  if (n_nodes == 0) return NFEM_OK;
+  if (!cell_vertices || !sign_mask || !ref_Psi || !ref_mhat || !ref_divhat || !inc_ptr || !inc || !node_codes ||
+      !row_ptr || !values || !rhs)
+    return NFEM_ERR_INVALID_ARG;
+  if (value_type == NFEM_F64 && !points) return NFEM_ERR_INVALID_ARG;
+  if (value_type == NFEM_F32 && !points_split) return NFEM_ERR_INVALID_ARG;
+  if (reinterpret_cast<uintptr_t>(cell_vertices) & 15) return NFEM_ERR_INVALID_ARG;
+  int rc = upload_cos_tables(ref_Psi, ref_mhat, ref_divhat, stream);
+  if (rc) return rc;
+  CosParams p;
+  p.n_nodes = n_nodes;
+  p.row0 = row0;
+  p.points = points;
+  p.split = points_split;
+  p.cv = cell_vertices;
+  p.sign = sign_mask;
+  p.par = nullptr;
+  p.lam_s = params7[0];
+  p.mu_s = params7[1];
+  p.kappa_s = params7[2];
+  p.lam_o = params7[3];
+  p.mu_o = params7[4];
+  p.kappa_o = params7[5];
+  p.l = params7[6];
+  p.force = force;
+  p.inc_ptr = inc_ptr;
+  p.inc = inc;
+  p.codes = node_codes;
+  p.row_ptr = row_ptr;
+  p.values = values;
+  p.rhs = rhs;
+  p.accumulate = accumulate != 0;
+  p.status = dev_status;
+  const int grid = grid_for(ceil_div(n_nodes, kCosWarps), 1, 8);
+  if (value_type == NFEM_F64)
+    cosserat_rows_kernel<double><<<grid, 32 * kCosWarps, 0, stream>>>(p);
+  else
+    cosserat_rows_kernel<float><<<grid, 32 * kCosWarps, 0, stream>>>(p);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}

@@ -1,0 +1,372 @@
+// Vector P2 linear elasticity: element integrals + CSR scatter (row owner),
+// and the boundary penalty form.
+//
+// Reference: LEPrimalWeakForm.evaluate_form
+// (src/weak_forms/le_primal_weak_form.py:10-129): for basis a, component i
+// and basis b, component j,
+//   j[(a,i),(b,j)] = int mu (grad phi_a . grad phi_b) delta_ij
+//                  + mu d_j phi_a d_i phi_b + lambda d_i phi_a d_j phi_b
+//   r[(a,i)]       = + int f_i phi_a        (alpha = 0)
+// LEPrimalWeakFormBCDirichlet (le_primal_weak_form.py:131-177): on boundary
+// facets j[(a,i),(b,i)] += beta int phi_a phi_b, beta = 1e12 (u_D = 0 here).
+//
+// Closed form on affine cells with cell-wise constant lambda, mu:
+//   A_ab[p][q] = int d_p phi_a d_q phi_b = |det J| (J^-T S_ab J^-1)_pq,
+//   S_ab[k][l] = int_ref dhat_k phihat_a dhat_l phihat_b  (exact reference table),
+//   K_ab[i][j] = mu delta_ij tr(A_ab) + mu A_ab[j][i] + lambda A_ab[i][j].
+//
+// GPU design: one warp per node owns the node's three component rows (they
+// are consecutive in the CSR and share one column structure of 3 x deg
+// entries).  Three groups of ten lanes each take one (cell, local node a)
+// incidence per step; lane b of a group evaluates the 3 x 3 block K_ab and
+// adds it into its group's shared-memory image of the three rows at the node
+// position given by the 8-bit node codes.  The three images are summed in a
+// fixed order and stored coalesced: each value written once, no atomics,
+// bitwise deterministic.
+#include <string.h>
+
+#include <mutex>
+
+#include "nfem_common.cuh"
+
+namespace nfem {
+
+constexpr int kElasDegMax = 96;  // node columns per node row
+constexpr int kElasWarps32 = 4;
+constexpr int kElasWarps64 = 2;
+
+__constant__ double c_S[10 * 10 * 9];
+__constant__ double c_m[10];
+__constant__ double c_Mf[6 * 6];
+
+static double h_S[10 * 10 * 9], h_m[10], h_Mf[36];
+static bool h_tables_set = false;
+static std::mutex h_tables_mutex;
+
+static int upload_tables(const double* S, const double* m, const double* Mf, cudaStream_t s) {
+  std::lock_guard<std::mutex> lock(h_tables_mutex);
+  if (h_tables_set && !memcmp(S, h_S, sizeof(h_S)) && !memcmp(m, h_m, sizeof(h_m)) &&
+      (!Mf || !memcmp(Mf, h_Mf, sizeof(h_Mf))))
+    return NFEM_OK;
+  memcpy(h_S, S, sizeof(h_S));
+  memcpy(h_m, m, sizeof(h_m));
+  if (Mf) memcpy(h_Mf, Mf, sizeof(h_Mf));
+  NFEM_TRY_CUDA(cudaMemcpyToSymbolAsync(c_S, h_S, sizeof(h_S), 0, cudaMemcpyHostToDevice, s));
+  NFEM_TRY_CUDA(cudaMemcpyToSymbolAsync(c_m, h_m, sizeof(h_m), 0, cudaMemcpyHostToDevice, s));
+  NFEM_TRY_CUDA(cudaMemcpyToSymbolAsync(c_Mf, h_Mf, sizeof(h_Mf), 0, cudaMemcpyHostToDevice, s));
+  NFEM_TRY_CUDA(cudaStreamSynchronize(s));
+  h_tables_set = true;
+  return NFEM_OK;
+}
+
+struct ElasParams {
+  int64_t n_nodes;
+  int64_t row0;  // first row of the space (dof_shift)
+  const double* points;
+  const float* split;
+  const int32_t* cv;
+  const void* lam;
+  const void* mu;
+  const void* force;
+  const int32_t* inc_ptr;
+  const int32_t* inc;
+  const uint8_t* codes;
+  const int32_t* row_ptr;
+  void* values;
+  void* rhs;
+  int accumulate;
+  int32_t* status;
+};
+
+template <typename T>
+__device__ __forceinline__ void tet_edges(const ElasParams& p, int32_t c, T (&J)[3][3]);
+
+template <>
+__device__ __forceinline__ void tet_edges<double>(const ElasParams& p, int32_t c, double (&J)[3][3]) {
+  const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+  const int vs[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      J[d][k] = __ldg(p.points + int64_t(vs[k + 1]) * 3 + d) - __ldg(p.points + int64_t(vs[0]) * 3 + d);
+}
+
+template <>
+__device__ __forceinline__ void tet_edges<float>(const ElasParams& p, int32_t c, float (&J)[3][3]) {
+  const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+  const int vs[4] = {v.x, v.y, v.z, v.w};
+  const float* s0 = p.split + int64_t(vs[0]) * 6;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float* sk = p.split + int64_t(vs[k + 1]) * 6;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) J[d][k] = (__ldg(sk + d) - __ldg(s0 + d)) + (__ldg(sk + 3 + d) - __ldg(s0 + 3 + d));
+  }
+}
+
+template <typename T, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasParams p) {
+  constexpr int IMG = 3 * 3 * kElasDegMax;  // 3 rows x 3 deg_max columns
+  __shared__ T img[WARPS][3][IMG];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane / 10, b = lane - 10 * (lane / 10);
+  const T* lam = static_cast<const T*>(p.lam);
+  const T* mu = static_cast<const T*>(p.mu);
+  const T* force = static_cast<const T*>(p.force);
+  T* values = static_cast<T*>(p.values);
+  T* rhs = static_cast<T*>(p.rhs);
+  for (int64_t v = int64_t(blockIdx.x) * WARPS + warp; v < p.n_nodes; v += int64_t(gridDim.x) * WARPS) {
+    const int64_t r0 = p.row0 + 3 * v;
+    const int32_t base = __ldg(p.row_ptr + r0);
+    const int len = __ldg(p.row_ptr + r0 + 1) - base;  // 3 x deg
+    if (len > 3 * kElasDegMax || len % 3 != 0) {
+      if (lane == 0) set_status(p.status, NFEM_ERR_UNSUPPORTED);
+      continue;
+    }
+    for (int i = lane; i < 3 * len; i += 32) {
+      img[warp][0][i] = T(0);
+      img[warp][1][i] = T(0);
+      img[warp][2][i] = T(0);
+    }
+    __syncwarp();
+    const int32_t kb = __ldg(p.inc_ptr + r0), ke = __ldg(p.inc_ptr + r0 + 1);
+    T rhs_acc[3] = {T(0), T(0), T(0)};
+    for (int32_t k0 = kb; k0 < ke; k0 += 3) {
+      const int32_t k = k0 + g;
+      if (lane < 30 && k < ke) {
+        const int32_t occ = __ldg(p.inc + k);
+        const int32_t c = occ / 30;
+        const int a = (occ - c * 30) / 3;
+        const int pos = __ldg(p.codes + int64_t(k) * 16 + b);
+        T J[3][3];
+        tet_edges<T>(p, c, J);
+        // cofactors: Jinv = adj(J) / det
+        const T c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const T c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const T c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const T det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        if (!(det != T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+        const T id = T(1) / det;
+        T Ji[3][3];  // Ji[k][p] = (J^-1)_{kp}
+        Ji[0][0] = c00 * id;
+        Ji[1][0] = c01 * id;
+        Ji[2][0] = c02 * id;
+        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+        const T adet = det < T(0) ? -det : det;
+        const double* S = c_S + (a * 10 + b) * 9;
+        // A = |det| Ji^T S Ji
+        T SJ[3][3];
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+          for (int q = 0; q < 3; ++q)
+            SJ[kk][q] = T(S[kk * 3 + 0]) * Ji[0][q] + T(S[kk * 3 + 1]) * Ji[1][q] + T(S[kk * 3 + 2]) * Ji[2][q];
+        T A[3][3];
+#pragma unroll
+        for (int pp = 0; pp < 3; ++pp)
+#pragma unroll
+          for (int q = 0; q < 3; ++q)
+            A[pp][q] = adet * (Ji[0][pp] * SJ[0][q] + Ji[1][pp] * SJ[1][q] + Ji[2][pp] * SJ[2][q]);
+        const T lc = __ldg(lam + c), mc = __ldg(mu + c);
+        const T tr = A[0][0] + A[1][1] + A[2][2];
+        T* im = img[warp][g];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const T kij = (i == j ? mc * tr : T(0)) + mc * A[j][i] + lc * A[i][j];
+            const int idx = min(i * len + 3 * pos + j, IMG - 1);
+            im[idx] += kij;
+          }
+        if (force && b == 0) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i) rhs_acc[i] += adet * T(c_m[a]) * __ldg(force + int64_t(c) * 3 + i);
+        }
+      }
+      __syncwarp();
+    }
+    // combine the three group images in a fixed order
+    for (int i = lane; i < len * 3; i += 32) {
+      const T s = img[warp][0][i] + img[warp][1][i] + img[warp][2][i];
+      if (p.accumulate) values[int64_t(base) + i] += s; else values[int64_t(base) + i] = s;
+    }
+    T r[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const T a0 = __shfl_sync(0xffffffffu, rhs_acc[i], 0);
+      const T a1 = __shfl_sync(0xffffffffu, rhs_acc[i], 10);
+      const T a2 = __shfl_sync(0xffffffffu, rhs_acc[i], 20);
+      r[i] = a0 + a1 + a2;
+    }
+    if (lane < 3) {
+      const T rv = lane == 0 ? r[0] : (lane == 1 ? r[1] : r[2]);
+      if (p.accumulate) rhs[r0 + lane] += rv; else rhs[r0 + lane] = rv;
+    }
+    __syncwarp();
+  }
+}
+
+// Boundary penalty: for each facet (6 P2 nodes), values at (dof_a,i),(dof_b,i)
+// += beta |det_F| Mf_ab for every component i (atomics: a facet row sums
+// contributions of the facets sharing its node).
+template <typename T>
+__global__ void penalty_kernel(int64_t n_facets, const int32_t* __restrict__ fdofs, const int32_t* __restrict__ fv,
+                               const double* __restrict__ points, const int32_t* __restrict__ row_ptr,
+                               const int32_t* __restrict__ col_idx, double beta, T* __restrict__ values,
+                               int32_t* status) {
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_facets * 36;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t f = t / 36;
+    const int ab = int(t - f * 36);
+    const int a = ab / 6, b = ab - 6 * (ab / 6);
+    double e1[3], e2[3];
+    const int32_t v0 = fv[f * 3], v1 = fv[f * 3 + 1], v2 = fv[f * 3 + 2];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      e1[d] = points[int64_t(v1) * 3 + d] - points[int64_t(v0) * 3 + d];
+      e2[d] = points[int64_t(v2) * 3 + d] - points[int64_t(v0) * 3 + d];
+    }
+    const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                 cz = e1[0] * e2[1] - e1[1] * e2[0];
+    const double detf = sqrt(cx * cx + cy * cy + cz * cz);
+    const double val = beta * detf * c_Mf[a * 6 + b];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const int32_t row = fdofs[f * 18 + a * 3 + i], col = fdofs[f * 18 + b * 3 + i];
+      int32_t lo = row_ptr[row], hi = row_ptr[row + 1];
+      const int32_t end = hi;
+      while (lo < hi) {
+        const int32_t mid = (lo + hi) >> 1;
+        if (col_idx[mid] < col) lo = mid + 1; else hi = mid;
+      }
+      if (lo < end && col_idx[lo] == col) atomicAdd(values + lo, T(val));
+      else set_status(status, NFEM_ERR_PATTERN);
+    }
+  }
+}
+
+// node codes: per incidence of a component-0 row, the node position (column
+// position / n_comp) of each local node's first column in that row
+__global__ void node_codes_kernel(const int32_t* __restrict__ cd, int n_loc, int n_comp, int64_t n_rows, int64_t row0,
+                                  const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                  const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col_idx,
+                                  uint8_t* __restrict__ codes, int32_t* status) {
+  const int n_nodes_loc = n_loc / n_comp;
+  for (int64_t r = row0 + (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) * n_comp; r < n_rows;
+       r += int64_t(gridDim.x) * blockDim.x * n_comp) {
+    const int32_t b0 = row_ptr[r], b1 = row_ptr[r + 1];
+    for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; ++k) {
+      const int32_t c = inc[k] / n_loc;
+      for (int b = 0; b < 16; ++b) {
+        int code = 255;
+        if (b < n_nodes_loc) {
+          const int32_t col = cd[int64_t(c) * n_loc + b * n_comp];
+          int32_t lo = b0, hi = b1;
+          while (lo < hi) {
+            const int32_t mid = (lo + hi) >> 1;
+            if (col_idx[mid] < col) lo = mid + 1; else hi = mid;
+          }
+          if (lo >= b1 || col_idx[lo] != col) set_status(status, NFEM_ERR_PATTERN);
+          const int np = (lo - b0) / n_comp;
+          if (np > 254) set_status(status, NFEM_ERR_UNSUPPORTED);
+          code = min(np, 254);
+        }
+        codes[int64_t(k) * 16 + b] = uint8_t(code);
+      }
+    }
+  }
+}
+
+}  // namespace nfem
+
+using namespace nfem;
+
+extern "C" int nfem_pattern_node_codes(const int32_t* cell_dofs, int64_t n_cells, int n_loc, int n_comp,
+                                       int64_t row0, int64_t n_rows, const int32_t* inc_ptr, const int32_t* inc,
+                                       const int32_t* row_ptr, const int32_t* col_idx, uint8_t* codes,
+                                       int32_t* dev_status, void* stream) {
+  if (n_cells < 0 || n_loc < 1 || n_comp < 1 || n_loc % n_comp || n_loc / n_comp > 16 || row0 < 0 ||
+      n_rows < row0 || (n_rows > row0 && (!cell_dofs || !inc_ptr || !inc || !row_ptr || !col_idx || !codes)))
+    return NFEM_ERR_INVALID_ARG;
+  if (n_rows == row0) return NFEM_OK;
+  node_codes_kernel<<<grid_for(ceil_div(n_rows - row0, n_comp), 256), 256, 0, (cudaStream_t)stream>>>(
+      cell_dofs, n_loc, n_comp, n_rows, row0, inc_ptr, inc, row_ptr, col_idx, codes, dev_status);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+extern "C" int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                                           const double* points, const float* points_split,
+                                           const int32_t* cell_vertices, const void* lambda_, const void* mu,
+                                           const void* force, const double* ref_S, const double* ref_m,
+                                           const int32_t* inc_ptr, const int32_t* inc, const uint8_t* node_codes,
+                                           const int32_t* row_ptr, void* values, void* rhs, int accumulate,
+                                           int32_t* dev_status, void* stream_) {
+  (void)n_cells;
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n_nodes < 0 || row0 < 0) return NFEM_ERR_INVALID_ARG;
+  if (n_nodes == 0) return NFEM_OK;
+  if (!cell_vertices || !lambda_ || !mu || !ref_S || !ref_m || !inc_ptr || !inc || !node_codes || !row_ptr ||
+      !values || !rhs)
+    return NFEM_ERR_INVALID_ARG;
+  if (value_type == NFEM_F64 && !points) return NFEM_ERR_INVALID_ARG;
+  if (value_type == NFEM_F32 && !points_split) return NFEM_ERR_INVALID_ARG;
+  if (reinterpret_cast<uintptr_t>(cell_vertices) & 15) return NFEM_ERR_INVALID_ARG;
+  int rc = upload_tables(ref_S, ref_m, nullptr, stream);
+  if (rc) return rc;
+  ElasParams p;
+  p.n_nodes = n_nodes;
+  p.row0 = row0;
+  p.points = points;
+  p.split = points_split;
+  p.cv = cell_vertices;
+  p.lam = lambda_;
+  p.mu = mu;
+  p.force = force;
+  p.inc_ptr = inc_ptr;
+  p.inc = inc;
+  p.codes = node_codes;
+  p.row_ptr = row_ptr;
+  p.values = values;
+  p.rhs = rhs;
+  p.accumulate = accumulate != 0;
+  p.status = dev_status;
+  if (value_type == NFEM_F64) {
+    elasticity_rows_kernel<double, kElasWarps64>
+        <<<grid_for(ceil_div(n_nodes, kElasWarps64), 1, 8), 32 * kElasWarps64, 0, stream>>>(p);
+  } else {
+    elasticity_rows_kernel<float, kElasWarps32>
+        <<<grid_for(ceil_div(n_nodes, kElasWarps32), 1, 8), 32 * kElasWarps32, 0, stream>>>(p);
+  }
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+extern "C" int nfem_elasticity_p2_penalty(int value_type, int64_t n_facets, const int32_t* facet_dofs,
+                                          const int32_t* facet_vertices, const double* points, double beta,
+                                          const double* ref_S, const double* ref_m, const double* ref_Mf,
+                                          const int32_t* row_ptr, const int32_t* col_idx, void* values,
+                                          int32_t* dev_status, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n_facets < 0) return NFEM_ERR_INVALID_ARG;
+  if (n_facets == 0) return NFEM_OK;
+  if (!facet_dofs || !facet_vertices || !points || !ref_S || !ref_m || !ref_Mf || !row_ptr || !col_idx || !values)
+    return NFEM_ERR_INVALID_ARG;
+  int rc = upload_tables(ref_S, ref_m, ref_Mf, stream);
+  if (rc) return rc;
+  const int g = grid_for(n_facets * 36, 256);
+  if (value_type == NFEM_F64)
+    penalty_kernel<double><<<g, 256, 0, stream>>>(n_facets, facet_dofs, facet_vertices, points, row_ptr, col_idx,
+                                                  beta, (double*)values, dev_status);
+  else
+    penalty_kernel<float><<<g, 256, 0, stream>>>(n_facets, facet_dofs, facet_vertices, points, row_ptr, col_idx,
+                                                 beta, (float*)values, dev_status);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}

@@ -1,87 +1,53 @@
-"""Learned preconditioner: a network that predicts the coarse pressure error.
+"""Learned preconditioner: a network that builds the coarse space of a
+two-level method for mixed Darcy.
 
-No reference counterpart (nfempy has no learned component).  The plain
-method is flexible GMRES with the cell-patch block Jacobi preconditioner
-B.  One-level block Jacobi cannot remove smooth pressure errors, which is
-why its iteration count grows with the mesh.  The learned preconditioner
-adds a coarse correction computed by a 3-layer MLP (width 256, BF16
-weights, FP32 accumulation):
+No reference counterpart (nfempy has no learned component).
 
-    M(v) = B(v) + P (s * f([R v / s, k]))
+The plain method is flexible GMRES with the cell-patch block Jacobi
+preconditioner B.  Block Jacobi is one-level and cannot remove smooth
+pressure errors, so its iteration count grows with the mesh.  The learned
+preconditioner adds a Galerkin coarse correction (solvers.TwoLevelCoarse):
 
-  * aggregates: the cells binned by centroid into an n_c^3 grid;
-  * R v: sum of v's pressure entries over each aggregate, s = ||R v||;
-  * k: mean log-permeability of each aggregate;
-  * f: the network, trained on (residual, error) pairs that the plain
-    solver's own iterates give on sampled permeability fields: for an
-    iterate x_j of a solve with solution x*, r_j = b - A x_j and the target
-    is the aggregate mean of the pressure part of x* - x_j;
-  * P: the predicted aggregate value added to the pressure DoFs of its cells.
+    z = B v;   z += P Ac^-1 P^T (v - A z),   Ac = P^T A P
 
-The forward, backward and Adam kernels are the library's own
-(nfem_mlp_forward / nfem_mlp_backward / nfem_adam_step); the preconditioner
-runs inside the device FGMRES (NFEM_PC_LEARNED).  Plain block-Jacobi FGMRES
-remains the fallback and the FP64 residual judges convergence.
+where P prolongs one value per aggregate of cells to the pressure DoFs of
+its cells (weight 1) and to the fluxes of the faces between aggregates
+(weight w_f times the face's divergence coupling).  The classical
+flux-extension weight is w_f = 1/|a_ff| (a lumped mass).  The network
+predicts w_f from local features of the face:
+  * log K of the two cells of the face;
+  * the mean log K of the two aggregates;
+  * log |a_ff| (normalised over the faces);
+  * whether the face lies on the domain boundary;
+  * the log K jump across the face.
+
+Training data are (residual, correction) pairs that the plain method's own
+solves give on sampled permeability fields.  For the iterates x_j of a
+solve with solution x* and the coarse pressure error e_c(j) (aggregate
+means of x* - x_j), the best weight of face f over the iterates is the
+least-squares fit of the face's flux error against the prolonged coarse
+error.  The network regresses log(w_f |a_ff|) on the face features.
+
+Network: 3 layers, width 256, BF16 weights, FP32 accumulation.  Forward,
+backward and Adam are the library's own kernels (nfem_mlp_forward /
+nfem_mlp_backward / nfem_adam_step), checked against oracle/mlp.py.  Plain
+block-Jacobi FGMRES stays the fallback, and the FP64 residual judges
+convergence.
 """
 import numpy as np
 import torch
 
 from . import _lib
 
-
-class CoarseGrid:
-    """Cells of a space binned into an n_c^3 (or n_c^2) grid of aggregates."""
-
-    def __init__(self, space, n_c):
-        self.space = space
-        self.n_c = int(n_c)
-        dim = space.dim
-        X = space.mesh.points[space.cells_host]
-        cent = X.mean(axis=1)[:, :dim]
-        lo = cent.min(axis=0)
-        hi = cent.max(axis=0)
-        idx = np.floor((cent - lo) / np.maximum(hi - lo, 1e-300) * self.n_c).astype(np.int64)
-        idx = np.clip(idx, 0, self.n_c - 1)
-        agg = np.zeros(space.n_cells, dtype=np.int64)
-        for d in range(dim):
-            agg = agg * self.n_c + idx[:, d]
-        self.n_agg = self.n_c ** dim
-        order = np.argsort(agg, kind="stable")
-        counts = np.bincount(agg, minlength=self.n_agg)
-        if np.any(counts == 0):
-            raise ValueError("empty aggregate: choose a coarser grid")
-        dev = space.device
-        self.cell_agg_host = agg
-        self.counts = counts
-        self.cell_agg = torch.as_tensor(agg.astype(np.int32), device=dev)
-        self.agg_cells = torch.as_tensor(order.astype(np.int32), device=dev)
-        self.agg_ptr = torch.as_tensor(np.concatenate([[0], np.cumsum(counts)]).astype(np.int32), device=dev)
-        self.p_base = space.field_offsets["p"]
-
-    def features(self, kappa):
-        logk = np.log(np.asarray(kappa, dtype=np.float64))
-        f = np.bincount(self.cell_agg_host, weights=logk, minlength=self.n_agg) / self.counts
-        return torch.as_tensor(f.astype(np.float32), device=self.space.device)
-
-    def restrict_sum(self, v):
-        """Aggregate sums of the pressure entries of v [.., n_dof] (torch, any device)."""
-        p = v[..., self.p_base:self.p_base + self.space.n_cells]
-        idx = torch.as_tensor(self.cell_agg_host, device=v.device)
-        out = torch.zeros(v.shape[:-1] + (self.n_agg,), dtype=v.dtype, device=v.device)
-        return out.index_add_(-1, idx, p)
-
-    def restrict_mean(self, v):
-        cnt = torch.as_tensor(self.counts, dtype=v.dtype, device=v.device)
-        return self.restrict_sum(v) / cnt
+N_FEAT = 8
 
 
-class CoarseMLP:
-    """The network f: [2 n_agg] -> [n_agg], dims {2 n_agg, width, width, n_agg}."""
+class MLP:
+    """dims {in, width, width, out}; FP32 master weights + BF16 inference copy."""
 
-    def __init__(self, n_agg, width=256, seed=0, device="cuda"):
-        self.dims = np.array([2 * n_agg, width, width, n_agg], dtype=np.int32)
+    def __init__(self, n_in, width=256, n_out=1, seed=0, device="cuda"):
+        self.dims = np.array([n_in, width, width, n_out], dtype=np.int32)
         self.dims_t = torch.as_tensor(self.dims)
-        self.n_agg = n_agg
         n = _lib.C.c_int64(0)
         _lib.call("nfem_mlp_param_count", self._dims_ptr(), _lib.C.byref(n))
         self.n_params = int(n.value)
@@ -91,38 +57,41 @@ class CoarseMLP:
             parts.append(rng.normal(0.0, np.sqrt(2.0 / a), (b, a)).ravel())
             parts.append(np.zeros(b))
         self.params = torch.as_tensor(np.concatenate(parts).astype(np.float32), device=device)
-        assert self.params.numel() == self.n_params
         self.params_bf16 = torch.empty(self.n_params, dtype=torch.bfloat16, device=device)
         _lib.call("nfem_to_bf16", self.n_params, _lib.ptr(self.params), _lib.ptr(self.params_bf16),
                   _lib.stream_ptr())
         self.m = torch.zeros_like(self.params)
         self.v = torch.zeros_like(self.params)
         self.step_count = 0
+        self._ws = None
 
     def _dims_ptr(self):
         return _lib.C.c_void_p(self.dims_t.data_ptr())
 
-    def forward(self, x, bf16=True):
+    def forward(self, x):
+        x = x.contiguous()
         B = x.shape[0]
         h1 = torch.empty((B, int(self.dims[1])), device=x.device)
         h2 = torch.empty((B, int(self.dims[2])), device=x.device)
         y = torch.empty((B, int(self.dims[3])), device=x.device)
-        if bf16:
-            _lib.call("nfem_mlp_forward", self._dims_ptr(), _lib.NFEM_BF16, _lib.ptr(self.params_bf16),
-                      _lib.ptr(self.params), B, _lib.ptr(x), _lib.ptr(h1), _lib.ptr(h2), _lib.ptr(y),
-                      _lib.stream_ptr())
-        else:
-            _lib.call("nfem_mlp_forward", self._dims_ptr(), _lib.NFEM_F32, _lib.ptr(self.params), None, B,
-                      _lib.ptr(x), _lib.ptr(h1), _lib.ptr(h2), _lib.ptr(y), _lib.stream_ptr())
+        _lib.call("nfem_mlp_forward", self._dims_ptr(), _lib.NFEM_BF16, _lib.ptr(self.params_bf16),
+                  _lib.ptr(self.params), B, _lib.ptr(x), _lib.ptr(h1), _lib.ptr(h2), _lib.ptr(y),
+                  _lib.stream_ptr())
         return h1, h2, y
+
+    def predict(self, x, chunk=1 << 16):
+        out = torch.empty((x.shape[0], int(self.dims[3])), device=x.device)
+        for s in range(0, x.shape[0], chunk):
+            out[s:s + chunk] = self.forward(x[s:s + chunk])[2]
+        return out
 
     def train_step(self, x, t, lr=1e-3):
         """One Adam step on a batch (BF16 forward weights, FP32 master weights)."""
         B = x.shape[0]
-        h1, h2, y = self.forward(x, bf16=True)
+        h1, h2, y = self.forward(x)
         wsb = _lib.C.c_size_t(0)
         _lib.call("nfem_mlp_backward_workspace_bytes", self._dims_ptr(), B, _lib.C.byref(wsb))
-        if getattr(self, "_ws", None) is None or self._ws.numel() < int(wsb.value):
+        if self._ws is None or self._ws.numel() < int(wsb.value):
             self._ws = torch.empty(int(wsb.value), dtype=torch.uint8, device=x.device)
             self._g = torch.empty_like(self.params)
             self._loss = torch.zeros(1, dtype=torch.float64, device=x.device)
@@ -149,43 +118,8 @@ class CoarseMLP:
                   _lib.stream_ptr())
 
 
-def make_pairs(grid, A, b, x_star, snapshots, feat):
-    """Training pairs from a solve: inputs [S, 2 n_agg], targets [S, n_agg] (FP32, device)."""
-    from .solvers import KrylovSolver  # noqa: F401  (same device)
-    S = snapshots.shape[0]
-    xs = snapshots.double()
-    r = b[None, :].expand(S, -1).clone()
-    for s in range(S):
-        r[s] = b - A.spmv(xs[s])
-    e = x_star[None, :] - xs
-    rc = grid.restrict_sum(r)
-    ec = grid.restrict_mean(e)
-    nrm = rc.norm(dim=1, keepdim=True).clamp_min(1e-300)
-    x_in = torch.cat([rc / nrm, feat[None, :].double().expand(S, -1)], dim=1).float()
-    tgt = (ec / nrm).float()
-    keep = (nrm[:, 0] > 0) & torch.isfinite(tgt).all(dim=1)
-    return x_in[keep], tgt[keep]
-
-
-class LearnedPreconditioner:
-    """Binds a trained CoarseMLP and a CoarseGrid to a KrylovSolver (pc="learned")."""
-
-    def __init__(self, grid, model, kappa, out_scale=1.0):
-        self.grid = grid
-        self.model = model
-        self.feat = grid.features(kappa)
-        dims = model.dims
-        self.work = torch.zeros(int(2 * grid.n_agg + dims[1] + dims[2] + 2 * grid.n_agg + 64),
-                                dtype=torch.float32, device=grid.space.device)
-        self.struct = _lib.LearnedCoarse(
-            grid.p_base, grid.n_agg, (_lib.C.c_int32 * 4)(*[int(d) for d in dims]), _lib.ptr(grid.agg_ptr).value,
-            _lib.ptr(grid.agg_cells).value, _lib.ptr(grid.cell_agg).value, _lib.ptr(self.feat).value,
-            _lib.ptr(model.params_bf16).value, _lib.ptr(model.params).value, _lib.ptr(self.work).value,
-            float(out_scale))
-
-
 class DarcyProblem:
-    """A Darcy RT1 x P0 space on cube(n) with reusable matrices (only K changes)."""
+    """Darcy RT1 x P0 on cube(n) with reusable FP64/FP32 matrices (only K changes)."""
 
     def __init__(self, n, device="cuda"):
         from . import meshes, workloads
@@ -212,12 +146,97 @@ class DarcyProblem:
         return -self.res
 
 
-def generate_pairs(problem, grid, seeds, restart=30, max_snapshots=64, max_iters=20000, log=None):
-    """Plain-solver (residual, error) pairs on the permeability fields of `seeds`."""
-    from .solvers import KrylovSolver
-    xs, ts, stats = [], [], []
+class FaceData:
+    """Faces of a TwoLevelCoarse prolongation (flux rows with P entries) and
+    their features for a given permeability field."""
+
+    def __init__(self, tl):
+        A = tl.A
+        sp = A.space
+        dev = A.values.device
+        self.tl = tl
+        n_flux = tl.p_base
+        p_agg = torch.as_tensor(tl.p_agg_host, device=dev)
+        self.rows = torch.nonzero(p_agg[:n_flux, 0] >= 0).flatten()
+        pairs = A.pairs.long()[self.rows]
+        n_loc = sp.n_loc
+        c0 = pairs[:, 0] // n_loc
+        c1 = torch.where(pairs[:, 1] >= 0, pairs[:, 1] // n_loc, c0)
+        self.cells = torch.stack([c0, c1], 1)
+        self.boundary = (pairs[:, 1] < 0).float()
+        cell_agg = torch.as_tensor(tl.cell_agg_host, device=dev)
+        self.aggs = cell_agg[self.cells]
+        self.counts = torch.as_tensor(tl.counts_host, dtype=torch.float64, device=dev)
+
+    def features(self, kappa):
+        tl = self.tl
+        dev = self.rows.device
+        logk = torch.as_tensor(np.log(np.asarray(kappa, dtype=np.float64)), device=dev)
+        agg_logk = torch.zeros(tl.n_agg, dtype=torch.float64, device=dev)
+        agg_logk.index_add_(0, torch.as_tensor(tl.cell_agg_host, device=dev), logk)
+        agg_logk /= self.counts
+        d = tl.A.diagonal()[self.rows].abs().clamp_min(1e-300).log()
+        d = d - d.mean()
+        lk = logk[self.cells]
+        f = torch.stack([lk[:, 0], lk[:, 1], agg_logk[self.aggs[:, 0]], agg_logk[self.aggs[:, 1]], d,
+                         self.boundary.double(), (lk[:, 0] - lk[:, 1]).abs(), torch.ones_like(d)], 1)
+        return f.float().contiguous()
+
+
+def csr_values_at(A, rows, cols):
+    """A[rows[k], cols[k]] (0 where the pattern has no entry)."""
+    rp = A.row_ptr.long()
+    start = rp[rows]
+    length = rp[rows + 1] - start
+    L = int(length.max().item()) if rows.numel() else 0
+    ar = torch.arange(L, device=rows.device)
+    idx = (start[:, None] + ar[None, :]).clamp(max=max(A.nnz - 1, 0))
+    valid = ar[None, :] < length[:, None]
+    hit = valid & (A.col_idx[idx].long() == cols[:, None])
+    return (A.values[idx].double() * hit).sum(1)
+
+
+def face_targets(tl, faces, A, x_star, snapshots, rel_floor=1e-6):
+    """Least-squares flux-extension weights of each face over the iterates,
+    as log(w* |a_ff|); returns (targets, mask of faces with a usable fit)."""
+    pb = tl.p_base
+    n_cells = A.space.n_cells
+    p_agg = torch.as_tensor(tl.p_agg_host, device=x_star.device)[faces.rows]
+    coef = torch.zeros((faces.rows.numel(), 2), dtype=torch.float64, device=x_star.device)
+    for sl in range(2):
+        a = p_agg[:, sl]
+        cell = torch.where(faces.aggs[:, 0] == a, faces.cells[:, 0], faces.cells[:, 1])
+        coef[:, sl] = torch.where(a >= 0, -csr_values_at(A, faces.rows, pb + cell), torch.zeros_like(coef[:, sl]))
+    e = x_star[None, :] - snapshots.double()
+    cell_agg = torch.as_tensor(tl.cell_agg_host, device=e.device)
+    ec = torch.zeros((e.shape[0], tl.n_agg), dtype=torch.float64, device=e.device)
+    ec.index_add_(1, cell_agg, e[:, pb:pb + n_cells])
+    ec /= faces.counts[None, :]
+    g = torch.zeros((e.shape[0], faces.rows.numel()), dtype=torch.float64, device=e.device)
+    for sl in range(2):
+        a = p_agg[:, sl]
+        ok = a >= 0
+        g[:, ok] += coef[ok, sl][None, :] * ec[:, a[ok]]
+    eu = e[:, faces.rows]
+    num = (eu * g).sum(0)
+    den = (g * g).sum(0)
+    wstar = num / den.clamp_min(1e-300)
+    good = (den > rel_floor * den.max()) & (wstar > 0)
+    t = torch.log((wstar * tl.A.diagonal()[faces.rows].abs()).clamp_min(1e-30))
+    return t.float(), good
+
+
+def generate_pairs(problem, coarse_sizes, seeds, restart=30, max_snapshots=64, max_iters=20000,
+                   faces_per_field=4096, log=None):
+    """(features, targets) from plain solves on the permeability fields of `seeds`."""
+    from .solvers import KrylovSolver, TwoLevelCoarse
+    dev = problem.A.values.device
     n = problem.A.n_rows
-    snaps = torch.empty((max_snapshots, n), dtype=torch.float32, device=problem.A.values.device)
+    snaps = torch.empty((max_snapshots, n), dtype=torch.float32, device=dev)
+    tls = [TwoLevelCoarse(problem.A, nc) for nc in coarse_sizes]
+    faces = [FaceData(t) for t in tls]
+    X, T, iters = [], [], []
+    g = torch.Generator(device="cpu").manual_seed(1234)
     for i, seed in enumerate(seeds):
         kappa = problem.field(seed)
         b = problem.assemble(kappa)
@@ -226,18 +245,21 @@ def generate_pairs(problem, grid, seeds, restart=30, max_snapshots=64, max_iters
         S = info.n_snapshots
         if S == 0 or info.status != 0:
             continue
-        feat = grid.features(kappa)
-        xi, ti = make_pairs(grid, problem.A, b, x, snaps[:S], feat)
-        xs.append(xi)
-        ts.append(ti)
-        stats.append(info.inner_iterations)
-        if log and (i % 50 == 0):
-            log(f"field {i}: seed {seed} iters {info.inner_iterations} pairs {xi.shape[0]}")
-    return torch.cat(xs), torch.cat(ts), stats
+        iters.append(info.inner_iterations)
+        for tl, fd in zip(tls, faces):
+            t, good = face_targets(tl, fd, problem.A, x, snaps[:S])
+            feat = fd.features(kappa)
+            idx = torch.nonzero(good).flatten()
+            if idx.numel() > faces_per_field:
+                idx = idx[torch.randperm(idx.numel(), generator=g)[:faces_per_field].to(dev)]
+            X.append(feat[idx])
+            T.append(t[idx, None])
+        if log and i % 50 == 0:
+            log(f"field {i}: seed {seed} plain iters {info.inner_iterations}")
+    return torch.cat(X), torch.cat(T), iters
 
 
-def train(model, X, T, steps=4000, batch=256, lr=1e-3, seed=0, log=None):
-    """Adam on the pairs with the library's kernels; returns the loss history."""
+def train(model, X, T, steps=3000, batch=512, lr=2e-3, seed=0, log=None):
     g = torch.Generator(device="cpu").manual_seed(seed)
     N = X.shape[0]
     hist = []
@@ -245,8 +267,17 @@ def train(model, X, T, steps=4000, batch=256, lr=1e-3, seed=0, log=None):
         idx = torch.randint(0, N, (batch,), generator=g).to(X.device)
         cur_lr = lr * 0.5 * (1 + np.cos(np.pi * s / steps))
         loss = model.train_step(X[idx].contiguous(), T[idx].contiguous(), lr=cur_lr)
-        if s % 200 == 0 or s == steps - 1:
+        if s % 500 == 0 or s == steps - 1:
             hist.append((s, float(loss.item())))
             if log:
                 log(f"step {s} loss {hist[-1][1]:.4e}")
     return hist
+
+
+def learned_weights(tl, model, kappa):
+    """Flux-extension weights predicted by the network for a TwoLevelCoarse."""
+    faces = FaceData(tl)
+    tau = model.predict(faces.features(kappa))[:, 0].double()
+    w = tl.classical_weights().double().clone()
+    w[faces.rows] = torch.exp(tau.clamp(-5.0, 5.0)) / tl.A.diagonal()[faces.rows].abs().clamp_min(1e-300)
+    return w.float()

@@ -167,6 +167,9 @@ class TwoLevelCoarse:
             agg = agg * n_c + idx[:, d]
         self.n_agg = int(n_c ** dim)
         self.cell_agg_host = agg
+        self.counts_host = np.bincount(agg, minlength=self.n_agg)
+        if np.any(self.counts_host == 0):
+            raise ValueError("empty aggregate: choose a coarser grid")
         n = A.n_rows
         pb = sp.field_offsets["p"]
         self.p_base = pb

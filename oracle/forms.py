@@ -200,3 +200,69 @@ def projector_element(fields, X, dim, quad, functions, signs=None):
         j[o:o + m, o:o + m] += jj
         o += m
     return r, j
+
+
+def cosserat_element(X, signs, quad, par, f_u, f_t):
+    """Mixed Cosserat element, 3-D (lce_dual_weak_form.py:410-648,
+    evaluate_form_vectorized).  Fields s (RT1, 3 rows), m (RT1, 3 rows),
+    u (P0^3), t (P0^3); local order s, m, u, t, basis-major / component-minor.
+    par: dict lambda_s, mu_s, kappa_s, lambda_o, mu_o, kappa_o, l (constants
+    on the cell).  f_u, f_t: body force and couple (3-vectors, constant)."""
+    dim = 3
+    pts, wts = quad
+    x, J, det, pinv = evaluate_mapping(dim, pts, X)
+    s_tab = tabulate_oriented("RT", dim, 1, pts, J, det, pinv, signs)
+    p_tab = tabulate_oriented("P", dim, 0, pts, J, det, pinv, discontinuous=True)
+    ns, nm, nu, nt = 12, 12, 3, 3
+    n = ns + nm + nu + nt
+    j = np.zeros((n, n))
+    r = np.zeros(n)
+    Q = len(wts)
+    wdet = det * wts
+    w0 = p_tab[0, :, 0, 0]  # P0 value (1)
+    # rhs_u, rhs_t
+    for c in range(3):
+        r[ns + nm + c] += -np.sum(wdet * w0) * f_u[c]
+        r[ns + nm + nu + c] += -np.sum(wdet * w0) * f_t[c]
+
+    def block(psi, mu_v, kappa_v, lam_v, scale):
+        # psi [Q, 4, 3]
+        out = np.zeros((12, 12))
+        vol = (1.0 / (2.0 * mu_v)) * (lam_v / (2.0 * mu_v + dim * lam_v))
+        for q in range(Q):
+            P = psi[q]
+            inner = np.zeros((12, 12))
+            outer = np.zeros((12, 12))
+            tro = np.outer(P.ravel(), P.ravel())
+            for i in range(4):
+                for jj in range(4):
+                    inner[i * 3:(i + 1) * 3, jj * 3:(jj + 1) * 3] = 0.5 * np.dot(P[i], P[jj]) * np.eye(3)
+                    outer[i * 3:(i + 1) * 3, jj * 3:(jj + 1) * 3] = 0.5 * np.outer(P[jj], P[i])
+            symm = inner + outer
+            skew = inner - outer
+            out += wdet[q] * scale * (symm / (2.0 * mu_v) + skew / (2.0 * kappa_v) - vol * tro)
+        return out
+
+    s_psi = s_tab[0, :, :, 0:dim]
+    j[0:ns, 0:ns] += block(s_psi, par["mu_s"], par["kappa_s"], par["lambda_s"], 1.0)
+    j[ns:ns + nm, ns:ns + nm] += block(s_psi, par["mu_o"], par["kappa_o"], par["lambda_o"], 1.0 / par["l"])
+    # (t,s) / (s,t): asymmetry coupling
+    A = [np.einsum("q,q,qi->i", wdet, w0, s_psi[:, :, k]) for k in range(3)]  # [3][4]
+    tmap = {0: ((2, A[1]), (1, -A[2])), 1: ((0, A[2]), (2, -A[0])), 2: ((1, A[0]), (0, -A[1]))}
+    for c in range(3):
+        tb = ns + nm + nu + c
+        for cs, op in tmap[c]:
+            for i in range(4):
+                j[tb, i * 3 + cs] += -op[i]
+                j[i * 3 + cs, tb] += -op[i]
+    # (u,s) and (t,m): divergence coupling, int w div psi
+    grad = s_tab[1:dim + 1, :, :, 0:dim]  # [d, Q, 4, d]
+    div = np.einsum("kqik->qi", grad)  # reference divergence (det cancels)
+    ub = np.einsum("q,q,qi->i", wts, w0, div)
+    for c in range(3):
+        for i in range(4):
+            j[ns + nm + c, i * 3 + c] += ub[i]
+            j[i * 3 + c, ns + nm + c] += ub[i]
+            j[ns + nm + nu + c, ns + i * 3 + c] += ub[i]
+            j[ns + i * 3 + c, ns + nm + nu + c] += ub[i]
+    return r, j

@@ -1,0 +1,101 @@
+"""Vector P2 elasticity assembly on the GPU vs the FP64 oracle.
+
+Tolerances: FP64 entries within 1e-12 and FP32 within 1e-5, relative to the
+largest entry of each row; residual likewise.  The boundary penalty (beta =
+1e12) is checked separately against an oracle facet mass."""
+import numpy as np
+import pytest
+import torch
+
+import nfempy_gb300 as nf
+from nfempy_gb300.assembly import LEPrimalWeakForm, LEPrimalWeakFormBCDirichlet
+from oracle import assembly, elements, forms, mesh_gen, quadrature, topology
+from tests.gpu_helpers import product_space
+
+pytestmark = pytest.mark.gpu
+FIELD = [("u", "P", 2, 3, False)]
+
+
+def oracle_system(m, lam, mu, f):
+    topo = topology.Topology(m)
+    cd, nd = topology.cell_dofs(topo, [topology.FieldSpec(*FIELD[0])])
+    X = m["points"][topo.cells]
+    quad = quadrature.make_quadrature(3, 5)
+    fq = np.repeat(np.asarray(f)[:, None, :], len(quad[1]), 1)
+    r, j = forms.elasticity_batch(X, 3, quad, lam, mu, fq)
+    A, res = assembly.assemble_csr(cd, j, r, nd)
+    return A, res, cd, topo
+
+
+def row_scaled_err(Ag, Ao):
+    d = (Ag - Ao).tocsr()
+    scale = np.maximum(abs(Ao).max(axis=1).toarray().ravel(), 1e-300)
+    return (abs(d).max(axis=1).toarray().ravel() / scale).max()
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
+@pytest.mark.parametrize("n", [1, 2, 4])
+def test_elasticity_matches_oracle(cuda_lib, dtype, tol, n):
+    m = mesh_gen.cube(n)
+    T = m["blocks"][-1][1].shape[0]
+    rng = np.random.default_rng(n)
+    lam = np.exp(rng.normal(0, 0.5, T))
+    mu = np.exp(rng.normal(0, 0.5, T))
+    f = np.stack([np.ones(T), 2 * np.ones(T), np.linspace(-1, 1, T)], 1)
+    sp = product_space(m, FIELD)
+    A = nf.CSRMatrix(sp, dtype=dtype)
+    res = torch.empty(A.n_rows, dtype=dtype, device="cuda")
+    wf = LEPrimalWeakForm(sp)
+    wf.functions = {"lambda": lam, "mu": mu, "rhs": f}
+    wf.assemble(A, res)
+    torch.cuda.synchronize()
+    A.check_status("elasticity")
+    Ao, ro, cd, topo = oracle_system(m, lam, mu, f)
+    np.testing.assert_array_equal(sp.all_destination_indexes(), cd)
+    Ag = A.to_scipy()
+    np.testing.assert_array_equal(Ag.indptr, Ao.indptr)
+    np.testing.assert_array_equal(Ag.indices, Ao.indices)
+    assert row_scaled_err(Ag, Ao) <= tol
+    rg = res.double().cpu().numpy()
+    assert np.abs(rg - ro).max() <= tol * np.abs(ro).max()
+
+
+def test_elasticity_penalty_matches_oracle(cuda_lib):
+    m = mesh_gen.cube(2)
+    T = m["blocks"][-1][1].shape[0]
+    sp = product_space(m, FIELD)
+    A = nf.CSRMatrix(sp, dtype=torch.float64)
+    res = torch.zeros(A.n_rows, dtype=torch.float64, device="cuda")
+    wf = LEPrimalWeakForm(sp)
+    wf.functions = {"lambda": 1.0, "mu": 1.0, "rhs": None}
+    wf.assemble(A, res)
+    bc = LEPrimalWeakFormBCDirichlet(sp)
+    bc.functions = {"u": None}
+    bc.assemble(A)
+    torch.cuda.synchronize()
+    A.check_status("penalty")
+    Ao, _, cd, topo = oracle_system(m, np.ones(T), np.ones(T), np.zeros((T, 3)))
+    # oracle facet penalty: beta int phi_a phi_b on each boundary triangle
+    fd = bc.facet_dofs()[0].cpu().numpy().astype(np.int64)
+    fv = bc.facet_dofs()[1].cpu().numpy().astype(np.int64)
+    quad = quadrature.make_quadrature(2, 5)
+    phi = elements.create_element("P", 2, 2).tabulate(0, quad[0])[0, :, :, 0]
+    Mref = np.einsum("q,qa,qb->ab", quad[1], phi, phi)
+    P = m["points"]
+    rows, cols, vals = [], [], []
+    for k in range(fd.shape[0]):
+        e1 = P[fv[k, 1]] - P[fv[k, 0]]
+        e2 = P[fv[k, 2]] - P[fv[k, 0]]
+        det = np.linalg.norm(np.cross(e1, e2))
+        for a in range(6):
+            for b in range(6):
+                for i in range(3):
+                    rows.append(fd[k, 3 * a + i]); cols.append(fd[k, 3 * b + i])
+                    vals.append(1e12 * det * Mref[a, b])
+    import scipy.sparse as sps
+    Pen = sps.coo_matrix((vals, (rows, cols)), shape=Ao.shape).tocsr()
+    Ag = A.to_scipy()
+    assert row_scaled_err(Ag, Ao + Pen) <= 1e-12
+    # every boundary facet vertex DoF is penalised
+    bnd_nodes = np.unique(fd)
+    assert np.all(Ag.diagonal()[bnd_nodes] > 1e9)
