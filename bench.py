@@ -110,13 +110,14 @@ def profiled_traffic(name):
     return None
 
 
-def algorithmic_bytes(T, V, nnz, n_dof, vbytes):
+def algorithmic_bytes(T, V, nnz, n_dof, vbytes, verts_per_cell=4):
     """Compulsory bytes of one assembly with `vbytes`-wide values: cell->vertex
-    ids (16 B/cell), point coordinates (24 B/point), kappa and f (one value
-    per cell), RT1 orientation mask (1 B/cell), CSR values written once, the
-    residual written once.  The CSR index structures are setup data and are
-    not counted (they are counted in the measured DRAM traffic)."""
-    return T * 16 + V * 24 + 2 * T * vbytes + T + nnz * vbytes + n_dof * vbytes
+    ids (4 B per vertex of a cell), point coordinates (24 B/point), kappa and
+    f (one value per cell), RT1 orientation mask (1 B/cell), CSR values
+    written once, the residual written once.  The CSR index structures are
+    setup data and are not counted (they are counted in the measured DRAM
+    traffic)."""
+    return T * 4 * verts_per_cell + V * 24 + 2 * T * vbytes + T + nnz * vbytes + n_dof * vbytes
 
 
 # ------------------------------------------------------------------ CPU (oracle) path
@@ -203,6 +204,184 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+
+def _timed_solve(ksp, b, args, stream):
+    import torch
+    ev0, ev1, ev2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    ev0.record(stream)
+    ksp.setup()
+    ev1.record(stream)
+    x, info = ksp.solve(b, rtol=1e-8, inner_rtol=1e-4, max_inner=args.max_iters, raise_on_failure=False)
+    ev2.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    relres = float(ksp.residual(x, b).norm() / b.norm())
+    return {"setup_ms": ev0.elapsed_time(ev1), "solve_ms": ev1.elapsed_time(ev2),
+            "time_to_solve_ms": ev0.elapsed_time(ev2), "wall_s": wall,
+            "inner_iterations": info.inner_iterations, "outer_iterations": info.outer_iterations,
+            "final_relres_fp64": relres, "status": info.status,
+            "ms_per_inner_iteration": ev1.elapsed_time(ev2) / max(1, info.inner_iterations)}
+
+
+def solve_bench(args, A, wf, coefs, res, stream):
+    """Time to ||b - A x|| / ||b|| <= 1e-8 (FP64) on the benchmark system:
+    plain block-Jacobi FGMRES, the two-level preconditioner with classical
+    flux weights, and with the network's weights (the learned preconditioner)."""
+    import torch
+    from nfempy_gb300.solvers import KrylovSolver, TwoLevelCoarse
+    A64 = A.with_dtype(torch.float64)
+    res64 = torch.empty(A.n_rows, dtype=torch.float64, device="cuda")
+    wf.assemble(A, res, coefficients=coefs)
+    wf.assemble(A64, res64, coefficients=wf.coefficients(torch.float64))
+    b = -res64
+    out = {"rtol": 1e-8, "krylov": f"FGMRES({args.restart}) FP32 inside FP64 iterative refinement",
+           "field": "log K GRF, correlation length 0.05, sigma 2.0, seed 20261208 (not a training seed)"}
+    ksp = KrylovSolver(A64, pc="cell_block", A32_values=A.values, restart=args.restart)
+    out["plain_block_jacobi"] = _timed_solve(ksp, b, args, stream)
+    nc = N_SIDE // 4
+    t0 = time.perf_counter()
+    tl = TwoLevelCoarse(A64, nc)
+    t_struct = time.perf_counter() - t0
+    ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.restart, two_level=tl)
+    out["two_level_classical"] = _timed_solve(ksp, b, args, stream)
+    out["two_level_classical"]["host_structure_s"] = t_struct
+    out["two_level_classical"]["aggregates"] = tl.n_agg
+    try:
+        from nfempy_gb300 import learned, train_learned
+        model, ck = train_learned.load()
+        alpha = ck["alphas_by_side_fraction"][4]["alpha"]
+        kappa = wf.functions["kappa"]
+        tl2 = TwoLevelCoarse(A64, nc)
+        tl2.set_weights(learned.learned_weights(tl2, model, kappa, alpha))
+        ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.restart, two_level=tl2)
+        out["learned"] = _timed_solve(ksp, b, args, stream)
+        out["learned"]["alpha"] = alpha
+        out["learned"]["training"] = {k: ck["record"][k] for k in ("n", "fields", "solves_used", "pairs",
+                                                                   "data_seconds", "train_seconds")}
+        plain = out["plain_block_jacobi"]["time_to_solve_ms"]
+        out["learned"]["speedup_vs_plain"] = plain / out["learned"]["time_to_solve_ms"]
+    except (OSError, FileNotFoundError, KeyError) as e:
+        out["learned"] = {"unavailable": f"no trained network checkpoint ({type(e).__name__})"}
+    out["two_level_classical"]["speedup_vs_plain"] = (out["plain_block_jacobi"]["time_to_solve_ms"]
+                                                      / out["two_level_classical"]["time_to_solve_ms"])
+    return out
+
+
+def _time_assembly(fn, steps, warmup):
+    import torch
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        flush.zero_()
+        fn()
+    ts = []
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        ts.append((e0, e1))
+    torch.cuda.synchronize()
+    import statistics
+    return statistics.mean(a.elapsed_time(b) for a, b in ts)
+
+
+def elasticity_bench(args):
+    """Vector P2 elasticity assembly: 40^3 x 6 tets, per-cell lognormal
+    lambda, mu (mean-log 0, sigma 0.5), body force (1, 1, 1), FP32."""
+    import numpy as np
+    import torch
+    import nfempy_gb300 as nf
+    from nfempy_gb300 import meshes
+    from nfempy_gb300.assembly import LEPrimalWeakForm
+    n = 40
+    m = meshes.cube(n)
+    mesh = nf.Mesh(3, data=m)
+    sp = nf.ProductSpace({"u": (3, 3, "Lagrange", 2, mesh)})
+    sp.build_structures({"u": [1]}, {})
+    A = nf.CSRMatrix(sp, dtype=torch.float32)
+    res = torch.empty(A.n_rows, dtype=torch.float32, device="cuda")
+    rng = np.random.default_rng(20261203 + 1)
+    T = sp.n_cells
+    wf = LEPrimalWeakForm(sp)
+    wf.functions = {"lambda": np.exp(rng.normal(0, 0.5, T)), "mu": np.exp(rng.normal(0, 0.5, T)),
+                    "rhs": np.array([1.0, 1.0, 1.0])}
+    coefs = wf.coefficients(torch.float32)
+    ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
+    A.check_status("elasticity bench")
+    V = m["points"].shape[0]
+    alg = T * 16 + V * 24 + T * 4 * 2 + T * 12 + A.nnz * 4 + A.n_rows * 4
+    peak, kind = measured_peaks()
+    ach = alg / (ms * 1e-3) / 1e9
+    return {"metric": "DoF/s assembled", "value": sp.n_dof / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
+            "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz, "kernel": "elasticity_rows_kernel",
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "algorithmic_bytes": alg, "peak_source": kind}}
+
+
+def cosserat_bench(args):
+    """Mixed Cosserat assembly: 24^3 x 6 tets, RT1^3 x RT1^3 x P0^3 x P0^3,
+    Lame 1/1, Cosserat coupling 0.5, FP32."""
+    import torch
+    import nfempy_gb300 as nf
+    from nfempy_gb300 import meshes
+    from nfempy_gb300.assembly import LCEDualWeakForm
+    n = 24
+    m = meshes.cube(n)
+    mesh = nf.Mesh(3, data=m)
+    sp = nf.ProductSpace({"s": (3, 3, "RT", 1, mesh), "m": (3, 3, "RT", 1, mesh), "u": (3, 3, "Lagrange", 0, mesh),
+                          "t": (3, 3, "Lagrange", 0, mesh)})
+    sp.make_subspaces_discontinuous({"u": True, "t": True})
+    sp.build_structures({k: [1] for k in "smut"}, {})
+    A = nf.CSRMatrix(sp, dtype=torch.float32)
+    res = torch.empty(A.n_rows, dtype=torch.float32, device="cuda")
+    wf = LCEDualWeakForm(sp)
+    wf.functions = dict(lambda_s=1.0, mu_s=1.0, kappa_s=0.5, lambda_o=1.0, mu_o=1.0, kappa_o=0.5, l=1.0,
+                        rhs=[1.0, 1.0, 1.0, 0.0, 0.0, 0.0])
+    coefs = wf.coefficients(torch.float32)
+    ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
+    A.check_status("cosserat bench")
+    T = sp.n_cells
+    V = m["points"].shape[0]
+    alg = T * 16 + V * 24 + T + T * 24 + A.nnz * 4 + A.n_rows * 4
+    peak, kind = measured_peaks()
+    ach = alg / (ms * 1e-3) / 1e9
+    return {"metric": "DoF/s assembled", "value": sp.n_dof / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
+            "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz, "kernel": "cosserat_rows_kernel",
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "algorithmic_bytes": alg, "peak_source": kind}}
+
+
+def batch2d_bench(args):
+    """512 independent 2-D mixed Darcy problems (n_i ~ U{8..128} squares per
+    side, 2 n_i^2 triangles, log K_i GRF with correlation length 0.1 and
+    sigma 1, f = 1) assembled in one launch over their disjoint union, FP32."""
+    import torch
+    import nfempy_gb300 as nf
+    from nfempy_gb300 import workloads as wl
+    m, sp, kappa, f, sides = wl.darcy2d_batch(512)
+    A = nf.CSRMatrix(sp, dtype=torch.float32)
+    res = torch.empty(A.n_rows, dtype=torch.float32, device="cuda")
+    wf = nf.LaplaceDualWeakForm(sp)
+    wf.functions = {"kappa": kappa, "rhs": f}
+    coefs = wf.coefficients(torch.float32)
+    ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
+    A.check_status("batch2d bench")
+    T = sp.n_cells
+    V = m["points"].shape[0]
+    alg = algorithmic_bytes(T, V, A.nnz, sp.n_dof, 4, verts_per_cell=3)
+    peak, kind = measured_peaks()
+    ach = alg / (ms * 1e-3) / 1e9
+    return {"metric": "DoF/s assembled", "value": sp.n_dof / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
+            "problems": len(sides), "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz, "kernel": "darcy_rows_kernel",
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "algorithmic_bytes": alg, "peak_source": kind}}
 
 
 # ------------------------------------------------------------------ GPU path
@@ -305,34 +484,12 @@ def run_ours(args):
     # ---------------- time to solve: FP64 system, FP32 inner iterations
     solve = None
     if not args.no_solve:
-        from nfempy_gb300.solvers import KrylovSolver
-        A64 = A.with_dtype(torch.float64)
-        res64 = torch.empty(A.n_rows, dtype=torch.float64, device="cuda")
-        coefs64 = wf.coefficients(torch.float64)
-        wf.assemble(A, res, coefficients=coefs)
-        wf.assemble(A64, res64, coefficients=coefs64)
-        b = -res64
-        torch.cuda.synchronize()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev2 = torch.cuda.Event(enable_timing=True)
-        t_wall = time.perf_counter()
-        ev0.record(stream)
-        ksp = KrylovSolver(A64, pc="cell_block", A32_values=A.values, restart=args.restart)
-        ksp.setup()
-        ev1.record(stream)
-        x, info = ksp.solve(b, rtol=1e-8, inner_rtol=1e-4, max_inner=args.max_iters, raise_on_failure=False)
-        ev2.record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t_wall
-        r = ksp.residual(x, b)
-        relres = float(r.norm() / b.norm())
-        solve = {"rtol": 1e-8, "precond": "cell-patch block Jacobi (weighted additive Schwarz)",
-                 "krylov": f"FGMRES({args.restart}) FP32 inside FP64 iterative refinement",
-                 "setup_ms": ev0.elapsed_time(ev1), "solve_ms": ev1.elapsed_time(ev2), "wall_s": wall,
-                 "inner_iterations": info.inner_iterations, "outer_iterations": info.outer_iterations,
-                 "final_relres_fp64": relres, "status": info.status,
-                 "ms_per_inner_iteration": ev1.elapsed_time(ev2) / max(1, info.inner_iterations)}
+        solve = solve_bench(args, A, wf, coefs, res, stream)
+    workloads = {}
+    if not args.no_extra:
+        workloads["elasticity_p2_cube40x6"] = elasticity_bench(args)
+        workloads["cosserat_cube24x6"] = cosserat_bench(args)
+        workloads["darcy2d_batch512"] = batch2d_bench(args)
 
     if rank != 0:
         return
@@ -365,6 +522,7 @@ def run_ours(args):
         "e2e": {"value": world * n_dof / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "solve": solve,
+        "workloads": workloads,
         "gpu_launches": args.steps,
         "clocks": clk,
     }
@@ -383,11 +541,18 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=3000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--restart", type=int, default=30)
     ap.add_argument("--max-iters", type=int, default=20000)
+    ap.add_argument("--only", choices=["elasticity", "cosserat", "batch2d"], default=None,
+                    help="time one secondary assembly workload alone and print its record (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.only:
+        fn = {"elasticity": elasticity_bench, "cosserat": cosserat_bench, "batch2d": batch2d_bench}[args.only]
+        print(json.dumps({"workload": args.only, **fn(args)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

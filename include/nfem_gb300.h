@@ -166,8 +166,28 @@ int nfem_pattern_pairs(const int32_t* inc_ptr, const int32_t* inc, const uint32_
                        int64_t n_rows, int32_t* pairs, uint32_t* pair_codes,
                        int32_t* dev_status, void* stream);
 
-/* Splits FP64 points into float hi/lo pairs [n_points, 6] = (hi xyz, lo xyz)
- * so FP32 kernels form cell edge vectors without FP64 arithmetic. */
+/* Cells per entry of the cell-chunk row table of the mixed Darcy layout. */
+#define NFEM_DARCY_CHUNK_CELLS 256
+
+/* Cell-chunk row table for nfem_darcy_rt1p0_assemble: chunk_rows
+ * [ceil(n_cells / NFEM_DARCY_CHUNK_CELLS) + 1], entry k = the first flux row
+ * whose first incidence lies in a cell >= k * NFEM_DARCY_CHUNK_CELLS.  Needs
+ * the first-appearance layout of a mixed RT1 x P0 space: flux rows
+ * [0, p_base), then one pressure row per cell in cell order
+ * (n_rows = p_base + n_cells); anything else returns NFEM_ERR_UNSUPPORTED
+ * (directly or through dev_status). */
+int nfem_pattern_darcy_chunks(const int32_t* pairs, int64_t n_rows, int n_loc, int64_t p_base,
+                              int64_t n_cells, int32_t* chunk_rows, int32_t* dev_status,
+                              void* stream);
+
+/* Packs FP64 points into 16-byte FP32 records so FP32 kernels form cell edge
+ * vectors with one load per vertex and without FP64 arithmetic.
+ * points_split: [1 + n_points, 4] floats, 16-byte aligned.  Record 0 =
+ * (lo_scale, cx, cy, cz); record v + 1 = (hx, hy, hz, q): h = float(x - c),
+ * q = three signed 10-bit fields (bits 0-9, 10-19, 20-29) with
+ * x - c - h ~= q * lo_scale.  c is the bounding-box centre, lo_scale about
+ * 2^-33 x the half-extent: edge vectors carry an absolute error below
+ * lo_scale, a relative error of about 1e-10 x (cells across the mesh). */
 int nfem_points_split(const double* points, int64_t n_points, float* points_split,
                       void* stream);
 
@@ -191,7 +211,12 @@ int nfem_points_split(const double* points, int64_t n_points, float* points_spli
  * nfem_pattern_pairs with cell_dofs = [flux_dofs | p_base + c].  accumulate == 0 overwrites
  * values/rhs (the first form of an assembly pass, like a zeroed PETSc Mat
  * and residual); accumulate != 0 adds to them (setValue(addv=True)).  Each CSR value and residual entry is written once
- * (row-owner gather; no atomics, deterministic). */
+ * (no atomics, deterministic).  chunk_rows (optional, from
+ * nfem_pattern_darcy_chunks with the same p_base) selects the cell-chunk
+ * kernel: each block evaluates the element matrices of a run of cells once
+ * into shared memory and writes the rows whose first incidence lies there;
+ * NULL selects the row-owner kernel, which evaluates every incidence of a row
+ * on its own.  Both give the same values. */
 int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t n_rows,
                               const double* points, const float* points_split,
                               const int32_t* cell_vertices, const int32_t* flux_dofs,
@@ -199,9 +224,34 @@ int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t 
                               const void* kappa, const void* source, int source_mode,
                               const double* qweights, int n_qp,
                               const int32_t* row_pairs, const uint32_t* pair_codes,
-                              const int32_t* row_ptr,
+                              const int32_t* row_ptr, const int32_t* chunk_rows,
                               void* values, void* rhs, int accumulate,
                               int32_t* dev_status, void* stream);
+
+/* Replaces LaplaceDualWeakFormBCDirichlet.evaluate_form
+ * (src/weak_forms/laplace_dual_weak_form.py:90-154) with its scatter: adds
+ * int_F p_D (psi_f . n) to the residual entry of each boundary facet's flux
+ * DoF.  facet_occ [n_facets] = cell * (dim + 1) + local face of the facet's
+ * cell; pd_q [n_facets, n_qp] = p_D at the facet quadrature points (rule of
+ * order 3 on the facet, n_qp <= 4, weights qweights on the host).  Each
+ * boundary facet's DoF belongs to one facet: plain additions, deterministic. */
+int nfem_darcy_rt1_dirichlet(int dim, int value_type, int64_t n_facets, const int32_t* facet_occ,
+                             const uint8_t* sign_mask, const int32_t* cell_dofs, int ld,
+                             const void* pd_q, const double* qweights, int n_qp, void* rhs,
+                             void* stream);
+
+/* Replaces l2_error (src/postprocess/l2_error_post_processor.py:7-63) for a
+ * mixed Darcy RT1 x P0 solution alpha (FP64): errors[0] = ||u - u_h||_L2,
+ * errors[1] = ||p - p_h||_L2 (device doubles), with the exact fields sampled
+ * at the quadrature points, u_exact_q [n_cells, n_qp, dim], p_exact_q
+ * [n_cells, n_qp]; qpoints [n_qp, dim] / qweights [n_qp] on the host.
+ * workspace >= 2 * 304 doubles.  FP64 throughout, fixed-order reduction. */
+int nfem_darcy_l2_error(int dim, int64_t n_cells, const double* points,
+                        const int32_t* cell_vertices, const uint8_t* sign_mask,
+                        const int32_t* cell_dofs, int ld, const double* alpha,
+                        const double* u_exact_q, const double* p_exact_q, const double* qpoints,
+                        const double* qweights, int n_qp, double* errors, void* workspace,
+                        size_t workspace_bytes, void* stream);
 
 /* ------------------------- vector P2 linear elasticity (a12, a13, a15)
  * Replaces LEPrimalWeakForm.evaluate_form

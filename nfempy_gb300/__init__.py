@@ -5,8 +5,11 @@ C-ABI CUDA library (libnfem_gb300.so, include/nfem_gb300.h) compiled for
 sm_103a.  Build with `nfempy_gb300.build.build()`.
 """
 from . import _lib  # noqa: F401
-from .assembly import CSRMatrix, LaplaceDualWeakForm, SequentialAssembler, WeakForm  # noqa: F401
+from .assembly import (CSRMatrix, LaplaceDualWeakForm, LaplaceDualWeakFormBCDirichlet,  # noqa: F401
+                       LCEDualWeakForm, LEPrimalWeakForm, LEPrimalWeakFormBCDirichlet, SequentialAssembler,
+                       WeakForm, l2_error)
 from .spaces import DiscreteSpace, Mesh, ProductSpace  # noqa: F401
 
-__all__ = ["CSRMatrix", "LaplaceDualWeakForm", "SequentialAssembler", "WeakForm", "DiscreteSpace", "Mesh",
-           "ProductSpace"]
+__all__ = ["CSRMatrix", "LaplaceDualWeakForm", "LaplaceDualWeakFormBCDirichlet", "LCEDualWeakForm",
+           "LEPrimalWeakForm", "LEPrimalWeakFormBCDirichlet", "SequentialAssembler", "WeakForm", "l2_error",
+           "DiscreteSpace", "Mesh", "ProductSpace"]

@@ -10,13 +10,14 @@ import os
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libnfem_gb300.so")
+LIB_PATH = os.environ.get("NFEM_GB300_LIB", os.path.join(HERE, "libnfem_gb300.so"))
 
 NFEM_OK = 0
 NFEM_F64 = 0
 NFEM_F32 = 1
 NFEM_BF16 = 2
 COEF_NONE, COEF_CELL, COEF_QPOINT = 0, 1, 2
+DARCY_CHUNK_CELLS = 256  # NFEM_DARCY_CHUNK_CELLS
 
 STATUS_NAMES = {
     0: "NFEM_OK", 1: "NFEM_ERR_INVALID_ARG", 2: "NFEM_ERR_CUDA", 3: "NFEM_ERR_WORKSPACE",
@@ -91,7 +92,8 @@ _SIGS = {
     "nfem_points_split": ([_P, _I64, _P, _P], _I),
     "nfem_pattern_pairs": ([_P, _P, _P, _I64, _P, _P, _P, _P], _I),
     "nfem_darcy_rt1p0_assemble": ([_I, _I, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P, _P, _I,
-                                   _P, _I, _P, _P, _P, _P, _P, _I, _P, _P], _I),
+                                   _P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P], _I),
+    "nfem_pattern_darcy_chunks": ([_P, _I64, _I, _I64, _I64, _P, _P, _P], _I),
     "nfem_spmv": ([_I, _I64, _P, _P, _P, _P, _P, _P], _I),
     "nfem_residual_f64": ([_I64, _P, _P, _P, _P, _P, _P, _P], _I),
     "nfem_precond_setup": ([C.POINTER(Precond), C.POINTER(Csr), _P, _P], _I),
@@ -113,6 +115,9 @@ _SIGS = {
     "nfem_cosserat_assemble": ([_I, _I64, _I64, _I64, _P, _P, _P, _P, C.POINTER(C.c_double), _P,
                                 C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), _P, _P, _P,
                                 _P, _P, _P, _I, _P, _P], _I),
+    "nfem_darcy_rt1_dirichlet": ([_I, _I, _I64, _P, _P, _P, _I, _P, C.POINTER(C.c_double), _I, _P, _P], _I),
+    "nfem_darcy_l2_error": ([_I, _I64, _P, _P, _P, _P, _I, _P, _P, _P, C.POINTER(C.c_double),
+                             C.POINTER(C.c_double), _I, _P, _P, _SZ, _P], _I),
 }
 
 _lib = None

@@ -75,6 +75,17 @@ class CSRMatrix:
             self.pair_codes = torch.empty((self.n_rows, 2), dtype=torch.int32, device=dev)
             _lib.call("nfem_pattern_pairs", _lib.ptr(self.inc_ptr), _lib.ptr(self.inc), _lib.ptr(self.codes),
                       self.n_rows, _lib.ptr(self.pairs), _lib.ptr(self.pair_codes), _lib.ptr(self.status), st)
+        self.chunk_rows = None
+        if self.pairs is not None and _mixed_rt1_p0(space):
+            # cell-chunk row table; a layout it does not cover keeps the row-owner kernel
+            n_chunks = -(-T // _lib.DARCY_CHUNK_CELLS)
+            cr = torch.empty(n_chunks + 1, dtype=torch.int32, device=dev)
+            cst = torch.zeros(1, dtype=torch.int32, device=dev)
+            rc = _lib.lib().nfem_pattern_darcy_chunks(_lib.ptr(self.pairs), self.n_rows, n_loc,
+                                                      space.field_offsets[space.names[1]], T, _lib.ptr(cr),
+                                                      _lib.ptr(cst), st)
+            if rc == _lib.NFEM_OK and int(cst.item()) == 0:
+                self.chunk_rows = cr
         self.values = torch.zeros(max(self.nnz, 1), dtype=dtype, device=dev)
         self.fresh = True
         self.check_status("pattern")
@@ -135,6 +146,15 @@ class CSRMatrix:
                              shape=(self.n_rows, self.n_rows))
 
 
+def _mixed_rt1_p0(space):
+    """True for a two-field RT1 x discontinuous P0 product space (mixed Darcy)."""
+    if len(space.names) != 2:
+        return False
+    u, p = (space.discrete_spaces[n] for n in space.names)
+    return (u.family == "RT" and u.k_order == 1 and u.n_comp == 1 and p.family == "Lagrange" and p.k_order == 0
+            and p.n_comp == 1 and p.discontinuous)
+
+
 def max_incidence(inc_ptr):
     return int((inc_ptr[1:] - inc_ptr[:-1]).max().item()) if inc_ptr.numel() > 1 else 0
 
@@ -180,7 +200,12 @@ class LaplaceDualWeakForm(WeakForm):
                "rhs"   - None, scalar, per-cell array [T], per-quadrature-point
                          array [T, Q], or f(x, y, z) -> [1, N] (sampled at the
                          quadrature points).
+
+    use_chunks: the cell-chunk kernel when the matrix has a chunk table (True),
+    else the row-owner kernel; both write the same values.
     """
+
+    use_chunks = True
 
     def _check_space(self):
         sp = self.space
@@ -251,12 +276,89 @@ class LaplaceDualWeakForm(WeakForm):
                   _lib.ptr(sp.points), _lib.ptr(sp.points_split), _lib.ptr(sp.cells), None,
                   sp.field_offsets["p"], _lib.ptr(sp.rt_sign_mask), _lib.ptr(kt), _lib.ptr(st), mode,
                   _lib.C.cast(qw, _lib.C.c_void_p), len(wts), _lib.ptr(jacobian.pairs),
-                  _lib.ptr(jacobian.pair_codes), _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate),
+                  _lib.ptr(jacobian.pair_codes), _lib.ptr(jacobian.row_ptr),
+                  _lib.ptr(jacobian.chunk_rows if self.use_chunks else None), _lib.ptr(jacobian.values),
+                  _lib.ptr(residual), int(accumulate),
                   _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
 
     def evaluate_form(self, element_index, alpha):
         raise NotImplementedError(
             "per-cell evaluation is not offered on the device; assemble with SequentialAssembler")
+
+
+class LaplaceDualWeakFormBCDirichlet(WeakForm):
+    """Pressure Dirichlet data on boundary facets for mixed Darcy RT1 x P0
+    (src/weak_forms/laplace_dual_weak_form.py:90-154): adds int_F p_D (psi . n)
+    to the flux DoF of each boundary facet whose physical tag is in
+    `bc_physical_tags` (default: the space's b_physical_tags["u"], or every
+    tagged facet).  functions: {"p": f(x, y, z) -> [1, N]} or a scalar.
+    Only the residual changes (the form's Jacobian is zero)."""
+
+    def __init__(self, space, bc_physical_tags=None):
+        super().__init__(space)
+        self.bc_physical_tags = bc_physical_tags
+
+    def facets(self):
+        if "facets" in self._cache:
+            return self._cache["facets"]
+        sp = self.space
+        dim = sp.dim
+        tags = self.bc_physical_tags
+        if tags is None:
+            tags = sp.b_physical_tags.get("u") or None
+        fl = sp.facet_flags.cpu().numpy()
+        occ = np.flatnonzero((fl.ravel() & 2) != 0)
+        c = occ // (dim + 1)
+        i = occ % (dim + 1)
+        from .elements import P2_EDGES
+        sub = np.array(P2_EDGES[2] if dim == 2 else ((1, 2, 3), (0, 2, 3), (0, 1, 3), (0, 1, 2)))
+        verts = np.sort(sp.cells_host[c[:, None], sub[i]], axis=1)
+        V = sp.mesh.points.shape[0]
+        key = np.zeros(len(occ), dtype=np.int64)
+        for k in range(dim):
+            key = key * V + verts[:, k]
+        from .meshes import BLOCK_DIM
+        fconn, ftag = [], []
+        for typ, conn, phys in sp.mesh.data["blocks"]:
+            if BLOCK_DIM[typ] == dim - 1:
+                fconn.append(np.asarray(conn, dtype=np.int64))
+                ftag.append(np.asarray(phys))
+        fconn = np.concatenate(fconn)
+        ftag = np.concatenate(ftag)
+        fkey = np.zeros(len(fconn), dtype=np.int64)
+        fs = np.sort(fconn, axis=1)
+        for k in range(dim):
+            fkey = fkey * V + fs[:, k]
+        order = np.argsort(fkey, kind="stable")
+        pos = order[np.searchsorted(fkey[order], key)]
+        keep = np.ones(len(occ), dtype=bool) if tags is None else np.isin(ftag[pos], np.asarray(tags))
+        out = (occ[keep].astype(np.int32), fconn[pos[keep]])
+        self._cache["facets"] = out
+        return out
+
+    def assemble(self, jacobian, residual, accumulate=True, stream=None):
+        sp = self.space
+        dim = sp.dim
+        occ, fverts = self.facets()
+        dtype = residual.dtype
+        vt = _lib.NFEM_F64 if dtype == torch.float64 else _lib.NFEM_F32
+        pts, wts = sp.bc_quadrature[dim - 1]
+        lam = lagrange_p1_values(dim - 1, pts)
+        xq = np.einsum("qv,fvg->fqg", lam, sp.mesh.points[fverts])
+        p = self.functions["p"]
+        if callable(p):
+            pv = np.asarray(p(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).reshape(-1, *xq.shape[:2])[0]
+        else:
+            pv = np.full(xq.shape[:2], float(p))
+        pd = torch.as_tensor(np.ascontiguousarray(pv), dtype=dtype, device=sp.device)
+        occ_t = torch.as_tensor(occ, device=sp.device)
+        qw = np.ascontiguousarray(wts, dtype=np.float64)
+        _lib.call("nfem_darcy_rt1_dirichlet", dim, vt, len(occ), _lib.ptr(occ_t), _lib.ptr(sp.rt_sign_mask),
+                  _lib.ptr(sp.cell_dofs), sp.n_loc, _lib.ptr(pd), qw.ctypes.data_as(_lib.C.POINTER(_lib.C.c_double)),
+                  len(wts), _lib.ptr(residual), _lib.stream_ptr(stream))
+        if not hasattr(self, "_keep"):
+            self._keep = []
+        self._keep = [pd, occ_t]
 
 
 class SequentialAssembler:
@@ -277,7 +379,7 @@ class SequentialAssembler:
 
     @property
     def form_type_to_callable_map(self):
-        return {"form": self._scatter_form}
+        return {"form": self._scatter_form, "bc_form": self._scatter_bc_form}
 
     @property
     def form_to_input_list(self):
@@ -297,6 +399,11 @@ class SequentialAssembler:
             raise NotImplementedError("linear forms are assembled at alpha = 0 (one Newton step)")
         form.assemble(self.jacobian, residual, accumulate=accumulate)
 
+    def _scatter_bc_form(self, form, sequence, alpha, residual, accumulate):
+        if not accumulate:
+            raise NotImplementedError("a boundary form adds to a pass that starts with a cell form")
+        form.assemble(self.jacobian, residual, accumulate=True)
+
     def scatter_forms(self, measure_time_q=False):
         host_res = None
         residual = self.residual
@@ -313,7 +420,7 @@ class SequentialAssembler:
             if form_type not in self.form_type_to_callable_map:
                 raise NotImplementedError(f"form type {form_type}")
             _, sequence, form, alpha = input_list[:4]
-            self._scatter_form(form, sequence, alpha, residual, accumulate or not first)
+            self.form_type_to_callable_map[form_type](form, sequence, alpha, residual, accumulate or not first)
             first = False
             if measure_time_q:
                 torch.cuda.synchronize()
@@ -514,3 +621,30 @@ class LCEDualWeakForm(WeakForm):
                   _lib.ptr(jacobian.inc_ptr), _lib.ptr(jacobian.inc), _lib.ptr(jacobian.node_codes),
                   _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate),
                   _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+
+
+def l2_error(dim, space, functions, alpha, stream=None):
+    """[||u - u_h||, ||p - p_h||] of a mixed Darcy RT1 x P0 solution, FP64 on the
+    device (src/postprocess/l2_error_post_processor.py:7-63).  functions:
+    {"u": f(x, y, z) -> [dim, N], "p": f(x, y, z) -> [N] or [1, N]}."""
+    sp = space
+    pts, wts = sp.quadrature[dim]
+    lam = lagrange_p1_values(dim, pts)
+    xq = np.einsum("qv,tvg->tqg", lam, sp.mesh.points[sp.cells_host])
+    ue = np.asarray(functions["u"](xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64)[:dim]
+    ue = np.ascontiguousarray(np.moveaxis(ue, 0, -1))  # [T, Q, dim]
+    pe = np.asarray(functions["p"](xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).reshape(xq.shape[:2])
+    dev = sp.device
+    ue_t = torch.as_tensor(ue, device=dev)
+    pe_t = torch.as_tensor(np.ascontiguousarray(pe), device=dev)
+    a = torch.as_tensor(alpha, dtype=torch.float64, device=dev).contiguous()
+    ws = torch.empty(2 * 304, dtype=torch.float64, device=dev)
+    out = torch.empty(2, dtype=torch.float64, device=dev)
+    qp = np.ascontiguousarray(pts, dtype=np.float64)
+    qw = np.ascontiguousarray(wts, dtype=np.float64)
+    dp = _lib.C.POINTER(_lib.C.c_double)
+    _lib.call("nfem_darcy_l2_error", dim, sp.n_cells, _lib.ptr(sp.points), _lib.ptr(sp.cells),
+              _lib.ptr(sp.rt_sign_mask), _lib.ptr(sp.cell_dofs), sp.n_loc, _lib.ptr(a), _lib.ptr(ue_t),
+              _lib.ptr(pe_t), qp.ctypes.data_as(dp), qw.ctypes.data_as(dp), len(wts), _lib.ptr(out), _lib.ptr(ws),
+              ws.numel() * 8, _lib.stream_ptr(stream))
+    return out.cpu().numpy().tolist()

@@ -35,8 +35,8 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _compile(src, extra):
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+def _compile(src, extra, bdir):
+    obj = os.path.join(bdir, os.path.basename(src)[:-3] + ".o")
     cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -44,24 +44,26 @@ def _compile(src, extra):
     return obj, r.stderr
 
 
-def build(verbose=False, extra=()):
+def build(verbose=False, extra=(), lib_path=None, build_dir=None):
     """Compile every csrc/*.cu for sm_103a and link libnfem_gb300.so."""
-    os.makedirs(BUILD, exist_ok=True)
+    lib_out = lib_path or LIB
+    bdir = build_dir or BUILD
+    os.makedirs(bdir, exist_ok=True)
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        results = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
+        results = list(ex.map(lambda s: _compile(s, list(extra), bdir), srcs))
     objs = [o for o, _ in results]
     if verbose:
         for _, err in results:
             if err.strip():
                 print(err)
-    tmp = LIB + ".tmp"
+    tmp = lib_out + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_out)
+    return lib_out
 
 
 if __name__ == "__main__":

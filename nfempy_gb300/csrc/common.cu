@@ -161,16 +161,102 @@ static int noalloc_scratch(int64_t** out) {
 }
 
 // ---------------------------------------------------------------- split
-__global__ void split_points_kernel(const double* __restrict__ p, int64_t n, float* __restrict__ out) {
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+// Packed point records (format in nfem_common.cuh).  Three launches: per-block
+// bounding boxes, one thread folding them into the header record (centre and
+// lo_scale), then the records.  The per-block boxes are parked in the output
+// buffer's point records, which the last launch overwrites.
+constexpr int kSplitBlocks = 152;
+
+__global__ void bbox_partial_kernel(const double* __restrict__ p, int64_t n, double* __restrict__ part) {
+  double mn[3], mx[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    mn[k] = 1.0 / 0.0;
+    mx[k] = -1.0 / 0.0;
+  }
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      double x = p[i * 3 + k];
-      float hi = __double2float_rn(x);
-      float lo = __double2float_rn(x - double(hi));
-      out[i * 6 + k] = hi;
-      out[i * 6 + 3 + k] = lo;
+      const double x = p[i * 3 + k];
+      mn[k] = fmin(mn[k], x);
+      mx[k] = fmax(mx[k], x);
     }
+  __shared__ double sh[32][6];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[k] = fmin(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+      mx[k] = fmax(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      sh[warp][k] = mn[k];
+      sh[warp][3 + k] = mx[k];
+    }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int k = threadIdx.x;
+    double v = sh[0][k];
+    for (int w = 1; w < int(blockDim.x >> 5); ++w) v = k < 3 ? fmin(v, sh[w][k]) : fmax(v, sh[w][k]);
+    part[blockIdx.x * 6 + k] = v;
+  }
+}
+
+// One thread: fold nb partial boxes (or, when nb == 0, the points themselves)
+// into the header record.  lo_scale = 2^(e - 34) with |point - c| < 2^e, so
+// |lo| <= 2^(e - 25) maps to |q| <= 512 (clamped to 511).
+__global__ void split_header_kernel(const double* __restrict__ part, int nb, const double* __restrict__ p,
+                                    int64_t n, float4* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double mn[3], mx[3];
+  for (int k = 0; k < 3; ++k) {
+    mn[k] = 1.0 / 0.0;
+    mx[k] = -1.0 / 0.0;
+  }
+  if (nb > 0) {
+    for (int b = 0; b < nb; ++b)
+      for (int k = 0; k < 3; ++k) {
+        mn[k] = fmin(mn[k], part[b * 6 + k]);
+        mx[k] = fmax(mx[k], part[b * 6 + 3 + k]);
+      }
+  } else {
+    for (int64_t i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) {
+        mn[k] = fmin(mn[k], p[i * 3 + k]);
+        mx[k] = fmax(mx[k], p[i * 3 + k]);
+      }
+  }
+  float c[3];
+  double ext = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    c[k] = n > 0 ? __double2float_rn(0.5 * (mn[k] + mx[k])) : 0.0f;
+    ext = fmax(ext, fmax(fabs(mn[k] - double(c[k])), fabs(mx[k] - double(c[k]))));
+  }
+  int e = 0;
+  frexp(ext, &e);  // ext < 2^e
+  e = max(e, -92);
+  out[0] = make_float4(float(ldexp(1.0, e - 34)), c[0], c[1], c[2]);
+}
+
+__global__ void split_points_kernel(const double* __restrict__ p, int64_t n, float4* __restrict__ out) {
+  const float4 hd = out[0];
+  const double s = double(hd.x);
+  const double c[3] = {double(hd.y), double(hd.z), double(hd.w)};
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    float h[3];
+    uint32_t q = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double y = p[i * 3 + k] - c[k];
+      h[k] = __double2float_rn(y);
+      const double lo = y - double(h[k]);
+      const int qi = max(-511, min(511, int(rint(lo / s))));
+      q |= (uint32_t(qi) & 1023u) << (10 * k);
+    }
+    out[1 + i] = make_float4(h[0], h[1], h[2], __uint_as_float(q));
   }
 }
 
@@ -210,10 +296,18 @@ extern "C" int nfem_exclusive_scan(const int32_t* counts, int64_t n, int64_t* of
   return exclusive_scan_i32(counts, n, offsets, ws, ws_bytes, (cudaStream_t)stream);
 }
 
-extern "C" int nfem_points_split(const double* points, int64_t n_points, float* out, void* stream) {
-  if (n_points < 0 || (n_points > 0 && (!points || !out))) return NFEM_ERR_INVALID_ARG;
-  if (n_points == 0) return NFEM_OK;
-  split_points_kernel<<<grid_for(n_points, 256), 256, 0, (cudaStream_t)stream>>>(points, n_points, out);
+extern "C" int nfem_points_split(const double* points, int64_t n_points, float* out, void* stream_) {
+  if (n_points < 0 || !out || (n_points > 0 && !points)) return NFEM_ERR_INVALID_ARG;
+  if (n_points > INT32_MAX) return NFEM_ERR_OVERFLOW;
+  if (reinterpret_cast<uintptr_t>(out) & 15) return NFEM_ERR_INVALID_ARG;
+  cudaStream_t stream = (cudaStream_t)stream_;
+  float4* rec = reinterpret_cast<float4*>(out);
+  // partial boxes (6 doubles per block) live in records 1.. until the last launch
+  const int nb = int(n_points / 3 < kSplitBlocks ? n_points / 3 : kSplitBlocks);
+  double* part = reinterpret_cast<double*>(rec + 1);
+  if (nb > 0) bbox_partial_kernel<<<nb, 256, 0, stream>>>(points, n_points, part);
+  split_header_kernel<<<1, 32, 0, stream>>>(part, nb, points, n_points, rec);
+  if (n_points > 0) split_points_kernel<<<grid_for(n_points, 256), 256, 0, stream>>>(points, n_points, rec);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }

@@ -32,10 +32,23 @@
 namespace nfem {
 
 constexpr int kDarcyWarps = 8;
+// minimum resident blocks per SM asked of the register allocator
+#ifndef NFEM_DARCY_MIN_BLOCKS
+#define NFEM_DARCY_MIN_BLOCKS 1
+#endif
 constexpr int kDarcyMaxRow = 16;
+// 2: both incidences of a row in straight-line code (their loads may
+// overlap); 1: one after the other (fewer live registers)
+#ifndef NFEM_DARCY_INC_UNROLL
+#define NFEM_DARCY_INC_UNROLL 2
+#endif
+constexpr int kDarcyIncUnroll = NFEM_DARCY_INC_UNROLL;
 
 struct DarcyParams {
   int64_t n_rows;
+  int64_t n_cells;
+  int64_t p_base;
+  const int32_t* chunk_rows;
   const double* points;
   const float* split;
   const int32_t* cv;
@@ -96,42 +109,31 @@ __device__ __forceinline__ void cell_edges<double, 2>(const DarcyParams& p, int3
     for (int d = 0; d < 3; ++d) J[k][d] = __ldg(p.points + int64_t(vs[k + 1]) * 3 + d) - x0[d];
 }
 
-// FP32: coordinates as float (hi, lo) pairs; differences of hi parts of
-// nearby points are exact, the lo parts restore what the split dropped.
-__device__ __forceinline__ void load_split(const float* s, int v, float (&hi)[3], float (&lo)[3]) {
-  const float2* q = reinterpret_cast<const float2*>(s + int64_t(v) * 6);
-  const float2 a = __ldg(q), b = __ldg(q + 1), d = __ldg(q + 2);
-  hi[0] = a.x; hi[1] = a.y; hi[2] = b.x;
-  lo[0] = b.y; lo[1] = d.x; lo[2] = d.y;
-}
-
+// FP32: one packed 16-byte record per vertex (nfem_points_split).
 template <>
 __device__ __forceinline__ void cell_edges<float, 3>(const DarcyParams& p, int32_t c, float (&J)[3][3]) {
   const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
-  const int vs[4] = {v.x, v.y, v.z, v.w};
-  float h0[3], l0[3];
-  load_split(p.split, vs[0], h0, l0);
+  const float s = packed_lo_scale(p.split);
+  const float4 r0 = packed_point(p.split, v.x), r1 = packed_point(p.split, v.y), r2 = packed_point(p.split, v.z),
+               r3 = packed_point(p.split, v.w);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    float h[3], l[3];
-    load_split(p.split, vs[k + 1], h, l);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) J[k][d] = (h[d] - h0[d]) + (l[d] - l0[d]);
+  for (int d = 0; d < 3; ++d) {
+    J[0][d] = packed_diff(r1, r0, d, s);
+    J[1][d] = packed_diff(r2, r0, d, s);
+    J[2][d] = packed_diff(r3, r0, d, s);
   }
 }
 
 template <>
 __device__ __forceinline__ void cell_edges<float, 2>(const DarcyParams& p, int32_t c, float (&J)[2][3]) {
   const int32_t* vp = p.cv + int64_t(c) * 3;
-  const int vs[3] = {__ldg(vp), __ldg(vp + 1), __ldg(vp + 2)};
-  float h0[3], l0[3];
-  load_split(p.split, vs[0], h0, l0);
+  const float s = packed_lo_scale(p.split);
+  const float4 r0 = packed_point(p.split, __ldg(vp)), r1 = packed_point(p.split, __ldg(vp + 1)),
+               r2 = packed_point(p.split, __ldg(vp + 2));
 #pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    float h[3], l[3];
-    load_split(p.split, vs[k + 1], h, l);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) J[k][d] = (h[d] - h0[d]) + (l[d] - l0[d]);
+  for (int d = 0; d < 3; ++d) {
+    J[0][d] = packed_diff(r1, r0, d, s);
+    J[1][d] = packed_diff(r2, r0, d, s);
   }
 }
 
@@ -281,7 +283,7 @@ __device__ __forceinline__ int row_len_from_codes(const RowHead& h) {
 }
 
 template <typename T, int DIM, int SRC>
-__global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const DarcyParams p) {
+__global__ void __launch_bounds__(32 * kDarcyWarps, NFEM_DARCY_MIN_BLOCKS) darcy_rows_kernel(const DarcyParams p) {
   constexpr int NLOC = DIM + 2;
   __shared__ T stage[kDarcyWarps][32 * kDarcyMaxRow];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -314,10 +316,6 @@ __global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const Darc
       a[t] = on[t] ? occ[t] - c[t] * NLOC : 0;
       geo[t] = on[t] && ((a[t] < DIM + 1) || (SRC != 0));
     }
-    Incidence<T, DIM> inc[2];
-#pragma unroll
-    for (int t = 0; t < 2; ++t) load_incidence<T, DIM, SRC>(p, c[t], geo[t], inc[t]);
-
     // row offsets inside the chunk: exclusive warp scan of the row lengths
     const int len = valid ? row_len_from_codes<NLOC>(h) : 0;
     int incl = len;
@@ -332,20 +330,42 @@ __global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const Darc
       if (lane == 0) set_status(p.status, NFEM_ERR_PATTERN);
       continue;
     }
-    for (int i = lane; i < span; i += 32) st[i] = T(0);
-    __syncwarp();
-    T rhs_val = T(0);
-#pragma unroll
+    const bool two = on[0] && on[1];
+    const int pos_a0 = int((code[0] >> (4 * a[0])) & 15u), pos_a1 = int((code[1] >> (4 * a[1])) & 15u);
+    // Two cells of a conforming simplicial mesh share exactly one column of a
+    // face row (the face itself): then the row has 2 NLOC - 1 entries and
+    // each is stored once, the diagonal summed in a register.  A warp with
+    // any other layout zero-fills its image and adds every contribution.
+    const bool simple = !on[0] || (two ? (len == 2 * NLOC - 1 && pos_a0 == pos_a1) : (len == NLOC));
+    const bool direct = __all_sync(0xffffffffu, simple);
+    if (!direct) {
+      for (int i = lane; i < span; i += 32) st[i] = T(0);
+      __syncwarp();
+    }
+    constexpr int kCap = 32 * kDarcyMaxRow - 1;
+    T rhs_val = T(0), diag = T(0);
+#pragma unroll kDarcyIncUnroll
     for (int t = 0; t < 2; ++t) {
       if (on[t]) {
-        T vals[NLOC];
-        element_row<T, DIM, SRC>(p, inc[t], a[t], geo[t], vals, rhs_val);
+        Incidence<T, DIM> x;
+        load_incidence<T, DIM, SRC>(p, c[t], geo[t], x);
+        T v[NLOC];
+        element_row<T, DIM, SRC>(p, x, a[t], geo[t], v, rhs_val);
+        const uint32_t cd = code[t];
+        const int at = a[t];
 #pragma unroll
         for (int b = 0; b < NLOC; ++b) {
           // codes index inside the row (< 16 entries); the clamp keeps a
           // corrupted code inside this warp's staging buffer
-          const int idx = min(off + int((code[t] >> (4 * b)) & 15u), 32 * kDarcyMaxRow - 1);
-          st[idx] += vals[b];
+          const int idx = min(off + int((cd >> (4 * b)) & 15u), kCap);
+          if (!direct) {
+            st[idx] += v[b];
+          } else if (two && b == at) {
+            if (t == 0) diag = v[b];
+            else st[idx] = diag + v[b];
+          } else {
+            st[idx] = v[b];
+          }
         }
       }
     }
@@ -361,18 +381,254 @@ __global__ void __launch_bounds__(32 * kDarcyWarps) darcy_rows_kernel(const Darc
   }
 }
 
+// ------------------------------------------------------------------ cell chunks
+// Cell-chunk variant of the same assembly.  Rows are numbered by first
+// appearance, so the flux rows whose first incidence lies in a run of K
+// consecutive cells are themselves consecutive (the chunk row table), and so
+// are the pressure rows of those cells.  A block (1) evaluates the element
+// matrices of its K cells once, with coalesced loads of the per-cell inputs,
+// into shared memory, (2) writes the K pressure rows and (3) the chunk's
+// flux rows from there.  Only a second incidence in a cell outside the chunk
+// (a neighbour in a later row or layer of the mesh) is evaluated from the
+// vertices as in the row-owner kernel.  Row images are staged per warp and
+// stored coalesced as there; each value is written once.
+constexpr int kChunkThreads = 256;
+constexpr int kChunkWarps = kChunkThreads / 32;
+
 template <typename T, int DIM>
-static int launch_darcy(const DarcyParams& p, int source_mode, cudaStream_t stream) {
-  const int block = 32 * kDarcyWarps;
-  const int grid = grid_for(ceil_div(p.n_rows, 32 * kDarcyWarps), 1, 8);
-  switch (source_mode) {
-    case NFEM_COEF_NONE: darcy_rows_kernel<T, DIM, NFEM_COEF_NONE><<<grid, block, 0, stream>>>(p); break;
-    case NFEM_COEF_CELL: darcy_rows_kernel<T, DIM, NFEM_COEF_CELL><<<grid, block, 0, stream>>>(p); break;
-    case NFEM_COEF_QPOINT: darcy_rows_kernel<T, DIM, NFEM_COEF_QPOINT><<<grid, block, 0, stream>>>(p); break;
-    default: return NFEM_ERR_INVALID_ARG;
+struct ChunkSmem {
+  T* M;           // [K][4][4] element matrix rows (flux x flux block)
+  T* rp;          // [K] residual entry of the cell's pressure row
+  uint32_t* sg;   // [K] orientation mask of the cell
+  T* stage;       // [warps][32 * kDarcyMaxRow]
+};
+
+template <typename T>
+static size_t chunk_smem_bytes(int K) {
+  return size_t(K) * 16 * sizeof(T) + size_t(K) * sizeof(T) + size_t(K) * sizeof(uint32_t) +
+         size_t(kChunkWarps) * 32 * kDarcyMaxRow * sizeof(T) + 16;
+}
+
+// rows [first, last) of the chunk whose cells are [c0, c0 + nk)
+template <typename T, int DIM, int SRC>
+__device__ __forceinline__ void chunk_rows_pass(const DarcyParams& p, const ChunkSmem<T, DIM>& sm, int64_t first,
+                                                int64_t last, int64_t c0, int64_t nk) {
+  constexpr int NF = DIM + 1, NLOC = DIM + 2;
+  using C = DarcyConst<T, DIM>;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* st = sm.stage + warp * 32 * kDarcyMaxRow;
+  T* values = static_cast<T*>(p.values);
+  T* rhs = static_cast<T*>(p.rhs);
+  constexpr int kCap = 32 * kDarcyMaxRow - 1;
+  for (int64_t r0 = first + 32 * warp; r0 < last; r0 += 32 * kChunkWarps) {
+    const int64_t r = r0 + lane;
+    const bool valid = r < last;
+    const RowHead h = load_head(p, valid ? r : p.n_rows);
+    const int32_t base = __ldg(p.row_ptr + r0);
+    const int occ[2] = {h.pr.x, h.pr.y};
+    const uint32_t code[2] = {h.cd.x, h.cd.y};
+    int32_t c[2];
+    int a[2];
+    bool on[2];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      on[t] = occ[t] >= 0;
+      c[t] = on[t] ? occ[t] / NLOC : 0;
+      a[t] = on[t] ? occ[t] - c[t] * NLOC : 0;
+    }
+    const int len = valid ? row_len_from_codes<NLOC>(h) : 0;
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int off = incl - len;
+    const int span = __shfl_sync(0xffffffffu, incl, 31);
+    if (span > 32 * kDarcyMaxRow) {
+      if (lane == 0) set_status(p.status, NFEM_ERR_PATTERN);
+      continue;
+    }
+    const bool two = on[0] && on[1];
+    const int pos_a0 = int((code[0] >> (4 * a[0])) & 15u), pos_a1 = int((code[1] >> (4 * a[1])) & 15u);
+    const bool simple = !on[0] || (two ? (len == 2 * NLOC - 1 && pos_a0 == pos_a1) : (len == NLOC));
+    const bool direct = __all_sync(0xffffffffu, simple);
+    if (!direct) {
+      for (int i = lane; i < span; i += 32) st[i] = T(0);
+      __syncwarp();
+    }
+    T rhs_val = T(0), diag = T(0);
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      if (on[t]) {
+        T v[NLOC];
+        const int64_t lc = int64_t(c[t]) - c0;
+        if (lc >= 0 && lc < nk) {
+          const uint32_t m = sm.sg[lc];
+          if (a[t] < NF) {
+            const T* Mr = sm.M + lc * 16 + a[t] * 4;
+#pragma unroll
+            for (int b = 0; b < NF; ++b) v[b] = Mr[b];
+            T sga = C::sigma(0);
+#pragma unroll
+            for (int i = 1; i < NF; ++i) sga = (a[t] == i) ? C::sigma(i) : sga;
+            sga = ((m >> a[t]) & 1u) ? -sga : sga;
+            v[NF] = -sga;
+          } else {
+#pragma unroll
+            for (int b = 0; b < NF; ++b) v[b] = ((m >> b) & 1u) ? -C::sigma(b) : C::sigma(b);
+            v[NF] = T(0);
+            rhs_val += sm.rp[lc];
+          }
+        } else {
+          Incidence<T, DIM> x;
+          const bool geo = (a[t] < NF) || (SRC != 0);
+          load_incidence<T, DIM, SRC>(p, c[t], geo, x);
+          element_row<T, DIM, SRC>(p, x, a[t], geo, v, rhs_val);
+        }
+        const uint32_t cd = code[t];
+        const int at = a[t];
+#pragma unroll
+        for (int b = 0; b < NLOC; ++b) {
+          const int idx = min(off + int((cd >> (4 * b)) & 15u), kCap);
+          if (!direct) {
+            st[idx] += v[b];
+          } else if (two && b == at) {
+            if (t == 0) diag = v[b];
+            else st[idx] = diag + v[b];
+          } else {
+            st[idx] = v[b];
+          }
+        }
+      }
+    }
+    __syncwarp();
+    if (p.accumulate) {
+      for (int i = lane; i < span; i += 32) values[int64_t(base) + i] += st[i];
+      if (valid) rhs[r] += rhs_val;
+    } else {
+      for (int i = lane; i < span; i += 32) values[int64_t(base) + i] = st[i];
+      if (valid) rhs[r] = rhs_val;
+    }
+    __syncwarp();
   }
+}
+
+template <typename T, int DIM, int SRC, int KC>
+__global__ void __launch_bounds__(kChunkThreads) darcy_cells_kernel(const DarcyParams p) {
+  constexpr int NF = DIM + 1;
+  constexpr int K = KC * NFEM_DARCY_CHUNK_CELLS;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  ChunkSmem<T, DIM> sm;
+  sm.M = reinterpret_cast<T*>(dsm);
+  sm.rp = sm.M + K * 16;
+  sm.sg = reinterpret_cast<uint32_t*>(sm.rp + K);
+  sm.stage = reinterpret_cast<T*>(sm.sg + K);
+  const int64_t n_chunks = (p.n_cells + K - 1) / K;
+  const int64_t n_table = (p.n_cells + NFEM_DARCY_CHUNK_CELLS - 1) / NFEM_DARCY_CHUNK_CELLS;
+  for (int64_t k = blockIdx.x; k < n_chunks; k += gridDim.x) {
+    const int64_t c0 = k * K;
+    const int64_t nk = min(int64_t(K), p.n_cells - c0);
+    // (1) element matrices of the chunk's cells
+    for (int i = threadIdx.x; i < nk; i += kChunkThreads) {
+      Incidence<T, DIM> x;
+      load_incidence<T, DIM, SRC>(p, int32_t(c0 + i), true, x);
+      T rp = T(0);
+#pragma unroll
+      for (int a = 0; a < NF; ++a) {
+        T v[DIM + 2];
+        element_row<T, DIM, SRC>(p, x, a, true, v, rp);
+#pragma unroll
+        for (int b = 0; b < NF; ++b) sm.M[i * 16 + a * 4 + b] = v[b];
+      }
+      T v[DIM + 2];
+      element_row<T, DIM, SRC>(p, x, NF, true, v, rp);
+      sm.rp[i] = rp;
+      sm.sg[i] = x.m;
+    }
+    __syncthreads();
+    // (2) pressure rows of the chunk's cells, (3) its flux rows
+    chunk_rows_pass<T, DIM, SRC>(p, sm, p.p_base + c0, p.p_base + c0 + nk, c0, nk);
+    const int32_t f0 = __ldg(p.chunk_rows + k * KC);
+    const int32_t f1 = __ldg(p.chunk_rows + min((k + 1) * KC, n_table));
+    chunk_rows_pass<T, DIM, SRC>(p, sm, f0, f1, c0, nk);
+    __syncthreads();
+  }
+}
+
+// One resident wave: blocks per SM from the occupancy calculator (queried
+// once per kernel instance), times the SM count, capped by the work.
+template <typename T, int DIM, int SRC>
+static int launch_darcy_src(const DarcyParams& p, cudaStream_t stream) {
+  const int block = 32 * kDarcyWarps;
+  static const int per_sm = [] {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, darcy_rows_kernel<T, DIM, SRC>, 32 * kDarcyWarps, 0) !=
+            cudaSuccess ||
+        n < 1)
+      n = 4;
+    return n;
+  }();
+  const int grid = grid_for(ceil_div(p.n_rows, 32 * kDarcyWarps), 1, per_sm);
+  darcy_rows_kernel<T, DIM, SRC><<<grid, block, 0, stream>>>(p);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
+}
+
+#ifndef NFEM_DARCY_CHUNK_KC
+#define NFEM_DARCY_CHUNK_KC 2
+#endif
+// table entries per chunk: FP32 chunks of 512 cells (44 KB of shared memory),
+// FP64 chunks of 256 cells (43 KB)
+template <typename T>
+struct ChunkKC {
+  static constexpr int value = NFEM_DARCY_CHUNK_KC;
+};
+template <>
+struct ChunkKC<double> {
+  static constexpr int value = 1;
+};
+
+template <typename T, int DIM, int SRC>
+static int launch_darcy_chunks(const DarcyParams& p, cudaStream_t stream) {
+  constexpr int KC = ChunkKC<T>::value;
+  const int K = KC * NFEM_DARCY_CHUNK_CELLS;
+  const size_t smem = chunk_smem_bytes<T>(K);
+  static const int per_sm = [smem] {
+    int n = 0;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(darcy_cells_kernel<T, DIM, SRC, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem)) != cudaSuccess)
+      return -1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, darcy_cells_kernel<T, DIM, SRC, KC>, kChunkThreads,
+                                                      smem) != cudaSuccess ||
+        n < 1)
+      n = 1;
+    return n;
+  }();
+  if (per_sm < 0) return NFEM_ERR_CUDA;
+  const int grid = grid_for(ceil_div(p.n_cells, K), 1, per_sm);
+  darcy_cells_kernel<T, DIM, SRC, KC><<<grid, kChunkThreads, smem, stream>>>(p);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+template <typename T, int DIM>
+static int launch_darcy(const DarcyParams& p, int source_mode, cudaStream_t stream) {
+  if (p.chunk_rows) {
+    switch (source_mode) {
+      case NFEM_COEF_NONE: return launch_darcy_chunks<T, DIM, NFEM_COEF_NONE>(p, stream);
+      case NFEM_COEF_CELL: return launch_darcy_chunks<T, DIM, NFEM_COEF_CELL>(p, stream);
+      case NFEM_COEF_QPOINT: return launch_darcy_chunks<T, DIM, NFEM_COEF_QPOINT>(p, stream);
+      default: return NFEM_ERR_INVALID_ARG;
+    }
+  }
+  switch (source_mode) {
+    case NFEM_COEF_NONE: return launch_darcy_src<T, DIM, NFEM_COEF_NONE>(p, stream);
+    case NFEM_COEF_CELL: return launch_darcy_src<T, DIM, NFEM_COEF_CELL>(p, stream);
+    case NFEM_COEF_QPOINT: return launch_darcy_src<T, DIM, NFEM_COEF_QPOINT>(p, stream);
+    default: return NFEM_ERR_INVALID_ARG;
+  }
 }
 
 }  // namespace nfem
@@ -385,11 +641,9 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
                                          const uint8_t* sign_mask, const void* kappa, const void* source,
                                          int source_mode, const double* qweights, int n_qp,
                                          const int32_t* row_pairs, const uint32_t* pair_codes,
-                                         const int32_t* row_ptr, void* values, void* rhs, int accumulate,
-                                         int32_t* dev_status, void* stream_) {
+                                         const int32_t* row_ptr, const int32_t* chunk_rows, void* values,
+                                         void* rhs, int accumulate, int32_t* dev_status, void* stream_) {
   (void)flux_dofs;
-  (void)p_base;
-  (void)n_cells;
   cudaStream_t stream = (cudaStream_t)stream_;
   if ((dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_rows < 0)
     return NFEM_ERR_INVALID_ARG;
@@ -397,14 +651,19 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   if (!cell_vertices || !sign_mask || !kappa || !row_pairs || !pair_codes || !row_ptr || !values || !rhs)
     return NFEM_ERR_INVALID_ARG;
   if (value_type == NFEM_F64 && !points) return NFEM_ERR_INVALID_ARG;
-  if (value_type == NFEM_F32 && !points_split) return NFEM_ERR_INVALID_ARG;
+  if (value_type == NFEM_F32 && (!points_split || (reinterpret_cast<uintptr_t>(points_split) & 15)))
+    return NFEM_ERR_INVALID_ARG;
   if (source_mode != NFEM_COEF_NONE && !source) return NFEM_ERR_INVALID_ARG;
   if (source_mode == NFEM_COEF_QPOINT && (!qweights || n_qp < 1 || n_qp > 32)) return NFEM_ERR_INVALID_ARG;
   if (dim == 3 && (reinterpret_cast<uintptr_t>(cell_vertices) & 15)) return NFEM_ERR_INVALID_ARG;
   if ((reinterpret_cast<uintptr_t>(row_pairs) & 7) || (reinterpret_cast<uintptr_t>(pair_codes) & 7))
     return NFEM_ERR_INVALID_ARG;
+  if (chunk_rows && (n_cells < 1 || p_base < 0 || p_base + n_cells != n_rows)) return NFEM_ERR_INVALID_ARG;
   DarcyParams p;
   p.n_rows = n_rows;
+  p.n_cells = n_cells;
+  p.p_base = p_base;
+  p.chunk_rows = chunk_rows;
   p.points = points;
   p.split = points_split;
   p.cv = cell_vertices;
@@ -423,4 +682,218 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   if (value_type == NFEM_F64)
     return dim == 3 ? launch_darcy<double, 3>(p, source_mode, stream) : launch_darcy<double, 2>(p, source_mode, stream);
   return dim == 3 ? launch_darcy<float, 3>(p, source_mode, stream) : launch_darcy<float, 2>(p, source_mode, stream);
+}
+
+// ------------------------------------------------------------------ Dirichlet
+// LaplaceDualWeakFormBCDirichlet (src/weak_forms/laplace_dual_weak_form.py:90-154):
+// on a boundary facet the RT1 function of that face has the constant normal
+// component sgn / |F| (sgn = +1 when its oriented normal points out of the
+// cell), so r_f = sgn * |det J_F| / |F| * sum_q w_q p_D(x_q), and
+// |det J_F| / |F| = 1 / |reference facet| (2 on triangles, 1 on intervals).
+namespace nfem {
+template <typename T, int DIM>
+__global__ void darcy_dirichlet_kernel(int64_t n_facets, const int32_t* __restrict__ focc,
+                                       const uint8_t* __restrict__ sign, const int32_t* __restrict__ cd, int ld,
+                                       const T* __restrict__ pd, int nq, const double qw0, const double qw1,
+                                       const double qw2, const double qw3, T* __restrict__ rhs) {
+  using C = DarcyConst<T, DIM>;
+  const double qw[4] = {qw0, qw1, qw2, qw3};
+  for (int64_t f = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; f < n_facets; f += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t occ = focc[f];
+    const int32_t c = occ / (DIM + 1);
+    const int i = occ - c * (DIM + 1);
+    const uint32_t m = sign[c];
+    T sg = C::sigma(i);
+    if ((m >> i) & 1u) sg = -sg;
+    T acc = T(0);
+    for (int q = 0; q < nq; ++q) acc += T(qw[q]) * pd[f * nq + q];
+    const T inv_ref = DIM == 3 ? T(2) : T(1);
+    rhs[cd[int64_t(c) * ld + i]] += sg * inv_ref * acc;
+  }
+}
+}  // namespace nfem
+
+extern "C" int nfem_darcy_rt1_dirichlet(int dim, int value_type, int64_t n_facets, const int32_t* facet_occ,
+                                        const uint8_t* sign_mask, const int32_t* cell_dofs, int ld,
+                                        const void* pd_q, const double* qweights, int n_qp, void* rhs,
+                                        void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if ((dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_facets < 0 ||
+      n_qp < 1 || n_qp > 4 || !qweights || ld < dim + 1)
+    return NFEM_ERR_INVALID_ARG;
+  if (n_facets == 0) return NFEM_OK;
+  if (!facet_occ || !sign_mask || !cell_dofs || !pd_q || !rhs) return NFEM_ERR_INVALID_ARG;
+  double w[4] = {0, 0, 0, 0};
+  for (int q = 0; q < n_qp; ++q) w[q] = qweights[q];
+  const int g = grid_for(n_facets, 256);
+  if (value_type == NFEM_F64) {
+    if (dim == 3)
+      darcy_dirichlet_kernel<double, 3><<<g, 256, 0, stream>>>(n_facets, facet_occ, sign_mask, cell_dofs, ld,
+                                                               (const double*)pd_q, n_qp, w[0], w[1], w[2], w[3],
+                                                               (double*)rhs);
+    else
+      darcy_dirichlet_kernel<double, 2><<<g, 256, 0, stream>>>(n_facets, facet_occ, sign_mask, cell_dofs, ld,
+                                                               (const double*)pd_q, n_qp, w[0], w[1], w[2], w[3],
+                                                               (double*)rhs);
+  } else {
+    if (dim == 3)
+      darcy_dirichlet_kernel<float, 3><<<g, 256, 0, stream>>>(n_facets, facet_occ, sign_mask, cell_dofs, ld,
+                                                              (const float*)pd_q, n_qp, w[0], w[1], w[2], w[3],
+                                                              (float*)rhs);
+    else
+      darcy_dirichlet_kernel<float, 2><<<g, 256, 0, stream>>>(n_facets, facet_occ, sign_mask, cell_dofs, ld,
+                                                              (const float*)pd_q, n_qp, w[0], w[1], w[2], w[3],
+                                                              (float*)rhs);
+  }
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+// ------------------------------------------------------------------ L2 error
+// l2_error (src/postprocess/l2_error_post_processor.py:7-63) for the RT1 x P0
+// solution: err_u^2 = sum_cells sum_q |det J| w_q |u(x_q) - u_h(x_q)|^2 (vector
+// branch :41-59), err_p^2 likewise with p_h = alpha_p (Lagrange branch
+// :35-40).  FP64; per-block partials added in a fixed order.
+namespace nfem {
+struct L2Params {
+  int64_t n_cells;
+  const double* points;
+  const int32_t* cv;
+  const uint8_t* sign;
+  const int32_t* cd;
+  int ld;
+  const double* alpha;
+  const double* ue;  // [T, Q, dim]
+  const double* pe;  // [T, Q]
+  int nq;
+  double qp[8][3];
+  double qw[8];
+  double* partial;   // [2, gridDim.x]
+};
+
+template <int DIM>
+__global__ void darcy_l2_kernel(const L2Params p) {
+  using C = DarcyConst<double, DIM>;
+  __shared__ double sh[2][32];
+  double eu = 0.0, ep = 0.0;
+  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < p.n_cells; c += int64_t(gridDim.x) * blockDim.x) {
+    double x0[3], J[3][DIM];
+    const int32_t v0 = p.cv[c * (DIM + 1)];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) x0[d] = p.points[int64_t(v0) * 3 + d];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      const int32_t vk = p.cv[c * (DIM + 1) + k + 1];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) J[d][k] = p.points[int64_t(vk) * 3 + d] - x0[d];
+    }
+    double det;
+    if (DIM == 3) {
+      det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+            J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      det = fabs(det);
+    } else {
+      double g00 = 0, g01 = 0, g11 = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        g00 += J[d][0] * J[d][0];
+        g01 += J[d][0] * J[d][DIM - 1];
+        g11 += J[d][DIM - 1] * J[d][DIM - 1];
+      }
+      det = sqrt(g00 * g11 - g01 * g01);
+    }
+    const uint32_t m = p.sign[c];
+    double a[DIM + 1];
+#pragma unroll
+    for (int i = 0; i <= DIM; ++i) {
+      double sg = C::sigma(i);
+      if ((m >> i) & 1u) sg = -sg;
+      a[i] = sg * p.alpha[p.cd[c * p.ld + i]];
+    }
+    const double ap = p.alpha[p.cd[c * p.ld + DIM + 1]];
+    const double kap = DIM == 3 ? 2.0 : 1.0;
+    for (int q = 0; q < p.nq; ++q) {
+      // uh = (1/|det|) J sum_i a_i kappa (xhat - vhat_i)
+      double ref[DIM];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        double s = 0.0;
+#pragma unroll
+        for (int i = 0; i <= DIM; ++i) s += a[i] * kap * (p.qp[q][k] - (i == k + 1 ? 1.0 : 0.0));
+        ref[k] = s;
+      }
+      double du2 = 0.0;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        double uh = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) uh += J[d][k] * ref[k];
+        uh /= det;
+        const double diff = p.ue[(c * p.nq + q) * DIM + d] - uh;
+        du2 += diff * diff;
+      }
+      const double dp = p.pe[c * p.nq + q] - ap;
+      eu += det * p.qw[q] * du2;
+      ep += det * p.qw[q] * dp * dp;
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    eu += __shfl_down_sync(0xffffffffu, eu, o);
+    ep += __shfl_down_sync(0xffffffffu, ep, o);
+  }
+  if (lane == 0) { sh[0][warp] = eu; sh[1][warp] = ep; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double su = 0, sp = 0;
+    for (int w = 0; w < (blockDim.x >> 5); ++w) { su += sh[0][w]; sp += sh[1][w]; }
+    p.partial[blockIdx.x] = su;
+    p.partial[gridDim.x + blockIdx.x] = sp;
+  }
+}
+
+__global__ void l2_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
+  if (threadIdx.x < 2) {
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) s += partial[threadIdx.x * nb + b];
+    out[threadIdx.x] = sqrt(s);
+  }
+}
+}  // namespace nfem
+
+extern "C" int nfem_darcy_l2_error(int dim, int64_t n_cells, const double* points, const int32_t* cell_vertices,
+                                   const uint8_t* sign_mask, const int32_t* cell_dofs, int ld, const double* alpha,
+                                   const double* u_exact_q, const double* p_exact_q, const double* qpoints,
+                                   const double* qweights, int n_qp, double* errors, void* workspace,
+                                   size_t workspace_bytes, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  const int nb = 304;
+  if ((dim != 2 && dim != 3) || n_cells < 0 || n_qp < 1 || n_qp > 8 || !qpoints || !qweights || !errors ||
+      ld < dim + 2)
+    return NFEM_ERR_INVALID_ARG;
+  if (!workspace || workspace_bytes < size_t(2 * nb) * sizeof(double)) return NFEM_ERR_WORKSPACE;
+  if (n_cells > 0 && (!points || !cell_vertices || !sign_mask || !cell_dofs || !alpha || !u_exact_q || !p_exact_q))
+    return NFEM_ERR_INVALID_ARG;
+  L2Params p;
+  p.n_cells = n_cells;
+  p.points = points;
+  p.cv = cell_vertices;
+  p.sign = sign_mask;
+  p.cd = cell_dofs;
+  p.ld = ld;
+  p.alpha = alpha;
+  p.ue = u_exact_q;
+  p.pe = p_exact_q;
+  p.nq = n_qp;
+  for (int q = 0; q < 8; ++q) {
+    p.qw[q] = q < n_qp ? qweights[q] : 0.0;
+    for (int k = 0; k < 3; ++k) p.qp[q][k] = (q < n_qp && k < dim) ? qpoints[q * dim + k] : 0.0;
+  }
+  p.partial = (double*)workspace;
+  if (dim == 3) darcy_l2_kernel<3><<<nb, 256, 0, stream>>>(p);
+  else darcy_l2_kernel<2><<<nb, 256, 0, stream>>>(p);
+  l2_final<<<1, 32, 0, stream>>>(p.partial, nb, errors);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
 }

@@ -95,13 +95,14 @@ __device__ __forceinline__ void tet_edges<double>(const ElasParams& p, int32_t c
 template <>
 __device__ __forceinline__ void tet_edges<float>(const ElasParams& p, int32_t c, float (&J)[3][3]) {
   const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
-  const int vs[4] = {v.x, v.y, v.z, v.w};
-  const float* s0 = p.split + int64_t(vs[0]) * 6;
+  const float s = packed_lo_scale(p.split);
+  const float4 r0 = packed_point(p.split, v.x), r1 = packed_point(p.split, v.y), r2 = packed_point(p.split, v.z),
+               r3 = packed_point(p.split, v.w);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float* sk = p.split + int64_t(vs[k + 1]) * 6;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) J[d][k] = (__ldg(sk + d) - __ldg(s0 + d)) + (__ldg(sk + 3 + d) - __ldg(s0 + 3 + d));
+  for (int d = 0; d < 3; ++d) {
+    J[d][0] = packed_diff(r1, r0, d, s);
+    J[d][1] = packed_diff(r2, r0, d, s);
+    J[d][2] = packed_diff(r3, r0, d, s);
   }
 }
 
@@ -316,7 +317,8 @@ extern "C" int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int6
       !values || !rhs)
     return NFEM_ERR_INVALID_ARG;
   if (value_type == NFEM_F64 && !points) return NFEM_ERR_INVALID_ARG;
-  if (value_type == NFEM_F32 && !points_split) return NFEM_ERR_INVALID_ARG;
+  if (value_type == NFEM_F32 && (!points_split || (reinterpret_cast<uintptr_t>(points_split) & 15)))
+    return NFEM_ERR_INVALID_ARG;
   if (reinterpret_cast<uintptr_t>(cell_vertices) & 15) return NFEM_ERR_INVALID_ARG;
   int rc = upload_tables(ref_S, ref_m, nullptr, stream);
   if (rc) return rc;

@@ -48,6 +48,28 @@ struct Carver {
   bool ok() const { return off <= cap; }
 };
 
+// Packed FP32 point records written by nfem_points_split: record 0 holds
+// (lo_scale, cx, cy, cz); record v + 1 holds (hx, hy, hz, q) for point v,
+// where hi + lo = point - c (c = the bounding-box centre rounded to float),
+// h = float(point - c) and q packs three signed 10-bit integers
+// (bits 0-9, 10-19, 20-29) with lo_d ~= q_d * lo_scale.  An edge component
+// is then (h1 - h0) + float(q1 - q0) * lo_scale: one 16-byte load per point,
+// no FP64 arithmetic, and an absolute error of lo_scale (about 2^-33 times
+// the half-extent of the mesh).
+__device__ __forceinline__ float4 packed_point(const float* split, int32_t v) {
+  return __ldg(reinterpret_cast<const float4*>(split) + 1 + v);
+}
+__device__ __forceinline__ float packed_lo_scale(const float* split) { return __ldg(split); }
+__device__ __forceinline__ int packed_q(float w, int d) {
+  return int(__float_as_uint(w) << (22 - 10 * d)) >> 22;
+}
+// edge component d of x1 - x0 from two packed records
+__device__ __forceinline__ float packed_diff(const float4& r1, const float4& r0, int d, float lo_scale) {
+  const float h1 = d == 0 ? r1.x : (d == 1 ? r1.y : r1.z);
+  const float h0 = d == 0 ? r0.x : (d == 1 ? r0.y : r0.z);
+  return (h1 - h0) + float(packed_q(r1.w, d) - packed_q(r0.w, d)) * lo_scale;
+}
+
 // exclusive scan of int32 counts into int64 offsets (n + 1 entries)
 size_t scan_workspace_bytes(int64_t n);
 int exclusive_scan_i32(const int32_t* in, int64_t n, int64_t* out, void* ws,

@@ -340,6 +340,58 @@ extern "C" int nfem_pattern_pairs(const int32_t* inc_ptr, const int32_t* inc, co
   return NFEM_OK;
 }
 
+// Cell-chunk row table for the mixed RT1 x P0 layout.  Rows [0, p_base) are
+// flux rows numbered by first appearance, so the first incidence's cell is
+// non-decreasing along them; chunk_rows[k] = the first flux row whose first
+// cell is >= k * chunk_cells (chunk_rows[n_chunks] = p_base).  Rows
+// [p_base, p_base + n_cells) must be the pressure rows of cells 0.. in order.
+// Any other layout sets NFEM_ERR_UNSUPPORTED.
+__global__ void chunk_rows_kernel(const int2* __restrict__ pairs, int64_t n_rows, int n_loc, int64_t p_base,
+                                  int64_t n_cells, int chunk_cells, int64_t n_chunks, int32_t* __restrict__ chunk_rows,
+                                  int32_t* status) {
+  for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n_rows; r += int64_t(gridDim.x) * blockDim.x) {
+    const int2 pr = pairs[r];
+    if (r >= p_base) {
+      const int64_t c = r - p_base;
+      if (pr.x != int32_t(c * n_loc + n_loc - 1) || pr.y != -1) set_status(status, NFEM_ERR_UNSUPPORTED);
+      continue;
+    }
+    if (pr.x < 0) {
+      set_status(status, NFEM_ERR_UNSUPPORTED);
+      continue;
+    }
+    const int64_t k = (pr.x / n_loc) / chunk_cells;
+    int64_t kp = -1;
+    if (r > 0) {
+      const int2 q = pairs[r - 1];
+      kp = q.x < 0 ? k : (q.x / n_loc) / chunk_cells;
+      if (kp > k) set_status(status, NFEM_ERR_UNSUPPORTED);
+    }
+    for (int64_t j = kp + 1; j <= k && j <= n_chunks; ++j) chunk_rows[j] = int32_t(r);
+    if (r == p_base - 1)
+      for (int64_t j = k + 1; j <= n_chunks; ++j) chunk_rows[j] = int32_t(p_base);
+  }
+}
+
+extern "C" int nfem_pattern_darcy_chunks(const int32_t* pairs, int64_t n_rows, int n_loc, int64_t p_base,
+                                         int64_t n_cells, int32_t* chunk_rows, int32_t* dev_status, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n_rows < 0 || n_loc < 2 || p_base < 0 || n_cells < 0 || !chunk_rows || (n_rows > 0 && !pairs))
+    return NFEM_ERR_INVALID_ARG;
+  if (reinterpret_cast<uintptr_t>(pairs) & 7) return NFEM_ERR_INVALID_ARG;
+  if (p_base + n_cells != n_rows || n_rows >= INT32_MAX) return NFEM_ERR_UNSUPPORTED;
+  const int64_t n_chunks = ceil_div(n_cells, NFEM_DARCY_CHUNK_CELLS);
+  if (p_base == 0) {
+    NFEM_TRY_CUDA(cudaMemsetAsync(chunk_rows, 0, size_t(n_chunks + 1) * sizeof(int32_t), stream));
+  }
+  if (n_rows == 0) return NFEM_OK;
+  chunk_rows_kernel<<<grid_for(n_rows, 256), 256, 0, stream>>>(reinterpret_cast<const int2*>(pairs), n_rows, n_loc,
+                                                               p_base, n_cells, NFEM_DARCY_CHUNK_CELLS, n_chunks,
+                                                               chunk_rows, dev_status);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
 extern "C" int nfem_pattern_slots(const int32_t* cd, int64_t n_cells, int n_loc, int ld, const int32_t* row_ptr,
                                   const int32_t* col_idx, int32_t* slots, int32_t* dev_status, void* stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;

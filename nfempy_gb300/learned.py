@@ -274,10 +274,36 @@ def train(model, X, T, steps=3000, batch=512, lr=2e-3, seed=0, log=None):
     return hist
 
 
-def learned_weights(tl, model, kappa):
-    """Flux-extension weights predicted by the network for a TwoLevelCoarse."""
+def learned_weights(tl, model, kappa, alpha=1.0):
+    """Flux-extension weights w_f = exp(alpha * tau_f) / |a_ff| with tau the
+    network's prediction (alpha = 0: the classical weights)."""
     faces = FaceData(tl)
     tau = model.predict(faces.features(kappa))[:, 0].double()
     w = tl.classical_weights().double().clone()
-    w[faces.rows] = torch.exp(tau.clamp(-5.0, 5.0)) / tl.A.diagonal()[faces.rows].abs().clamp_min(1e-300)
+    w[faces.rows] = torch.exp(alpha * tau.clamp(-5.0, 5.0)) / tl.A.diagonal()[faces.rows].abs().clamp_min(1e-300)
     return w.float()
+
+
+def select_alpha(model, problem, n_c, seed, alphas=(0.0, 0.25, 0.5, 1.0), max_iters=20000, log=None):
+    """Scale of the network's correction chosen on a validation field (a seed
+    used neither in training nor in testing): the alpha whose two-level
+    preconditioner needs the fewest iterations to 1e-8.  alpha = 0 (the
+    classical weights) is among the candidates, so the chosen preconditioner
+    is never worse on the validation field than the classical one."""
+    from .solvers import KrylovSolver, TwoLevelCoarse
+    kappa = problem.field(seed)
+    b = problem.assemble(kappa)
+    best = None
+    results = {}
+    for a in alphas:
+        tl = TwoLevelCoarse(problem.A, n_c)
+        tl.set_weights(learned_weights(tl, model, kappa, a))
+        ksp = KrylovSolver(problem.A, pc="two_level", A32_values=problem.A32.values, two_level=tl)
+        x, info = ksp.solve(b, rtol=1e-8, max_inner=max_iters, raise_on_failure=False)
+        it = info.inner_iterations if info.status == 0 else 10 ** 9
+        results[a] = it
+        if log:
+            log(f"alpha {a}: {info.inner_iterations} iterations, status {info.status}")
+        if best is None or it < results[best]:
+            best = a
+    return best, results

@@ -104,6 +104,34 @@ def cube(n):
     return {"dim": 3, "points": points, "blocks": blocks}
 
 
+def union(meshes_list):
+    """Disjoint union of meshes of one dimension: points concatenated (each
+    mesh's vertex ids offset by the points before it), blocks of one type
+    concatenated in mesh order with their tags.  The cells of mesh 0 come
+    first, so first-appearance numbering gives each mesh a contiguous range
+    of every entity block and the assembled system is block diagonal up to
+    that interleaving of blocks.  Used for batches of independent problems
+    assembled in one launch."""
+    dim = meshes_list[0]["dim"]
+    pts, off = [], 0
+    by_type = {}
+    order = []
+    for m in meshes_list:
+        if m["dim"] != dim:
+            raise ValueError("union: meshes of different dimensions")
+        pts.append(np.asarray(m["points"], dtype=np.float64))
+        for typ, conn, tags in m["blocks"]:
+            if typ not in by_type:
+                by_type[typ] = ([], [])
+                order.append(typ)
+            by_type[typ][0].append(np.asarray(conn, dtype=np.int64) + off)
+            by_type[typ][1].append(np.asarray(tags))
+        off += pts[-1].shape[0]
+    order.sort(key=lambda t: BLOCK_DIM[t])
+    blocks = [(t, np.concatenate(by_type[t][0]), np.concatenate(by_type[t][1])) for t in order]
+    return {"dim": dim, "points": np.concatenate(pts), "blocks": blocks}
+
+
 def grf_log_field(x, corr_len, sigma, seed, n_features=512, device=None, chunk=1 << 20):
     """Gaussian random field values at points x [N, 3] (numpy or torch).
 

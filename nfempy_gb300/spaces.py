@@ -164,7 +164,7 @@ class ProductSpace:
         self.cells_host = cells
         self.cells = torch.as_tensor(cells.astype(np.int32), device=dev).contiguous()
         self.points = torch.as_tensor(mesh.points, dtype=torch.float64, device=dev).contiguous()
-        self.points_split = torch.empty((mesh.points.shape[0], 6), dtype=torch.float32, device=dev)
+        self.points_split = torch.empty((mesh.points.shape[0] + 1, 4), dtype=torch.float32, device=dev)
         _lib.call("nfem_points_split", _lib.ptr(self.points), mesh.points.shape[0], _lib.ptr(self.points_split), st)
         # boundary facets of the mesh file (all tagged lower-dimensional blocks)
         facet_blocks, facets_first, seen_cells = [], 1, False

@@ -4,6 +4,11 @@ darcy3d(n): unit cube, n^3 hexahedra x 6 Kuhn tetrahedra, RT1 x P0,
   log K from a Gaussian random field (correlation length 0.05, sigma 2.0,
   sampled at cell centroids), source f = 1 per cell.  n = 64 gives
   1,572,864 tets, 4,743,168 DoF, nnz 36,200,448.
+darcy2d_batch(n_problems): a batch of independent 2-D mixed Darcy
+  problems assembled in one launch as one disjoint-union mesh: problem i is
+  the unit square with n_i x n_i squares x 2 triangles, n_i ~ U{8..128},
+  log K_i a Gaussian random field (correlation length 0.1, sigma 1.0,
+  seed + i) at the cell centroids, f = 1.  512 problems give about 15 M DoF.
 darcy2d(n): unit square, n x n squares x 2 triangles, RT1 x P0, K = 1,
   f = 2 pi^2 sin(pi x) sin(pi y) at the quadrature points (n = 32: 2,048
   triangles, 5,184 DoF).
@@ -39,3 +44,19 @@ def darcy3d(n=64, device=None):
     sp = darcy_space(m, device=device)
     kappa, f = darcy3d_coefficients(m)
     return m, sp, kappa, f
+
+
+def darcy2d_batch(n_problems=512, n_min=8, n_max=128, corr_len=0.1, sigma=1.0, seed=SEED + 3, device=None):
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(n_min, n_max + 1, size=n_problems)
+    ms, kappas = [], []
+    for i, n in enumerate(sides):
+        m = meshes.square(int(n))
+        cells = m["blocks"][-1][1]
+        centroids = m["points"][cells].mean(axis=1)
+        kappas.append(np.exp(meshes.grf_log_field(centroids, corr_len, sigma, seed + 1 + i, device="cpu")))
+        ms.append(m)
+    u = meshes.union(ms)
+    sp = darcy_space(u, device=device)
+    kappa = np.concatenate(kappas)
+    return u, sp, kappa, np.ones(kappa.shape[0]), sides

@@ -266,3 +266,39 @@ def cosserat_element(X, signs, quad, par, f_u, f_t):
             j[ns + nm + nu + c, ns + i * 3 + c] += ub[i]
             j[ns + i * 3 + c, ns + nm + nu + c] += ub[i]
     return r, j
+
+
+def darcy_dirichlet_facet(Xc, signs_c, local_face, Xf, dim, quad_f, p_D):
+    """LaplaceDualWeakFormBCDirichlet.evaluate_form (laplace_dual_weak_form.py:90-154)
+    for one boundary facet: r = sum_q |det J_F| w_q p_D(x_q) (psi_f . n), with
+    psi_f the neighbour cell's oriented RT1 function of that face and n the
+    outward unit normal of compute_normal.py:7-24.  Xc [d+1, 3] cell
+    vertices, Xf [d, 3] facet vertices (file order).  Returns the scalar
+    residual entry of the face's flux DoF."""
+    from .geometry import evaluate_mapping as emap
+    pts, wts = quad_f
+    xf, Jf, detf, _ = emap(dim - 1, pts, Xf)
+    # outward normal (compute_normal.py): from the cell centroid to the facet centroid
+    xc1 = Xf.mean(axis=0)
+    xc0 = Xc.mean(axis=0)
+    out = (xc1 - xc0) / np.linalg.norm(xc1 - xc0)
+    if dim == 3:
+        v = Xf[0] - xc1
+        w = Xf[1] - xc1
+        nrm = np.cross(v, w)
+        nrm /= np.linalg.norm(nrm)
+    else:
+        v = (Xf[1] - Xf[0]) / np.linalg.norm(Xf[1] - Xf[0])
+        w = np.cross(v, out)
+        w /= np.linalg.norm(w)
+        nrm = np.cross(v, w)
+    if nrm @ out < 0:
+        nrm = -nrm
+    # psi_f at the facet points, through the neighbour cell's mapping
+    Jc = (Xc[1:] - Xc[0]).T  # [3, d]
+    xhat = np.linalg.lstsq(Jc, (xf - Xc[0]).T, rcond=None)[0].T  # reference coordinates
+    x, J, det, pinv = emap(dim, xhat, Xc)
+    tab = tabulate_oriented("RT", dim, 1, xhat, J, det, pinv, signs_c)
+    psi = tab[0, :, local_face, :]  # [Q, 3]
+    pd = np.ravel(np.asarray(p_D(xf[:, 0], xf[:, 1], xf[:, 2]))[0]) * np.ones(len(wts))
+    return float(np.sum(detf * wts * pd * (psi @ nrm)))

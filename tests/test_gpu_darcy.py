@@ -22,11 +22,12 @@ def f2d(x, y, z):
     return np.array([2 * PI ** 2 * np.sin(PI * x) * np.sin(PI * y)])
 
 
-def assemble_gpu(m, kappa, rhs, dtype):
+def assemble_gpu(m, kappa, rhs, dtype, use_chunks=True):
     sp = product_space(m, DARCY)
     A = nf.CSRMatrix(sp, dtype=dtype)
     res = torch.empty(A.n_rows, dtype=dtype, device="cuda")
     wf = nf.LaplaceDualWeakForm(sp)
+    wf.use_chunks = use_chunks
     wf.functions = {"kappa": kappa, "rhs": rhs}
     asm = nf.SequentialAssembler(sp, A, res)
     asm.form_to_input_list = {"darcy": ["form", range(sp.n_cells), wf, None]}
@@ -42,14 +43,18 @@ def row_scaled_err(Ag, Ao):
     return (abs(d).max(axis=1).toarray().ravel() / scale).max()
 
 
+@pytest.mark.parametrize("use_chunks", [True, False], ids=["cell_chunks", "row_owner"])
 @pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
-@pytest.mark.parametrize("gen,n", [("square", 4), ("square", 32), ("cube", 2), ("cube", 6)])
-def test_darcy_matrix_matches_oracle(cuda_lib, dtype, tol, gen, n):
+@pytest.mark.parametrize("gen,n", [("square", 4), ("square", 32), ("cube", 2), ("cube", 6), ("cube", 12)])
+def test_darcy_matrix_matches_oracle(cuda_lib, dtype, tol, gen, n, use_chunks):
+    """Both Darcy kernels against the oracle; cube(12) has 10,368 cells, so the
+    cell-chunk kernel runs several chunks and meets neighbours outside them."""
     m = getattr(mesh_gen, gen)(n)
     T = m["blocks"][-1][1].shape[0]
     kappa = np.exp(np.sin(np.arange(T) * 0.37))
     f_cell = np.cos(np.arange(T) * 0.11)
-    sp, A, res = assemble_gpu(m, kappa, f_cell, dtype)
+    sp, A, res = assemble_gpu(m, kappa, f_cell, dtype, use_chunks)
+    assert (A.chunk_rows is not None) == (sp.dof_shift == 0)
     Ao, ro, cd, nd, topo = darcy_oracle(m, kappa, f_cell=f_cell)
     Ag = A.to_scipy()
     np.testing.assert_array_equal(Ag.indptr, Ao.indptr)
@@ -112,3 +117,128 @@ def test_darcy_host_residual_and_deterministic(cuda_lib):
     assert torch.equal(v1, A.values)  # bitwise reproducible
     np.testing.assert_array_equal(host, host2)
     assert np.abs(host).max() > 0
+
+
+@pytest.mark.parametrize("gen,n", [("square", 6), ("cube", 3)])
+def test_darcy_dirichlet_matches_oracle(cuda_lib, gen, n):
+    """LaplaceDualWeakFormBCDirichlet: residual of the boundary flux DoFs for
+    p_D = 1 + x + 2y + z^2, compared with the oracle's faithful restatement
+    (normal from compute_normal, basis traced from the neighbour cell)."""
+    from oracle import forms, quadrature, topology
+    m = getattr(mesh_gen, gen)(n)
+    dim = m["dim"]
+    sp = product_space(m, DARCY)
+    A = nf.CSRMatrix(sp, dtype=torch.float64)
+    res = torch.zeros(A.n_rows, dtype=torch.float64, device="cuda")
+    pD = lambda x, y, z: np.array([1 + x + 2 * y + z * z])
+    bc = nf.assembly.LaplaceDualWeakFormBCDirichlet(sp)
+    bc.functions = {"p": pD}
+    bc.assemble(A, res)
+    torch.cuda.synchronize()
+    rg = res.cpu().numpy()
+    topo = topology.Topology(m)
+    cd, nd = topology.cell_dofs(topo, [topology.FieldSpec(*f) for f in DARCY])
+    X = m["points"][topo.cells]
+    s = topo.rt1_signs()
+    qf = quadrature.make_quadrature(dim - 1, 3)
+    ro = np.zeros(nd)
+    occ, fverts = bc.facets()
+    for o, fv in zip(occ, fverts):
+        c, i = divmod(int(o), dim + 1)
+        ro[cd[c, i]] += forms.darcy_dirichlet_facet(X[c], s[c], i, m["points"][fv], dim, qf, pD)
+    assert len(occ) == (4 * n if dim == 2 else 12 * n * n)
+    np.testing.assert_allclose(rg, ro, rtol=1e-12, atol=1e-13)
+
+
+def test_darcy_l2_error_matches_oracle(cuda_lib):
+    """Device L2 errors of a solved 2-D / 3-D Darcy problem equal the oracle's
+    (src/postprocess/l2_error_post_processor.py:7-63) to 1e-12 relative."""
+    from oracle import quadrature
+
+    def p_ex(x, y, z):
+        return np.sin(PI * x) * np.sin(PI * y)
+
+    def u_ex(x, y, z):
+        return np.array([-PI * np.cos(PI * x) * np.sin(PI * y), -PI * np.sin(PI * x) * np.cos(PI * y),
+                         np.zeros_like(x)])
+
+    for m in (mesh_gen.square(16), mesh_gen.cube(4)):
+        dim = m["dim"]
+        sp, A, res = assemble_gpu(m, 1.0, f2d, torch.float64)
+        Ao, ro, cd, nd, topo = darcy_oracle(m, np.ones(sp.n_cells), f_callable=f2d)
+        x = solve.solve_newton_step(Ao, ro)
+        got = nf.l2_error(dim, sp, {"u": u_ex, "p": p_ex}, x)
+        quad = quadrature.make_quadrature(dim, 3)
+        assert len(quad[1]) == len(sp.quadrature[dim][1])
+        want = solve.l2_error_darcy(m["points"][topo.cells], topo.rt1_signs(), dim, quad, cd, x, u_ex, p_ex)
+        np.testing.assert_allclose(got, want, rtol=1e-12)
+        if dim == 2:
+            assert want[1] < 0.05 and want[0] < 0.3
+
+
+def test_darcy_batched_union_matches_oracle(cuda_lib):
+    """A batch of independent 2-D problems assembled in one launch over their
+    disjoint union: equal to the oracle's assembly of the union (FP64, 1e-12),
+    block diagonal across problems, and each problem's solution equal to the
+    oracle's solve of that problem alone."""
+    from nfempy_gb300 import meshes
+    rng = np.random.default_rng(3)
+    sides = [3, 7, 4, 9, 5, 6]
+    ms = [mesh_gen.square(n) for n in sides]
+    u = meshes.union(ms)
+    kap = np.exp(rng.normal(0.0, 1.0, sum(2 * n * n for n in sides)))
+    sp, A, res = assemble_gpu(u, kap, 1.0, torch.float64)
+    Ao, ro, cd, nd, topo = darcy_oracle(u, kap, f_cell=np.ones(len(kap)))
+    Ag = A.to_scipy()
+    assert row_scaled_err(Ag, Ao) <= 1e-12
+    rg = res.double().cpu().numpy()
+    assert np.abs(rg - ro).max() <= 1e-12 * np.abs(ro).max()
+    # cells of problem k own only DoFs of problem k
+    owner = np.full(nd, -1)
+    c0 = 0
+    for k, n in enumerate(sides):
+        dofs = np.unique(cd[c0:c0 + 2 * n * n])
+        assert (owner[dofs] == -1).all()
+        owner[dofs] = k
+        c0 += 2 * n * n
+    coo = Ag.tocoo()
+    assert (owner[coo.row] == owner[coo.col]).all()
+    x = solve.solve_newton_step(Ag, rg)
+    c0 = 0
+    for k, n in enumerate(sides):
+        Ak, rk, cdk, ndk, _ = darcy_oracle(ms[k], kap[c0:c0 + 2 * n * n], f_cell=np.ones(2 * n * n))
+        xk = solve.solve_newton_step(Ak, rk)
+        # the union numbers problem k's DoFs in the same relative order
+        glob = np.unique(cd[c0:c0 + 2 * n * n])
+        loc = np.empty(ndk, dtype=np.int64)
+        loc[cdk.ravel()] = cd[c0:c0 + 2 * n * n].ravel()
+        np.testing.assert_allclose(x[loc], xk, rtol=1e-9, atol=1e-12 * np.abs(xk).max())
+        assert len(glob) == ndk
+        c0 += 2 * n * n
+
+
+def test_darcy_chunk_table_and_kernels_agree(cuda_lib):
+    """The chunk row table against a host recomputation, and the two kernels'
+    FP32 values against each other on a 16^3 x 6 mesh with a random field."""
+    m = mesh_gen.cube(16)
+    T = m["blocks"][-1][1].shape[0]
+    rng = np.random.default_rng(11)
+    kappa = np.exp(rng.normal(0.0, 2.0, T))
+    f_cell = rng.normal(0.0, 1.0, T)
+    sp, A, res = assemble_gpu(m, kappa, f_cell, torch.float32, True)
+    pairs = A.pairs.cpu().numpy()
+    p_base = sp.field_offsets["p"]
+    first_cell = pairs[:p_base, 0] // sp.n_loc
+    K = nf._lib.DARCY_CHUNK_CELLS
+    want = np.searchsorted(first_cell, np.arange(0, -(-T // K) + 1) * K, side="left")
+    np.testing.assert_array_equal(A.chunk_rows.cpu().numpy(), want)
+    v_chunks = A.values.clone()
+    r_chunks = res.clone()
+    wf = nf.LaplaceDualWeakForm(sp)
+    wf.use_chunks = False
+    wf.functions = {"kappa": kappa, "rhs": f_cell}
+    wf.assemble(A, res)
+    torch.cuda.synchronize()
+    scale = torch.maximum(v_chunks.abs(), A.values.abs()).clamp_min(1e-30)
+    assert ((v_chunks - A.values).abs() / scale).max().item() <= 2e-6
+    assert ((r_chunks - res).abs().max() / res.abs().max()).item() <= 2e-6
