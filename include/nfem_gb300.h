@@ -166,6 +166,13 @@ int nfem_pattern_pairs(const int32_t* inc_ptr, const int32_t* inc, const uint32_
                        int64_t n_rows, int32_t* pairs, uint32_t* pair_codes,
                        int32_t* dev_status, void* stream);
 
+/* Copies `bytes` from src to dst with a kernel (16-byte vectors when both are
+ * 16-byte aligned).  Either pointer may be pinned host memory mapped into the
+ * device address space (cudaHostAlloc), so results reach the host without a
+ * copy engine; pageable host memory is refused (NFEM_ERR_INVALID_ARG).  No
+ * reference counterpart (host I/O helper). */
+int nfem_copy_bytes(const void* src, void* dst, size_t bytes, void* stream);
+
 /* Cells per entry of the cell-chunk row table of the mixed Darcy layout. */
 #define NFEM_DARCY_CHUNK_CELLS 256
 
@@ -267,13 +274,18 @@ int nfem_pattern_node_codes(const int32_t* cell_dofs, int64_t n_cells, int n_loc
                             int64_t row0, int64_t n_rows, const int32_t* inc_ptr,
                             const int32_t* inc, const int32_t* row_ptr, const int32_t* col_idx,
                             uint8_t* node_codes, int32_t* dev_status, void* stream);
+/* Workspace of nfem_elasticity_p2_assemble: the per-cell geometry
+ * (J^-1, lambda |det J|, mu |det J|, |det J|), 12 values of value_type per
+ * cell, evaluated once per cell before the node rows read it. */
+int nfem_elasticity_p2_workspace_bytes(int value_type, int64_t n_cells, size_t* bytes);
 int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
                                 const double* points, const float* points_split,
                                 const int32_t* cell_vertices, const void* lambda_,
                                 const void* mu, const void* force, const double* ref_S,
                                 const double* ref_m, const int32_t* inc_ptr, const int32_t* inc,
                                 const uint8_t* node_codes, const int32_t* row_ptr, void* values,
-                                void* rhs, int accumulate, int32_t* dev_status, void* stream);
+                                void* rhs, int accumulate, void* workspace,
+                                size_t workspace_bytes, int32_t* dev_status, void* stream);
 /* Replaces LEPrimalWeakFormBCDirichlet.evaluate_form
  * (src/weak_forms/le_primal_weak_form.py:131-177) with u_D = 0: adds
  * beta * int_F phi_a phi_b to every component's (a, b) entry of the boundary

@@ -94,6 +94,7 @@ _SIGS = {
     "nfem_darcy_rt1p0_assemble": ([_I, _I, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P, _P, _I,
                                    _P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P], _I),
     "nfem_pattern_darcy_chunks": ([_P, _I64, _I, _I64, _I64, _P, _P, _P], _I),
+    "nfem_copy_bytes": ([_P, _P, _SZ, _P], _I),
     "nfem_spmv": ([_I, _I64, _P, _P, _P, _P, _P, _P], _I),
     "nfem_residual_f64": ([_I64, _P, _P, _P, _P, _P, _P, _P], _I),
     "nfem_precond_setup": ([C.POINTER(Precond), C.POINTER(Csr), _P, _P], _I),
@@ -109,7 +110,8 @@ _SIGS = {
     "nfem_to_bf16": ([_I64, _P, _P, _P], _I),
     "nfem_pattern_node_codes": ([_P, _I64, _I, _I, _I64, _I64, _P, _P, _P, _P, _P, _P, _P], _I),
     "nfem_elasticity_p2_assemble": ([_I, _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_double),
-                                     C.POINTER(C.c_double), _P, _P, _P, _P, _P, _P, _I, _P, _P], _I),
+                                     C.POINTER(C.c_double), _P, _P, _P, _P, _P, _P, _I, _P, _SZ, _P, _P], _I),
+    "nfem_elasticity_p2_workspace_bytes": ([_I, _I64, C.POINTER(C.c_size_t)], _I),
     "nfem_elasticity_p2_penalty": ([_I, _I64, _P, _P, _P, C.c_double, C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), _P, _P, _P, _P, _P], _I),
     "nfem_cosserat_assemble": ([_I, _I64, _I64, _I64, _P, _P, _P, _P, C.POINTER(C.c_double), _P,

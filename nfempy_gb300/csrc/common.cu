@@ -260,9 +260,68 @@ __global__ void split_points_kernel(const double* __restrict__ p, int64_t n, flo
   }
 }
 
+// ---------------------------------------------------------------- copies
+// Copy through the SMs (16-byte vectors, grid-stride).  Between device memory
+// and pinned host memory this runs over the chip-to-chip link with every SM
+// issuing loads and stores, rather than through one copy engine.
+__global__ void copy16_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, int64_t n16) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n16; i += int64_t(gridDim.x) * blockDim.x)
+    dst[i] = src[i];
+}
+
+__global__ void copy1_kernel(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    dst[i] = src[i];
+}
+
 }  // namespace nfem
 
 using namespace nfem;
+
+// Device-side address of p: device memory as is, pinned host memory through
+// its mapping; anything else (pageable host memory) is refused.
+static int device_address(const void* p, const void** out) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return NFEM_ERR_INVALID_ARG;
+  }
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+    *out = p;
+    return NFEM_OK;
+  }
+  if (at.type == cudaMemoryTypeHost && at.devicePointer) {
+    *out = at.devicePointer;
+    return NFEM_OK;
+  }
+  return NFEM_ERR_INVALID_ARG;
+}
+
+extern "C" int nfem_copy_bytes(const void* src_, void* dst_, size_t bytes, void* stream_) {
+  if (bytes == 0) return NFEM_OK;
+  if (!src_ || !dst_) return NFEM_ERR_INVALID_ARG;
+  const void* src = nullptr;
+  const void* dstc = nullptr;
+  if (device_address(src_, &src) != NFEM_OK || device_address(dst_, &dstc) != NFEM_OK) return NFEM_ERR_INVALID_ARG;
+  void* dst = const_cast<void*>(dstc);
+  cudaStream_t stream = (cudaStream_t)stream_;
+  const uintptr_t a = reinterpret_cast<uintptr_t>(src), b = reinterpret_cast<uintptr_t>(dst);
+  if (((a | b) & 15) == 0) {
+    const int64_t n16 = int64_t(bytes / 16);
+    if (n16 > 0)
+      copy16_kernel<<<grid_for(n16, 256, 4), 256, 0, stream>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst),
+                                                              n16);
+    const int64_t tail = int64_t(bytes - size_t(n16) * 16);
+    if (tail > 0)
+      copy1_kernel<<<1, 32, 0, stream>>>(static_cast<const uint8_t*>(src) + n16 * 16,
+                                         static_cast<uint8_t*>(dst) + n16 * 16, tail);
+  } else {
+    copy1_kernel<<<grid_for(int64_t(bytes), 256, 4), 256, 0, stream>>>(static_cast<const uint8_t*>(src),
+                                                                      static_cast<uint8_t*>(dst), int64_t(bytes));
+  }
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
 
 extern "C" int nfem_abi_version(void) { return 1; }
 

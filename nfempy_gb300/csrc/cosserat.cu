@@ -108,8 +108,15 @@ __device__ __forceinline__ void cos_edges<float>(const CosParams& p, int32_t c, 
 // 3 x 3 block between local nodes a (row) and b (column); node kinds:
 // 0..3 s-faces, 4..7 m-faces, 8 u, 9 t.
 template <typename T>
-__device__ __forceinline__ void cos_block(const CosParams& p, const T (&J)[3][3], T adet, uint32_t m, int a, int b,
-                                          T (&K)[3][3]) {
+struct CosTables {
+  T Psi[4 * 4 * 9];
+  T mhat[12];
+  T divhat[4];
+};
+
+template <typename T>
+__device__ __forceinline__ void cos_block(const CosParams& p, const CosTables<T>& tb, const T (&J)[3][3], T adet,
+                                          uint32_t m, int a, int b, T (&K)[3][3]) {
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -121,13 +128,13 @@ __device__ __forceinline__ void cos_block(const CosParams& p, const T (&J)[3][3]
   const T sgb = ((m >> fb) & 1u) ? T(-1) : T(1);
   if ((as && bs) || (am && bm)) {
     // Phi = sga sgb J Psihat_ab J^T / |det|
-    const double* Ps = c_Psi + (fa * 4 + fb) * 9;
+    const T* Ps = tb.Psi + (fa * 4 + fb) * 9;
     T PJ[3][3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
       for (int q = 0; q < 3; ++q)
-        PJ[k][q] = T(Ps[k * 3 + 0]) * J[q][0] + T(Ps[k * 3 + 1]) * J[q][1] + T(Ps[k * 3 + 2]) * J[q][2];
+        PJ[k][q] = Ps[k * 3 + 0] * J[q][0] + Ps[k * 3 + 1] * J[q][1] + Ps[k * 3 + 2] * J[q][2];
     T Phi[3][3];
     const T sc = sga * sgb / adet;
 #pragma unroll
@@ -151,7 +158,7 @@ __device__ __forceinline__ void cos_block(const CosParams& p, const T (&J)[3][3]
     T v[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
-      v[k] = sg * (J[k][0] * T(c_mhat[f * 3 + 0]) + J[k][1] * T(c_mhat[f * 3 + 1]) + J[k][2] * T(c_mhat[f * 3 + 2]));
+      v[k] = sg * (J[k][0] * tb.mhat[f * 3 + 0] + J[k][1] * tb.mhat[f * 3 + 1] + J[k][2] * tb.mhat[f * 3 + 2]);
     T M[3][3] = {{T(0), v[2], -v[1]}, {-v[2], T(0), v[0]}, {v[1], -v[0], T(0)}};
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -160,7 +167,7 @@ __device__ __forceinline__ void cos_block(const CosParams& p, const T (&J)[3][3]
   } else if ((au && bs) || (as && bu) || (at && bm) || (am && bt)) {
     const int f = (au || at) ? fb : fa;
     const T sg = (au || at) ? sgb : sga;
-    const T val = sg * T(c_divhat[f]);
+    const T val = sg * tb.divhat[f];
 #pragma unroll
     for (int c = 0; c < 3; ++c) K[c][c] = val;
   }
@@ -169,7 +176,14 @@ __device__ __forceinline__ void cos_block(const CosParams& p, const T (&J)[3][3]
 template <typename T>
 __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const CosParams p) {
   constexpr int IMG = 3 * 3 * kCosDegMax;
-  __shared__ T img[kCosWarps][2][IMG];
+  constexpr int IMGP = IMG + 3;  // odd pad: the two group images in different banks
+  __shared__ T img[kCosWarps][2][IMGP];
+  // reference tables read with per-lane indices: shared, not constant, memory
+  __shared__ CosTables<T> tb;
+  for (int i = threadIdx.x; i < 144; i += blockDim.x) tb.Psi[i] = T(c_Psi[i]);
+  if (threadIdx.x < 12) tb.mhat[threadIdx.x] = T(c_mhat[threadIdx.x]);
+  if (threadIdx.x < 4) tb.divhat[threadIdx.x] = T(c_divhat[threadIdx.x]);
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / 10, b = lane - 10 * (lane / 10);
   const T* force = static_cast<const T*>(p.force);
@@ -204,7 +218,7 @@ __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const Cos
       const T adet = det < T(0) ? -det : det;
       const uint32_t m = __ldg(p.sign + c);
       T K[3][3];
-      cos_block<T>(p, J, adet, m, a, b, K);
+      cos_block<T>(p, tb, J, adet, m, a, b, K);
       T* im = img[warp][g];
 #pragma unroll
       for (int i = 0; i < 3; ++i)

@@ -249,6 +249,52 @@ __device__ __forceinline__ void element_row(const DarcyParams& p, const Incidenc
   }
 }
 
+// The flux x flux block of a cell's element matrix, rows a < NF at
+// M[a * 4 + b] (the same expressions as element_row, evaluated once for the
+// whole matrix), and the residual entry of its pressure row.
+template <typename T, int DIM, int SRC>
+__device__ __forceinline__ T cell_matrix(const DarcyParams& p, const Incidence<T, DIM>& x, T* M) {
+  constexpr int NF = DIM + 1;
+  using C = DarcyConst<T, DIM>;
+  T sg[NF];
+#pragma unroll
+  for (int i = 0; i < NF; ++i) sg[i] = ((x.m >> i) & 1u) ? -C::sigma(i) : C::sigma(i);
+  T G[DIM][DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) G[i][j] = x.J[i][0] * x.J[j][0] + x.J[i][1] * x.J[j][1] + x.J[i][2] * x.J[j][2];
+  const T det = abs_det<T, DIM>(x.J, G);
+  if (!(det > T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+  T R[DIM];
+  T trG = T(0), sumG = T(0);
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
+    R[i] = T(0);
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) R[i] += G[i][j];
+    trG += G[i][i];
+    sumG += R[i];
+  }
+  const T tgs = (trG + sumG) * T(C::f2);
+  const T scale = T(C::kappa2) / (x.kap * det);
+#pragma unroll
+  for (int a = 0; a < NF; ++a) {
+    const T gma = a > 0 ? R[a - 1] * T(C::f1) : T(0);
+#pragma unroll
+    for (int b = a; b < NF; ++b) {
+      const T gmb = b > 0 ? R[b - 1] * T(C::f1) : T(0);
+      const T gv = (a > 0 && b > 0) ? G[a - 1][b - 1] * T(C::area) : T(0);
+      const T v = scale * sg[a] * sg[b] * (tgs - gma - gmb + gv);
+      M[a * 4 + b] = v;
+      if (b != a) M[b * 4 + a] = v;
+    }
+  }
+  if constexpr (SRC == NFEM_COEF_CELL) return -det * T(C::area) * x.src;
+  if constexpr (SRC == NFEM_COEF_QPOINT) return -det * x.src;
+  return T(0);
+}
+
 struct RowHead {
   int2 pr;
   uint2 cd;
@@ -385,36 +431,108 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, NFEM_DARCY_MIN_BLOCKS) darcy
 // Cell-chunk variant of the same assembly.  Rows are numbered by first
 // appearance, so the flux rows whose first incidence lies in a run of K
 // consecutive cells are themselves consecutive (the chunk row table), and so
-// are the pressure rows of those cells.  A block (1) evaluates the element
-// matrices of its K cells once, with coalesced loads of the per-cell inputs,
-// into shared memory, (2) writes the K pressure rows and (3) the chunk's
-// flux rows from there.  Only a second incidence in a cell outside the chunk
-// (a neighbour in a later row or layer of the mesh) is evaluated from the
-// vertices as in the row-owner kernel.  Row images are staged per warp and
-// stored coalesced as there; each value is written once.
+// are the pressure rows of those cells.  A block, per chunk:
+//  (1) evaluates the element matrices of its K cells once, with coalesced
+//      loads of the per-cell inputs, into shared memory;
+//  (2) queues the second incidences of its flux rows that lie in a cell
+//      outside the chunk (a neighbour in a later row or layer of the mesh)
+//      and (3) evaluates them densely, one per thread, from the vertices;
+//  (4) writes the chunk's pressure rows and flux rows from shared memory,
+//      staged per warp and stored coalesced as in the row-owner kernel.
+// Each value is written once; the queue order does not affect any value.
 constexpr int kChunkThreads = 256;
 constexpr int kChunkWarps = kChunkThreads / 32;
+constexpr int kMStride = 17;  // element matrix words per cell: odd, so cells spread over the banks
 
-template <typename T, int DIM>
+template <typename T>
 struct ChunkSmem {
-  T* M;           // [K][4][4] element matrix rows (flux x flux block)
-  T* rp;          // [K] residual entry of the cell's pressure row
-  uint32_t* sg;   // [K] orientation mask of the cell
-  T* stage;       // [warps][32 * kDarcyMaxRow]
+  T* M;             // [K][kMStride]: rows a < NF of the flux x flux block at a * 4 + b
+  T* rp;            // [K] residual entry of the cell's pressure row
+  uint32_t* sg;     // [K] orientation mask
+  T* qv;            // [4K][NLOC] values of queued (out-of-chunk) incidences
+  int32_t* qocc;    // [4K] their occurrences (cell * NLOC + local)
+  int16_t* slot;    // [4K] queue slot of each flux row of the chunk, or -1
+  T* stage;         // [warps][32 * kDarcyMaxRow]
+  int32_t* count;   // queue length
 };
 
 template <typename T>
-static size_t chunk_smem_bytes(int K) {
-  return size_t(K) * 16 * sizeof(T) + size_t(K) * sizeof(T) + size_t(K) * sizeof(uint32_t) +
-         size_t(kChunkWarps) * 32 * kDarcyMaxRow * sizeof(T) + 16;
+static size_t chunk_smem_bytes(int K, int nloc) {
+  size_t b = 0;
+  b += size_t(K) * kMStride * sizeof(T);
+  b += size_t(K) * sizeof(T) + size_t(K) * sizeof(uint32_t);
+  b += size_t(4 * K) * nloc * sizeof(T) + size_t(4 * K) * sizeof(int32_t) + size_t(4 * K) * sizeof(int16_t);
+  b = (b + 15) & ~size_t(15);
+  b += size_t(kChunkWarps) * 32 * kDarcyMaxRow * sizeof(T) + 16;
+  return b;
 }
 
-// rows [first, last) of the chunk whose cells are [c0, c0 + nk)
-template <typename T, int DIM, int SRC>
-__device__ __forceinline__ void chunk_rows_pass(const DarcyParams& p, const ChunkSmem<T, DIM>& sm, int64_t first,
-                                                int64_t last, int64_t c0, int64_t nk) {
+template <typename T, int DIM>
+__device__ __forceinline__ ChunkSmem<T> chunk_carve(unsigned char* base, int K) {
+  constexpr int NLOC = DIM + 2;
+  ChunkSmem<T> sm;
+  size_t o = 0;
+  sm.M = reinterpret_cast<T*>(base + o);
+  o += size_t(K) * kMStride * sizeof(T);
+  sm.rp = reinterpret_cast<T*>(base + o);
+  o += size_t(K) * sizeof(T);
+  sm.qv = reinterpret_cast<T*>(base + o);
+  o += size_t(4 * K) * NLOC * sizeof(T);
+  sm.sg = reinterpret_cast<uint32_t*>(base + o);
+  o += size_t(K) * sizeof(uint32_t);
+  sm.qocc = reinterpret_cast<int32_t*>(base + o);
+  o += size_t(4 * K) * sizeof(int32_t);
+  sm.slot = reinterpret_cast<int16_t*>(base + o);
+  o += size_t(4 * K) * sizeof(int16_t);
+  o = (o + 15) & ~size_t(15);
+  sm.stage = reinterpret_cast<T*>(base + o);
+  o += size_t(kChunkWarps) * 32 * kDarcyMaxRow * sizeof(T);
+  sm.count = reinterpret_cast<int32_t*>(base + o);
+  return sm;
+}
+
+// values of incidence (cell c, local a) from shared memory: the chunk's own
+// cells from the element matrices, the others from the queue
+template <typename T, int DIM>
+__device__ __forceinline__ void chunk_incidence(const DarcyParams& p, const ChunkSmem<T>& sm, int64_t lc, int64_t nk,
+                                                int a, int qslot, T (&v)[DIM + 2], T& rhs_val) {
   constexpr int NF = DIM + 1, NLOC = DIM + 2;
   using C = DarcyConst<T, DIM>;
+  if (qslot >= 0) {
+#pragma unroll
+    for (int b = 0; b < NLOC; ++b) v[b] = sm.qv[qslot * NLOC + b];
+    return;
+  }
+  if (lc < 0 || lc >= nk) {  // only a corrupted chunk table leads here
+    set_status(p.status, NFEM_ERR_PATTERN);
+#pragma unroll
+    for (int b = 0; b < NLOC; ++b) v[b] = T(0);
+    return;
+  }
+  const uint32_t m = sm.sg[lc];
+  if (a < NF) {
+    const T* Mr = sm.M + lc * kMStride + a * 4;
+#pragma unroll
+    for (int b = 0; b < NF; ++b) v[b] = Mr[b];
+    T sga = C::sigma(0);
+#pragma unroll
+    for (int i = 1; i < NF; ++i) sga = (a == i) ? C::sigma(i) : sga;
+    sga = ((m >> a) & 1u) ? -sga : sga;
+    v[NF] = -sga;
+  } else {
+#pragma unroll
+    for (int b = 0; b < NF; ++b) v[b] = ((m >> b) & 1u) ? -C::sigma(b) : C::sigma(b);
+    v[NF] = T(0);
+    rhs_val += sm.rp[lc];
+  }
+}
+
+// rows [first, last); flux rows (is_flux) find their second incidence's
+// values through the queue slots
+template <typename T, int DIM>
+__device__ __forceinline__ void chunk_rows_pass(const DarcyParams& p, const ChunkSmem<T>& sm, int64_t first,
+                                                int64_t last, int64_t c0, int64_t nk, bool is_flux) {
+  constexpr int NLOC = DIM + 2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* st = sm.stage + warp * 32 * kDarcyMaxRow;
   T* values = static_cast<T*>(p.values);
@@ -436,6 +554,7 @@ __device__ __forceinline__ void chunk_rows_pass(const DarcyParams& p, const Chun
       c[t] = on[t] ? occ[t] / NLOC : 0;
       a[t] = on[t] ? occ[t] - c[t] * NLOC : 0;
     }
+    const int q1 = (is_flux && valid && on[1]) ? int(sm.slot[r - first]) : -1;
     const int len = valid ? row_len_from_codes<NLOC>(h) : 0;
     int incl = len;
 #pragma unroll
@@ -462,30 +581,7 @@ __device__ __forceinline__ void chunk_rows_pass(const DarcyParams& p, const Chun
     for (int t = 0; t < 2; ++t) {
       if (on[t]) {
         T v[NLOC];
-        const int64_t lc = int64_t(c[t]) - c0;
-        if (lc >= 0 && lc < nk) {
-          const uint32_t m = sm.sg[lc];
-          if (a[t] < NF) {
-            const T* Mr = sm.M + lc * 16 + a[t] * 4;
-#pragma unroll
-            for (int b = 0; b < NF; ++b) v[b] = Mr[b];
-            T sga = C::sigma(0);
-#pragma unroll
-            for (int i = 1; i < NF; ++i) sga = (a[t] == i) ? C::sigma(i) : sga;
-            sga = ((m >> a[t]) & 1u) ? -sga : sga;
-            v[NF] = -sga;
-          } else {
-#pragma unroll
-            for (int b = 0; b < NF; ++b) v[b] = ((m >> b) & 1u) ? -C::sigma(b) : C::sigma(b);
-            v[NF] = T(0);
-            rhs_val += sm.rp[lc];
-          }
-        } else {
-          Incidence<T, DIM> x;
-          const bool geo = (a[t] < NF) || (SRC != 0);
-          load_incidence<T, DIM, SRC>(p, c[t], geo, x);
-          element_row<T, DIM, SRC>(p, x, a[t], geo, v, rhs_val);
-        }
+        chunk_incidence<T, DIM>(p, sm, int64_t(c[t]) - c0, nk, a[t], t == 1 ? q1 : -1, v, rhs_val);
         const uint32_t cd = code[t];
         const int at = a[t];
 #pragma unroll
@@ -516,42 +612,72 @@ __device__ __forceinline__ void chunk_rows_pass(const DarcyParams& p, const Chun
 
 template <typename T, int DIM, int SRC, int KC>
 __global__ void __launch_bounds__(kChunkThreads) darcy_cells_kernel(const DarcyParams p) {
-  constexpr int NF = DIM + 1;
+  constexpr int NF = DIM + 1, NLOC = DIM + 2;
   constexpr int K = KC * NFEM_DARCY_CHUNK_CELLS;
   extern __shared__ __align__(16) unsigned char dsm[];
-  ChunkSmem<T, DIM> sm;
-  sm.M = reinterpret_cast<T*>(dsm);
-  sm.rp = sm.M + K * 16;
-  sm.sg = reinterpret_cast<uint32_t*>(sm.rp + K);
-  sm.stage = reinterpret_cast<T*>(sm.sg + K);
+  const ChunkSmem<T> sm = chunk_carve<T, DIM>(dsm, K);
   const int64_t n_chunks = (p.n_cells + K - 1) / K;
   const int64_t n_table = (p.n_cells + NFEM_DARCY_CHUNK_CELLS - 1) / NFEM_DARCY_CHUNK_CELLS;
+  const int lane = threadIdx.x & 31;
   for (int64_t k = blockIdx.x; k < n_chunks; k += gridDim.x) {
     const int64_t c0 = k * K;
     const int64_t nk = min(int64_t(K), p.n_cells - c0);
+    const int32_t f0 = __ldg(p.chunk_rows + k * KC);
+    const int32_t f1 = __ldg(p.chunk_rows + min((k + 1) * KC, n_table));
+    if (threadIdx.x == 0) *sm.count = 0;
+    const bool rows_ok = f1 - f0 <= 4 * nk;  // every cell opens at most NF flux rows
+    if (!rows_ok && threadIdx.x == 0) set_status(p.status, NFEM_ERR_PATTERN);
     // (1) element matrices of the chunk's cells
     for (int i = threadIdx.x; i < nk; i += kChunkThreads) {
       Incidence<T, DIM> x;
       load_incidence<T, DIM, SRC>(p, int32_t(c0 + i), true, x);
-      T rp = T(0);
-#pragma unroll
-      for (int a = 0; a < NF; ++a) {
-        T v[DIM + 2];
-        element_row<T, DIM, SRC>(p, x, a, true, v, rp);
-#pragma unroll
-        for (int b = 0; b < NF; ++b) sm.M[i * 16 + a * 4 + b] = v[b];
-      }
-      T v[DIM + 2];
-      element_row<T, DIM, SRC>(p, x, NF, true, v, rp);
-      sm.rp[i] = rp;
+      T* Mi = sm.M + i * kMStride;
+      sm.rp[i] = cell_matrix<T, DIM, SRC>(p, x, Mi);
       sm.sg[i] = x.m;
     }
     __syncthreads();
-    // (2) pressure rows of the chunk's cells, (3) its flux rows
-    chunk_rows_pass<T, DIM, SRC>(p, sm, p.p_base + c0, p.p_base + c0 + nk, c0, nk);
-    const int32_t f0 = __ldg(p.chunk_rows + k * KC);
-    const int32_t f1 = __ldg(p.chunk_rows + min((k + 1) * KC, n_table));
-    chunk_rows_pass<T, DIM, SRC>(p, sm, f0, f1, c0, nk);
+    // (2) queue the out-of-chunk second incidences of the flux rows
+    if (rows_ok) {
+      for (int64_t r = f0 + threadIdx.x; r - threadIdx.x < f1; r += kChunkThreads) {
+        int32_t occ = -1;
+        if (r < f1) {
+          occ = __ldg(p.pairs + 2 * r + 1);
+          if (occ >= 0 && occ / NLOC < c0 + nk) occ = -1;
+        }
+        const unsigned want = __ballot_sync(0xffffffffu, occ >= 0);
+        int basis = 0;
+        if (lane == 0 && want) basis = atomicAdd(sm.count, __popc(want));
+        basis = __shfl_sync(0xffffffffu, basis, 0);
+        if (r < f1) {
+          int16_t q = -1;
+          if (occ >= 0) {
+            const int s = basis + __popc(want & ((1u << lane) - 1u));
+            sm.qocc[s] = occ;
+            q = int16_t(s);
+          }
+          sm.slot[r - f0] = q;
+        }
+      }
+    }
+    __syncthreads();
+    // (3) evaluate the queue densely
+    const int nq = *sm.count;
+    for (int i = threadIdx.x; i < nq; i += kChunkThreads) {
+      const int32_t occ = sm.qocc[i];
+      const int32_t c = occ / NLOC;
+      const int a = occ - c * NLOC;
+      Incidence<T, DIM> x;
+      const bool geo = (a < NF) || (SRC != 0);
+      load_incidence<T, DIM, SRC>(p, c, geo, x);
+      T v[NLOC], unused = T(0);
+      element_row<T, DIM, SRC>(p, x, a, geo, v, unused);
+#pragma unroll
+      for (int b = 0; b < NLOC; ++b) sm.qv[i * NLOC + b] = v[b];
+    }
+    __syncthreads();
+    // (4) pressure rows of the chunk's cells, then its flux rows
+    chunk_rows_pass<T, DIM>(p, sm, p.p_base + c0, p.p_base + c0 + nk, c0, nk, false);
+    if (rows_ok) chunk_rows_pass<T, DIM>(p, sm, f0, f1, c0, nk, true);
     __syncthreads();
   }
 }
@@ -576,10 +702,10 @@ static int launch_darcy_src(const DarcyParams& p, cudaStream_t stream) {
 }
 
 #ifndef NFEM_DARCY_CHUNK_KC
-#define NFEM_DARCY_CHUNK_KC 2
+#define NFEM_DARCY_CHUNK_KC 1
 #endif
-// table entries per chunk: FP32 chunks of 512 cells (44 KB of shared memory),
-// FP64 chunks of 256 cells (43 KB)
+// table entries per chunk: chunks of 256 cells (FP32: 63 KB of shared
+// memory, FP64: 103 KB)
 template <typename T>
 struct ChunkKC {
   static constexpr int value = NFEM_DARCY_CHUNK_KC;
@@ -593,7 +719,7 @@ template <typename T, int DIM, int SRC>
 static int launch_darcy_chunks(const DarcyParams& p, cudaStream_t stream) {
   constexpr int KC = ChunkKC<T>::value;
   const int K = KC * NFEM_DARCY_CHUNK_CELLS;
-  const size_t smem = chunk_smem_bytes<T>(K);
+  const size_t smem = chunk_smem_bytes<T>(K, DIM + 2);
   static const int per_sm = [smem] {
     int n = 0;
     if (smem > 48 * 1024 &&

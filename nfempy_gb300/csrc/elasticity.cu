@@ -61,6 +61,8 @@ static int upload_tables(const double* S, const double* m, const double* Mf, cud
 
 struct ElasParams {
   int64_t n_nodes;
+  int64_t n_cells;
+  void* geom;  // [n_cells][12]: J^-1 (row-major, 9), lambda |det J|, mu |det J|, |det J|
   int64_t row0;  // first row of the space (dof_shift)
   const double* points;
   const float* split;
@@ -106,14 +108,79 @@ __device__ __forceinline__ void tet_edges<float>(const ElasParams& p, int32_t c,
   }
 }
 
+// Per-cell geometry, once per cell (every cell is read by the rows of its
+// ten nodes): J^-1, lambda |det J|, mu |det J|, |det J|.
+template <typename T>
+__global__ void elas_geom_kernel(const ElasParams p) {
+  const T* lam = static_cast<const T*>(p.lam);
+  const T* mu = static_cast<const T*>(p.mu);
+  T* out = static_cast<T*>(p.geom);
+  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < p.n_cells;
+       c += int64_t(gridDim.x) * blockDim.x) {
+    T J[3][3];
+    tet_edges<T>(p, int32_t(c), J);
+    const T c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const T c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    const T c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    const T det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    if (!(det != T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+    const T id = T(1) / det;
+    const T adet = det < T(0) ? -det : det;
+    T g[12];
+    g[0] = c00 * id;
+    g[3] = c01 * id;
+    g[6] = c02 * id;
+    g[1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+    g[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+    g[7] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+    g[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+    g[5] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+    g[8] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+    g[9] = __ldg(lam + c) * adet;
+    g[10] = __ldg(mu + c) * adet;
+    g[11] = adet;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) out[c * 12 + k] = g[k];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void load_geom(const ElasParams& p, int32_t c, T (&g)[12]);
+template <>
+__device__ __forceinline__ void load_geom<float>(const ElasParams& p, int32_t c, float (&g)[12]) {
+  const float4* q = static_cast<const float4*>(p.geom) + int64_t(c) * 3;
+  const float4 a = __ldg(q), b = __ldg(q + 1), d = __ldg(q + 2);
+  g[0] = a.x; g[1] = a.y; g[2] = a.z; g[3] = a.w;
+  g[4] = b.x; g[5] = b.y; g[6] = b.z; g[7] = b.w;
+  g[8] = d.x; g[9] = d.y; g[10] = d.z; g[11] = d.w;
+}
+template <>
+__device__ __forceinline__ void load_geom<double>(const ElasParams& p, int32_t c, double (&g)[12]) {
+  const double2* q = static_cast<const double2*>(p.geom) + int64_t(c) * 6;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const double2 v = __ldg(q + k);
+    g[2 * k] = v.x;
+    g[2 * k + 1] = v.y;
+  }
+}
+
 template <typename T, int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasParams p) {
   constexpr int IMG = 3 * 3 * kElasDegMax;  // 3 rows x 3 deg_max columns
-  __shared__ T img[WARPS][3][IMG];
+  // an odd pad puts the three group images in different banks (every group
+  // writes its row node's own column at the same offset)
+  constexpr int IMGP = IMG + 3;
+  __shared__ T img[WARPS][3][IMGP];
+  // reference tables read with per-lane indices (a, b): shared memory serves
+  // those in one pass, the constant cache would serialise them
+  __shared__ T sS[10 * 10 * 9];
+  __shared__ T sm_m[10];
+  for (int i = threadIdx.x; i < 900; i += blockDim.x) sS[i] = T(c_S[i]);
+  if (threadIdx.x < 10) sm_m[threadIdx.x] = T(c_m[threadIdx.x]);
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / 10, b = lane - 10 * (lane / 10);
-  const T* lam = static_cast<const T*>(p.lam);
-  const T* mu = static_cast<const T*>(p.mu);
   const T* force = static_cast<const T*>(p.force);
   T* values = static_cast<T*>(p.values);
   T* rhs = static_cast<T*>(p.rhs);
@@ -139,42 +206,27 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
         const int32_t occ = __ldg(p.inc + k);
         const int32_t c = occ / 30;
         const int a = (occ - c * 30) / 3;
-        const int pos = __ldg(p.codes + int64_t(k) * 16 + b);
-        T J[3][3];
-        tet_edges<T>(p, c, J);
-        // cofactors: Jinv = adj(J) / det
-        const T c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-        const T c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-        const T c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-        const T det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-        if (!(det != T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
-        const T id = T(1) / det;
-        T Ji[3][3];  // Ji[k][p] = (J^-1)_{kp}
-        Ji[0][0] = c00 * id;
-        Ji[1][0] = c01 * id;
-        Ji[2][0] = c02 * id;
-        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-        const T adet = det < T(0) ? -det : det;
-        const double* S = c_S + (a * 10 + b) * 9;
-        // A = |det| Ji^T S Ji
+        // node position inside the row; the clamp keeps a corrupted code in
+        // this node's image (a valid one is < len / 3)
+        const int pos = min(int(__ldg(p.codes + int64_t(k) * 16 + b)), len / 3 - 1);
+        T gm[12];
+        load_geom<T>(p, c, gm);
+        const T(&Ji)[12] = gm;  // Ji[k * 3 + q] = (J^-1)_{kq}
+        const T* S = sS + (a * 10 + b) * 9;
+        // A / |det| = Ji^T S Ji; lambda |det| and mu |det| carry the |det|
         T SJ[3][3];
 #pragma unroll
         for (int kk = 0; kk < 3; ++kk)
 #pragma unroll
           for (int q = 0; q < 3; ++q)
-            SJ[kk][q] = T(S[kk * 3 + 0]) * Ji[0][q] + T(S[kk * 3 + 1]) * Ji[1][q] + T(S[kk * 3 + 2]) * Ji[2][q];
+            SJ[kk][q] = S[kk * 3 + 0] * Ji[0 * 3 + q] + S[kk * 3 + 1] * Ji[1 * 3 + q] + S[kk * 3 + 2] * Ji[2 * 3 + q];
         T A[3][3];
 #pragma unroll
         for (int pp = 0; pp < 3; ++pp)
 #pragma unroll
           for (int q = 0; q < 3; ++q)
-            A[pp][q] = adet * (Ji[0][pp] * SJ[0][q] + Ji[1][pp] * SJ[1][q] + Ji[2][pp] * SJ[2][q]);
-        const T lc = __ldg(lam + c), mc = __ldg(mu + c);
+            A[pp][q] = Ji[0 * 3 + pp] * SJ[0][q] + Ji[1 * 3 + pp] * SJ[1][q] + Ji[2 * 3 + pp] * SJ[2][q];
+        const T lc = gm[9], mc = gm[10], adet = gm[11];
         const T tr = A[0][0] + A[1][1] + A[2][2];
         T* im = img[warp][g];
 #pragma unroll
@@ -182,12 +234,11 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
 #pragma unroll
           for (int j = 0; j < 3; ++j) {
             const T kij = (i == j ? mc * tr : T(0)) + mc * A[j][i] + lc * A[i][j];
-            const int idx = min(i * len + 3 * pos + j, IMG - 1);
-            im[idx] += kij;
+            im[i * len + 3 * pos + j] += kij;
           }
         if (force && b == 0) {
 #pragma unroll
-          for (int i = 0; i < 3; ++i) rhs_acc[i] += adet * T(c_m[a]) * __ldg(force + int64_t(c) * 3 + i);
+          for (int i = 0; i < 3; ++i) rhs_acc[i] += adet * sm_m[a] * __ldg(force + int64_t(c) * 3 + i);
         }
       }
       __syncwarp();
@@ -302,15 +353,22 @@ extern "C" int nfem_pattern_node_codes(const int32_t* cell_dofs, int64_t n_cells
   return NFEM_OK;
 }
 
+extern "C" int nfem_elasticity_p2_workspace_bytes(int value_type, int64_t n_cells, size_t* bytes) {
+  if (!bytes || n_cells < 0 || (value_type != NFEM_F64 && value_type != NFEM_F32)) return NFEM_ERR_INVALID_ARG;
+  *bytes = size_t(n_cells) * 12 * (value_type == NFEM_F64 ? sizeof(double) : sizeof(float));
+  return NFEM_OK;
+}
+
 extern "C" int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
                                            const double* points, const float* points_split,
                                            const int32_t* cell_vertices, const void* lambda_, const void* mu,
                                            const void* force, const double* ref_S, const double* ref_m,
                                            const int32_t* inc_ptr, const int32_t* inc, const uint8_t* node_codes,
                                            const int32_t* row_ptr, void* values, void* rhs, int accumulate,
-                                           int32_t* dev_status, void* stream_) {
-  (void)n_cells;
+                                           void* workspace, size_t workspace_bytes, int32_t* dev_status,
+                                           void* stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;
+  if (n_cells < 0) return NFEM_ERR_INVALID_ARG;
   if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n_nodes < 0 || row0 < 0) return NFEM_ERR_INVALID_ARG;
   if (n_nodes == 0) return NFEM_OK;
   if (!cell_vertices || !lambda_ || !mu || !ref_S || !ref_m || !inc_ptr || !inc || !node_codes || !row_ptr ||
@@ -339,6 +397,15 @@ extern "C" int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int6
   p.rhs = rhs;
   p.accumulate = accumulate != 0;
   p.status = dev_status;
+  const size_t vb = value_type == NFEM_F64 ? sizeof(double) : sizeof(float);
+  if (!workspace || workspace_bytes < size_t(n_cells) * 12 * vb || (reinterpret_cast<uintptr_t>(workspace) & 15))
+    return NFEM_ERR_WORKSPACE;
+  p.n_cells = n_cells;
+  p.geom = workspace;
+  if (value_type == NFEM_F64)
+    elas_geom_kernel<double><<<grid_for(n_cells, 256), 256, 0, stream>>>(p);
+  else
+    elas_geom_kernel<float><<<grid_for(n_cells, 256), 256, 0, stream>>>(p);
   if (value_type == NFEM_F64) {
     elasticity_rows_kernel<double, kElasWarps64>
         <<<grid_for(ceil_div(n_nodes, kElasWarps64), 1, 8), 32 * kElasWarps64, 0, stream>>>(p);
