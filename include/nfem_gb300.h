@@ -174,7 +174,7 @@ int nfem_pattern_pairs(const int32_t* inc_ptr, const int32_t* inc, const uint32_
 int nfem_copy_bytes(const void* src, void* dst, size_t bytes, void* stream);
 
 /* Cells per entry of the cell-chunk row table of the mixed Darcy layout. */
-#define NFEM_DARCY_CHUNK_CELLS 256
+#define NFEM_DARCY_CHUNK_CELLS 32
 
 /* Cell-chunk row table for nfem_darcy_rt1p0_assemble: chunk_rows
  * [ceil(n_cells / NFEM_DARCY_CHUNK_CELLS) + 1], entry k = the first flux row
@@ -220,10 +220,10 @@ int nfem_points_split(const double* points, int64_t n_points, float* points_spli
  * and residual); accumulate != 0 adds to them (setValue(addv=True)).  Each CSR value and residual entry is written once
  * (no atomics, deterministic).  chunk_rows (optional, from
  * nfem_pattern_darcy_chunks with the same p_base) selects the cell-chunk
- * kernel: each block evaluates the element matrices of a run of cells once
- * into shared memory and writes the rows whose first incidence lies there;
- * NULL selects the row-owner kernel, which evaluates every incidence of a row
- * on its own.  Both give the same values. */
+ * kernel: each warp evaluates the element matrices of 32 consecutive cells
+ * once and writes the rows whose first incidence lies there; NULL selects
+ * the row-owner kernel, which evaluates every incidence of a row on its own.
+ * Both give the same values up to rounding. */
 int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t n_rows,
                               const double* points, const float* points_split,
                               const int32_t* cell_vertices, const int32_t* flux_dofs,
@@ -268,8 +268,10 @@ int nfem_darcy_l2_error(int dim, int64_t n_cells, const double* points,
  * field, 3 components, DoF = row0 + 3 * node + component.  lambda and mu are
  * per cell, force per cell [n_cells, 3] or NULL.  ref_S [10*10*3*3]
  * (int dhat_k phihat_a dhat_l phihat_b) and ref_m [10] (int phihat_a) are the
- * exact reference-tetrahedron tables (host arrays).  Row owner, each value
- * written once, deterministic. */
+ * exact reference-tetrahedron tables (host arrays).  max_node_degree = the
+ * largest number of node columns of any node row (row length / 3; <= 255),
+ * or 0 for the library bound of 96: it sizes the shared-memory row images.
+ * Row owner, each value written once, deterministic. */
 int nfem_pattern_node_codes(const int32_t* cell_dofs, int64_t n_cells, int n_loc, int n_comp,
                             int64_t row0, int64_t n_rows, const int32_t* inc_ptr,
                             const int32_t* inc, const int32_t* row_ptr, const int32_t* col_idx,
@@ -283,9 +285,10 @@ int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int64_t n_nodes
                                 const int32_t* cell_vertices, const void* lambda_,
                                 const void* mu, const void* force, const double* ref_S,
                                 const double* ref_m, const int32_t* inc_ptr, const int32_t* inc,
-                                const uint8_t* node_codes, const int32_t* row_ptr, void* values,
-                                void* rhs, int accumulate, void* workspace,
-                                size_t workspace_bytes, int32_t* dev_status, void* stream);
+                                const uint8_t* node_codes, const int32_t* row_ptr,
+                                int max_node_degree, void* values, void* rhs, int accumulate,
+                                void* workspace, size_t workspace_bytes, int32_t* dev_status,
+                                void* stream);
 /* Replaces LEPrimalWeakFormBCDirichlet.evaluate_form
  * (src/weak_forms/le_primal_weak_form.py:131-177) with u_D = 0: adds
  * beta * int_F phi_a phi_b to every component's (a, b) entry of the boundary

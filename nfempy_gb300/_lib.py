@@ -17,7 +17,7 @@ NFEM_F64 = 0
 NFEM_F32 = 1
 NFEM_BF16 = 2
 COEF_NONE, COEF_CELL, COEF_QPOINT = 0, 1, 2
-DARCY_CHUNK_CELLS = 256  # NFEM_DARCY_CHUNK_CELLS
+DARCY_CHUNK_CELLS = 32  # NFEM_DARCY_CHUNK_CELLS
 
 STATUS_NAMES = {
     0: "NFEM_OK", 1: "NFEM_ERR_INVALID_ARG", 2: "NFEM_ERR_CUDA", 3: "NFEM_ERR_WORKSPACE",
@@ -110,7 +110,7 @@ _SIGS = {
     "nfem_to_bf16": ([_I64, _P, _P, _P], _I),
     "nfem_pattern_node_codes": ([_P, _I64, _I, _I, _I64, _I64, _P, _P, _P, _P, _P, _P, _P], _I),
     "nfem_elasticity_p2_assemble": ([_I, _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_double),
-                                     C.POINTER(C.c_double), _P, _P, _P, _P, _P, _P, _I, _P, _SZ, _P, _P], _I),
+                                     C.POINTER(C.c_double), _P, _P, _P, _P, _I, _P, _P, _I, _P, _SZ, _P, _P], _I),
     "nfem_elasticity_p2_workspace_bytes": ([_I, _I64, C.POINTER(C.c_size_t)], _I),
     "nfem_elasticity_p2_penalty": ([_I, _I64, _P, _P, _P, C.c_double, C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), _P, _P, _P, _P, _P], _I),

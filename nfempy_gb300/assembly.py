@@ -90,6 +90,15 @@ class CSRMatrix:
         self.fresh = True
         self.check_status("pattern")
 
+    def max_node_degree(self):
+        """Largest number of node columns in a node row (row length / n_comp),
+        computed once from row_ptr."""
+        if getattr(self, "_max_node_degree", None) is None:
+            lens = self.row_ptr[1:].long() - self.row_ptr[:-1].long()
+            n_comp = getattr(self, "n_comp", 1) or 1
+            self._max_node_degree = int(-(-int(lens.max().item()) // n_comp)) if lens.numel() else 1
+        return self._max_node_degree
+
     def with_dtype(self, dtype):
         """A matrix with the same pattern (index arrays shared) and its own values."""
         other = object.__new__(CSRMatrix)
@@ -507,9 +516,9 @@ class LEPrimalWeakForm(WeakForm):
         _lib.call("nfem_elasticity_p2_assemble", vt, sp.n_cells, sp.n_dof // 3, sp.dof_shift, _lib.ptr(sp.points),
                   _lib.ptr(sp.points_split), _lib.ptr(sp.cells), _lib.ptr(lam), _lib.ptr(mu), _lib.ptr(f),
                   S.ctypes.data_as(dp), m.ctypes.data_as(dp), _lib.ptr(jacobian.inc_ptr), _lib.ptr(jacobian.inc),
-                  _lib.ptr(jacobian.node_codes), _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values),
-                  _lib.ptr(residual), int(accumulate), _lib.ptr(ws), ws.numel(), _lib.ptr(jacobian.status),
-                  _lib.stream_ptr(stream))
+                  _lib.ptr(jacobian.node_codes), _lib.ptr(jacobian.row_ptr), jacobian.max_node_degree(),
+                  _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate), _lib.ptr(ws), ws.numel(),
+                  _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
 
 
 class LEPrimalWeakFormBCDirichlet(WeakForm):

@@ -205,35 +205,50 @@ __global__ void bbox_partial_kernel(const double* __restrict__ p, int64_t n, dou
   }
 }
 
-// One thread: fold nb partial boxes (or, when nb == 0, the points themselves)
-// into the header record.  lo_scale = 2^(e - 34) with |point - c| < 2^e, so
-// |lo| <= 2^(e - 25) maps to |q| <= 512 (clamped to 511).
+// One block: fold nb partial boxes (or, when nb == 0, the points
+// themselves) into the header record.  lo_scale = 2^(e - 34) with
+// |point - c| < 2^e, so |lo| <= 2^(e - 25) maps to |q| <= 512 (clamped to
+// 511).
 __global__ void split_header_kernel(const double* __restrict__ part, int nb, const double* __restrict__ p,
                                     int64_t n, float4* __restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ double sh[6][256];
   double mn[3], mx[3];
   for (int k = 0; k < 3; ++k) {
     mn[k] = 1.0 / 0.0;
     mx[k] = -1.0 / 0.0;
   }
   if (nb > 0) {
-    for (int b = 0; b < nb; ++b)
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
       for (int k = 0; k < 3; ++k) {
         mn[k] = fmin(mn[k], part[b * 6 + k]);
         mx[k] = fmax(mx[k], part[b * 6 + 3 + k]);
       }
   } else {
-    for (int64_t i = 0; i < n; ++i)
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
       for (int k = 0; k < 3; ++k) {
         mn[k] = fmin(mn[k], p[i * 3 + k]);
         mx[k] = fmax(mx[k], p[i * 3 + k]);
       }
   }
+  for (int k = 0; k < 3; ++k) {
+    sh[k][threadIdx.x] = mn[k];
+    sh[3 + k][threadIdx.x] = mx[k];
+  }
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int k = 0; k < 3; ++k) {
+        sh[k][threadIdx.x] = fmin(sh[k][threadIdx.x], sh[k][threadIdx.x + w]);
+        sh[3 + k][threadIdx.x] = fmax(sh[3 + k][threadIdx.x], sh[3 + k][threadIdx.x + w]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
   float c[3];
   double ext = 0.0;
   for (int k = 0; k < 3; ++k) {
-    c[k] = n > 0 ? __double2float_rn(0.5 * (mn[k] + mx[k])) : 0.0f;
-    ext = fmax(ext, fmax(fabs(mn[k] - double(c[k])), fabs(mx[k] - double(c[k]))));
+    c[k] = n > 0 ? __double2float_rn(0.5 * (sh[k][0] + sh[3 + k][0])) : 0.0f;
+    ext = fmax(ext, fmax(fabs(sh[k][0] - double(c[k])), fabs(sh[3 + k][0] - double(c[k]))));
   }
   int e = 0;
   frexp(ext, &e);  // ext < 2^e
@@ -365,7 +380,7 @@ extern "C" int nfem_points_split(const double* points, int64_t n_points, float* 
   const int nb = int(n_points / 3 < kSplitBlocks ? n_points / 3 : kSplitBlocks);
   double* part = reinterpret_cast<double*>(rec + 1);
   if (nb > 0) bbox_partial_kernel<<<nb, 256, 0, stream>>>(points, n_points, part);
-  split_header_kernel<<<1, 32, 0, stream>>>(part, nb, points, n_points, rec);
+  split_header_kernel<<<1, 256, 0, stream>>>(part, nb, points, n_points, rec);
   if (n_points > 0) split_points_kernel<<<grid_for(n_points, 256), 256, 0, stream>>>(points, n_points, rec);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;

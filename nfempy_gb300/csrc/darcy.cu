@@ -194,11 +194,15 @@ __device__ __forceinline__ void element_row(const DarcyParams& p, const Incidenc
   T sg[NF];
 #pragma unroll
   for (int i = 0; i < NF; ++i) sg[i] = ((x.m >> i) & 1u) ? -C::sigma(i) : C::sigma(i);
+  // G = J^T J only where it is used: the flux rows, and the 2-D |det J|
   T G[DIM][DIM];
+  auto metric = [&]() {
 #pragma unroll
-  for (int i = 0; i < DIM; ++i)
+    for (int i = 0; i < DIM; ++i)
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) G[i][j] = x.J[i][0] * x.J[j][0] + x.J[i][1] * x.J[j][1] + x.J[i][2] * x.J[j][2];
+      for (int j = 0; j < DIM; ++j) G[i][j] = x.J[i][0] * x.J[j][0] + x.J[i][1] * x.J[j][1] + x.J[i][2] * x.J[j][2];
+  };
+  if (DIM == 2 || a < NF) metric();
   T det = T(1);
   if (need_geo) {
     det = abs_det<T, DIM>(x.J, G);
@@ -339,16 +343,20 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, NFEM_DARCY_MIN_BLOCKS) darcy
   const int64_t stride = int64_t(gridDim.x) * kDarcyWarps * 32;
 
   int64_t r0 = (int64_t(blockIdx.x) * kDarcyWarps + warp) * 32;
+  // row_ptr of the lane's row and of the row after the chunk (clamped to n_rows)
+  auto rp_at = [&](int64_t r) { return __ldg(p.row_ptr + (r < p.n_rows ? r : p.n_rows)); };
   RowHead head = load_head(p, r0 + lane);
-  int32_t base_next = r0 < p.n_rows ? __ldg(p.row_ptr + r0) : 0;
+  int32_t rp_lane = rp_at(r0 + lane), rp_end = rp_at(r0 + 32);
   for (; r0 < p.n_rows; r0 += stride) {
     const int64_t r = r0 + lane;
     const bool valid = r < p.n_rows;
     const RowHead h = head;
-    const int32_t base = base_next;
+    const int32_t rpl = rp_lane, rpe = rp_end;
     // prefetch the next chunk of this warp (overlaps its latency with this one)
     head = load_head(p, r0 + stride + lane);
-    base_next = (r0 + stride < p.n_rows) ? __ldg(p.row_ptr + r0 + stride) : 0;
+    rp_lane = rp_at(r0 + stride + lane);
+    rp_end = rp_at(r0 + stride + 32);
+    const int32_t base = __shfl_sync(0xffffffffu, rpl, 0);
 
     const int occ[2] = {h.pr.x, h.pr.y};
     const uint32_t code[2] = {h.cd.x, h.cd.y};
@@ -362,17 +370,12 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, NFEM_DARCY_MIN_BLOCKS) darcy
       a[t] = on[t] ? occ[t] - c[t] * NLOC : 0;
       geo[t] = on[t] && ((a[t] < DIM + 1) || (SRC != 0));
     }
-    // row offsets inside the chunk: exclusive warp scan of the row lengths
-    const int len = valid ? row_len_from_codes<NLOC>(h) : 0;
-    int incl = len;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const int off = incl - len;
-    const int span = __shfl_sync(0xffffffffu, incl, 31);
-    if (span > 32 * kDarcyMaxRow) {  // cannot happen for codes built with rows <= 16
+    // row lengths and offsets inside the chunk straight from row_ptr
+    const int32_t rpn = lane == 31 ? rpe : __shfl_down_sync(0xffffffffu, rpl, 1);
+    const int len = valid ? rpn - rpl : 0;
+    const int off = rpl - base;
+    const int span = rpe - base;
+    if (span > 32 * kDarcyMaxRow || span < 0) {  // rows of at most 16 entries fit
       if (lane == 0) set_status(p.status, NFEM_ERR_PATTERN);
       continue;
     }
@@ -399,19 +402,23 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, NFEM_DARCY_MIN_BLOCKS) darcy
         element_row<T, DIM, SRC>(p, x, a[t], geo[t], v, rhs_val);
         const uint32_t cd = code[t];
         const int at = a[t];
+        if (direct) {
+          // the first incidence stores all its entries; the second stores its
+          // own and overwrites the shared diagonal with the sum
+          T d = T(0);
 #pragma unroll
-        for (int b = 0; b < NLOC; ++b) {
-          // codes index inside the row (< 16 entries); the clamp keeps a
-          // corrupted code inside this warp's staging buffer
-          const int idx = min(off + int((cd >> (4 * b)) & 15u), kCap);
-          if (!direct) {
-            st[idx] += v[b];
-          } else if (two && b == at) {
-            if (t == 0) diag = v[b];
-            else st[idx] = diag + v[b];
-          } else {
-            st[idx] = v[b];
+          for (int b = 0; b < NLOC; ++b) d = (b == at) ? v[b] : d;
+#pragma unroll
+          for (int b = 0; b < NLOC; ++b) {
+            // codes index inside the row (< 16 entries); the clamp keeps a
+            // corrupted code inside this warp's staging buffer
+            const int idx = min(off + int((cd >> (4 * b)) & 15u), kCap);
+            st[idx] = (t == 1 && b == at) ? v[b] + diag : v[b];
           }
+          if (t == 0) diag = d;
+        } else {
+#pragma unroll
+          for (int b = 0; b < NLOC; ++b) st[min(off + int((cd >> (4 * b)) & 15u), kCap)] += v[b];
         }
       }
     }
@@ -428,117 +435,48 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, NFEM_DARCY_MIN_BLOCKS) darcy
 }
 
 // ------------------------------------------------------------------ cell chunks
-// Cell-chunk variant of the same assembly.  Rows are numbered by first
-// appearance, so the flux rows whose first incidence lies in a run of K
-// consecutive cells are themselves consecutive (the chunk row table), and so
-// are the pressure rows of those cells.  A block, per chunk:
-//  (1) evaluates the element matrices of its K cells once, with coalesced
-//      loads of the per-cell inputs, into shared memory;
-//  (2) queues the second incidences of its flux rows that lie in a cell
-//      outside the chunk (a neighbour in a later row or layer of the mesh)
-//      and (3) evaluates them densely, one per thread, from the vertices;
-//  (4) writes the chunk's pressure rows and flux rows from shared memory,
-//      staged per warp and stored coalesced as in the row-owner kernel.
-// Each value is written once; the queue order does not affect any value.
-constexpr int kChunkThreads = 256;
-constexpr int kChunkWarps = kChunkThreads / 32;
-constexpr int kMStride = 17;  // element matrix words per cell: odd, so cells spread over the banks
+// Cell-chunk variant of the same assembly, one chunk of 32 consecutive cells
+// per warp.  Rows are numbered by first appearance, so the flux rows whose
+// first incidence lies in the chunk are consecutive (the chunk row table),
+// and so are the pressure rows of its cells.  Per chunk the warp:
+//  (1) evaluates its 32 cells' element matrices once (lane = cell, coalesced
+//      per-cell loads) into its shared-memory slice;
+//  (2) queues the flux rows' second incidences that lie in a cell outside
+//      the chunk (neighbours in a later row or layer of the mesh) and
+//  (3) evaluates them densely, one per lane;
+//  (4) writes the pressure rows and flux rows from shared memory, staged and
+//      stored coalesced as in the row-owner kernel.
+// Warps are independent (no block barriers).  Each value is written once and
+// the queue order does not affect any value.
+constexpr int kChunkWarps = 8;
+constexpr int kChunkThreads = 32 * kChunkWarps;
+constexpr int kMStride = 17;  // words per cell: odd, so the cells of a warp spread over the banks
+constexpr int kQMax = 64;     // queued incidences per chunk; more are evaluated in the row pass
+static_assert(NFEM_DARCY_CHUNK_CELLS == 32, "one warp per chunk");
 
-template <typename T>
-struct ChunkSmem {
-  T* M;             // [K][kMStride]: rows a < NF of the flux x flux block at a * 4 + b
-  T* rp;            // [K] residual entry of the cell's pressure row
-  uint32_t* sg;     // [K] orientation mask
-  T* qv;            // [4K][NLOC] values of queued (out-of-chunk) incidences
-  int32_t* qocc;    // [4K] their occurrences (cell * NLOC + local)
-  int16_t* slot;    // [4K] queue slot of each flux row of the chunk, or -1
-  T* stage;         // [warps][32 * kDarcyMaxRow]
-  int32_t* count;   // queue length
+template <typename T, int DIM>
+struct WarpChunk {
+  T M[32 * kMStride];          // rows a < NF of each cell's flux x flux block at a * 4 + b
+  T rp[32];                    // residual entry of each cell's pressure row
+  uint32_t sg[32];             // orientation masks
+  T qv[kQMax * (DIM + 2)];     // values of the queued incidences
+  int32_t qocc[kQMax];         // their occurrences (cell * NLOC + local)
+  int16_t slot[4 * 32];        // queue slot per flux row of the chunk: -1 local, -2 not queued
+  T stage[32 * kDarcyMaxRow];  // row images
 };
 
-template <typename T>
-static size_t chunk_smem_bytes(int K, int nloc) {
-  size_t b = 0;
-  b += size_t(K) * kMStride * sizeof(T);
-  b += size_t(K) * sizeof(T) + size_t(K) * sizeof(uint32_t);
-  b += size_t(4 * K) * nloc * sizeof(T) + size_t(4 * K) * sizeof(int32_t) + size_t(4 * K) * sizeof(int16_t);
-  b = (b + 15) & ~size_t(15);
-  b += size_t(kChunkWarps) * 32 * kDarcyMaxRow * sizeof(T) + 16;
-  return b;
-}
-
-template <typename T, int DIM>
-__device__ __forceinline__ ChunkSmem<T> chunk_carve(unsigned char* base, int K) {
-  constexpr int NLOC = DIM + 2;
-  ChunkSmem<T> sm;
-  size_t o = 0;
-  sm.M = reinterpret_cast<T*>(base + o);
-  o += size_t(K) * kMStride * sizeof(T);
-  sm.rp = reinterpret_cast<T*>(base + o);
-  o += size_t(K) * sizeof(T);
-  sm.qv = reinterpret_cast<T*>(base + o);
-  o += size_t(4 * K) * NLOC * sizeof(T);
-  sm.sg = reinterpret_cast<uint32_t*>(base + o);
-  o += size_t(K) * sizeof(uint32_t);
-  sm.qocc = reinterpret_cast<int32_t*>(base + o);
-  o += size_t(4 * K) * sizeof(int32_t);
-  sm.slot = reinterpret_cast<int16_t*>(base + o);
-  o += size_t(4 * K) * sizeof(int16_t);
-  o = (o + 15) & ~size_t(15);
-  sm.stage = reinterpret_cast<T*>(base + o);
-  o += size_t(kChunkWarps) * 32 * kDarcyMaxRow * sizeof(T);
-  sm.count = reinterpret_cast<int32_t*>(base + o);
-  return sm;
-}
-
-// values of incidence (cell c, local a) from shared memory: the chunk's own
-// cells from the element matrices, the others from the queue
-template <typename T, int DIM>
-__device__ __forceinline__ void chunk_incidence(const DarcyParams& p, const ChunkSmem<T>& sm, int64_t lc, int64_t nk,
-                                                int a, int qslot, T (&v)[DIM + 2], T& rhs_val) {
+// rows [first, last) of the warp's chunk (cells [c0, c0 + nk))
+template <typename T, int DIM, int SRC>
+__device__ __forceinline__ void warp_chunk_rows(const DarcyParams& p, WarpChunk<T, DIM>& w, int64_t first,
+                                                int64_t last, int64_t c0, int64_t nk, bool is_flux) {
   constexpr int NF = DIM + 1, NLOC = DIM + 2;
   using C = DarcyConst<T, DIM>;
-  if (qslot >= 0) {
-#pragma unroll
-    for (int b = 0; b < NLOC; ++b) v[b] = sm.qv[qslot * NLOC + b];
-    return;
-  }
-  if (lc < 0 || lc >= nk) {  // only a corrupted chunk table leads here
-    set_status(p.status, NFEM_ERR_PATTERN);
-#pragma unroll
-    for (int b = 0; b < NLOC; ++b) v[b] = T(0);
-    return;
-  }
-  const uint32_t m = sm.sg[lc];
-  if (a < NF) {
-    const T* Mr = sm.M + lc * kMStride + a * 4;
-#pragma unroll
-    for (int b = 0; b < NF; ++b) v[b] = Mr[b];
-    T sga = C::sigma(0);
-#pragma unroll
-    for (int i = 1; i < NF; ++i) sga = (a == i) ? C::sigma(i) : sga;
-    sga = ((m >> a) & 1u) ? -sga : sga;
-    v[NF] = -sga;
-  } else {
-#pragma unroll
-    for (int b = 0; b < NF; ++b) v[b] = ((m >> b) & 1u) ? -C::sigma(b) : C::sigma(b);
-    v[NF] = T(0);
-    rhs_val += sm.rp[lc];
-  }
-}
-
-// rows [first, last); flux rows (is_flux) find their second incidence's
-// values through the queue slots
-template <typename T, int DIM>
-__device__ __forceinline__ void chunk_rows_pass(const DarcyParams& p, const ChunkSmem<T>& sm, int64_t first,
-                                                int64_t last, int64_t c0, int64_t nk, bool is_flux) {
-  constexpr int NLOC = DIM + 2;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* st = sm.stage + warp * 32 * kDarcyMaxRow;
+  const int lane = threadIdx.x & 31;
+  T* st = w.stage;
   T* values = static_cast<T*>(p.values);
   T* rhs = static_cast<T*>(p.rhs);
   constexpr int kCap = 32 * kDarcyMaxRow - 1;
-  for (int64_t r0 = first + 32 * warp; r0 < last; r0 += 32 * kChunkWarps) {
+  for (int64_t r0 = first; r0 < last; r0 += 32) {
     const int64_t r = r0 + lane;
     const bool valid = r < last;
     const RowHead h = load_head(p, valid ? r : p.n_rows);
@@ -554,7 +492,7 @@ __device__ __forceinline__ void chunk_rows_pass(const DarcyParams& p, const Chun
       c[t] = on[t] ? occ[t] / NLOC : 0;
       a[t] = on[t] ? occ[t] - c[t] * NLOC : 0;
     }
-    const int q1 = (is_flux && valid && on[1]) ? int(sm.slot[r - first]) : -1;
+    const int q1 = (is_flux && valid && on[1]) ? int(w.slot[r - first]) : -1;
     const int len = valid ? row_len_from_codes<NLOC>(h) : 0;
     int incl = len;
 #pragma unroll
@@ -581,7 +519,34 @@ __device__ __forceinline__ void chunk_rows_pass(const DarcyParams& p, const Chun
     for (int t = 0; t < 2; ++t) {
       if (on[t]) {
         T v[NLOC];
-        chunk_incidence<T, DIM>(p, sm, int64_t(c[t]) - c0, nk, a[t], t == 1 ? q1 : -1, v, rhs_val);
+        const int64_t lc = int64_t(c[t]) - c0;
+        const int qs = t == 1 ? q1 : -1;
+        if (qs >= 0) {
+#pragma unroll
+          for (int b = 0; b < NLOC; ++b) v[b] = w.qv[qs * NLOC + b];
+        } else if (lc >= 0 && lc < nk) {
+          const uint32_t m = w.sg[lc];
+          if (a[t] < NF) {
+            const T* Mr = w.M + lc * kMStride + a[t] * 4;
+#pragma unroll
+            for (int b = 0; b < NF; ++b) v[b] = Mr[b];
+            T sga = C::sigma(0);
+#pragma unroll
+            for (int i = 1; i < NF; ++i) sga = (a[t] == i) ? C::sigma(i) : sga;
+            sga = ((m >> a[t]) & 1u) ? -sga : sga;
+            v[NF] = -sga;
+          } else {
+#pragma unroll
+            for (int b = 0; b < NF; ++b) v[b] = ((m >> b) & 1u) ? -C::sigma(b) : C::sigma(b);
+            v[NF] = T(0);
+            rhs_val += w.rp[lc];
+          }
+        } else {  // a second incidence the queue did not hold (or a chunk-table mismatch)
+          Incidence<T, DIM> x;
+          const bool geo = (a[t] < NF) || (SRC != 0);
+          load_incidence<T, DIM, SRC>(p, c[t], geo, x);
+          element_row<T, DIM, SRC>(p, x, a[t], geo, v, rhs_val);
+        }
         const uint32_t cd = code[t];
         const int at = a[t];
 #pragma unroll
@@ -610,60 +575,61 @@ __device__ __forceinline__ void chunk_rows_pass(const DarcyParams& p, const Chun
   }
 }
 
-template <typename T, int DIM, int SRC, int KC>
+template <typename T, int DIM, int SRC>
 __global__ void __launch_bounds__(kChunkThreads) darcy_cells_kernel(const DarcyParams p) {
   constexpr int NF = DIM + 1, NLOC = DIM + 2;
-  constexpr int K = KC * NFEM_DARCY_CHUNK_CELLS;
   extern __shared__ __align__(16) unsigned char dsm[];
-  const ChunkSmem<T> sm = chunk_carve<T, DIM>(dsm, K);
-  const int64_t n_chunks = (p.n_cells + K - 1) / K;
-  const int64_t n_table = (p.n_cells + NFEM_DARCY_CHUNK_CELLS - 1) / NFEM_DARCY_CHUNK_CELLS;
   const int lane = threadIdx.x & 31;
-  for (int64_t k = blockIdx.x; k < n_chunks; k += gridDim.x) {
-    const int64_t c0 = k * K;
-    const int64_t nk = min(int64_t(K), p.n_cells - c0);
-    const int32_t f0 = __ldg(p.chunk_rows + k * KC);
-    const int32_t f1 = __ldg(p.chunk_rows + min((k + 1) * KC, n_table));
-    if (threadIdx.x == 0) *sm.count = 0;
-    const bool rows_ok = f1 - f0 <= 4 * nk;  // every cell opens at most NF flux rows
-    if (!rows_ok && threadIdx.x == 0) set_status(p.status, NFEM_ERR_PATTERN);
-    // (1) element matrices of the chunk's cells
-    for (int i = threadIdx.x; i < nk; i += kChunkThreads) {
+  WarpChunk<T, DIM>& w = reinterpret_cast<WarpChunk<T, DIM>*>(dsm)[threadIdx.x >> 5];
+  const int64_t n_chunks = (p.n_cells + 31) / 32;
+  const int64_t n_warps = int64_t(gridDim.x) * kChunkWarps;
+  for (int64_t k = int64_t(blockIdx.x) * kChunkWarps + (threadIdx.x >> 5); k < n_chunks; k += n_warps) {
+    const int64_t c0 = k * 32;
+    const int64_t nk = min(int64_t(32), p.n_cells - c0);
+    const int32_t f0 = __ldg(p.chunk_rows + k);
+    const int32_t f1 = __ldg(p.chunk_rows + k + 1);
+    // (1) element matrices, lane = cell
+    if (lane < nk) {
       Incidence<T, DIM> x;
-      load_incidence<T, DIM, SRC>(p, int32_t(c0 + i), true, x);
-      T* Mi = sm.M + i * kMStride;
-      sm.rp[i] = cell_matrix<T, DIM, SRC>(p, x, Mi);
-      sm.sg[i] = x.m;
+      load_incidence<T, DIM, SRC>(p, int32_t(c0 + lane), true, x);
+      w.rp[lane] = cell_matrix<T, DIM, SRC>(p, x, w.M + lane * kMStride);
+      w.sg[lane] = x.m;
     }
-    __syncthreads();
-    // (2) queue the out-of-chunk second incidences of the flux rows
+    // every cell opens at most NF flux rows; anything else is a table mismatch
+    const bool rows_ok = f1 >= f0 && f1 - f0 <= NF * nk;
+    if (!rows_ok && lane == 0) set_status(p.status, NFEM_ERR_PATTERN);
+    // (2) queue the out-of-chunk second incidences
+    int nq = 0;
     if (rows_ok) {
-      for (int64_t r = f0 + threadIdx.x; r - threadIdx.x < f1; r += kChunkThreads) {
+      for (int64_t rb = f0; rb < f1; rb += 32) {
+        const int64_t r = rb + lane;
         int32_t occ = -1;
         if (r < f1) {
           occ = __ldg(p.pairs + 2 * r + 1);
           if (occ >= 0 && occ / NLOC < c0 + nk) occ = -1;
         }
         const unsigned want = __ballot_sync(0xffffffffu, occ >= 0);
-        int basis = 0;
-        if (lane == 0 && want) basis = atomicAdd(sm.count, __popc(want));
-        basis = __shfl_sync(0xffffffffu, basis, 0);
+        const int s = nq + __popc(want & ((1u << lane) - 1u));
         if (r < f1) {
           int16_t q = -1;
           if (occ >= 0) {
-            const int s = basis + __popc(want & ((1u << lane) - 1u));
-            sm.qocc[s] = occ;
-            q = int16_t(s);
+            if (s < kQMax) {
+              w.qocc[s] = occ;
+              q = int16_t(s);
+            } else {
+              q = -2;
+            }
           }
-          sm.slot[r - f0] = q;
+          w.slot[r - f0] = q;
         }
+        nq += __popc(want);
       }
     }
-    __syncthreads();
-    // (3) evaluate the queue densely
-    const int nq = *sm.count;
-    for (int i = threadIdx.x; i < nq; i += kChunkThreads) {
-      const int32_t occ = sm.qocc[i];
+    nq = min(nq, kQMax);
+    __syncwarp();
+    // (3) the queue, one incidence per lane
+    for (int i = lane; i < nq; i += 32) {
+      const int32_t occ = w.qocc[i];
       const int32_t c = occ / NLOC;
       const int a = occ - c * NLOC;
       Incidence<T, DIM> x;
@@ -672,13 +638,13 @@ __global__ void __launch_bounds__(kChunkThreads) darcy_cells_kernel(const DarcyP
       T v[NLOC], unused = T(0);
       element_row<T, DIM, SRC>(p, x, a, geo, v, unused);
 #pragma unroll
-      for (int b = 0; b < NLOC; ++b) sm.qv[i * NLOC + b] = v[b];
+      for (int b = 0; b < NLOC; ++b) w.qv[i * NLOC + b] = v[b];
     }
-    __syncthreads();
-    // (4) pressure rows of the chunk's cells, then its flux rows
-    chunk_rows_pass<T, DIM>(p, sm, p.p_base + c0, p.p_base + c0 + nk, c0, nk, false);
-    if (rows_ok) chunk_rows_pass<T, DIM>(p, sm, f0, f1, c0, nk, true);
-    __syncthreads();
+    __syncwarp();
+    // (4) pressure rows, then flux rows
+    warp_chunk_rows<T, DIM, SRC>(p, w, p.p_base + c0, p.p_base + c0 + nk, c0, nk, false);
+    if (rows_ok) warp_chunk_rows<T, DIM, SRC>(p, w, f0, f1, c0, nk, true);
+    __syncwarp();
   }
 }
 
@@ -701,40 +667,24 @@ static int launch_darcy_src(const DarcyParams& p, cudaStream_t stream) {
   return NFEM_OK;
 }
 
-#ifndef NFEM_DARCY_CHUNK_KC
-#define NFEM_DARCY_CHUNK_KC 1
-#endif
-// table entries per chunk: chunks of 256 cells (FP32: 63 KB of shared
-// memory, FP64: 103 KB)
-template <typename T>
-struct ChunkKC {
-  static constexpr int value = NFEM_DARCY_CHUNK_KC;
-};
-template <>
-struct ChunkKC<double> {
-  static constexpr int value = 1;
-};
-
 template <typename T, int DIM, int SRC>
 static int launch_darcy_chunks(const DarcyParams& p, cudaStream_t stream) {
-  constexpr int KC = ChunkKC<T>::value;
-  const int K = KC * NFEM_DARCY_CHUNK_CELLS;
-  const size_t smem = chunk_smem_bytes<T>(K, DIM + 2);
-  static const int per_sm = [smem] {
-    int n = 0;
+  constexpr size_t smem = sizeof(WarpChunk<T, DIM>) * kChunkWarps;
+  static const int per_sm = [] {
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(darcy_cells_kernel<T, DIM, SRC, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(darcy_cells_kernel<T, DIM, SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              int(smem)) != cudaSuccess)
       return -1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, darcy_cells_kernel<T, DIM, SRC, KC>, kChunkThreads,
-                                                      smem) != cudaSuccess ||
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, darcy_cells_kernel<T, DIM, SRC>, kChunkThreads, smem) !=
+            cudaSuccess ||
         n < 1)
       n = 1;
     return n;
   }();
   if (per_sm < 0) return NFEM_ERR_CUDA;
-  const int grid = grid_for(ceil_div(p.n_cells, K), 1, per_sm);
-  darcy_cells_kernel<T, DIM, SRC, KC><<<grid, kChunkThreads, smem, stream>>>(p);
+  const int grid = grid_for(ceil_div(p.n_cells, 32 * kChunkWarps), 1, per_sm);
+  darcy_cells_kernel<T, DIM, SRC><<<grid, kChunkThreads, smem, stream>>>(p);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }

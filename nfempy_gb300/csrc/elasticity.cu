@@ -61,6 +61,7 @@ static int upload_tables(const double* S, const double* m, const double* Mf, cud
 
 struct ElasParams {
   int64_t n_nodes;
+  int deg_max;  // largest node degree (columns / 3) of any node row
   int64_t n_cells;
   void* geom;  // [n_cells][12]: J^-1 (row-major, 9), lambda |det J|, mu |det J|, |det J|
   int64_t row0;  // first row of the space (dof_shift)
@@ -165,17 +166,47 @@ __device__ __forceinline__ void load_geom<double>(const ElasParams& p, int32_t c
   }
 }
 
+// 4-wide slot of a node column in a row image: (j = 0, 1, 2, pad)
+template <typename T>
+struct Slot4;
+template <>
+struct Slot4<float> {
+  float4 v;
+  __device__ __forceinline__ void load(const float* a) { v = *reinterpret_cast<const float4*>(a); }
+  __device__ __forceinline__ void store(float* a) const { *reinterpret_cast<float4*>(a) = v; }
+  __device__ __forceinline__ float& operator[](int j) { return j == 0 ? v.x : (j == 1 ? v.y : v.z); }
+};
+template <>
+struct Slot4<double> {
+  double2 lo, hi;
+  __device__ __forceinline__ void load(const double* a) {
+    lo = reinterpret_cast<const double2*>(a)[0];
+    hi = reinterpret_cast<const double2*>(a)[1];
+  }
+  __device__ __forceinline__ void store(double* a) const {
+    reinterpret_cast<double2*>(a)[0] = lo;
+    reinterpret_cast<double2*>(a)[1] = hi;
+  }
+  __device__ __forceinline__ double& operator[](int j) { return j == 0 ? lo.x : (j == 1 ? lo.y : hi.x); }
+};
+
+// Row images: per warp, per group, rows i = 0..2 of the node, one 4-wide slot
+// per node column (the column's components j = 0..2 and a pad), so a 3 x 3
+// block is added with three 16-byte read-modify-writes.
+template <typename T>
+__host__ __device__ constexpr size_t elas_image_words(int deg) {
+  return size_t(3) * 3 * size_t(deg) * 4;
+}
+
 template <typename T, int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasParams p) {
-  constexpr int IMG = 3 * 3 * kElasDegMax;  // 3 rows x 3 deg_max columns
-  // an odd pad puts the three group images in different banks (every group
-  // writes its row node's own column at the same offset)
-  constexpr int IMGP = IMG + 3;
-  __shared__ T img[WARPS][3][IMGP];
+  extern __shared__ __align__(16) unsigned char dsm[];
+  const int deg_max = p.deg_max;
+  T* images = reinterpret_cast<T*>(dsm);  // [WARPS][3 groups][3 rows][deg_max][4]
   // reference tables read with per-lane indices (a, b): shared memory serves
   // those in one pass, the constant cache would serialise them
-  __shared__ T sS[10 * 10 * 9];
-  __shared__ T sm_m[10];
+  T* sS = images + WARPS * elas_image_words<T>(deg_max);
+  T* sm_m = sS + 900;
   for (int i = threadIdx.x; i < 900; i += blockDim.x) sS[i] = T(c_S[i]);
   if (threadIdx.x < 10) sm_m[threadIdx.x] = T(c_m[threadIdx.x]);
   __syncthreads();
@@ -184,18 +215,25 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
   const T* force = static_cast<const T*>(p.force);
   T* values = static_cast<T*>(p.values);
   T* rhs = static_cast<T*>(p.rhs);
+  T* wimg = images + warp * elas_image_words<T>(deg_max);
   for (int64_t v = int64_t(blockIdx.x) * WARPS + warp; v < p.n_nodes; v += int64_t(gridDim.x) * WARPS) {
     const int64_t r0 = p.row0 + 3 * v;
     const int32_t base = __ldg(p.row_ptr + r0);
     const int len = __ldg(p.row_ptr + r0 + 1) - base;  // 3 x deg
-    if (len > 3 * kElasDegMax || len % 3 != 0) {
+    const int deg = len / 3;
+    if (deg > deg_max || len % 3 != 0 || deg < 1) {
       if (lane == 0) set_status(p.status, NFEM_ERR_UNSUPPORTED);
       continue;
     }
-    for (int i = lane; i < 3 * len; i += 32) {
-      img[warp][0][i] = T(0);
-      img[warp][1][i] = T(0);
-      img[warp][2][i] = T(0);
+    // the group images of this node: [3 groups][3 rows][deg][4]
+    const int gstride = 3 * deg * 4;
+    for (int q = lane; q < 3 * 3 * deg; q += 32) {
+      Slot4<T> z;
+      z[0] = T(0);
+      z[1] = T(0);
+      z[2] = T(0);
+      if constexpr (sizeof(T) == 4) z.v.w = 0.0f; else z.hi.y = 0.0;
+      z.store(wimg + q * 4);
     }
     __syncwarp();
     const int32_t kb = __ldg(p.inc_ptr + r0), ke = __ldg(p.inc_ptr + r0 + 1);
@@ -207,8 +245,8 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
         const int32_t c = occ / 30;
         const int a = (occ - c * 30) / 3;
         // node position inside the row; the clamp keeps a corrupted code in
-        // this node's image (a valid one is < len / 3)
-        const int pos = min(int(__ldg(p.codes + int64_t(k) * 16 + b)), len / 3 - 1);
+        // this node's image (a valid one is < deg)
+        const int pos = min(int(__ldg(p.codes + int64_t(k) * 16 + b)), deg - 1);
         T gm[12];
         load_geom<T>(p, c, gm);
         const T(&Ji)[12] = gm;  // Ji[k * 3 + q] = (J^-1)_{kq}
@@ -228,14 +266,16 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
             A[pp][q] = Ji[0 * 3 + pp] * SJ[0][q] + Ji[1 * 3 + pp] * SJ[1][q] + Ji[2 * 3 + pp] * SJ[2][q];
         const T lc = gm[9], mc = gm[10], adet = gm[11];
         const T tr = A[0][0] + A[1][1] + A[2][2];
-        T* im = img[warp][g];
+        T* im = wimg + g * gstride;
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
+        for (int i = 0; i < 3; ++i) {
+          T* slot = im + (i * deg + pos) * 4;
+          Slot4<T> s4;
+          s4.load(slot);
 #pragma unroll
-          for (int j = 0; j < 3; ++j) {
-            const T kij = (i == j ? mc * tr : T(0)) + mc * A[j][i] + lc * A[i][j];
-            im[i * len + 3 * pos + j] += kij;
-          }
+          for (int j = 0; j < 3; ++j) s4[j] += (i == j ? mc * tr : T(0)) + mc * A[j][i] + lc * A[i][j];
+          s4.store(slot);
+        }
         if (force && b == 0) {
 #pragma unroll
           for (int i = 0; i < 3; ++i) rhs_acc[i] += adet * sm_m[a] * __ldg(force + int64_t(c) * 3 + i);
@@ -243,10 +283,19 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
       }
       __syncwarp();
     }
-    // combine the three group images in a fixed order
-    for (int i = lane; i < len * 3; i += 32) {
-      const T s = img[warp][0][i] + img[warp][1][i] + img[warp][2][i];
-      if (p.accumulate) values[int64_t(base) + i] += s; else values[int64_t(base) + i] = s;
+    // combine the three group images in a fixed order: one (row i, column) slot per lane
+    for (int q = lane; q < 3 * deg; q += 32) {
+      Slot4<T> s0, s1, s2;
+      s0.load(wimg + q * 4);
+      s1.load(wimg + gstride + q * 4);
+      s2.load(wimg + 2 * gstride + q * 4);
+      const int i = q / deg, pos = q - i * deg;
+      T* out = values + int64_t(base) + i * len + 3 * pos;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const T sum = s0[j] + s1[j] + s2[j];
+        if (p.accumulate) out[j] += sum; else out[j] = sum;
+      }
     }
     T r[3];
 #pragma unroll
@@ -353,6 +402,24 @@ extern "C" int nfem_pattern_node_codes(const int32_t* cell_dofs, int64_t n_cells
   return NFEM_OK;
 }
 
+template <typename T, int WARPS>
+static int launch_elasticity(const ElasParams& p, cudaStream_t stream) {
+  const size_t smem = (WARPS * elas_image_words<T>(p.deg_max) + 910) * sizeof(T);
+  if (smem > 227 * 1024) return NFEM_ERR_UNSUPPORTED;
+  if (smem > 48 * 1024)
+    NFEM_TRY_CUDA(cudaFuncSetAttribute(elasticity_rows_kernel<T, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(smem)));
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, elasticity_rows_kernel<T, WARPS>, 32 * WARPS, smem) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  elasticity_rows_kernel<T, WARPS>
+      <<<grid_for(ceil_div(p.n_nodes, WARPS), 1, per_sm), 32 * WARPS, smem, stream>>>(p);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
 extern "C" int nfem_elasticity_p2_workspace_bytes(int value_type, int64_t n_cells, size_t* bytes) {
   if (!bytes || n_cells < 0 || (value_type != NFEM_F64 && value_type != NFEM_F32)) return NFEM_ERR_INVALID_ARG;
   *bytes = size_t(n_cells) * 12 * (value_type == NFEM_F64 ? sizeof(double) : sizeof(float));
@@ -364,9 +431,9 @@ extern "C" int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int6
                                            const int32_t* cell_vertices, const void* lambda_, const void* mu,
                                            const void* force, const double* ref_S, const double* ref_m,
                                            const int32_t* inc_ptr, const int32_t* inc, const uint8_t* node_codes,
-                                           const int32_t* row_ptr, void* values, void* rhs, int accumulate,
-                                           void* workspace, size_t workspace_bytes, int32_t* dev_status,
-                                           void* stream_) {
+                                           const int32_t* row_ptr, int max_node_degree, void* values, void* rhs,
+                                           int accumulate, void* workspace, size_t workspace_bytes,
+                                           int32_t* dev_status, void* stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;
   if (n_cells < 0) return NFEM_ERR_INVALID_ARG;
   if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n_nodes < 0 || row0 < 0) return NFEM_ERR_INVALID_ARG;
@@ -406,13 +473,14 @@ extern "C" int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int6
     elas_geom_kernel<double><<<grid_for(n_cells, 256), 256, 0, stream>>>(p);
   else
     elas_geom_kernel<float><<<grid_for(n_cells, 256), 256, 0, stream>>>(p);
+  p.deg_max = max_node_degree > 0 ? max_node_degree : kElasDegMax;
+  if (p.deg_max > 255) return NFEM_ERR_UNSUPPORTED;  // node codes are bytes
   if (value_type == NFEM_F64) {
-    elasticity_rows_kernel<double, kElasWarps64>
-        <<<grid_for(ceil_div(n_nodes, kElasWarps64), 1, 8), 32 * kElasWarps64, 0, stream>>>(p);
+    rc = launch_elasticity<double, kElasWarps64>(p, stream);
   } else {
-    elasticity_rows_kernel<float, kElasWarps32>
-        <<<grid_for(ceil_div(n_nodes, kElasWarps32), 1, 8), 32 * kElasWarps32, 0, stream>>>(p);
+    rc = launch_elasticity<float, kElasWarps32>(p, stream);
   }
+  if (rc) return rc;
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }

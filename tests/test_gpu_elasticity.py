@@ -99,3 +99,33 @@ def test_elasticity_penalty_matches_oracle(cuda_lib):
     # every boundary facet vertex DoF is penalised
     bnd_nodes = np.unique(fd)
     assert np.all(Ag.diagonal()[bnd_nodes] > 1e9)
+
+
+def test_elasticity_clamped_solve(cuda_lib):
+    """The elasticity driver's step (cg_elasticity_example_1.py:147-181): the
+    penalised system A u = -r solved on the device (FGMRES with point Jacobi
+    inside FP64 refinement) to 1e-8 FP64 relative residual, and equal to
+    SuperLU's solution of the same system."""
+    from nfempy_gb300.solvers import KrylovSolver
+    from oracle import solve
+    m = mesh_gen.cube(3)
+    T = m["blocks"][-1][1].shape[0]
+    rng = np.random.default_rng(5)
+    sp = product_space(m, FIELD)
+    A = nf.CSRMatrix(sp, dtype=torch.float64)
+    res = torch.zeros(A.n_rows, dtype=torch.float64, device="cuda")
+    wf = LEPrimalWeakForm(sp)
+    wf.functions = {"lambda": np.exp(rng.normal(0, 0.5, T)), "mu": np.exp(rng.normal(0, 0.5, T)),
+                    "rhs": np.array([1.0, 1.0, 1.0])}
+    wf.assemble(A, res)
+    bc = LEPrimalWeakFormBCDirichlet(sp)
+    bc.functions = {"u": None}
+    bc.assemble(A)
+    torch.cuda.synchronize()
+    ksp = KrylovSolver(A, pc="jacobi", restart=60)
+    x, info = ksp.solve(-res, rtol=1e-8, max_inner=20000)
+    assert info.status == 0 and info.final_relres <= 1e-8
+    Ag = A.to_scipy()
+    xo = solve.solve_newton_step(Ag, res.cpu().numpy())
+    xg = x.cpu().numpy()
+    assert np.linalg.norm(xg - xo) <= 1e-5 * np.linalg.norm(xo)
