@@ -288,6 +288,34 @@ def solve_bench(args, A, wf, coefs, res, stream):
     return out
 
 
+def solve_only(args):
+    """The benchmark system's solves alone (profiling runs): plain block-Jacobi
+    and two-level FGMRES on 64^3 x 6 tets, to 1e-8 or --max-iters inner
+    iterations."""
+    import torch
+    import nfempy_gb300 as nf
+    from nfempy_gb300 import workloads as wl
+    from nfempy_gb300.solvers import KrylovSolver, TwoLevelCoarse
+    m, sp, kappa, f = wl.darcy3d(N_SIDE)
+    A32 = nf.CSRMatrix(sp, dtype=torch.float32)
+    A64 = A32.with_dtype(torch.float64)
+    r32 = torch.empty(A32.n_rows, dtype=torch.float32, device="cuda")
+    r64 = torch.empty(A32.n_rows, dtype=torch.float64, device="cuda")
+    wf = nf.LaplaceDualWeakForm(sp)
+    wf.functions = {"kappa": kappa, "rhs": f}
+    wf.assemble(A32, r32)
+    wf.assemble(A64, r64)
+    b = -r64
+    stream = torch.cuda.current_stream()
+    out = {"workload": "solve", "n_dof": sp.n_dof, "restart": args.restart, "max_inner": args.max_iters}
+    out["plain_block_jacobi"] = _timed_solve(KrylovSolver(A64, pc="cell_block", A32_values=A32.values,
+                                                          restart=args.restart), b, args, stream)
+    tl = TwoLevelCoarse(A64, N_SIDE // 4)
+    out["two_level"] = _timed_solve(KrylovSolver(A64, pc="two_level", A32_values=A32.values,
+                                                 restart=args.restart, two_level=tl), b, args, stream)
+    return out
+
+
 def _time_assembly(fn, steps, warmup):
     import torch
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -608,13 +636,14 @@ def main():
     ap.add_argument("--max-iters", type=int, default=20000)
     ap.add_argument("--kernel", choices=["rows", "chunks"], default="rows",
                     help="Darcy assembly kernel: row owner (default) or cell chunks")
-    ap.add_argument("--only", choices=["elasticity", "cosserat", "batch2d"], default=None,
+    ap.add_argument("--only", choices=["elasticity", "cosserat", "batch2d", "solve"], default=None,
                     help="time one secondary assembly workload alone and print its record (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.only:
-        fn = {"elasticity": elasticity_bench, "cosserat": cosserat_bench, "batch2d": batch2d_bench}[args.only]
+        fn = {"elasticity": elasticity_bench, "cosserat": cosserat_bench, "batch2d": batch2d_bench,
+              "solve": solve_only}[args.only]
         print(json.dumps({"workload": args.only, **fn(args)}), flush=True)
         return
     if args.impl == "reference":

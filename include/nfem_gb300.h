@@ -310,6 +310,9 @@ int nfem_elasticity_p2_penalty(int value_type, int64_t n_facets, const int32_t* 
  * NULL; ref_Psi [4*4*3*3] = int psihat_i psihat_j^T, ref_mhat [4*3] =
  * int psihat_i, ref_divhat [4] = int div psihat_i on the reference
  * tetrahedron (host).  Row owner over node rows, each value written once. */
+/* Workspace of nfem_cosserat_assemble: the per-cell geometry (J, |det J|,
+ * orientation), 12 values of value_type per cell. */
+int nfem_cosserat_workspace_bytes(int value_type, int64_t n_cells, size_t* bytes);
 int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
                            const double* points, const float* points_split,
                            const int32_t* cell_vertices, const uint8_t* sign_mask,
@@ -317,7 +320,8 @@ int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int
                            const double* ref_mhat, const double* ref_divhat,
                            const int32_t* inc_ptr, const int32_t* inc,
                            const uint8_t* node_codes, const int32_t* row_ptr, void* values,
-                           void* rhs, int accumulate, int32_t* dev_status, void* stream);
+                           void* rhs, int accumulate, void* workspace, size_t workspace_bytes,
+                           int32_t* dev_status, void* stream);
 
 /* -------------------------------------------- K5 + K7: Krylov solve (a17)
  * Replaces the PETSc KSP solves of the drivers

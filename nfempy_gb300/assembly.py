@@ -632,12 +632,18 @@ class LCEDualWeakForm(WeakForm):
             raise NotImplementedError("matrix built without node codes")
         par, f, Psi, mhat, divhat = coefficients if coefficients is not None else self.coefficients(dtype)
         dp = _lib.C.POINTER(_lib.C.c_double)
+        key = ("geom", dtype)
+        if key not in self._cache:
+            nb = _lib.C.c_size_t(0)
+            _lib.call("nfem_cosserat_workspace_bytes", vt, sp.n_cells, _lib.C.byref(nb))
+            self._cache[key] = torch.empty(max(int(nb.value), 16), dtype=torch.uint8, device=sp.device)
+        ws = self._cache[key]
         _lib.call("nfem_cosserat_assemble", vt, sp.n_cells, sp.n_dof // 3, sp.dof_shift, _lib.ptr(sp.points),
                   _lib.ptr(sp.points_split), _lib.ptr(sp.cells), _lib.ptr(sp.rt_sign_mask), par.ctypes.data_as(dp),
                   _lib.ptr(f), Psi.ctypes.data_as(dp), mhat.ctypes.data_as(dp), divhat.ctypes.data_as(dp),
                   _lib.ptr(jacobian.inc_ptr), _lib.ptr(jacobian.inc), _lib.ptr(jacobian.node_codes),
                   _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate),
-                  _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+                  _lib.ptr(ws), ws.numel(), _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
 
 
 def l2_error(dim, space, functions, alpha, stream=None):

@@ -59,6 +59,8 @@ static int upload_cos_tables(const double* Psi, const double* mhat, const double
 
 struct CosParams {
   int64_t n_nodes;
+  int64_t n_cells;
+  void* geom;  // [n_cells][12]: J (row-major, 9), |det J|, orientation mask (as bits), pad
   int64_t row0;
   const double* points;
   const float* split;
@@ -103,6 +105,61 @@ __device__ __forceinline__ void cos_edges<float>(const CosParams& p, int32_t c, 
     J[d][1] = packed_diff(r2, r0, d, s);
     J[d][2] = packed_diff(r3, r0, d, s);
   }
+}
+
+// Per-cell geometry once per cell (each cell is read by the rows of its ten
+// nodes): J, |det J| and the orientation mask.
+template <typename T>
+__global__ void cos_geom_kernel(const CosParams p) {
+  T* out = static_cast<T*>(p.geom);
+  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < p.n_cells;
+       c += int64_t(gridDim.x) * blockDim.x) {
+    T J[3][3];
+    cos_edges<T>(p, int32_t(c), J);
+    const T det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                  J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    if (!(det != T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+    T g[12];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) g[i * 3 + k] = J[i][k];
+    g[9] = det < T(0) ? -det : det;
+    g[10] = T(__ldg(p.sign + c));
+    g[11] = T(0);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) out[c * 12 + k] = g[k];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void cos_load_geom(const CosParams& p, int32_t c, T (&J)[3][3], T& adet, uint32_t& m) {
+  T g[12];
+  if constexpr (sizeof(T) == 4) {
+    const float4* q = static_cast<const float4*>(p.geom) + int64_t(c) * 3;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float4 v = __ldg(q + k);
+      g[4 * k] = v.x;
+      g[4 * k + 1] = v.y;
+      g[4 * k + 2] = v.z;
+      g[4 * k + 3] = v.w;
+    }
+  } else {
+    const double2* q = static_cast<const double2*>(p.geom) + int64_t(c) * 6;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const double2 v = __ldg(q + k);
+      g[2 * k] = v.x;
+      g[2 * k + 1] = v.y;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) J[i][k] = g[i * 3 + k];
+  adet = g[9];
+  m = uint32_t(g[10]);
 }
 
 // 3 x 3 block between local nodes a (row) and b (column); node kinds:
@@ -175,9 +232,10 @@ __device__ __forceinline__ void cos_block(const CosParams& p, const CosTables<T>
 
 template <typename T>
 __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const CosParams p) {
-  constexpr int IMG = 3 * 3 * kCosDegMax;
-  constexpr int IMGP = IMG + 3;  // odd pad: the two group images in different banks
-  __shared__ T img[kCosWarps][2][IMGP];
+  // per warp, per group: rows i = 0..2 of the node, one 4-wide slot per node
+  // column (components j = 0..2 and a pad), so a 3 x 3 block is added with
+  // three 16-byte read-modify-writes
+  __shared__ __align__(16) T img[kCosWarps][2][3 * kCosDegMax * 4];
   // reference tables read with per-lane indices: shared, not constant, memory
   __shared__ CosTables<T> tb;
   for (int i = threadIdx.x; i < 144; i += blockDim.x) tb.Psi[i] = T(c_Psi[i]);
@@ -194,13 +252,16 @@ __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const Cos
     const int32_t base = __ldg(p.row_ptr + r0);
     const int len = __ldg(p.row_ptr + r0 + 1) - base;
     const int32_t kb = __ldg(p.inc_ptr + r0), ke = __ldg(p.inc_ptr + r0 + 1);
-    if (len > 3 * kCosDegMax || len % 3 != 0 || ke - kb > 2) {
+    if (len > 3 * kCosDegMax || len < 3 || len % 3 != 0 || ke - kb > 2) {
       if (lane == 0) set_status(p.status, NFEM_ERR_UNSUPPORTED);
       continue;
     }
-    for (int i = lane; i < 3 * len; i += 32) {
-      img[warp][0][i] = T(0);
-      img[warp][1][i] = T(0);
+    const int deg = len / 3;
+    for (int q = lane; q < 2 * 3 * deg; q += 32) {
+      T* slot = (q < 3 * deg ? img[warp][0] : img[warp][1]) + (q < 3 * deg ? q : q - 3 * deg) * 4;
+      Slot4<T> z;
+      z.zero();
+      z.store(slot);
     }
     __syncwarp();
     T rhs_acc[3] = {T(0), T(0), T(0)};
@@ -209,21 +270,24 @@ __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const Cos
       const int32_t occ = __ldg(p.inc + k);
       const int32_t c = occ / 30;
       const int a = (occ - c * 30) / 3;
-      const int pos = __ldg(p.codes + int64_t(k) * 16 + b);
-      T J[3][3];
-      cos_edges<T>(p, c, J);
-      const T det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                    J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-      if (!(det != T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
-      const T adet = det < T(0) ? -det : det;
-      const uint32_t m = __ldg(p.sign + c);
+      // node position inside the row; the clamp keeps a corrupted code in
+      // this node's image (a valid one is < deg)
+      const int pos = min(int(__ldg(p.codes + int64_t(k) * 16 + b)), deg - 1);
+      T J[3][3], adet;
+      uint32_t m;
+      cos_load_geom<T>(p, c, J, adet, m);
       T K[3][3];
       cos_block<T>(p, tb, J, adet, m, a, b, K);
       T* im = img[warp][g];
 #pragma unroll
-      for (int i = 0; i < 3; ++i)
+      for (int i = 0; i < 3; ++i) {
+        T* slot = im + (i * deg + pos) * 4;
+        Slot4<T> s4;
+        s4.load(slot);
 #pragma unroll
-        for (int j = 0; j < 3; ++j) im[min(i * len + 3 * pos + j, IMG - 1)] += K[i][j];
+        for (int j = 0; j < 3; ++j) s4[j] += K[i][j];
+        s4.store(slot);
+      }
       if (b == 0 && force && (a == 8 || a == 9)) {
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -231,9 +295,18 @@ __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const Cos
       }
     }
     __syncwarp();
-    for (int i = lane; i < len * 3; i += 32) {
-      const T s = img[warp][0][i] + img[warp][1][i];
-      if (p.accumulate) values[int64_t(base) + i] += s; else values[int64_t(base) + i] = s;
+    // combine the two group images in a fixed order: one (row i, column) slot per lane
+    for (int q = lane; q < 3 * deg; q += 32) {
+      Slot4<T> s0, s1;
+      s0.load(img[warp][0] + q * 4);
+      s1.load(img[warp][1] + q * 4);
+      const int i = q / deg, pos = q - i * deg;
+      T* out = values + int64_t(base) + i * len + 3 * pos;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const T sum = s0[j] + s1[j];
+        if (p.accumulate) out[j] += sum; else out[j] = sum;
+      }
     }
     T r[3];
 #pragma unroll
@@ -250,15 +323,22 @@ __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const Cos
 
 using namespace nfem;
 
+extern "C" int nfem_cosserat_workspace_bytes(int value_type, int64_t n_cells, size_t* bytes) {
+  if (!bytes || n_cells < 0 || (value_type != NFEM_F64 && value_type != NFEM_F32)) return NFEM_ERR_INVALID_ARG;
+  *bytes = size_t(n_cells) * 12 * (value_type == NFEM_F64 ? sizeof(double) : sizeof(float));
+  return NFEM_OK;
+}
+
 extern "C" int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
                                       const double* points, const float* points_split, const int32_t* cell_vertices,
                                       const uint8_t* sign_mask, const double* params7, const void* force,
                                       const double* ref_Psi, const double* ref_mhat, const double* ref_divhat,
                                       const int32_t* inc_ptr, const int32_t* inc, const uint8_t* node_codes,
                                       const int32_t* row_ptr, void* values, void* rhs, int accumulate,
-                                      int32_t* dev_status, void* stream_) {
-  (void)n_cells;
+                                      void* workspace, size_t workspace_bytes, int32_t* dev_status,
+                                      void* stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;
+  if (n_cells < 0) return NFEM_ERR_INVALID_ARG;
   if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n_nodes < 0 || row0 < 0 || !params7)
     return NFEM_ERR_INVALID_ARG;
   if (n_nodes == 0) return NFEM_OK;
@@ -295,11 +375,19 @@ extern "C" int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n
   p.rhs = rhs;
   p.accumulate = accumulate != 0;
   p.status = dev_status;
+  const size_t vb = value_type == NFEM_F64 ? sizeof(double) : sizeof(float);
+  if (!workspace || workspace_bytes < size_t(n_cells) * 12 * vb || (reinterpret_cast<uintptr_t>(workspace) & 15))
+    return NFEM_ERR_WORKSPACE;
+  p.n_cells = n_cells;
+  p.geom = workspace;
   const int grid = grid_for(ceil_div(n_nodes, kCosWarps), 1, 8);
-  if (value_type == NFEM_F64)
+  if (value_type == NFEM_F64) {
+    cos_geom_kernel<double><<<grid_for(n_cells, 256), 256, 0, stream>>>(p);
     cosserat_rows_kernel<double><<<grid, 32 * kCosWarps, 0, stream>>>(p);
-  else
+  } else {
+    cos_geom_kernel<float><<<grid_for(n_cells, 256), 256, 0, stream>>>(p);
     cosserat_rows_kernel<float><<<grid, 32 * kCosWarps, 0, stream>>>(p);
+  }
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }

@@ -137,6 +137,11 @@ __device__ __forceinline__ void cell_edges<float, 2>(const DarcyParams& p, int32
   }
 }
 
+// 1 / v: correctly rounded reciprocal (no division sequence) in FP32, exact
+// division in FP64
+__device__ __forceinline__ float recip(float v) { return __frcp_rn(v); }
+__device__ __forceinline__ double recip(double v) { return 1.0 / v; }
+
 template <typename T, int DIM>
 __device__ __forceinline__ T abs_det(const T (&J)[DIM][3], const T (&G)[DIM][DIM]) {
   if constexpr (DIM == 3) {
@@ -220,7 +225,7 @@ __device__ __forceinline__ void element_row(const DarcyParams& p, const Incidenc
       sumG += R[i];
     }
     const T tgs = (trG + sumG) * T(C::f2);
-    const T scale = T(C::kappa2) / (x.kap * det);
+    const T scale = T(C::kappa2) * recip(x.kap * det);
     // row a-1 of G and R[a-1] through selects (no local-memory indexing)
     T Ga[DIM];
     T Ra = T(0);
@@ -281,7 +286,7 @@ __device__ __forceinline__ T cell_matrix(const DarcyParams& p, const Incidence<T
     sumG += R[i];
   }
   const T tgs = (trG + sumG) * T(C::f2);
-  const T scale = T(C::kappa2) / (x.kap * det);
+  const T scale = T(C::kappa2) * recip(x.kap * det);
 #pragma unroll
   for (int a = 0; a < NF; ++a) {
     const T gma = a > 0 ? R[a - 1] * T(C::f1) : T(0);
@@ -371,7 +376,9 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, NFEM_DARCY_MIN_BLOCKS) darcy
       geo[t] = on[t] && ((a[t] < DIM + 1) || (SRC != 0));
     }
     // row lengths and offsets inside the chunk straight from row_ptr
-    const int32_t rpn = lane == 31 ? rpe : __shfl_down_sync(0xffffffffu, rpl, 1);
+    // every lane takes part in the shuffle; lane 31 then uses the chunk end
+    const int32_t rp_down = __shfl_down_sync(0xffffffffu, rpl, 1);
+    const int32_t rpn = lane == 31 ? rpe : rp_down;
     const int len = valid ? rpn - rpl : 0;
     const int off = rpl - base;
     const int span = rpe - base;

@@ -166,30 +166,6 @@ __device__ __forceinline__ void load_geom<double>(const ElasParams& p, int32_t c
   }
 }
 
-// 4-wide slot of a node column in a row image: (j = 0, 1, 2, pad)
-template <typename T>
-struct Slot4;
-template <>
-struct Slot4<float> {
-  float4 v;
-  __device__ __forceinline__ void load(const float* a) { v = *reinterpret_cast<const float4*>(a); }
-  __device__ __forceinline__ void store(float* a) const { *reinterpret_cast<float4*>(a) = v; }
-  __device__ __forceinline__ float& operator[](int j) { return j == 0 ? v.x : (j == 1 ? v.y : v.z); }
-};
-template <>
-struct Slot4<double> {
-  double2 lo, hi;
-  __device__ __forceinline__ void load(const double* a) {
-    lo = reinterpret_cast<const double2*>(a)[0];
-    hi = reinterpret_cast<const double2*>(a)[1];
-  }
-  __device__ __forceinline__ void store(double* a) const {
-    reinterpret_cast<double2*>(a)[0] = lo;
-    reinterpret_cast<double2*>(a)[1] = hi;
-  }
-  __device__ __forceinline__ double& operator[](int j) { return j == 0 ? lo.x : (j == 1 ? lo.y : hi.x); }
-};
-
 // Row images: per warp, per group, rows i = 0..2 of the node, one 4-wide slot
 // per node column (the column's components j = 0..2 and a pad), so a 3 x 3
 // block is added with three 16-byte read-modify-writes.
@@ -229,10 +205,7 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
     const int gstride = 3 * deg * 4;
     for (int q = lane; q < 3 * 3 * deg; q += 32) {
       Slot4<T> z;
-      z[0] = T(0);
-      z[1] = T(0);
-      z[2] = T(0);
-      if constexpr (sizeof(T) == 4) z.v.w = 0.0f; else z.hi.y = 0.0;
+      z.zero();
       z.store(wimg + q * 4);
     }
     __syncwarp();

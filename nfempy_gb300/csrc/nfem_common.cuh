@@ -70,6 +70,36 @@ __device__ __forceinline__ float packed_diff(const float4& r1, const float4& r0,
   return (h1 - h0) + float(packed_q(r1.w, d) - packed_q(r0.w, d)) * lo_scale;
 }
 
+// 4-wide slot of a node column in a row image of the node-row kernels:
+// (component j = 0, 1, 2, pad), read and written as 16-byte vectors
+template <typename T>
+struct Slot4;
+template <>
+struct Slot4<float> {
+  float4 v;
+  __device__ __forceinline__ void load(const float* a) { v = *reinterpret_cast<const float4*>(a); }
+  __device__ __forceinline__ void store(float* a) const { *reinterpret_cast<float4*>(a) = v; }
+  __device__ __forceinline__ float& operator[](int j) { return j == 0 ? v.x : (j == 1 ? v.y : v.z); }
+  __device__ __forceinline__ void zero() { v = make_float4(0.f, 0.f, 0.f, 0.f); }
+};
+template <>
+struct Slot4<double> {
+  double2 lo, hi;
+  __device__ __forceinline__ void load(const double* a) {
+    lo = reinterpret_cast<const double2*>(a)[0];
+    hi = reinterpret_cast<const double2*>(a)[1];
+  }
+  __device__ __forceinline__ void store(double* a) const {
+    reinterpret_cast<double2*>(a)[0] = lo;
+    reinterpret_cast<double2*>(a)[1] = hi;
+  }
+  __device__ __forceinline__ double& operator[](int j) { return j == 0 ? lo.x : (j == 1 ? lo.y : hi.x); }
+  __device__ __forceinline__ void zero() {
+    lo = make_double2(0.0, 0.0);
+    hi = lo;
+  }
+};
+
 // exclusive scan of int32 counts into int64 offsets (n + 1 entries)
 size_t scan_workspace_bytes(int64_t n);
 int exclusive_scan_i32(const int32_t* in, int64_t n, int64_t* out, void* ws,

@@ -86,3 +86,35 @@ def test_grf_is_seeded():
     assert np.abs(a - c).max() > 1e-3
     big = meshes.grf_log_field(np.random.default_rng(1).random((20000, 3)) * 50, 0.1, 2.0, 3, device="cpu")
     assert abs(big.std() - 2.0) < 0.15
+
+
+def test_new_workspace_queries_and_argument_checks(lib_path):
+    """Host-side checks of the entry points added for the P2 elasticity and
+    Cosserat geometry workspaces, the copy helper and the chunk table: sizes,
+    and invalid arguments refused before any device work."""
+    lib = _lib.lib()
+    b = ctypes.c_size_t(0)
+    assert lib.nfem_elasticity_p2_workspace_bytes(_lib.NFEM_F32, 1000, ctypes.byref(b)) == 0 and b.value == 48000
+    assert lib.nfem_elasticity_p2_workspace_bytes(_lib.NFEM_F64, 1000, ctypes.byref(b)) == 0 and b.value == 96000
+    assert lib.nfem_cosserat_workspace_bytes(_lib.NFEM_F32, 10, ctypes.byref(b)) == 0 and b.value == 480
+    assert lib.nfem_elasticity_p2_workspace_bytes(7, 10, ctypes.byref(b)) == 1
+    assert lib.nfem_cosserat_workspace_bytes(_lib.NFEM_F32, -1, ctypes.byref(b)) == 1
+    assert lib.nfem_copy_bytes(None, None, 0, None) == 0          # nothing to copy
+    assert lib.nfem_copy_bytes(None, None, 16, None) == 1         # null pointers
+    # chunk table: a layout that is not flux rows + one pressure row per cell
+    assert lib.nfem_pattern_darcy_chunks(None, 10, 5, 4, 7, None, None, None) == 1     # null table
+    dummy = ctypes.c_void_p(64)
+    rc = lib.nfem_pattern_darcy_chunks(dummy, 10, 5, 4, 7, dummy, None, None)  # p_base + n_cells != n_rows
+    assert _lib.STATUS_NAMES[rc] == "NFEM_ERR_UNSUPPORTED"
+    # Darcy assembly: bad dimension, value type, and a chunk table that does not fit the rows
+    args = [0] * 24
+    assert lib.nfem_darcy_rt1p0_assemble(4, 1, *args[2:]) == 1
+    assert lib.nfem_darcy_rt1p0_assemble(3, 9, *args[2:]) == 1
+
+
+def test_status_string_for_every_code(lib_path):
+    lib = _lib.lib()
+    for code, name in _lib.STATUS_NAMES.items():
+        s = lib.nfem_status_string(code)
+        assert s and s != b"unknown status", name
+    assert lib.nfem_status_string(999) == b"unknown status"
