@@ -308,11 +308,13 @@ def solve_only(args):
     b = -r64
     stream = torch.cuda.current_stream()
     out = {"workload": "solve", "n_dof": sp.n_dof, "restart": args.restart, "max_inner": args.max_iters}
-    out["plain_block_jacobi"] = _timed_solve(KrylovSolver(A64, pc="cell_block", A32_values=A32.values,
-                                                          restart=args.restart), b, args, stream)
-    tl = TwoLevelCoarse(A64, N_SIDE // 4)
-    out["two_level"] = _timed_solve(KrylovSolver(A64, pc="two_level", A32_values=A32.values,
-                                                 restart=args.restart, two_level=tl), b, args, stream)
+    if args.solver in ("both", "plain"):
+        out["plain_block_jacobi"] = _timed_solve(KrylovSolver(A64, pc="cell_block", A32_values=A32.values,
+                                                              restart=args.restart), b, args, stream)
+    if args.solver in ("both", "two_level"):
+        tl = TwoLevelCoarse(A64, N_SIDE // 4)
+        out["two_level"] = _timed_solve(KrylovSolver(A64, pc="two_level", A32_values=A32.values,
+                                                     restart=args.restart, two_level=tl), b, args, stream)
     return out
 
 
@@ -634,6 +636,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--restart", type=int, default=30)
     ap.add_argument("--max-iters", type=int, default=20000)
+    ap.add_argument("--solver", choices=["both", "plain", "two_level"], default="both",
+                    help="with --only solve: which preconditioners to run")
     ap.add_argument("--kernel", choices=["rows", "chunks"], default="rows",
                     help="Darcy assembly kernel: row owner (default) or cell chunks")
     ap.add_argument("--only", choices=["elasticity", "cosserat", "batch2d", "solve"], default=None,

@@ -189,9 +189,70 @@ __global__ void reduce_partials(const double* __restrict__ partial, int nb, int 
   if (threadIdx.x == 0) out[j] = mode == 1 ? sqrt(t) : sign * t;
 }
 
+// FP32 basis vectors with 16-byte rows (n and the stride multiples of 4,
+// aligned pointers): float4 loads, eight vectors per pass sharing one read
+// of y, FP32 products folded into FP64 every 16 elements per thread.
+__global__ void __launch_bounds__(kRedThreads)
+    multidot_partial_v4(int64_t n4, int k, const float4* __restrict__ X, int64_t ldx4,
+                        const float4* __restrict__ y, double* __restrict__ partial) {
+  __shared__ double sh[kDotGroup][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int j0 = 0; j0 < k; j0 += kDotGroup) {
+    const int g = min(kDotGroup, k - j0);
+    double acc[kDotGroup];
+    float accf[kDotGroup];
+#pragma unroll
+    for (int q = 0; q < kDotGroup; ++q) { acc[q] = 0.0; accf[q] = 0.f; }
+    int cnt = 0;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n4; i += stride) {
+      const float4 yv = __ldg(y + i);
+#pragma unroll
+      for (int q = 0; q < kDotGroup; ++q) {
+        if (q < g) {
+          const float4 xv = __ldg(X + int64_t(j0 + q) * ldx4 + i);
+          accf[q] = fmaf(xv.x, yv.x, fmaf(xv.y, yv.y, fmaf(xv.z, yv.z, fmaf(xv.w, yv.w, accf[q]))));
+        }
+      }
+      if (++cnt == 16) {
+#pragma unroll
+        for (int q = 0; q < kDotGroup; ++q) { acc[q] += double(accf[q]); accf[q] = 0.f; }
+        cnt = 0;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kDotGroup; ++q) {
+      double v = acc[q] + double(accf[q]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) sh[q][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < g) {
+      double t = 0.0;
+      for (int w = 0; w < (kRedThreads / 32); ++w) t += sh[threadIdx.x][w];
+      partial[int64_t(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+    }
+    __syncthreads();
+  }
+}
+
+static bool rows16(int64_t n, int64_t ldx, const void* a, const void* b) {
+  return n % 4 == 0 && ldx % 4 == 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) == 0;
+}
+
 template <typename T>
 static int multidot(int64_t n, int k, const T* X, int64_t ldx, const T* y, double* partial, double* out, int mode,
                     cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (rows16(n, ldx, X, y)) {
+      multidot_partial_v4<<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, reinterpret_cast<const float4*>(X), ldx / 4,
+                                                             reinterpret_cast<const float4*>(y), partial);
+      reduce_partials<<<k, 256, 0, s>>>(partial, kRedBlocks, k, out, mode, 1.0);
+      NFEM_CHECK_LAUNCH();
+      return NFEM_OK;
+    }
+  }
   multidot_partial<T><<<kRedBlocks, kRedThreads, 0, s>>>(n, k, X, ldx, y, partial);
   reduce_partials<<<k, 256, 0, s>>>(partial, kRedBlocks, k, out, mode, 1.0);
   NFEM_CHECK_LAUNCH();
@@ -219,6 +280,43 @@ __global__ void multi_axpy(int64_t n, int k, const T* __restrict__ X, int64_t ld
     }
     w[i] = T(float(w[i]) - a0);
     if (has2) w[i2] = T(float(w[i2]) - a1);
+  }
+}
+
+// float4 form of multi_axpy for 16-byte rows
+__global__ void multi_axpy_v4(int64_t n4, int k, const float4* __restrict__ X, int64_t ldx4,
+                              const double* __restrict__ h, float4* __restrict__ w, double hsign) {
+  __shared__ float hs[kMaxRestart + 1];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = float(hsign * h[j]);
+  __syncthreads();
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n4; i += int64_t(gridDim.x) * blockDim.x) {
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+    for (int j = 0; j < k; ++j) {
+      const float hj = hs[j];
+      const float4 xv = __ldg(X + int64_t(j) * ldx4 + i);
+      a.x = fmaf(hj, xv.x, a.x);
+      a.y = fmaf(hj, xv.y, a.y);
+      a.z = fmaf(hj, xv.z, a.z);
+      a.w = fmaf(hj, xv.w, a.w);
+    }
+    float4 v = w[i];
+    v.x -= a.x;
+    v.y -= a.y;
+    v.z -= a.z;
+    v.w -= a.w;
+    w[i] = v;
+  }
+}
+
+// w -= sign * X h over k vectors, choosing the float4 form when it applies
+static void multi_axpy_f32(int64_t n, int k, const float* X, int64_t ldx, const double* h, float* w, double hsign,
+                           cudaStream_t s) {
+  if (rows16(n, ldx, X, w)) {
+    multi_axpy_v4<<<grid_for(n / 4, 256), 256, 0, s>>>(n / 4, k, reinterpret_cast<const float4*>(X), ldx / 4, h,
+                                                        reinterpret_cast<float4*>(w), hsign);
+  } else {
+    multi_axpy<float><<<grid_for(n, 256), 256, 0, s>>>(n, k, X, ldx, h, w, hsign);
   }
 }
 
@@ -425,32 +523,45 @@ __global__ void gj_init(const double* __restrict__ ac, int n, double* __restrict
   }
 }
 
-// rc[alpha] = sum over P^T's list of alpha (rows in ascending order) of p_val * r
+// rc[alpha] = sum over P^T's list of alpha (rows in ascending order) of
+// p_val * r: one block per aggregate (its list has thousands of entries),
+// each thread a fixed stride of the list, partial sums added in a fixed order.
 __global__ void twolevel_restrict(int n_agg, const int32_t* __restrict__ pt_ptr, const int32_t* __restrict__ pt_row,
                                   const float* __restrict__ pt_val, const float* __restrict__ r,
                                   float* __restrict__ rc) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= n_agg) return;
+  __shared__ double sh[32];
+  const int agg = blockIdx.x;
+  if (agg >= n_agg) return;
   float acc = 0.f;
-  for (int32_t k = pt_ptr[warp] + lane; k < pt_ptr[warp + 1]; k += 32) acc = fmaf(pt_val[k], r[pt_row[k]], acc);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if (lane == 0) rc[warp] = acc;
+  for (int32_t k = pt_ptr[agg] + threadIdx.x; k < pt_ptr[agg + 1]; k += blockDim.x)
+    acc = fmaf(__ldg(pt_val + k), __ldg(r + __ldg(pt_row + k)), acc);
+  const double t = block_sum(double(acc), sh);
+  if (threadIdx.x == 0) rc[agg] = float(t);
 }
 
-// ec = Ainv rc  (one warp per row)
+// ec = Ainv rc  (one warp per row; 16-byte loads when n % 4 == 0 and both
+// arrays are 16-byte aligned)
 __global__ void dense_gemv(int n, const float* __restrict__ Ainv, const float* __restrict__ x, float* __restrict__ y) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= n) return;
   const float* row = Ainv + int64_t(warp) * n;
   float acc = 0.f;
-  for (int j = lane; j < n; j += 32) acc = fmaf(row[j], x[j], acc);
+  if ((n & 3) == 0 && ((reinterpret_cast<uintptr_t>(Ainv) | reinterpret_cast<uintptr_t>(x)) & 15) == 0) {
+    const float4* row4 = reinterpret_cast<const float4*>(row);
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+#pragma unroll 4
+    for (int j = lane; j < n / 4; j += 32) {
+      const float4 a = __ldg(row4 + j), b = __ldg(x4 + j);
+      acc = fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, acc))));
+    }
+  } else {
+    for (int j = lane; j < n; j += 32) acc = fmaf(row[j], x[j], acc);
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if (lane == 0) y[warp] = acc;
 }
 
-// z[i] += sum_s p_val[2i + s] ec[p_agg[2i + s]]
 __global__ void twolevel_prolong(int64_t n_rows, const int32_t* __restrict__ p_agg, const float* __restrict__ p_val,
                                  const float* __restrict__ ec, float* __restrict__ z) {
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows; i += int64_t(gridDim.x) * blockDim.x) {
@@ -762,8 +873,7 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
     float* ec = rc + na;
     NFEM_RC(spmv<float, float, float>(n, pc->a32->row_ptr, pc->a32->col_idx, (const float*)pc->a32->values, z, r2, v,
                                       1, s));
-    twolevel_restrict<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->pt_ptr, L->pt_row, L->pt_val,
-                                                                                r2, rc);
+    twolevel_restrict<<<unsigned(na), 256, 0, s>>>(na, L->pt_ptr, L->pt_row, L->pt_val, r2, rc);
     dense_gemv<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->ac_inv, rc, ec);
     twolevel_prolong<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z);
     NFEM_CHECK_LAUNCH();
@@ -893,9 +1003,9 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
         double* hcol = w.H + int64_t(j) * ldh;
         // classical Gram-Schmidt, twice
         NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, hcol, 0, s));
-        multi_axpy<float><<<gv, B, 0, s>>>(n, j + 1, w.V, n, hcol, w.w, 1.0);
+        multi_axpy_f32(n, j + 1, w.V, n, hcol, w.w, 1.0, s);
         NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, w.y, 0, s));
-        multi_axpy<float><<<gv, B, 0, s>>>(n, j + 1, w.V, n, w.y, w.w, 1.0);
+        multi_axpy_f32(n, j + 1, w.V, n, w.y, w.w, 1.0, s);
         add_small<<<1, 64, 0, s>>>(j + 1, w.y, hcol);  // h += second-pass coefficients
         NFEM_RC(multidot<float>(n, 1, w.w, n, w.w, w.partial, hcol + j + 1, 1, s));
         scale_by_inv<float><<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * n);
@@ -913,7 +1023,7 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       inner_res = hist[k - 1];
       upper_solve<<<1, 32, 0, s>>>(w.H, ldh, w.g, k, w.y);
       // d += Z y   (multi_axpy subtracts: pass -1 via hsign)
-      multi_axpy<float><<<gv, B, 0, s>>>(n, k, w.Z, n, w.y, w.d32, -1.0);
+      multi_axpy_f32(n, k, w.Z, n, w.y, w.d32, -1.0, s);
       NFEM_CHECK_LAUNCH();
       if (prm->snapshots && info->n_snapshots < prm->max_snapshots) {
         snapshot_kernel<<<gv, B, 0, s>>>(n, x, w.d32, prm->snapshots + int64_t(info->n_snapshots) * n);
