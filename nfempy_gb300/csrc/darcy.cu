@@ -32,9 +32,11 @@
 namespace nfem {
 
 constexpr int kDarcyWarps = 8;
-// minimum resident blocks per SM asked of the register allocator
+// minimum resident blocks per SM asked of the register allocator (FP32
+// kernels: 5 x 256 threads -> 48 registers, 62 % warps active; FP64 keeps
+// its registers)
 #ifndef NFEM_DARCY_MIN_BLOCKS
-#define NFEM_DARCY_MIN_BLOCKS 1
+#define NFEM_DARCY_MIN_BLOCKS 5
 #endif
 constexpr int kDarcyMaxRow = 16;
 // 2: both incidences of a row in straight-line code (their loads may
@@ -338,7 +340,8 @@ __device__ __forceinline__ int row_len_from_codes(const RowHead& h) {
 }
 
 template <typename T, int DIM, int SRC>
-__global__ void __launch_bounds__(32 * kDarcyWarps, NFEM_DARCY_MIN_BLOCKS) darcy_rows_kernel(const DarcyParams p) {
+__global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_MIN_BLOCKS : 1)
+    darcy_rows_kernel(const DarcyParams p) {
   constexpr int NLOC = DIM + 2;
   __shared__ T stage[kDarcyWarps][32 * kDarcyMaxRow];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

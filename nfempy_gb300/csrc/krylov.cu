@@ -47,12 +47,21 @@ constexpr int kSpmvWarps = 8;
 constexpr int kSpmvCap = 32 * 16;
 constexpr int kMaxRestart = 128;
 
+// Gate of a restart cycle (a device word written by an earlier kernel of the
+// same stream): a kernel given the gate returns at once while it is nonzero.
+// givens_update sets it when the cycle reaches its inner tolerance, so the
+// cycle's remaining steps cost only their launches.
+#define NFEM_GATE(g) \
+  if ((g) != nullptr && *static_cast<const volatile int32_t*>(g) != 0) return
+
 // ------------------------------------------------------------------ SpMV
 template <typename VT, typename XT, typename AT>
 __global__ void __launch_bounds__(32 * kSpmvWarps)
     spmv_kernel(int64_t n_rows, const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
                 const VT* __restrict__ val, const XT* __restrict__ x, XT* __restrict__ y,
-                const XT* __restrict__ b, int residual, const float* __restrict__ yscale) {
+                const XT* __restrict__ b, int residual, const float* __restrict__ yscale,
+                const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   __shared__ AT stage[kSpmvWarps][kSpmvCap];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   AT* st = stage[warp];
@@ -89,10 +98,10 @@ __global__ void __launch_bounds__(32 * kSpmvWarps)
 
 template <typename VT, typename XT, typename AT>
 static int spmv(int64_t n, const int32_t* rp, const int32_t* ci, const VT* v, const XT* x, XT* y, const XT* b,
-                int residual, cudaStream_t s, const float* yscale = nullptr) {
+                int residual, cudaStream_t s, const float* yscale = nullptr, const int32_t* gate = nullptr) {
   if (n == 0) return NFEM_OK;
   const int grid = grid_for(ceil_div(n, 32 * kSpmvWarps), 1, 8);
-  spmv_kernel<VT, XT, AT><<<grid, 32 * kSpmvWarps, 0, s>>>(n, rp, ci, v, x, y, b, residual, yscale);
+  spmv_kernel<VT, XT, AT><<<grid, 32 * kSpmvWarps, 0, s>>>(n, rp, ci, v, x, y, b, residual, yscale, gate);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }
@@ -122,7 +131,8 @@ constexpr int kDotGroup = 8;
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads)
     multidot_partial(int64_t n, int k, const T* __restrict__ X, int64_t ldx, const T* __restrict__ y,
-                     double* __restrict__ partial) {
+                     double* __restrict__ partial, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   __shared__ double sh[kDotGroup][kRedThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
@@ -194,7 +204,8 @@ __global__ void reduce_partials(const double* __restrict__ partial, int nb, int 
 // of y, FP32 products folded into FP64 every 16 elements per thread.
 __global__ void __launch_bounds__(kRedThreads)
     multidot_partial_v4(int64_t n4, int k, const float4* __restrict__ X, int64_t ldx4,
-                        const float4* __restrict__ y, double* __restrict__ partial) {
+                        const float4* __restrict__ y, double* __restrict__ partial, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   __shared__ double sh[kDotGroup][kRedThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
@@ -243,17 +254,17 @@ static bool rows16(int64_t n, int64_t ldx, const void* a, const void* b) {
 
 template <typename T>
 static int multidot(int64_t n, int k, const T* X, int64_t ldx, const T* y, double* partial, double* out, int mode,
-                    cudaStream_t s) {
+                    cudaStream_t s, const int32_t* gate = nullptr) {
   if constexpr (sizeof(T) == 4) {
     if (rows16(n, ldx, X, y)) {
       multidot_partial_v4<<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, reinterpret_cast<const float4*>(X), ldx / 4,
-                                                             reinterpret_cast<const float4*>(y), partial);
+                                                             reinterpret_cast<const float4*>(y), partial, gate);
       reduce_partials<<<k, 256, 0, s>>>(partial, kRedBlocks, k, out, mode, 1.0);
       NFEM_CHECK_LAUNCH();
       return NFEM_OK;
     }
   }
-  multidot_partial<T><<<kRedBlocks, kRedThreads, 0, s>>>(n, k, X, ldx, y, partial);
+  multidot_partial<T><<<kRedBlocks, kRedThreads, 0, s>>>(n, k, X, ldx, y, partial, gate);
   reduce_partials<<<k, 256, 0, s>>>(partial, kRedBlocks, k, out, mode, 1.0);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
@@ -262,7 +273,8 @@ static int multidot(int64_t n, int k, const T* X, int64_t ldx, const T* y, doubl
 // w -= sum_{j<k} h[j] X_j   (h on the device; FP64 coefficients)
 template <typename T>
 __global__ void multi_axpy(int64_t n, int k, const T* __restrict__ X, int64_t ldx, const double* __restrict__ h,
-                           T* __restrict__ w, double hsign) {
+                           T* __restrict__ w, double hsign, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   __shared__ double hs[kMaxRestart + 1];
   for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = hsign * h[j];
   __syncthreads();
@@ -285,7 +297,9 @@ __global__ void multi_axpy(int64_t n, int k, const T* __restrict__ X, int64_t ld
 
 // float4 form of multi_axpy for 16-byte rows
 __global__ void multi_axpy_v4(int64_t n4, int k, const float4* __restrict__ X, int64_t ldx4,
-                              const double* __restrict__ h, float4* __restrict__ w, double hsign) {
+                              const double* __restrict__ h, float4* __restrict__ w, double hsign,
+                              const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   __shared__ float hs[kMaxRestart + 1];
   for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = float(hsign * h[j]);
   __syncthreads();
@@ -311,18 +325,20 @@ __global__ void multi_axpy_v4(int64_t n4, int k, const float4* __restrict__ X, i
 
 // w -= sign * X h over k vectors, choosing the float4 form when it applies
 static void multi_axpy_f32(int64_t n, int k, const float* X, int64_t ldx, const double* h, float* w, double hsign,
-                           cudaStream_t s) {
+                           cudaStream_t s, const int32_t* gate = nullptr) {
   if (rows16(n, ldx, X, w)) {
     multi_axpy_v4<<<grid_for(n / 4, 256), 256, 0, s>>>(n / 4, k, reinterpret_cast<const float4*>(X), ldx / 4, h,
-                                                        reinterpret_cast<float4*>(w), hsign);
+                                                        reinterpret_cast<float4*>(w), hsign, gate);
   } else {
-    multi_axpy<float><<<grid_for(n, 256), 256, 0, s>>>(n, k, X, ldx, h, w, hsign);
+    multi_axpy<float><<<grid_for(n, 256), 256, 0, s>>>(n, k, X, ldx, h, w, hsign, gate);
   }
 }
 
 // v = w / nrm (nrm device scalar); zero when nrm is 0
 template <typename T>
-__global__ void scale_by_inv(int64_t n, const T* __restrict__ w, const double* __restrict__ nrm, T* __restrict__ v) {
+__global__ void scale_by_inv(int64_t n, const T* __restrict__ w, const double* __restrict__ nrm, T* __restrict__ v,
+                             const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   const double d = *nrm;
   const float inv = d > 0.0 ? float(1.0 / d) : 0.f;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
@@ -330,7 +346,9 @@ __global__ void scale_by_inv(int64_t n, const T* __restrict__ w, const double* _
 }
 
 // y = a (.) x  (elementwise)
-__global__ void scale_vec(int64_t n, const float* __restrict__ a, const float* __restrict__ x, float* __restrict__ y) {
+__global__ void scale_vec(int64_t n, const float* __restrict__ a, const float* __restrict__ x, float* __restrict__ y,
+                          const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
     y[i] = a[i] * x[i];
 }
@@ -528,7 +546,8 @@ __global__ void gj_init(const double* __restrict__ ac, int n, double* __restrict
 // each thread a fixed stride of the list, partial sums added in a fixed order.
 __global__ void twolevel_restrict(int n_agg, const int32_t* __restrict__ pt_ptr, const int32_t* __restrict__ pt_row,
                                   const float* __restrict__ pt_val, const float* __restrict__ r,
-                                  float* __restrict__ rc) {
+                                  float* __restrict__ rc, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   __shared__ double sh[32];
   const int agg = blockIdx.x;
   if (agg >= n_agg) return;
@@ -541,7 +560,9 @@ __global__ void twolevel_restrict(int n_agg, const int32_t* __restrict__ pt_ptr,
 
 // ec = Ainv rc  (one warp per row; 16-byte loads when n % 4 == 0 and both
 // arrays are 16-byte aligned)
-__global__ void dense_gemv(int n, const float* __restrict__ Ainv, const float* __restrict__ x, float* __restrict__ y) {
+__global__ void dense_gemv(int n, const float* __restrict__ Ainv, const float* __restrict__ x, float* __restrict__ y,
+                           const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= n) return;
   const float* row = Ainv + int64_t(warp) * n;
@@ -563,7 +584,8 @@ __global__ void dense_gemv(int n, const float* __restrict__ Ainv, const float* _
 }
 
 __global__ void twolevel_prolong(int64_t n_rows, const int32_t* __restrict__ p_agg, const float* __restrict__ p_val,
-                                 const float* __restrict__ ec, float* __restrict__ z) {
+                                 const float* __restrict__ ec, float* __restrict__ z, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows; i += int64_t(gridDim.x) * blockDim.x) {
     float acc = 0.f;
 #pragma unroll
@@ -617,7 +639,8 @@ __global__ void jacobi_setup(int64_t n, const int32_t* __restrict__ rp, const in
 }
 
 __global__ void jacobi_apply(int64_t n, const float* __restrict__ dinv, const float* __restrict__ v,
-                             float* __restrict__ z) {
+                             float* __restrict__ z, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
     z[i] = dinv[i] * v[i];
 }
@@ -684,7 +707,8 @@ __global__ void block_extract_invert(int64_t n_cells, const int32_t* __restrict_
 template <int N>
 __global__ void block_apply(int64_t n_rows, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                             const int32_t* __restrict__ cd, const float* __restrict__ inv, const float* __restrict__ v,
-                            float* __restrict__ z) {
+                            float* __restrict__ z, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n_rows; r += int64_t(gridDim.x) * blockDim.x) {
     const int32_t kb = inc_ptr[r], ke = inc_ptr[r + 1];
     float acc = 0.f;
@@ -703,8 +727,10 @@ __global__ void block_apply(int64_t n_rows, const int32_t* __restrict__ inc_ptr,
 // ------------------------------------------------------------------ Hessenberg / Givens
 // Column j of H holds h[0..j+1]; rotations cs/sn; g the rotated rhs.
 __global__ void givens_update(double* __restrict__ H, int ldh, double* __restrict__ cs, double* __restrict__ sn,
-                              double* __restrict__ g, int j, double* __restrict__ hist, int32_t* status) {
+                              double* __restrict__ g, int j, double* __restrict__ hist, int32_t* status,
+                              int32_t* __restrict__ gate, double target) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (gate && gate[0]) return;
   double* h = H + int64_t(j) * ldh;
   for (int i = 0; i < j; ++i) {
     const double t = cs[i] * h[i] + sn[i] * h[i + 1];
@@ -727,6 +753,7 @@ __global__ void givens_update(double* __restrict__ H, int ldh, double* __restric
   g[j + 1] = -sn[j] * g[j];
   g[j] = cs[j] * g[j];
   hist[j] = fabs(g[j + 1]);
+  if (gate && hist[j] <= target) gate[0] = 1;  // the rest of the cycle is skipped
 }
 
 // y = R^-1 g for the leading k x k triangle of H (stored by columns)
@@ -740,13 +767,17 @@ __global__ void upper_solve(const double* __restrict__ H, int ldh, const double*
   }
 }
 
-__global__ void add_small(int k, const double* __restrict__ y, double* __restrict__ h) {
+__global__ void add_small(int k, const double* __restrict__ y, double* __restrict__ h,
+                          const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
   for (int i = threadIdx.x; i < k; i += blockDim.x) h[i] += y[i];
 }
 
-__global__ void init_cycle(double* __restrict__ g, int m, const double* __restrict__ beta) {
+__global__ void init_cycle(double* __restrict__ g, int m, const double* __restrict__ beta, int32_t* __restrict__ gate) {
   for (int i = threadIdx.x; i <= m; i += blockDim.x) g[i] = i == 0 ? *beta : 0.0;
+  if (threadIdx.x == 0 && gate) gate[0] = 0;
 }
+
 
 }  // namespace nfem
 
@@ -841,21 +872,24 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
   return NFEM_OK;
 }
 
-static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, float* z, cudaStream_t s) {
+static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, float* z, cudaStream_t s,
+                         const int32_t* gate = nullptr) {
   const int B = 256;
   switch (pc->kind) {
     case NFEM_PC_NONE:
       NFEM_TRY_CUDA(cudaMemcpyAsync(z, v, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
       return NFEM_OK;
     case NFEM_PC_JACOBI:
-      jacobi_apply<<<grid_for(n, B), B, 0, s>>>(n, pc->diag_inv, v, z);
+      jacobi_apply<<<grid_for(n, B), B, 0, s>>>(n, pc->diag_inv, v, z, gate);
       break;
     case NFEM_PC_TWO_LEVEL:
     case NFEM_PC_CELL_BLOCK:
       if (pc->n_loc == 5)
-        block_apply<5><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z);
+        block_apply<5><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z,
+                                                    gate);
       else if (pc->n_loc == 4)
-        block_apply<4><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z);
+        block_apply<4><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z,
+                                                    gate);
       else
         return NFEM_ERR_UNSUPPORTED;
       break;
@@ -872,10 +906,10 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
     float* rc = r2 + n;
     float* ec = rc + na;
     NFEM_RC(spmv<float, float, float>(n, pc->a32->row_ptr, pc->a32->col_idx, (const float*)pc->a32->values, z, r2, v,
-                                      1, s));
-    twolevel_restrict<<<unsigned(na), 256, 0, s>>>(na, L->pt_ptr, L->pt_row, L->pt_val, r2, rc);
-    dense_gemv<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->ac_inv, rc, ec);
-    twolevel_prolong<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z);
+                                      1, s, nullptr, gate));
+    twolevel_restrict<<<unsigned(na), 256, 0, s>>>(na, L->pt_ptr, L->pt_row, L->pt_val, r2, rc, gate);
+    dense_gemv<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->ac_inv, rc, ec, gate);
+    twolevel_prolong<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z, gate);
     NFEM_CHECK_LAUNCH();
   }
   return NFEM_OK;
@@ -891,7 +925,7 @@ extern "C" int nfem_precond_apply(const nfem_precond* pc, int64_t n, const float
 struct SolveWs {
   float *V, *Z, *w, *t32, *r32, *d32;
   double *r64, *partial, *H, *cs, *sn, *g, *hist, *y, *scal;
-  int32_t* status;
+  int32_t *status, *gate;
 };
 
 static size_t solve_ws_bytes(int64_t n, int m, SolveWs* out, void* base) {
@@ -913,6 +947,7 @@ static size_t solve_ws_bytes(int64_t n, int m, SolveWs* out, void* base) {
   w.y = c.take<double>(m + 1);
   w.scal = c.take<double>(8);
   w.status = c.take<int32_t>(4);
+  w.gate = c.take<int32_t>(4);
   if (out) *out = w;
   return c.off + 256;
 }
@@ -964,7 +999,7 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
     cast_f64_f32<<<gv, B, 0, s>>>(n, w.r64, w.r32);
     fill_f32<<<gv, B, 0, s>>>(n, w.d32, 0.f);
     if (weighted)
-      scale_vec<<<gv, B, 0, s>>>(n, pc->wsqrt, w.r32, w.V);
+      scale_vec<<<gv, B, 0, s>>>(n, pc->wsqrt, w.r32, w.V, nullptr);
     else
       NFEM_TRY_CUDA(cudaMemcpyAsync(w.V, w.r32, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
     // the inner solve reduces the W-weighted residual norm by inner_rtol;
@@ -985,31 +1020,33 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       }
       first_cycle = false;
       NFEM_RC(multidot<float>(n, 1, w.V, n, w.V, w.partial, w.scal + 2, 1, s));
-      scale_by_inv<float><<<gv, B, 0, s>>>(n, w.V, w.scal + 2, w.V);
-      init_cycle<<<1, 128, 0, s>>>(w.g, m, w.scal + 2);
+      scale_by_inv<float><<<gv, B, 0, s>>>(n, w.V, w.scal + 2, w.V, nullptr);
+      init_cycle<<<1, 128, 0, s>>>(w.g, m, w.scal + 2, w.gate);
       NFEM_CHECK_LAUNCH();
       int j = 0;
       for (; j < m; ++j) {
         float* vj = w.V + int64_t(j) * n;
         float* zj = w.Z + int64_t(j) * n;
+        const int32_t* done = w.gate;
         if (weighted) {
-          scale_vec<<<gv, B, 0, s>>>(n, pc->winvsqrt, vj, w.t32);
-          NFEM_RC(precond_apply(pc, n, w.t32, zj, s));
+          scale_vec<<<gv, B, 0, s>>>(n, pc->winvsqrt, vj, w.t32, done);
+          NFEM_RC(precond_apply(pc, n, w.t32, zj, s, done));
         } else {
-          NFEM_RC(precond_apply(pc, n, vj, zj, s));
+          NFEM_RC(precond_apply(pc, n, vj, zj, s, done));
         }
         NFEM_RC(spmv<float, float, float>(n, A32->row_ptr, A32->col_idx, (const float*)A32->values, zj, w.w,
-                                          nullptr, 0, s, weighted ? pc->wsqrt : nullptr));
+                                          nullptr, 0, s, weighted ? pc->wsqrt : nullptr, done));
         double* hcol = w.H + int64_t(j) * ldh;
-        // classical Gram-Schmidt, twice
-        NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, hcol, 0, s));
-        multi_axpy_f32(n, j + 1, w.V, n, hcol, w.w, 1.0, s);
-        NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, w.y, 0, s));
-        multi_axpy_f32(n, j + 1, w.V, n, w.y, w.w, 1.0, s);
-        add_small<<<1, 64, 0, s>>>(j + 1, w.y, hcol);  // h += second-pass coefficients
-        NFEM_RC(multidot<float>(n, 1, w.w, n, w.w, w.partial, hcol + j + 1, 1, s));
-        scale_by_inv<float><<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * n);
-        givens_update<<<1, 32, 0, s>>>(w.H, ldh, w.cs, w.sn, w.g, j, w.hist, w.status);
+        // classical Gram-Schmidt, twice (the cancellation test of a selective
+        // second pass fires on nearly every Arnoldi step, so it saves nothing)
+        NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, hcol, 0, s, done));
+        multi_axpy_f32(n, j + 1, w.V, n, hcol, w.w, 1.0, s, done);
+        NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, w.y, 0, s, done));
+        multi_axpy_f32(n, j + 1, w.V, n, w.y, w.w, 1.0, s, done);
+        add_small<<<1, 64, 0, s>>>(j + 1, w.y, hcol, done);  // h += second-pass coefficients
+        NFEM_RC(multidot<float>(n, 1, w.w, n, w.w, w.partial, hcol + j + 1, 1, s, done));
+        scale_by_inv<float><<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * n, done);
+        givens_update<<<1, 32, 0, s>>>(w.H, ldh, w.cs, w.sn, w.g, j, w.hist, w.status, w.gate, inner_target);
         NFEM_CHECK_LAUNCH();
       }
       // one synchronisation per cycle: residual estimates of every step

@@ -8,8 +8,11 @@ kernels by nfempy_gb300.train_learned on seeded permeability fields; the
 scale alpha of the network's correction was chosen on a validation field).
 On a held-out field (seed 7) of 3-D mixed Darcy, 32^3 x 6 tetrahedra, both
 reach ||b - A x|| / ||b|| <= 1e-8 in FP64; the learned one needs at least
-3x fewer iterations.  The classical-weight two-level method is reported
-beside it so the network's own share stays visible."""
+3x fewer iterations.  The classical-weight two-level method runs beside
+it so the network's own share stays visible: validation chose alpha = 0 for
+the shipped checkpoint (the network's weights did not beat the classical
+ones), so the learned and classical runs match and the gain over the plain
+method comes from the two-level structure; the test checks that match."""
 import os
 
 import pytest
@@ -44,3 +47,5 @@ def test_learned_preconditioner_gain(cuda_lib):
         assert info.status == 0
         assert float(plain.residual(x, b).norm() / b.norm()) <= 1e-8
     assert i1.inner_iterations * 3 <= i0.inner_iterations
+    if alpha == 0.0:  # the network's correction is off: the same preconditioner
+        assert i1.inner_iterations == i2.inner_iterations
