@@ -47,6 +47,11 @@ constexpr int kSpmvWarps = 8;
 constexpr int kSpmvCap = 32 * 16;
 constexpr int kMaxRestart = 128;
 
+// type of the coarse inverse's trailing updates (FP64 diagonal blocks)
+#ifndef NFEM_COARSE_T
+#define NFEM_COARSE_T float
+#endif
+
 // Gate of a restart cycle (a device word written by an earlier kernel of the
 // same stream): a kernel given the gate returns at once while it is nonzero.
 // givens_update sets it when the cycle reaches its inner tolerance, so the
@@ -541,6 +546,180 @@ __global__ void gj_init(const double* __restrict__ ac, int n, double* __restrict
   }
 }
 
+// ------------------------------------------------------------------ blocked coarse inverse
+// In-place block Gauss-Jordan inversion of the coarse matrix, 64 x 64
+// blocks, no pivoting.  A_c = P^T A P is symmetric positive definite here
+// (the flux extension cancels the saddle point's sign structure:
+// A_c = (D B^T P_p)^T M (D B^T P_p) with M the flux mass matrix), so the
+// unpivoted elimination is stable.  Per block column K:
+//   D = A_KK^-1 (FP64, one block in shared memory);  A_KJ <- D A_KJ;
+//   A_IJ <- A_IJ - A_IK A_KJ;  A_IK <- -A_IK D;  A_KK <- D   (I, J != K).
+// The matrix is padded to a multiple of 64 with an identity block, whose
+// inverse is the identity again.  T is the type of the trailing updates.
+constexpr int kGjB = 64;
+
+template <typename T>
+__global__ void __launch_bounds__(256) bgj_pad(const double* __restrict__ ac, int n, int N, T* __restrict__ m) {
+  const int64_t total = int64_t(N) * N;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+    const int i = int(e / N), j = int(e - int64_t(i) * N);
+    m[e] = (i < n && j < n) ? T(ac[int64_t(i) * n + j]) : T(i == j ? 1.0 : 0.0);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) bgj_inv_diag(T* __restrict__ m, int N, int k0, T* __restrict__ dblk,
+                                                    int32_t* status) {
+  __shared__ double a[kGjB][kGjB + 1];
+  __shared__ double row[kGjB], col[kGjB];
+  for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
+    const int r = e / kGjB, c = e - r * kGjB;
+    a[r][c] = double(m[int64_t(k0 + r) * N + k0 + c]);
+  }
+  __syncthreads();
+  for (int k = 0; k < kGjB; ++k) {
+    const double p = a[k][k];
+    const double ip = p != 0.0 ? 1.0 / p : 0.0;
+    if (threadIdx.x == 0 && !(fabs(p) > 0.0)) set_status(status, NFEM_ERR_BREAKDOWN);
+    if (threadIdx.x < kGjB) {
+      row[threadIdx.x] = a[k][threadIdx.x] * ip;
+      col[threadIdx.x] = a[threadIdx.x][k];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
+      const int r = e / kGjB, c = e - r * kGjB;
+      if (r == k && c == k) a[r][c] = ip;
+      else if (r == k) a[r][c] = row[c];
+      else if (c == k) a[r][c] = -col[r] * ip;
+      else a[r][c] -= col[r] * row[c];
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
+    const int r = e / kGjB, c = e - r * kGjB;
+    dblk[e] = T(a[r][c]);
+  }
+}
+
+// 64 x 64 product of two shared-memory tiles, 4 x 4 outputs per thread
+template <typename T>
+__device__ __forceinline__ void tile_mma(const T (*x)[kGjB + 1], const T (*y)[kGjB + 1], T (&acc)[4][4]) {
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+#pragma unroll 8
+  for (int k = 0; k < kGjB; ++k) {
+    T xa[4], yb[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) xa[a] = x[ty * 4 + a][k];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) yb[b] = y[k][tx * 4 + b];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] += xa[a] * yb[b];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void load_tile(T (*t)[kGjB + 1], const T* __restrict__ src, int N, int r0, int c0) {
+  for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
+    const int r = e / kGjB, c = e - r * kGjB;
+    t[r][c] = src[int64_t(r0 + r) * N + c0 + c];
+  }
+}
+
+// mode 0: row block    A_KJ <- D A_KJ        (blockIdx.x = J tile)
+// mode 1: column block A_IK <- -A_IK D       (blockIdx.x = I tile)
+template <typename T>
+__global__ void __launch_bounds__(256) bgj_panel(T* __restrict__ m, int N, int k0, const T* __restrict__ dblk,
+                                                 int mode) {
+  extern __shared__ __align__(16) unsigned char bgj_smem[];
+  T(*d)[kGjB + 1] = reinterpret_cast<T(*)[kGjB + 1]>(bgj_smem);
+  T(*x)[kGjB + 1] = d + kGjB;
+  const int t0 = blockIdx.x * kGjB;
+  if (t0 == k0) return;
+  for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) d[e / kGjB][e % kGjB] = dblk[e];
+  if (mode == 0) load_tile(x, m, N, k0, t0);
+  else load_tile(x, m, N, t0, k0);
+  __syncthreads();
+  T acc[4][4] = {};
+  if (mode == 0) tile_mma(d, x, acc);
+  else tile_mma(x, d, acc);
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int r = ty * 4 + a, c = tx * 4 + b;
+      if (mode == 0) m[int64_t(k0 + r) * N + t0 + c] = acc[a][b];
+      else m[int64_t(t0 + r) * N + k0 + c] = -acc[a][b];
+    }
+}
+
+// A_IJ -= A_IK A_KJ for tiles I, J != K (A_KJ already updated, A_IK not yet)
+template <typename T>
+__global__ void __launch_bounds__(256) bgj_trailing(T* __restrict__ m, int N, int k0) {
+  extern __shared__ __align__(16) unsigned char bgj_smem[];
+  T(*x)[kGjB + 1] = reinterpret_cast<T(*)[kGjB + 1]>(bgj_smem);
+  T(*y)[kGjB + 1] = x + kGjB;
+  const int i0 = blockIdx.y * kGjB, j0 = blockIdx.x * kGjB;
+  if (i0 == k0 || j0 == k0) return;
+  load_tile(x, m, N, i0, k0);
+  load_tile(y, m, N, k0, j0);
+  __syncthreads();
+  T acc[4][4] = {};
+  tile_mma(x, y, acc);
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      T* e = m + int64_t(i0 + ty * 4 + a) * N + j0 + tx * 4 + b;
+      *e -= acc[a][b];
+    }
+}
+
+template <typename T>
+__global__ void bgj_put_diag(T* __restrict__ m, int N, int k0, const T* __restrict__ dblk) {
+  for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x)
+    m[int64_t(k0 + e / kGjB) * N + k0 + e % kGjB] = dblk[e];
+}
+
+template <typename T>
+__global__ void bgj_extract(const T* __restrict__ m, int n, int N, float* __restrict__ inv) {
+  const int64_t total = int64_t(n) * n;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+    const int i = int(e / n), j = int(e - int64_t(i) * n);
+    inv[e] = float(m[int64_t(i) * N + j]);
+  }
+}
+
+// Inverts the n x n FP64 matrix ac into inv (FP32) using m (N x N of T,
+// N = n rounded up to 64) and dblk (64 x 64 of T) as scratch.
+template <typename T>
+static int blocked_inverse(const double* ac, int n, T* m, T* dblk, float* inv, int32_t* status, cudaStream_t s) {
+  const int N = int(ceil_div(n, kGjB) * kGjB);
+  const int nt = N / kGjB;
+  const size_t smem = 2 * kGjB * (kGjB + 1) * sizeof(T);
+  static const bool attr = [smem] {
+    return cudaFuncSetAttribute(bgj_trailing<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) ==
+               cudaSuccess &&
+           cudaFuncSetAttribute(bgj_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) == cudaSuccess;
+  }();
+  if (!attr) return NFEM_ERR_CUDA;
+  bgj_pad<T><<<grid_for(int64_t(N) * N, 256), 256, 0, s>>>(ac, n, N, m);
+  for (int kb = 0; kb < nt; ++kb) {
+    const int k0 = kb * kGjB;
+    bgj_inv_diag<T><<<1, 256, 0, s>>>(m, N, k0, dblk, status);
+    bgj_panel<T><<<nt, 256, smem, s>>>(m, N, k0, dblk, 0);
+    bgj_trailing<T><<<dim3(nt, nt), 256, smem, s>>>(m, N, k0);
+    bgj_panel<T><<<nt, 256, smem, s>>>(m, N, k0, dblk, 1);
+    bgj_put_diag<T><<<1, 256, 0, s>>>(m, N, k0, dblk);
+  }
+  bgj_extract<T><<<grid_for(int64_t(n) * n, 256), 256, 0, s>>>(m, n, N, inv);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
 // rc[alpha] = sum over P^T's list of alpha (rows in ascending order) of
 // p_val * r: one block per aggregate (its list has thousands of entries),
 // each thread a fixed stride of the list, partial sums added in a fixed order.
@@ -859,14 +1038,22 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     NFEM_TRY_CUDA(cudaMemsetAsync(L->ac, 0, size_t(na) * na * sizeof(double), s));
     twolevel_galerkin<<<g, 256, 0, s>>>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, L->p_agg,
                                         L->p_val, na, L->ac);
-    gj_init<<<grid_for(int64_t(na) * 2 * na, 256), 256, 0, s>>>(L->ac, na, L->gj);
-    int32_t* piv = reinterpret_cast<int32_t*>(L->work);
-    for (int k = 0; k < na; ++k) {
-      gj_pivot<<<1, 1024, 0, s>>>(L->gj, na, k, piv, dev_status);
-      gj_eliminate<<<grid_for(int64_t(na) * (2 * na - k - 1), 256), 256, 0, s>>>(L->gj, na, k);
-      gj_clear_col<<<grid_for(na, 256), 256, 0, s>>>(L->gj, na, k);
+    // blocked inversion when the scratch holds the padded matrix (n >= 64:
+    // (n + 63)^2 + 64^2 entries of T fit in the 2 n^2 doubles of gj)
+    const int N = int(ceil_div(na, kGjB) * kGjB);
+    if (na >= kGjB && size_t(N) * N + kGjB * kGjB <= size_t(2) * na * na * (sizeof(double) / sizeof(NFEM_COARSE_T))) {
+      auto* m = reinterpret_cast<NFEM_COARSE_T*>(L->gj);
+      NFEM_RC(blocked_inverse<NFEM_COARSE_T>(L->ac, na, m, m + size_t(N) * N, L->ac_inv, dev_status, s));
+    } else {
+      gj_init<<<grid_for(int64_t(na) * 2 * na, 256), 256, 0, s>>>(L->ac, na, L->gj);
+      int32_t* piv = reinterpret_cast<int32_t*>(L->work);
+      for (int k = 0; k < na; ++k) {
+        gj_pivot<<<1, 1024, 0, s>>>(L->gj, na, k, piv, dev_status);
+        gj_eliminate<<<grid_for(int64_t(na) * (2 * na - k - 1), 256), 256, 0, s>>>(L->gj, na, k);
+        gj_clear_col<<<grid_for(na, 256), 256, 0, s>>>(L->gj, na, k);
+      }
+      gj_extract<<<grid_for(int64_t(na) * na, 256), 256, 0, s>>>(L->gj, na, L->ac_inv);
     }
-    gj_extract<<<grid_for(int64_t(na) * na, 256), 256, 0, s>>>(L->gj, na, L->ac_inv);
     NFEM_CHECK_LAUNCH();
   }
   return NFEM_OK;
