@@ -187,14 +187,14 @@ int nfem_pattern_darcy_chunks(const int32_t* pairs, int64_t n_rows, int n_loc, i
                               int64_t n_cells, int32_t* chunk_rows, int32_t* dev_status,
                               void* stream);
 
-/* Packs FP64 points into 16-byte FP32 records so FP32 kernels form cell edge
- * vectors with one load per vertex and without FP64 arithmetic.
- * points_split: [1 + n_points, 4] floats, 16-byte aligned.  Record 0 =
- * (lo_scale, cx, cy, cz); record v + 1 = (hx, hy, hz, q): h = float(x - c),
- * q = three signed 10-bit fields (bits 0-9, 10-19, 20-29) with
- * x - c - h ~= q * lo_scale.  c is the bounding-box centre, lo_scale about
- * 2^-33 x the half-extent: edge vectors carry an absolute error below
- * lo_scale, a relative error of about 1e-10 x (cells across the mesh). */
+/* Packs FP64 points into 16-byte fixed-point records so FP32 kernels form
+ * cell edge vectors with one load per vertex, an exact integer difference
+ * and no FP64 arithmetic.  points_split: [1 + n_points, 4] 32-bit words,
+ * 16-byte aligned.  Record 0 = (scale, cx, cy, cz) as floats; record v + 1 =
+ * (qx, qy, qz, 0) as int32, q = round((x - c) / scale), c the bounding-box
+ * centre, scale = 2^(e - 30) for a half-extent below 2^e (|q| < 2^30).  Edge
+ * vectors carry an absolute error below scale: a relative error below
+ * 1e-9 x (cells across the mesh). */
 int nfem_points_split(const double* points, int64_t n_points, float* points_split,
                       void* stream);
 

@@ -161,7 +161,7 @@ static int noalloc_scratch(int64_t** out) {
 }
 
 // ---------------------------------------------------------------- split
-// Packed point records (format in nfem_common.cuh).  Three launches: per-block
+// Packed fixed-point point records (format in nfem_common.cuh).  Three launches: per-block
 // bounding boxes, one thread folding them into the header record (centre and
 // lo_scale), then the records.  The per-block boxes are parked in the output
 // buffer's point records, which the last launch overwrites.
@@ -206,9 +206,8 @@ __global__ void bbox_partial_kernel(const double* __restrict__ p, int64_t n, dou
 }
 
 // One block: fold nb partial boxes (or, when nb == 0, the points
-// themselves) into the header record.  lo_scale = 2^(e - 34) with
-// |point - c| < 2^e, so |lo| <= 2^(e - 25) maps to |q| <= 512 (clamped to
-// 511).
+// themselves) into the header record.  scale = 2^(e - 30) with
+// |point - c| < 2^e, so the fixed-point coordinates stay below 2^30.
 __global__ void split_header_kernel(const double* __restrict__ part, int nb, const double* __restrict__ p,
                                     int64_t n, float4* __restrict__ out) {
   __shared__ double sh[6][256];
@@ -252,26 +251,22 @@ __global__ void split_header_kernel(const double* __restrict__ part, int nb, con
   }
   int e = 0;
   frexp(ext, &e);  // ext < 2^e
-  e = max(e, -92);
-  out[0] = make_float4(float(ldexp(1.0, e - 34)), c[0], c[1], c[2]);
+  e = max(e, -96);
+  out[0] = make_float4(float(ldexp(1.0, e - 30)), c[0], c[1], c[2]);
 }
 
 __global__ void split_points_kernel(const double* __restrict__ p, int64_t n, float4* __restrict__ out) {
   const float4 hd = out[0];
-  const double s = double(hd.x);
+  const double inv = 1.0 / double(hd.x);
   const double c[3] = {double(hd.y), double(hd.z), double(hd.w)};
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
-    float h[3];
-    uint32_t q = 0;
+    int q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double y = p[i * 3 + k] - c[k];
-      h[k] = __double2float_rn(y);
-      const double lo = y - double(h[k]);
-      const int qi = max(-511, min(511, int(rint(lo / s))));
-      q |= (uint32_t(qi) & 1023u) << (10 * k);
+      const double t = rint((p[i * 3 + k] - c[k]) * inv);
+      q[k] = int(fmax(-1073741823.0, fmin(1073741823.0, t)));  // |q| < 2^30
     }
-    out[1 + i] = make_float4(h[0], h[1], h[2], __uint_as_float(q));
+    out[1 + i] = make_float4(__int_as_float(q[0]), __int_as_float(q[1]), __int_as_float(q[2]), 0.0f);
   }
 }
 

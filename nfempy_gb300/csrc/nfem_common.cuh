@@ -48,26 +48,23 @@ struct Carver {
   bool ok() const { return off <= cap; }
 };
 
-// Packed FP32 point records written by nfem_points_split: record 0 holds
-// (lo_scale, cx, cy, cz); record v + 1 holds (hx, hy, hz, q) for point v,
-// where hi + lo = point - c (c = the bounding-box centre rounded to float),
-// h = float(point - c) and q packs three signed 10-bit integers
-// (bits 0-9, 10-19, 20-29) with lo_d ~= q_d * lo_scale.  An edge component
-// is then (h1 - h0) + float(q1 - q0) * lo_scale: one 16-byte load per point,
-// no FP64 arithmetic, and an absolute error of lo_scale (about 2^-33 times
-// the half-extent of the mesh).
+// Packed point records written by nfem_points_split: record 0 holds
+// (scale, cx, cy, cz) as floats; record v + 1 holds point v as three 32-bit
+// fixed-point integers q = round((x - c) / scale) (and a zero), with c the
+// bounding-box centre rounded to float and scale = 2^(e - 30) for a
+// half-extent below 2^e, so |q| < 2^30 and differences of two q fit in 32
+// bits.  An edge component is float(q1 - q0) * scale: one 16-byte load per
+// point, an exact integer difference, no FP64 arithmetic; absolute error at
+// most scale, i.e. a relative edge error below 1e-9 x (cells across the mesh).
 __device__ __forceinline__ float4 packed_point(const float* split, int32_t v) {
   return __ldg(reinterpret_cast<const float4*>(split) + 1 + v);
 }
 __device__ __forceinline__ float packed_lo_scale(const float* split) { return __ldg(split); }
-__device__ __forceinline__ int packed_q(float w, int d) {
-  return int(__float_as_uint(w) << (22 - 10 * d)) >> 22;
-}
 // edge component d of x1 - x0 from two packed records
-__device__ __forceinline__ float packed_diff(const float4& r1, const float4& r0, int d, float lo_scale) {
-  const float h1 = d == 0 ? r1.x : (d == 1 ? r1.y : r1.z);
-  const float h0 = d == 0 ? r0.x : (d == 1 ? r0.y : r0.z);
-  return (h1 - h0) + float(packed_q(r1.w, d) - packed_q(r0.w, d)) * lo_scale;
+__device__ __forceinline__ float packed_diff(const float4& r1, const float4& r0, int d, float scale) {
+  const float a = d == 0 ? r1.x : (d == 1 ? r1.y : r1.z);
+  const float b = d == 0 ? r0.x : (d == 1 ? r0.y : r0.z);
+  return float(__float_as_int(a) - __float_as_int(b)) * scale;
 }
 
 // 4-wide slot of a node column in a row image of the node-row kernels:
