@@ -548,11 +548,11 @@ __global__ void gj_init(const double* __restrict__ ac, int n, double* __restrict
 
 // ------------------------------------------------------------------ blocked coarse inverse
 // In-place block Gauss-Jordan inversion of the coarse matrix, 64 x 64
-// blocks, no pivoting.  A_c = P^T A P is symmetric positive definite here
+// blocks, no pivoting, FP32 (the inverse is stored and applied in FP32).  A_c = P^T A P is symmetric positive definite here
 // (the flux extension cancels the saddle point's sign structure:
 // A_c = (D B^T P_p)^T M (D B^T P_p) with M the flux mass matrix), so the
 // unpivoted elimination is stable.  Per block column K:
-//   D = A_KK^-1 (FP64, one block in shared memory);  A_KJ <- D A_KJ;
+//   D = A_KK^-1 (one block in shared memory);  A_KJ <- D A_KJ;
 //   A_IJ <- A_IJ - A_IK A_KJ;  A_IK <- -A_IK D;  A_KK <- D   (I, J != K).
 // The matrix is padded to a multiple of 64 with an identity block, whose
 // inverse is the identity again.  T is the type of the trailing updates.
@@ -567,19 +567,23 @@ __global__ void __launch_bounds__(256) bgj_pad(const double* __restrict__ ac, in
   }
 }
 
+#ifndef NFEM_COARSE_DIAG_T
+#define NFEM_COARSE_DIAG_T float
+#endif
 template <typename T>
 __global__ void __launch_bounds__(256) bgj_inv_diag(T* __restrict__ m, int N, int k0, T* __restrict__ dblk,
                                                     int32_t* status) {
-  __shared__ double a[kGjB][kGjB + 1];
-  __shared__ double row[kGjB], col[kGjB];
+  using D = NFEM_COARSE_DIAG_T;
+  __shared__ D a[kGjB][kGjB + 1];
+  __shared__ D row[kGjB], col[kGjB];
   for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
     const int r = e / kGjB, c = e - r * kGjB;
-    a[r][c] = double(m[int64_t(k0 + r) * N + k0 + c]);
+    a[r][c] = D(m[int64_t(k0 + r) * N + k0 + c]);
   }
   __syncthreads();
   for (int k = 0; k < kGjB; ++k) {
-    const double p = a[k][k];
-    const double ip = p != 0.0 ? 1.0 / p : 0.0;
+    const D p = a[k][k];
+    const D ip = p != D(0) ? D(1) / p : D(0);
     if (threadIdx.x == 0 && !(fabs(p) > 0.0)) set_status(status, NFEM_ERR_BREAKDOWN);
     if (threadIdx.x < kGjB) {
       row[threadIdx.x] = a[k][threadIdx.x] * ip;
