@@ -153,19 +153,28 @@ class TwoLevelCoarse:
     pressure columns).  w = None gives the classical weights 1/|a_ff|; the
     learned preconditioner passes the network's prediction."""
 
-    def __init__(self, A, n_c, w=None):
+    def __init__(self, A, n_c, w=None, cell_agg=None):
+        """cell_agg: optional aggregate of every cell (0 .. n_agg - 1) in place
+        of the centroid grid, e.g. per-problem grids for a batch of
+        independent problems assembled as one disjoint union."""
         sp = A.space
         self.A = A
         dim = sp.dim
         dev = A.values.device
-        X = sp.mesh.points[sp.cells_host]
-        cent = X.mean(axis=1)[:, :dim]
-        lo, hi = cent.min(axis=0), cent.max(axis=0)
-        idx = np.clip(np.floor((cent - lo) / np.maximum(hi - lo, 1e-300) * n_c).astype(np.int64), 0, n_c - 1)
-        agg = np.zeros(sp.n_cells, dtype=np.int64)
-        for d in range(dim):
-            agg = agg * n_c + idx[:, d]
-        self.n_agg = int(n_c ** dim)
+        if cell_agg is not None:
+            agg = np.asarray(cell_agg, dtype=np.int64)
+            if agg.shape != (sp.n_cells,) or agg.min() < 0:
+                raise ValueError("cell_agg needs one aggregate index >= 0 per cell")
+            self.n_agg = int(agg.max()) + 1
+        else:
+            X = sp.mesh.points[sp.cells_host]
+            cent = X.mean(axis=1)[:, :dim]
+            lo, hi = cent.min(axis=0), cent.max(axis=0)
+            idx = np.clip(np.floor((cent - lo) / np.maximum(hi - lo, 1e-300) * n_c).astype(np.int64), 0, n_c - 1)
+            agg = np.zeros(sp.n_cells, dtype=np.int64)
+            for d in range(dim):
+                agg = agg * n_c + idx[:, d]
+            self.n_agg = int(n_c ** dim)
         self.cell_agg_host = agg
         self.counts_host = np.bincount(agg, minlength=self.n_agg)
         if np.any(self.counts_host == 0):

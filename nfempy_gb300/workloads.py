@@ -60,3 +60,20 @@ def darcy2d_batch(n_problems=512, n_min=8, n_max=128, corr_len=0.1, sigma=1.0, s
     sp = darcy_space(u, device=device)
     kappa = np.concatenate(kappas)
     return u, sp, kappa, np.ones(kappa.shape[0]), sides
+
+
+def batch_aggregates(sides, k=4):
+    """Per-problem coarse aggregates of a darcy2d_batch union: problem i's
+    n_i x n_i square split into k x k blocks of squares (two triangles per
+    square, in meshes.square's cell order), aggregate ids offset per problem,
+    so no aggregate spans two problems."""
+    out, off = [], 0
+    for n in sides:
+        n = int(n)
+        kk = min(k, n)
+        sq = np.arange(n * n)
+        i, j = sq % n, sq // n
+        loc = (j * kk // n) * kk + (i * kk // n)
+        out.append(np.repeat(loc, 2) + off)
+        off += kk * kk
+    return np.concatenate(out)

@@ -30,3 +30,27 @@ def test_copy_bytes_refuses_pageable_host(cuda_lib):
     pageable = np.zeros(64, dtype=np.uint8)
     rc = _lib.lib().nfem_copy_bytes(_lib.ptr(d), _lib.C.c_void_p(pageable.ctypes.data), 64, _lib.stream_ptr())
     assert _lib.STATUS_NAMES[rc] == "NFEM_ERR_INVALID_ARG"
+
+
+@pytest.mark.parametrize("n_points", [1, 2, 3, 7, 1000])
+def test_points_split_records(cuda_lib, n_points):
+    """Packed fixed-point point records: the header holds a power-of-two
+    scale and the bounding-box centre, every coordinate is recovered to
+    within the scale, and edge differences come out exact in integers.  The
+    sizes cover the single-block fold (fewer than 3 points) and the partial
+    boxes of larger sets."""
+    rng = np.random.default_rng(n_points)
+    pts = rng.uniform(-3.0, 5.0, size=(n_points, 3))
+    p = torch.as_tensor(pts, device="cuda")
+    out = torch.empty((n_points + 1, 4), dtype=torch.float32, device="cuda")
+    _lib.call("nfem_points_split", _lib.ptr(p), n_points, _lib.ptr(out), _lib.stream_ptr())
+    torch.cuda.synchronize()
+    o = out.cpu()
+    scale = float(o[0, 0])
+    c = o[0, 1:].double().numpy()
+    assert np.log2(scale) == np.round(np.log2(scale))
+    np.testing.assert_allclose(c, 0.5 * (pts.min(0) + pts.max(0)), rtol=1e-6, atol=1e-6)
+    q = o[1:, :3].contiguous().view(torch.int32).numpy().astype(np.int64)
+    assert np.abs(q).max() < 2 ** 30
+    rec = q * scale + c[None, :]
+    assert np.abs(rec - pts).max() <= 0.5 * scale * (1 + 1e-9)

@@ -97,3 +97,42 @@ def test_not_converged_reports_status(cuda_lib):
     x, info = ksp.solve(-res, rtol=1e-12, max_inner=3, raise_on_failure=False)
     assert info.status == 8  # NFEM_ERR_NOT_CONVERGED
     assert info.inner_iterations <= 5
+
+
+def test_batched_union_two_level_solve(cuda_lib):
+    """A batch of independent 2-D problems solved at once: two-level FGMRES on
+    their disjoint union with aggregates inside each problem reaches 1e-8 in
+    FP64, and every problem's part equals SuperLU's solve of that problem
+    alone."""
+    import numpy as np
+    from nfempy_gb300 import meshes, workloads
+    from nfempy_gb300.solvers import KrylovSolver, TwoLevelCoarse
+    from oracle import mesh_gen, solve
+    from tests.gpu_helpers import darcy_oracle, product_space
+    sides = [6, 9, 12, 8]
+    ms = [mesh_gen.square(n) for n in sides]
+    u = meshes.union(ms)
+    rng = np.random.default_rng(2)
+    kap = np.exp(rng.normal(0.0, 1.0, sum(2 * n * n for n in sides)))
+    sp = product_space(u, [("u", "RT", 1, 1, False), ("p", "P", 0, 1, True)])
+    A = nf.CSRMatrix(sp, dtype=torch.float64)
+    res = torch.empty(A.n_rows, dtype=torch.float64, device="cuda")
+    wf = nf.LaplaceDualWeakForm(sp)
+    wf.functions = {"kappa": kap, "rhs": 1.0}
+    wf.assemble(A, res)
+    agg = workloads.batch_aggregates(sides, 3)
+    tl = TwoLevelCoarse(A, None, cell_agg=agg)
+    assert tl.n_agg == 4 * 9
+    ksp = KrylovSolver(A, pc="two_level", two_level=tl)
+    x, info = ksp.solve(-res, rtol=1e-8, max_inner=5000)
+    assert info.status == 0 and info.final_relres <= 1e-8
+    xg = x.cpu().numpy()
+    _, _, cd, nd, _ = darcy_oracle(u, kap, f_cell=np.ones(len(kap)))
+    c0 = 0
+    for k, n in enumerate(sides):
+        Ak, rk, cdk, ndk, _ = darcy_oracle(ms[k], kap[c0:c0 + 2 * n * n], f_cell=np.ones(2 * n * n))
+        xk = solve.solve_newton_step(Ak, rk)
+        loc = np.empty(ndk, dtype=np.int64)
+        loc[cdk.ravel()] = cd[c0:c0 + 2 * n * n].ravel()
+        assert np.linalg.norm(xg[loc] - xk) <= 1e-6 * np.linalg.norm(xk)
+        c0 += 2 * n * n
