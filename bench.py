@@ -255,7 +255,8 @@ def solve_bench(args, A, wf, coefs, res, stream):
     wf.assemble(A, res, coefficients=coefs)
     wf.assemble(A64, res64, coefficients=wf.coefficients(torch.float64))
     b = -res64
-    out = {"rtol": 1e-8, "krylov": f"FGMRES({args.restart}) FP32 inside FP64 iterative refinement",
+    out = {"rtol": 1e-8, "krylov": (f"FGMRES FP32 inside FP64 iterative refinement; restart {args.restart} "
+                                    f"(plain), {args.tl_restart} (two-level)"),
            "field": "log K GRF, correlation length 0.05, sigma 2.0, seed 20261208 (not a training seed)"}
     ksp = KrylovSolver(A64, pc="cell_block", A32_values=A.values, restart=args.restart)
     out["plain_block_jacobi"] = _timed_solve(ksp, b, args, stream)
@@ -263,7 +264,7 @@ def solve_bench(args, A, wf, coefs, res, stream):
     t0 = time.perf_counter()
     tl = TwoLevelCoarse(A64, nc)
     t_struct = time.perf_counter() - t0
-    ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.restart, two_level=tl)
+    ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.tl_restart, two_level=tl)
     out["two_level_classical"] = _timed_solve(ksp, b, args, stream)
     out["two_level_classical"]["host_structure_s"] = t_struct
     out["two_level_classical"]["aggregates"] = tl.n_agg
@@ -274,7 +275,7 @@ def solve_bench(args, A, wf, coefs, res, stream):
         kappa = wf.functions["kappa"]
         tl2 = TwoLevelCoarse(A64, nc)
         tl2.set_weights(learned.learned_weights(tl2, model, kappa, alpha))
-        ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.restart, two_level=tl2)
+        ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.tl_restart, two_level=tl2)
         out["learned"] = _timed_solve(ksp, b, args, stream)
         out["learned"]["alpha"] = alpha
         out["learned"]["training"] = {k: ck["record"][k] for k in ("n", "fields", "solves_used", "pairs",
@@ -314,7 +315,7 @@ def solve_only(args):
     if args.solver in ("both", "two_level"):
         tl = TwoLevelCoarse(A64, N_SIDE // 4)
         out["two_level"] = _timed_solve(KrylovSolver(A64, pc="two_level", A32_values=A32.values,
-                                                     restart=args.restart, two_level=tl), b, args, stream)
+                                                     restart=args.tl_restart, two_level=tl), b, args, stream)
     return out
 
 
@@ -448,7 +449,7 @@ def batch2d_bench(args):
         t0 = time.perf_counter()
         tl = TwoLevelCoarse(A64, None, cell_agg=wl.batch_aggregates(sides, 4))
         t_struct = time.perf_counter() - t0
-        ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.restart, two_level=tl)
+        ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.tl_restart, two_level=tl)
         out["solve"] = _timed_solve(ksp, -r64, args, torch.cuda.current_stream())
         out["solve"].update({"preconditioner": "two-level, 4x4 aggregates per problem", "aggregates": tl.n_agg,
                              "host_structure_s": t_struct})
@@ -657,7 +658,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
-    ap.add_argument("--restart", type=int, default=30)
+    ap.add_argument("--restart", type=int, default=50, help="FGMRES restart of the plain block-Jacobi solve")
+    ap.add_argument("--tl-restart", type=int, default=20, help="FGMRES restart of the two-level solves")
     ap.add_argument("--max-iters", type=int, default=20000)
     ap.add_argument("--solver", choices=["both", "plain", "two_level"], default="both",
                     help="with --only solve: which preconditioners to run")

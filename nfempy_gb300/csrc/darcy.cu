@@ -490,7 +490,11 @@ __device__ __forceinline__ void warp_chunk_rows(const DarcyParams& p, WarpChunk<
     const int64_t r = r0 + lane;
     const bool valid = r < last;
     const RowHead h = load_head(p, valid ? r : p.n_rows);
-    const int32_t base = __ldg(p.row_ptr + r0);
+    // row lengths and offsets from row_ptr (every lane joins the shuffles)
+    const int32_t rpl = __ldg(p.row_ptr + (r < p.n_rows ? r : p.n_rows));
+    const int32_t rpe = __ldg(p.row_ptr + (r0 + 32 < last ? r0 + 32 : last));
+    const int32_t base = __shfl_sync(0xffffffffu, rpl, 0);
+    const int32_t rp_down = __shfl_down_sync(0xffffffffu, rpl, 1);
     const int occ[2] = {h.pr.x, h.pr.y};
     const uint32_t code[2] = {h.cd.x, h.cd.y};
     int32_t c[2];
@@ -503,16 +507,11 @@ __device__ __forceinline__ void warp_chunk_rows(const DarcyParams& p, WarpChunk<
       a[t] = on[t] ? occ[t] - c[t] * NLOC : 0;
     }
     const int q1 = (is_flux && valid && on[1]) ? int(w.slot[r - first]) : -1;
-    const int len = valid ? row_len_from_codes<NLOC>(h) : 0;
-    int incl = len;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const int off = incl - len;
-    const int span = __shfl_sync(0xffffffffu, incl, 31);
-    if (span > 32 * kDarcyMaxRow) {
+    const int32_t rpn = lane == 31 ? rpe : rp_down;
+    const int len = valid ? rpn - rpl : 0;
+    const int off = rpl - base;
+    const int span = rpe - base;
+    if (span > 32 * kDarcyMaxRow || span < 0) {
       if (lane == 0) set_status(p.status, NFEM_ERR_PATTERN);
       continue;
     }
@@ -559,17 +558,19 @@ __device__ __forceinline__ void warp_chunk_rows(const DarcyParams& p, WarpChunk<
         }
         const uint32_t cd = code[t];
         const int at = a[t];
+        if (direct) {
+          T d = T(0);
 #pragma unroll
-        for (int b = 0; b < NLOC; ++b) {
-          const int idx = min(off + int((cd >> (4 * b)) & 15u), kCap);
-          if (!direct) {
-            st[idx] += v[b];
-          } else if (two && b == at) {
-            if (t == 0) diag = v[b];
-            else st[idx] = diag + v[b];
-          } else {
-            st[idx] = v[b];
+          for (int b = 0; b < NLOC; ++b) d = (b == at) ? v[b] : d;
+#pragma unroll
+          for (int b = 0; b < NLOC; ++b) {
+            const int idx = min(off + int((cd >> (4 * b)) & 15u), kCap);
+            st[idx] = (t == 1 && b == at) ? v[b] + diag : v[b];
           }
+          if (t == 0) diag = d;
+        } else {
+#pragma unroll
+          for (int b = 0; b < NLOC; ++b) st[min(off + int((cd >> (4 * b)) & 15u), kCap)] += v[b];
         }
       }
     }
