@@ -31,7 +31,10 @@
 
 namespace nfem {
 
-constexpr int kDarcyWarps = 8;
+#ifndef NFEM_DARCY_WARPS
+#define NFEM_DARCY_WARPS 8
+#endif
+constexpr int kDarcyWarps = NFEM_DARCY_WARPS;  // warps per block of the row-owner kernel
 // minimum resident blocks per SM asked of the register allocator (FP32
 // kernels: 5 x 256 threads -> 48 registers, 62 % warps active; FP64 keeps
 // its registers)

@@ -81,17 +81,21 @@ __global__ void __launch_bounds__(32 * kSpmvWarps)
     const int32_t end = __shfl_sync(0xffffffffu, re, last);
     const int span = end - base;
     AT acc = AT(0);
-    if (span <= kSpmvCap) {
-      for (int i = lane; i < span; i += 32) {
-        const int64_t k = int64_t(base) + i;
+    // the warp's contiguous segment in pieces of kSpmvCap products, each
+    // loaded coalesced; every lane then sums its own row's part in column
+    // order (long rows, e.g. vector P2 elasticity, take several pieces)
+    for (int c0 = 0; c0 < span; c0 += kSpmvCap) {
+      const int cl = min(kSpmvCap, span - c0);
+      for (int i = lane; i < cl; i += 32) {
+        const int64_t k = int64_t(base) + c0 + i;
         st[i] = AT(__ldg(val + k)) * AT(__ldg(x + __ldg(col + k)));
       }
       __syncwarp();
-      if (valid)
-        for (int32_t k = rb - base; k < re - base; ++k) acc += st[k];
+      if (valid) {
+        const int k0 = max(rb - base, c0), k1 = min(re - base, c0 + cl);
+        for (int k = k0; k < k1; ++k) acc += st[k - c0];
+      }
       __syncwarp();
-    } else if (valid) {
-      for (int32_t k = rb; k < re; ++k) acc += AT(__ldg(val + k)) * AT(__ldg(x + __ldg(col + k)));
     }
     if (valid) {
       AT out = residual ? AT(b[r]) - acc : acc;
