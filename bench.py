@@ -198,7 +198,7 @@ def run_reference(args):
         return
     import multiprocessing as mp
     cores = os.cpu_count() or 1
-    per_core = 120
+    per_core = 600
     prob = cpu_problem(N_SIDE, per_core * cores)
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:

@@ -32,14 +32,15 @@
 namespace nfem {
 
 #ifndef NFEM_DARCY_WARPS
-#define NFEM_DARCY_WARPS 8
+#define NFEM_DARCY_WARPS 4
 #endif
 constexpr int kDarcyWarps = NFEM_DARCY_WARPS;  // warps per block of the row-owner kernel
 // minimum resident blocks per SM asked of the register allocator (FP32
-// kernels: 5 x 256 threads -> 48 registers, 62 % warps active; FP64 keeps
-// its registers)
+// kernels: 10 x 128 threads -> 48 registers, 62 % warps active; FP64 keeps
+// its registers).  Measured at 64^3 x 6: 4 warps x 10 blocks 98.2 us,
+// 8 x 5 99.2 us, 16 x 2 110 us, 4 x 12 (40 registers, spills) 177 us.
 #ifndef NFEM_DARCY_MIN_BLOCKS
-#define NFEM_DARCY_MIN_BLOCKS 5
+#define NFEM_DARCY_MIN_BLOCKS 10
 #endif
 constexpr int kDarcyMaxRow = 16;
 // 2: both incidences of a row in straight-line code (their loads may
