@@ -426,6 +426,7 @@ def batch2d_bench(args):
     """512 independent 2-D mixed Darcy problems (n_i ~ U{8..128} squares per
     side, 2 n_i^2 triangles, log K_i GRF with correlation length 0.1 and
     sigma 1, f = 1) assembled in one launch over their disjoint union, FP32."""
+    import numpy as np
     import torch
     import nfempy_gb300 as nf
     from nfempy_gb300 import workloads as wl
@@ -456,17 +457,21 @@ def batch2d_bench(args):
                         "algorithmic_bytes": alg, "peak_source": kind}}
     if not args.no_solve:
         # every problem at once: two-level FGMRES on the block-diagonal union,
-        # with 4 x 4 aggregates inside each problem (none spans two problems)
+        # aggregates of about s x s squares inside each problem (none spans
+        # two problems) and the coarse matrix stored per problem
         from nfempy_gb300.solvers import KrylovSolver, TwoLevelCoarse
         A64 = A.with_dtype(torch.float64)
         r64 = torch.empty(A.n_rows, dtype=torch.float64, device="cuda")
         wf.assemble(A64, r64, coefficients=wf.coefficients(torch.float64))
         t0 = time.perf_counter()
-        tl = TwoLevelCoarse(A64, None, cell_agg=wl.batch_aggregates(sides, 4))
+        agg, bp = wl.batch_aggregates(sides, size=args.batch_agg, blocks=True)
+        tl = TwoLevelCoarse(A64, None, cell_agg=agg, blocks=bp)
         t_struct = time.perf_counter() - t0
         ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.tl_restart, two_level=tl)
         out["solve"] = _timed_solve(ksp, -r64, args, torch.cuda.current_stream())
-        out["solve"].update({"preconditioner": "two-level, 4x4 aggregates per problem", "aggregates": tl.n_agg,
+        out["solve"].update({"preconditioner": f"two-level, {args.batch_agg}x{args.batch_agg}-square aggregates, "
+                                               "coarse matrix block-diagonal per problem",
+                             "aggregates": tl.n_agg, "largest_block": int(np.diff(bp).max()),
                              "host_structure_s": t_struct})
     return out
 
@@ -676,6 +681,8 @@ def main():
     ap.add_argument("--restart", type=int, default=50, help="FGMRES restart of the plain block-Jacobi solve")
     ap.add_argument("--tl-restart", type=int, default=20, help="FGMRES restart of the two-level solves")
     ap.add_argument("--max-iters", type=int, default=20000)
+    ap.add_argument("--batch-agg", type=int, default=8,
+                    help="aggregate side in squares of the batched 2-D two-level solve")
     ap.add_argument("--solver", choices=["both", "plain", "two_level"], default="both",
                     help="with --only solve: which preconditioners to run")
     ap.add_argument("--kernel", choices=["rows", "chunks"], default="rows",

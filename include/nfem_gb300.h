@@ -371,11 +371,27 @@ typedef struct {
   const int32_t* pt_row;     /* [pt_nnz] */
   const int32_t* pt_slot;    /* [pt_nnz] index 2 * row + slot into p_val */
   float* pt_val;             /* [pt_nnz] filled by nfem_precond_setup */
-  double* ac;                /* [n_agg, n_agg] Galerkin coarse matrix */
-  double* gj;                /* [n_agg, 2 n_agg] Gauss-Jordan scratch */
-  float* ac_inv;             /* [n_agg, n_agg] */
+  double* ac;                /* [n_agg, n_agg] Galerkin coarse matrix (blocks: [ac_entries]) */
+  double* gj;                /* [n_agg, 2 n_agg] Gauss-Jordan scratch (blocks: [ac_entries]) */
+  float* ac_inv;             /* [n_agg, n_agg] (blocks: [ac_entries]) */
   float* work;               /* [64 + n_rows + 2 n_agg] */
+  /* Block-diagonal coarse matrix (n_blocks > 0): a batch of independent
+   * problems assembled as one disjoint union has no coupling between the
+   * aggregates of different problems, so Ac is stored, inverted and applied
+   * block by block.  The aggregates of block b are blk_ptr[b] ..
+   * blk_ptr[b + 1] - 1; block b's s_b x s_b entries (row-major) start at
+   * blk_off[b] in ac, gj and ac_inv.  A nonzero of A coupling two blocks is
+   * an error (NFEM_ERR_INVALID_ARG in the device status).  n_blocks = 0 keeps
+   * the dense n_agg x n_agg layout and leaves the fields below unread. */
+  int32_t n_blocks;
+  int32_t blk_max;           /* largest s_b, at most NFEM_COARSE_BLOCK_MAX */
+  int64_t ac_entries;        /* blk_off[n_blocks] */
+  const int32_t* blk_ptr;    /* [n_blocks + 1] */
+  const int64_t* blk_off;    /* [n_blocks + 1] */
+  const int32_t* agg_blk;    /* [n_agg] block of each aggregate */
 } nfem_two_level;
+
+#define NFEM_COARSE_BLOCK_MAX 1024
 
 typedef struct {
   int kind;

@@ -18,6 +18,7 @@ NFEM_F32 = 1
 NFEM_BF16 = 2
 COEF_NONE, COEF_CELL, COEF_QPOINT = 0, 1, 2
 DARCY_CHUNK_CELLS = 32  # NFEM_DARCY_CHUNK_CELLS
+COARSE_BLOCK_MAX = 1024  # NFEM_COARSE_BLOCK_MAX
 
 STATUS_NAMES = {
     0: "NFEM_OK", 1: "NFEM_ERR_INVALID_ARG", 2: "NFEM_ERR_CUDA", 3: "NFEM_ERR_WORKSPACE",
@@ -47,7 +48,9 @@ class TwoLevel(C.Structure):
     _fields_ = [("p_base", C.c_int64), ("n_agg", C.c_int32), ("cell_agg", C.c_void_p), ("w", C.c_void_p),
                 ("p_agg", C.c_void_p), ("p_val", C.c_void_p), ("pt_nnz", C.c_int64), ("pt_ptr", C.c_void_p),
                 ("pt_row", C.c_void_p), ("pt_slot", C.c_void_p), ("pt_val", C.c_void_p), ("ac", C.c_void_p),
-                ("gj", C.c_void_p), ("ac_inv", C.c_void_p), ("work", C.c_void_p)]
+                ("gj", C.c_void_p), ("ac_inv", C.c_void_p), ("work", C.c_void_p), ("n_blocks", C.c_int32),
+                ("blk_max", C.c_int32), ("ac_entries", C.c_int64), ("blk_ptr", C.c_void_p), ("blk_off", C.c_void_p),
+                ("agg_blk", C.c_void_p)]
 
 
 class Precond(C.Structure):

@@ -26,6 +26,7 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "nfem_common.cuh"
@@ -45,6 +46,10 @@ constexpr int kRedBlocks = 1216;  // 8 x 152 SMs
 constexpr int kRedThreads = 256;
 constexpr int kSpmvWarps = 8;
 constexpr int kSpmvCap = 32 * 16;
+#ifndef NFEM_SPMV_UNROLL
+#define NFEM_SPMV_UNROLL 4
+#endif
+constexpr int kSpmvUnroll = NFEM_SPMV_UNROLL;
 constexpr int kMaxRestart = 128;
 
 // type of the coarse inverse's trailing updates (FP64 diagonal blocks)
@@ -86,9 +91,23 @@ __global__ void __launch_bounds__(32 * kSpmvWarps)
     // order (long rows, e.g. vector P2 elasticity, take several pieces)
     for (int c0 = 0; c0 < span; c0 += kSpmvCap) {
       const int cl = min(kSpmvCap, span - c0);
-      for (int i = lane; i < cl; i += 32) {
-        const int64_t k = int64_t(base) + c0 + i;
-        st[i] = AT(__ldg(val + k)) * AT(__ldg(x + __ldg(col + k)));
+      // kSpmvUnroll products per lane in flight: the columns and values
+      // first, then the gathers of x they name
+      for (int i0 = lane; i0 < cl; i0 += 32 * kSpmvUnroll) {
+        int32_t cc[kSpmvUnroll];
+        VT vv[kSpmvUnroll];
+#pragma unroll
+        for (int u = 0; u < kSpmvUnroll; ++u) {
+          const int i = i0 + 32 * u;
+          const int64_t k = int64_t(base) + c0 + i;
+          cc[u] = i < cl ? __ldg(col + k) : 0;
+          vv[u] = i < cl ? __ldg(val + k) : VT(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kSpmvUnroll; ++u) {
+          const int i = i0 + 32 * u;
+          if (i < cl) st[i] = AT(vv[u]) * AT(__ldg(x + cc[u]));
+        }
       }
       __syncwarp();
       if (valid) {
@@ -449,10 +468,27 @@ __global__ void twolevel_fill_p(int64_t n_rows, const int32_t* __restrict__ rp, 
   }
 }
 
+// Position of coarse entry (alpha, beta): dense row-major, or inside the
+// diagonal block of alpha (block layout); -1 when beta lies in another block.
+struct CoarseIndex {
+  int n_agg;
+  const int32_t* blk_ptr;
+  const int64_t* blk_off;
+  const int32_t* agg_blk;  // nullptr: dense
+  __device__ int64_t operator()(int32_t a, int32_t b) const {
+    if (!agg_blk) return int64_t(a) * n_agg + b;
+    const int32_t blk = agg_blk[a];
+    if (agg_blk[b] != blk) return -1;
+    const int32_t b0 = blk_ptr[blk];
+    return blk_off[blk] + int64_t(a - b0) * (blk_ptr[blk + 1] - b0) + (b - b0);
+  }
+};
+
 // ac[alpha, beta] += P[i, alpha] A[i, j] P[j, beta] over the nonzeros of A
 __global__ void twolevel_galerkin(int64_t n_rows, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                   const double* __restrict__ v, const int32_t* __restrict__ p_agg,
-                                  const float* __restrict__ p_val, int n_agg, double* __restrict__ ac) {
+                                  const float* __restrict__ p_val, CoarseIndex at, double* __restrict__ ac,
+                                  int32_t* status) {
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows; i += int64_t(gridDim.x) * blockDim.x) {
     const int32_t ai0 = p_agg[2 * i], ai1 = p_agg[2 * i + 1];
     const double pi0 = p_val[2 * i], pi1 = p_val[2 * i + 1];
@@ -465,8 +501,18 @@ __global__ void twolevel_galerkin(int64_t n_rows, const int32_t* __restrict__ rp
         const int32_t bj = p_agg[2 * j + sj];
         const double pj = p_val[2 * j + sj];
         if (bj < 0 || pj == 0.0) continue;
-        if (ai0 >= 0 && pi0 != 0.0) atomicAdd(ac + int64_t(ai0) * n_agg + bj, pi0 * aij * pj);
-        if (ai1 >= 0 && pi1 != 0.0) atomicAdd(ac + int64_t(ai1) * n_agg + bj, pi1 * aij * pj);
+#pragma unroll
+        for (int si = 0; si < 2; ++si) {
+          const int32_t ai = si ? ai1 : ai0;
+          const double pi = si ? pi1 : pi0;
+          if (ai < 0 || pi == 0.0) continue;
+          const int64_t e = at(ai, bj);
+          if (e < 0) {
+            set_status(status, NFEM_ERR_INVALID_ARG);
+            continue;
+          }
+          atomicAdd(ac + e, pi * aij * pj);
+        }
       }
     }
   }
@@ -728,6 +774,75 @@ static int blocked_inverse(const double* ac, int n, T* m, T* dblk, float* inv, i
   return NFEM_OK;
 }
 
+// ------------------------------------------------------------------ block-diagonal coarse inverse
+// One CTA per diagonal block: in-place Gauss-Jordan inversion in FP64 of the
+// block copied into gj, no pivoting (each block is a Galerkin matrix of the
+// same SPD form as the dense case), then rounded into ac_inv.  Step k:
+//   p = 1 / a_kk;  a_kj *= p (j != k);  a_ij -= a_ik a_kj (i, j != k);
+//   a_ik = -a_ik p (i != k);  a_kk = p.
+__global__ void __launch_bounds__(256) coarse_block_inverse(int n_blocks, const int32_t* __restrict__ blk_ptr,
+                                                            const int64_t* __restrict__ blk_off,
+                                                            const double* __restrict__ ac, double* __restrict__ gj,
+                                                            float* __restrict__ inv, int32_t* status) {
+  __shared__ double piv;
+  for (int blk = blockIdx.x; blk < n_blocks; blk += gridDim.x) {
+    const int s = blk_ptr[blk + 1] - blk_ptr[blk];
+    const int64_t ss = int64_t(s) * s;
+    const double* a0 = ac + blk_off[blk];
+    double* m = gj + blk_off[blk];
+    for (int64_t e = threadIdx.x; e < ss; e += blockDim.x) m[e] = a0[e];
+    __syncthreads();
+    for (int k = 0; k < s; ++k) {
+      if (threadIdx.x == 0) {
+        const double d = m[int64_t(k) * s + k];
+        if (!(d > 0.0)) set_status(status, NFEM_ERR_BREAKDOWN);
+        piv = d > 0.0 ? 1.0 / d : 0.0;
+      }
+      __syncthreads();
+      const double p = piv;
+      for (int j = threadIdx.x; j < s; j += blockDim.x)
+        if (j != k) m[int64_t(k) * s + j] *= p;
+      __syncthreads();
+      for (int i = threadIdx.x >> 5; i < s; i += blockDim.x >> 5) {
+        if (i == k) continue;
+        double* mi = m + int64_t(i) * s;
+        const double f = mi[k];
+        if (f != 0.0)
+          for (int j = threadIdx.x & 31; j < s; j += 32)
+            if (j != k) mi[j] = fma(-f, m[int64_t(k) * s + j], mi[j]);
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < s; i += blockDim.x) {
+        if (i != k) m[int64_t(i) * s + k] *= -p;
+        else m[int64_t(k) * s + k] = p;
+      }
+      __syncthreads();
+    }
+    float* out = inv + blk_off[blk];
+    for (int64_t e = threadIdx.x; e < ss; e += blockDim.x) out[e] = float(m[e]);
+    __syncthreads();
+  }
+}
+
+// ec[alpha] = sum over alpha's block of Ainv[alpha, beta] rc[beta]  (one warp
+// per aggregate)
+__global__ void block_gemv(int n_agg, const int32_t* __restrict__ blk_ptr, const int64_t* __restrict__ blk_off,
+                           const int32_t* __restrict__ agg_blk, const float* __restrict__ Ainv,
+                           const float* __restrict__ x, float* __restrict__ y, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n_agg) return;
+  const int32_t blk = __ldg(agg_blk + warp);
+  const int32_t b0 = __ldg(blk_ptr + blk), s = __ldg(blk_ptr + blk + 1) - b0;
+  const float* row = Ainv + __ldg(blk_off + blk) + int64_t(warp - b0) * s;
+  const float* xb = x + b0;
+  float acc = 0.f;
+  for (int j = lane; j < s; j += 32) acc = fmaf(__ldg(row + j), __ldg(xb + j), acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) y[warp] = acc;
+}
+
 // rc[alpha] = sum over P^T's list of alpha (rows in ascending order) of
 // p_val * r: one block per aggregate (its list has thousands of entries),
 // each thread a fixed stride of the list, partial sums added in a fixed order.
@@ -743,6 +858,24 @@ __global__ void twolevel_restrict(int n_agg, const int32_t* __restrict__ pt_ptr,
     acc = fmaf(__ldg(pt_val + k), __ldg(r + __ldg(pt_row + k)), acc);
   const double t = block_sum(double(acc), sh);
   if (threadIdx.x == 0) rc[agg] = float(t);
+}
+
+// The same sum with one warp per aggregate, for short lists (many small
+// aggregates): lanes take a fixed stride of the list, then a fixed-order
+// shuffle reduction.
+__global__ void twolevel_restrict_warp(int n_agg, const int32_t* __restrict__ pt_ptr,
+                                       const int32_t* __restrict__ pt_row, const float* __restrict__ pt_val,
+                                       const float* __restrict__ r, float* __restrict__ rc,
+                                       const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
+  const int agg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (agg >= n_agg) return;
+  float acc = 0.f;
+  for (int32_t k = __ldg(pt_ptr + agg) + lane; k < __ldg(pt_ptr + agg + 1); k += 32)
+    acc = fmaf(__ldg(pt_val + k), __ldg(r + __ldg(pt_row + k)), acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) rc[agg] = acc;
 }
 
 // ec = Ainv rc  (one warp per row; 16-byte loads when n % 4 == 0 and both
@@ -1004,6 +1137,9 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
       if (!L || L->n_agg < 1 || !L->cell_agg || !L->w || !L->p_agg || !L->p_val || !L->pt_ptr || !L->pt_row ||
           !L->pt_slot || !L->pt_val || !L->ac || !L->ac_inv || !L->gj || !L->work)
         return NFEM_ERR_INVALID_ARG;
+      if (L->n_blocks < 0 || (L->n_blocks > 0 && (!L->blk_ptr || !L->blk_off || !L->agg_blk || L->blk_max < 1 ||
+                                                  L->blk_max > NFEM_COARSE_BLOCK_MAX || L->ac_entries < 1)))
+        return NFEM_ERR_INVALID_ARG;
     }
     const int g = grid_for(pc->n_cells, 128);
     switch (pc->n_loc) {
@@ -1043,9 +1179,18 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     twolevel_fill_p<<<g, 256, 0, s>>>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, L->p_base,
                                       pc->n_cells, L->cell_agg, L->w, L->p_agg, L->p_val);
     twolevel_fill_pt<<<grid_for(L->pt_nnz, 256), 256, 0, s>>>(L->pt_nnz, L->pt_slot, L->p_val, L->pt_val);
-    NFEM_TRY_CUDA(cudaMemsetAsync(L->ac, 0, size_t(na) * na * sizeof(double), s));
+    const bool blocks = L->n_blocks > 0;
+    const CoarseIndex at{na, L->blk_ptr, L->blk_off, blocks ? L->agg_blk : nullptr};
+    NFEM_TRY_CUDA(cudaMemsetAsync(L->ac, 0, size_t(blocks ? L->ac_entries : int64_t(na) * na) * sizeof(double), s));
     twolevel_galerkin<<<g, 256, 0, s>>>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, L->p_agg,
-                                        L->p_val, na, L->ac);
+                                        L->p_val, at, L->ac, dev_status);
+    if (blocks) {
+      coarse_block_inverse<<<unsigned(std::min(L->n_blocks, 65535)), 256, 0, s>>>(L->n_blocks, L->blk_ptr,
+                                                                                L->blk_off, L->ac, L->gj,
+                                                                                L->ac_inv, dev_status);
+      NFEM_CHECK_LAUNCH();
+      return NFEM_OK;
+    }
     // blocked inversion when the scratch holds the padded matrix (n >= 64:
     // (n + 63)^2 + 64^2 entries of T fit in the 2 n^2 doubles of gj)
     const int N = int(ceil_div(na, kGjB) * kGjB);
@@ -1105,8 +1250,17 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
     // against 205 iterations and a longer solve at 64^3 x 6)
     NFEM_RC(spmv<float, float, float>(n, pc->a32->row_ptr, pc->a32->col_idx, (const float*)pc->a32->values, z, r2, v,
                                       1, s, nullptr, gate));
-    twolevel_restrict<<<unsigned(na), 256, 0, s>>>(na, L->pt_ptr, L->pt_row, L->pt_val, r2, rc, gate);
-    dense_gemv<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->ac_inv, rc, ec, gate);
+    // a block per aggregate for long P^T lists, a warp per aggregate for short ones
+    if (L->pt_nnz >= int64_t(na) * 1024)
+      twolevel_restrict<<<unsigned(na), 256, 0, s>>>(na, L->pt_ptr, L->pt_row, L->pt_val, r2, rc, gate);
+    else
+      twolevel_restrict_warp<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->pt_ptr, L->pt_row,
+                                                                                       L->pt_val, r2, rc, gate);
+    if (L->n_blocks > 0)
+      block_gemv<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->blk_ptr, L->blk_off, L->agg_blk,
+                                                                           L->ac_inv, rc, ec, gate);
+    else
+      dense_gemv<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->ac_inv, rc, ec, gate);
     twolevel_prolong<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z, gate);
     NFEM_CHECK_LAUNCH();
   }
@@ -1120,21 +1274,32 @@ extern "C" int nfem_precond_apply(const nfem_precond* pc, int64_t n, const float
 }
 
 // workspace layout of the solver
+// entries n .. ld - 1 of count vectors of stride ld set to zero
+__global__ void zero_tails(float* __restrict__ base, int count, int64_t ld, int64_t n) {
+  const int w = int(ld - n);
+  for (int e = threadIdx.x; e < count * w; e += blockDim.x) base[int64_t(e / w) * ld + n + e % w] = 0.f;
+}
+
 struct SolveWs {
   float *V, *Z, *w, *t32, *r32, *d32;
   double *r64, *partial, *H, *cs, *sn, *g, *hist, *y, *scal;
   int32_t *status, *gate;
 };
 
+// FP32 Krylov vectors are padded to a multiple of four entries (zero tails)
+// so that the Gram-Schmidt kernels always take 16-byte rows.
+static int64_t padded4(int64_t n) { return (n + 3) & ~int64_t(3); }
+
 static size_t solve_ws_bytes(int64_t n, int m, SolveWs* out, void* base) {
   Carver c{reinterpret_cast<char*>(base), 0, ~size_t(0)};
   SolveWs w;
-  w.V = c.take<float>(size_t(m + 1) * n);
-  w.Z = c.take<float>(size_t(m) * n);
-  w.w = c.take<float>(n);
-  w.t32 = c.take<float>(n);
-  w.r32 = c.take<float>(n);
-  w.d32 = c.take<float>(n);
+  const int64_t ld = padded4(n);
+  w.V = c.take<float>(size_t(m + 1) * ld);
+  w.Z = c.take<float>(size_t(m) * ld);
+  w.w = c.take<float>(ld);
+  w.t32 = c.take<float>(ld);
+  w.r32 = c.take<float>(ld);
+  w.d32 = c.take<float>(ld);
   w.r64 = c.take<double>(n);
   w.partial = c.take<double>(size_t(kRedBlocks) * (m + 2));
   w.H = c.take<double>(size_t(m) * (m + 1));
@@ -1175,6 +1340,18 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
   const int gv = grid_for(n, B);
   const int ldh = m + 1;
   NFEM_TRY_CUDA(cudaMemsetAsync(w.status, 0, 4 * sizeof(int32_t), s));
+  // ld: stride of the basis vectors; entries n .. ld - 1 of every FP32 vector
+  // are zero and stay zero (kernels of length n never write them, the
+  // Gram-Schmidt updates of length ld add zero to them)
+  const int64_t ld = padded4(n);
+  if (ld > n) {
+    zero_tails<<<1, 256, 0, s>>>(w.V, m + 1, ld, n);
+    zero_tails<<<1, 256, 0, s>>>(w.Z, m, ld, n);
+    zero_tails<<<1, 64, 0, s>>>(w.w, 1, ld, n);
+    zero_tails<<<1, 64, 0, s>>>(w.t32, 1, ld, n);
+    zero_tails<<<1, 64, 0, s>>>(w.r32, 1, ld, n);
+    zero_tails<<<1, 64, 0, s>>>(w.d32, 1, ld, n);
+  }
   info->inner_iterations = 0;
   info->outer_iterations = 0;
   info->n_snapshots = 0;
@@ -1202,7 +1379,7 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       NFEM_TRY_CUDA(cudaMemcpyAsync(w.V, w.r32, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
     // the inner solve reduces the W-weighted residual norm by inner_rtol;
     // the outer loop measures the true FP64 residual
-    NFEM_RC(multidot<float>(n, 1, w.V, n, w.V, w.partial, w.scal + 3, 1, s));
+    NFEM_RC(multidot<float>(ld, 1, w.V, ld, w.V, w.partial, w.scal + 3, 1, s));
     double wr0 = 0.0;
     NFEM_TRY_CUDA(cudaMemcpyAsync(&wr0, w.scal + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
     NFEM_TRY_CUDA(cudaStreamSynchronize(s));
@@ -1217,14 +1394,14 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
                                           w.r32, 1, s, weighted ? pc->wsqrt : nullptr));
       }
       first_cycle = false;
-      NFEM_RC(multidot<float>(n, 1, w.V, n, w.V, w.partial, w.scal + 2, 1, s));
+      NFEM_RC(multidot<float>(ld, 1, w.V, ld, w.V, w.partial, w.scal + 2, 1, s));
       scale_by_inv<float><<<gv, B, 0, s>>>(n, w.V, w.scal + 2, w.V, nullptr);
       init_cycle<<<1, 128, 0, s>>>(w.g, m, w.scal + 2, w.gate);
       NFEM_CHECK_LAUNCH();
       int j = 0;
       for (; j < m; ++j) {
-        float* vj = w.V + int64_t(j) * n;
-        float* zj = w.Z + int64_t(j) * n;
+        float* vj = w.V + int64_t(j) * ld;
+        float* zj = w.Z + int64_t(j) * ld;
         const int32_t* done = w.gate;
         if (weighted) {
           scale_vec<<<gv, B, 0, s>>>(n, pc->winvsqrt, vj, w.t32, done);
@@ -1237,13 +1414,13 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
         double* hcol = w.H + int64_t(j) * ldh;
         // classical Gram-Schmidt, twice (the cancellation test of a selective
         // second pass fires on nearly every Arnoldi step, so it saves nothing)
-        NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, hcol, 0, s, done));
-        multi_axpy_f32(n, j + 1, w.V, n, hcol, w.w, 1.0, s, done);
-        NFEM_RC(multidot<float>(n, j + 1, w.V, n, w.w, w.partial, w.y, 0, s, done));
-        multi_axpy_f32(n, j + 1, w.V, n, w.y, w.w, 1.0, s, done);
+        NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, hcol, 0, s, done));
+        multi_axpy_f32(ld, j + 1, w.V, ld, hcol, w.w, 1.0, s, done);
+        NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, w.y, 0, s, done));
+        multi_axpy_f32(ld, j + 1, w.V, ld, w.y, w.w, 1.0, s, done);
         add_small<<<1, 64, 0, s>>>(j + 1, w.y, hcol, done);  // h += second-pass coefficients
-        NFEM_RC(multidot<float>(n, 1, w.w, n, w.w, w.partial, hcol + j + 1, 1, s, done));
-        scale_by_inv<float><<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * n, done);
+        NFEM_RC(multidot<float>(ld, 1, w.w, ld, w.w, w.partial, hcol + j + 1, 1, s, done));
+        scale_by_inv<float><<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * ld, done);
         givens_update<<<1, 32, 0, s>>>(w.H, ldh, w.cs, w.sn, w.g, j, w.hist, w.status, w.gate, inner_target);
         NFEM_CHECK_LAUNCH();
       }
@@ -1258,7 +1435,7 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       inner_res = hist[k - 1];
       upper_solve<<<1, 32, 0, s>>>(w.H, ldh, w.g, k, w.y);
       // d += Z y   (multi_axpy subtracts: pass -1 via hsign)
-      multi_axpy_f32(n, k, w.Z, n, w.y, w.d32, -1.0, s);
+      multi_axpy_f32(ld, k, w.Z, ld, w.y, w.d32, -1.0, s);
       NFEM_CHECK_LAUNCH();
       if (prm->snapshots && info->n_snapshots < prm->max_snapshots) {
         snapshot_kernel<<<gv, B, 0, s>>>(n, x, w.d32, prm->snapshots + int64_t(info->n_snapshots) * n);

@@ -153,10 +153,16 @@ class TwoLevelCoarse:
     pressure columns).  w = None gives the classical weights 1/|a_ff|; the
     learned preconditioner passes the network's prediction."""
 
-    def __init__(self, A, n_c, w=None, cell_agg=None):
+    def __init__(self, A, n_c, w=None, cell_agg=None, blocks=None):
         """cell_agg: optional aggregate of every cell (0 .. n_agg - 1) in place
         of the centroid grid, e.g. per-problem grids for a batch of
-        independent problems assembled as one disjoint union."""
+        independent problems assembled as one disjoint union.
+
+        blocks: optional [n_blocks + 1] ascending aggregate offsets when the
+        aggregates of block b (blocks[b] .. blocks[b + 1] - 1) couple to no
+        other block -- the problems of such a batch.  The coarse matrix is then
+        stored, inverted and applied block by block (sum of s_b^2 entries in
+        place of n_agg^2), which admits many more aggregates."""
         sp = A.space
         self.A = A
         dim = sp.dim
@@ -225,17 +231,40 @@ class TwoLevelCoarse:
         self.pt_slot = i32(pt_slot)
         self.pt_val = torch.zeros(max(1, pt_slot.size), dtype=torch.float32, device=dev)
         na = self.n_agg
-        self.ac = torch.zeros((na, na), dtype=torch.float64, device=dev)
-        self.gj = torch.zeros((na, 2 * na), dtype=torch.float64, device=dev)
-        self.ac_inv = torch.zeros((na, na), dtype=torch.float32, device=dev)
+        self.n_blocks = 0
+        if blocks is not None:
+            bp = np.asarray(blocks, dtype=np.int64)
+            sizes = np.diff(bp)
+            if bp.ndim != 1 or bp.size < 2 or bp[0] != 0 or bp[-1] != na or np.any(sizes < 1):
+                raise ValueError("blocks must rise strictly from 0 to n_agg")
+            if sizes.max() > _lib.COARSE_BLOCK_MAX:
+                raise ValueError(f"a coarse block has {sizes.max()} aggregates (at most {_lib.COARSE_BLOCK_MAX})")
+            off = np.concatenate([[0], np.cumsum(sizes * sizes)])
+            self.n_blocks = int(sizes.size)
+            self.blk_ptr = i32(bp)
+            self.blk_off = torch.as_tensor(off, dtype=torch.int64, device=dev)
+            self.agg_blk = i32(np.repeat(np.arange(sizes.size), sizes))
+            entries = int(off[-1])
+            self.ac = torch.zeros(entries, dtype=torch.float64, device=dev)
+            self.gj = torch.zeros(entries, dtype=torch.float64, device=dev)
+            self.ac_inv = torch.zeros(entries, dtype=torch.float32, device=dev)
+        else:
+            entries = 0
+            self.ac = torch.zeros((na, na), dtype=torch.float64, device=dev)
+            self.gj = torch.zeros((na, 2 * na), dtype=torch.float64, device=dev)
+            self.ac_inv = torch.zeros((na, na), dtype=torch.float32, device=dev)
         self.work = torch.zeros(64 + n + 2 * na, dtype=torch.float32, device=dev)
         self.set_weights(w)
+        blk = (self.n_blocks, int(np.diff(blocks).max()) if self.n_blocks else 0, entries,
+               _lib.ptr(self.blk_ptr).value if self.n_blocks else None,
+               _lib.ptr(self.blk_off).value if self.n_blocks else None,
+               _lib.ptr(self.agg_blk).value if self.n_blocks else None)
         self.struct = _lib.TwoLevel(pb, na, _lib.ptr(self.cell_agg).value, _lib.ptr(self.w).value,
                                     _lib.ptr(self.p_agg).value, _lib.ptr(self.p_val).value, int(pt_slot.size),
                                     _lib.ptr(self.pt_ptr).value, _lib.ptr(self.pt_row).value,
                                     _lib.ptr(self.pt_slot).value, _lib.ptr(self.pt_val).value,
                                     _lib.ptr(self.ac).value, _lib.ptr(self.gj).value, _lib.ptr(self.ac_inv).value,
-                                    _lib.ptr(self.work).value)
+                                    _lib.ptr(self.work).value, *blk)
 
     def classical_weights(self):
         d = self.A.diagonal().abs()

@@ -62,18 +62,22 @@ def darcy2d_batch(n_problems=512, n_min=8, n_max=128, corr_len=0.1, sigma=1.0, s
     return u, sp, kappa, np.ones(kappa.shape[0]), sides
 
 
-def batch_aggregates(sides, k=4):
+def batch_aggregates(sides, k=4, size=None, blocks=False):
     """Per-problem coarse aggregates of a darcy2d_batch union: problem i's
     n_i x n_i square split into k x k blocks of squares (two triangles per
     square, in meshes.square's cell order), aggregate ids offset per problem,
-    so no aggregate spans two problems."""
-    out, off = [], 0
+    so no aggregate spans two problems.  size: aggregates of about size x size
+    squares instead (k_i = round(n_i / size), at least 1).  blocks=True also
+    returns the [n_problems + 1] aggregate offsets of the problems, the
+    diagonal blocks of the coarse matrix."""
+    out, ptr = [], [0]
     for n in sides:
         n = int(n)
-        kk = min(k, n)
+        kk = min(k, n) if size is None else max(1, min(n, int(round(n / size))))
         sq = np.arange(n * n)
         i, j = sq % n, sq // n
         loc = (j * kk // n) * kk + (i * kk // n)
-        out.append(np.repeat(loc, 2) + off)
-        off += kk * kk
-    return np.concatenate(out)
+        out.append(np.repeat(loc, 2) + ptr[-1])
+        ptr.append(ptr[-1] + kk * kk)
+    agg = np.concatenate(out)
+    return (agg, np.asarray(ptr, dtype=np.int64)) if blocks else agg

@@ -99,11 +99,12 @@ def test_not_converged_reports_status(cuda_lib):
     assert info.inner_iterations <= 5
 
 
-def test_batched_union_two_level_solve(cuda_lib):
+@pytest.mark.parametrize("blocks", [False, True])
+def test_batched_union_two_level_solve(cuda_lib, blocks):
     """A batch of independent 2-D problems solved at once: two-level FGMRES on
     their disjoint union with aggregates inside each problem reaches 1e-8 in
     FP64, and every problem's part equals SuperLU's solve of that problem
-    alone."""
+    alone.  blocks=True stores and inverts the coarse matrix per problem."""
     import numpy as np
     from nfempy_gb300 import meshes, workloads
     from nfempy_gb300.solvers import KrylovSolver, TwoLevelCoarse
@@ -120,9 +121,9 @@ def test_batched_union_two_level_solve(cuda_lib):
     wf = nf.LaplaceDualWeakForm(sp)
     wf.functions = {"kappa": kap, "rhs": 1.0}
     wf.assemble(A, res)
-    agg = workloads.batch_aggregates(sides, 3)
-    tl = TwoLevelCoarse(A, None, cell_agg=agg)
-    assert tl.n_agg == 4 * 9
+    agg, bp = workloads.batch_aggregates(sides, 3, blocks=True)
+    tl = TwoLevelCoarse(A, None, cell_agg=agg, blocks=bp if blocks else None)
+    assert tl.n_agg == 4 * 9 and tl.n_blocks == (4 if blocks else 0)
     ksp = KrylovSolver(A, pc="two_level", two_level=tl)
     x, info = ksp.solve(-res, rtol=1e-8, max_inner=5000)
     assert info.status == 0 and info.final_relres <= 1e-8
@@ -136,3 +137,48 @@ def test_batched_union_two_level_solve(cuda_lib):
         loc[cdk.ravel()] = cd[c0:c0 + 2 * n * n].ravel()
         assert np.linalg.norm(xg[loc] - xk) <= 1e-6 * np.linalg.norm(xk)
         c0 += 2 * n * n
+
+
+def test_block_coarse_matches_dense(cuda_lib):
+    """The block-diagonal coarse storage is the dense coarse matrix's diagonal
+    blocks: on a batch union, the block inverse equals the dense inverse's
+    blocks (FP32 round-off), the dense inverse is zero off the blocks, and
+    both give the same iterations and solution."""
+    import numpy as np
+    from nfempy_gb300 import meshes, workloads
+    from nfempy_gb300.solvers import KrylovSolver, TwoLevelCoarse
+    from oracle import mesh_gen
+    from tests.gpu_helpers import product_space
+    sides = [10, 7, 13]
+    u = meshes.union([mesh_gen.square(n) for n in sides])
+    rng = np.random.default_rng(5)
+    kap = np.exp(rng.normal(0.0, 1.0, sum(2 * n * n for n in sides)))
+    sp = product_space(u, [("u", "RT", 1, 1, False), ("p", "P", 0, 1, True)])
+    A = nf.CSRMatrix(sp, dtype=torch.float64)
+    res = torch.empty(A.n_rows, dtype=torch.float64, device="cuda")
+    wf = nf.LaplaceDualWeakForm(sp)
+    wf.functions = {"kappa": kap, "rhs": 1.0}
+    wf.assemble(A, res)
+    agg, bp = workloads.batch_aggregates(sides, size=3, blocks=True)
+    out = {}
+    for blk in (False, True):
+        tl = TwoLevelCoarse(A, None, cell_agg=agg, blocks=bp if blk else None)
+        ksp = KrylovSolver(A, pc="two_level", two_level=tl)
+        x, info = ksp.solve(-res, rtol=1e-8, max_inner=5000)
+        assert info.status == 0 and info.final_relres <= 1e-8
+        out[blk] = (tl, x, info)
+    dense, blockwise = out[False][0], out[True][0]
+    inv_d = dense.ac_inv.cpu().numpy()
+    inv_b = blockwise.ac_inv.cpu().numpy()
+    off = blockwise.blk_off.cpu().numpy()
+    mask = np.zeros_like(inv_d, dtype=bool)
+    for b in range(len(bp) - 1):
+        s0, s1 = bp[b], bp[b + 1]
+        blk = inv_b[off[b]:off[b + 1]].reshape(s1 - s0, s1 - s0)
+        ref = inv_d[s0:s1, s0:s1]
+        assert np.abs(blk - ref).max() <= 1e-4 * np.abs(ref).max()
+        mask[s0:s1, s0:s1] = True
+    assert np.abs(inv_d[~mask]).max() <= 1e-5 * np.abs(inv_d).max()
+    assert abs(out[False][2].inner_iterations - out[True][2].inner_iterations) <= 2
+    xd, xb = out[False][1], out[True][1]
+    assert torch.linalg.norm(xd - xb) <= 1e-6 * torch.linalg.norm(xd)
