@@ -681,7 +681,7 @@ def main():
     ap.add_argument("--restart", type=int, default=50, help="FGMRES restart of the plain block-Jacobi solve")
     ap.add_argument("--tl-restart", type=int, default=20, help="FGMRES restart of the two-level solves")
     ap.add_argument("--max-iters", type=int, default=20000)
-    ap.add_argument("--batch-agg", type=int, default=8,
+    ap.add_argument("--batch-agg", type=int, default=4,
                     help="aggregate side in squares of the batched 2-D two-level solve")
     ap.add_argument("--solver", choices=["both", "plain", "two_level"], default="both",
                     help="with --only solve: which preconditioners to run")

@@ -372,7 +372,7 @@ typedef struct {
   const int32_t* pt_slot;    /* [pt_nnz] index 2 * row + slot into p_val */
   float* pt_val;             /* [pt_nnz] filled by nfem_precond_setup */
   double* ac;                /* [n_agg, n_agg] Galerkin coarse matrix (blocks: [ac_entries]) */
-  double* gj;                /* [n_agg, 2 n_agg] Gauss-Jordan scratch (blocks: [ac_entries]) */
+  double* gj;                /* [n_agg, 2 n_agg] Gauss-Jordan scratch (blocks: unused, may be NULL) */
   float* ac_inv;             /* [n_agg, n_agg] (blocks: [ac_entries]) */
   float* work;               /* [64 + n_rows + 2 n_agg] */
   /* Block-diagonal coarse matrix (n_blocks > 0): a batch of independent
@@ -380,7 +380,7 @@ typedef struct {
    * aggregates of different problems, so Ac is stored, inverted and applied
    * block by block.  The aggregates of block b are blk_ptr[b] ..
    * blk_ptr[b + 1] - 1; block b's s_b x s_b entries (row-major) start at
-   * blk_off[b] in ac, gj and ac_inv.  A nonzero of A coupling two blocks is
+   * blk_off[b] in ac and ac_inv.  A nonzero of A coupling two blocks is
    * an error (NFEM_ERR_INVALID_ARG in the device status).  n_blocks = 0 keeps
    * the dense n_agg x n_agg layout and leaves the fields below unread. */
   int32_t n_blocks;

@@ -775,53 +775,145 @@ static int blocked_inverse(const double* ac, int n, T* m, T* dblk, float* inv, i
 }
 
 // ------------------------------------------------------------------ block-diagonal coarse inverse
-// One CTA per diagonal block: in-place Gauss-Jordan inversion in FP64 of the
-// block copied into gj, no pivoting (each block is a Galerkin matrix of the
-// same SPD form as the dense case), then rounded into ac_inv.  Step k:
-//   p = 1 / a_kk;  a_kj *= p (j != k);  a_ij -= a_ik a_kj (i, j != k);
-//   a_ik = -a_ik p (i != k);  a_kk = p.
-__global__ void __launch_bounds__(256) coarse_block_inverse(int n_blocks, const int32_t* __restrict__ blk_ptr,
-                                                            const int64_t* __restrict__ blk_off,
-                                                            const double* __restrict__ ac, double* __restrict__ gj,
-                                                            float* __restrict__ inv, int32_t* status) {
-  __shared__ double piv;
+// The blocked Gauss-Jordan above, batched over the diagonal blocks of a
+// block-diagonal coarse matrix and run in place in ac_inv (FP32, the copy of
+// ac): 64 x 64 tiles, edge tiles clipped to the block (loads zero-filled,
+// stores masked), every block in the same launches (grid z or y = block).
+// Per tile column K of each block with s_b > K:
+//   A_KK <- A_KK^-1;  A_KJ <- A_KK^-1 A_KJ;  A_IJ -= A_IK A_KJ;
+//   A_IK <- -A_IK A_KK^-1   (I, J != K).
+// A_KK is read only by the panel products after its inversion, so the
+// inverse is written to its place at once.
+__device__ __forceinline__ void load_tile_clip(float (*t)[kGjB + 1], const float* __restrict__ src, int ld, int r0,
+                                               int c0) {
+  for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
+    const int r = e / kGjB, c = e - r * kGjB;
+    t[r][c] = (r0 + r < ld && c0 + c < ld) ? src[int64_t(r0 + r) * ld + c0 + c] : 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(256) bbgj_diag(int n_blocks, const int32_t* __restrict__ blk_ptr,
+                                                 const int64_t* __restrict__ blk_off, float* __restrict__ inv,
+                                                 int k0, int max_size, int32_t* status) {
+  __shared__ float a[kGjB][kGjB + 1];
+  __shared__ float row[kGjB], col[kGjB];
   for (int blk = blockIdx.x; blk < n_blocks; blk += gridDim.x) {
     const int s = blk_ptr[blk + 1] - blk_ptr[blk];
-    const int64_t ss = int64_t(s) * s;
-    const double* a0 = ac + blk_off[blk];
-    double* m = gj + blk_off[blk];
-    for (int64_t e = threadIdx.x; e < ss; e += blockDim.x) m[e] = a0[e];
+    if (k0 == 0 && s > max_size && threadIdx.x == 0) set_status(status, NFEM_ERR_INVALID_ARG);
+    if (k0 >= s) continue;
+    const int rem = min(kGjB, s - k0);
+    float* m = inv + blk_off[blk] + int64_t(k0) * s + k0;
+    for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
+      const int r = e / kGjB, c = e - r * kGjB;
+      a[r][c] = (r < rem && c < rem) ? m[int64_t(r) * s + c] : (r == c ? 1.f : 0.f);
+    }
     __syncthreads();
-    for (int k = 0; k < s; ++k) {
-      if (threadIdx.x == 0) {
-        const double d = m[int64_t(k) * s + k];
-        if (!(d > 0.0)) set_status(status, NFEM_ERR_BREAKDOWN);
-        piv = d > 0.0 ? 1.0 / d : 0.0;
+    for (int k = 0; k < rem; ++k) {
+      const float p = a[k][k];
+      const float ip = p > 0.f ? 1.f / p : 0.f;
+      if (threadIdx.x == 0 && !(p > 0.f)) set_status(status, NFEM_ERR_BREAKDOWN);
+      if (threadIdx.x < kGjB) {
+        row[threadIdx.x] = a[k][threadIdx.x] * ip;
+        col[threadIdx.x] = a[threadIdx.x][k];
       }
       __syncthreads();
-      const double p = piv;
-      for (int j = threadIdx.x; j < s; j += blockDim.x)
-        if (j != k) m[int64_t(k) * s + j] *= p;
-      __syncthreads();
-      for (int i = threadIdx.x >> 5; i < s; i += blockDim.x >> 5) {
-        if (i == k) continue;
-        double* mi = m + int64_t(i) * s;
-        const double f = mi[k];
-        if (f != 0.0)
-          for (int j = threadIdx.x & 31; j < s; j += 32)
-            if (j != k) mi[j] = fma(-f, m[int64_t(k) * s + j], mi[j]);
-      }
-      __syncthreads();
-      for (int i = threadIdx.x; i < s; i += blockDim.x) {
-        if (i != k) m[int64_t(i) * s + k] *= -p;
-        else m[int64_t(k) * s + k] = p;
+      for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
+        const int r = e / kGjB, c = e - r * kGjB;
+        if (r == k && c == k) a[r][c] = ip;
+        else if (r == k) a[r][c] = row[c];
+        else if (c == k) a[r][c] = -col[r] * ip;
+        else a[r][c] = fmaf(-col[r], row[c], a[r][c]);
       }
       __syncthreads();
     }
-    float* out = inv + blk_off[blk];
-    for (int64_t e = threadIdx.x; e < ss; e += blockDim.x) out[e] = float(m[e]);
+    for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
+      const int r = e / kGjB, c = e - r * kGjB;
+      if (r < rem && c < rem) m[int64_t(r) * s + c] = a[r][c];
+    }
     __syncthreads();
   }
+}
+
+// mode 0: A_KJ <- D A_KJ (blockIdx.x = J);  mode 1: A_IK <- -A_IK D (blockIdx.x = I)
+__global__ void __launch_bounds__(256) bbgj_panel(int n_blocks, const int32_t* __restrict__ blk_ptr,
+                                                  const int64_t* __restrict__ blk_off, float* __restrict__ inv,
+                                                  int k0, int mode) {
+  __shared__ float d[kGjB][kGjB + 1];
+  __shared__ float x[kGjB][kGjB + 1];
+  const int t0 = blockIdx.x * kGjB;
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  for (int blk = blockIdx.y; blk < n_blocks; blk += gridDim.y) {
+    const int s = blk_ptr[blk + 1] - blk_ptr[blk];
+    if (k0 >= s || t0 >= s || t0 == k0) continue;
+    float* m = inv + blk_off[blk];
+    load_tile_clip(d, m, s, k0, k0);
+    if (mode == 0) load_tile_clip(x, m, s, k0, t0);
+    else load_tile_clip(x, m, s, t0, k0);
+    __syncthreads();
+    float acc[4][4] = {};
+    if (mode == 0) tile_mma<float>(d, x, acc);
+    else tile_mma<float>(x, d, acc);
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int r = ty * 4 + a, c = tx * 4 + b;
+        if (mode == 0) {
+          if (k0 + r < s && t0 + c < s) m[int64_t(k0 + r) * s + t0 + c] = acc[a][b];
+        } else {
+          if (t0 + r < s && k0 + c < s) m[int64_t(t0 + r) * s + k0 + c] = -acc[a][b];
+        }
+      }
+    __syncthreads();
+  }
+}
+
+// A_IJ -= A_IK A_KJ for I, J != K (A_KJ updated, A_IK not yet)
+__global__ void __launch_bounds__(256) bbgj_trailing(int n_blocks, const int32_t* __restrict__ blk_ptr,
+                                                     const int64_t* __restrict__ blk_off, float* __restrict__ inv,
+                                                     int k0) {
+  __shared__ float x[kGjB][kGjB + 1];
+  __shared__ float y[kGjB][kGjB + 1];
+  const int i0 = blockIdx.y * kGjB, j0 = blockIdx.x * kGjB;
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  for (int blk = blockIdx.z; blk < n_blocks; blk += gridDim.z) {
+    const int s = blk_ptr[blk + 1] - blk_ptr[blk];
+    if (k0 >= s || i0 >= s || j0 >= s || i0 == k0 || j0 == k0) continue;
+    float* m = inv + blk_off[blk];
+    load_tile_clip(x, m, s, i0, k0);
+    load_tile_clip(y, m, s, k0, j0);
+    __syncthreads();
+    float acc[4][4] = {};
+    tile_mma<float>(x, y, acc);
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int r = i0 + ty * 4 + a, c = j0 + tx * 4 + b;
+        if (r < s && c < s) m[int64_t(r) * s + c] -= acc[a][b];
+      }
+    __syncthreads();
+  }
+}
+
+__global__ void cast_f64_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b);
+
+static int block_diag_inverse(const nfem_two_level* L, int32_t* status, cudaStream_t s) {
+  const int nt = int(ceil_div(L->blk_max, kGjB));
+  const unsigned nb = unsigned(std::min(L->n_blocks, 65535));
+  cast_f64_f32<<<grid_for(L->ac_entries, 256), 256, 0, s>>>(L->ac_entries, L->ac, L->ac_inv);
+  for (int kb = 0; kb < nt; ++kb) {
+    const int k0 = kb * kGjB;
+    bbgj_diag<<<nb, 256, 0, s>>>(L->n_blocks, L->blk_ptr, L->blk_off, L->ac_inv, k0, nt * kGjB, status);
+    if (nt > 1) {
+      bbgj_panel<<<dim3(nt, nb), 256, 0, s>>>(L->n_blocks, L->blk_ptr, L->blk_off, L->ac_inv, k0, 0);
+      bbgj_trailing<<<dim3(nt, nt, std::min(nb, 65535u)), 256, 0, s>>>(L->n_blocks, L->blk_ptr, L->blk_off,
+                                                                        L->ac_inv, k0);
+      bbgj_panel<<<dim3(nt, nb), 256, 0, s>>>(L->n_blocks, L->blk_ptr, L->blk_off, L->ac_inv, k0, 1);
+    }
+  }
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
 }
 
 // ec[alpha] = sum over alpha's block of Ainv[alpha, beta] rc[beta]  (one warp
@@ -1135,7 +1227,7 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     if (pc->kind == NFEM_PC_TWO_LEVEL) {
       const nfem_two_level* L = pc->two_level;
       if (!L || L->n_agg < 1 || !L->cell_agg || !L->w || !L->p_agg || !L->p_val || !L->pt_ptr || !L->pt_row ||
-          !L->pt_slot || !L->pt_val || !L->ac || !L->ac_inv || !L->gj || !L->work)
+          !L->pt_slot || !L->pt_val || !L->ac || !L->ac_inv || (!L->gj && L->n_blocks == 0) || !L->work)
         return NFEM_ERR_INVALID_ARG;
       if (L->n_blocks < 0 || (L->n_blocks > 0 && (!L->blk_ptr || !L->blk_off || !L->agg_blk || L->blk_max < 1 ||
                                                   L->blk_max > NFEM_COARSE_BLOCK_MAX || L->ac_entries < 1)))
@@ -1185,11 +1277,7 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     twolevel_galerkin<<<g, 256, 0, s>>>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, L->p_agg,
                                         L->p_val, at, L->ac, dev_status);
     if (blocks) {
-      coarse_block_inverse<<<unsigned(std::min(L->n_blocks, 65535)), 256, 0, s>>>(L->n_blocks, L->blk_ptr,
-                                                                                L->blk_off, L->ac, L->gj,
-                                                                                L->ac_inv, dev_status);
-      NFEM_CHECK_LAUNCH();
-      return NFEM_OK;
+      return block_diag_inverse(L, dev_status, s);
     }
     // blocked inversion when the scratch holds the padded matrix (n >= 64:
     // (n + 63)^2 + 64^2 entries of T fit in the 2 n^2 doubles of gj)

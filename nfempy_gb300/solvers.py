@@ -246,7 +246,7 @@ class TwoLevelCoarse:
             self.agg_blk = i32(np.repeat(np.arange(sizes.size), sizes))
             entries = int(off[-1])
             self.ac = torch.zeros(entries, dtype=torch.float64, device=dev)
-            self.gj = torch.zeros(entries, dtype=torch.float64, device=dev)
+            self.gj = torch.zeros(1, dtype=torch.float64, device=dev)  # unused by the block layout
             self.ac_inv = torch.zeros(entries, dtype=torch.float32, device=dev)
         else:
             entries = 0
