@@ -224,15 +224,19 @@ def run_reference(args):
 
 
 
-def _timed_solve(ksp, b, args, stream):
+def _timed_solve(ksp, b, args, stream, two_level=False):
+    """Setup + solve to 1e-8 (FP64 residual); the FP32 inner solves stop at
+    the preconditioner's inner tolerance (--inner-rtol / --tl-inner-rtol)."""
     import torch
+    from nfempy_gb300.solvers import INNER_RTOL
+    inner_rtol = args.tl_inner_rtol if two_level else args.inner_rtol
     ev0, ev1, ev2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     torch.cuda.synchronize()
     t_wall = time.perf_counter()
     ev0.record(stream)
     ksp.setup()
     ev1.record(stream)
-    x, info = ksp.solve(b, rtol=1e-8, inner_rtol=1e-4, max_inner=args.max_iters, raise_on_failure=False)
+    x, info = ksp.solve(b, rtol=1e-8, inner_rtol=inner_rtol, max_inner=args.max_iters, raise_on_failure=False)
     ev2.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall
@@ -241,7 +245,8 @@ def _timed_solve(ksp, b, args, stream):
             "time_to_solve_ms": ev0.elapsed_time(ev2), "wall_s": wall,
             "inner_iterations": info.inner_iterations, "outer_iterations": info.outer_iterations,
             "final_relres_fp64": relres, "status": info.status,
-            "ms_per_inner_iteration": ev1.elapsed_time(ev2) / max(1, info.inner_iterations)}
+            "ms_per_inner_iteration": ev1.elapsed_time(ev2) / max(1, info.inner_iterations),
+            "restart": ksp.restart, "inner_rtol": inner_rtol if inner_rtol is not None else INNER_RTOL[ksp.pc_kind]}
 
 
 def solve_bench(args, A, wf, coefs, res, stream):
@@ -265,7 +270,7 @@ def solve_bench(args, A, wf, coefs, res, stream):
     tl = TwoLevelCoarse(A64, nc)
     t_struct = time.perf_counter() - t0
     ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.tl_restart, two_level=tl)
-    out["two_level_classical"] = _timed_solve(ksp, b, args, stream)
+    out["two_level_classical"] = _timed_solve(ksp, b, args, stream, two_level=True)
     out["two_level_classical"]["host_structure_s"] = t_struct
     out["two_level_classical"]["aggregates"] = tl.n_agg
     try:
@@ -276,7 +281,7 @@ def solve_bench(args, A, wf, coefs, res, stream):
         tl2 = TwoLevelCoarse(A64, nc)
         tl2.set_weights(learned.learned_weights(tl2, model, kappa, alpha))
         ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.tl_restart, two_level=tl2)
-        out["learned"] = _timed_solve(ksp, b, args, stream)
+        out["learned"] = _timed_solve(ksp, b, args, stream, two_level=True)
         out["learned"]["alpha"] = alpha
         out["learned"]["training"] = {k: ck["record"][k] for k in ("n", "fields", "solves_used", "pairs",
                                                                    "data_seconds", "train_seconds")}
@@ -315,7 +320,8 @@ def solve_only(args):
     if args.solver in ("both", "two_level"):
         tl = TwoLevelCoarse(A64, N_SIDE // 4)
         out["two_level"] = _timed_solve(KrylovSolver(A64, pc="two_level", A32_values=A32.values,
-                                                     restart=args.tl_restart, two_level=tl), b, args, stream)
+                                                     restart=args.tl_restart, two_level=tl), b, args, stream,
+                                        two_level=True)
     return out
 
 
@@ -468,7 +474,7 @@ def batch2d_bench(args):
         tl = TwoLevelCoarse(A64, None, cell_agg=agg, blocks=bp)
         t_struct = time.perf_counter() - t0
         ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.tl_restart, two_level=tl)
-        out["solve"] = _timed_solve(ksp, -r64, args, torch.cuda.current_stream())
+        out["solve"] = _timed_solve(ksp, -r64, args, torch.cuda.current_stream(), two_level=True)
         out["solve"].update({"preconditioner": f"two-level, {args.batch_agg}x{args.batch_agg}-square aggregates, "
                                                "coarse matrix block-diagonal per problem",
                              "aggregates": tl.n_agg, "largest_block": int(np.diff(bp).max()),
@@ -679,8 +685,12 @@ def main():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--restart", type=int, default=50, help="FGMRES restart of the plain block-Jacobi solve")
-    ap.add_argument("--tl-restart", type=int, default=20, help="FGMRES restart of the two-level solves")
+    ap.add_argument("--tl-restart", type=int, default=15, help="FGMRES restart of the two-level solves")
     ap.add_argument("--max-iters", type=int, default=20000)
+    ap.add_argument("--inner-rtol", type=float, default=None,
+                    help="FP32 inner tolerance of the block-Jacobi and point-Jacobi solves (default: the solver's)")
+    ap.add_argument("--tl-inner-rtol", type=float, default=None,
+                    help="FP32 inner tolerance of the two-level solves (default: the solver's)")
     ap.add_argument("--batch-agg", type=int, default=4,
                     help="aggregate side in squares of the batched 2-D two-level solve")
     ap.add_argument("--solver", choices=["both", "plain", "two_level"], default="both",

@@ -115,32 +115,47 @@ __device__ __forceinline__ void cell_edges<double, 2>(const DarcyParams& p, int3
     for (int d = 0; d < 3; ++d) J[k][d] = __ldg(p.points + int64_t(vs[k + 1]) * 3 + d) - x0[d];
 }
 
-// FP32: one packed 16-byte record per vertex (nfem_points_split).
+// FP32: one packed 16-byte record per vertex (nfem_points_split).  The edges
+// are left in units of the record's scale s (a power of two): every product
+// of the metric, the determinant and the element row then carries an exact
+// power of s, folded in once per incidence (element_row), which gives the
+// same rounded values as scaling each edge component.
 template <>
 __device__ __forceinline__ void cell_edges<float, 3>(const DarcyParams& p, int32_t c, float (&J)[3][3]) {
   const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
-  const float s = packed_lo_scale(p.split);
   const float4 r0 = packed_point(p.split, v.x), r1 = packed_point(p.split, v.y), r2 = packed_point(p.split, v.z),
                r3 = packed_point(p.split, v.w);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    J[0][d] = packed_diff(r1, r0, d, s);
-    J[1][d] = packed_diff(r2, r0, d, s);
-    J[2][d] = packed_diff(r3, r0, d, s);
+    J[0][d] = packed_diff(r1, r0, d, 1.f);
+    J[1][d] = packed_diff(r2, r0, d, 1.f);
+    J[2][d] = packed_diff(r3, r0, d, 1.f);
   }
 }
 
 template <>
 __device__ __forceinline__ void cell_edges<float, 2>(const DarcyParams& p, int32_t c, float (&J)[2][3]) {
   const int32_t* vp = p.cv + int64_t(c) * 3;
-  const float s = packed_lo_scale(p.split);
   const float4 r0 = packed_point(p.split, __ldg(vp)), r1 = packed_point(p.split, __ldg(vp + 1)),
                r2 = packed_point(p.split, __ldg(vp + 2));
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    J[0][d] = packed_diff(r1, r0, d, s);
-    J[1][d] = packed_diff(r2, r0, d, s);
+    J[0][d] = packed_diff(r1, r0, d, 1.f);
+    J[1][d] = packed_diff(r2, r0, d, 1.f);
   }
+}
+
+// Unit of the edges cell_edges returns: the packed records' scale in FP32,
+// 1 in FP64 (plain coordinates).
+template <typename T>
+__device__ __forceinline__ T edge_unit(const DarcyParams& p);
+template <>
+__device__ __forceinline__ float edge_unit<float>(const DarcyParams& p) {
+  return packed_lo_scale(p.split);
+}
+template <>
+__device__ __forceinline__ double edge_unit<double>(const DarcyParams&) {
+  return 1.0;
 }
 
 // 1 / v: correctly rounded reciprocal (no division sequence) in FP32, exact
@@ -214,10 +229,14 @@ __device__ __forceinline__ void element_row(const DarcyParams& p, const Incidenc
       for (int j = 0; j < DIM; ++j) G[i][j] = x.J[i][0] * x.J[j][0] + x.J[i][1] * x.J[j][1] + x.J[i][2] * x.J[j][2];
   };
   if (DIM == 2 || a < NF) metric();
-  T det = T(1);
+  // G and det are in edge units u: G = u^2 G_true, det = u^DIM det_true; the
+  // flux entries are kappa2 / (kap det_true) * u^2 (bracket in edge units)
+  const T u = edge_unit<T>(p);
+  T det = T(1), det_true = T(1);
   if (need_geo) {
     det = abs_det<T, DIM>(x.J, G);
     if (!(det > T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+    det_true = DIM == 3 ? det * (u * u * u) : det * (u * u);
   }
   if (a < NF) {
     T R[DIM];
@@ -231,7 +250,7 @@ __device__ __forceinline__ void element_row(const DarcyParams& p, const Incidenc
       sumG += R[i];
     }
     const T tgs = (trG + sumG) * T(C::f2);
-    const T scale = T(C::kappa2) * recip(x.kap * det);
+    const T scale = T(C::kappa2) * recip(x.kap * (DIM == 3 ? det * u : det));
     // row a-1 of G and R[a-1] through selects (no local-memory indexing)
     T Ga[DIM];
     T Ra = T(0);
@@ -259,8 +278,8 @@ __device__ __forceinline__ void element_row(const DarcyParams& p, const Incidenc
 #pragma unroll
     for (int b = 0; b < NF; ++b) vals[b] = sg[b];
     vals[NF] = T(0);
-    if constexpr (SRC == NFEM_COEF_CELL) rhs_val += -det * T(C::area) * x.src;
-    if constexpr (SRC == NFEM_COEF_QPOINT) rhs_val += -det * x.src;
+    if constexpr (SRC == NFEM_COEF_CELL) rhs_val += -det_true * T(C::area) * x.src;
+    if constexpr (SRC == NFEM_COEF_QPOINT) rhs_val += -det_true * x.src;
   }
 }
 
@@ -279,8 +298,10 @@ __device__ __forceinline__ T cell_matrix(const DarcyParams& p, const Incidence<T
   for (int i = 0; i < DIM; ++i)
 #pragma unroll
     for (int j = 0; j < DIM; ++j) G[i][j] = x.J[i][0] * x.J[j][0] + x.J[i][1] * x.J[j][1] + x.J[i][2] * x.J[j][2];
-  const T det = abs_det<T, DIM>(x.J, G);
+  const T det = abs_det<T, DIM>(x.J, G);  // edge units, as in element_row
   if (!(det > T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+  const T u = edge_unit<T>(p);
+  const T det_true = DIM == 3 ? det * (u * u * u) : det * (u * u);
   T R[DIM];
   T trG = T(0), sumG = T(0);
 #pragma unroll
@@ -292,7 +313,7 @@ __device__ __forceinline__ T cell_matrix(const DarcyParams& p, const Incidence<T
     sumG += R[i];
   }
   const T tgs = (trG + sumG) * T(C::f2);
-  const T scale = T(C::kappa2) * recip(x.kap * det);
+  const T scale = T(C::kappa2) * recip(x.kap * (DIM == 3 ? det * u : det));
 #pragma unroll
   for (int a = 0; a < NF; ++a) {
     const T gma = a > 0 ? R[a - 1] * T(C::f1) : T(0);
@@ -305,8 +326,8 @@ __device__ __forceinline__ T cell_matrix(const DarcyParams& p, const Incidence<T
       if (b != a) M[b * 4 + a] = v;
     }
   }
-  if constexpr (SRC == NFEM_COEF_CELL) return -det * T(C::area) * x.src;
-  if constexpr (SRC == NFEM_COEF_QPOINT) return -det * x.src;
+  if constexpr (SRC == NFEM_COEF_CELL) return -det_true * T(C::area) * x.src;
+  if constexpr (SRC == NFEM_COEF_QPOINT) return -det_true * x.src;
   return T(0);
 }
 
