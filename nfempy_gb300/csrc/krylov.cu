@@ -351,6 +351,162 @@ __global__ void multi_axpy_v4(int64_t n4, int k, const float4* __restrict__ X, i
   }
 }
 
+// ---- fused Gram-Schmidt passes (16-byte rows, k <= KM basis vectors)
+// The second classical Gram-Schmidt pass needs w' = w - X h before its dot
+// products X^T w'; each thread holds its k basis entries in registers, so
+// the update and the products share one read of X.  The last update and
+// the norm of its result share the next read.  Partial sums follow
+// multidot_partial_v4: FP32 per thread, folded into FP64 every 16
+// elements (here into shared memory, to keep the registers for X), a
+// fixed-order block reduction, one partial per (vector, block).
+template <int KM>
+__device__ __forceinline__ void block_partials(int k, const float (&accf)[KM], double (*sacc)[kRedThreads],
+                                               double (*sh)[kRedThreads / 32], double* __restrict__ partial) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < KM; ++q) {
+    if (q < k) {
+      double v = sacc[q][threadIdx.x] + double(accf[q]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) sh[q][warp] = v;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < k) {
+    double t = 0.0;
+    for (int w = 0; w < (kRedThreads / 32); ++w) t += sh[threadIdx.x][w];
+    partial[int64_t(threadIdx.x) * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// w <- w - X h;  partial = per-block sums of X^T w (the updated w)
+#ifndef NFEM_CGS_MIN_BLOCKS
+#define NFEM_CGS_MIN_BLOCKS 2
+#endif
+template <int KM>
+__global__ void __launch_bounds__(kRedThreads, NFEM_CGS_MIN_BLOCKS)
+    axpy_dot_v4(int64_t n4, int k, const float4* __restrict__ X, int64_t ldx4, const double* __restrict__ h,
+                float4* __restrict__ w, double* __restrict__ partial, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
+  __shared__ float hs[KM];
+  __shared__ double sacc[KM][kRedThreads];
+  __shared__ double sh[KM][kRedThreads / 32];
+  for (int q = threadIdx.x; q < k; q += blockDim.x) hs[q] = float(h[q]);
+#pragma unroll
+  for (int q = 0; q < KM; ++q) sacc[q][threadIdx.x] = 0.0;
+  __syncthreads();
+  float accf[KM];
+#pragma unroll
+  for (int q = 0; q < KM; ++q) accf[q] = 0.f;
+  int cnt = 0;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n4; i += stride) {
+    float4 xv[KM];
+    const float4* xq = X + i;
+#pragma unroll
+    for (int q = 0; q < KM; ++q) {
+      if (q < k) xv[q] = __ldg(xq);
+      xq += ldx4;
+    }
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < KM; ++q) {
+      if (q < k) {
+        const float hq = hs[q];
+        a.x = fmaf(hq, xv[q].x, a.x);
+        a.y = fmaf(hq, xv[q].y, a.y);
+        a.z = fmaf(hq, xv[q].z, a.z);
+        a.w = fmaf(hq, xv[q].w, a.w);
+      }
+    }
+    float4 v = w[i];
+    v.x -= a.x;
+    v.y -= a.y;
+    v.z -= a.z;
+    v.w -= a.w;
+    w[i] = v;
+#pragma unroll
+    for (int q = 0; q < KM; ++q)
+      if (q < k) accf[q] = fmaf(xv[q].x, v.x, fmaf(xv[q].y, v.y, fmaf(xv[q].z, v.z, fmaf(xv[q].w, v.w, accf[q]))));
+    if (++cnt == 16) {
+#pragma unroll
+      for (int q = 0; q < KM; ++q) {
+        sacc[q][threadIdx.x] += double(accf[q]);
+        accf[q] = 0.f;
+      }
+      cnt = 0;
+    }
+  }
+  block_partials<KM>(k, accf, sacc, sh, partial);
+}
+
+// w <- w - X h;  partial = per-block sums of w . w (the updated w)
+template <int KM>
+__global__ void __launch_bounds__(kRedThreads)
+    axpy_norm_v4(int64_t n4, int k, const float4* __restrict__ X, int64_t ldx4, const double* __restrict__ h,
+                 float4* __restrict__ w, double* __restrict__ partial, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
+  __shared__ float hs[KM];
+  __shared__ double sacc[1][kRedThreads];
+  __shared__ double sh[1][kRedThreads / 32];
+  for (int q = threadIdx.x; q < k; q += blockDim.x) hs[q] = float(h[q]);
+  sacc[0][threadIdx.x] = 0.0;
+  __syncthreads();
+  float accf[1] = {0.f};
+  int cnt = 0;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n4; i += stride) {
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < KM; ++q) {
+      if (q < k) {
+        const float hq = hs[q];
+        const float4 xv = __ldg(X + int64_t(q) * ldx4 + i);
+        a.x = fmaf(hq, xv.x, a.x);
+        a.y = fmaf(hq, xv.y, a.y);
+        a.z = fmaf(hq, xv.z, a.z);
+        a.w = fmaf(hq, xv.w, a.w);
+      }
+    }
+    float4 v = w[i];
+    v.x -= a.x;
+    v.y -= a.y;
+    v.z -= a.z;
+    v.w -= a.w;
+    w[i] = v;
+    accf[0] = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, accf[0]))));
+    if (++cnt == 16) {
+      sacc[0][threadIdx.x] += double(accf[0]);
+      accf[0] = 0.f;
+      cnt = 0;
+    }
+  }
+  block_partials<1>(1, accf, sacc, sh, partial);
+}
+
+// The second Gram-Schmidt pass and the norm, given the first pass's
+// coefficients h (k <= 16 basis vectors, 16-byte rows): w <- w - X h,
+// y = X^T w, w <- w - X y, nrm = ||w||.  Returns false (nothing launched)
+// when the fused form does not apply.
+static bool cgs2_fused(int64_t n, int k, const float* X, int64_t ldx, const double* h, float* w, double* y,
+                       double* nrm, double* partial, cudaStream_t s, const int32_t* gate) {
+  if (k > 16 || !rows16(n, ldx, X, w)) return false;
+  const auto* X4 = reinterpret_cast<const float4*>(X);
+  auto* w4 = reinterpret_cast<float4*>(w);
+  if (k <= 8) {
+    axpy_dot_v4<8><<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, h, w4, partial, gate);
+    reduce_partials<<<k, 256, 0, s>>>(partial, kRedBlocks, k, y, 0, 1.0);
+    axpy_norm_v4<8><<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, y, w4, partial, gate);
+  } else {
+    axpy_dot_v4<16><<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, h, w4, partial, gate);
+    reduce_partials<<<k, 256, 0, s>>>(partial, kRedBlocks, k, y, 0, 1.0);
+    axpy_norm_v4<16><<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, y, w4, partial, gate);
+  }
+  reduce_partials<<<1, 256, 0, s>>>(partial, kRedBlocks, 1, nrm, 1, 1.0);
+  return true;
+}
+
 // w -= sign * X h over k vectors, choosing the float4 form when it applies
 static void multi_axpy_f32(int64_t n, int k, const float* X, int64_t ldx, const double* h, float* w, double hsign,
                            cudaStream_t s, const int32_t* gate = nullptr) {
@@ -1503,11 +1659,13 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
         // classical Gram-Schmidt, twice (the cancellation test of a selective
         // second pass fires on nearly every Arnoldi step, so it saves nothing)
         NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, hcol, 0, s, done));
-        multi_axpy_f32(ld, j + 1, w.V, ld, hcol, w.w, 1.0, s, done);
-        NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, w.y, 0, s, done));
-        multi_axpy_f32(ld, j + 1, w.V, ld, w.y, w.w, 1.0, s, done);
+        if (!cgs2_fused(ld, j + 1, w.V, ld, hcol, w.w, w.y, hcol + j + 1, w.partial, s, done)) {
+          multi_axpy_f32(ld, j + 1, w.V, ld, hcol, w.w, 1.0, s, done);
+          NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, w.y, 0, s, done));
+          multi_axpy_f32(ld, j + 1, w.V, ld, w.y, w.w, 1.0, s, done);
+          NFEM_RC(multidot<float>(ld, 1, w.w, ld, w.w, w.partial, hcol + j + 1, 1, s, done));
+        }
         add_small<<<1, 64, 0, s>>>(j + 1, w.y, hcol, done);  // h += second-pass coefficients
-        NFEM_RC(multidot<float>(ld, 1, w.w, ld, w.w, w.partial, hcol + j + 1, 1, s, done));
         scale_by_inv<float><<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * ld, done);
         givens_update<<<1, 32, 0, s>>>(w.H, ldh, w.cs, w.sn, w.g, j, w.hist, w.status, w.gate, inner_target);
         NFEM_CHECK_LAUNCH();
