@@ -227,67 +227,133 @@ __global__ void reduce_partials(const double* __restrict__ partial, int nb, int 
   if (threadIdx.x == 0) out[j] = mode == 1 ? sqrt(t) : sign * t;
 }
 
-// FP32 basis vectors with 16-byte rows (n and the stride multiples of 4,
-// aligned pointers): float4 loads, eight vectors per pass sharing one read
-// of y, FP32 products folded into FP64 every 16 elements per thread.
-__global__ void __launch_bounds__(kRedThreads)
-    multidot_partial_v4(int64_t n4, int k, const float4* __restrict__ X, int64_t ldx4,
-                        const float4* __restrict__ y, double* __restrict__ partial, const int32_t* __restrict__ gate) {
-  NFEM_GATE(gate);
-  __shared__ double sh[kDotGroup][kRedThreads / 32];
+// ---- FP32 reductions over 16-byte rows
+// Partial sums: FP32 per thread, folded into FP64 in shared memory every 16
+// elements (the registers stay with the loads), a fixed-order block
+// reduction, one partial per (vector, block).  With a counter, the last
+// block to finish adds the partials of each vector in block order and
+// writes the result (sqrt for mode 1) -- no separate reduction launch; the
+// counter returns to 0.  The grids are the resident grids of the kernels
+// (blocks per SM x SMs), so every block streams its share in one wave.
+
+// Called by all threads of every block after the partials of vectors
+// q < k were written (partial[q * gridDim.x + blockIdx.x]).
+__device__ __forceinline__ void finish_partials(const double* partial, int k, double* __restrict__ out, int mode,
+                                                unsigned int* counter) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int q = warp; q < k; q += nw) {
+    double v = 0.0;
+    for (int b = lane; b < int(gridDim.x); b += 32) v += __ldcg(partial + int64_t(q) * gridDim.x + b);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) out[q] = mode == 1 ? sqrt(v) : v;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+template <int KM>
+__device__ __forceinline__ void block_partials(int k, const float (&accf)[KM], double (*sacc)[kRedThreads],
+                                               double (*sh)[kRedThreads / 32], double* __restrict__ partial) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  for (int j0 = 0; j0 < k; j0 += kDotGroup) {
-    const int g = min(kDotGroup, k - j0);
-    double acc[kDotGroup];
-    float accf[kDotGroup];
 #pragma unroll
-    for (int q = 0; q < kDotGroup; ++q) { acc[q] = 0.0; accf[q] = 0.f; }
-    int cnt = 0;
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n4; i += stride) {
-      const float4 yv = __ldg(y + i);
-#pragma unroll
-      for (int q = 0; q < kDotGroup; ++q) {
-        if (q < g) {
-          const float4 xv = __ldg(X + int64_t(j0 + q) * ldx4 + i);
-          accf[q] = fmaf(xv.x, yv.x, fmaf(xv.y, yv.y, fmaf(xv.z, yv.z, fmaf(xv.w, yv.w, accf[q]))));
-        }
-      }
-      if (++cnt == 16) {
-#pragma unroll
-        for (int q = 0; q < kDotGroup; ++q) { acc[q] += double(accf[q]); accf[q] = 0.f; }
-        cnt = 0;
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < kDotGroup; ++q) {
-      double v = acc[q] + double(accf[q]);
+  for (int q = 0; q < KM; ++q) {
+    if (q < k) {
+      double v = sacc[q][threadIdx.x] + double(accf[q]);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
       if (lane == 0) sh[q][warp] = v;
     }
-    __syncthreads();
-    if (threadIdx.x < g) {
-      double t = 0.0;
-      for (int w = 0; w < (kRedThreads / 32); ++w) t += sh[threadIdx.x][w];
-      partial[int64_t(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < k) {
+    double t = 0.0;
+    for (int w = 0; w < (kRedThreads / 32); ++w) t += sh[threadIdx.x][w];
+    partial[int64_t(threadIdx.x) * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// partial[q][block] = sum_i X_q[i] . y[i], q < k, eight vectors per pass
+// sharing one read of y
+__global__ void __launch_bounds__(kRedThreads)
+    multidot_partial_v4(int64_t n4, int k, const float4* __restrict__ X, int64_t ldx4,
+                        const float4* __restrict__ y, double* __restrict__ partial, double* __restrict__ out,
+                        int mode, unsigned int* counter, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
+  __shared__ double sacc[kDotGroup][kRedThreads];
+  __shared__ double sh[kDotGroup][kRedThreads / 32];
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int j0 = 0; j0 < k; j0 += kDotGroup) {
+    const int g = min(kDotGroup, k - j0);
+#pragma unroll
+    for (int q = 0; q < kDotGroup; ++q) sacc[q][threadIdx.x] = 0.0;
+    float accf[kDotGroup];
+#pragma unroll
+    for (int q = 0; q < kDotGroup; ++q) accf[q] = 0.f;
+    int cnt = 0;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n4; i += stride) {
+      const float4 yv = __ldg(y + i);
+      const float4* xq = X + int64_t(j0) * ldx4 + i;
+#pragma unroll
+      for (int q = 0; q < kDotGroup; ++q) {
+        if (q < g) {
+          const float4 xv = __ldg(xq);
+          accf[q] = fmaf(xv.x, yv.x, fmaf(xv.y, yv.y, fmaf(xv.z, yv.z, fmaf(xv.w, yv.w, accf[q]))));
+        }
+        xq += ldx4;
+      }
+      if (++cnt == 16) {
+#pragma unroll
+        for (int q = 0; q < kDotGroup; ++q) {
+          sacc[q][threadIdx.x] += double(accf[q]);
+          accf[q] = 0.f;
+        }
+        cnt = 0;
+      }
     }
+    block_partials<kDotGroup>(g, accf, sacc, sh, partial + int64_t(j0) * gridDim.x);
     __syncthreads();
   }
+  if (counter) finish_partials(partial, k, out, mode, counter);
 }
 
 static bool rows16(int64_t n, int64_t ldx, const void* a, const void* b) {
   return n % 4 == 0 && ldx % 4 == 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) == 0;
 }
 
+// Blocks of `kernel` resident on the whole device at kRedThreads threads
+// (at most kRedBlocks, the partial buffers' width); cached per kernel.
+template <typename K>
+static int resident_grid(K kernel, int* cache) {
+  if (*cache > 0) return *cache;
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kRedThreads, 0) != cudaSuccess || per < 1)
+    return kRedBlocks;
+  *cache = std::min(per * sms, kRedBlocks);
+  return *cache;
+}
+
+// out[q] = X_q . y (q < k), sqrt of it for mode 1.  counter: the FP32
+// 16-byte-row form finishes the sum in the kernel (see finish_partials).
 template <typename T>
 static int multidot(int64_t n, int k, const T* X, int64_t ldx, const T* y, double* partial, double* out, int mode,
-                    cudaStream_t s, const int32_t* gate = nullptr) {
+                    cudaStream_t s, const int32_t* gate = nullptr, unsigned int* counter = nullptr) {
   if constexpr (sizeof(T) == 4) {
     if (rows16(n, ldx, X, y)) {
-      multidot_partial_v4<<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, reinterpret_cast<const float4*>(X), ldx / 4,
-                                                             reinterpret_cast<const float4*>(y), partial, gate);
-      reduce_partials<<<k, 256, 0, s>>>(partial, kRedBlocks, k, out, mode, 1.0);
+      static int cache = 0;
+      const int nb = resident_grid(multidot_partial_v4, &cache);
+      multidot_partial_v4<<<nb, kRedThreads, 0, s>>>(n / 4, k, reinterpret_cast<const float4*>(X), ldx / 4,
+                                                     reinterpret_cast<const float4*>(y), partial, out, mode, counter,
+                                                     gate);
+      if (!counter) reduce_partials<<<k, 256, 0, s>>>(partial, nb, k, out, mode, 1.0);
       NFEM_CHECK_LAUNCH();
       return NFEM_OK;
     }
@@ -359,27 +425,6 @@ __global__ void multi_axpy_v4(int64_t n4, int k, const float4* __restrict__ X, i
 // multidot_partial_v4: FP32 per thread, folded into FP64 every 16
 // elements (here into shared memory, to keep the registers for X), a
 // fixed-order block reduction, one partial per (vector, block).
-template <int KM>
-__device__ __forceinline__ void block_partials(int k, const float (&accf)[KM], double (*sacc)[kRedThreads],
-                                               double (*sh)[kRedThreads / 32], double* __restrict__ partial) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int q = 0; q < KM; ++q) {
-    if (q < k) {
-      double v = sacc[q][threadIdx.x] + double(accf[q]);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-      if (lane == 0) sh[q][warp] = v;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < k) {
-    double t = 0.0;
-    for (int w = 0; w < (kRedThreads / 32); ++w) t += sh[threadIdx.x][w];
-    partial[int64_t(threadIdx.x) * gridDim.x + blockIdx.x] = t;
-  }
-}
-
 // w <- w - X h;  partial = per-block sums of X^T w (the updated w)
 #ifndef NFEM_CGS_MIN_BLOCKS
 #define NFEM_CGS_MIN_BLOCKS 2
@@ -387,7 +432,8 @@ __device__ __forceinline__ void block_partials(int k, const float (&accf)[KM], d
 template <int KM>
 __global__ void __launch_bounds__(kRedThreads, NFEM_CGS_MIN_BLOCKS)
     axpy_dot_v4(int64_t n4, int k, const float4* __restrict__ X, int64_t ldx4, const double* __restrict__ h,
-                float4* __restrict__ w, double* __restrict__ partial, const int32_t* __restrict__ gate) {
+                float4* __restrict__ w, double* __restrict__ partial, double* __restrict__ out,
+                unsigned int* counter, const int32_t* __restrict__ gate) {
   NFEM_GATE(gate);
   __shared__ float hs[KM];
   __shared__ double sacc[KM][kRedThreads];
@@ -439,13 +485,15 @@ __global__ void __launch_bounds__(kRedThreads, NFEM_CGS_MIN_BLOCKS)
     }
   }
   block_partials<KM>(k, accf, sacc, sh, partial);
+  finish_partials(partial, k, out, 0, counter);
 }
 
 // w <- w - X h;  partial = per-block sums of w . w (the updated w)
 template <int KM>
 __global__ void __launch_bounds__(kRedThreads)
     axpy_norm_v4(int64_t n4, int k, const float4* __restrict__ X, int64_t ldx4, const double* __restrict__ h,
-                 float4* __restrict__ w, double* __restrict__ partial, const int32_t* __restrict__ gate) {
+                 float4* __restrict__ w, double* __restrict__ partial, double* __restrict__ out,
+                 unsigned int* counter, const int32_t* __restrict__ gate) {
   NFEM_GATE(gate);
   __shared__ float hs[KM];
   __shared__ double sacc[1][kRedThreads];
@@ -483,6 +531,7 @@ __global__ void __launch_bounds__(kRedThreads)
     }
   }
   block_partials<1>(1, accf, sacc, sh, partial);
+  finish_partials(partial, 1, out, 1, counter);
 }
 
 // The second Gram-Schmidt pass and the norm, given the first pass's
@@ -490,20 +539,24 @@ __global__ void __launch_bounds__(kRedThreads)
 // y = X^T w, w <- w - X y, nrm = ||w||.  Returns false (nothing launched)
 // when the fused form does not apply.
 static bool cgs2_fused(int64_t n, int k, const float* X, int64_t ldx, const double* h, float* w, double* y,
-                       double* nrm, double* partial, cudaStream_t s, const int32_t* gate) {
+                       double* nrm, double* partial, unsigned int* counter, cudaStream_t s,
+                       const int32_t* gate) {
   if (k > 16 || !rows16(n, ldx, X, w)) return false;
   const auto* X4 = reinterpret_cast<const float4*>(X);
   auto* w4 = reinterpret_cast<float4*>(w);
   if (k <= 8) {
-    axpy_dot_v4<8><<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, h, w4, partial, gate);
-    reduce_partials<<<k, 256, 0, s>>>(partial, kRedBlocks, k, y, 0, 1.0);
-    axpy_norm_v4<8><<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, y, w4, partial, gate);
+    static int c1 = 0, c2 = 0;
+    axpy_dot_v4<8><<<resident_grid(axpy_dot_v4<8>, &c1), kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, h, w4, partial,
+                                                                              y, counter, gate);
+    axpy_norm_v4<8><<<resident_grid(axpy_norm_v4<8>, &c2), kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, y, w4,
+                                                                                partial, nrm, counter, gate);
   } else {
-    axpy_dot_v4<16><<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, h, w4, partial, gate);
-    reduce_partials<<<k, 256, 0, s>>>(partial, kRedBlocks, k, y, 0, 1.0);
-    axpy_norm_v4<16><<<kRedBlocks, kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, y, w4, partial, gate);
+    static int c1 = 0, c2 = 0;
+    axpy_dot_v4<16><<<resident_grid(axpy_dot_v4<16>, &c1), kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, h, w4,
+                                                                                partial, y, counter, gate);
+    axpy_norm_v4<16><<<resident_grid(axpy_norm_v4<16>, &c2), kRedThreads, 0, s>>>(n / 4, k, X4, ldx / 4, y, w4,
+                                                                                  partial, nrm, counter, gate);
   }
-  reduce_partials<<<1, 256, 0, s>>>(partial, kRedBlocks, 1, nrm, 1, 1.0);
   return true;
 }
 
@@ -1294,12 +1347,14 @@ __global__ void block_apply(int64_t n_rows, const int32_t* __restrict__ inc_ptr,
 
 // ------------------------------------------------------------------ Hessenberg / Givens
 // Column j of H holds h[0..j+1]; rotations cs/sn; g the rotated rhs.
-__global__ void givens_update(double* __restrict__ H, int ldh, double* __restrict__ cs, double* __restrict__ sn,
-                              double* __restrict__ g, int j, double* __restrict__ hist, int32_t* status,
-                              int32_t* __restrict__ gate, double target) {
+__global__ void givens_update(double* __restrict__ H, int ldh, const double* __restrict__ h2,
+                              double* __restrict__ cs, double* __restrict__ sn, double* __restrict__ g, int j,
+                              double* __restrict__ hist, int32_t* status, int32_t* __restrict__ gate,
+                              double target) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (gate && gate[0]) return;
   double* h = H + int64_t(j) * ldh;
+  for (int i = 0; i <= j; ++i) h[i] += h2[i];  // second Gram-Schmidt pass
   for (int i = 0; i < j; ++i) {
     const double t = cs[i] * h[i] + sn[i] * h[i + 1];
     h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
@@ -1333,12 +1388,6 @@ __global__ void upper_solve(const double* __restrict__ H, int ldh, const double*
     for (int j = i + 1; j < k; ++j) s -= H[int64_t(j) * ldh + i] * y[j];
     y[i] = s / H[int64_t(i) * ldh + i];
   }
-}
-
-__global__ void add_small(int k, const double* __restrict__ y, double* __restrict__ h,
-                          const int32_t* __restrict__ gate) {
-  NFEM_GATE(gate);
-  for (int i = threadIdx.x; i < k; i += blockDim.x) h[i] += y[i];
 }
 
 __global__ void init_cycle(double* __restrict__ g, int m, const double* __restrict__ beta, int32_t* __restrict__ gate) {
@@ -1528,6 +1577,7 @@ struct SolveWs {
   float *V, *Z, *w, *t32, *r32, *d32;
   double *r64, *partial, *H, *cs, *sn, *g, *hist, *y, *scal;
   int32_t *status, *gate;
+  unsigned int* counter;  // finish_partials (returns to 0 after every use)
 };
 
 // FP32 Krylov vectors are padded to a multiple of four entries (zero tails)
@@ -1555,6 +1605,7 @@ static size_t solve_ws_bytes(int64_t n, int m, SolveWs* out, void* base) {
   w.scal = c.take<double>(8);
   w.status = c.take<int32_t>(4);
   w.gate = c.take<int32_t>(4);
+  w.counter = c.take<unsigned int>(4);
   if (out) *out = w;
   return c.off + 256;
 }
@@ -1584,6 +1635,7 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
   const int gv = grid_for(n, B);
   const int ldh = m + 1;
   NFEM_TRY_CUDA(cudaMemsetAsync(w.status, 0, 4 * sizeof(int32_t), s));
+  NFEM_TRY_CUDA(cudaMemsetAsync(w.counter, 0, 4 * sizeof(unsigned int), s));
   // ld: stride of the basis vectors; entries n .. ld - 1 of every FP32 vector
   // are zero and stay zero (kernels of length n never write them, the
   // Gram-Schmidt updates of length ld add zero to them)
@@ -1623,7 +1675,7 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       NFEM_TRY_CUDA(cudaMemcpyAsync(w.V, w.r32, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
     // the inner solve reduces the W-weighted residual norm by inner_rtol;
     // the outer loop measures the true FP64 residual
-    NFEM_RC(multidot<float>(ld, 1, w.V, ld, w.V, w.partial, w.scal + 3, 1, s));
+    NFEM_RC(multidot<float>(ld, 1, w.V, ld, w.V, w.partial, w.scal + 3, 1, s, nullptr, w.counter));
     double wr0 = 0.0;
     NFEM_TRY_CUDA(cudaMemcpyAsync(&wr0, w.scal + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
     NFEM_TRY_CUDA(cudaStreamSynchronize(s));
@@ -1638,7 +1690,7 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
                                           w.r32, 1, s, weighted ? pc->wsqrt : nullptr));
       }
       first_cycle = false;
-      NFEM_RC(multidot<float>(ld, 1, w.V, ld, w.V, w.partial, w.scal + 2, 1, s));
+      NFEM_RC(multidot<float>(ld, 1, w.V, ld, w.V, w.partial, w.scal + 2, 1, s, nullptr, w.counter));
       scale_by_inv<float><<<gv, B, 0, s>>>(n, w.V, w.scal + 2, w.V, nullptr);
       init_cycle<<<1, 128, 0, s>>>(w.g, m, w.scal + 2, w.gate);
       NFEM_CHECK_LAUNCH();
@@ -1658,16 +1710,16 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
         double* hcol = w.H + int64_t(j) * ldh;
         // classical Gram-Schmidt, twice (the cancellation test of a selective
         // second pass fires on nearly every Arnoldi step, so it saves nothing)
-        NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, hcol, 0, s, done));
-        if (!cgs2_fused(ld, j + 1, w.V, ld, hcol, w.w, w.y, hcol + j + 1, w.partial, s, done)) {
+        NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, hcol, 0, s, done, w.counter));
+        if (!cgs2_fused(ld, j + 1, w.V, ld, hcol, w.w, w.y, hcol + j + 1, w.partial, w.counter, s, done)) {
           multi_axpy_f32(ld, j + 1, w.V, ld, hcol, w.w, 1.0, s, done);
-          NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, w.y, 0, s, done));
+          NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, w.y, 0, s, done, w.counter));
           multi_axpy_f32(ld, j + 1, w.V, ld, w.y, w.w, 1.0, s, done);
-          NFEM_RC(multidot<float>(ld, 1, w.w, ld, w.w, w.partial, hcol + j + 1, 1, s, done));
+          NFEM_RC(multidot<float>(ld, 1, w.w, ld, w.w, w.partial, hcol + j + 1, 1, s, done, w.counter));
         }
-        add_small<<<1, 64, 0, s>>>(j + 1, w.y, hcol, done);  // h += second-pass coefficients
         scale_by_inv<float><<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * ld, done);
-        givens_update<<<1, 32, 0, s>>>(w.H, ldh, w.cs, w.sn, w.g, j, w.hist, w.status, w.gate, inner_target);
+        // h += the second pass's coefficients w.y, then the rotations
+        givens_update<<<1, 32, 0, s>>>(w.H, ldh, w.y, w.cs, w.sn, w.g, j, w.hist, w.status, w.gate, inner_target);
         NFEM_CHECK_LAUNCH();
       }
       // one synchronisation per cycle: residual estimates of every step
