@@ -389,6 +389,17 @@ typedef struct {
   const int32_t* blk_ptr;    /* [n_blocks + 1] */
   const int64_t* blk_off;    /* [n_blocks + 1] */
   const int32_t* agg_blk;    /* [n_agg] block of each aggregate */
+  /* Optional product A P of the FP32 matrix and the prolongation (CSR,
+   * columns = aggregates).  With it the preconditioner also returns A z for
+   * the z it computes, as (v - r) + (A P) e from the residual r = v - A z_s
+   * of its smoother step and the coarse correction e, and the Krylov solver
+   * skips its own SpMV with A.  ap_ptr [n_rows + 1] and ap_col [ap_nnz] come
+   * from nfem_two_level_ap_pattern; nfem_precond_setup fills ap_val [ap_nnz]
+   * from the FP32 matrix (a32 in nfem_precond).  ap_ptr == NULL: not used. */
+  int64_t ap_nnz;
+  const int32_t* ap_ptr;
+  const int32_t* ap_col;
+  float* ap_val;
 } nfem_two_level;
 
 #define NFEM_COARSE_BLOCK_MAX 1024
@@ -447,6 +458,16 @@ int nfem_residual_f64(int64_t n_rows, const int32_t* row_ptr, const int32_t* col
  * FP64 Gauss-Jordan, stored FP32). */
 int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, int32_t* dev_status,
                        void* stream);
+/* Pattern of A P (see nfem_two_level.ap_ptr) from the pattern of A and the
+ * aggregates of P (L->p_agg).  ap_col == NULL: counts the distinct aggregates
+ * of each row into the offsets ap_ptr [n_rows + 1] and returns their total in
+ * *nnz_host (synchronises `stream`).  Otherwise fills ap_col [*nnz_host],
+ * ascending in each row, for the ap_ptr of the first call.  Rows with more
+ * than 64 distinct aggregates report NFEM_ERR_CAPACITY. */
+int nfem_two_level_ap_workspace_bytes(int64_t n_rows, size_t* bytes);
+int nfem_two_level_ap_pattern(const nfem_csr* A, const nfem_two_level* L, void* workspace,
+                              size_t workspace_bytes, int32_t* ap_ptr, int32_t* ap_col,
+                              int64_t* nnz_host, int32_t* dev_status, void* stream);
 int nfem_precond_apply(const nfem_precond* pc, int64_t n, const float* v, float* z, void* stream);
 int nfem_solve_workspace_bytes(int64_t n_rows, int restart, size_t* bytes);
 /* Synchronises on `stream` once per GMRES cycle and per refinement step. */

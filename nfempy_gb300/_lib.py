@@ -50,7 +50,8 @@ class TwoLevel(C.Structure):
                 ("pt_row", C.c_void_p), ("pt_slot", C.c_void_p), ("pt_val", C.c_void_p), ("ac", C.c_void_p),
                 ("gj", C.c_void_p), ("ac_inv", C.c_void_p), ("work", C.c_void_p), ("n_blocks", C.c_int32),
                 ("blk_max", C.c_int32), ("ac_entries", C.c_int64), ("blk_ptr", C.c_void_p), ("blk_off", C.c_void_p),
-                ("agg_blk", C.c_void_p)]
+                ("agg_blk", C.c_void_p), ("ap_nnz", C.c_int64), ("ap_ptr", C.c_void_p), ("ap_col", C.c_void_p),
+                ("ap_val", C.c_void_p)]
 
 
 class Precond(C.Structure):
@@ -102,6 +103,9 @@ _SIGS = {
     "nfem_residual_f64": ([_I64, _P, _P, _P, _P, _P, _P, _P], _I),
     "nfem_precond_setup": ([C.POINTER(Precond), C.POINTER(Csr), _P, _P], _I),
     "nfem_precond_apply": ([C.POINTER(Precond), _I64, _P, _P, _P], _I),
+    "nfem_two_level_ap_workspace_bytes": ([_I64, C.POINTER(_SZ)], _I),
+    "nfem_two_level_ap_pattern": ([C.POINTER(Csr), C.POINTER(TwoLevel), _P, _SZ, _P, _P, C.POINTER(_I64), _P, _P],
+                                  _I),
     "nfem_solve_workspace_bytes": ([_I64, _I, C.POINTER(_SZ)], _I),
     "nfem_solve_ir_fgmres": ([C.POINTER(Csr), C.POINTER(Csr), C.POINTER(Precond), _P, _P, C.POINTER(SolveParams),
                               _P, _SZ, C.POINTER(SolveInfo), _P], _I),

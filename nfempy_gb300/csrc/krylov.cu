@@ -1218,6 +1218,121 @@ __global__ void twolevel_prolong(int64_t n_rows, const int32_t* __restrict__ p_a
   }
 }
 
+// ---- A P (FP32 matrix times prolongation), for the fused apply
+constexpr int kApCap = 64;  // distinct aggregates of one row
+
+// Sorted distinct aggregates of the P rows named by the columns of row i.
+__device__ __forceinline__ int ap_row_aggs(int64_t i, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                           const int32_t* __restrict__ p_agg, int32_t (&list)[kApCap],
+                                           int32_t* status) {
+  int m = 0;
+  for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+    const int64_t j = ci[k];
+#pragma unroll
+    for (int sl = 0; sl < 2; ++sl) {
+      int32_t a = p_agg[2 * j + sl];
+      if (a < 0) continue;
+      int pos = 0;
+      while (pos < m && list[pos] < a) ++pos;
+      if (pos < m && list[pos] == a) continue;
+      if (m == kApCap) {
+        set_status(status, NFEM_ERR_CAPACITY);
+        return m;
+      }
+      for (int t = m; t > pos; --t) list[t] = list[t - 1];
+      list[pos] = a;
+      ++m;
+    }
+  }
+  return m;
+}
+
+__global__ void ap_count(int64_t n_rows, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                         const int32_t* __restrict__ p_agg, int32_t* __restrict__ counts, int32_t* status) {
+  int32_t list[kApCap];
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows; i += int64_t(gridDim.x) * blockDim.x)
+    counts[i] = ap_row_aggs(i, rp, ci, p_agg, list, status);
+}
+
+__global__ void ap_fill_cols(int64_t n_rows, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                             const int32_t* __restrict__ p_agg, const int32_t* __restrict__ ap_ptr,
+                             int32_t* __restrict__ ap_col, int32_t* status) {
+  int32_t list[kApCap];
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int m = ap_row_aggs(i, rp, ci, p_agg, list, status);
+    if (m != ap_ptr[i + 1] - ap_ptr[i]) {
+      set_status(status, NFEM_ERR_PATTERN);
+      continue;
+    }
+    for (int t = 0; t < m; ++t) ap_col[ap_ptr[i] + t] = list[t];
+  }
+}
+
+// ap_val = sum over the row's nonzeros j and P slots s of a_ij p_val[j, s],
+// in column order (FP64 sums of the FP32 products' operands, rounded once)
+__global__ void ap_fill_values(int64_t n_rows, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                               const float* __restrict__ a32, const int32_t* __restrict__ p_agg,
+                               const float* __restrict__ p_val, const int32_t* __restrict__ ap_ptr,
+                               const int32_t* __restrict__ ap_col, float* __restrict__ ap_val, int32_t* status) {
+  double acc[kApCap];
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t e0 = ap_ptr[i];
+    const int m = ap_ptr[i + 1] - e0;
+    if (m > kApCap) {
+      set_status(status, NFEM_ERR_CAPACITY);
+      continue;
+    }
+    for (int t = 0; t < m; ++t) acc[t] = 0.0;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+      const int64_t j = ci[k];
+#pragma unroll
+      for (int sl = 0; sl < 2; ++sl) {
+        const int32_t a = p_agg[2 * j + sl];
+        if (a < 0) continue;
+        int t = 0;
+        while (t < m && ap_col[e0 + t] != a) ++t;
+        if (t == m) {
+          set_status(status, NFEM_ERR_PATTERN);
+          continue;
+        }
+        acc[t] += double(a32[k]) * double(p_val[2 * j + sl]);
+      }
+    }
+    for (int t = 0; t < m; ++t) ap_val[e0 + t] = float(acc[t]);
+  }
+}
+
+__global__ void offsets_i32(const int64_t* __restrict__ in, int64_t n, int32_t* __restrict__ out) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = int32_t(in[i]);
+}
+
+// z += P ec and, with A P, w = yscale (.) ((v - r) + (A P) ec) = yscale (.) A z
+__global__ void twolevel_prolong_ap(int64_t n_rows, const int32_t* __restrict__ p_agg,
+                                    const float* __restrict__ p_val, const float* __restrict__ ec,
+                                    float* __restrict__ z, const int32_t* __restrict__ ap_ptr,
+                                    const int32_t* __restrict__ ap_col, const float* __restrict__ ap_val,
+                                    const float* __restrict__ v, const float* __restrict__ r,
+                                    const float* __restrict__ yscale, float* __restrict__ w,
+                                    const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows; i += int64_t(gridDim.x) * blockDim.x) {
+    float acc = 0.f;
+#pragma unroll
+    for (int sl = 0; sl < 2; ++sl) {
+      const int32_t a = p_agg[2 * i + sl];
+      if (a >= 0) acc = fmaf(p_val[2 * i + sl], ec[a], acc);
+    }
+    z[i] += acc;
+    float ap = 0.f;
+    for (int32_t e = ap_ptr[i]; e < ap_ptr[i + 1]; ++e) ap = fmaf(__ldg(ap_val + e), __ldg(ec + __ldg(ap_col + e)), ap);
+    const float az = (v[i] - r[i]) + ap;
+    w[i] = yscale ? yscale[i] * az : az;
+  }
+}
+
 // pt_val[k] = p_val of the (row, slot) that P^T entry k refers to
 __global__ void twolevel_fill_pt(int64_t nnz, const int32_t* __restrict__ pt_slot, const float* __restrict__ p_val,
                                  float* __restrict__ pt_val) {
@@ -1476,6 +1591,13 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     twolevel_fill_p<<<g, 256, 0, s>>>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, L->p_base,
                                       pc->n_cells, L->cell_agg, L->w, L->p_agg, L->p_val);
     twolevel_fill_pt<<<grid_for(L->pt_nnz, 256), 256, 0, s>>>(L->pt_nnz, L->pt_slot, L->p_val, L->pt_val);
+    if (L->ap_ptr) {
+      if (!L->ap_col || !L->ap_val || !pc->a32 || pc->a32->value_type != NFEM_F32 || pc->a32->n_rows != n)
+        return NFEM_ERR_INVALID_ARG;
+      ap_fill_values<<<g, 256, 0, s>>>(n, pc->a32->row_ptr, pc->a32->col_idx, (const float*)pc->a32->values,
+                                       L->p_agg, L->p_val, L->ap_ptr, L->ap_col, L->ap_val, dev_status);
+      NFEM_CHECK_LAUNCH();
+    }
     const bool blocks = L->n_blocks > 0;
     const CoarseIndex at{na, L->blk_ptr, L->blk_off, blocks ? L->agg_blk : nullptr};
     NFEM_TRY_CUDA(cudaMemsetAsync(L->ac, 0, size_t(blocks ? L->ac_entries : int64_t(na) * na) * sizeof(double), s));
@@ -1505,8 +1627,12 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
   return NFEM_OK;
 }
 
+// z = M v.  With w_out and the two-level A P, also w_out = yscale (.) A z
+// (*w_done = true); the caller's SpMV is then not needed.
 static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, float* z, cudaStream_t s,
-                         const int32_t* gate = nullptr) {
+                         const int32_t* gate = nullptr, float* w_out = nullptr, const float* yscale = nullptr,
+                         bool* w_done = nullptr) {
+  if (w_done) *w_done = false;
   const int B = 256;
   switch (pc->kind) {
     case NFEM_PC_NONE:
@@ -1554,7 +1680,13 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
                                                                            L->ac_inv, rc, ec, gate);
     else
       dense_gemv<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->ac_inv, rc, ec, gate);
-    twolevel_prolong<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z, gate);
+    if (w_out && L->ap_ptr) {
+      twolevel_prolong_ap<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z, L->ap_ptr, L->ap_col,
+                                                           L->ap_val, v, r2, yscale, w_out, gate);
+      if (w_done) *w_done = true;
+    } else {
+      twolevel_prolong<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z, gate);
+    }
     NFEM_CHECK_LAUNCH();
   }
   return NFEM_OK;
@@ -1564,6 +1696,47 @@ extern "C" int nfem_precond_apply(const nfem_precond* pc, int64_t n, const float
   if (!pc || n < 0 || (n > 0 && (!v || !z))) return NFEM_ERR_INVALID_ARG;
   if (n == 0) return NFEM_OK;
   return precond_apply(pc, n, v, z, (cudaStream_t)stream);
+}
+
+extern "C" int nfem_two_level_ap_workspace_bytes(int64_t n_rows, size_t* bytes) {
+  if (!bytes || n_rows < 0) return NFEM_ERR_INVALID_ARG;
+  *bytes = align256(size_t(n_rows) * 4) + align256(size_t(n_rows + 1) * 8) + scan_workspace_bytes(n_rows) + 1024;
+  return NFEM_OK;
+}
+
+extern "C" int nfem_two_level_ap_pattern(const nfem_csr* A, const nfem_two_level* L, void* workspace,
+                                         size_t workspace_bytes, int32_t* ap_ptr, int32_t* ap_col,
+                                         int64_t* nnz_host, int32_t* dev_status, void* stream) {
+  if (!A || !L || !ap_ptr || !nnz_host || !L->p_agg || A->n_rows < 0 || !A->row_ptr || !A->col_idx)
+    return NFEM_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t n = A->n_rows;
+  const int g = grid_for(n, 128);
+  if (ap_col) {
+    if (n > 0) ap_fill_cols<<<g, 128, 0, s>>>(n, A->row_ptr, A->col_idx, L->p_agg, ap_ptr, ap_col, dev_status);
+    NFEM_CHECK_LAUNCH();
+    return NFEM_OK;
+  }
+  size_t need = 0;
+  nfem_two_level_ap_workspace_bytes(n, &need);
+  if (!workspace || workspace_bytes < need) return NFEM_ERR_WORKSPACE;
+  Carver cw{reinterpret_cast<char*>(workspace), 0, workspace_bytes};
+  int32_t* counts = cw.take<int32_t>(n);
+  int64_t* off = cw.take<int64_t>(n + 1);
+  const size_t sws_b = scan_workspace_bytes(n);
+  void* sws = cw.take<char>(sws_b);
+  if (!cw.ok()) return NFEM_ERR_WORKSPACE;
+  if (n > 0) ap_count<<<g, 128, 0, s>>>(n, A->row_ptr, A->col_idx, L->p_agg, counts, dev_status);
+  NFEM_CHECK_LAUNCH();
+  NFEM_RC(exclusive_scan_i32(counts, n, off, sws, sws_b, s));
+  int64_t total = 0;
+  NFEM_TRY_CUDA(cudaMemcpyAsync(&total, off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  NFEM_TRY_CUDA(cudaStreamSynchronize(s));
+  if (total >= INT32_MAX) return NFEM_ERR_OVERFLOW;
+  offsets_i32<<<grid_for(n + 1, 256), 256, 0, s>>>(off, n + 1, ap_ptr);
+  NFEM_CHECK_LAUNCH();
+  *nnz_host = total;
+  return NFEM_OK;
 }
 
 // workspace layout of the solver
@@ -1699,14 +1872,17 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
         float* vj = w.V + int64_t(j) * ld;
         float* zj = w.Z + int64_t(j) * ld;
         const int32_t* done = w.gate;
+        // w = W^1/2 A z_j: from the two-level apply when it carries A P
+        bool w_done = false;
         if (weighted) {
           scale_vec<<<gv, B, 0, s>>>(n, pc->winvsqrt, vj, w.t32, done);
-          NFEM_RC(precond_apply(pc, n, w.t32, zj, s, done));
+          NFEM_RC(precond_apply(pc, n, w.t32, zj, s, done, w.w, pc->wsqrt, &w_done));
         } else {
-          NFEM_RC(precond_apply(pc, n, vj, zj, s, done));
+          NFEM_RC(precond_apply(pc, n, vj, zj, s, done, w.w, nullptr, &w_done));
         }
-        NFEM_RC(spmv<float, float, float>(n, A32->row_ptr, A32->col_idx, (const float*)A32->values, zj, w.w,
-                                          nullptr, 0, s, weighted ? pc->wsqrt : nullptr, done));
+        if (!w_done)
+          NFEM_RC(spmv<float, float, float>(n, A32->row_ptr, A32->col_idx, (const float*)A32->values, zj, w.w,
+                                            nullptr, 0, s, weighted ? pc->wsqrt : nullptr, done));
         double* hcol = w.H + int64_t(j) * ldh;
         // classical Gram-Schmidt, twice (the cancellation test of a selective
         // second pass fires on nearly every Arnoldi step, so it saves nothing)

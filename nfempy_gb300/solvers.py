@@ -167,7 +167,7 @@ class TwoLevelCoarse:
     pressure columns).  w = None gives the classical weights 1/|a_ff|; the
     learned preconditioner passes the network's prediction."""
 
-    def __init__(self, A, n_c, w=None, cell_agg=None, blocks=None):
+    def __init__(self, A, n_c, w=None, cell_agg=None, blocks=None, fuse_ap=True):
         """cell_agg: optional aggregate of every cell (0 .. n_agg - 1) in place
         of the centroid grid, e.g. per-problem grids for a batch of
         independent problems assembled as one disjoint union.
@@ -176,7 +176,11 @@ class TwoLevelCoarse:
         aggregates of block b (blocks[b] .. blocks[b + 1] - 1) couple to no
         other block -- the problems of such a batch.  The coarse matrix is then
         stored, inverted and applied block by block (sum of s_b^2 entries in
-        place of n_agg^2), which admits many more aggregates."""
+        place of n_agg^2), which admits many more aggregates.
+
+        fuse_ap: keep the product A P (its pattern is built here, its values
+        in every preconditioner setup), so that the preconditioner hands back
+        A z with z and the solver saves one SpMV per iteration."""
         sp = A.space
         self.A = A
         dim = sp.dim
@@ -279,6 +283,35 @@ class TwoLevelCoarse:
                                     _lib.ptr(self.pt_slot).value, _lib.ptr(self.pt_val).value,
                                     _lib.ptr(self.ac).value, _lib.ptr(self.gj).value, _lib.ptr(self.ac_inv).value,
                                     _lib.ptr(self.work).value, *blk)
+        if fuse_ap:
+            self._build_ap()
+
+    def _build_ap(self):
+        A = self.A
+        n = A.n_rows
+        dev = A.values.device
+        csr = _csr(A)
+        ws_b = _lib.C.c_size_t(0)
+        _lib.call("nfem_two_level_ap_workspace_bytes", n, _lib.C.byref(ws_b))
+        ws = torch.empty(int(ws_b.value), dtype=torch.uint8, device=dev)
+        status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.ap_ptr = torch.empty(n + 1, dtype=torch.int32, device=dev)
+        nnz = _lib.C.c_int64(0)
+        _lib.call("nfem_two_level_ap_pattern", _lib.C.byref(csr), _lib.C.byref(self.struct), _lib.ptr(ws),
+                  ws.numel(), _lib.ptr(self.ap_ptr), None, _lib.C.byref(nnz), _lib.ptr(status), _lib.stream_ptr())
+        self.ap_col = torch.empty(max(1, nnz.value), dtype=torch.int32, device=dev)
+        self.ap_val = torch.zeros(max(1, nnz.value), dtype=torch.float32, device=dev)
+        _lib.call("nfem_two_level_ap_pattern", _lib.C.byref(csr), _lib.C.byref(self.struct), _lib.ptr(ws),
+                  ws.numel(), _lib.ptr(self.ap_ptr), _lib.ptr(self.ap_col), _lib.C.byref(nnz), _lib.ptr(status),
+                  _lib.stream_ptr())
+        st = int(status.item())
+        if st:
+            raise _lib.NfemError(st, "A P pattern")
+        self.ap_nnz = int(nnz.value)
+        self.struct.ap_nnz = self.ap_nnz
+        self.struct.ap_ptr = _lib.ptr(self.ap_ptr).value
+        self.struct.ap_col = _lib.ptr(self.ap_col).value
+        self.struct.ap_val = _lib.ptr(self.ap_val).value
 
     def classical_weights(self):
         d = self.A.diagonal().abs()

@@ -112,6 +112,30 @@ def test_new_workspace_queries_and_argument_checks(lib_path):
     assert lib.nfem_darcy_rt1p0_assemble(3, 9, *args[2:]) == 1
 
 
+def test_two_level_ap_queries_and_argument_checks(lib_path):
+    """Host-side checks of the A P pattern entry points: the workspace size
+    grows with the rows, and missing structures are refused before any device
+    work."""
+    lib = _lib.lib()
+    b = ctypes.c_size_t(0)
+    assert lib.nfem_two_level_ap_workspace_bytes(1000, ctypes.byref(b)) == 0
+    small = b.value
+    assert lib.nfem_two_level_ap_workspace_bytes(100000, ctypes.byref(b)) == 0 and b.value > small > 12000
+    assert lib.nfem_two_level_ap_workspace_bytes(-1, ctypes.byref(b)) == 1
+    nnz = ctypes.c_int64(0)
+    csr = _lib.Csr(10, None, None, None, _lib.NFEM_F32)
+    tl = _lib.TwoLevel()
+    # no P aggregates, then no CSR arrays
+    assert lib.nfem_two_level_ap_pattern(ctypes.byref(csr), ctypes.byref(tl), None, 0, ctypes.c_void_p(64), None,
+                                         ctypes.byref(nnz), None, None) == 1
+    tl.p_agg = 64
+    assert lib.nfem_two_level_ap_pattern(ctypes.byref(csr), ctypes.byref(tl), None, 0, ctypes.c_void_p(64), None,
+                                         ctypes.byref(nnz), None, None) == 1
+    csr2 = _lib.Csr(10, 64, 64, None, _lib.NFEM_F32)
+    assert lib.nfem_two_level_ap_pattern(ctypes.byref(csr2), ctypes.byref(tl), None, 0, ctypes.c_void_p(64), None,
+                                         ctypes.byref(nnz), None, None) == 3  # NFEM_ERR_WORKSPACE
+
+
 def test_status_string_for_every_code(lib_path):
     lib = _lib.lib()
     for code, name in _lib.STATUS_NAMES.items():
