@@ -571,15 +571,19 @@ static void multi_axpy_f32(int64_t n, int k, const float* X, int64_t ldx, const 
   }
 }
 
-// v = w / nrm (nrm device scalar); zero when nrm is 0
-template <typename T>
-__global__ void scale_by_inv(int64_t n, const T* __restrict__ w, const double* __restrict__ nrm, T* __restrict__ v,
-                             const int32_t* __restrict__ gate) {
+// v = w / nrm and, with a, t = a (.) v (the next preconditioner input of
+// the weighted inner product)
+// (w and v may be the same vector)
+__global__ void scale_by_inv_w(int64_t n, const float* w, const double* __restrict__ nrm, float* v,
+                               const float* __restrict__ a, float* __restrict__ t, const int32_t* __restrict__ gate) {
   NFEM_GATE(gate);
   const double d = *nrm;
   const float inv = d > 0.0 ? float(1.0 / d) : 0.f;
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
-    v[i] = T(float(w[i]) * inv);
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const float x = w[i] * inv;
+    v[i] = x;
+    if (a) t[i] = a[i] * x;
+  }
 }
 
 // y = a (.) x  (elementwise)
@@ -1669,12 +1673,16 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
     // against 205 iterations and a longer solve at 64^3 x 6)
     NFEM_RC(spmv<float, float, float>(n, pc->a32->row_ptr, pc->a32->col_idx, (const float*)pc->a32->values, z, r2, v,
                                       1, s, nullptr, gate));
-    // a block per aggregate for long P^T lists, a warp per aggregate for short ones
-    if (L->pt_nnz >= int64_t(na) * 1024)
-      twolevel_restrict<<<unsigned(na), 256, 0, s>>>(na, L->pt_ptr, L->pt_row, L->pt_val, r2, rc, gate);
-    else
+    // a warp per aggregate for short P^T lists (under 64 entries on
+    // average), else a block per aggregate with about four entries a thread
+    const int64_t avg = L->pt_nnz / na;
+    if (avg < 64) {
       twolevel_restrict_warp<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->pt_ptr, L->pt_row,
                                                                                        L->pt_val, r2, rc, gate);
+    } else {
+      const int threads = int(std::min<int64_t>(256, ceil_div(avg, 4 * 32) * 32));
+      twolevel_restrict<<<unsigned(na), threads, 0, s>>>(na, L->pt_ptr, L->pt_row, L->pt_val, r2, rc, gate);
+    }
     if (L->n_blocks > 0)
       block_gemv<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->blk_ptr, L->blk_off, L->agg_blk,
                                                                            L->ac_inv, rc, ec, gate);
@@ -1864,7 +1872,8 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       }
       first_cycle = false;
       NFEM_RC(multidot<float>(ld, 1, w.V, ld, w.V, w.partial, w.scal + 2, 1, s, nullptr, w.counter));
-      scale_by_inv<float><<<gv, B, 0, s>>>(n, w.V, w.scal + 2, w.V, nullptr);
+      // V0 = V0 / ||V0||, and the first preconditioner input W^-1/2 V0
+      scale_by_inv_w<<<gv, B, 0, s>>>(n, w.V, w.scal + 2, w.V, weighted ? pc->winvsqrt : nullptr, w.t32, nullptr);
       init_cycle<<<1, 128, 0, s>>>(w.g, m, w.scal + 2, w.gate);
       NFEM_CHECK_LAUNCH();
       int j = 0;
@@ -1874,8 +1883,7 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
         const int32_t* done = w.gate;
         // w = W^1/2 A z_j: from the two-level apply when it carries A P
         bool w_done = false;
-        if (weighted) {
-          scale_vec<<<gv, B, 0, s>>>(n, pc->winvsqrt, vj, w.t32, done);
+        if (weighted) {  // w.t32 = W^-1/2 v_j, written with v_j
           NFEM_RC(precond_apply(pc, n, w.t32, zj, s, done, w.w, pc->wsqrt, &w_done));
         } else {
           NFEM_RC(precond_apply(pc, n, vj, zj, s, done, w.w, nullptr, &w_done));
@@ -1893,7 +1901,8 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
           multi_axpy_f32(ld, j + 1, w.V, ld, w.y, w.w, 1.0, s, done);
           NFEM_RC(multidot<float>(ld, 1, w.w, ld, w.w, w.partial, hcol + j + 1, 1, s, done, w.counter));
         }
-        scale_by_inv<float><<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * ld, done);
+        scale_by_inv_w<<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * ld,
+                                        weighted ? pc->winvsqrt : nullptr, w.t32, done);
         // h += the second pass's coefficients w.y, then the rotations
         givens_update<<<1, 32, 0, s>>>(w.H, ldh, w.y, w.cs, w.sn, w.g, j, w.hist, w.status, w.gate, inner_target);
         NFEM_CHECK_LAUNCH();
