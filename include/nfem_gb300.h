@@ -436,6 +436,8 @@ typedef struct {
                          every restart cycle (training data for the learned
                          preconditioner); NULL = none */
   int max_snapshots;
+  int no_graphs;      /* 0: from the second restart cycle on, the cycle's steps
+                         are replayed as one CUDA graph; 1: launched one by one */
 } nfem_solve_params;
 
 typedef struct {

@@ -63,7 +63,8 @@ class Precond(C.Structure):
 
 class SolveParams(C.Structure):
     _fields_ = [("rtol", C.c_double), ("inner_rtol", C.c_double), ("restart", C.c_int), ("max_inner", C.c_int),
-                ("max_outer", C.c_int), ("snapshots", C.c_void_p), ("max_snapshots", C.c_int)]
+                ("max_outer", C.c_int), ("snapshots", C.c_void_p), ("max_snapshots", C.c_int),
+                ("no_graphs", C.c_int)]
 
 
 class SolveInfo(C.Structure):

@@ -1469,7 +1469,8 @@ __global__ void block_apply(int64_t n_rows, const int32_t* __restrict__ inc_ptr,
 __global__ void givens_update(double* __restrict__ H, int ldh, const double* __restrict__ h2,
                               double* __restrict__ cs, double* __restrict__ sn, double* __restrict__ g, int j,
                               double* __restrict__ hist, int32_t* status, int32_t* __restrict__ gate,
-                              double target) {
+                              const double* __restrict__ target_ptr) {
+  const double target = *target_ptr;
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (gate && gate[0]) return;
   double* h = H + int64_t(j) * ldh;
@@ -1508,6 +1509,8 @@ __global__ void upper_solve(const double* __restrict__ H, int ldh, const double*
     y[i] = s / H[int64_t(i) * ldh + i];
   }
 }
+
+__global__ void set_scalar(double* __restrict__ p, double v) { *p = v; }
 
 __global__ void init_cycle(double* __restrict__ g, int m, const double* __restrict__ beta, int32_t* __restrict__ gate) {
   for (int i = threadIdx.x; i <= m; i += blockDim.x) g[i] = i == 0 ? *beta : 0.0;
@@ -1791,6 +1794,74 @@ static size_t solve_ws_bytes(int64_t n, int m, SolveWs* out, void* base) {
   return c.off + 256;
 }
 
+// The m Arnoldi steps of one FGMRES cycle (no host synchronisation, a fixed
+// launch sequence: the Givens kernel's gate ends a converged cycle's work).
+static int arnoldi_steps(const nfem_precond* pc, const nfem_csr* A32, int64_t n, int64_t ld, int m, int ldh,
+                         const SolveWs& w, bool weighted, int gv, cudaStream_t s) {
+  const int B = 256;
+  for (int j = 0; j < m; ++j) {
+    float* vj = w.V + int64_t(j) * ld;
+    float* zj = w.Z + int64_t(j) * ld;
+    const int32_t* done = w.gate;
+    // w = W^1/2 A z_j: from the two-level apply when it carries A P
+    bool w_done = false;
+    if (weighted) {  // w.t32 = W^-1/2 v_j, written with v_j
+      NFEM_RC(precond_apply(pc, n, w.t32, zj, s, done, w.w, pc->wsqrt, &w_done));
+    } else {
+      NFEM_RC(precond_apply(pc, n, vj, zj, s, done, w.w, nullptr, &w_done));
+    }
+    if (!w_done)
+      NFEM_RC(spmv<float, float, float>(n, A32->row_ptr, A32->col_idx, (const float*)A32->values, zj, w.w,
+                                        nullptr, 0, s, weighted ? pc->wsqrt : nullptr, done));
+    double* hcol = w.H + int64_t(j) * ldh;
+    // classical Gram-Schmidt, twice (the cancellation test of a selective
+    // second pass fires on nearly every Arnoldi step, so it saves nothing)
+    NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, hcol, 0, s, done, w.counter));
+    if (!cgs2_fused(ld, j + 1, w.V, ld, hcol, w.w, w.y, hcol + j + 1, w.partial, w.counter, s, done)) {
+      multi_axpy_f32(ld, j + 1, w.V, ld, hcol, w.w, 1.0, s, done);
+      NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, w.y, 0, s, done, w.counter));
+      multi_axpy_f32(ld, j + 1, w.V, ld, w.y, w.w, 1.0, s, done);
+      NFEM_RC(multidot<float>(ld, 1, w.w, ld, w.w, w.partial, hcol + j + 1, 1, s, done, w.counter));
+    }
+    scale_by_inv_w<<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * ld,
+                                    weighted ? pc->winvsqrt : nullptr, w.t32, done);
+    // h += the second pass's coefficients w.y, then the rotations
+    givens_update<<<1, 32, 0, s>>>(w.H, ldh, w.y, w.cs, w.sn, w.g, j, w.hist, w.status, w.gate, w.scal + 4);
+    NFEM_CHECK_LAUNCH();
+  }
+  return NFEM_OK;
+}
+
+// A CUDA graph of one cycle's steps, captured on a private stream.
+struct CycleGraph {
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cap = nullptr;
+  template <typename F>
+  int capture(F&& launch) {
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return NFEM_ERR_CUDA;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return NFEM_ERR_CUDA;
+    const int rc = launch(cap);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(cap, &graph);
+    if (rc != NFEM_OK || e != cudaSuccess || !graph) {
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return rc != NFEM_OK ? rc : NFEM_ERR_CUDA;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      exec = nullptr;
+      return NFEM_ERR_CUDA;
+    }
+    return NFEM_OK;
+  }
+  ~CycleGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (cap) cudaStreamDestroy(cap);
+  }
+};
+
 extern "C" int nfem_solve_workspace_bytes(int64_t n, int restart, size_t* bytes) {
   if (!bytes || n < 0 || restart < 1 || restart > kMaxRestart) return NFEM_ERR_INVALID_ARG;
   *bytes = solve_ws_bytes(n, restart, nullptr, nullptr);
@@ -1844,6 +1915,9 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
   double rel = hb[1] / nb;
   info->initial_relres = rel;
   std::vector<double> hist(m + 1);
+  const bool graphs = prm->no_graphs == 0;
+  CycleGraph cycle_graph;
+  bool first_solve_cycle = true;
   while (rel > prm->rtol && info->outer_iterations < prm->max_outer &&
          info->inner_iterations < prm->max_inner) {
     info->outer_iterations++;
@@ -1861,6 +1935,7 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
     NFEM_TRY_CUDA(cudaMemcpyAsync(&wr0, w.scal + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
     NFEM_TRY_CUDA(cudaStreamSynchronize(s));
     const double inner_target = prm->inner_rtol * wr0;
+    set_scalar<<<1, 1, 0, s>>>(w.scal + 4, inner_target);  // read by the Givens kernel
     double inner_res = wr0;
     bool inner_done = wr0 == 0.0;
     bool first_cycle = true;
@@ -1876,37 +1951,21 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       scale_by_inv_w<<<gv, B, 0, s>>>(n, w.V, w.scal + 2, w.V, weighted ? pc->winvsqrt : nullptr, w.t32, nullptr);
       init_cycle<<<1, 128, 0, s>>>(w.g, m, w.scal + 2, w.gate);
       NFEM_CHECK_LAUNCH();
-      int j = 0;
-      for (; j < m; ++j) {
-        float* vj = w.V + int64_t(j) * ld;
-        float* zj = w.Z + int64_t(j) * ld;
-        const int32_t* done = w.gate;
-        // w = W^1/2 A z_j: from the two-level apply when it carries A P
-        bool w_done = false;
-        if (weighted) {  // w.t32 = W^-1/2 v_j, written with v_j
-          NFEM_RC(precond_apply(pc, n, w.t32, zj, s, done, w.w, pc->wsqrt, &w_done));
-        } else {
-          NFEM_RC(precond_apply(pc, n, vj, zj, s, done, w.w, nullptr, &w_done));
-        }
-        if (!w_done)
-          NFEM_RC(spmv<float, float, float>(n, A32->row_ptr, A32->col_idx, (const float*)A32->values, zj, w.w,
-                                            nullptr, 0, s, weighted ? pc->wsqrt : nullptr, done));
-        double* hcol = w.H + int64_t(j) * ldh;
-        // classical Gram-Schmidt, twice (the cancellation test of a selective
-        // second pass fires on nearly every Arnoldi step, so it saves nothing)
-        NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, hcol, 0, s, done, w.counter));
-        if (!cgs2_fused(ld, j + 1, w.V, ld, hcol, w.w, w.y, hcol + j + 1, w.partial, w.counter, s, done)) {
-          multi_axpy_f32(ld, j + 1, w.V, ld, hcol, w.w, 1.0, s, done);
-          NFEM_RC(multidot<float>(ld, j + 1, w.V, ld, w.w, w.partial, w.y, 0, s, done, w.counter));
-          multi_axpy_f32(ld, j + 1, w.V, ld, w.y, w.w, 1.0, s, done);
-          NFEM_RC(multidot<float>(ld, 1, w.w, ld, w.w, w.partial, hcol + j + 1, 1, s, done, w.counter));
-        }
-        scale_by_inv_w<<<gv, B, 0, s>>>(n, w.w, hcol + j + 1, w.V + int64_t(j + 1) * ld,
-                                        weighted ? pc->winvsqrt : nullptr, w.t32, done);
-        // h += the second pass's coefficients w.y, then the rotations
-        givens_update<<<1, 32, 0, s>>>(w.H, ldh, w.y, w.cs, w.sn, w.g, j, w.hist, w.status, w.gate, inner_target);
-        NFEM_CHECK_LAUNCH();
+      if (graphs && cycle_graph.exec == nullptr && !first_solve_cycle) {
+        // second cycle onwards: the m steps as one CUDA graph, captured once
+        // on a private stream (the caller's may be the legacy stream) and
+        // replayed on `s` every cycle; the launch sequence is fixed (the
+        // gate ends a converged cycle's work on the device)
+        NFEM_RC(cycle_graph.capture([&](cudaStream_t cs_) {
+          return arnoldi_steps(pc, A32, n, ld, m, ldh, w, weighted, gv, cs_);
+        }));
       }
+      if (cycle_graph.exec) {
+        NFEM_TRY_CUDA(cudaGraphLaunch(cycle_graph.exec, s));
+      } else {
+        NFEM_RC(arnoldi_steps(pc, A32, n, ld, m, ldh, w, weighted, gv, s));
+      }
+      first_solve_cycle = false;
       // one synchronisation per cycle: residual estimates of every step
       NFEM_TRY_CUDA(cudaMemcpyAsync(hist.data(), w.hist, m * sizeof(double), cudaMemcpyDeviceToHost, s));
       NFEM_TRY_CUDA(cudaStreamSynchronize(s));

@@ -52,11 +52,14 @@ INNER_RTOL = {"two_level": 1e-2, "cell_block": 1e-3, "jacobi": 1e-2, "none": 1e-
 
 
 class KrylovSolver:
-    def __init__(self, A, pc="cell_block", A32_values=None, restart=30, weighted=True, two_level=None):
+    def __init__(self, A, pc="cell_block", A32_values=None, restart=30, weighted=True, two_level=None, graphs=True):
+        """graphs: replay each restart cycle after the first as one CUDA graph
+        (False launches every kernel from the host)."""
         if A.dtype != torch.float64:
             raise ValueError("A must be the FP64 matrix (the residual is measured in FP64)")
         self.A = A
         self.restart = int(restart)
+        self.graphs = bool(graphs)
         self.values32 = A32_values
         self.pc_kind = pc
         self.weighted = weighted
@@ -135,6 +138,7 @@ class KrylovSolver:
         if inner_rtol is None:
             inner_rtol = INNER_RTOL.get(self.pc_kind, 1e-4)
         prm = _lib.SolveParams(float(rtol), float(inner_rtol), self.restart, int(max_inner), int(max_outer))
+        prm.no_graphs = 0 if self.graphs else 1
         if snapshots is not None:
             prm.snapshots = _lib.ptr(snapshots).value
             prm.max_snapshots = int(snapshots.shape[0])
