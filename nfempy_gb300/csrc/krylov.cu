@@ -833,39 +833,48 @@ __global__ void __launch_bounds__(256) bgj_pad(const double* __restrict__ ac, in
 #ifndef NFEM_COARSE_DIAG_T
 #define NFEM_COARSE_DIAG_T float
 #endif
+// One 64 x 64 diagonal block inverted by 1024 threads, four entries of a
+// row in each thread's registers; per step the pivot row and column go
+// through double-buffered shared memory (one barrier a step).
 template <typename T>
-__global__ void __launch_bounds__(256) bgj_inv_diag(T* __restrict__ m, int N, int k0, T* __restrict__ dblk,
-                                                    int32_t* status) {
+__global__ void __launch_bounds__(1024) bgj_inv_diag(T* __restrict__ m, int N, int k0, T* __restrict__ dblk,
+                                                     int32_t* status) {
   using D = NFEM_COARSE_DIAG_T;
-  __shared__ D a[kGjB][kGjB + 1];
-  __shared__ D row[kGjB], col[kGjB];
-  for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
-    const int r = e / kGjB, c = e - r * kGjB;
-    a[r][c] = D(m[int64_t(k0 + r) * N + k0 + c]);
-  }
-  __syncthreads();
+  static_assert(kGjB == 64, "16 threads x 4 entries per row");
+  __shared__ D rowb[2][kGjB], colb[2][kGjB];
+  const int r = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
+  D a[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) a[q] = D(m[int64_t(k0 + r) * N + k0 + c0 + q]);
   for (int k = 0; k < kGjB; ++k) {
-    const D p = a[k][k];
+    const int b = k & 1;
+    if (r == k) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) rowb[b][c0 + q] = a[q];
+    }
+    if (k >= c0 && k < c0 + 4) {
+      D v = a[0];
+#pragma unroll
+      for (int q = 1; q < 4; ++q) v = (k - c0 == q) ? a[q] : v;
+      colb[b][r] = v;
+    }
+    __syncthreads();
+    const D p = rowb[b][k];
     const D ip = p != D(0) ? D(1) / p : D(0);
     if (threadIdx.x == 0 && !(fabs(p) > 0.0)) set_status(status, NFEM_ERR_BREAKDOWN);
-    if (threadIdx.x < kGjB) {
-      row[threadIdx.x] = a[k][threadIdx.x] * ip;
-      col[threadIdx.x] = a[threadIdx.x][k];
+    const D cr = colb[b][r];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = c0 + q;
+      const D rc = rowb[b][c] * ip;
+      if (r == k && c == k) a[q] = ip;
+      else if (r == k) a[q] = rc;
+      else if (c == k) a[q] = -cr * ip;
+      else a[q] -= cr * rc;
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
-      const int r = e / kGjB, c = e - r * kGjB;
-      if (r == k && c == k) a[r][c] = ip;
-      else if (r == k) a[r][c] = row[c];
-      else if (c == k) a[r][c] = -col[r] * ip;
-      else a[r][c] -= col[r] * row[c];
-    }
-    __syncthreads();
   }
-  for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x) {
-    const int r = e / kGjB, c = e - r * kGjB;
-    dblk[e] = T(a[r][c]);
-  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) dblk[r * kGjB + c0 + q] = T(a[q]);
 }
 
 // 64 x 64 product of two shared-memory tiles, 4 x 4 outputs per thread
@@ -945,6 +954,55 @@ __global__ void __launch_bounds__(256) bgj_trailing(T* __restrict__ m, int N, in
     }
 }
 
+// A_IJ -= A_IK A_KJ on 128 x 128 output tiles (FP32): 8 x 8 outputs per
+// thread from K-major shared tiles (16-byte reads), rows and columns of the
+// K block left to the panel kernels, edges clipped to N.
+constexpr int kTr = 128;
+constexpr int kTrLd = kTr + 4;  // padded row of the K-major tiles (floats)
+
+__global__ void __launch_bounds__(256) bgj_trailing128(float* __restrict__ m, int N, int k0) {
+  extern __shared__ __align__(16) unsigned char tr_smem[];
+  float(*xs)[kTrLd] = reinterpret_cast<float(*)[kTrLd]>(tr_smem);  // xs[k][i] = A[i0 + i][k0 + k]
+  float(*ys)[kTrLd] = xs + kGjB;                                    // ys[k][j] = A[k0 + k][j0 + j]
+  const int i0 = blockIdx.y * kTr, j0 = blockIdx.x * kTr;
+  for (int e = threadIdx.x; e < kGjB * kTr; e += blockDim.x) {
+    const int i = e / kGjB, k = e - i * kGjB;
+    xs[k][i] = i0 + i < N ? m[int64_t(i0 + i) * N + k0 + k] : 0.f;
+    const int kk = e / kTr, j = e - kk * kTr;
+    ys[kk][j] = j0 + j < N ? m[int64_t(k0 + kk) * N + j0 + j] : 0.f;
+  }
+  __syncthreads();
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  float acc[8][8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < kGjB; ++k) {
+    const float4 x0 = *reinterpret_cast<const float4*>(&xs[k][ty * 8]);
+    const float4 x1 = *reinterpret_cast<const float4*>(&xs[k][ty * 8 + 4]);
+    const float4 y0 = *reinterpret_cast<const float4*>(&ys[k][tx * 8]);
+    const float4 y1 = *reinterpret_cast<const float4*>(&ys[k][tx * 8 + 4]);
+    const float xa[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+    const float yb[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(xa[a], yb[b], acc[a][b]);
+  }
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const int r = i0 + ty * 8 + a;
+    if (r >= N || (r >= k0 && r < k0 + kGjB)) continue;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int c = j0 + tx * 8 + b;
+      if (c < N && (c < k0 || c >= k0 + kGjB)) m[int64_t(r) * N + c] -= acc[a][b];
+    }
+  }
+}
+
 template <typename T>
 __global__ void bgj_put_diag(T* __restrict__ m, int N, int k0, const T* __restrict__ dblk) {
   for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x)
@@ -967,18 +1025,26 @@ static int blocked_inverse(const double* ac, int n, T* m, T* dblk, float* inv, i
   const int N = int(ceil_div(n, kGjB) * kGjB);
   const int nt = N / kGjB;
   const size_t smem = 2 * kGjB * (kGjB + 1) * sizeof(T);
-  static const bool attr = [smem] {
+  const size_t smem128 = 2 * kGjB * kTrLd * sizeof(float);
+  static const bool attr = [smem, smem128] {
     return cudaFuncSetAttribute(bgj_trailing<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) ==
                cudaSuccess &&
-           cudaFuncSetAttribute(bgj_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) == cudaSuccess;
+           cudaFuncSetAttribute(bgj_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) ==
+               cudaSuccess &&
+           cudaFuncSetAttribute(bgj_trailing128, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem128)) ==
+               cudaSuccess;
   }();
   if (!attr) return NFEM_ERR_CUDA;
+  const int nt128 = int(ceil_div(N, kTr));
   bgj_pad<T><<<grid_for(int64_t(N) * N, 256), 256, 0, s>>>(ac, n, N, m);
   for (int kb = 0; kb < nt; ++kb) {
     const int k0 = kb * kGjB;
-    bgj_inv_diag<T><<<1, 256, 0, s>>>(m, N, k0, dblk, status);
+    bgj_inv_diag<T><<<1, 1024, 0, s>>>(m, N, k0, dblk, status);
     bgj_panel<T><<<nt, 256, smem, s>>>(m, N, k0, dblk, 0);
-    bgj_trailing<T><<<dim3(nt, nt), 256, smem, s>>>(m, N, k0);
+    if constexpr (sizeof(T) == 4)
+      bgj_trailing128<<<dim3(nt128, nt128), 256, smem128, s>>>(m, N, k0);
+    else
+      bgj_trailing<T><<<dim3(nt, nt), 256, smem, s>>>(m, N, k0);
     bgj_panel<T><<<nt, 256, smem, s>>>(m, N, k0, dblk, 1);
     bgj_put_diag<T><<<1, 256, 0, s>>>(m, N, k0, dblk);
   }

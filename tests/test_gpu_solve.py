@@ -224,3 +224,28 @@ def test_two_level_ap_product_and_fused_solve(cuda_lib):
     ptr = tl.ap_ptr.cpu().numpy()
     assert all(np.all(np.diff(cols[ptr[i]:ptr[i + 1]]) > 0) for i in range(0, n, 97))
     assert abs(out[True][3].inner_iterations - out[False][3].inner_iterations) <= 3
+
+
+@pytest.mark.parametrize("n_c", [4, 7])
+def test_dense_coarse_inverse(cuda_lib, n_c):
+    """The stored FP32 inverse of the Galerkin coarse matrix: 64 aggregates
+    (one tile) and 343 (tiles clipped at the padded edge, 128-wide trailing
+    tiles straddling the pivot block) both give ||X A_c - I|| within FP32
+    round-off times the conditioning."""
+    from nfempy_gb300 import meshes
+    from nfempy_gb300.solvers import TwoLevelCoarse
+    m = mesh_gen.cube(14)
+    cent = m["points"][m["blocks"][-1][1]].mean(axis=1)
+    kappa = np.exp(meshes.grf_log_field(cent, 0.1, 1.0, 3))
+    sp, A, res = assembled(m, kappa, 1.0)
+    tl = TwoLevelCoarse(A, n_c)
+    ksp = KrylovSolver(A, pc="two_level", restart=15, two_level=tl)
+    ksp.setup()
+    torch.cuda.synchronize()
+    Ac = tl.ac.cpu().numpy()
+    X = tl.ac_inv.cpu().numpy().astype(np.float64)
+    na = tl.n_agg
+    assert Ac.shape == (na, na) and np.allclose(Ac, Ac.T, rtol=1e-10, atol=1e-12 * np.abs(Ac).max())
+    cond = np.linalg.cond(Ac)
+    err = np.abs(X @ Ac - np.eye(na)).max()
+    assert err <= max(1e-4, 64 * cond * 6e-8), (err, cond)
