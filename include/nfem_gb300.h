@@ -233,7 +233,16 @@ int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t 
                               const int32_t* row_pairs, const uint32_t* pair_codes,
                               const int32_t* row_ptr, const int32_t* chunk_rows,
                               void* values, void* rhs, int accumulate,
+                              void* workspace, size_t workspace_bytes,
                               int32_t* dev_status, void* stream);
+/* Record workspace of the two-pass row-owner assembly: with workspace !=
+ * NULL (and chunk_rows == NULL) a cell pass first evaluates, once per cell,
+ * the metric terms all rows of the cell's element matrix are made of
+ * (12 words per tetrahedron, 8 per triangle, of the value type) and the row
+ * pass reads them in place of the vertices; the values agree with the one
+ * pass to rounding (the same expressions, fused alike or not).  NULL: one pass that evaluates every (row, cell) incidence from the
+ * vertices.  The workspace is 16-byte aligned, of at least this size. */
+int nfem_darcy_workspace_bytes(int dim, int value_type, int64_t n_cells, size_t* bytes);
 
 /* Replaces LaplaceDualWeakFormBCDirichlet.evaluate_form
  * (src/weak_forms/laplace_dual_weak_form.py:90-154) with its scatter: adds

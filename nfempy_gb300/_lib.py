@@ -97,7 +97,8 @@ _SIGS = {
     "nfem_points_split": ([_P, _I64, _P, _P], _I),
     "nfem_pattern_pairs": ([_P, _P, _P, _I64, _P, _P, _P, _P], _I),
     "nfem_darcy_rt1p0_assemble": ([_I, _I, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P, _P, _I,
-                                   _P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P], _I),
+                                   _P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _SZ, _P, _P], _I),
+    "nfem_darcy_workspace_bytes": ([_I, _I, _I64, C.POINTER(_SZ)], _I),
     "nfem_pattern_darcy_chunks": ([_P, _I64, _I, _I64, _I64, _P, _P, _P], _I),
     "nfem_copy_bytes": ([_P, _P, _SZ, _P], _I),
     "nfem_spmv": ([_I, _I64, _P, _P, _P, _P, _P, _P], _I),

@@ -70,6 +70,7 @@ struct DarcyParams {
   int accumulate;
   int n_qp;
   double qw[32];
+  void* rec;  // per-cell records of the two-pass path (NULL: single pass)
 };
 
 template <typename T, int DIM>
@@ -331,6 +332,173 @@ __device__ __forceinline__ T cell_matrix(const DarcyParams& p, const Incidence<T
   return T(0);
 }
 
+// ------------------------------------------------------------------ two-pass form
+// Pass 1, one thread per cell (coalesced): the metric terms every row of the
+// cell's element matrix is made of, evaluated once per cell instead of once
+// per (row, cell) incidence, with the same operations and rounding as
+// element_row:
+//   3-D: [tr G + sum G, R1, R2, R3 | G11, G12, G13, scale | G22, G23, G33, r_p]
+//   2-D: [tr G + sum G, R1, R2, G11 | G12, G22, scale, r_p]
+// (R the row sums of G, r_p the pressure row's residual entry).  The
+// constant factors are applied in the row pass, in element_row's
+// expressions, so that both forms round (and contract) alike.
+// Pass 2 is the row-owner kernel reading these records in place of the
+// vertices: 48 (3-D) or 32 (2-D) bytes of FP32 per incidence.
+template <int DIM>
+struct RecWords;
+template <>
+struct RecWords<3> {
+  static constexpr int n = 12;
+};
+template <>
+struct RecWords<2> {
+  static constexpr int n = 8;
+};
+
+template <typename T, int DIM, int SRC>
+__global__ void __launch_bounds__(256) darcy_records_kernel(const DarcyParams p) {
+  constexpr int NW = RecWords<DIM>::n;
+  using C = DarcyConst<T, DIM>;
+  T* rec = static_cast<T*>(p.rec);
+  const T u = edge_unit<T>(p);
+  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < p.n_cells;
+       c += int64_t(gridDim.x) * blockDim.x) {
+    Incidence<T, DIM> x;
+    load_incidence<T, DIM, SRC>(p, int32_t(c), true, x);
+    T G[DIM][DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) G[i][j] = x.J[i][0] * x.J[j][0] + x.J[i][1] * x.J[j][1] + x.J[i][2] * x.J[j][2];
+    const T det = abs_det<T, DIM>(x.J, G);
+    if (!(det > T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+    const T det_true = DIM == 3 ? det * (u * u * u) : det * (u * u);
+    T R[DIM];
+    T trG = T(0), sumG = T(0);
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      R[i] = T(0);
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) R[i] += G[i][j];
+      trG += G[i][i];
+      sumG += R[i];
+    }
+    T w[NW];
+    w[0] = trG + sumG;
+    const T scale = T(C::kappa2) * recip(x.kap * (DIM == 3 ? det * u : det));
+    T rp = T(0);
+    if constexpr (SRC == NFEM_COEF_CELL) rp = -det_true * T(C::area) * x.src;
+    if constexpr (SRC == NFEM_COEF_QPOINT) rp = -det_true * x.src;
+    if constexpr (DIM == 3) {
+      w[1] = R[0];
+      w[2] = R[1];
+      w[3] = R[2];
+      w[4] = G[0][0];
+      w[5] = G[0][1];
+      w[6] = G[0][2];
+      w[7] = scale;
+      w[8] = G[1][1];
+      w[9] = G[1][2];
+      w[10] = G[2][2];
+      w[11] = rp;
+    } else {
+      w[1] = R[0];
+      w[2] = R[1];
+      w[3] = G[0][0];
+      w[4] = G[0][1];
+      w[5] = G[1][1];
+      w[6] = scale;
+      w[7] = rp;
+    }
+    // 16-byte stores: a record never straddles a 32-byte sector per store
+    if constexpr (sizeof(T) == 4) {
+      float4* out = reinterpret_cast<float4*>(rec + c * NW);
+#pragma unroll
+      for (int k = 0; k < NW / 4; ++k) out[k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+    } else {
+      double2* out = reinterpret_cast<double2*>(rec + c * NW);
+#pragma unroll
+      for (int k = 0; k < NW / 2; ++k) out[k] = make_double2(w[2 * k], w[2 * k + 1]);
+    }
+  }
+}
+
+// Record words of cell c (vector loads: the record is 16-byte aligned).
+template <typename T, int DIM>
+__device__ __forceinline__ void load_record(const T* __restrict__ rec, int32_t c, T (&w)[RecWords<DIM>::n]) {
+  constexpr int NW = RecWords<DIM>::n;
+  if constexpr (sizeof(T) == 4) {
+    const float4* q = reinterpret_cast<const float4*>(rec + int64_t(c) * NW);
+#pragma unroll
+    for (int k = 0; k < NW / 4; ++k) {
+      const float4 v = __ldg(q + k);
+      w[4 * k] = v.x;
+      w[4 * k + 1] = v.y;
+      w[4 * k + 2] = v.z;
+      w[4 * k + 3] = v.w;
+    }
+  } else {
+    const double2* q = reinterpret_cast<const double2*>(rec + int64_t(c) * NW);
+#pragma unroll
+    for (int k = 0; k < NW / 2; ++k) {
+      const double2 v = __ldg(q + k);
+      w[2 * k] = v.x;
+      w[2 * k + 1] = v.y;
+    }
+  }
+}
+
+// Row a of cell c's element matrix from its record (element_row's values).
+template <typename T, int DIM>
+__device__ __forceinline__ void record_row(const T (&w)[RecWords<DIM>::n], uint32_t m, int a, T (&vals)[DIM + 2],
+                                           T& rhs_val) {
+  constexpr int NF = DIM + 1;
+  using C = DarcyConst<T, DIM>;
+  T sg[NF];
+#pragma unroll
+  for (int i = 0; i < NF; ++i) sg[i] = ((m >> i) & 1u) ? -C::sigma(i) : C::sigma(i);
+  if (a < NF) {
+    T R[DIM], Ga[DIM];
+    T scale;
+    if constexpr (DIM == 3) {
+      R[0] = w[1]; R[1] = w[2]; R[2] = w[3];
+      scale = w[7];
+      // row a-1 of G: a = 1 -> (G11, G12, G13), 2 -> (G12, G22, G23), 3 -> (G13, G23, G33)
+      Ga[0] = a == 1 ? w[4] : (a == 2 ? w[5] : w[6]);
+      Ga[1] = a == 1 ? w[5] : (a == 2 ? w[8] : w[9]);
+      Ga[2] = a == 1 ? w[6] : (a == 2 ? w[9] : w[10]);
+      if (a == 0) Ga[0] = Ga[1] = Ga[2] = T(0);  // as element_row
+    } else {
+      R[0] = w[1]; R[1] = w[2];
+      scale = w[6];
+      Ga[0] = a == 1 ? w[3] : w[4];
+      Ga[1] = a == 1 ? w[4] : w[5];
+      if (a == 0) Ga[0] = Ga[1] = T(0);
+    }
+    // element_row's expressions from here on
+    const T tgs = w[0] * T(C::f2);
+    T Ra = T(0);
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) Ra = (a == i + 1) ? R[i] : Ra;
+    T sga = sg[0];
+#pragma unroll
+    for (int i = 1; i < NF; ++i) sga = (a == i) ? sg[i] : sga;
+    const T gma = Ra * T(C::f1);
+#pragma unroll
+    for (int b = 0; b < NF; ++b) {
+      const T gmb = b > 0 ? R[b - 1] * T(C::f1) : T(0);
+      const T gv = b > 0 ? Ga[b - 1] * T(C::area) : T(0);
+      vals[b] = scale * sga * sg[b] * (tgs - gma - gmb + gv);
+    }
+    vals[NF] = -sga;
+  } else {
+#pragma unroll
+    for (int b = 0; b < NF; ++b) vals[b] = sg[b];
+    vals[NF] = T(0);
+    rhs_val += w[RecWords<DIM>::n - 1];
+  }
+}
+
 struct RowHead {
   int2 pr;
   uint2 cd;
@@ -364,7 +532,7 @@ __device__ __forceinline__ int row_len_from_codes(const RowHead& h) {
   return len;
 }
 
-template <typename T, int DIM, int SRC>
+template <typename T, int DIM, int SRC, bool REC = false>
 __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_MIN_BLOCKS : 1)
     darcy_rows_kernel(const DarcyParams p) {
   constexpr int NLOC = DIM + 2;
@@ -431,10 +599,16 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_
 #pragma unroll kDarcyIncUnroll
     for (int t = 0; t < 2; ++t) {
       if (on[t]) {
-        Incidence<T, DIM> x;
-        load_incidence<T, DIM, SRC>(p, c[t], geo[t], x);
         T v[NLOC];
-        element_row<T, DIM, SRC>(p, x, a[t], geo[t], v, rhs_val);
+        if constexpr (REC) {
+          T w[RecWords<DIM>::n];
+          load_record<T, DIM>(static_cast<const T*>(p.rec), c[t], w);
+          record_row<T, DIM>(w, __ldg(p.sign + c[t]), a[t], v, rhs_val);
+        } else {
+          Incidence<T, DIM> x;
+          load_incidence<T, DIM, SRC>(p, c[t], geo[t], x);
+          element_row<T, DIM, SRC>(p, x, a[t], geo[t], v, rhs_val);
+        }
         const uint32_t cd = code[t];
         const int at = a[t];
         if (direct) {
@@ -686,21 +860,31 @@ __global__ void __launch_bounds__(kChunkThreads) darcy_cells_kernel(const DarcyP
 
 // One resident wave: blocks per SM from the occupancy calculator (queried
 // once per kernel instance), times the SM count, capped by the work.
-template <typename T, int DIM, int SRC>
-static int launch_darcy_src(const DarcyParams& p, cudaStream_t stream) {
+template <typename T, int DIM, int SRC, bool REC>
+static int launch_darcy_rows(const DarcyParams& p, cudaStream_t stream) {
   const int block = 32 * kDarcyWarps;
   static const int per_sm = [] {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, darcy_rows_kernel<T, DIM, SRC>, 32 * kDarcyWarps, 0) !=
-            cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, darcy_rows_kernel<T, DIM, SRC, REC>, 32 * kDarcyWarps,
+                                                      0) != cudaSuccess ||
         n < 1)
       n = 4;
     return n;
   }();
   const int grid = grid_for(ceil_div(p.n_rows, 32 * kDarcyWarps), 1, per_sm);
-  darcy_rows_kernel<T, DIM, SRC><<<grid, block, 0, stream>>>(p);
+  darcy_rows_kernel<T, DIM, SRC, REC><<<grid, block, 0, stream>>>(p);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
+}
+
+// Single pass (the row kernel evaluates every incidence from the vertices)
+// or, with the record workspace, the cell pass followed by the row pass.
+template <typename T, int DIM, int SRC>
+static int launch_darcy_src(const DarcyParams& p, cudaStream_t stream) {
+  if (!p.rec) return launch_darcy_rows<T, DIM, SRC, false>(p, stream);
+  if (p.n_cells > 0) darcy_records_kernel<T, DIM, SRC><<<grid_for(p.n_cells, 256), 256, 0, stream>>>(p);
+  NFEM_CHECK_LAUNCH();
+  return launch_darcy_rows<T, DIM, NFEM_COEF_NONE, true>(p, stream);
 }
 
 template <typename T, int DIM, int SRC>
@@ -747,6 +931,13 @@ static int launch_darcy(const DarcyParams& p, int source_mode, cudaStream_t stre
 
 using namespace nfem;
 
+extern "C" int nfem_darcy_workspace_bytes(int dim, int value_type, int64_t n_cells, size_t* bytes) {
+  if (!bytes || (dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_cells < 0)
+    return NFEM_ERR_INVALID_ARG;
+  *bytes = size_t(n_cells) * (dim == 3 ? 12 : 8) * (value_type == NFEM_F64 ? 8 : 4);
+  return NFEM_OK;
+}
+
 extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t n_rows,
                                          const double* points, const float* points_split,
                                          const int32_t* cell_vertices, const int32_t* flux_dofs, int64_t p_base,
@@ -754,7 +945,8 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
                                          int source_mode, const double* qweights, int n_qp,
                                          const int32_t* row_pairs, const uint32_t* pair_codes,
                                          const int32_t* row_ptr, const int32_t* chunk_rows, void* values,
-                                         void* rhs, int accumulate, int32_t* dev_status, void* stream_) {
+                                         void* rhs, int accumulate, void* workspace, size_t workspace_bytes,
+                                         int32_t* dev_status, void* stream_) {
   (void)flux_dofs;
   cudaStream_t stream = (cudaStream_t)stream_;
   if ((dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_rows < 0)
@@ -791,6 +983,14 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   p.accumulate = accumulate != 0;
   p.n_qp = source_mode == NFEM_COEF_QPOINT ? n_qp : 0;
   for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
+  p.rec = nullptr;
+  if (workspace && !chunk_rows) {
+    size_t need = 0;
+    nfem_darcy_workspace_bytes(dim, value_type, n_cells, &need);
+    if (workspace_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 15) || n_cells < 0)
+      return NFEM_ERR_WORKSPACE;
+    p.rec = workspace;
+  }
   if (value_type == NFEM_F64)
     return dim == 3 ? launch_darcy<double, 3>(p, source_mode, stream) : launch_darcy<double, 2>(p, source_mode, stream);
   return dim == 3 ? launch_darcy<float, 3>(p, source_mode, stream) : launch_darcy<float, 2>(p, source_mode, stream);

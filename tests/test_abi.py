@@ -107,9 +107,13 @@ def test_new_workspace_queries_and_argument_checks(lib_path):
     rc = lib.nfem_pattern_darcy_chunks(dummy, 10, 5, 4, 7, dummy, None, None)  # p_base + n_cells != n_rows
     assert _lib.STATUS_NAMES[rc] == "NFEM_ERR_UNSUPPORTED"
     # Darcy assembly: bad dimension, value type, and a chunk table that does not fit the rows
-    args = [0] * 24
+    args = [0] * 26
     assert lib.nfem_darcy_rt1p0_assemble(4, 1, *args[2:]) == 1
     assert lib.nfem_darcy_rt1p0_assemble(3, 9, *args[2:]) == 1
+    # record workspace of the two-pass form: 12 words per tetrahedron, 8 per triangle
+    assert lib.nfem_darcy_workspace_bytes(3, _lib.NFEM_F32, 1000, ctypes.byref(b)) == 0 and b.value == 48000
+    assert lib.nfem_darcy_workspace_bytes(2, _lib.NFEM_F64, 1000, ctypes.byref(b)) == 0 and b.value == 64000
+    assert lib.nfem_darcy_workspace_bytes(4, _lib.NFEM_F32, 10, ctypes.byref(b)) == 1
 
 
 def test_two_level_ap_queries_and_argument_checks(lib_path):

@@ -22,12 +22,13 @@ def f2d(x, y, z):
     return np.array([2 * PI ** 2 * np.sin(PI * x) * np.sin(PI * y)])
 
 
-def assemble_gpu(m, kappa, rhs, dtype, use_chunks=False):
+def assemble_gpu(m, kappa, rhs, dtype, use_chunks=False, use_records=None):
     sp = product_space(m, DARCY)
     A = nf.CSRMatrix(sp, dtype=dtype)
     res = torch.empty(A.n_rows, dtype=dtype, device="cuda")
     wf = nf.LaplaceDualWeakForm(sp)
     wf.use_chunks = use_chunks
+    wf.use_records = use_records
     wf.functions = {"kappa": kappa, "rhs": rhs}
     asm = nf.SequentialAssembler(sp, A, res)
     asm.form_to_input_list = {"darcy": ["form", range(sp.n_cells), wf, None]}
@@ -43,17 +44,17 @@ def row_scaled_err(Ag, Ao):
     return (abs(d).max(axis=1).toarray().ravel() / scale).max()
 
 
-@pytest.mark.parametrize("use_chunks", [True, False], ids=["cell_chunks", "row_owner"])
+@pytest.mark.parametrize("kernel", ["cell_chunks", "row_records", "row_one_pass"])
 @pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
 @pytest.mark.parametrize("gen,n", [("square", 4), ("square", 32), ("cube", 2), ("cube", 6), ("cube", 12)])
-def test_darcy_matrix_matches_oracle(cuda_lib, dtype, tol, gen, n, use_chunks):
-    """Both Darcy kernels against the oracle; cube(12) has 10,368 cells, so the
+def test_darcy_matrix_matches_oracle(cuda_lib, dtype, tol, gen, n, kernel):
+    """The Darcy kernels against the oracle; cube(12) has 10,368 cells, so the
     cell-chunk kernel runs several chunks and meets neighbours outside them."""
     m = getattr(mesh_gen, gen)(n)
     T = m["blocks"][-1][1].shape[0]
     kappa = np.exp(np.sin(np.arange(T) * 0.37))
     f_cell = np.cos(np.arange(T) * 0.11)
-    sp, A, res = assemble_gpu(m, kappa, f_cell, dtype, use_chunks)
+    sp, A, res = assemble_gpu(m, kappa, f_cell, dtype, kernel == "cell_chunks", kernel == "row_records")
     assert (A.chunk_rows is not None) == (sp.dof_shift == 0)
     Ao, ro, cd, nd, topo = darcy_oracle(m, kappa, f_cell=f_cell)
     Ag = A.to_scipy()
@@ -242,3 +243,22 @@ def test_darcy_chunk_table_and_kernels_agree(cuda_lib):
     # entries that cancel to round-off are compared at the scale of their row
     assert row_scaled_err(A_chunks, A.to_scipy()) <= 2e-6
     assert ((r_chunks - res).abs().max() / res.abs().max()).item() <= 2e-6
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("gen,n,qpoint", [("square", 24, False), ("cube", 10, False), ("cube", 6, True)])
+def test_darcy_records_equal_one_pass(cuda_lib, dtype, gen, n, qpoint):
+    """The two-pass form (cell records, then rows) writes the single pass's
+    values and residual up to the last bits: the records hold the same
+    intermediate quantities and the row pass applies element_row's
+    expressions (the compiler may still fuse a multiply-add differently)."""
+    m = getattr(mesh_gen, gen)(n)
+    T = m["blocks"][-1][1].shape[0]
+    rng = np.random.default_rng(4)
+    kappa = np.exp(rng.normal(0.0, 2.0, T))
+    rhs = f2d if qpoint else rng.normal(0.0, 1.0, T)
+    sp, A1, r1 = assemble_gpu(m, kappa, rhs, dtype, use_records=False)
+    _, A2, r2 = assemble_gpu(m, kappa, rhs, dtype, use_records=True)
+    tol = 1e-6 if dtype == torch.float32 else 1e-14
+    assert row_scaled_err(A1.to_scipy(), A2.to_scipy()) <= tol
+    assert ((r1 - r2).abs().max() / r1.abs().max()).item() <= tol
