@@ -457,7 +457,8 @@ def batch2d_bench(args):
     peak, kind = measured_peaks()
     ach = alg / (ms * 1e-3) / 1e9
     out = {"metric": "DoF/s assembled", "value": sp.n_dof / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
-           "problems": len(sides), "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz, "kernel": "darcy_rows_kernel",
+           "problems": len(sides), "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz,
+           "kernel": "darcy_records_kernel + darcy_rows_kernel",
            "graph_replay_ms_per_step": graph_ms,
            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                         "algorithmic_bytes": alg, "peak_source": kind}}
@@ -504,6 +505,7 @@ def run_ours(args):
     A = nf.CSRMatrix(sp, dtype=dtype)
     wf = nf.LaplaceDualWeakForm(sp)
     wf.use_chunks = args.kernel == "chunks"
+    wf.use_records = args.kernel == "records"
     wf.functions = {"kappa": kappa, "rhs": f}
     coefs = wf.coefficients(dtype)
     res = torch.empty(A.n_rows, dtype=dtype, device="cuda")
@@ -634,7 +636,10 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     alg = algorithmic_bytes(T, V, A.nnz, n_dof, vbytes)
     achieved = alg / (ms * 1e-3) / 1e9
-    kname = "darcy_cells" if args.kernel == "chunks" else "darcy_rows"
+    kname = {"chunks": "darcy_cells", "rows": "darcy_rows", "records": "darcy_records_rows"}[args.kernel]
+    kernels = {"chunks": "darcy_cells_kernel", "rows": "darcy_rows_kernel",
+               "records": "darcy_records_kernel + darcy_rows_kernel (two passes)"}[args.kernel]
+    launches_per_step = 2 if args.kernel == "records" else 1
     prof_name = f"{kname}_{args.precision}_cube64.txt"
     traffic = profiled_traffic(prof_name)
     cpu = None
@@ -651,7 +656,7 @@ def run_ours(args):
         "config": {"workload": f"darcy3d_rt1p0_cube{N_SIDE}x6", "n_cells": T, "n_points": V, "n_dof": n_dof,
                    "nnz": A.nnz, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "flushed before every timed step (256 MB write, outside the step events)",
-                   "bracket_ms_incl_flush": bracket_ms, "kernel": f"{kname}_kernel"},
+                   "bracket_ms_incl_flush": bracket_ms, "kernel": kernels},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes": alg, "peak_source": peak_kind},
@@ -665,7 +670,7 @@ def run_ours(args):
                            "mode": "points, kappa, f up, split, assemble, values + residual down; one stream"}},
         "solve": solve,
         "workloads": workloads,
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * launches_per_step,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
@@ -695,8 +700,8 @@ def main():
                     help="aggregate side in squares of the batched 2-D two-level solve")
     ap.add_argument("--solver", choices=["both", "plain", "two_level"], default="both",
                     help="with --only solve: which preconditioners to run")
-    ap.add_argument("--kernel", choices=["rows", "chunks"], default="rows",
-                    help="Darcy assembly kernel: row owner (default) or cell chunks")
+    ap.add_argument("--kernel", choices=["records", "rows", "chunks"], default="records",
+                    help="Darcy assembly: cell records then rows (default), rows alone, or cell chunks")
     ap.add_argument("--only", choices=["elasticity", "cosserat", "batch2d", "solve"], default=None,
                     help="time one secondary assembly workload alone and print its record (profiling runs)")
     args = ap.parse_args()

@@ -238,7 +238,9 @@ int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t 
 /* Record workspace of the two-pass row-owner assembly: with workspace !=
  * NULL (and chunk_rows == NULL) a cell pass first evaluates, once per cell,
  * the metric terms all rows of the cell's element matrix are made of
- * (12 words per tetrahedron, 8 per triangle, of the value type) and the row
+ * (G = J^T J, the scale and the pressure row's residual entry: 8 FP32 words
+ * per cell; FP64 adds the row sums of G: 12 words per tetrahedron, 8 per
+ * triangle) and the row
  * pass reads them in place of the vertices; the values agree with the one
  * pass to rounding (the same expressions, fused alike or not).  NULL: one pass that evaluates every (row, cell) incidence from the
  * vertices.  The workspace is 16-byte aligned, of at least this size. */

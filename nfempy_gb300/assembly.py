@@ -215,15 +215,14 @@ class LaplaceDualWeakForm(WeakForm):
     tets); both write the same values up to rounding.
     use_records: the row-owner kernel reads per-cell metric records from a
     first cell pass (True) instead of evaluating each (row, cell) incidence
-    from the vertices (False); the values agree to rounding.  None (default)
-    picks per precision from measurements at 64^3 x 6 tets: FP64 two-pass
-    0.54 ms against 1.12 ms (the FP64 geometry is evaluated once per cell
-    instead of once per incidence), FP32 one pass 0.100 ms against 0.110 ms
-    (the FP32 geometry is cheap next to the records' extra traffic).
+    from the vertices (False); the values agree to rounding.  Measured at
+    64^3 x 6 tets: FP32 0.096 ms against 0.101 ms, FP64 0.50 ms against
+    1.12 ms (the geometry is evaluated once per cell instead of once per
+    incidence).
     """
 
     use_chunks = False
-    use_records = None
+    use_records = True
 
     def _check_space(self):
         sp = self.space
@@ -291,8 +290,7 @@ class LaplaceDualWeakForm(WeakForm):
         pts, wts = sp.quadrature[sp.dim]
         qw = (_lib.C.c_double * len(wts))(*wts.tolist())
         ws = None
-        records = self.use_records if self.use_records is not None else dtype == torch.float64
-        if records and not self.use_chunks:
+        if self.use_records and not self.use_chunks:
             key = ("records", dtype)
             if key not in self._cache:
                 nb = _lib.C.c_size_t(0)

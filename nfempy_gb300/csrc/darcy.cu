@@ -333,46 +333,51 @@ __device__ __forceinline__ T cell_matrix(const DarcyParams& p, const Incidence<T
 }
 
 // ------------------------------------------------------------------ two-pass form
-// Pass 1, one thread per cell (coalesced): the metric terms every row of the
-// cell's element matrix is made of, evaluated once per cell instead of once
-// per (row, cell) incidence, with the same operations and rounding as
-// element_row:
-//   3-D: [tr G + sum G, R1, R2, R3 | G11, G12, G13, scale | G22, G23, G33, r_p]
-//   2-D: [tr G + sum G, R1, R2, G11 | G12, G22, scale, r_p]
-// (R the row sums of G, r_p the pressure row's residual entry).  The
-// constant factors are applied in the row pass, in element_row's
-// expressions, so that both forms round (and contract) alike.
+// Pass 1, one thread per cell (coalesced): the metric G = J^T J, the scale
+// kappa^2 / (kappa |det J|) and the pressure row's residual entry r_p,
+// evaluated once per cell instead of once per (row, cell) incidence, with
+// element_row's operations and rounding.  FP32 records (one 32-byte sector):
+//   3-D: [G11, G12, G13, scale | G22, G23, G33, r_p]
+//   2-D: [G11, G12, G22, scale | r_p, 0, 0, 0]
+// FP64 records also carry the row sums R of G and S = tr G + sum G (the
+// FP64 units are scarce here, FP32 ones are not):
+//   3-D: [S, R1, R2, R3 | G11, G12, G13, scale | G22, G23, G33, r_p]
+//   2-D: [S, R1, R2, G11 | G12, G22, scale, r_p]
 // Pass 2 is the row-owner kernel reading these records in place of the
-// vertices: 48 (3-D) or 32 (2-D) bytes of FP32 per incidence.
-template <int DIM>
-struct RecWords;
-template <>
-struct RecWords<3> {
-  static constexpr int n = 12;
-};
-template <>
-struct RecWords<2> {
-  static constexpr int n = 8;
+// vertices; it forms the rest of the row in element_row's expressions and
+// order, so that both forms round (and contract) alike.
+template <typename T, int DIM>
+struct RecLayout {
+  static constexpr bool sums = sizeof(T) == 8;           // R and S stored
+  static constexpr int n = (sums && DIM == 3) ? 12 : 8;  // words per cell
+  static constexpr int rp = n - 1 - ((!sums && DIM == 2) ? 3 : 0);  // r_p position
+  static constexpr int scale = sums ? (DIM == 3 ? 7 : 6) : 3;
+  static constexpr int g0 = sums ? (DIM == 3 ? 4 : 3) : 0;  // first G word
 };
 
+// Record of one cell from its loaded incidence (see the layout above).
 template <typename T, int DIM, int SRC>
-__global__ void __launch_bounds__(256) darcy_records_kernel(const DarcyParams p) {
-  constexpr int NW = RecWords<DIM>::n;
+__device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, const Incidence<T, DIM>& x, T u) {
+  using L = RecLayout<T, DIM>;
+  constexpr int NW = L::n;
   using C = DarcyConst<T, DIM>;
   T* rec = static_cast<T*>(p.rec);
-  const T u = edge_unit<T>(p);
-  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < p.n_cells;
-       c += int64_t(gridDim.x) * blockDim.x) {
-    Incidence<T, DIM> x;
-    load_incidence<T, DIM, SRC>(p, int32_t(c), true, x);
-    T G[DIM][DIM];
+  T G[DIM][DIM];
 #pragma unroll
-    for (int i = 0; i < DIM; ++i)
+  for (int i = 0; i < DIM; ++i)
 #pragma unroll
-      for (int j = 0; j < DIM; ++j) G[i][j] = x.J[i][0] * x.J[j][0] + x.J[i][1] * x.J[j][1] + x.J[i][2] * x.J[j][2];
-    const T det = abs_det<T, DIM>(x.J, G);
-    if (!(det > T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
-    const T det_true = DIM == 3 ? det * (u * u * u) : det * (u * u);
+    for (int j = 0; j < DIM; ++j) G[i][j] = x.J[i][0] * x.J[j][0] + x.J[i][1] * x.J[j][1] + x.J[i][2] * x.J[j][2];
+  const T det = abs_det<T, DIM>(x.J, G);
+  if (!(det > T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+  const T det_true = DIM == 3 ? det * (u * u * u) : det * (u * u);
+  const T scale = T(C::kappa2) * recip(x.kap * (DIM == 3 ? det * u : det));
+  T rp = T(0);
+  if constexpr (SRC == NFEM_COEF_CELL) rp = -det_true * T(C::area) * x.src;
+  if constexpr (SRC == NFEM_COEF_QPOINT) rp = -det_true * x.src;
+  T w[NW];
+#pragma unroll
+  for (int k = 0; k < NW; ++k) w[k] = T(0);
+  if constexpr (L::sums) {
     T R[DIM];
     T trG = T(0), sumG = T(0);
 #pragma unroll
@@ -383,54 +388,61 @@ __global__ void __launch_bounds__(256) darcy_records_kernel(const DarcyParams p)
       trG += G[i][i];
       sumG += R[i];
     }
-    T w[NW];
     w[0] = trG + sumG;
-    const T scale = T(C::kappa2) * recip(x.kap * (DIM == 3 ? det * u : det));
-    T rp = T(0);
-    if constexpr (SRC == NFEM_COEF_CELL) rp = -det_true * T(C::area) * x.src;
-    if constexpr (SRC == NFEM_COEF_QPOINT) rp = -det_true * x.src;
-    if constexpr (DIM == 3) {
-      w[1] = R[0];
-      w[2] = R[1];
-      w[3] = R[2];
-      w[4] = G[0][0];
-      w[5] = G[0][1];
-      w[6] = G[0][2];
-      w[7] = scale;
-      w[8] = G[1][1];
-      w[9] = G[1][2];
-      w[10] = G[2][2];
-      w[11] = rp;
-    } else {
-      w[1] = R[0];
-      w[2] = R[1];
-      w[3] = G[0][0];
-      w[4] = G[0][1];
-      w[5] = G[1][1];
-      w[6] = scale;
-      w[7] = rp;
-    }
-    // 16-byte stores: a record never straddles a 32-byte sector per store
-    if constexpr (sizeof(T) == 4) {
-      float4* out = reinterpret_cast<float4*>(rec + c * NW);
 #pragma unroll
-      for (int k = 0; k < NW / 4; ++k) out[k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
-    } else {
-      double2* out = reinterpret_cast<double2*>(rec + c * NW);
+    for (int i = 0; i < DIM; ++i) w[1 + i] = R[i];
+  }
+  if constexpr (DIM == 3) {
+    w[L::g0 + 0] = G[0][0];
+    w[L::g0 + 1] = G[0][1];
+    w[L::g0 + 2] = G[0][2];
+    w[L::g0 + 4] = G[1][1];
+    w[L::g0 + 5] = G[1][2];
+    w[L::g0 + 6] = G[2][2];
+  } else {
+    w[L::g0 + 0] = G[0][0];
+    w[L::g0 + 1] = G[0][1];
+    w[L::g0 + 2] = G[1][1];
+  }
+  w[L::scale] = scale;
+  w[L::rp] = rp;
+  // 16-byte stores: a record never straddles a 32-byte sector per store
+  if constexpr (sizeof(T) == 4) {
+    float4* out = reinterpret_cast<float4*>(rec + c * NW);
 #pragma unroll
-      for (int k = 0; k < NW / 2; ++k) out[k] = make_double2(w[2 * k], w[2 * k + 1]);
-    }
+    for (int k = 0; k < NW / 4; ++k) out[k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+  } else {
+    double2* out = reinterpret_cast<double2*>(rec + c * NW);
+#pragma unroll
+    for (int k = 0; k < NW / 2; ++k) out[k] = make_double2(w[2 * k], w[2 * k + 1]);
   }
 }
 
-// Record words of cell c (vector loads: the record is 16-byte aligned).
+// One cell per thread and iteration (two in flight per thread measured
+// slower: 100.8 against 96.0 us for the whole FP32 assembly at 64^3 x 6).
+template <typename T, int DIM, int SRC>
+__global__ void __launch_bounds__(256) darcy_records_kernel(const DarcyParams p) {
+  const T u = edge_unit<T>(p);
+  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < p.n_cells;
+       c += int64_t(gridDim.x) * blockDim.x) {
+    Incidence<T, DIM> x;
+    load_incidence<T, DIM, SRC>(p, int32_t(c), true, x);
+    write_record<T, DIM, SRC>(p, c, x, u);
+  }
+}
+
+// Record words of cell c (vector loads: the record is 16-byte aligned); a
+// pressure row (full == false) needs only the chunk holding r_p.
 template <typename T, int DIM>
-__device__ __forceinline__ void load_record(const T* __restrict__ rec, int32_t c, T (&w)[RecWords<DIM>::n]) {
-  constexpr int NW = RecWords<DIM>::n;
+__device__ __forceinline__ void load_record(const T* __restrict__ rec, int32_t c, bool full,
+                                            T (&w)[RecLayout<T, DIM>::n]) {
+  using L = RecLayout<T, DIM>;
+  constexpr int NW = L::n;
   if constexpr (sizeof(T) == 4) {
     const float4* q = reinterpret_cast<const float4*>(rec + int64_t(c) * NW);
 #pragma unroll
     for (int k = 0; k < NW / 4; ++k) {
+      if (!full && k != L::rp / 4) continue;
       const float4 v = __ldg(q + k);
       w[4 * k] = v.x;
       w[4 * k + 1] = v.y;
@@ -441,6 +453,7 @@ __device__ __forceinline__ void load_record(const T* __restrict__ rec, int32_t c
     const double2* q = reinterpret_cast<const double2*>(rec + int64_t(c) * NW);
 #pragma unroll
     for (int k = 0; k < NW / 2; ++k) {
+      if (!full && k != L::rp / 2) continue;
       const double2 v = __ldg(q + k);
       w[2 * k] = v.x;
       w[2 * k + 1] = v.y;
@@ -450,36 +463,56 @@ __device__ __forceinline__ void load_record(const T* __restrict__ rec, int32_t c
 
 // Row a of cell c's element matrix from its record (element_row's values).
 template <typename T, int DIM>
-__device__ __forceinline__ void record_row(const T (&w)[RecWords<DIM>::n], uint32_t m, int a, T (&vals)[DIM + 2],
-                                           T& rhs_val) {
+__device__ __forceinline__ void record_row(const T (&w)[RecLayout<T, DIM>::n], uint32_t m, int a,
+                                           T (&vals)[DIM + 2], T& rhs_val) {
+  using L = RecLayout<T, DIM>;
   constexpr int NF = DIM + 1;
   using C = DarcyConst<T, DIM>;
   T sg[NF];
 #pragma unroll
   for (int i = 0; i < NF; ++i) sg[i] = ((m >> i) & 1u) ? -C::sigma(i) : C::sigma(i);
   if (a < NF) {
-    T R[DIM], Ga[DIM];
-    T scale;
+    T G[DIM][DIM];
     if constexpr (DIM == 3) {
-      R[0] = w[1]; R[1] = w[2]; R[2] = w[3];
-      scale = w[7];
-      // row a-1 of G: a = 1 -> (G11, G12, G13), 2 -> (G12, G22, G23), 3 -> (G13, G23, G33)
-      Ga[0] = a == 1 ? w[4] : (a == 2 ? w[5] : w[6]);
-      Ga[1] = a == 1 ? w[5] : (a == 2 ? w[8] : w[9]);
-      Ga[2] = a == 1 ? w[6] : (a == 2 ? w[9] : w[10]);
-      if (a == 0) Ga[0] = Ga[1] = Ga[2] = T(0);  // as element_row
+      G[0][0] = w[L::g0]; G[0][1] = w[L::g0 + 1]; G[0][2] = w[L::g0 + 2];
+      G[1][0] = G[0][1]; G[1][1] = w[L::g0 + 4]; G[1][2] = w[L::g0 + 5];
+      G[2][0] = G[0][2]; G[2][1] = G[1][2]; G[2][2] = w[L::g0 + 6];
     } else {
-      R[0] = w[1]; R[1] = w[2];
-      scale = w[6];
-      Ga[0] = a == 1 ? w[3] : w[4];
-      Ga[1] = a == 1 ? w[4] : w[5];
-      if (a == 0) Ga[0] = Ga[1] = T(0);
+      G[0][0] = w[L::g0]; G[0][1] = w[L::g0 + 1];
+      G[1][0] = G[0][1]; G[1][1] = w[L::g0 + 2];
     }
+    const T scale = w[L::scale];
     // element_row's expressions from here on
-    const T tgs = w[0] * T(C::f2);
+    T R[DIM];
+    T S;
+    if constexpr (L::sums) {
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) R[i] = w[1 + i];
+      S = w[0];
+    } else {
+      T trG = T(0), sumG = T(0);
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) {
+        R[i] = T(0);
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) R[i] += G[i][j];
+        trG += G[i][i];
+        sumG += R[i];
+      }
+      S = trG + sumG;
+    }
+    const T tgs = S * T(C::f2);
+    T Ga[DIM];
     T Ra = T(0);
 #pragma unroll
-    for (int i = 0; i < DIM; ++i) Ra = (a == i + 1) ? R[i] : Ra;
+    for (int j = 0; j < DIM; ++j) Ga[j] = T(0);
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      const bool hit = (a == i + 1);
+      Ra = hit ? R[i] : Ra;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) Ga[j] = hit ? G[i][j] : Ga[j];
+    }
     T sga = sg[0];
 #pragma unroll
     for (int i = 1; i < NF; ++i) sga = (a == i) ? sg[i] : sga;
@@ -495,7 +528,7 @@ __device__ __forceinline__ void record_row(const T (&w)[RecWords<DIM>::n], uint3
 #pragma unroll
     for (int b = 0; b < NF; ++b) vals[b] = sg[b];
     vals[NF] = T(0);
-    rhs_val += w[RecWords<DIM>::n - 1];
+    rhs_val += w[L::rp];
   }
 }
 
@@ -601,8 +634,8 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_
       if (on[t]) {
         T v[NLOC];
         if constexpr (REC) {
-          T w[RecWords<DIM>::n];
-          load_record<T, DIM>(static_cast<const T*>(p.rec), c[t], w);
+          T w[RecLayout<T, DIM>::n];
+          load_record<T, DIM>(static_cast<const T*>(p.rec), c[t], a[t] < DIM + 1, w);
           record_row<T, DIM>(w, __ldg(p.sign + c[t]), a[t], v, rhs_val);
         } else {
           Incidence<T, DIM> x;
@@ -934,7 +967,8 @@ using namespace nfem;
 extern "C" int nfem_darcy_workspace_bytes(int dim, int value_type, int64_t n_cells, size_t* bytes) {
   if (!bytes || (dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_cells < 0)
     return NFEM_ERR_INVALID_ARG;
-  *bytes = size_t(n_cells) * (dim == 3 ? 12 : 8) * (value_type == NFEM_F64 ? 8 : 4);
+  // FP32: 8 words per cell; FP64: 12 (tetrahedra) or 8 (triangles)
+  *bytes = value_type == NFEM_F64 ? size_t(n_cells) * (dim == 3 ? 12 : 8) * 8 : size_t(n_cells) * 8 * 4;
   return NFEM_OK;
 }
 
