@@ -532,6 +532,25 @@ __device__ __forceinline__ void record_row(const T (&w)[RecLayout<T, DIM>::n], u
   }
 }
 
+// Bulk (TMA) store of a warp's staged CSR segment: one elected lane copies
+// the 16-byte-aligned middle of the segment from shared to global memory;
+// the lanes store the unaligned head and tail.  Both addresses and the size
+// are multiples of 16 bytes (checked by the caller).
+#ifndef NFEM_DARCY_BULK
+#define NFEM_DARCY_BULK 1
+#endif
+__device__ __forceinline__ void bulk_store_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
+               "r"(static_cast<uint32_t>(__cvta_generic_to_shared(ssrc))), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// the staged source of every committed bulk store has been read
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// every committed bulk store has completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 struct RowHead {
   int2 pr;
   uint2 cd;
@@ -569,7 +588,8 @@ template <typename T, int DIM, int SRC, bool REC = false>
 __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_MIN_BLOCKS : 1)
     darcy_rows_kernel(const DarcyParams p) {
   constexpr int NLOC = DIM + 2;
-  __shared__ T stage[kDarcyWarps][32 * kDarcyMaxRow];
+  constexpr int VEC = 16 / int(sizeof(T));  // values per 16 bytes
+  __shared__ __align__(16) T stage[kDarcyWarps][32 * kDarcyMaxRow];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* st = stage[warp];
   T* values = static_cast<T*>(p.values);
@@ -581,7 +601,12 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_
   auto rp_at = [&](int64_t r) { return __ldg(p.row_ptr + (r < p.n_rows ? r : p.n_rows)); };
   RowHead head = load_head(p, r0 + lane);
   int32_t rp_lane = rp_at(r0 + lane), rp_end = rp_at(r0 + 32);
+  const bool bulk = NFEM_DARCY_BULK && !p.accumulate && (reinterpret_cast<uintptr_t>(values) & 15) == 0;
   for (; r0 < p.n_rows; r0 += stride) {
+    if (bulk) {  // the staging buffer is free once the last bulk store has read it
+      if (lane == 0) bulk_wait_read();
+      __syncwarp();
+    }
     const int64_t r = r0 + lane;
     const bool valid = r < p.n_rows;
     const RowHead h = head;
@@ -609,9 +634,12 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_
     const int32_t rp_down = __shfl_down_sync(0xffffffffu, rpl, 1);
     const int32_t rpn = lane == 31 ? rpe : rp_down;
     const int len = valid ? rpn - rpl : 0;
-    const int off = rpl - base;
+    // staging index q of global entry base - sh + q: the bulk store's middle
+    // is 16-byte aligned in both memories
+    const int sh = bulk ? (base & (VEC - 1)) : 0;
+    const int off = rpl - base + sh;
     const int span = rpe - base;
-    if (span > 32 * kDarcyMaxRow || span < 0) {  // rows of at most 16 entries fit
+    if (span + sh > 32 * kDarcyMaxRow || span < 0) {  // rows of at most 16 entries fit
       if (lane == 0) set_status(p.status, NFEM_ERR_PATTERN);
       continue;
     }
@@ -624,7 +652,7 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_
     const bool simple = !on[0] || (two ? (len == 2 * NLOC - 1 && pos_a0 == pos_a1) : (len == NLOC));
     const bool direct = __all_sync(0xffffffffu, simple);
     if (!direct) {
-      for (int i = lane; i < span; i += 32) st[i] = T(0);
+      for (int i = lane; i < span; i += 32) st[sh + i] = T(0);
       __syncwarp();
     }
     constexpr int kCap = 32 * kDarcyMaxRow - 1;
@@ -666,14 +694,24 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_
     }
     __syncwarp();
     if (p.accumulate) {
-      for (int i = lane; i < span; i += 32) values[int64_t(base) + i] += st[i];
+      for (int i = lane; i < span; i += 32) values[int64_t(base) + i] += st[sh + i];
       if (valid) rhs[r] += rhs_val;
     } else {
-      for (int i = lane; i < span; i += 32) values[int64_t(base) + i] = st[i];
+      const int qe = sh + span;
+      const int q0 = (sh + VEC - 1) & ~(VEC - 1), q1 = qe & ~(VEC - 1);
+      T* gseg = values + (int64_t(base) - sh);  // global address of staging index 0
+      if (bulk && q1 > q0) {
+        if (lane == 0) bulk_store_s2g(gseg + q0, st + q0, uint32_t(q1 - q0) * uint32_t(sizeof(T)));
+        if (lane < q0 - sh) gseg[sh + lane] = st[sh + lane];             // head: < VEC entries
+        if (lane >= 16 && lane - 16 < qe - q1) gseg[q1 + lane - 16] = st[q1 + lane - 16];  // tail
+      } else {
+        for (int i = lane; i < span; i += 32) values[int64_t(base) + i] = st[sh + i];
+      }
       if (valid) rhs[r] = rhs_val;
     }
     __syncwarp();
   }
+  if (bulk && lane == 0) bulk_wait_all();
 }
 
 // ------------------------------------------------------------------ cell chunks
