@@ -273,6 +273,7 @@ def solve_bench(args, A, wf, coefs, res, stream):
     out["two_level_classical"] = _timed_solve(ksp, b, args, stream, two_level=True)
     out["two_level_classical"]["host_structure_s"] = t_struct
     out["two_level_classical"]["aggregates"] = tl.n_agg
+    out["two_level_classical"]["cycle"] = "symmetric (pre- and post-smoothing), omega 0.9"
     try:
         from nfempy_gb300 import learned, train_learned
         model, ck = train_learned.load()
@@ -476,8 +477,9 @@ def batch2d_bench(args):
         t_struct = time.perf_counter() - t0
         ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.tl_restart, two_level=tl)
         out["solve"] = _timed_solve(ksp, -r64, args, torch.cuda.current_stream(), two_level=True)
-        out["solve"].update({"preconditioner": f"two-level, {args.batch_agg}x{args.batch_agg}-square aggregates, "
-                                               "coarse matrix block-diagonal per problem",
+        out["solve"].update({"preconditioner": f"two-level (symmetric cycle, omega 0.9), {args.batch_agg}x"
+                                               f"{args.batch_agg}-square aggregates, coarse matrix block-diagonal "
+                                               "per problem",
                              "aggregates": tl.n_agg, "largest_block": int(np.diff(bp).max()),
                              "host_structure_s": t_struct})
     return out

@@ -411,6 +411,12 @@ typedef struct {
   const int32_t* ap_ptr;
   const int32_t* ap_col;
   float* ap_val;
+  /* Cycle: omega (> 0; 0 means 1) damps the cell-block smoother, z = omega B v;
+   * post_smooth != 0 adds z += omega B (v - A z) after the coarse correction
+   * (a symmetric two-level cycle: one more smoother apply and SpMV per
+   * application, fewer Krylov iterations). */
+  float omega;
+  int32_t post_smooth;
 } nfem_two_level;
 
 #define NFEM_COARSE_BLOCK_MAX 1024

@@ -51,7 +51,7 @@ class TwoLevel(C.Structure):
                 ("gj", C.c_void_p), ("ac_inv", C.c_void_p), ("work", C.c_void_p), ("n_blocks", C.c_int32),
                 ("blk_max", C.c_int32), ("ac_entries", C.c_int64), ("blk_ptr", C.c_void_p), ("blk_off", C.c_void_p),
                 ("agg_blk", C.c_void_p), ("ap_nnz", C.c_int64), ("ap_ptr", C.c_void_p), ("ap_col", C.c_void_p),
-                ("ap_val", C.c_void_p)]
+                ("ap_val", C.c_void_p), ("omega", C.c_float), ("post_smooth", C.c_int32)]
 
 
 class Precond(C.Structure):

@@ -1379,6 +1379,27 @@ __global__ void offsets_i32(const int64_t* __restrict__ in, int64_t n, int32_t* 
     out[i] = int32_t(in[i]);
 }
 
+// z += P ec and r -= (A P) ec: r stays the residual v - A z of the new z
+__global__ void twolevel_prolong_res(int64_t n_rows, const int32_t* __restrict__ p_agg,
+                                     const float* __restrict__ p_val, const float* __restrict__ ec,
+                                     float* __restrict__ z, const int32_t* __restrict__ ap_ptr,
+                                     const int32_t* __restrict__ ap_col, const float* __restrict__ ap_val,
+                                     float* __restrict__ r, const int32_t* __restrict__ gate) {
+  NFEM_GATE(gate);
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n_rows; i += int64_t(gridDim.x) * blockDim.x) {
+    float acc = 0.f;
+#pragma unroll
+    for (int sl = 0; sl < 2; ++sl) {
+      const int32_t a = p_agg[2 * i + sl];
+      if (a >= 0) acc = fmaf(p_val[2 * i + sl], ec[a], acc);
+    }
+    z[i] += acc;
+    float ap = 0.f;
+    for (int32_t e = ap_ptr[i]; e < ap_ptr[i + 1]; ++e) ap = fmaf(__ldg(ap_val + e), __ldg(ec + __ldg(ap_col + e)), ap);
+    r[i] -= ap;
+  }
+}
+
 // z += P ec and, with A P, w = yscale (.) ((v - r) + (A P) ec) = yscale (.) A z
 __global__ void twolevel_prolong_ap(int64_t n_rows, const int32_t* __restrict__ p_agg,
                                     const float* __restrict__ p_val, const float* __restrict__ ec,
@@ -1510,10 +1531,12 @@ __global__ void block_extract_invert(int64_t n_cells, const int32_t* __restrict_
 }
 
 // z_r = (1 / m_r) sum over the incidences (c, a) of row r of (A_c^-1 v[dofs_c])_a
+// omega scales the result; accumulate adds it into z (a post-smoothing step)
 template <int N>
 __global__ void block_apply(int64_t n_rows, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                             const int32_t* __restrict__ cd, const float* __restrict__ inv, const float* __restrict__ v,
-                            float* __restrict__ z, const int32_t* __restrict__ gate) {
+                            float* __restrict__ z, const int32_t* __restrict__ gate, float omega = 1.f,
+                            int accumulate = 0) {
   NFEM_GATE(gate);
   for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n_rows; r += int64_t(gridDim.x) * blockDim.x) {
     const int32_t kb = inc_ptr[r], ke = inc_ptr[r + 1];
@@ -1526,7 +1549,9 @@ __global__ void block_apply(int64_t n_rows, const int32_t* __restrict__ inc_ptr,
 #pragma unroll
       for (int b = 0; b < N; ++b) acc = fmaf(__ldg(row + b), __ldg(v + __ldg(cd + int64_t(c) * N + b)), acc);
     }
-    z[r] = ke > kb ? acc / float(ke - kb) : v[r];
+    const float zr = ke > kb ? acc / float(ke - kb) : v[r];
+    if (accumulate) z[r] += omega * zr;
+    else z[r] = omega == 1.f ? zr : omega * zr;
   }
 }
 
@@ -1700,6 +1725,27 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
   return NFEM_OK;
 }
 
+// cell-block smoother: z = omega B v, or z += omega B v
+static int smoother(const nfem_precond* pc, int64_t n, const float* v, float* z, float omega, int accumulate,
+                    cudaStream_t s, const int32_t* gate) {
+  const int B = 256;
+  if (pc->n_loc == 5)
+    block_apply<5><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z, gate,
+                                                omega, accumulate);
+  else if (pc->n_loc == 4)
+    block_apply<4><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z, gate,
+                                                omega, accumulate);
+  else
+    return NFEM_ERR_UNSUPPORTED;
+  return NFEM_OK;
+}
+
+static float pre_omega(const nfem_precond* pc) {
+  if (pc->kind != NFEM_PC_TWO_LEVEL || !pc->two_level) return 1.f;
+  const float w = pc->two_level->omega;
+  return w > 0.f ? w : 1.f;
+}
+
 // z = M v.  With w_out and the two-level A P, also w_out = yscale (.) A z
 // (*w_done = true); the caller's SpMV is then not needed.
 static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, float* z, cudaStream_t s,
@@ -1716,14 +1762,7 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
       break;
     case NFEM_PC_TWO_LEVEL:
     case NFEM_PC_CELL_BLOCK:
-      if (pc->n_loc == 5)
-        block_apply<5><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z,
-                                                    gate);
-      else if (pc->n_loc == 4)
-        block_apply<4><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z,
-                                                    gate);
-      else
-        return NFEM_ERR_UNSUPPORTED;
+      NFEM_RC(smoother(pc, n, v, z, pre_omega(pc), 0, s, gate));
       break;
     default:
       return NFEM_ERR_UNSUPPORTED;
@@ -1757,7 +1796,18 @@ static int precond_apply(const nfem_precond* pc, int64_t n, const float* v, floa
                                                                            L->ac_inv, rc, ec, gate);
     else
       dense_gemv<<<unsigned(ceil_div(int64_t(na) * 32, 256)), 256, 0, s>>>(na, L->ac_inv, rc, ec, gate);
-    if (w_out && L->ap_ptr) {
+    if (L->post_smooth) {
+      // z += omega B (v - A z) after the coarse correction (symmetric cycle)
+      if (L->ap_ptr) {
+        twolevel_prolong_res<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z, L->ap_ptr, L->ap_col,
+                                                              L->ap_val, r2, gate);
+      } else {
+        twolevel_prolong<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z, gate);
+        NFEM_RC(spmv<float, float, float>(n, pc->a32->row_ptr, pc->a32->col_idx, (const float*)pc->a32->values, z,
+                                          r2, v, 1, s, nullptr, gate));
+      }
+      NFEM_RC(smoother(pc, n, r2, z, pre_omega(pc), 1, s, gate));
+    } else if (w_out && L->ap_ptr) {
       twolevel_prolong_ap<<<grid_for(n, 256), 256, 0, s>>>(n, L->p_agg, L->p_val, ec, z, L->ap_ptr, L->ap_col,
                                                            L->ap_val, v, r2, yscale, w_out, gate);
       if (w_done) *w_done = true;

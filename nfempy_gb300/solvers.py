@@ -171,7 +171,7 @@ class TwoLevelCoarse:
     pressure columns).  w = None gives the classical weights 1/|a_ff|; the
     learned preconditioner passes the network's prediction."""
 
-    def __init__(self, A, n_c, w=None, cell_agg=None, blocks=None, fuse_ap=True):
+    def __init__(self, A, n_c, w=None, cell_agg=None, blocks=None, fuse_ap=True, post_smooth=True, omega=0.9):
         """cell_agg: optional aggregate of every cell (0 .. n_agg - 1) in place
         of the centroid grid, e.g. per-problem grids for a batch of
         independent problems assembled as one disjoint union.
@@ -184,7 +184,14 @@ class TwoLevelCoarse:
 
         fuse_ap: keep the product A P (its pattern is built here, its values
         in every preconditioner setup), so that the preconditioner hands back
-        A z with z and the solver saves one SpMV per iteration."""
+        A z with z and the solver saves one SpMV per iteration.
+
+        post_smooth, omega: a damped smoother (z = omega B v) and, with
+        post_smooth, a second smoothing step after the coarse correction.
+        Measured at 64^3 x 6 (restart 15, inner 1e-2): pre-smoothing only,
+        omega 1: 175 iterations, 80 ms; symmetric cycle, omega 0.9: 103
+        iterations, 67 ms (omega 1 does not converge with post-smoothing);
+        the 512-problem batch: 168 -> 65 iterations, 196 -> 107 ms."""
         sp = A.space
         self.A = A
         dim = sp.dim
@@ -287,6 +294,8 @@ class TwoLevelCoarse:
                                     _lib.ptr(self.pt_slot).value, _lib.ptr(self.pt_val).value,
                                     _lib.ptr(self.ac).value, _lib.ptr(self.gj).value, _lib.ptr(self.ac_inv).value,
                                     _lib.ptr(self.work).value, *blk)
+        self.struct.omega = float(omega)
+        self.struct.post_smooth = 1 if post_smooth else 0
         if fuse_ap:
             self._build_ap()
 
