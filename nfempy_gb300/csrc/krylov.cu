@@ -954,55 +954,6 @@ __global__ void __launch_bounds__(256) bgj_trailing(T* __restrict__ m, int N, in
     }
 }
 
-// A_IJ -= A_IK A_KJ on 128 x 128 output tiles (FP32): 8 x 8 outputs per
-// thread from K-major shared tiles (16-byte reads), rows and columns of the
-// K block left to the panel kernels, edges clipped to N.
-constexpr int kTr = 128;
-constexpr int kTrLd = kTr + 4;  // padded row of the K-major tiles (floats)
-
-__global__ void __launch_bounds__(256) bgj_trailing128(float* __restrict__ m, int N, int k0) {
-  extern __shared__ __align__(16) unsigned char tr_smem[];
-  float(*xs)[kTrLd] = reinterpret_cast<float(*)[kTrLd]>(tr_smem);  // xs[k][i] = A[i0 + i][k0 + k]
-  float(*ys)[kTrLd] = xs + kGjB;                                    // ys[k][j] = A[k0 + k][j0 + j]
-  const int i0 = blockIdx.y * kTr, j0 = blockIdx.x * kTr;
-  for (int e = threadIdx.x; e < kGjB * kTr; e += blockDim.x) {
-    const int i = e / kGjB, k = e - i * kGjB;
-    xs[k][i] = i0 + i < N ? m[int64_t(i0 + i) * N + k0 + k] : 0.f;
-    const int kk = e / kTr, j = e - kk * kTr;
-    ys[kk][j] = j0 + j < N ? m[int64_t(k0 + kk) * N + j0 + j] : 0.f;
-  }
-  __syncthreads();
-  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-  float acc[8][8];
-#pragma unroll
-  for (int a = 0; a < 8; ++a)
-#pragma unroll
-    for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
-#pragma unroll 4
-  for (int k = 0; k < kGjB; ++k) {
-    const float4 x0 = *reinterpret_cast<const float4*>(&xs[k][ty * 8]);
-    const float4 x1 = *reinterpret_cast<const float4*>(&xs[k][ty * 8 + 4]);
-    const float4 y0 = *reinterpret_cast<const float4*>(&ys[k][tx * 8]);
-    const float4 y1 = *reinterpret_cast<const float4*>(&ys[k][tx * 8 + 4]);
-    const float xa[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-    const float yb[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
-#pragma unroll
-    for (int a = 0; a < 8; ++a)
-#pragma unroll
-      for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(xa[a], yb[b], acc[a][b]);
-  }
-#pragma unroll
-  for (int a = 0; a < 8; ++a) {
-    const int r = i0 + ty * 8 + a;
-    if (r >= N || (r >= k0 && r < k0 + kGjB)) continue;
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const int c = j0 + tx * 8 + b;
-      if (c < N && (c < k0 || c >= k0 + kGjB)) m[int64_t(r) * N + c] -= acc[a][b];
-    }
-  }
-}
-
 template <typename T>
 __global__ void bgj_put_diag(T* __restrict__ m, int N, int k0, const T* __restrict__ dblk) {
   for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x)
@@ -1025,26 +976,18 @@ static int blocked_inverse(const double* ac, int n, T* m, T* dblk, float* inv, i
   const int N = int(ceil_div(n, kGjB) * kGjB);
   const int nt = N / kGjB;
   const size_t smem = 2 * kGjB * (kGjB + 1) * sizeof(T);
-  const size_t smem128 = 2 * kGjB * kTrLd * sizeof(float);
-  static const bool attr = [smem, smem128] {
+  static const bool attr = [smem] {
     return cudaFuncSetAttribute(bgj_trailing<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) ==
                cudaSuccess &&
-           cudaFuncSetAttribute(bgj_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) ==
-               cudaSuccess &&
-           cudaFuncSetAttribute(bgj_trailing128, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem128)) ==
-               cudaSuccess;
+           cudaFuncSetAttribute(bgj_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) == cudaSuccess;
   }();
   if (!attr) return NFEM_ERR_CUDA;
-  const int nt128 = int(ceil_div(N, kTr));
   bgj_pad<T><<<grid_for(int64_t(N) * N, 256), 256, 0, s>>>(ac, n, N, m);
   for (int kb = 0; kb < nt; ++kb) {
     const int k0 = kb * kGjB;
     bgj_inv_diag<T><<<1, 1024, 0, s>>>(m, N, k0, dblk, status);
     bgj_panel<T><<<nt, 256, smem, s>>>(m, N, k0, dblk, 0);
-    if constexpr (sizeof(T) == 4)
-      bgj_trailing128<<<dim3(nt128, nt128), 256, smem128, s>>>(m, N, k0);
-    else
-      bgj_trailing<T><<<dim3(nt, nt), 256, smem, s>>>(m, N, k0);
+    bgj_trailing<T><<<dim3(nt, nt), 256, smem, s>>>(m, N, k0);
     bgj_panel<T><<<nt, 256, smem, s>>>(m, N, k0, dblk, 1);
     bgj_put_diag<T><<<1, 256, 0, s>>>(m, N, k0, dblk);
   }
