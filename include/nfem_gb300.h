@@ -441,6 +441,12 @@ typedef struct {
   double* setup_scratch;
   const nfem_two_level* two_level; /* NFEM_PC_TWO_LEVEL only (host pointer) */
   const nfem_csr* a32;             /* FP32 matrix, NFEM_PC_TWO_LEVEL only (host pointer) */
+  /* Optional (host pointer): the cell-block smoother (times the two-level
+   * omega) stored in A's CSR pattern, FP32 values [nnz] filled by
+   * nfem_precond_setup; row_ptr and col_idx must be A64's.  With it each
+   * smoother application is one SpMV.  NULL: applied cell block by cell
+   * block. */
+  const nfem_csr* smoother;
 } nfem_precond;
 
 typedef struct {

@@ -58,7 +58,7 @@ class Precond(C.Structure):
     _fields_ = [("kind", C.c_int), ("n_loc", C.c_int), ("n_cells", C.c_int64), ("cell_dofs", C.c_void_p),
                 ("inc_ptr", C.c_void_p), ("inc", C.c_void_p), ("block_inv", C.c_void_p), ("diag_inv", C.c_void_p),
                 ("wsqrt", C.c_void_p), ("winvsqrt", C.c_void_p), ("setup_scratch", C.c_void_p),
-                ("two_level", C.POINTER(TwoLevel)), ("a32", C.POINTER(Csr))]
+                ("two_level", C.POINTER(TwoLevel)), ("a32", C.POINTER(Csr)), ("smoother", C.POINTER(Csr))]
 
 
 class SolveParams(C.Structure):

@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(32 * kSpmvWarps)
       __syncwarp();
     }
     if (valid) {
-      AT out = residual ? AT(b[r]) - acc : acc;
+      AT out = residual == 1 ? AT(b[r]) - acc : (residual == 2 ? AT(b[r]) + acc : acc);
       if (yscale) out *= AT(yscale[r]);
       y[r] = XT(out);
     }
@@ -1474,6 +1474,53 @@ __global__ void block_extract_invert(int64_t n_cells, const int32_t* __restrict_
 }
 
 // z_r = (1 / m_r) sum over the incidences (c, a) of row r of (A_c^-1 v[dofs_c])_a
+// The cell-block smoother as a matrix in A's pattern: row r of
+// omega / m_r sum over the incidences (c, a) of r of row a of A_c^-1, at the
+// columns dofs_c (the pattern of A is the union of the cells' cliques).
+// damping of the cell-block smoother (the two-level cycle's omega, else 1)
+static float pre_omega(const nfem_precond* pc) {
+  if (pc->kind != NFEM_PC_TWO_LEVEL || !pc->two_level) return 1.f;
+  const float w = pc->two_level->omega;
+  return w > 0.f ? w : 1.f;
+}
+
+template <int N>
+__global__ void smoother_fill(int64_t n_rows, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                              const int32_t* __restrict__ cd, const float* __restrict__ inv,
+                              const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, float omega,
+                              float* __restrict__ sv, int32_t* status) {
+  for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n_rows; r += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t b0 = rp[r], b1 = rp[r + 1];
+    for (int32_t e = b0; e < b1; ++e) sv[e] = 0.f;
+    const int32_t kb = inc_ptr[r], ke = inc_ptr[r + 1];
+    if (ke == kb) {  // a row of no cell: the smoother leaves it as it is
+      int32_t e = b0;
+      while (e < b1 && ci[e] != r) ++e;
+      if (e < b1) sv[e] = omega;
+      else set_status(status, NFEM_ERR_PATTERN);
+      continue;
+    }
+    const float scale = omega / float(ke - kb);
+    for (int32_t k = kb; k < ke; ++k) {
+      const int32_t occ = inc[k];
+      const int32_t c = occ / N;
+      const int a = occ - c * N;
+      const float* row = inv + (int64_t(c) * N + a) * N;
+#pragma unroll
+      for (int b = 0; b < N; ++b) {
+        const int32_t j = cd[int64_t(c) * N + b];
+        int32_t lo = b0, hi = b1;
+        while (lo < hi) {
+          const int32_t mid = (lo + hi) >> 1;
+          if (ci[mid] < j) lo = mid + 1; else hi = mid;
+        }
+        if (lo < b1 && ci[lo] == j) sv[lo] += scale * row[b];
+        else set_status(status, NFEM_ERR_PATTERN);
+      }
+    }
+  }
+}
+
 // omega scales the result; accumulate adds it into z (a post-smoothing step)
 template <int N>
 __global__ void block_apply(int64_t n_rows, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
@@ -1602,6 +1649,21 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
                                                         (const double*)A64->values, pc->block_inv, dev_status); break;
       default: return NFEM_ERR_UNSUPPORTED;
     }
+    if (pc->smoother) {
+      const nfem_csr* S = pc->smoother;
+      if (S->value_type != NFEM_F32 || S->n_rows != A64->n_rows || !S->values || S->row_ptr != A64->row_ptr ||
+          S->col_idx != A64->col_idx)
+        return NFEM_ERR_INVALID_ARG;
+      const int gr = grid_for(A64->n_rows, 256);
+      if (pc->n_loc == 5)
+        smoother_fill<5><<<gr, 256, 0, s>>>(A64->n_rows, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv,
+                                            A64->row_ptr, A64->col_idx, pre_omega(pc), (float*)S->values,
+                                            dev_status);
+      else
+        smoother_fill<4><<<gr, 256, 0, s>>>(A64->n_rows, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv,
+                                            A64->row_ptr, A64->col_idx, pre_omega(pc), (float*)S->values,
+                                            dev_status);
+    }
   } else if (pc->kind != NFEM_PC_NONE) {
     return NFEM_ERR_UNSUPPORTED;
   }
@@ -1672,6 +1734,11 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
 static int smoother(const nfem_precond* pc, int64_t n, const float* v, float* z, float omega, int accumulate,
                     cudaStream_t s, const int32_t* gate) {
   const int B = 256;
+  if (pc->smoother) {  // omega B is stored in A's pattern: one SpMV
+    const nfem_csr* S = pc->smoother;
+    return spmv<float, float, float>(n, S->row_ptr, S->col_idx, (const float*)S->values, v, z, accumulate ? z : nullptr,
+                                     accumulate ? 2 : 0, s, nullptr, gate);
+  }
   if (pc->n_loc == 5)
     block_apply<5><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z, gate,
                                                 omega, accumulate);
@@ -1683,11 +1750,6 @@ static int smoother(const nfem_precond* pc, int64_t n, const float* v, float* z,
   return NFEM_OK;
 }
 
-static float pre_omega(const nfem_precond* pc) {
-  if (pc->kind != NFEM_PC_TWO_LEVEL || !pc->two_level) return 1.f;
-  const float w = pc->two_level->omega;
-  return w > 0.f ? w : 1.f;
-}
 
 // z = M v.  With w_out and the two-level A P, also w_out = yscale (.) A z
 // (*w_done = true); the caller's SpMV is then not needed.

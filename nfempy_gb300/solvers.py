@@ -52,14 +52,18 @@ INNER_RTOL = {"two_level": 1e-2, "cell_block": 1e-3, "jacobi": 1e-2, "none": 1e-
 
 
 class KrylovSolver:
-    def __init__(self, A, pc="cell_block", A32_values=None, restart=30, weighted=True, two_level=None, graphs=True):
+    def __init__(self, A, pc="cell_block", A32_values=None, restart=30, weighted=True, two_level=None, graphs=True,
+                 smoother_matrix=True):
         """graphs: replay each restart cycle after the first as one CUDA graph
-        (False launches every kernel from the host)."""
+        (False launches every kernel from the host).  smoother_matrix: store
+        the cell-block smoother in A's CSR pattern (one SpMV per smoothing
+        step, nnz more FP32 values) instead of applying it cell by cell."""
         if A.dtype != torch.float64:
             raise ValueError("A must be the FP64 matrix (the residual is measured in FP64)")
         self.A = A
         self.restart = int(restart)
         self.graphs = bool(graphs)
+        self.smoother_matrix = bool(smoother_matrix)
         self.values32 = A32_values
         self.pc_kind = pc
         self.weighted = weighted
@@ -95,6 +99,10 @@ class KrylovSolver:
             self.pc = _lib.Precond(kind, n_loc, sp.n_cells, _lib.ptr(sp.cell_dofs).value,
                                    _lib.ptr(A.inc_ptr).value, _lib.ptr(A.inc).value,
                                    _lib.ptr(self.block_inv).value, None, None, None, None)
+            if self.smoother_matrix:
+                self.smoother_vals = torch.empty(max(1, A.nnz), dtype=torch.float32, device=dev)
+                self._smoother = _csr(A, self.smoother_vals)
+                self.pc.smoother = _lib.C.pointer(self._smoother)
             if self.pc_kind == "two_level":
                 if self.two_level is None:
                     raise ValueError("pc='two_level' needs two_level=TwoLevelCoarse(...)")

@@ -249,3 +249,34 @@ def test_dense_coarse_inverse(cuda_lib, n_c):
     cond = np.linalg.cond(Ac)
     err = np.abs(X @ Ac - np.eye(na)).max()
     assert err <= max(1e-4, 64 * cond * 6e-8), (err, cond)
+
+
+@pytest.mark.parametrize("pc", ["cell_block", "two_level"])
+def test_smoother_matrix_matches_cell_blocks(cuda_lib, pc):
+    """The cell-block smoother stored in A's pattern applies the same operator
+    as the cell-by-cell form (FP32 rounding), and both solves reach 1e-8 in
+    a similar number of iterations."""
+    from nfempy_gb300 import _lib, meshes
+    from nfempy_gb300.solvers import TwoLevelCoarse
+    m = mesh_gen.cube(8)
+    cent = m["points"][m["blocks"][-1][1]].mean(axis=1)
+    kappa = np.exp(meshes.grf_log_field(cent, 0.05, 2.0, 5))
+    sp, A, res = assembled(m, kappa, 1.0)
+    b = -res
+    out = {}
+    v = torch.randn(A.n_rows, dtype=torch.float32, device="cuda")
+    for mat in (False, True):
+        tl = TwoLevelCoarse(A, 2) if pc == "two_level" else None
+        ksp = KrylovSolver(A, pc=pc, restart=15, two_level=tl, smoother_matrix=mat)
+        ksp.setup()
+        z = torch.empty_like(v)
+        _lib.call("nfem_precond_apply", _lib.C.byref(ksp.pc), A.n_rows, _lib.ptr(v), _lib.ptr(z), _lib.stream_ptr())
+        x, info = ksp.solve(b, rtol=1e-8, max_inner=20000)
+        assert info.status == 0 and info.final_relres <= 1e-8
+        out[mat] = (z, info.inner_iterations)
+    z0, z1 = out[False][0], out[True][0]
+    assert (z0 - z1).abs().max().item() <= 1e-5 * z0.abs().max().item()
+    # restarted block-Jacobi FGMRES is sensitive to round-off in its
+    # iteration count (hundreds of iterations here); the two-level one is not
+    slack = out[False][1] // 4 if pc == "cell_block" else max(3, out[False][1] // 20)
+    assert abs(out[False][1] - out[True][1]) <= slack
