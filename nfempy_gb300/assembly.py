@@ -215,14 +215,16 @@ class LaplaceDualWeakForm(WeakForm):
     tets); both write the same values up to rounding.
     use_records: the row-owner kernel reads per-cell metric records from a
     first cell pass (True) instead of evaluating each (row, cell) incidence
-    from the vertices (False); the values agree to rounding.  Measured at
-    64^3 x 6 tets: FP32 0.096 ms against 0.101 ms, FP64 0.50 ms against
-    1.12 ms (the geometry is evaluated once per cell instead of once per
-    incidence).
+    from the vertices (False); the values agree to rounding.  None (default)
+    takes the two passes for tetrahedra and for FP64, one pass for FP32
+    triangles, from measurements: 64^3 x 6 tets FP32 0.096 ms against
+    0.101 ms, FP64 0.50 ms against 1.12 ms (the geometry is evaluated once
+    per cell instead of once per incidence); the 512-problem triangle batch
+    FP32 0.280 ms against 0.250 ms (a triangle's geometry is cheap).
     """
 
     use_chunks = False
-    use_records = True
+    use_records = None
 
     def _check_space(self):
         sp = self.space
@@ -290,7 +292,10 @@ class LaplaceDualWeakForm(WeakForm):
         pts, wts = sp.quadrature[sp.dim]
         qw = (_lib.C.c_double * len(wts))(*wts.tolist())
         ws = None
-        if self.use_records and not self.use_chunks:
+        records = self.use_records
+        if records is None:
+            records = sp.dim == 3 or dtype == torch.float64
+        if records and not self.use_chunks:
             key = ("records", dtype)
             if key not in self._cache:
                 nb = _lib.C.c_size_t(0)
