@@ -32,7 +32,10 @@
 namespace nfem {
 
 constexpr int kElasDegMax = 96;  // node columns per node row
-constexpr int kElasWarps32 = 4;
+#ifndef NFEM_ELAS_WARPS
+#define NFEM_ELAS_WARPS 4
+#endif
+constexpr int kElasWarps32 = NFEM_ELAS_WARPS;
 constexpr int kElasWarps64 = 2;
 
 __constant__ double c_S[10 * 10 * 9];
@@ -169,9 +172,20 @@ __device__ __forceinline__ void load_geom<double>(const ElasParams& p, int32_t c
 // Row images: per warp, per group, rows i = 0..2 of the node, one 4-wide slot
 // per node column (the column's components j = 0..2 and a pad), so a 3 x 3
 // block is added with three 16-byte read-modify-writes.
+// NFEM_ELAS_IMAGES: 3 = one image per group (the groups add at once, and
+// the images are summed at the end); 1 = one image per warp, the groups'
+// read-modify-writes in turn (a third of the shared memory per warp, so
+// twice the resident warps).  Measured at 40^3 x 6 FP32: 3 images 0.690 ms,
+// 1 image 0.612 ms.
+#ifndef NFEM_ELAS_IMAGES
+#define NFEM_ELAS_IMAGES 1
+#endif
+constexpr int kElasImages = NFEM_ELAS_IMAGES;
+static_assert(kElasImages == 1 || kElasImages == 3, "one image per group or one per warp");
+
 template <typename T>
 __host__ __device__ constexpr size_t elas_image_words(int deg) {
-  return size_t(3) * 3 * size_t(deg) * 4;
+  return size_t(kElasImages) * 3 * size_t(deg) * 4;
 }
 
 template <typename T, int WARPS>
@@ -201,9 +215,9 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
       if (lane == 0) set_status(p.status, NFEM_ERR_UNSUPPORTED);
       continue;
     }
-    // the group images of this node: [3 groups][3 rows][deg][4]
-    const int gstride = 3 * deg * 4;
-    for (int q = lane; q < 3 * 3 * deg; q += 32) {
+    // the group images of this node: [images][3 rows][deg][4]
+    const int gstride = kElasImages == 3 ? 3 * deg * 4 : 0;
+    for (int q = lane; q < kElasImages * 3 * deg; q += 32) {
       Slot4<T> z;
       z.zero();
       z.store(wimg + q * 4);
@@ -213,13 +227,16 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
     T rhs_acc[3] = {T(0), T(0), T(0)};
     for (int32_t k0 = kb; k0 < ke; k0 += 3) {
       const int32_t k = k0 + g;
-      if (lane < 30 && k < ke) {
+      const bool act = lane < 30 && k < ke;
+      T K[3][3];
+      int pos = 0;
+      if (act) {
         const int32_t occ = __ldg(p.inc + k);
         const int32_t c = occ / 30;
         const int a = (occ - c * 30) / 3;
         // node position inside the row; the clamp keeps a corrupted code in
         // this node's image (a valid one is < deg)
-        const int pos = min(int(__ldg(p.codes + int64_t(k) * 16 + b)), deg - 1);
+        pos = min(int(__ldg(p.codes + int64_t(k) * 16 + b)), deg - 1);
         T gm[12];
         load_geom<T>(p, c, gm);
         const T(&Ji)[12] = gm;  // Ji[k * 3 + q] = (J^-1)_{kq}
@@ -239,34 +256,48 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
             A[pp][q] = Ji[0 * 3 + pp] * SJ[0][q] + Ji[1 * 3 + pp] * SJ[1][q] + Ji[2 * 3 + pp] * SJ[2][q];
         const T lc = gm[9], mc = gm[10], adet = gm[11];
         const T tr = A[0][0] + A[1][1] + A[2][2];
-        T* im = wimg + g * gstride;
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          T* slot = im + (i * deg + pos) * 4;
-          Slot4<T> s4;
-          s4.load(slot);
+        for (int i = 0; i < 3; ++i)
 #pragma unroll
-          for (int j = 0; j < 3; ++j) s4[j] += (i == j ? mc * tr : T(0)) + mc * A[j][i] + lc * A[i][j];
-          s4.store(slot);
-        }
+          for (int j = 0; j < 3; ++j) K[i][j] = (i == j ? mc * tr : T(0)) + mc * A[j][i] + lc * A[i][j];
         if (force && b == 0) {
 #pragma unroll
           for (int i = 0; i < 3; ++i) rhs_acc[i] += adet * sm_m[a] * __ldg(force + int64_t(c) * 3 + i);
         }
       }
-      __syncwarp();
+      // add the 3 x 3 block at the node column: three images take every
+      // group at once; one image takes the groups in turn (two cells of the
+      // node may share a column), the whole warp stepping together
+#pragma unroll
+      for (int gg = 0; gg < (kElasImages == 1 ? 3 : 1); ++gg) {
+        if (act && (kElasImages == 3 || g == gg)) {
+          T* im = wimg + g * gstride;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            T* slot = im + (i * deg + pos) * 4;
+            Slot4<T> s4;
+            s4.load(slot);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) s4[j] += K[i][j];
+            s4.store(slot);
+          }
+        }
+        __syncwarp();
+      }
     }
-    // combine the three group images in a fixed order: one (row i, column) slot per lane
+    // combine the group images in a fixed order: one (row i, column) slot per lane
     for (int q = lane; q < 3 * deg; q += 32) {
       Slot4<T> s0, s1, s2;
       s0.load(wimg + q * 4);
-      s1.load(wimg + gstride + q * 4);
-      s2.load(wimg + 2 * gstride + q * 4);
+      if (kElasImages == 3) {
+        s1.load(wimg + gstride + q * 4);
+        s2.load(wimg + 2 * gstride + q * 4);
+      }
       const int i = q / deg, pos = q - i * deg;
       T* out = values + int64_t(base) + i * len + 3 * pos;
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        const T sum = s0[j] + s1[j] + s2[j];
+        const T sum = kElasImages == 3 ? s0[j] + s1[j] + s2[j] : s0[j];
         if (p.accumulate) out[j] += sum; else out[j] = sum;
       }
     }
