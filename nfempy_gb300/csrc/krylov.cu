@@ -1640,6 +1640,17 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
       if (L->n_blocks < 0 || (L->n_blocks > 0 && (!L->blk_ptr || !L->blk_off || !L->agg_blk || L->blk_max < 1 ||
                                                   L->blk_max > NFEM_COARSE_BLOCK_MAX || L->ac_entries < 1)))
         return NFEM_ERR_INVALID_ARG;
+      if (L->ap_ptr && (!L->ap_col || !L->ap_val || !pc->a32 || pc->a32->value_type != NFEM_F32 ||
+                        pc->a32->n_rows != A64->n_rows))
+        return NFEM_ERR_INVALID_ARG;
+    }
+    // every argument is checked before the first launch
+    if (pc->n_loc != 4 && pc->n_loc != 5) return NFEM_ERR_UNSUPPORTED;
+    if (pc->smoother) {
+      const nfem_csr* S = pc->smoother;
+      if (S->value_type != NFEM_F32 || S->n_rows != A64->n_rows || !S->values || S->row_ptr != A64->row_ptr ||
+          S->col_idx != A64->col_idx)
+        return NFEM_ERR_INVALID_ARG;
     }
     const int g = grid_for(pc->n_cells, 128);
     switch (pc->n_loc) {
@@ -1651,9 +1662,6 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     }
     if (pc->smoother) {
       const nfem_csr* S = pc->smoother;
-      if (S->value_type != NFEM_F32 || S->n_rows != A64->n_rows || !S->values || S->row_ptr != A64->row_ptr ||
-          S->col_idx != A64->col_idx)
-        return NFEM_ERR_INVALID_ARG;
       const int gr = grid_for(A64->n_rows, 256);
       if (pc->n_loc == 5)
         smoother_fill<5><<<gr, 256, 0, s>>>(A64->n_rows, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv,
@@ -1694,9 +1702,7 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
     twolevel_fill_p<<<g, 256, 0, s>>>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, L->p_base,
                                       pc->n_cells, L->cell_agg, L->w, L->p_agg, L->p_val);
     twolevel_fill_pt<<<grid_for(L->pt_nnz, 256), 256, 0, s>>>(L->pt_nnz, L->pt_slot, L->p_val, L->pt_val);
-    if (L->ap_ptr) {
-      if (!L->ap_col || !L->ap_val || !pc->a32 || pc->a32->value_type != NFEM_F32 || pc->a32->n_rows != n)
-        return NFEM_ERR_INVALID_ARG;
+    if (L->ap_ptr) {  // (arguments checked above)
       ap_fill_values<<<g, 256, 0, s>>>(n, pc->a32->row_ptr, pc->a32->col_idx, (const float*)pc->a32->values,
                                        L->p_agg, L->p_val, L->ap_ptr, L->ap_col, L->ap_val, dev_status);
       NFEM_CHECK_LAUNCH();

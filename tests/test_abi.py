@@ -141,6 +141,24 @@ def test_two_level_ap_queries_and_argument_checks(lib_path):
                                          ctypes.byref(nnz), None, None) == 3  # NFEM_ERR_WORKSPACE
 
 
+def test_precond_setup_checks_arguments_before_launching(lib_path):
+    """nfem_precond_setup refuses bad arguments before any device work: a
+    smoother matrix that does not share A's pattern, an unsupported block
+    size, an FP32 matrix where the FP64 one is needed."""
+    lib = _lib.lib()
+    fake = 64
+    A64 = _lib.Csr(100, fake, fake, fake, _lib.NFEM_F64)
+    pc = _lib.Precond(_lib.PC_CELL_BLOCK, 5, 20, fake, fake, fake, fake, None, None, None, None)
+    other = _lib.Csr(100, fake + 16, fake, fake, _lib.NFEM_F32)
+    pc.smoother = ctypes.pointer(other)
+    assert lib.nfem_precond_setup(ctypes.byref(pc), ctypes.byref(A64), None, None) == 1
+    pc.smoother = None
+    pc.n_loc = 6
+    assert lib.nfem_precond_setup(ctypes.byref(pc), ctypes.byref(A64), None, None) == 7  # NFEM_ERR_UNSUPPORTED
+    A32 = _lib.Csr(100, fake, fake, fake, _lib.NFEM_F32)
+    assert lib.nfem_precond_setup(ctypes.byref(pc), ctypes.byref(A32), None, None) == 1
+
+
 def test_status_string_for_every_code(lib_path):
     lib = _lib.lib()
     for code, name in _lib.STATUS_NAMES.items():
