@@ -10,16 +10,20 @@
 //  * CSR SpMV in FP32 (inner) and FP64 (outer residual r = b - A x), warp
 //    chunks of 32 rows whose contiguous CSR segment is streamed with
 //    coalesced loads into shared memory, then reduced per row.
-//  * Deterministic reductions: a fixed grid of kRedBlocks blocks writes
-//    partial sums, one block adds them in a fixed order (bitwise
-//    reproducible dots and norms).
-//  * Preconditioners: point Jacobi, and cell-patch block Jacobi (weighted
+//  * Deterministic reductions: a fixed grid of blocks writes partial sums
+//    and the last block to finish adds them in a fixed order (bitwise
+//    reproducible dots and norms, no separate reduction launch).
+//  * Preconditioners: point Jacobi; cell-patch block Jacobi (weighted
 //    additive Schwarz over the element cliques: z = sum_c R_c^T D_c A_c^-1 R_c v
-//    with D_c = 1 / multiplicity, applied row-owner, no atomics).
+//    with D_c = 1 / multiplicity), applied row-owner or, stored in A's CSR
+//    pattern, as one SpMV; and a two-level Galerkin cycle (damped smoother
+//    before and after a coarse correction with a dense or block-diagonal
+//    stored inverse, A P kept to update residuals without an SpMV).
 //  * Flexible GMRES(m) with classical Gram-Schmidt and one
-//    re-orthogonalisation; the Hessenberg matrix, Givens rotations and
-//    residual estimates live on the device, so a restart cycle synchronises
-//    with the host once.
+//    re-orthogonalisation, the second pass and the norm fused with the
+//    updates; the Hessenberg matrix, Givens rotations and residual
+//    estimates live on the device, so a restart cycle synchronises with the
+//    host once, and cycles after the first are replayed as a CUDA graph.
 //  * Mixed precision: inner FGMRES in FP32 on the FP32 matrix, outer
 //    refinement with the FP64 residual of the FP64 matrix until
 //    ||b - A x|| / ||b|| <= rtol (the stopping test is always FP64).
@@ -42,7 +46,7 @@ extern "C" int nfem_mlp_forward(const int32_t* dims, int weight_type, const void
 
 namespace nfem {
 
-constexpr int kRedBlocks = 1216;  // 8 x 152 SMs
+constexpr int kRedBlocks = 1216;  // 8 x 152 SMs; the widest reduction grid (partial buffers)
 constexpr int kRedThreads = 256;
 constexpr int kSpmvWarps = 8;
 constexpr int kSpmvCap = 32 * 16;
