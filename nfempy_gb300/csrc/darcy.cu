@@ -25,8 +25,11 @@
 // that row of the element matrix from the cell's vertices and adds it into a
 // warp-private shared-memory image of the warp's contiguous CSR segment at
 // the positions given by the precomputed 4-bit slot codes.  The segment is
-// then stored with coalesced writes.  Every CSR value and residual entry is
-// written exactly once: no atomics, no zero-fill pass, deterministic sums.
+// then stored with coalesced writes (its 16-byte-aligned middle by one TMA
+// bulk copy).  Every CSR value and residual entry is written exactly once:
+// no atomics, no zero-fill pass, deterministic sums.  With a record
+// workspace a cell pass first evaluates each cell's metric terms once, and
+// the row pass reads those records instead of the vertices (two-pass form).
 #include "nfem_common.cuh"
 
 namespace nfem {
