@@ -69,7 +69,9 @@ int nfem_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offsets,
  * array's device address; make that first call before any stream capture.
  * All calls on a device share the one array: calls whose kernels overlap on
  * the GPU (different streams, or different host threads without ordering)
- * race and must be serialised by the caller.  Allocates nothing. */
+ * race and must be serialised by the caller.  The looked-up address lives
+ * as long as the device's primary context: do not call this scan after a
+ * cudaDeviceReset in the same process.  Allocates nothing. */
 int nfem_exclusive_scan_noalloc(const int32_t* counts, int64_t n, int64_t* offsets,
                                 void* stream);
 

@@ -141,6 +141,10 @@ static __device__ __align__(256) int64_t g_noalloc_scan_scratch[kNoAllocMaxTiles
 // Device address of g_noalloc_scan_scratch, looked up once per device.  In
 // host code the symbol's name is only a host-side stand-in and must never be
 // handed to a kernel; cudaGetSymbolAddress gives the real device address.
+// The cached address is valid for the lifetime of the device's primary
+// context: a cudaDeviceReset in this process destroys that context (the
+// module is loaded again on next use, possibly at another address), so the
+// no-allocation scan must not be called after a device reset.
 constexpr int kMaxDevices = 64;
 static int64_t* g_noalloc_scratch_ptr[kMaxDevices] = {nullptr};
 static std::mutex g_noalloc_mutex;

@@ -60,7 +60,7 @@ def main(argv=None):
 
 
 def load(path=DEFAULT_OUT, device="cuda"):
-    ck = torch.load(path, map_location="cpu", weights_only=False)
+    ck = torch.load(path, map_location="cpu", weights_only=True)  # tensors and plain containers only
     model = learned.MLP(learned.N_FEAT, device=device)
     model.load_state_dict(ck["model"])
     return model, ck

@@ -25,3 +25,32 @@ def golden(name):
 def to_product_fields(fields):
     """Oracle family names -> reference names ('P' -> 'Lagrange')."""
     return [(n, "Lagrange" if f == "P" else f, k, nc, d) for n, f, k, nc, d in fields]
+
+
+# Coefficient functions of the element-form fixtures.  The reference's weak
+# forms call them on quadrature-point coordinates: kappa point by point
+# (laplace_dual_weak_form.py:71), the others on arrays (le_primal_weak_form.py:
+# 37-39, lce_dual_weak_form.py:476-489).  Every Cosserat parameter differs so
+# that each term of the form is pinned on its own.
+def _const(v):
+    return lambda x, y, z: np.full(np.shape(x), float(v))
+
+
+COSSERAT_PARAMS = dict(lambda_s=1.3, mu_s=0.7, kappa_s=0.45, lambda_o=0.9, mu_o=1.1, kappa_o=0.35, l=0.8)
+COSSERAT_RHS = (1.0, -2.0, 0.5, 0.3, 0.2, -0.4)
+
+FORM_FUNCTIONS = {
+    "darcy": {
+        "kappa": lambda x, y, z: 1.0 + 0.5 * x + 0.25 * y * y + 0.1 * z,
+        "rhs": lambda x, y, z: np.array([np.sin(np.pi * x) * np.sin(np.pi * y) + z]),
+    },
+    "elast": {
+        "lambda": lambda x, y, z: 1.0 + x + 0.0 * y,
+        "mu": lambda x, y, z: 2.0 + y * z + 0.5 * x,
+        "rhs": lambda x, y, z: np.array([x + 0.0 * y, 1.0 + 0.0 * x, z * z + y]),
+    },
+    "cosserat": {
+        **{k: _const(v) for k, v in COSSERAT_PARAMS.items()},
+        "rhs": lambda x, y, z: np.array([np.full(np.shape(x), v) for v in COSSERAT_RHS]),
+    },
+}

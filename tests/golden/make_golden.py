@@ -10,6 +10,9 @@ stand-ins:
   * basix    - element metadata, tabulation and push-forward from
                oracle.elements, quadrature from oracle.quadrature
   * matplotlib - empty module (imported but unused by src/assembly/ScatterFormData.py:2)
+  * auto_diff  - forward-mode AutoDiff / VecValDer written from the weak
+                 forms' own call sites (the forms are linear in alpha, so the
+                 derivative carried through is the element Jacobian)
 
 What the fixtures pin, from the reference's own code paths:
   * destination indices of every cell   (ProductSpace.destination_indexes,
@@ -21,8 +24,17 @@ What the fixtures pin, from the reference's own code paths:
   * the oriented, pushed-forward RT1 basis (FiniteElement.evaluate_basis,
     src/basis/finite_element.py:156-186) - its Piola/orientation logic is the
     reference's, its reference-cell tables come from the basix stand-in.
+  * element residuals and Jacobians (r_el, j_el) of every cell from the
+    reference's own weak forms: LaplaceDualWeakForm.evaluate_form
+    (src/weak_forms/laplace_dual_weak_form.py:10-86), LEPrimalWeakForm
+    (src/weak_forms/le_primal_weak_form.py:10-129) and
+    LCEDualWeakForm.evaluate_form_vectorized
+    (src/weak_forms/lce_dual_weak_form.py:410-648), with the coefficient
+    functions of FORM_FUNCTIONS below (tests/cases.py restates them for the
+    oracle side).
 
-Run:  python -B tests/golden/make_golden.py   (writes tests/golden/*.npz)
+Run:  python -B tests/golden/make_golden.py --reference-src <nfempy>/src
+      (or set NFEM_REFERENCE_SRC; writes tests/golden/*.npz)
 """
 import os
 import sys
@@ -31,8 +43,24 @@ import types
 sys.dont_write_bytecode = True
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF_SRC = "/root/reference/src"
 sys.path.insert(0, REPO)
+
+
+def reference_src():
+    """The reference's src/ directory: --reference-src PATH, else the
+    NFEM_REFERENCE_SRC environment variable."""
+    path = None
+    if "--reference-src" in sys.argv:
+        i = sys.argv.index("--reference-src")
+        path = sys.argv[i + 1] if i + 1 < len(sys.argv) else None
+    path = path or os.environ.get("NFEM_REFERENCE_SRC")
+    if not path or not os.path.isdir(os.path.join(path, "weak_forms")):
+        sys.exit("make_golden.py: pass --reference-src <nfempy checkout>/src (or set NFEM_REFERENCE_SRC); "
+                 f"got {path!r}, which holds no weak_forms/ directory")
+    return path
+
+
+REF_SRC = reference_src() if __name__ == "__main__" else None
 
 import numpy as np  # noqa: E402
 
@@ -122,8 +150,134 @@ basix.make_quadrature = lambda cell, degree, rule=None: quadrature.make_quadratu
 matplotlib = types.ModuleType("matplotlib")
 matplotlib.pyplot = types.ModuleType("matplotlib.pyplot")
 
+
+_np_zeros = np.zeros  # the stand-in's own arrays (np.zeros is replaced inside AutoDiff)
+
+
+class VecValDer:
+    """A value and its derivative with respect to the N local coefficients:
+    der has shape val.shape + (N,).  Written from the operations the weak
+    forms apply (slicing, @ with arrays, scalar and array products, sums,
+    .T, reshape, item assignment)."""
+
+    __array_ufunc__ = None  # ndarray op VecValDer defers to the reflected method
+
+    def __init__(self, val, der):
+        self.val = np.asarray(val, dtype=np.float64)
+        self.der = np.asarray(der, dtype=np.float64)
+
+    @property
+    def n(self):
+        return self.der.shape[-1]
+
+    @property
+    def shape(self):
+        return self.val.shape
+
+    def _lift(self, o):
+        if isinstance(o, VecValDer):
+            return o
+        a = np.asarray(o, dtype=np.float64)
+        return VecValDer(a, _np_zeros(a.shape + (self.n,)))
+
+    def __add__(self, o):
+        o = self._lift(o)
+        return VecValDer(self.val + o.val, self.der + o.der)
+
+    __radd__ = __add__
+
+    def __neg__(self):
+        return VecValDer(-self.val, -self.der)
+
+    def __sub__(self, o):
+        return self + (-self._lift(o))
+
+    def __rsub__(self, o):
+        return self._lift(o) - self
+
+    def __mul__(self, o):
+        if isinstance(o, VecValDer):
+            return VecValDer(self.val * o.val, self.der * o.val[..., None] + self.val[..., None] * o.der)
+        a = np.asarray(o, dtype=np.float64)
+        return VecValDer(self.val * a, self.der * a[..., None])
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, o):
+        a = np.asarray(o, dtype=np.float64)
+        return VecValDer(self.val / a, self.der / a[..., None])
+
+    def __matmul__(self, o):
+        if isinstance(o, VecValDer):
+            raise NotImplementedError("product of two differentiated operands")
+        a = np.asarray(o, dtype=np.float64)
+        if a.ndim == 1:
+            return VecValDer(self.val @ a, np.einsum("...kn,k->...n", self.der, a))
+        return VecValDer(self.val @ a, np.einsum("...kn,km->...mn", self.der, a))
+
+    def __rmatmul__(self, o):
+        a = np.asarray(o, dtype=np.float64)
+        if self.val.ndim == 1:
+            return VecValDer(a @ self.val, np.einsum("pk,kn->pn", a, self.der))
+        return VecValDer(a @ self.val, np.einsum("pk,kmn->pmn", a, self.der))
+
+    @property
+    def T(self):
+        k = self.val.ndim
+        return VecValDer(self.val.T, self.der.transpose(tuple(reversed(range(k))) + (k,)))
+
+    def reshape(self, *shape):
+        if len(shape) == 1 and isinstance(shape[0], tuple):
+            shape = shape[0]
+        return VecValDer(self.val.reshape(shape), self.der.reshape(tuple(shape) + (self.n,)))
+
+    def __getitem__(self, idx):
+        return VecValDer(self.val[idx], self.der[idx])
+
+    def __setitem__(self, idx, o):
+        o = self._lift(o)
+        self.val[idx] = o.val
+        self.der[idx] = o.der
+
+
+class AutoDiff:
+    """`with AutoDiff(alpha) as alpha:` yields alpha as a (1, N) row carrying
+    the identity derivative; arrays the form creates with np.zeros inside the
+    block carry a (zero) derivative too, so entries assigned into them keep
+    theirs."""
+
+    def __init__(self, x):
+        self.x = np.asarray(x, dtype=np.float64).ravel()
+
+    def __enter__(self):
+        n = self.x.size
+        real_zeros = _np_zeros
+
+        def zeros(shape, dtype=float, *a, **k):
+            if dtype not in (float, np.float64) or a or k:
+                return real_zeros(shape, dtype, *a, **k)
+            shape = (shape,) if np.isscalar(shape) else tuple(shape)
+            return VecValDer(real_zeros(shape), real_zeros(shape + (n,)))
+
+        np.zeros = zeros
+        return VecValDer(self.x.reshape(1, n), np.eye(n).reshape(1, n, n))
+
+    def __exit__(self, *exc):
+        np.zeros = _np_zeros
+        return False
+
+
+auto_diff = types.ModuleType("auto_diff")
+auto_diff.AutoDiff = AutoDiff
+auto_diff.VecValDer = VecValDer
+auto_diff.vecvalder = types.ModuleType("auto_diff.vecvalder")
+auto_diff.vecvalder.VecValDer = VecValDer
+
 sys.modules.update({"meshio": meshio, "basix": basix, "matplotlib": matplotlib,
-                    "matplotlib.pyplot": matplotlib.pyplot})
+                    "matplotlib.pyplot": matplotlib.pyplot, "auto_diff": auto_diff,
+                    "auto_diff.vecvalder": auto_diff.vecvalder})
+if REF_SRC is None:
+    raise ImportError("make_golden.py runs as a script (it needs the reference's src/ directory)")
 sys.path.insert(0, REF_SRC)
 
 from mesh.mesh import Mesh  # noqa: E402
@@ -131,6 +285,12 @@ from spaces.product_space import ProductSpace  # noqa: E402
 from assembly.SequentialAssembler import SequentialAssembler  # noqa: E402
 from basis.permute_and_transform import (  # noqa: E402
     _validate_edge_orientation_2d, _validate_face_orientation_3d)
+from weak_forms.laplace_dual_weak_form import LaplaceDualWeakForm  # noqa: E402
+from weak_forms.le_primal_weak_form import LEPrimalWeakForm  # noqa: E402
+from weak_forms.lce_dual_weak_form import LCEDualWeakForm  # noqa: E402
+
+sys.path.insert(0, os.path.dirname(HERE))
+from cases import FORM_FUNCTIONS  # noqa: E402
 
 
 class RecordingMat:
@@ -153,6 +313,28 @@ class CountingForm:
     def evaluate_form(self, i, alpha):
         n = len(alpha)
         return np.zeros(n), np.ones((n, n))
+
+
+def element_forms(name, space, n_el):
+    """r_el, j_el of every cell from the reference's own weak form (alpha = 0)."""
+    kind = name.split("_")[0].rstrip("23d")
+    if kind == "darcy":
+        wf = LaplaceDualWeakForm(space)
+        ev = wf.evaluate_form
+    elif kind == "elast":
+        wf = LEPrimalWeakForm(space)
+        ev = wf.evaluate_form
+    else:
+        wf = LCEDualWeakForm(space)
+        ev = wf.evaluate_form_vectorized
+    wf.functions = FORM_FUNCTIONS[kind]
+    rs, js = [], []
+    for i in range(n_el):
+        n = len(space.destination_indexes(i))
+        r, j = ev(i, np.zeros(n))
+        rs.append(np.asarray(r, dtype=np.float64).ravel())
+        js.append(np.asarray(j, dtype=np.float64))
+    return np.array(rs), np.array(js)
 
 
 def make_case(name, mesh, fields):
@@ -213,6 +395,7 @@ def make_case(name, mesh, fields):
         out["rt_basis"] = np.array(tabs)
         out["quad_points"] = pts
         out["quad_weights"] = wts
+    out["r_el"], out["j_el"] = element_forms(name, space, n_el)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "cells", n_el, "n_dof", space.n_dof, "nnz", len(keys))
 

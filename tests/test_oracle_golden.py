@@ -61,3 +61,38 @@ def test_pattern_b_filter():
     ip, ix = assembly.pattern_b(cd, j, 3)
     rows = np.repeat(np.arange(3), np.diff(ip))
     assert list(zip(rows.tolist(), ix.tolist())) == [(0, 0), (0, 2), (1, 1), (1, 2), (2, 2)]
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_element_forms_match_reference(name):
+    """The oracle's element residuals and Jacobians against the ones the
+    reference's own weak forms computed (LaplaceDualWeakForm, LEPrimalWeakForm
+    through a forward-mode auto_diff stand-in; LCEDualWeakForm.
+    evaluate_form_vectorized), cell by cell, with the same coefficient
+    functions.  Bar: 1e-13 of the largest entry of the cell."""
+    from tests.cases import COSSERAT_PARAMS, COSSERAT_RHS, FORM_FUNCTIONS
+    mk, fields = CASES[name]
+    m = mk()
+    g = golden(name)
+    dim = m["dim"]
+    topo = topology.Topology(m, physical_tags=[1])
+    X = m["points"][topo.cells]
+    kmax = max(f[2] for f in fields)
+    quad = quadrature.make_quadrature(dim, 2 * kmax + 1)
+    kind = name.split("_")[0].rstrip("23d")
+    F = FORM_FUNCTIONS[kind]
+    signs = topo.rt1_signs() if kind != "elast" else None
+    assert g["j_el"].shape[0] == topo.n_cells
+    for c in range(topo.n_cells):
+        if kind == "darcy":
+            r, j = forms.darcy_element(X[c], signs[c], dim, quad, F["kappa"], F["rhs"])
+        elif kind == "elast":
+            r, j = forms.elasticity_element(X[c], dim, quad, F["lambda"], F["mu"], F["rhs"])
+        else:
+            r, j = forms.cosserat_element(X[c], signs[c], quad, COSSERAT_PARAMS, COSSERAT_RHS[:3], COSSERAT_RHS[3:])
+        jr, rr = g["j_el"][c], g["r_el"][c]
+        assert j.shape == jr.shape and r.shape == rr.shape
+        scale = np.abs(jr).max()
+        np.testing.assert_allclose(j, jr, rtol=0, atol=1e-13 * scale, err_msg=f"{name} cell {c} j_el")
+        np.testing.assert_allclose(r, rr, rtol=0, atol=1e-13 * max(np.abs(rr).max(), 1e-300),
+                                   err_msg=f"{name} cell {c} r_el")
