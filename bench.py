@@ -287,11 +287,21 @@ def solve_bench(args, A, wf, coefs, res, stream):
         out["learned"]["training"] = {k: ck["record"][k] for k in ("n", "fields", "solves_used", "pairs",
                                                                    "data_seconds", "train_seconds")}
         plain = out["plain_block_jacobi"]["time_to_solve_ms"]
-        out["learned"]["speedup_vs_plain"] = plain / out["learned"]["time_to_solve_ms"]
+        out["learned"]["network_active"] = bool(alpha > 0)
+        out["learned"]["speedup_vs_classical_two_level"] = (out["two_level_classical"]["time_to_solve_ms"]
+                                                            / out["learned"]["time_to_solve_ms"])
+        if alpha > 0:
+            out["learned"]["speedup_vs_plain"] = plain / out["learned"]["time_to_solve_ms"]
+        else:
+            out["learned"]["note"] = ("alpha = 0 on validation: the network's correction is switched off and this "
+                                      "arm equals the classical two-level preconditioner")
     except (OSError, FileNotFoundError, KeyError) as e:
         out["learned"] = {"unavailable": f"no trained network checkpoint ({type(e).__name__})"}
-    out["two_level_classical"]["speedup_vs_plain"] = (out["plain_block_jacobi"]["time_to_solve_ms"]
-                                                      / out["two_level_classical"]["time_to_solve_ms"])
+    tl = out["two_level_classical"]
+    tl["speedup_vs_plain"] = out["plain_block_jacobi"]["time_to_solve_ms"] / tl["time_to_solve_ms"]
+    tl["time_to_solve_incl_host_structure_ms"] = tl["time_to_solve_ms"] + 1e3 * tl["host_structure_s"]
+    tl["speedup_vs_plain_incl_host_structure"] = (out["plain_block_jacobi"]["time_to_solve_ms"]
+                                                  / tl["time_to_solve_incl_host_structure_ms"])
     return out
 
 
@@ -350,23 +360,16 @@ def _time_assembly(fn, steps, warmup):
 def elasticity_bench(args):
     """Vector P2 elasticity assembly: 40^3 x 6 tets, per-cell lognormal
     lambda, mu (mean-log 0, sigma 0.5), body force (1, 1, 1), FP32."""
-    import numpy as np
     import torch
     import nfempy_gb300 as nf
-    from nfempy_gb300 import meshes
+    from nfempy_gb300 import workloads as wl
     from nfempy_gb300.assembly import LEPrimalWeakForm
-    n = 40
-    m = meshes.cube(n)
-    mesh = nf.Mesh(3, data=m)
-    sp = nf.ProductSpace({"u": (3, 3, "Lagrange", 2, mesh)})
-    sp.build_structures({"u": [1]}, {})
+    m, sp, functions = wl.elasticity3d(40)
     A = nf.CSRMatrix(sp, dtype=torch.float32)
     res = torch.empty(A.n_rows, dtype=torch.float32, device="cuda")
-    rng = np.random.default_rng(20261203 + 1)
     T = sp.n_cells
     wf = LEPrimalWeakForm(sp)
-    wf.functions = {"lambda": np.exp(rng.normal(0, 0.5, T)), "mu": np.exp(rng.normal(0, 0.5, T)),
-                    "rhs": np.array([1.0, 1.0, 1.0])}
+    wf.functions = functions
     coefs = wf.coefficients(torch.float32)
     ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
     A.check_status("elasticity bench")
@@ -398,23 +401,17 @@ def elasticity_bench(args):
 
 def cosserat_bench(args):
     """Mixed Cosserat assembly: 24^3 x 6 tets, RT1^3 x RT1^3 x P0^3 x P0^3,
-    Lame 1/1, Cosserat coupling 0.5, FP32."""
+    Lame 1/1, Cosserat coupling 0.5, the manufactured solution's load and the
+    material as callables (sampled once), FP32."""
     import torch
     import nfempy_gb300 as nf
-    from nfempy_gb300 import meshes
+    from nfempy_gb300 import workloads as wl
     from nfempy_gb300.assembly import LCEDualWeakForm
-    n = 24
-    m = meshes.cube(n)
-    mesh = nf.Mesh(3, data=m)
-    sp = nf.ProductSpace({"s": (3, 3, "RT", 1, mesh), "m": (3, 3, "RT", 1, mesh), "u": (3, 3, "Lagrange", 0, mesh),
-                          "t": (3, 3, "Lagrange", 0, mesh)})
-    sp.make_subspaces_discontinuous({"u": True, "t": True})
-    sp.build_structures({k: [1] for k in "smut"}, {})
+    m, sp, functions, exact = wl.cosserat3d(24)
     A = nf.CSRMatrix(sp, dtype=torch.float32)
     res = torch.empty(A.n_rows, dtype=torch.float32, device="cuda")
     wf = LCEDualWeakForm(sp)
-    wf.functions = dict(lambda_s=1.0, mu_s=1.0, kappa_s=0.5, lambda_o=1.0, mu_o=1.0, kappa_o=0.5, l=1.0,
-                        rhs=[1.0, 1.0, 1.0, 0.0, 0.0, 0.0])
+    wf.functions = functions
     coefs = wf.coefficients(torch.float32)
     ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
     A.check_status("cosserat bench")
@@ -426,7 +423,8 @@ def cosserat_bench(args):
     return {"metric": "DoF/s assembled", "value": sp.n_dof / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
             "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz, "kernel": "cosserat_rows_kernel",
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "algorithmic_bytes": alg, "peak_source": kind}}
+                         "algorithmic_bytes": alg, "peak_source": kind,
+                         "traffic": profiled_traffic("cosserat_rows_f32_cube24.txt")}}
 
 
 def batch2d_bench(args):
@@ -462,7 +460,8 @@ def batch2d_bench(args):
            "kernel": "darcy_rows_kernel (one pass: triangles, FP32)",
            "graph_replay_ms_per_step": graph_ms,
            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                        "algorithmic_bytes": alg, "peak_source": kind}}
+                        "algorithmic_bytes": alg, "peak_source": kind,
+                        "traffic": profiled_traffic("darcy_rows_f32_batch512.txt")}}
     if not args.no_solve:
         # every problem at once: two-level FGMRES on the block-diagonal union,
         # aggregates of about s x s squares inside each problem (none spans
@@ -481,7 +480,8 @@ def batch2d_bench(args):
                                                f"{args.batch_agg}-square aggregates, coarse matrix block-diagonal "
                                                "per problem",
                              "aggregates": tl.n_agg, "largest_block": int(np.diff(bp).max()),
-                             "host_structure_s": t_struct})
+                             "host_structure_s": t_struct,
+                             "time_to_solve_incl_host_structure_ms": out["solve"]["time_to_solve_ms"] + 1e3 * t_struct})
     return out
 
 
@@ -619,7 +619,27 @@ def run_ours(args):
     e2e_ms = max_over_ranks(timed(e2e_step, n_e2e, True), dist, "cuda")
     e2e_ok = torch.equal(vals_h[0], vals_h[1]) and torch.equal(vals_h[0], A.values[: A.nnz].cpu())
     A.check_status("bench")
+
+    # ---------------- the other precision, timed the same way (its own roofline)
+    other = "f64" if args.precision == "f32" else "f32"
+    odt = torch.float64 if other == "f64" else torch.float32
+    ob = 8 if other == "f64" else 4
+    A_o = A.with_dtype(odt)
+    res_o = torch.empty(A.n_rows, dtype=odt, device="cuda")
+    coefs_o = wf.coefficients(odt)
+    ms_o = _time_assembly(lambda: wf.assemble(A_o, res_o, coefficients=coefs_o), args.steps, args.warmup)
+    A_o.check_status("bench other precision")
+    ms_o = max_over_ranks(ms_o, dist, "cuda")
     clk = clocks.stop()
+    v32, v64 = (A.values, A_o.values) if other == "f64" else (A_o.values, A.values)
+    r32, r64 = (res, res_o) if other == "f64" else (res_o, res)
+    rp = A.row_ptr.long()
+    rows_of = torch.repeat_interleave(torch.arange(A.n_rows, device=rp.device), rp[1:] - rp[:-1])
+    a64 = v64[: A.nnz].abs()
+    rowmax = torch.zeros(A.n_rows, dtype=torch.float64, device=rp.device).scatter_reduce(0, rows_of, a64, "amax")
+    f32_vs_f64 = float(((v32[: A.nnz].double() - v64[: A.nnz]).abs() / rowmax[rows_of].clamp_min(1e-300)).max())
+    f32_vs_f64_rhs = float((r32.double() - r64).abs().max() / r64.abs().max())
+    del rows_of, a64
 
     # ---------------- time to solve: FP64 system, FP32 inner iterations
     solve = None
@@ -651,6 +671,19 @@ def run_ours(args):
                "sample": (f"oracle per-cell loop (reference structure: mapping, tabulation, Piola, orientation, "
                           f"element matrix, entry-wise scatter) over {cpu_prob['X'].shape[0]} of {cpu_prob['T']} "
                           f"cells, 1 thread, {secs:.1f} s; DoF/s extrapolated to the full mesh")}
+    alg_o = algorithmic_bytes(T, V, A.nnz, n_dof, ob)
+    ach_o = alg_o / (ms_o * 1e-3) / 1e9
+    legs = {args.precision: {"ms_per_step": ms, "value": value, "algorithmic_bytes": alg,
+                             "roofline_frac": achieved / peak, "headline": True},
+            other: {"ms_per_step": ms_o, "value": job_rate(n_dof, world, ms_o), "unit": UNIT,
+                    "kernel": kernels, "algorithmic_bytes": alg_o,
+                    "roofline": {"bound": "hbm", "achieved": ach_o, "peak": peak, "unit": "GB/s",
+                                 "frac": ach_o / peak, "algorithmic_bytes": alg_o, "peak_source": peak_kind,
+                                 "traffic": profiled_traffic(f"{kname}_{other}_cube64.txt")}}}
+    legs["f32"]["max_row_scaled_diff_vs_f64"] = f32_vs_f64
+    legs["f32"]["max_rhs_diff_vs_f64"] = f32_vs_f64_rhs
+    legs["f64"]["parity"] = ("FP64 values within 1e-12 of the FP64 oracle, row-scaled, at this size "
+                             "(tests/test_gpu_fullsize.py)")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -670,6 +703,7 @@ def run_ours(args):
                 "serial": {"value": job_rate(n_dof, world, e2e_serial_ms), "ms_per_step": e2e_serial_ms,
                            "h2d_bytes_per_step": h2d_serial, "d2h_bytes_per_step": d2h,
                            "mode": "points, kappa, f up, split, assemble, values + residual down; one stream"}},
+        "precision_legs": legs,
         "solve": solve,
         "workloads": workloads,
         "gpu_launches": args.steps * launches_per_step,

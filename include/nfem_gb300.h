@@ -38,7 +38,8 @@ typedef enum {
   NFEM_ERR_NOT_CONVERGED = 8, /* Krylov iteration cap reached */
   NFEM_ERR_BREAKDOWN = 9,     /* Krylov breakdown (zero or non-finite denominator) */
   NFEM_ERR_NONFINITE = 10,    /* NaN / Inf detected in an input or residual */
-  NFEM_ERR_DEGENERATE = 11    /* a cell with |det J| == 0 */
+  NFEM_ERR_DEGENERATE = 11,   /* a cell with |det J| == 0 */
+  NFEM_ERR_DOMAIN = 12        /* a coefficient outside its domain (kappa <= 0, mu <= 0) */
 } nfem_status;
 
 typedef enum { NFEM_F64 = 0, NFEM_F32 = 1, NFEM_BF16 = 2 } nfem_value_type;

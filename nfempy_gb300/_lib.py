@@ -24,7 +24,7 @@ STATUS_NAMES = {
     0: "NFEM_OK", 1: "NFEM_ERR_INVALID_ARG", 2: "NFEM_ERR_CUDA", 3: "NFEM_ERR_WORKSPACE",
     4: "NFEM_ERR_OVERFLOW", 5: "NFEM_ERR_CAPACITY", 6: "NFEM_ERR_PATTERN", 7: "NFEM_ERR_UNSUPPORTED",
     8: "NFEM_ERR_NOT_CONVERGED", 9: "NFEM_ERR_BREAKDOWN", 10: "NFEM_ERR_NONFINITE",
-    11: "NFEM_ERR_DEGENERATE",
+    11: "NFEM_ERR_DEGENERATE", 12: "NFEM_ERR_DOMAIN",
 }
 
 

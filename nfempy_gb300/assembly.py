@@ -605,8 +605,15 @@ class LCEDualWeakForm(WeakForm):
     fields s (RT1, 3 rows), m (RT1, 3 rows), u (P0^3), t (P0^3) in that order.
 
     functions: lambda_s, mu_s, kappa_s, lambda_o, mu_o, kappa_o, l - scalars
-    (constant material, as the reference drivers use); "rhs" - None, a
-    6-vector (f_u, f_t), or a per-cell array [T, 6]."""
+    or f(x, y, z) callables like the reference drivers pass
+    (mfe_cosserat_elasticity_example_3.py:120-125), sampled at the quadrature
+    points and required to be constant over the mesh (the material of every
+    benchmark and driver is); "rhs" - None, a 6-vector (f_u, f_t), a per-cell
+    array [T, 6], or f(x, y, z) -> [6, N] sampled at the quadrature points.
+    The u and t test functions are P0, so the reference's load
+    -sum_q |det J| w_q f(x_q) (lce_dual_weak_form.py:490-502) is exactly the
+    cell's quadrature-weighted mean of f times -|T|: that mean is what goes
+    to the device."""
 
     NAMES = ("lambda_s", "mu_s", "kappa_s", "lambda_o", "mu_o", "kappa_o", "l")
 
@@ -629,12 +636,30 @@ class LCEDualWeakForm(WeakForm):
             return self._cache[key]
         sp = self.space
         T = sp.n_cells
-        par = np.array([float(np.ravel(self.functions[k])[0]) for k in self.NAMES], dtype=np.float64)
+        xq = None
+        par = []
+        for k in self.NAMES:
+            v = self.functions[k]
+            if callable(v):
+                xq = self.quadrature_points() if xq is None else xq
+                vals = np.asarray(v(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).ravel()
+                if vals.size == 0 or np.abs(vals - vals[0]).max() > 1e-14 * max(1.0, np.abs(vals).max()):
+                    raise NotImplementedError(f"{k} must be constant over the mesh (the device form takes one material)")
+                par.append(float(vals[0]))
+            else:
+                par.append(float(np.ravel(v)[0]))
+        par = np.array(par, dtype=np.float64)
         f = self.functions.get("rhs")
         ft = None
         if f is not None:
-            fv = np.asarray(f, dtype=np.float64)
-            fv = np.broadcast_to(fv.reshape(1, 6) if fv.size == 6 else fv.reshape(T, 6), (T, 6))
+            if callable(f):
+                xq = self.quadrature_points() if xq is None else xq
+                _, wts = sp.quadrature[sp.dim]
+                fq = np.asarray(f(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).reshape(6, T, -1)
+                fv = np.einsum("ktq,q->tk", fq, np.asarray(wts)) / float(np.sum(wts))
+            else:
+                fv = np.asarray(f, dtype=np.float64)
+                fv = np.broadcast_to(fv.reshape(1, 6) if fv.size == 6 else fv.reshape(T, 6), (T, 6))
             ft = torch.as_tensor(np.ascontiguousarray(fv), dtype=dtype, device=sp.device)
         from .elements import rt1_tet_tables
         Psi, mhat, divhat = rt1_tet_tables()

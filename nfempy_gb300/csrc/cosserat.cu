@@ -24,6 +24,8 @@
 // 3 x 3 block of local node b; group images summed in a fixed order.
 #include <string.h>
 
+#include <cmath>
+
 #include <mutex>
 
 #include "nfem_common.cuh"
@@ -349,6 +351,12 @@ extern "C" int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n
   if (value_type == NFEM_F32 && (!points_split || (reinterpret_cast<uintptr_t>(points_split) & 15)))
     return NFEM_ERR_INVALID_ARG;
   if (reinterpret_cast<uintptr_t>(cell_vertices) & 15) return NFEM_ERR_INVALID_ARG;
+  // the material is one set of host constants: checked here (lambda may be
+  // negative down to -2 mu / 3; the moduli mu, kappa and the length l not)
+  for (int k = 0; k < 7; ++k)
+    if (!std::isfinite(params7[k])) return NFEM_ERR_NONFINITE;
+  if (!(params7[1] > 0) || !(params7[2] > 0) || !(params7[4] > 0) || !(params7[5] > 0) || !(params7[6] > 0))
+    return NFEM_ERR_DOMAIN;
   int rc = upload_cos_tables(ref_Psi, ref_mhat, ref_divhat, stream);
   if (rc) return rc;
   CosParams p;

@@ -204,6 +204,8 @@ __device__ __forceinline__ void load_incidence(const DarcyParams& p, int32_t c, 
       if (q < p.n_qp) acc += T(p.qw[q]) * __ldg(src + int64_t(c) * p.n_qp + q);
     x.src = acc;
   }
+  check_positive(p.status, x.kap);
+  check_finite(p.status, x.src);
   if (need_geo) {
     cell_edges<T, DIM>(p, c, x.J);
   } else {

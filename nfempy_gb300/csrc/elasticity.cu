@@ -140,8 +140,11 @@ __global__ void elas_geom_kernel(const ElasParams p) {
     g[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
     g[5] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
     g[8] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-    g[9] = __ldg(lam + c) * adet;
-    g[10] = __ldg(mu + c) * adet;
+    const T lam_c = __ldg(lam + c), mu_c = __ldg(mu + c);
+    check_finite(p.status, lam_c);
+    check_positive(p.status, mu_c);
+    g[9] = lam_c * adet;
+    g[10] = mu_c * adet;
     g[11] = adet;
 #pragma unroll
     for (int k = 0; k < 12; ++k) out[c * 12 + k] = g[k];

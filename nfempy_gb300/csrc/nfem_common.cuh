@@ -32,6 +32,18 @@ __device__ __forceinline__ void set_status(int32_t* status, int32_t code) {
   if (status) atomicCAS(status, 0, code);
 }
 
+// A coefficient that must be finite: NaN or +-Inf sets NFEM_ERR_NONFINITE.
+template <typename T>
+__device__ __forceinline__ void check_finite(int32_t* status, T v) {
+  if (!isfinite(v)) set_status(status, NFEM_ERR_NONFINITE);
+}
+// A coefficient that must be finite and positive (a permeability, a shear
+// modulus): NaN / Inf -> NFEM_ERR_NONFINITE, v <= 0 -> NFEM_ERR_DOMAIN.
+template <typename T>
+__device__ __forceinline__ void check_positive(int32_t* status, T v) {
+  if (!(v > T(0)) || !isfinite(v)) set_status(status, isfinite(v) ? NFEM_ERR_DOMAIN : NFEM_ERR_NONFINITE);
+}
+
 // Align a byte offset up to 256 bytes (workspace carving).
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 

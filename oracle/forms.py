@@ -8,6 +8,7 @@ basis-major / component-minor inside a field.
   * darcy_element      LaplaceDualWeakForm        laplace_dual_weak_form.py:10-86
   * elasticity_element LEPrimalWeakForm           le_primal_weak_form.py:10-129
   * projector_element  L2ProjectorWeakForm        l2_projector_weak_form.py:8-93
+  * cosserat_element   LCEDualWeakForm            lce_dual_weak_form.py:410-648
 
 The *_batch functions compute the same matrices for many cells at once with
 numpy (the vectorised CPU baseline); they are checked against the per-cell
@@ -207,7 +208,10 @@ def cosserat_element(X, signs, quad, par, f_u, f_t):
     evaluate_form_vectorized).  Fields s (RT1, 3 rows), m (RT1, 3 rows),
     u (P0^3), t (P0^3); local order s, m, u, t, basis-major / component-minor.
     par: dict lambda_s, mu_s, kappa_s, lambda_o, mu_o, kappa_o, l (constants
-    on the cell).  f_u, f_t: body force and couple (3-vectors, constant)."""
+    on the cell).  f_u, f_t: body force and couple (3-vectors, constant), or
+    f_u a callable f(x, y, z) -> [6, Q] (f_u then f_t, evaluated at the
+    physical quadrature points like the reference's f_rhs, :472, :490-502)
+    and f_t None."""
     dim = 3
     pts, wts = quad
     x, J, det, pinv = evaluate_mapping(dim, pts, X)
@@ -221,9 +225,15 @@ def cosserat_element(X, signs, quad, par, f_u, f_t):
     wdet = det * wts
     w0 = p_tab[0, :, 0, 0]  # P0 value (1)
     # rhs_u, rhs_t
-    for c in range(3):
-        r[ns + nm + c] += -np.sum(wdet * w0) * f_u[c]
-        r[ns + nm + nu + c] += -np.sum(wdet * w0) * f_t[c]
+    if callable(f_u):
+        fq = np.asarray(f_u(x[:, 0], x[:, 1], x[:, 2]), dtype=np.float64).reshape(6, Q)
+        for c in range(3):
+            r[ns + nm + c] += -np.sum(wdet * w0 * fq[c])
+            r[ns + nm + nu + c] += -np.sum(wdet * w0 * fq[3 + c])
+    else:
+        for c in range(3):
+            r[ns + nm + c] += -np.sum(wdet * w0) * f_u[c]
+            r[ns + nm + nu + c] += -np.sum(wdet * w0) * f_t[c]
 
     def block(psi, mu_v, kappa_v, lam_v, scale):
         # psi [Q, 4, 3]
@@ -265,6 +275,56 @@ def cosserat_element(X, signs, quad, par, f_u, f_t):
             j[i * 3 + c, ns + nm + c] += ub[i]
             j[ns + nm + nu + c, ns + i * 3 + c] += ub[i]
             j[ns + i * 3 + c, ns + nm + nu + c] += ub[i]
+    return r, j
+
+
+def cosserat_batch(X, signs, quad, par, f_q):
+    """cosserat_element for many cells at once (numpy, FP64).  X [T, 4, 3],
+    signs [T, 4], par the seven constants, f_q [T, Q, 6] the load (f_u, f_t)
+    at the quadrature points.  Returns r [T, 30], j [T, 30, 30]; checked
+    against the per-cell restatement in tests/."""
+    pts, wts = quad
+    T = X.shape[0]
+    J, det, pinv = cell_jacobians(X)
+    ref = el.create_element("RT", 3, 1).tabulate(1, pts)  # [4, Q, 4, 3]
+    sg = np.asarray(signs, dtype=np.float64)
+    psi = np.einsum("tgd,qid->tqig", J, ref[0]) / det[:, None, None, None] * sg[:, None, :, None]
+    wdet = det[:, None] * wts[None, :]
+    Phi = np.einsum("tq,tqia,tqjb->tijab", wdet, psi, psi)  # [T, 4, 4, 3, 3]
+    eye = np.eye(3)
+    tr = np.einsum("tijaa->tij", Phi)
+    inner = 0.5 * np.einsum("tij,cd->ticjd", tr, eye)
+    outer = 0.5 * np.einsum("tijdc->ticjd", Phi)
+    tro = np.einsum("tijcd->ticjd", Phi)
+
+    def block(mu_v, kappa_v, lam_v, scale):
+        vol = (1.0 / (2.0 * mu_v)) * (lam_v / (2.0 * mu_v + 3 * lam_v))
+        b = scale * ((inner + outer) / (2.0 * mu_v) + (inner - outer) / (2.0 * kappa_v) - vol * tro)
+        return b.reshape(T, 12, 12)
+
+    n = 30
+    j = np.zeros((T, n, n))
+    j[:, 0:12, 0:12] = block(par["mu_s"], par["kappa_s"], par["lambda_s"], 1.0)
+    j[:, 12:24, 12:24] = block(par["mu_o"], par["kappa_o"], par["lambda_o"], 1.0 / par["l"])
+    v = np.einsum("tq,tqik->tki", wdet, psi)  # [T, 3 (component k), 4]
+    tmap = {0: ((2, v[:, 1]), (1, -v[:, 2])), 1: ((0, v[:, 2]), (2, -v[:, 0])), 2: ((1, v[:, 0]), (0, -v[:, 1]))}
+    for c in range(3):
+        tb = 27 + c
+        for cs, op in tmap[c]:
+            for i in range(4):
+                j[:, tb, i * 3 + cs] += -op[:, i]
+                j[:, i * 3 + cs, tb] += -op[:, i]
+    divhat = np.einsum("kqik->qi", ref[1:4])  # [Q, 4]
+    ub = np.einsum("q,qi->i", wts, divhat)[None, :] * sg  # [T, 4]
+    for c in range(3):
+        for i in range(4):
+            j[:, 24 + c, i * 3 + c] += ub[:, i]
+            j[:, i * 3 + c, 24 + c] += ub[:, i]
+            j[:, 27 + c, 12 + i * 3 + c] += ub[:, i]
+            j[:, 12 + i * 3 + c, 27 + c] += ub[:, i]
+    r = np.zeros((T, n))
+    r[:, 24:27] = -np.einsum("tq,tqk->tk", wdet, f_q[:, :, 0:3])
+    r[:, 27:30] = -np.einsum("tq,tqk->tk", wdet, f_q[:, :, 3:6])
     return r, j
 
 

@@ -39,6 +39,13 @@ def _const(v):
 COSSERAT_PARAMS = dict(lambda_s=1.3, mu_s=0.7, kappa_s=0.45, lambda_o=0.9, mu_o=1.1, kappa_o=0.35, l=0.8)
 COSSERAT_RHS = (1.0, -2.0, 0.5, 0.3, 0.2, -0.4)
 
+
+def cosserat_rhs(x, y, z):
+    """A load that varies inside the cells (f_u then f_t, [6, N])."""
+    return np.array([COSSERAT_RHS[0] + x, COSSERAT_RHS[1] + y * z, COSSERAT_RHS[2] + np.sin(np.pi * z),
+                     COSSERAT_RHS[3] * x * y, COSSERAT_RHS[4] + 0.0 * x, COSSERAT_RHS[5] + y * y])
+
+
 FORM_FUNCTIONS = {
     "darcy": {
         "kappa": lambda x, y, z: 1.0 + 0.5 * x + 0.25 * y * y + 0.1 * z,
@@ -51,6 +58,6 @@ FORM_FUNCTIONS = {
     },
     "cosserat": {
         **{k: _const(v) for k, v in COSSERAT_PARAMS.items()},
-        "rhs": lambda x, y, z: np.array([np.full(np.shape(x), v) for v in COSSERAT_RHS]),
+        "rhs": cosserat_rhs,
     },
 }

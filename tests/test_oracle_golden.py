@@ -70,7 +70,7 @@ def test_element_forms_match_reference(name):
     through a forward-mode auto_diff stand-in; LCEDualWeakForm.
     evaluate_form_vectorized), cell by cell, with the same coefficient
     functions.  Bar: 1e-13 of the largest entry of the cell."""
-    from tests.cases import COSSERAT_PARAMS, COSSERAT_RHS, FORM_FUNCTIONS
+    from tests.cases import COSSERAT_PARAMS, FORM_FUNCTIONS
     mk, fields = CASES[name]
     m = mk()
     g = golden(name)
@@ -89,7 +89,7 @@ def test_element_forms_match_reference(name):
         elif kind == "elast":
             r, j = forms.elasticity_element(X[c], dim, quad, F["lambda"], F["mu"], F["rhs"])
         else:
-            r, j = forms.cosserat_element(X[c], signs[c], quad, COSSERAT_PARAMS, COSSERAT_RHS[:3], COSSERAT_RHS[3:])
+            r, j = forms.cosserat_element(X[c], signs[c], quad, COSSERAT_PARAMS, F["rhs"], None)
         jr, rr = g["j_el"][c], g["r_el"][c]
         assert j.shape == jr.shape and r.shape == rr.shape
         scale = np.abs(jr).max()

@@ -116,3 +116,24 @@ def test_elasticity_loop_equals_batch():
             # rigid translations are in the kernel
             t = np.tile(np.eye(dim)[0], j1.shape[0] // dim)
             assert np.abs(j1 @ t).max() < 1e-12
+
+
+def test_cosserat_batch_equals_element():
+    """The vectorised Cosserat oracle against the per-cell restatement that the
+    reference's own form pins (load varying inside the cells)."""
+    from oracle import forms, mesh_gen, quadrature, topology
+    from tests.cases import COSSERAT_PARAMS, cosserat_rhs
+    m = mesh_gen.cube(2)
+    topo = topology.Topology(m)
+    X = m["points"][topo.cells]
+    s = topo.rt1_signs()
+    quad = quadrature.make_quadrature(3, 3)
+    from oracle.elements import create_element
+    lam = create_element("P", 3, 1).tabulate(0, quad[0])[0, :, :, 0]
+    xq = np.einsum("qv,tvg->tqg", lam, X)
+    fq = np.moveaxis(cosserat_rhs(xq[..., 0], xq[..., 1], xq[..., 2]), 0, -1)
+    rb, jb = forms.cosserat_batch(X, s, quad, COSSERAT_PARAMS, fq)
+    for c in range(topo.n_cells):
+        r, j = forms.cosserat_element(X[c], s[c], quad, COSSERAT_PARAMS, cosserat_rhs, None)
+        np.testing.assert_allclose(jb[c], j, rtol=0, atol=1e-14 * np.abs(j).max())
+        np.testing.assert_allclose(rb[c], r, rtol=0, atol=1e-14 * np.abs(r).max())
