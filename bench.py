@@ -162,14 +162,20 @@ def _cpu_worker(args):
     return time.perf_counter() - t0, A.nnz
 
 
+_CPU_MESH = {}
+
+
 def cpu_problem(n_side, sample):
     import numpy as np
     from oracle import mesh_gen, topology
     from nfempy_gb300.workloads import darcy3d_coefficients
-    m = mesh_gen.cube(n_side)
-    topo = topology.Topology(m)
-    cd, nd = topology.cell_dofs(topo, [topology.FieldSpec("u", "RT", 1), topology.FieldSpec("p", "P", 0, 1, True)])
-    kappa, f = darcy3d_coefficients(m)
+    if n_side not in _CPU_MESH:  # the oracle's numbering of the mesh, built once
+        m = mesh_gen.cube(n_side)
+        topo = topology.Topology(m)
+        cd, nd = topology.cell_dofs(topo, [topology.FieldSpec("u", "RT", 1),
+                                           topology.FieldSpec("p", "P", 0, 1, True)])
+        _CPU_MESH[n_side] = (m, topo, cd, nd, darcy3d_coefficients(m))
+    m, topo, cd, nd, (kappa, f) = _CPU_MESH[n_side]
     idx = np.linspace(0, topo.n_cells - 1, sample).astype(np.int64)
     X = m["points"][topo.cells[idx]]
     return dict(X=X, signs=topo.rt1_signs()[idx], kappa=kappa[idx], f=f[idx], dest=cd[idx], T=topo.n_cells, n_dof=nd)
@@ -190,6 +196,83 @@ def cpu_rate(prob, workers, pool=None):
     dt = time.perf_counter() - t0
     t_full = dt * prob["T"] / S
     return prob["n_dof"] / t_full, dt
+
+
+def _cpu_vec_worker(job):
+    """Vectorised numpy assembly of a chunk of cells: element matrices of all
+    cells at once (oracle.forms.darcy_batch) scattered into a CSR matrix."""
+    import numpy as np
+    from oracle import assembly, forms, quadrature
+    X, signs, kappa, f, dest, n_dof = job
+    quad = quadrature.make_quadrature(3, 3)
+    Q = len(quad[1])
+    t0 = time.perf_counter()
+    r, j = forms.darcy_batch(X, signs, 3, quad, np.repeat(kappa[:, None], Q, 1), np.repeat(f[:, None], Q, 1))
+    assembly.assemble_csr(dest, j, r, n_dof)
+    return time.perf_counter() - t0
+
+
+def cpu_vectorised(n_side, sample, workers):
+    """Vectorised numpy assembly (oracle.forms.darcy_batch + a COO -> CSR
+    scatter) over `sample` evenly spaced cells, split over `workers` spawn
+    processes; DoF/s extrapolated linearly to the full mesh."""
+    import multiprocessing as mp
+    import numpy as np
+    prob = cpu_problem(n_side, sample)
+    chunks = np.array_split(np.arange(prob["X"].shape[0]), workers)
+    jobs = [(prob["X"][c], prob["signs"][c], prob["kappa"][c], prob["f"][c], prob["dest"][c], prob["n_dof"])
+            for c in chunks]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        pool.map(_cpu_vec_worker, jobs[:workers])  # warm the workers (imports)
+        t0 = time.perf_counter()
+        pool.map(_cpu_vec_worker, jobs)
+        wall = time.perf_counter() - t0
+    rate = prob["n_dof"] / (wall * prob["T"] / prob["X"].shape[0])
+    return {"value": rate, "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": (f"vectorised numpy (oracle.forms.darcy_batch + COO -> CSR scatter) over {prob['X'].shape[0]} "
+                       f"of {prob['T']} cells in {workers} spawn workers, {wall:.2f} s; DoF/s extrapolated")}
+
+
+def cpu_solve_baselines(n_side=16):
+    """Host solves (scipy, FP64): SuperLU on the 2-D 32x32 manufactured Darcy
+    problem, and GMRES(50) with the cell-block Jacobi preconditioner (the plain
+    method) to 1e-8 on 3-D mixed Darcy at n_side^3 x 6 with the bench's field
+    statistics.  Returns the record and the 3-D system for the GPU to solve."""
+    import numpy as np
+    import scipy.sparse.linalg as spla
+    from nfempy_gb300 import meshes
+    from oracle import assembly, forms, mesh_gen, quadrature, solve, topology
+    out = {}
+    m = mesh_gen.square(32)
+    topo = topology.Topology(m)
+    cd, nd = topology.cell_dofs(topo, [topology.FieldSpec("u", "RT", 1), topology.FieldSpec("p", "P", 0, 1, True)])
+    X = m["points"][topo.cells]
+    quad = quadrature.make_quadrature(2, 3)
+    from oracle.elements import create_element
+    lam = create_element("P", 2, 1).tabulate(0, quad[0])[0, :, :, 0]
+    xq = np.einsum("qv,tvg->tqg", lam, X)
+    fq = 2 * np.pi ** 2 * np.sin(np.pi * xq[..., 0]) * np.sin(np.pi * xq[..., 1])
+    r, j = forms.darcy_batch(X, topo.rt1_signs(), 2, quad, np.ones_like(fq), fq)
+    A, res = assembly.assemble_csr(cd, j, r, nd)
+    t0 = time.perf_counter()
+    x = spla.spsolve(A.tocsc(), -res)
+    out["superlu_darcy2d_32x32"] = {"n_dof": nd, "seconds": time.perf_counter() - t0,
+                                    "relres": solve.relative_residual(A, x, -res)}
+    m = mesh_gen.cube(n_side)
+    topo = topology.Topology(m)
+    cd, nd = topology.cell_dofs(topo, [topology.FieldSpec("u", "RT", 1), topology.FieldSpec("p", "P", 0, 1, True)])
+    X = m["points"][topo.cells]
+    quad = quadrature.make_quadrature(3, 3)
+    kappa = np.exp(meshes.grf_log_field(X.mean(axis=1), 0.05, 2.0, 20261208, device="cpu"))
+    T = topo.n_cells
+    r, j = forms.darcy_batch(X, topo.rt1_signs(), 3, quad, np.repeat(kappa[:, None], 8, 1), np.ones((T, 8)))
+    A, res = assembly.assemble_csr(cd, j, r, nd)
+    t0 = time.perf_counter()
+    x, its, rel = solve.gmres_block_jacobi(A, -res, cd, rtol=1e-8, restart=50)
+    out[f"gmres_block_jacobi_darcy3d_{n_side}x6"] = {"n_dof": nd, "seconds": time.perf_counter() - t0,
+                                                     "iterations": its, "relres": rel, "restart": 50}
+    out["cores"] = "scipy (SuperLU and the GMRES loop single-threaded; numpy kernels may use BLAS threads)"
+    return out, (kappa, n_side)
 
 
 def run_reference(args):
@@ -302,6 +385,39 @@ def solve_bench(args, A, wf, coefs, res, stream):
     tl["time_to_solve_incl_host_structure_ms"] = tl["time_to_solve_ms"] + 1e3 * tl["host_structure_s"]
     tl["speedup_vs_plain_incl_host_structure"] = (out["plain_block_jacobi"]["time_to_solve_ms"]
                                                   / tl["time_to_solve_incl_host_structure_ms"])
+    return out
+
+
+def small_system_gpu(args, kappa, n_side):
+    """GPU time to 1e-8 on the host baseline's 16^3 x 6 Darcy system: plain
+    block-Jacobi FGMRES and the two-level preconditioner (setup included;
+    the two-level host structure reported apart)."""
+    import torch
+    import nfempy_gb300 as nf
+    from nfempy_gb300 import workloads as wl
+    from nfempy_gb300.solvers import KrylovSolver, TwoLevelCoarse
+    from nfempy_gb300 import meshes
+    sp = wl.darcy_space(meshes.cube(n_side))
+    A32 = nf.CSRMatrix(sp, dtype=torch.float32)
+    A64 = A32.with_dtype(torch.float64)
+    r32 = torch.empty(A32.n_rows, dtype=torch.float32, device="cuda")
+    r64 = torch.empty(A32.n_rows, dtype=torch.float64, device="cuda")
+    wf = nf.LaplaceDualWeakForm(sp)
+    wf.functions = {"kappa": kappa, "rhs": 1.0}
+    wf.assemble(A32, r32)
+    wf.assemble(A64, r64)
+    b = -r64
+    stream = torch.cuda.current_stream()
+    out = {"n_dof": sp.n_dof}
+    out["plain_block_jacobi"] = _timed_solve(KrylovSolver(A64, pc="cell_block", A32_values=A32.values,
+                                                          restart=args.restart), b, args, stream)
+    t0 = time.perf_counter()
+    tl = TwoLevelCoarse(A64, max(2, n_side // 4))
+    t_struct = time.perf_counter() - t0
+    out["two_level"] = _timed_solve(KrylovSolver(A64, pc="two_level", A32_values=A32.values,
+                                                 restart=args.tl_restart, two_level=tl), b, args, stream,
+                                    two_level=True)
+    out["two_level"]["host_structure_s"] = t_struct
     return out
 
 
@@ -488,9 +604,12 @@ def batch2d_bench(args):
 # ------------------------------------------------------------------ GPU path
 def run_ours(args):
     rank, world, local = env_rank()
-    cpu_prob = None
+    cpu_prob = cpu_vec = cpu_solve = None
     if rank == 0 and not args.no_cpu:
         cpu_prob = cpu_problem(N_SIDE, args.cpu_sample)  # before any CUDA use
+        cpu_vec = cpu_vectorised(N_SIDE, args.cpu_vec_sample, os.cpu_count() or 1)
+        if not args.no_solve:
+            cpu_solve, small = cpu_solve_baselines(16)
     import numpy as np
     import torch
     torch.cuda.set_device(local)
@@ -645,6 +764,9 @@ def run_ours(args):
     solve = None
     if not args.no_solve:
         solve = solve_bench(args, A, wf, coefs, res, stream)
+    if cpu_solve is not None:
+        # the same 16^3 x 6 system solved on the GPU, for a same-size comparison
+        cpu_solve["gpu_same_system"] = small_system_gpu(args, *small)
     workloads = {}
     if not args.no_extra:
         workloads["elasticity_p2_cube40x6"] = elasticity_bench(args)
@@ -696,6 +818,8 @@ def run_ours(args):
                      "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes": alg, "peak_source": peak_kind},
         "cpu_baseline": cpu,
+        "cpu_baseline_vectorised": cpu_vec,
+        "cpu_solve_baseline": cpu_solve,
         "e2e": {"value": job_rate(n_dof, world, e2e_ms), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
                 "mode": "pipelined: kappa, f up and values, residual down every step (two buffer sets, two "
@@ -722,6 +846,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
     ap.add_argument("--cpu-sample", type=int, default=3000)
+    ap.add_argument("--cpu-vec-sample", type=int, default=262144,
+                    help="cells of the vectorised all-core numpy assembly baseline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
