@@ -30,6 +30,7 @@
 // no atomics, no zero-fill pass, deterministic sums.  With a record
 // workspace a cell pass first evaluates each cell's metric terms once, and
 // the row pass reads those records instead of the vertices (two-pass form).
+#include "df64.cuh"
 #include "nfem_common.cuh"
 
 namespace nfem {
@@ -436,6 +437,139 @@ __global__ void __launch_bounds__(256) darcy_records_kernel(const DarcyParams p)
   }
 }
 
+// ------------------------------------------------------------------ FP64 tetrahedra
+// FP64 records of tetrahedra hold the finished flux block, evaluated once
+// per cell in double-float arithmetic on the FP32 pipes (df64.cuh) and
+// packed into FP64 words by integer operations; only the nine edge
+// subtractions run on the FP64 units.  Layout (12 doubles, 96 bytes):
+//   [U00, U01, U02, U03, U11, U12, U13, U22, U23, U33, r_p, 0]
+// U_ab = T120_ab / (30 kappa |det J|) without the orientation signs, with
+//   T120_ab = (tr G + sum G) - 5 (R_a + R_b) + 20 G_ab,
+// R_0 = 0, G_0b = 0 and R_a, G_ab (a, b >= 1) the row sums and entries of
+// G = J^T J for the edges a - 1, b - 1: 120 times element_row's bracket
+// tgs - gma - gmb + gv, so U_ab = scale * bracket with scale = 4 / (kappa
+// |det J|).  The row pass applies the signs by flipping sign bits and adds
+// the two incidences of a face's diagonal (its only FP64 operation).
+
+// position of U_ab (= U_ba) in the record: the upper triangle row by row
+__host__ __device__ constexpr int final_idx(int a, int b) {
+  return (a < b ? a : b) * 4 - (a < b ? a : b) * ((a < b ? a : b) - 1) / 2 + (a < b ? b - a : a - b);
+}
+constexpr int kFinalRp = 10;
+
+template <int SRC>
+__global__ void __launch_bounds__(256) darcy_records_df_kernel(const DarcyParams p) {
+  const double* __restrict__ kappa = static_cast<const double*>(p.kappa);
+  const double* __restrict__ src = static_cast<const double*>(p.source);
+  double* __restrict__ rec = static_cast<double*>(p.rec);
+  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < p.n_cells;
+       c += int64_t(gridDim.x) * blockDim.x) {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+    const int vs[3] = {v.y, v.z, v.w};
+    double x0[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) x0[d] = __ldg(p.points + int64_t(v.x) * 3 + d);
+    dfloat E[3][3];  // E[k][d]: edge k, component d (an exactly rounded FP64 difference)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) E[k][d] = df_from_double(__ldg(p.points + int64_t(vs[k]) * 3 + d) - x0[d]);
+    const double kap = __ldg(kappa + c);
+    check_positive(p.status, kap);
+    double f = 0.0;
+    if constexpr (SRC == NFEM_COEF_CELL) f = __ldg(src + c) * (1.0 / 6.0);
+    if constexpr (SRC == NFEM_COEF_QPOINT) {
+#pragma unroll 4
+      for (int q = 0; q < 32; ++q)
+        if (q < p.n_qp) f += p.qw[q] * __ldg(src + c * p.n_qp + q);
+    }
+    check_finite(p.status, f);
+    const float one[3] = {1.f, 1.f, 1.f};
+    // G = E E^T (edges as rows)
+    dfloat G[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = i; j < 3; ++j) G[i][j] = df_dot<3>(E[i], E[j], one);
+    // |det J| = |E0 . (E1 x E2)|
+    dfloat cr[3];
+    {
+      const float pm[2] = {1.f, -1.f};
+      const dfloat a0[2] = {E[1][1], E[1][2]}, b0[2] = {E[2][2], E[2][1]};
+      const dfloat a1[2] = {E[1][2], E[1][0]}, b1[2] = {E[2][0], E[2][2]};
+      const dfloat a2[2] = {E[1][0], E[1][1]}, b2[2] = {E[2][1], E[2][0]};
+      cr[0] = df_dot<2>(a0, b0, pm);
+      cr[1] = df_dot<2>(a1, b1, pm);
+      cr[2] = df_dot<2>(a2, b2, pm);
+    }
+    const dfloat det = df_abs(df_dot<3>(E[0], cr, one));
+    if (!(det.hi > 0.f)) set_status(p.status, NFEM_ERR_DEGENERATE);
+    // row sums R_i, S = tr G + sum G
+    dfloat R[3];
+    R[0] = df_add(df_add(G[0][0], G[0][1]), G[0][2]);
+    R[1] = df_add(df_add(G[0][1], G[1][1]), G[1][2]);
+    R[2] = df_add(df_add(G[0][2], G[1][2]), G[2][2]);
+    const dfloat trG = df_add(df_add(G[0][0], G[1][1]), G[2][2]);
+    const dfloat S = df_add(trG, df_add(df_add(R[0], R[1]), R[2]));
+    // W = 1 / (30 kappa |det J|)
+    const dfloat W = df_recip(df_mul_f(df_mul(df_from_double(kap), det), 30.f));
+    dfloat R5[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) R5[i] = df_mul_f(R[i], 5.f);
+    double out[12];
+    out[0] = df_to_double(df_mul(W, S));
+#pragma unroll
+    for (int b = 1; b < 4; ++b) out[b] = df_to_double(df_mul(W, df_sub(S, R5[b - 1])));
+#pragma unroll
+    for (int a = 1; a < 4; ++a)
+#pragma unroll
+      for (int b = a; b < 4; ++b) {
+        const dfloat t = df_add(df_sub(S, df_add(R5[a - 1], R5[b - 1])), df_mul_f(G[a - 1][b - 1], 20.f));
+        out[final_idx(a, b)] = df_to_double(df_mul(W, t));
+      }
+    out[kFinalRp] = (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double(df_neg(df_mul(det, df_from_double(f))));
+    out[11] = 0.0;
+    double2* o = reinterpret_cast<double2*>(rec + c * 12);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o[k] = make_double2(out[2 * k], out[2 * k + 1]);
+  }
+}
+
+// Flips the sign of x when neg (a sign-bit operation, no FP64 instruction).
+__device__ __forceinline__ double flip_sign(double x, bool neg) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (static_cast<long long>(neg) << 63));
+}
+
+// Row a of cell c from a finished FP64 record: the four U_ab with the
+// orientation signs, the divergence column, and the pressure row's r_p.
+__device__ __forceinline__ void final_row(const double* __restrict__ rec, int32_t c, uint32_t m, int a,
+                                          double (&vals)[5], double& rhs_val) {
+  using C = DarcyConst<double, 3>;
+  const double* r = rec + int64_t(c) * 12;
+  bool neg[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) neg[i] = (((m >> i) & 1u) != 0) != (C::sigma(i) < 0.0);  // sg_i < 0
+  if (a < 4) {
+    bool na = neg[0];
+#pragma unroll
+    for (int i = 1; i < 4; ++i) na = (a == i) ? neg[i] : na;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      // index of U_ab in the record without local-memory tables
+      int idx = final_idx(0, b);
+#pragma unroll
+      for (int i = 1; i < 4; ++i) idx = (a == i) ? final_idx(i, b) : idx;
+      vals[b] = flip_sign(__ldg(r + idx), na != neg[b]);
+    }
+    vals[4] = na ? 1.0 : -1.0;  // -sg_a
+  } else {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) vals[b] = neg[b] ? -1.0 : 1.0;
+    vals[4] = 0.0;
+    rhs_val += __ldg(r + kFinalRp);
+  }
+}
+
 // Record words of cell c (vector loads: the record is 16-byte aligned); a
 // pressure row (full == false) needs only the chunk holding r_p.
 template <typename T, int DIM>
@@ -666,7 +800,9 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_
     for (int t = 0; t < 2; ++t) {
       if (on[t]) {
         T v[NLOC];
-        if constexpr (REC) {
+        if constexpr (REC && sizeof(T) == 8 && DIM == 3) {
+          final_row(static_cast<const double*>(p.rec), c[t], __ldg(p.sign + c[t]), a[t], v, rhs_val);
+        } else if constexpr (REC) {
           T w[RecLayout<T, DIM>::n];
           load_record<T, DIM>(static_cast<const T*>(p.rec), c[t], a[t] < DIM + 1, w);
           record_row<T, DIM>(w, __ldg(p.sign + c[t]), a[t], v, rhs_val);
@@ -958,7 +1094,11 @@ static int launch_darcy_rows(const DarcyParams& p, cudaStream_t stream) {
 template <typename T, int DIM, int SRC>
 static int launch_darcy_src(const DarcyParams& p, cudaStream_t stream) {
   if (!p.rec) return launch_darcy_rows<T, DIM, SRC, false>(p, stream);
-  if (p.n_cells > 0) darcy_records_kernel<T, DIM, SRC><<<grid_for(p.n_cells, 256), 256, 0, stream>>>(p);
+  if constexpr (sizeof(T) == 8 && DIM == 3) {
+    if (p.n_cells > 0) darcy_records_df_kernel<SRC><<<grid_for(p.n_cells, 256), 256, 0, stream>>>(p);
+  } else {
+    if (p.n_cells > 0) darcy_records_kernel<T, DIM, SRC><<<grid_for(p.n_cells, 256), 256, 0, stream>>>(p);
+  }
   NFEM_CHECK_LAUNCH();
   return launch_darcy_rows<T, DIM, NFEM_COEF_NONE, true>(p, stream);
 }

@@ -1,0 +1,240 @@
+// Double-float arithmetic for the FP64 assembly: a value is the unevaluated
+// sum hi + lo of two FP32 numbers, |lo| <= ulp(hi) / 2 after normalisation,
+// which carries about 48 significant bits.  GB300 issues FP64 operations at
+// a small fraction of its FP32 rate; these routines keep the FP64 path's
+// arithmetic on the FP32 pipes and FP64 only where a value enters or leaves.
+//
+// Building blocks (published methods):
+//   two_sum        Knuth, TAOCP vol. 2, 4.2.2: s + e == a + b exactly;
+//   quick_two_sum  Dekker (1971): the same for |a| >= |b|;
+//   exact products with a fused multiply-add: p = a * b, e = fma(a, b, -p)
+//                  gives p + e == a * b exactly;
+//   reciprocal     one Newton step r' = r + r (1 - x r) from the FP32
+//                  reciprocal, evaluated in double-float.
+// Conversions FP64 <-> double-float are done on the bit patterns with
+// integer operations (no FP64 instruction):
+//   df_from_double  hi = x with its significand cut to 24 bits, lo = the rest
+//                   (the remaining 29 bits rounded to 24): |hi + lo - x| <=
+//                   2^-48 |x|;
+//   df_to_double    the FP64 bit pattern of hi, plus lo counted in units of
+//                   the FP64 ulp of hi, rounded: the nearest FP64 value to
+//                   hi + lo up to half an ulp.
+// The header compiles for the device and for the host (tests check it there
+// against long double).
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define DF_HD __host__ __device__ __forceinline__
+#else
+#define DF_HD inline
+#endif
+
+#if !defined(__CUDA_ARCH__)
+#include <cmath>
+#include <cstring>
+#endif
+
+namespace nfem {
+
+struct dfloat {
+  float hi, lo;
+};
+
+DF_HD uint32_t df_bits(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(x);
+#else
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  return u;
+#endif
+}
+DF_HD float df_float(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float x;
+  std::memcpy(&x, &u, 4);
+  return x;
+#endif
+}
+DF_HD uint64_t df_bits64(double x) {
+#if defined(__CUDA_ARCH__)
+  return static_cast<uint64_t>(__double_as_longlong(x));
+#else
+  uint64_t u;
+  std::memcpy(&u, &x, 8);
+  return u;
+#endif
+}
+DF_HD double df_double(uint64_t u) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double(static_cast<long long>(u));
+#else
+  double x;
+  std::memcpy(&x, &u, 8);
+  return x;
+#endif
+}
+// Rounded FP32 operations that the compiler may not fuse or reorder.
+DF_HD float df_add_rn(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fadd_rn(a, b);
+#else
+  volatile float s = a + b;
+  return s;
+#endif
+}
+DF_HD float df_sub_rn(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fsub_rn(a, b);
+#else
+  volatile float s = a - b;
+  return s;
+#endif
+}
+DF_HD float df_mul_rn(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fmul_rn(a, b);
+#else
+  volatile float s = a * b;
+  return s;
+#endif
+}
+DF_HD float df_fma(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+  return __fmaf_rn(a, b, c);
+#else
+  return std::fmaf(a, b, c);
+#endif
+}
+DF_HD float df_u32_to_float(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint2float_rn(u);
+#else
+  return static_cast<float>(u);  // round to nearest (default mode)
+#endif
+}
+DF_HD int32_t df_float_to_i32(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float2int_rn(x);
+#else
+  return static_cast<int32_t>(std::nearbyint(x));
+#endif
+}
+
+DF_HD dfloat two_sum(float a, float b) {
+  const float s = df_add_rn(a, b);
+  const float bb = df_sub_rn(s, a);
+  const float e = df_add_rn(df_sub_rn(a, df_sub_rn(s, bb)), df_sub_rn(b, bb));
+  return {s, e};
+}
+DF_HD dfloat quick_two_sum(float a, float b) {
+  const float s = df_add_rn(a, b);
+  return {s, df_sub_rn(b, df_sub_rn(s, a))};
+}
+DF_HD dfloat df_make(float x) { return {x, 0.f}; }
+DF_HD dfloat df_neg(dfloat x) { return {-x.hi, -x.lo}; }
+DF_HD dfloat df_abs(dfloat x) { return x.hi < 0.f ? df_neg(x) : x; }
+
+// x + y; error below 2^-47 (|x| + |y|)
+DF_HD dfloat df_add(dfloat x, dfloat y) {
+  dfloat s = two_sum(x.hi, y.hi);
+  return quick_two_sum(s.hi, df_add_rn(s.lo, df_add_rn(x.lo, y.lo)));
+}
+DF_HD dfloat df_sub(dfloat x, dfloat y) { return df_add(x, df_neg(y)); }
+// x * y; relative error below 2^-46
+DF_HD dfloat df_mul(dfloat x, dfloat y) {
+  const float p = df_mul_rn(x.hi, y.hi);
+  float e = df_fma(x.hi, y.hi, -p);
+  e = df_fma(x.hi, y.lo, e);
+  e = df_fma(x.lo, y.hi, e);
+  return quick_two_sum(p, e);
+}
+// x * f for an FP32 f (exact for the small integers used as weights)
+DF_HD dfloat df_mul_f(dfloat x, float f) {
+  const float p = df_mul_rn(x.hi, f);
+  float e = df_fma(x.hi, f, -p);
+  e = df_fma(x.lo, f, e);
+  return quick_two_sum(p, e);
+}
+// sum_k sgn_k a_k b_k over N terms (sgn_k = +-1): exact products of the high
+// parts, their rounding errors and the cross terms collected in FP32
+template <int N>
+DF_HD dfloat df_dot(const dfloat (&a)[N], const dfloat (&b)[N], const float (&sgn)[N]) {
+  float p[N], e[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    const float ah = a[k].hi * sgn[k], al = a[k].lo * sgn[k];  // sign flips are exact
+    p[k] = df_mul_rn(ah, b[k].hi);
+    e[k] = df_fma(ah, b[k].hi, -p[k]);
+    e[k] = df_fma(ah, b[k].lo, e[k]);
+    e[k] = df_fma(al, b[k].hi, e[k]);
+  }
+  dfloat s = {p[0], e[0]};
+#pragma unroll
+  for (int k = 1; k < N; ++k) {
+    const dfloat t = two_sum(s.hi, p[k]);
+    s.hi = t.hi;
+    s.lo = df_add_rn(s.lo, df_add_rn(t.lo, e[k]));
+  }
+  return quick_two_sum(s.hi, s.lo);
+}
+// 1 / x; relative error below 2^-45
+DF_HD dfloat df_recip(dfloat x) {
+  const float r = 1.0f / x.hi;
+  const dfloat xr = df_mul_f(x, r);            // ~ 1
+  const dfloat e = df_sub(df_make(1.0f), xr);  // 1 - x r
+  return df_add(df_make(r), df_mul_f(e, r));   // r + r (1 - x r)
+}
+
+// FP64 -> double-float by bits.  Magnitudes outside the FP32 normal range
+// (below 2^-126 or from 2^128) become 0 and +-inf; the callers' values
+// (coordinates, edge vectors, coefficients) lie well inside it.
+DF_HD dfloat df_from_double(double x) {
+  const uint64_t b = df_bits64(x);
+  const uint32_t sgn = static_cast<uint32_t>(b >> 32) & 0x80000000u;
+  const int32_t e = static_cast<int32_t>((b >> 52) & 0x7ff);
+  const uint64_t m = b & 0xFFFFFFFFFFFFFull;
+  const int32_t fe = e - 896;  // FP32 biased exponent of the same binade
+  if (fe < 1) return {0.f, 0.f};
+  if (fe > 254) return {df_float(sgn | 0x7f800000u), 0.f};
+  const float hi = df_float(sgn | (static_cast<uint32_t>(fe) << 23) | static_cast<uint32_t>(m >> 29));
+  const uint32_t rem = static_cast<uint32_t>(m & 0x1FFFFFFFull);  // rem * 2^(e - 1075)
+  float lo = 0.f;
+  if (rem) {
+    const uint32_t rb = df_bits(df_u32_to_float(rem));
+    const int32_t le = static_cast<int32_t>(rb >> 23) + (e - 1075);
+    if (le > 0) lo = df_float(sgn | (static_cast<uint32_t>(le) << 23) | (rb & 0x7fffffu));
+  }
+  return {hi, lo};
+}
+
+// Normalised double-float (|lo| <= ulp(hi) / 2) -> FP64 by bits.
+DF_HD double df_to_double(dfloat x) {
+  const uint32_t hb = df_bits(x.hi);
+  const int32_t he = static_cast<int32_t>((hb >> 23) & 0xff);
+  if (he == 0) return 0.0;     // |hi| < 2^-126: treated as zero
+  if (he == 255) return x.hi;  // inf / nan pass through
+  uint64_t db = (static_cast<uint64_t>(hb & 0x80000000u) << 32) | (static_cast<uint64_t>(he + 896) << 52) |
+                (static_cast<uint64_t>(hb & 0x7fffffu) << 29);
+  const uint32_t lb = df_bits(x.lo);
+  const int32_t le = static_cast<int32_t>((lb >> 23) & 0xff);
+  if (le == 0) return df_double(db);
+  // lo in units of the FP64 ulp of hi, 2^(he - 127 - 52); one binade lower
+  // (half that unit) when hi is a power of two and lo points below it.  A
+  // normalised lo is below 2^28 such units, less than the distance from the
+  // largest FP32 significand to the next binade, so no carry crosses upward.
+  const bool opposite = ((hb ^ lb) & 0x80000000u) != 0;
+  const bool down = opposite && (hb & 0x7fffffu) == 0;
+  const int32_t ne = le + 179 - he + (down ? 1 : 0);
+  if (ne <= 0) return df_double(db);  // below half an FP64 ulp
+  const int32_t k = df_float_to_i32(df_float((lb & 0x807fffffu) | (static_cast<uint32_t>(ne) << 23)));
+  const int32_t ak = k < 0 ? -k : k;
+  const int64_t step = opposite ? -static_cast<int64_t>(ak) : static_cast<int64_t>(ak);
+  const uint64_t mag = (db & 0x7FFFFFFFFFFFFFFFull) + static_cast<uint64_t>(step);
+  return df_double((db & 0x8000000000000000ull) | mag);
+}
+
+}  // namespace nfem

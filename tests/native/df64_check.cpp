@@ -1,0 +1,49 @@
+// Host check of the double-float routines (nfempy_gb300/csrc/df64.cuh)
+// against long double: random operands over many binades, the largest
+// relative error of each operation printed as "name max_rel".
+#include <cmath>
+#include <cstdio>
+#include <random>
+
+#include "../../nfempy_gb300/csrc/df64.cuh"
+
+using nfem::dfloat;
+static long double val(dfloat x) { return (long double)x.hi + (long double)x.lo; }
+
+int main() {
+  std::mt19937_64 g(20261204);
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  std::uniform_int_distribution<int> ex(-40, 40);
+  auto rnd = [&]() { return std::ldexp(u(g), ex(g)); };
+  long double e_split = 0, e_pack = 0, e_add = 0, e_mul = 0, e_rec = 0, e_dot = 0, e_round = 0;
+  for (int it = 0; it < 200000; ++it) {
+    double a = rnd(), b = rnd(), c = rnd();
+    if (a == 0 || b == 0 || c == 0) continue;
+    dfloat A = nfem::df_from_double(a), B = nfem::df_from_double(b), C = nfem::df_from_double(c);
+    e_split = std::fmax(e_split, std::fabs((val(A) - a) / a));
+    // round trip of a normalised pair through FP64
+    dfloat An = nfem::quick_two_sum(A.hi, A.lo);
+    double back = nfem::df_to_double(An);
+    e_round = std::fmax(e_round, std::fabs(((long double)back - val(An)) / val(An)));
+    long double ra = a, rb = b;
+    dfloat s = nfem::df_add(A, B);
+    e_add = std::fmax(e_add, std::fabs(val(s) - (ra + rb)) / (std::fabs(ra) + std::fabs(rb)));
+    dfloat p = nfem::df_mul(A, B);
+    e_mul = std::fmax(e_mul, std::fabs((val(p) - ra * rb) / (ra * rb)));
+    dfloat r = nfem::df_recip(A);
+    e_rec = std::fmax(e_rec, std::fabs((val(r) - 1.0L / ra) * ra));
+    dfloat x3[3] = {A, B, C}, y3[3] = {C, A, B};
+    float sg[3] = {1.f, -1.f, 1.f};
+    dfloat d = nfem::df_dot<3>(x3, y3, sg);
+    long double td = (long double)a * c - (long double)b * a + (long double)c * b;
+    long double scale = std::fabs((long double)a * c) + std::fabs((long double)b * a) + std::fabs((long double)c * b);
+    e_dot = std::fmax(e_dot, std::fabs(val(d) - td) / scale);
+    // packing of a normalised pair whose hi is a power of two and lo points below it
+    dfloat q = nfem::quick_two_sum(std::ldexp(1.0f, ex(g)), -std::ldexp((float)std::fabs(u(g)), -30 + ex(g)));
+    double qd = nfem::df_to_double(q);
+    e_pack = std::fmax(e_pack, std::fabs(((long double)qd - val(q)) / val(q)));
+  }
+  std::printf("split %.3Le\nround %.3Le\npack %.3Le\nadd %.3Le\nmul %.3Le\nrecip %.3Le\ndot %.3Le\n", e_split,
+              e_round, e_pack, e_add, e_mul, e_rec, e_dot);
+  return 0;
+}

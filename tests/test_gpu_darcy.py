@@ -249,9 +249,11 @@ def test_darcy_chunk_table_and_kernels_agree(cuda_lib):
 @pytest.mark.parametrize("gen,n,qpoint", [("square", 24, False), ("cube", 10, False), ("cube", 6, True)])
 def test_darcy_records_equal_one_pass(cuda_lib, dtype, gen, n, qpoint):
     """The two-pass form (cell records, then rows) writes the single pass's
-    values and residual up to the last bits: the records hold the same
+    values and residual up to the last bits: the FP32 records hold the same
     intermediate quantities and the row pass applies element_row's
-    expressions (the compiler may still fuse a multiply-add differently)."""
+    expressions (the compiler may still fuse a multiply-add differently).
+    FP64 tetrahedra form their records in double-float arithmetic (about 48
+    significant bits, df64.cuh) against the one pass's FP64: 1e-13."""
     m = getattr(mesh_gen, gen)(n)
     T = m["blocks"][-1][1].shape[0]
     rng = np.random.default_rng(4)
@@ -259,6 +261,6 @@ def test_darcy_records_equal_one_pass(cuda_lib, dtype, gen, n, qpoint):
     rhs = f2d if qpoint else rng.normal(0.0, 1.0, T)
     sp, A1, r1 = assemble_gpu(m, kappa, rhs, dtype, use_records=False)
     _, A2, r2 = assemble_gpu(m, kappa, rhs, dtype, use_records=True)
-    tol = 1e-6 if dtype == torch.float32 else 1e-14
+    tol = 1e-6 if dtype == torch.float32 else (1e-13 if gen == "cube" else 1e-14)
     assert row_scaled_err(A1.to_scipy(), A2.to_scipy()) <= tol
     assert ((r1 - r2).abs().max() / r1.abs().max()).item() <= tol
