@@ -421,6 +421,32 @@ def small_system_gpu(args, kappa, n_side):
     return out
 
 
+def assembly_only(args):
+    """The headline assembly alone (64^3 x 6 tets, --precision, --kernel),
+    timed like the main run: the profiling runs capture it."""
+    import torch
+    import nfempy_gb300 as nf
+    from nfempy_gb300 import workloads as wl
+    dtype = torch.float32 if args.precision == "f32" else torch.float64
+    m, sp, kappa, f = wl.darcy3d(N_SIDE)
+    A = nf.CSRMatrix(sp, dtype=dtype)
+    res = torch.empty(A.n_rows, dtype=dtype, device="cuda")
+    wf = nf.LaplaceDualWeakForm(sp)
+    wf.use_chunks = args.kernel == "chunks"
+    wf.use_records = args.kernel == "records"
+    wf.functions = {"kappa": kappa, "rhs": f}
+    coefs = wf.coefficients(dtype)
+    ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
+    A.check_status("assembly")
+    vb = 4 if dtype == torch.float32 else 8
+    alg = algorithmic_bytes(sp.n_cells, m["points"].shape[0], A.nnz, sp.n_dof, vb)
+    peak, kind = measured_peaks()
+    ach = alg / (ms * 1e-3) / 1e9
+    return {"precision": args.precision, "kernel": args.kernel, "ms_per_step": ms, "value": sp.n_dof / (ms * 1e-3),
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "frac": ach / peak, "algorithmic_bytes": alg,
+                         "peak_source": kind}}
+
+
 def solve_only(args):
     """The benchmark system's solves alone (profiling runs): plain block-Jacobi
     and two-level FGMRES on 64^3 x 6 tets, to 1e-8 or --max-iters inner
@@ -691,7 +717,10 @@ def run_ours(args):
         sp.points.copy_(pts_h, non_blocking=True)
         k_d[0].copy_(k_h[0], non_blocking=True)
         f_d[0].copy_(f_h[0], non_blocking=True)
-        _lib.call("nfem_points_split", _lib.ptr(sp.points), V, _lib.ptr(sp.points_split), _lib.stream_ptr())
+        if dtype == torch.float32:
+            _lib.call("nfem_points_split", _lib.ptr(sp.points), V, _lib.ptr(sp.points_split), _lib.stream_ptr())
+        else:
+            _lib.call("nfem_points_fixed64", _lib.ptr(sp.points), V, _lib.ptr(sp.points_fixed64), _lib.stream_ptr())
         wf.assemble(A, res, coefficients=(k_d[0], f_d[0], coefs[2]))
         vals_h[0].copy_(A.values[: A.nnz], non_blocking=True)
         res_h[0].copy_(res, non_blocking=True)
@@ -864,13 +893,13 @@ def main():
                     help="with --only solve: which preconditioners to run")
     ap.add_argument("--kernel", choices=["records", "rows", "chunks"], default="records",
                     help="Darcy assembly: cell records then rows (default), rows alone, or cell chunks")
-    ap.add_argument("--only", choices=["elasticity", "cosserat", "batch2d", "solve"], default=None,
+    ap.add_argument("--only", choices=["assembly", "elasticity", "cosserat", "batch2d", "solve"], default=None,
                     help="time one secondary assembly workload alone and print its record (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.only:
-        fn = {"elasticity": elasticity_bench, "cosserat": cosserat_bench, "batch2d": batch2d_bench,
+        fn = {"assembly": assembly_only, "elasticity": elasticity_bench, "cosserat": cosserat_bench, "batch2d": batch2d_bench,
               "solve": solve_only}[args.only]
         print(json.dumps({"workload": args.only, **fn(args)}), flush=True)
         return

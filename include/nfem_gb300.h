@@ -169,6 +169,17 @@ int nfem_pattern_pairs(const int32_t* inc_ptr, const int32_t* inc, const uint32_
                        int64_t n_rows, int32_t* pairs, uint32_t* pair_codes,
                        int32_t* dev_status, void* stream);
 
+/* Exact 64-bit fixed-point point records for the FP64 assembly of
+ * tetrahedra: records [1 + n_points, 4] int64, 16-byte aligned.  Record 0 =
+ * (shift, 0, 0, 0); record v + 1 = (qx, qy, qz, 0) with q = x * 2^shift
+ * rounded to the nearest integer and shift = 1084 - (biased FP64 exponent
+ * of max |x|), so |q| < 2^62.  No centring: q holds every bit of x at or
+ * above 2^-shift, and an edge vector q1 - q0 is an exact integer difference
+ * (accurate to 2^-62 max |x|), which the FP64 kernels turn into
+ * double-float values with integer operations.  No reference counterpart
+ * (device data layout). */
+int nfem_points_fixed64(const double* points, int64_t n_points, int64_t* records, void* stream);
+
 /* Copies `bytes` from src to dst with a kernel (16-byte vectors when both are
  * 16-byte aligned).  Either pointer may be pinned host memory mapped into the
  * device address space (cudaHostAlloc), so results reach the host without a
@@ -214,7 +225,10 @@ int nfem_points_split(const double* points, int64_t n_points, float* points_spli
  * 4 points on triangles, 8 on tetrahedra; ordering as in the reference).
  * value_type selects FP64 (coordinates `points`) or FP32 (coordinates
  * `points_split` from nfem_points_split); kappa/source/values/rhs then have
- * that type.  flux_dofs [n_cells, dim + 1] are the RT1 DoFs, the pressure DoF
+ * that type.  For FP64 tetrahedra with the record workspace, `points_split`
+ * may instead carry the int64 records of nfem_points_fixed64 (cast to
+ * const float*): the cell pass then forms its edges from them with no FP64
+ * instruction; NULL keeps FP64 subtraction of `points`.  flux_dofs [n_cells, dim + 1] are the RT1 DoFs, the pressure DoF
  * of cell c is p_base + c.  qweights (host, n_qp entries) are the reference
  * quadrature weights, read only when source_mode == NFEM_COEF_QPOINT.
  * row_pairs/pair_codes come from nfem_pattern_rows, nfem_pattern_local_codes and
@@ -273,6 +287,29 @@ int nfem_darcy_l2_error(int dim, int64_t n_cells, const double* points,
                         const double* u_exact_q, const double* p_exact_q, const double* qpoints,
                         const double* qweights, int n_qp, double* errors, void* workspace,
                         size_t workspace_bytes, void* stream);
+
+/* Replaces l2_error (src/postprocess/l2_error_post_processor.py:7-63),
+ * div_error (:185-238), div_scaled_error (:240-306) and, with alpha == NULL,
+ * l2_norm / div_norm (src/postprocess/solution_norms_post_processor.py:7-78)
+ * for one field of a product space on affine simplices, FP64:
+ * *result (device double) = sqrt(sum_cells sum_q |det J| w_q |e - u_h|^2).
+ * family: 0 Lagrange (ref_table [n_qp, n_phi] values), 1 RT1 (ref_table
+ * [n_qp, n_phi, dim] reference values with the reference normal signs,
+ * ref_div [n_phi] their divergences; cell signs from sign_mask).
+ * quantity: 0 values (exact_q [T, n_qp, n_cmp] for Lagrange, components
+ * 0..n_cmp-1; [T, n_qp, n_comp, n_cmp] for the rows of an RT1 field),
+ * 1 divergence of each RT1 row (exact_q [T, n_qp, n_comp]), 2 the scaled
+ * divergence grad l . psi + l div psi (gamma_q [T, n_qp], grad_gamma_q
+ * [T, n_qp, dim]).  The field's local DoFs start at dof_offset in each row
+ * of cell_dofs (basis-major, component-minor).  n_qp <= 32, n_phi <= 10,
+ * n_comp <= 3.  Block partials added in a fixed order (deterministic). */
+int nfem_field_error_workspace_bytes(size_t* bytes);
+int nfem_field_error(int dim, int family, int quantity, int64_t n_cells, const double* points,
+                     const int32_t* cell_vertices, const uint8_t* sign_mask, const int32_t* cell_dofs,
+                     int ld, int dof_offset, int n_phi, int n_comp, int n_cmp, const double* alpha,
+                     const double* exact_q, const double* gamma_q, const double* grad_gamma_q,
+                     const double* ref_table, const double* ref_div, const double* qweights, int n_qp,
+                     double* result, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ------------------------- vector P2 linear elasticity (a12, a13, a15)
  * Replaces LEPrimalWeakForm.evaluate_form

@@ -95,6 +95,10 @@ _SIGS = {
     "nfem_pattern_slots": ([_P, _I64, _I, _I, _P, _P, _P, _P, _P], _I),
     "nfem_pattern_local_codes": ([_P, _I64, _I, _I, _I64, _P, _P, _P, _P, _P, _P, _P], _I),
     "nfem_points_split": ([_P, _I64, _P, _P], _I),
+    "nfem_points_fixed64": ([_P, _I64, _P, _P], _I),
+    "nfem_field_error_workspace_bytes": ([_P], _I),
+    "nfem_field_error": ([_I, _I, _I, _I64, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _I,
+                          _P, _P, _SZ, _P], _I),
     "nfem_pattern_pairs": ([_P, _P, _P, _I64, _P, _P, _P, _P], _I),
     "nfem_darcy_rt1p0_assemble": ([_I, _I, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P, _P, _I,
                                    _P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _SZ, _P, _P], _I),

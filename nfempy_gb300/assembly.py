@@ -302,8 +302,10 @@ class LaplaceDualWeakForm(WeakForm):
                 _lib.call("nfem_darcy_workspace_bytes", sp.dim, vt, sp.n_cells, _lib.C.byref(nb))
                 self._cache[key] = torch.empty(max(int(nb.value), 16), dtype=torch.uint8, device=sp.device)
             ws = self._cache[key]
+        # coordinates: FP32 packed records, or the FP64 fixed-point records
+        split = sp.points_split if dtype == torch.float32 else sp.points_fixed64
         _lib.call("nfem_darcy_rt1p0_assemble", sp.dim, vt, sp.n_cells, jacobian.n_rows,
-                  _lib.ptr(sp.points), _lib.ptr(sp.points_split), _lib.ptr(sp.cells), None,
+                  _lib.ptr(sp.points), _lib.ptr(split), _lib.ptr(sp.cells), None,
                   sp.field_offsets["p"], _lib.ptr(sp.rt_sign_mask), _lib.ptr(kt), _lib.ptr(st), mode,
                   _lib.C.cast(qw, _lib.C.c_void_p), len(wts), _lib.ptr(jacobian.pairs),
                   _lib.ptr(jacobian.pair_codes), _lib.ptr(jacobian.row_ptr),
@@ -691,28 +693,148 @@ class LCEDualWeakForm(WeakForm):
                   _lib.ptr(ws), ws.numel(), _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
 
 
-def l2_error(dim, space, functions, alpha, stream=None):
-    """[||u - u_h||, ||p - p_h||] of a mixed Darcy RT1 x P0 solution, FP64 on the
-    device (src/postprocess/l2_error_post_processor.py:7-63).  functions:
-    {"u": f(x, y, z) -> [dim, N], "p": f(x, y, z) -> [N] or [1, N]}."""
+# ---------------------------------------------------------------- norms
+_RT1_SIGMA = {2: np.array([-1.0, 1.0, -1.0]), 3: np.array([1.0, -1.0, 1.0, -1.0])}
+
+
+def _field_tables(space, name):
+    """(family code, n_phi, reference table, reference divergences) of a field
+    at the space's quadrature points: Lagrange P0/P1/P2 values [Q, n_phi];
+    RT1 values [Q, n_phi, dim] with the reference normal signs (psihat_i =
+    sigma_i kappa (xhat - vhat_i), kappa = 2 on tetrahedra, 1 on triangles)
+    and their divergences."""
+    from .elements import lagrange_p2
+    s = space.discrete_spaces[name]
+    dim = space.dim
+    pts, _ = space.quadrature[dim]
+    if s.family == "Lagrange" and s.k_order in (0, 1, 2):
+        if s.k_order == 0:
+            tab = np.ones((pts.shape[0], 1))
+        elif s.k_order == 1:
+            tab = lagrange_p1_values(dim, pts)
+        else:
+            tab = lagrange_p2(dim, pts)[0]
+        return 0, tab.shape[1], np.ascontiguousarray(tab), None
+    if s.family == "RT" and s.k_order == 1:
+        verts = np.vstack([np.zeros(dim), np.eye(dim)])
+        kap = 2.0 if dim == 3 else 1.0
+        sig = _RT1_SIGMA[dim]
+        psi = kap * sig[None, :, None] * (pts[:, None, :] - verts[None, :, :])
+        return 1, dim + 1, np.ascontiguousarray(psi), np.ascontiguousarray(kap * dim * sig)
+    raise NotImplementedError(f"norms of a {s.family} k={s.k_order} field")
+
+
+def _quad_x(space):
+    pts, _ = space.quadrature[space.dim]
+    lam = lagrange_p1_values(space.dim, pts)
+    return np.einsum("qv,tvg->tqg", lam, space.mesh.points[space.cells_host])
+
+
+def _eval_rows(fn, xq, rows):
+    """f(x, y, z) on the [T, Q] point arrays -> [rows, ..., T, Q] float64."""
+    T, Q = xq.shape[:2]
+    v = np.asarray(fn(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64)
+    return v.reshape(rows, -1, T, Q)
+
+
+def _field_error(space, name, quantity, exact_q, alpha, gamma_q=None, grad_gamma_q=None, stream=None):
     sp = space
+    dim = sp.dim
+    fam, n_phi, tab, div = _field_tables(sp, name)
+    s = sp.discrete_spaces[name]
     pts, wts = sp.quadrature[dim]
-    lam = lagrange_p1_values(dim, pts)
-    xq = np.einsum("qv,tvg->tqg", lam, sp.mesh.points[sp.cells_host])
-    ue = np.asarray(functions["u"](xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64)[:dim]
-    ue = np.ascontiguousarray(np.moveaxis(ue, 0, -1))  # [T, Q, dim]
-    pe = np.asarray(functions["p"](xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).reshape(xq.shape[:2])
+    n_cmp = exact_q.shape[-1] if (fam == 0 or quantity == 0) else 1
     dev = sp.device
-    ue_t = torch.as_tensor(ue, device=dev)
-    pe_t = torch.as_tensor(np.ascontiguousarray(pe), device=dev)
-    a = torch.as_tensor(alpha, dtype=torch.float64, device=dev).contiguous()
-    ws = torch.empty(2 * 304, dtype=torch.float64, device=dev)
-    out = torch.empty(2, dtype=torch.float64, device=dev)
-    qp = np.ascontiguousarray(pts, dtype=np.float64)
-    qw = np.ascontiguousarray(wts, dtype=np.float64)
+    ex = torch.as_tensor(np.ascontiguousarray(exact_q), dtype=torch.float64, device=dev)
+    a = None if alpha is None else torch.as_tensor(alpha, dtype=torch.float64, device=dev).contiguous()
+    g = None if gamma_q is None else torch.as_tensor(np.ascontiguousarray(gamma_q), dtype=torch.float64, device=dev)
+    gg = None if grad_gamma_q is None else torch.as_tensor(np.ascontiguousarray(grad_gamma_q), dtype=torch.float64,
+                                                           device=dev)
+    nb = _lib.C.c_size_t(0)
+    _lib.call("nfem_field_error_workspace_bytes", _lib.C.byref(nb))
+    ws = torch.empty(int(nb.value) // 8 + 1, dtype=torch.float64, device=dev)
+    out = torch.empty(1, dtype=torch.float64, device=dev)
     dp = _lib.C.POINTER(_lib.C.c_double)
-    _lib.call("nfem_darcy_l2_error", dim, sp.n_cells, _lib.ptr(sp.points), _lib.ptr(sp.cells),
-              _lib.ptr(sp.rt_sign_mask), _lib.ptr(sp.cell_dofs), sp.n_loc, _lib.ptr(a), _lib.ptr(ue_t),
-              _lib.ptr(pe_t), qp.ctypes.data_as(dp), qw.ctypes.data_as(dp), len(wts), _lib.ptr(out), _lib.ptr(ws),
-              ws.numel() * 8, _lib.stream_ptr(stream))
-    return out.cpu().numpy().tolist()
+    qw = np.ascontiguousarray(wts, dtype=np.float64)
+    off = sp.field_slices[name].start
+    _lib.call("nfem_field_error", dim, fam, quantity, sp.n_cells, _lib.ptr(sp.points), _lib.ptr(sp.cells),
+              _lib.ptr(sp.rt_sign_mask) if fam == 1 else None, _lib.ptr(sp.cell_dofs), sp.n_loc, off, n_phi, s.n_comp,
+              n_cmp, _lib.ptr(a), _lib.ptr(ex), _lib.ptr(g), _lib.ptr(gg), tab.ctypes.data_as(dp),
+              None if div is None else div.ctypes.data_as(dp), qw.ctypes.data_as(dp), len(wts), _lib.ptr(out),
+              _lib.ptr(ws), ws.numel() * 8, _lib.stream_ptr(stream))
+    return float(out.item())
+
+
+def _value_exact(space, name, fn, xq):
+    s = space.discrete_spaces[name]
+    dim = space.dim
+    if s.family == "Lagrange":
+        v = _eval_rows(fn, xq, 1).reshape(-1, *xq.shape[:2])  # [rows, T, Q]
+        n_cmp = min(dim, s.n_comp, v.shape[0])
+        return np.moveaxis(v[:n_cmp], 0, -1)  # [T, Q, n_cmp]
+    v = _eval_rows(fn, xq, s.n_comp)[:, :dim]  # [n_comp, dim, T, Q]
+    return np.moveaxis(np.moveaxis(v, 0, -1), 0, -1)  # [T, Q, n_comp, dim]
+
+
+def l2_error(dim, space, functions, alpha, skip_fields=(), stream=None):
+    """||u - u_h||_L2 of every field of the space, FP64 on the device, like
+    l2_error (src/postprocess/l2_error_post_processor.py:7-63): Lagrange
+    fields compare components 0..dim-1 (functions[name](x, y, z) -> [n, N]),
+    RT1 fields every row (functions[name] -> [n_comp, 3, N], or [3, N] for one
+    row).  Returns one value per field not in skip_fields, in field order."""
+    sp = space
+    xq = _quad_x(sp)
+    out = []
+    for name in sp.names:
+        if name in skip_fields:
+            continue
+        out.append(_field_error(sp, name, 0, _value_exact(sp, name, functions[name], xq), alpha, stream=stream))
+    return out
+
+
+def l2_norm(dim, space, functions, skip_fields=(), stream=None):
+    """||u||_L2 of the exact fields (solution_norms_post_processor.py:7-39),
+    on the device: the l2_error kernel with no discrete solution."""
+    return l2_error(dim, space, functions, None, skip_fields, stream)
+
+
+def _rt_fields(space, skip_fields):
+    return [n for n in space.names if space.discrete_spaces[n].family == "RT" and n not in skip_fields]
+
+
+def div_error(dim, space, functions, alpha, skip_fields=(), stream=None):
+    """||div u - div u_h||_L2 of every RT field (l2_error_post_processor.py:
+    185-238); functions["div_" + name](x, y, z) -> [n_comp, N] (or [N])."""
+    sp = space
+    xq = _quad_x(sp)
+    out = []
+    for name in _rt_fields(sp, skip_fields):
+        nc = sp.discrete_spaces[name].n_comp
+        ex = np.moveaxis(_eval_rows(functions["div_" + name], xq, nc).reshape(nc, *xq.shape[:2]), 0, -1)
+        out.append(_field_error(sp, name, 1, ex, alpha, stream=stream))
+    return out
+
+
+def div_norm(dim, space, functions, skip_fields=(), stream=None):
+    """||div u||_L2 of the exact RT fields (solution_norms_post_processor.py:42-78)."""
+    return div_error(dim, space, functions, None, skip_fields, stream)
+
+
+def div_scaled_error(dim, space, functions, alpha, skip_fields=(), stream=None):
+    """||div(l u) - div(l u_h)|| style error of l2_error_post_processor.py:
+    240-306: the discrete divergence is grad l . psi + l div psi with
+    functions["l"](x, y, z) -> [N] and functions["grad_l"] -> [dim, N]; an
+    empty list when either is missing (as the reference skips)."""
+    sp = space
+    if functions.get("l") is None or functions.get("grad_l") is None:
+        return []
+    xq = _quad_x(sp)
+    T, Q = xq.shape[:2]
+    gam = _eval_rows(functions["l"], xq, 1).reshape(T, Q)
+    ggam = np.moveaxis(_eval_rows(functions["grad_l"], xq, 1).reshape(-1, T, Q)[:sp.dim], 0, -1)
+    out = []
+    for name in _rt_fields(sp, skip_fields):
+        nc = sp.discrete_spaces[name].n_comp
+        ex = np.moveaxis(_eval_rows(functions["div_" + name], xq, nc).reshape(nc, T, Q), 0, -1)
+        out.append(_field_error(sp, name, 2, ex, alpha, gam, ggam, stream=stream))
+    return out

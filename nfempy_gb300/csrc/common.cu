@@ -386,6 +386,58 @@ extern "C" int nfem_points_split(const double* points, int64_t n_points, float* 
   return NFEM_OK;
 }
 
+// ---------------------------------------------------------------- fixed64
+// Exact 64-bit fixed-point records for the FP64 assembly of tetrahedra:
+// x = q * 2^-shift with shift = 1084 - (biased exponent of max |x|), so
+// |q| < 2^62 and no centring: q holds every bit of x at or above 2^-shift
+// (all of them for |x| >= 2^-10 max |x|, otherwise x is rounded to 2^-63
+// max |x|), and an edge q1 - q0 is an exact integer difference.
+__global__ void absmax_bits_kernel(const double* __restrict__ p, int64_t n3, unsigned long long* __restrict__ out) {
+  unsigned long long m = 0ull;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n3; i += int64_t(gridDim.x) * blockDim.x) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(p[i])) & 0x7FFFFFFFFFFFFFFFull;
+    m = b > m ? b : m;  // ordered like |x| for non-negative finite values
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, m, o);
+    m = y > m ? y : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// header record: shift from the maximum parked in rec[1] by absmax_bits_kernel
+__global__ void fixed64_header_kernel(int64_t* __restrict__ rec) {
+  const unsigned long long amax = static_cast<unsigned long long>(rec[1]);
+  const int e = int((amax >> 52) & 0x7ff);
+  rec[0] = amax == 0ull ? 0 : 1084 - e;
+  rec[1] = rec[2] = rec[3] = 0;
+}
+
+__global__ void fixed64_points_kernel(const double* __restrict__ p, int64_t n, int64_t* __restrict__ rec) {
+  const int shift = int(rec[0]);
+  for (int64_t v = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; v < n; v += int64_t(gridDim.x) * blockDim.x) {
+    longlong2* out = reinterpret_cast<longlong2*>(rec + 4 * (v + 1));
+    out[0] = make_longlong2(__double2ll_rn(scalbn(p[3 * v], shift)), __double2ll_rn(scalbn(p[3 * v + 1], shift)));
+    out[1] = make_longlong2(__double2ll_rn(scalbn(p[3 * v + 2], shift)), 0);
+  }
+}
+
+extern "C" int nfem_points_fixed64(const double* points, int64_t n_points, int64_t* records, void* stream_) {
+  if (n_points < 0 || !records || (n_points > 0 && !points)) return NFEM_ERR_INVALID_ARG;
+  if (n_points > INT32_MAX) return NFEM_ERR_OVERFLOW;
+  if (reinterpret_cast<uintptr_t>(records) & 15) return NFEM_ERR_INVALID_ARG;
+  cudaStream_t stream = (cudaStream_t)stream_;
+  NFEM_TRY_CUDA(cudaMemsetAsync(records, 0, 4 * sizeof(int64_t), stream));
+  if (n_points > 0)
+    absmax_bits_kernel<<<grid_for(3 * n_points, 256), 256, 0, stream>>>(
+        points, 3 * n_points, reinterpret_cast<unsigned long long*>(records + 1));
+  fixed64_header_kernel<<<1, 1, 0, stream>>>(records);
+  if (n_points > 0) fixed64_points_kernel<<<grid_for(n_points, 256), 256, 0, stream>>>(points, n_points, records);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
 extern "C" int nfem_exclusive_scan_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, void* stream) {
   if (n < 0 || !offsets || (n > 0 && !counts)) return NFEM_ERR_INVALID_ARG;
   if (n > kNoAllocMaxCounts) return NFEM_ERR_CAPACITY;

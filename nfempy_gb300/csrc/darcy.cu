@@ -75,6 +75,7 @@ struct DarcyParams {
   int n_qp;
   double qw[32];
   void* rec;  // per-cell records of the two-pass path (NULL: single pass)
+  const int64_t* fixed;  // FP64 tetrahedra: nfem_points_fixed64 records (NULL: FP64 edge subtraction)
 };
 
 template <typename T, int DIM>
@@ -466,24 +467,49 @@ __global__ void __launch_bounds__(256) darcy_records_df_kernel(const DarcyParams
        c += int64_t(gridDim.x) * blockDim.x) {
     const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
     const int vs[3] = {v.y, v.z, v.w};
-    double x0[3];
+    dfloat E[3][3];  // E[k][d]: edge k, component d
+    if (p.fixed) {
+      // exact integer differences of the fixed-point records, converted by
+      // integer operations (no FP64 instruction)
+      const int shift = int(__ldg(p.fixed));
+      const longlong2* R = reinterpret_cast<const longlong2*>(p.fixed);
+      const longlong2 a0 = __ldg(R + 2 * (int64_t(v.x) + 1)), a1 = __ldg(R + 2 * (int64_t(v.x) + 1) + 1);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) x0[d] = __ldg(p.points + int64_t(v.x) * 3 + d);
-    dfloat E[3][3];  // E[k][d]: edge k, component d (an exactly rounded FP64 difference)
+      for (int k = 0; k < 3; ++k) {
+        const longlong2 b0 = __ldg(R + 2 * (int64_t(vs[k]) + 1)), b1 = __ldg(R + 2 * (int64_t(vs[k]) + 1) + 1);
+        E[k][0] = df_from_i64(b0.x - a0.x, shift);
+        E[k][1] = df_from_i64(b0.y - a0.y, shift);
+        E[k][2] = df_from_i64(b1.x - a1.x, shift);
+      }
+    } else {  // exactly rounded FP64 differences
+      double x0[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
+      for (int d = 0; d < 3; ++d) x0[d] = __ldg(p.points + int64_t(v.x) * 3 + d);
 #pragma unroll
-      for (int d = 0; d < 3; ++d) E[k][d] = df_from_double(__ldg(p.points + int64_t(vs[k]) * 3 + d) - x0[d]);
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) E[k][d] = df_from_double(__ldg(p.points + int64_t(vs[k]) * 3 + d) - x0[d]);
+    }
+    // coefficient checks on the bit patterns
     const double kap = __ldg(kappa + c);
-    check_positive(p.status, kap);
-    double f = 0.0;
-    if constexpr (SRC == NFEM_COEF_CELL) f = __ldg(src + c) * (1.0 / 6.0);
+    if (!df_bits_positive(kap)) set_status(p.status, df_bits_finite(kap) ? NFEM_ERR_DOMAIN : NFEM_ERR_NONFINITE);
+    dfloat F = df_make(0.f);  // the source integrated over the reference cell
+    if constexpr (SRC == NFEM_COEF_CELL) {
+      const double s = __ldg(src + c);
+      if (!df_bits_finite(s)) set_status(p.status, NFEM_ERR_NONFINITE);
+      // 1/6 as a double-float constant (its FP32 part and the remainder)
+      constexpr float kSixthHi = float(1.0 / 6.0);
+      constexpr float kSixthLo = float(1.0 / 6.0 - double(kSixthHi));
+      F = df_mul(df_from_double(s), dfloat{kSixthHi, kSixthLo});
+    }
     if constexpr (SRC == NFEM_COEF_QPOINT) {
+      double f = 0.0;
 #pragma unroll 4
       for (int q = 0; q < 32; ++q)
         if (q < p.n_qp) f += p.qw[q] * __ldg(src + c * p.n_qp + q);
+      if (!df_bits_finite(f)) set_status(p.status, NFEM_ERR_NONFINITE);
+      F = df_from_double(f);
     }
-    check_finite(p.status, f);
     const float one[3] = {1.f, 1.f, 1.f};
     // G = E E^T (edges as rows)
     dfloat G[3][3];
@@ -527,7 +553,7 @@ __global__ void __launch_bounds__(256) darcy_records_df_kernel(const DarcyParams
         const dfloat t = df_add(df_sub(S, df_add(R5[a - 1], R5[b - 1])), df_mul_f(G[a - 1][b - 1], 20.f));
         out[final_idx(a, b)] = df_to_double(df_mul(W, t));
       }
-    out[kFinalRp] = (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double(df_neg(df_mul(det, df_from_double(f))));
+    out[kFinalRp] = (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double(df_neg(df_mul(det, F)));
     out[11] = 0.0;
     double2* o = reinterpret_cast<double2*>(rec + c * 12);
 #pragma unroll
@@ -1201,6 +1227,11 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   p.n_qp = source_mode == NFEM_COEF_QPOINT ? n_qp : 0;
   for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
   p.rec = nullptr;
+  p.fixed = nullptr;
+  if (value_type == NFEM_F64 && points_split) {
+    if (reinterpret_cast<uintptr_t>(points_split) & 15) return NFEM_ERR_INVALID_ARG;
+    p.fixed = reinterpret_cast<const int64_t*>(points_split);
+  }
   if (workspace && !chunk_rows) {
     size_t need = 0;
     nfem_darcy_workspace_bytes(dim, value_type, n_cells, &need);

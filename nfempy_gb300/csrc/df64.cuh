@@ -211,6 +211,47 @@ DF_HD dfloat df_from_double(double x) {
   return {hi, lo};
 }
 
+DF_HD int df_clz64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return __clzll(static_cast<long long>(x));
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+// The integer d times 2^-shift as a double-float, by integer operations:
+// hi = the leading 24 bits of |d|, lo = the next 24 (both truncated, so
+// |hi + lo - d 2^-shift| < 2^-47 |d 2^-shift|).  Results below the FP32
+// normal range become 0.
+DF_HD dfloat df_from_i64(int64_t d, int shift) {
+  if (d == 0) return {0.f, 0.f};
+  const uint32_t sgn = d < 0 ? 0x80000000u : 0u;
+  const uint64_t a = d < 0 ? static_cast<uint64_t>(-(d + 1)) + 1u : static_cast<uint64_t>(d);
+  const int lz = df_clz64(a);
+  const uint64_t n = a << lz;            // leading bit at position 63
+  const int e = 63 - lz - shift + 127;   // FP32 biased exponent of the leading bit
+  if (e < 1) return {0.f, 0.f};
+  const float hi = df_float(sgn | (static_cast<uint32_t>(e) << 23) | static_cast<uint32_t>((n >> 40) & 0x7fffffu));
+  const uint64_t rem = n << 24;          // the 40 bits after the leading 24
+  float lo = 0.f;
+  if (rem) {
+    const int lz2 = df_clz64(rem);
+    const uint64_t n2 = rem << lz2;
+    const int e2 = e - 24 - lz2;
+    if (e2 >= 1) lo = df_float(sgn | (static_cast<uint32_t>(e2) << 23) | static_cast<uint32_t>((n2 >> 40) & 0x7fffffu));
+  }
+  return {hi, lo};
+}
+
+// Bit tests on an FP64 value (no FP64 instruction): finite; finite and > 0
+// with a magnitude inside the FP32 normal range of the double-float code.
+DF_HD bool df_bits_finite(double x) { return ((df_bits64(x) >> 52) & 0x7ff) != 0x7ff; }
+DF_HD bool df_bits_positive(double x) {
+  const uint64_t b = df_bits64(x);
+  const int e = static_cast<int>((b >> 52) & 0x7ff);
+  return (b >> 63) == 0 && e > 896 && e < 1151;
+}
+
 // Normalised double-float (|lo| <= ulp(hi) / 2) -> FP64 by bits.
 DF_HD double df_to_double(dfloat x) {
   const uint32_t hb = df_bits(x.hi);

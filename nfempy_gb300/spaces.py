@@ -166,6 +166,10 @@ class ProductSpace:
         self.points = torch.as_tensor(mesh.points, dtype=torch.float64, device=dev).contiguous()
         self.points_split = torch.empty((mesh.points.shape[0] + 1, 4), dtype=torch.float32, device=dev)
         _lib.call("nfem_points_split", _lib.ptr(self.points), mesh.points.shape[0], _lib.ptr(self.points_split), st)
+        # exact 64-bit fixed-point records for the FP64 kernels of tetrahedra
+        self.points_fixed64 = torch.empty((mesh.points.shape[0] + 1, 4), dtype=torch.int64, device=dev)
+        _lib.call("nfem_points_fixed64", _lib.ptr(self.points), mesh.points.shape[0], _lib.ptr(self.points_fixed64),
+                  st)
         # boundary facets of the mesh file (all tagged lower-dimensional blocks)
         facet_blocks, facets_first, seen_cells = [], 1, False
         for typ, conn, phys in mesh.data["blocks"]:

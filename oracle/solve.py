@@ -93,3 +93,53 @@ def gmres_block_jacobi(A, b, cell_dofs, rtol=1e-8, restart=50, maxiter=20000):
         if rel <= rtol or its[0] == before:
             break
     return x, its[0], rel
+
+
+def field_error(family, dim, quad, X, signs, dest, n_comp, degree, alpha, exact, quantity="value",
+                scale=None, grad_scale=None):
+    """One field's error norm, restating the reference's per-cell loops:
+      value, Lagrange   l2_error Lagrange branch (l2_error_post_processor.py:35-40),
+                        components 0..dim-1, exact vectorised over the points;
+      value, RT         vector branch (:41-59), exact called point by point,
+                        [n_comp, 3] per point, its first dim columns compared;
+      "div"             div_error (:185-238): trace of the oriented reference
+                        gradients / det J, exact per point [n_comp];
+      "div_scaled"      div_scaled_error (:240-306): grad l . psi + l div psi.
+    X [T, d+1, 3], signs [T, d+1] (RT), dest [T, n_phi * n_comp] the field's
+    DoFs of each cell, alpha the global solution (None: the exact norm, as in
+    solution_norms_post_processor.py:7-78)."""
+    from .forms import tabulate_oriented
+    from .geometry import evaluate_mapping
+    pts, wts = quad
+    total = 0.0
+    fam = "P" if family == "Lagrange" else family
+    for c in range(X.shape[0]):
+        x, J, det, pinv = evaluate_mapping(dim, pts, X[c])
+        tab = tabulate_oriented(fam, dim, degree, pts, J, det, pinv, signs[c] if fam == "RT" else None,
+                                discontinuous=(fam == "P" and degree == 0))
+        n_phi = tab.shape[2]
+        a = np.zeros(len(dest[c])) if alpha is None else np.asarray(alpha)[dest[c]]
+        a_star = np.array(np.split(a, n_phi))  # [n_phi, n_comp]
+        if quantity == "value" and fam == "P":
+            fe = np.asarray(exact(x[:, 0], x[:, 1], x[:, 2]), dtype=np.float64).reshape(-1, len(wts))[0:dim, :]
+            fh = (tab[0, :, :, 0] @ a_star[:, 0:dim]).T
+            total += np.sum(det * wts * (fe - fh) * (fe - fh))
+        elif quantity == "value":
+            fe = np.array([np.asarray(exact(xv[0], xv[1], xv[2]), dtype=np.float64).reshape(n_comp, -1)
+                           for xv in x])[:, :, 0:dim]
+            fh = np.array([np.vstack([tab[0, k, :, 0:dim].T @ a_star[:, cc] for cc in range(n_comp)])
+                           for k in range(len(pts))])
+            d = fe - fh
+            total += np.sum(det * wts * np.array([np.trace(e.T @ e) for e in d]))
+        else:
+            grad = tab[1:dim + 1, :, :, 0:dim]
+            div = np.trace(grad, axis1=0, axis2=3).T * (1.0 / det)  # [n_phi, Q]
+            if quantity == "div_scaled":
+                gam = np.ravel(scale(x[:, 0], x[:, 1], x[:, 2])) * np.ones(len(wts))
+                ggam = np.asarray(grad_scale(x[:, 0], x[:, 1], x[:, 2]), dtype=np.float64).reshape(-1, len(wts))
+                div = np.array([[np.trace(np.outer(ggam[:dim, i], tab[0, i, j, 0:dim])) for i in range(len(pts))]
+                                for j in range(n_phi)]) + div * gam[None, :]
+            fe = np.array([np.asarray(exact(xv[0], xv[1], xv[2]), dtype=np.float64).reshape(n_comp) for xv in x])
+            fh = div.T @ a_star
+            total += np.sum(((fe - fh) * (fe - fh)).T @ (det * wts))
+    return float(np.sqrt(total))

@@ -15,7 +15,9 @@ int main() {
   std::uniform_real_distribution<double> u(-1.0, 1.0);
   std::uniform_int_distribution<int> ex(-40, 40);
   auto rnd = [&]() { return std::ldexp(u(g), ex(g)); };
-  long double e_split = 0, e_pack = 0, e_add = 0, e_mul = 0, e_rec = 0, e_dot = 0, e_round = 0;
+  long double e_split = 0, e_pack = 0, e_add = 0, e_mul = 0, e_rec = 0, e_dot = 0, e_round = 0, e_i64 = 0;
+  std::uniform_int_distribution<int64_t> iq(-(int64_t(1) << 62), int64_t(1) << 62);
+  std::uniform_int_distribution<int> sh(0, 120);
   for (int it = 0; it < 200000; ++it) {
     double a = rnd(), b = rnd(), c = rnd();
     if (a == 0 || b == 0 || c == 0) continue;
@@ -38,12 +40,20 @@ int main() {
     long double td = (long double)a * c - (long double)b * a + (long double)c * b;
     long double scale = std::fabs((long double)a * c) + std::fabs((long double)b * a) + std::fabs((long double)c * b);
     e_dot = std::fmax(e_dot, std::fabs(val(d) - td) / scale);
+    // fixed-point integers over all magnitudes (shifted right by a random amount of bits)
+    int64_t qi = iq(g) >> (it % 62);
+    int shift = sh(g);
+    if (qi != 0) {
+      dfloat Q = nfem::df_from_i64(qi, shift);
+      long double want = std::ldexp((long double)qi, -shift);
+      e_i64 = std::fmax(e_i64, std::fabs((val(Q) - want) / want));
+    }
     // packing of a normalised pair whose hi is a power of two and lo points below it
     dfloat q = nfem::quick_two_sum(std::ldexp(1.0f, ex(g)), -std::ldexp((float)std::fabs(u(g)), -30 + ex(g)));
     double qd = nfem::df_to_double(q);
     e_pack = std::fmax(e_pack, std::fabs(((long double)qd - val(q)) / val(q)));
   }
-  std::printf("split %.3Le\nround %.3Le\npack %.3Le\nadd %.3Le\nmul %.3Le\nrecip %.3Le\ndot %.3Le\n", e_split,
-              e_round, e_pack, e_add, e_mul, e_rec, e_dot);
+  std::printf("split %.9Le\nround %.9Le\npack %.9Le\nadd %.9Le\nmul %.9Le\nrecip %.9Le\ndot %.9Le\ni64 %.9Le\n",
+              e_split, e_round, e_pack, e_add, e_mul, e_rec, e_dot, e_i64);
   return 0;
 }

@@ -1,6 +1,7 @@
 """The double-float routines of the FP64 assembly (nfempy_gb300/csrc/df64.cuh)
 compiled for the host with g++ and checked against long double: FP64 ->
-double-float split within 2^-48, the packing back to FP64 to half an ulp,
+double-float split within 2^-48, 64-bit fixed-point integers within
+2^-47, the packing back to FP64 to half an ulp,
 add / multiply / reciprocal / 3-term dot products within 2^-44 (operand
 splits included).  No GPU needed."""
 import os
@@ -23,7 +24,7 @@ def test_df64_routines_against_long_double():
                        check=True)
         out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
     err = {k: float(v) for k, v in (line.split() for line in out.strip().splitlines())}
-    assert err["split"] <= 2.0 ** -48
+    assert err["split"] <= 2.0 ** -48 and err["i64"] <= 2.0 ** -47
     assert err["round"] <= 2.0 ** -53 and err["pack"] <= 2.0 ** -53
     for k in ("add", "mul", "recip", "dot"):
         assert err[k] <= 2.0 ** -44, (k, err[k])

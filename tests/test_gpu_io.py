@@ -54,3 +54,30 @@ def test_points_split_records(cuda_lib, n_points):
     assert np.abs(q).max() < 2 ** 30
     rec = q * scale + c[None, :]
     assert np.abs(rec - pts).max() <= 0.5 * scale * (1 + 1e-9)
+
+
+@pytest.mark.parametrize("n_points", [1, 5, 1000])
+def test_points_fixed64_records(cuda_lib, n_points):
+    """64-bit fixed-point records of the FP64 kernels: x = q 2^-shift with
+    |q| < 2^62; coordinates of a uniform grid and every FP64 coordinate of
+    at least 2^-10 max |x| are held exactly, the rest to within 2^-63 max |x|."""
+    from fractions import Fraction
+    rng = np.random.default_rng(n_points)
+    pts = rng.uniform(-3.0, 5.0, size=(n_points, 3))
+    pts[0] = [0.0, 1.0 / 64, 1e-9]  # a grid coordinate and a tiny one
+    p = torch.as_tensor(pts, device="cuda")
+    out = torch.empty((n_points + 1, 4), dtype=torch.int64, device="cuda")
+    _lib.call("nfem_points_fixed64", _lib.ptr(p), n_points, _lib.ptr(out), _lib.stream_ptr())
+    torch.cuda.synchronize()
+    o = out.cpu().numpy()
+    shift = int(o[0, 0])
+    q = o[1:, :3]
+    assert np.abs(q).max() < 2 ** 62 and np.abs(q).max() >= 2 ** 61
+    amax = np.abs(pts).max()
+    for v in range(n_points):
+        for d in range(3):
+            err = abs(Fraction(int(q[v, d]), 2 ** shift) - Fraction(pts[v, d]))
+            if abs(pts[v, d]) >= amax / 1024:
+                assert err == 0, (v, d)
+            else:
+                assert err <= Fraction(amax) / 2 ** 63

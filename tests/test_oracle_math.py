@@ -137,3 +137,21 @@ def test_cosserat_batch_equals_element():
         r, j = forms.cosserat_element(X[c], s[c], quad, COSSERAT_PARAMS, cosserat_rhs, None)
         np.testing.assert_allclose(jb[c], j, rtol=0, atol=1e-14 * np.abs(j).max())
         np.testing.assert_allclose(rb[c], r, rtol=0, atol=1e-14 * np.abs(r).max())
+
+
+def test_field_error_matches_darcy_l2():
+    """The per-field restatement of l2_error equals the Darcy-specific one."""
+    m, topo, cd, nd, X, s, quad, xq = darcy_problem(2, 6)
+    rng = np.random.default_rng(2)
+    alpha = rng.normal(size=nd)
+
+    def u_ex(x, y, z):
+        return np.array([np.sin(x) + y, x * y, 0.0 * x])
+
+    def p_ex(x, y, z):
+        return np.array([np.cos(x + y)])
+
+    want = solve.l2_error_darcy(X, s, 2, quad, cd, alpha, u_ex, p_ex)
+    eu = solve.field_error("RT", 2, quad, X, s, cd[:, :3], 1, 1, alpha, u_ex)
+    ep = solve.field_error("Lagrange", 2, quad, X, s, cd[:, 3:], 1, 0, alpha, p_ex)
+    np.testing.assert_allclose([eu, ep], want, rtol=1e-13)
