@@ -390,8 +390,8 @@ extern "C" int nfem_points_split(const double* points, int64_t n_points, float* 
 // Exact 64-bit fixed-point records for the FP64 assembly of tetrahedra:
 // x = q * 2^-shift with shift = 1084 - (biased exponent of max |x|), so
 // |q| < 2^62 and no centring: q holds every bit of x at or above 2^-shift
-// (all of them for |x| >= 2^-10 max |x|, otherwise x is rounded to 2^-63
-// max |x|), and an edge q1 - q0 is an exact integer difference.
+// (all of them for |x| >= 2^-10 max |x|, otherwise x is rounded to within
+// 2^-62 max |x|), and an edge q1 - q0 is an exact integer difference.
 __global__ void absmax_bits_kernel(const double* __restrict__ p, int64_t n3, unsigned long long* __restrict__ out) {
   unsigned long long m = 0ull;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n3; i += int64_t(gridDim.x) * blockDim.x) {

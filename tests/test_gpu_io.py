@@ -60,7 +60,7 @@ def test_points_split_records(cuda_lib, n_points):
 def test_points_fixed64_records(cuda_lib, n_points):
     """64-bit fixed-point records of the FP64 kernels: x = q 2^-shift with
     |q| < 2^62; coordinates of a uniform grid and every FP64 coordinate of
-    at least 2^-10 max |x| are held exactly, the rest to within 2^-63 max |x|."""
+    at least 2^-10 max |x| are held exactly, the rest to within 2^-62 max |x|."""
     from fractions import Fraction
     rng = np.random.default_rng(n_points)
     pts = rng.uniform(-3.0, 5.0, size=(n_points, 3))
@@ -80,4 +80,4 @@ def test_points_fixed64_records(cuda_lib, n_points):
             if abs(pts[v, d]) >= amax / 1024:
                 assert err == 0, (v, d)
             else:
-                assert err <= Fraction(amax) / 2 ** 63
+                assert err <= Fraction(amax) / 2 ** 62
