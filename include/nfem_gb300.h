@@ -263,6 +263,44 @@ int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t 
  * vertices.  The workspace is 16-byte aligned, of at least this size. */
 int nfem_darcy_workspace_bytes(int dim, int value_type, int64_t n_cells, size_t* bytes);
 
+/* Overlapped form of nfem_darcy_rt1p0_assemble for tetrahedra (same
+ * reference interface, same values up to rounding): the mesh is cut into
+ * K = ceil(n_cells / 2^slice_shift) slices of consecutive cells and the
+ * assembly runs as K + 1 launches on `stream`, each writing the rows of one
+ * slice while a quarter-share of its blocks forms the cell records of the
+ * slice two ahead.  The records live in `ring` (three slices, from
+ * nfem_darcy_ring_bytes), small enough to stay in L2, so the cell pass and
+ * the row pass overlap and the records never travel to HBM and back.
+ * Needs the first-appearance layout of a mixed RT1 x P0 space (flux rows
+ * [0, p_base), pressure row p_base + c of cell c), the pairs / pair_codes /
+ * row_ptr of nfem_pattern_pairs, and a host plan:
+ *   flux_row_begin [K + 1] (host): first flux row whose first incidence
+ *     lies in slice k (the chunk table of nfem_pattern_darcy_chunks at the
+ *     slice starts), flux_row_begin[K] = p_base;
+ *   lookahead_cells: the largest (second incidence cell - first incidence
+ *     cell) over the flux rows, which must be below 2^slice_shift
+ *     (NFEM_ERR_UNSUPPORTED otherwise);
+ *   record_quarters (1..3): quarters of the blocks of a launch that form
+ *     records while the others write rows.
+ * point_records: nfem_points_split records (FP32) or nfem_points_fixed64
+ * records (FP64; NULL: FP64 subtraction of `points`). */
+typedef struct {
+  int32_t slice_shift;
+  int32_t lookahead_cells;
+  int32_t record_quarters;
+  const int64_t* flux_row_begin;
+} nfem_darcy_slices;
+int nfem_darcy_ring_bytes(int value_type, int slice_shift, size_t* bytes);
+int nfem_darcy_rt1p0_assemble_sliced(int value_type, int64_t n_cells, int64_t n_rows,
+                                     const double* points, const void* point_records,
+                                     const int32_t* cell_vertices, int64_t p_base,
+                                     const uint8_t* sign_mask, const void* kappa, const void* source,
+                                     int source_mode, const double* qweights, int n_qp,
+                                     const int32_t* row_pairs, const uint32_t* pair_codes,
+                                     const int32_t* row_ptr, const nfem_darcy_slices* slices,
+                                     void* values, void* rhs, int accumulate, void* ring,
+                                     size_t ring_bytes, int32_t* dev_status, void* stream);
+
 /* Replaces LaplaceDualWeakFormBCDirichlet.evaluate_form
  * (src/weak_forms/laplace_dual_weak_form.py:90-154) with its scatter: adds
  * int_F p_D (psi_f . n) to the residual entry of each boundary facet's flux

@@ -39,6 +39,11 @@ class DofBlock(C.Structure):
     _fields_ = [("occ_rank", C.c_void_p), ("n_ent", C.c_int32), ("width", C.c_int32), ("base", C.c_int64)]
 
 
+class DarcySlices(C.Structure):
+    _fields_ = [("slice_shift", C.c_int32), ("lookahead_cells", C.c_int32), ("record_quarters", C.c_int32),
+                ("flux_row_begin", C.c_void_p)]
+
+
 class Csr(C.Structure):
     _fields_ = [("n_rows", C.c_int64), ("row_ptr", C.c_void_p), ("col_idx", C.c_void_p), ("values", C.c_void_p),
                 ("value_type", C.c_int)]
@@ -103,6 +108,9 @@ _SIGS = {
     "nfem_darcy_rt1p0_assemble": ([_I, _I, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P, _P, _I,
                                    _P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _SZ, _P, _P], _I),
     "nfem_darcy_workspace_bytes": ([_I, _I, _I64, C.POINTER(_SZ)], _I),
+    "nfem_darcy_ring_bytes": ([_I, _I, C.POINTER(_SZ)], _I),
+    "nfem_darcy_rt1p0_assemble_sliced": ([_I, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _I, _P, _I, _P, _P, _P,
+                                          C.POINTER(DarcySlices), _P, _P, _I, _P, _SZ, _P, _P], _I),
     "nfem_pattern_darcy_chunks": ([_P, _I64, _I, _I64, _I64, _P, _P, _P], _I),
     "nfem_copy_bytes": ([_P, _P, _SZ, _P], _I),
     "nfem_spmv": ([_I, _I64, _P, _P, _P, _P, _P, _P], _I),

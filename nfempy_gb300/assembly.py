@@ -86,6 +86,14 @@ class CSRMatrix:
                                                       _lib.ptr(cst), st)
             if rc == _lib.NFEM_OK and int(cst.item()) == 0:
                 self.chunk_rows = cr
+                # host copy of the chunk table and the largest distance between
+                # a flux row's two cells: the plan of the overlapped assembly
+                self.chunk_rows_host = cr.cpu().numpy().astype(np.int64)
+                p_base = space.field_offsets[space.names[1]]
+                pr = self.pairs[:p_base].long()
+                two = pr[:, 1] >= 0
+                gap = (pr[two, 1] // n_loc - pr[two, 0] // n_loc)
+                self.lookahead_cells = int(gap.max().item()) if gap.numel() else 0
         self.values = torch.zeros(max(self.nnz, 1), dtype=dtype, device=dev)
         self.fresh = True
         self.check_status("pattern")
@@ -225,6 +233,12 @@ class LaplaceDualWeakForm(WeakForm):
 
     use_chunks = False
     use_records = None
+    # overlapped assembly of tetrahedra (nfem_darcy_rt1p0_assemble_sliced):
+    # slices of at least 2^min_slice_shift cells, record_quarters blocks of
+    # every four forming records while the others write rows
+    use_slices = True
+    min_slice_shift = 17
+    record_quarters = {torch.float64: 2, torch.float32: 1}
 
     def _check_space(self):
         sp = self.space
@@ -291,6 +305,17 @@ class LaplaceDualWeakForm(WeakForm):
         kt, st, mode = coefficients if coefficients is not None else self.coefficients(dtype)
         pts, wts = sp.quadrature[sp.dim]
         qw = (_lib.C.c_double * len(wts))(*wts.tolist())
+        split = sp.points_split if dtype == torch.float32 else sp.points_fixed64
+        if (self.use_slices and not self.use_chunks and self.use_records is not False and sp.dim == 3
+                and getattr(jacobian, "chunk_rows_host", None) is not None):
+            plan, ring = self._slice_plan(jacobian, dtype, vt)
+            _lib.call("nfem_darcy_rt1p0_assemble_sliced", vt, sp.n_cells, jacobian.n_rows, _lib.ptr(sp.points),
+                      _lib.ptr(split), _lib.ptr(sp.cells), sp.field_offsets["p"], _lib.ptr(sp.rt_sign_mask),
+                      _lib.ptr(kt), _lib.ptr(st), mode, _lib.C.cast(qw, _lib.C.c_void_p), len(wts),
+                      _lib.ptr(jacobian.pairs), _lib.ptr(jacobian.pair_codes), _lib.ptr(jacobian.row_ptr),
+                      _lib.C.byref(plan), _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate),
+                      _lib.ptr(ring), ring.numel(), _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+            return
         ws = None
         records = self.use_records
         if records is None:
@@ -302,8 +327,6 @@ class LaplaceDualWeakForm(WeakForm):
                 _lib.call("nfem_darcy_workspace_bytes", sp.dim, vt, sp.n_cells, _lib.C.byref(nb))
                 self._cache[key] = torch.empty(max(int(nb.value), 16), dtype=torch.uint8, device=sp.device)
             ws = self._cache[key]
-        # coordinates: FP32 packed records, or the FP64 fixed-point records
-        split = sp.points_split if dtype == torch.float32 else sp.points_fixed64
         _lib.call("nfem_darcy_rt1p0_assemble", sp.dim, vt, sp.n_cells, jacobian.n_rows,
                   _lib.ptr(sp.points), _lib.ptr(split), _lib.ptr(sp.cells), None,
                   sp.field_offsets["p"], _lib.ptr(sp.rt_sign_mask), _lib.ptr(kt), _lib.ptr(st), mode,
@@ -312,6 +335,28 @@ class LaplaceDualWeakForm(WeakForm):
                   _lib.ptr(jacobian.chunk_rows if self.use_chunks else None), _lib.ptr(jacobian.values),
                   _lib.ptr(residual), int(accumulate), _lib.ptr(ws), 0 if ws is None else ws.numel(),
                   _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+
+    def _slice_plan(self, jacobian, dtype, vt):
+        """(nfem_darcy_slices, ring workspace) of the overlapped assembly,
+        built once per matrix pattern and precision."""
+        key = ("slices", dtype, id(jacobian.chunk_rows_host))
+        if key not in self._cache:
+            sp = self.space
+            need = max(5, int(jacobian.lookahead_cells).bit_length())  # 2^shift > lookahead
+            shift = max(need, int(self.min_slice_shift))
+            S = 1 << shift
+            K = -(-sp.n_cells // S)
+            cr = jacobian.chunk_rows_host
+            F = np.array([cr[k * S // 32] for k in range(K)] + [sp.field_offsets["p"]], dtype=np.int64)
+            nb = _lib.C.c_size_t(0)
+            _lib.call("nfem_darcy_ring_bytes", vt, shift, _lib.C.byref(nb))
+            ring = torch.empty(int(nb.value), dtype=torch.uint8, device=sp.device)
+            plan = _lib.DarcySlices(shift, int(jacobian.lookahead_cells), 1, F.ctypes.data)
+            self._cache[key] = (plan, ring, F)
+        plan, ring, F = self._cache[key]
+        rq = self.record_quarters
+        plan.record_quarters = int(rq[dtype] if isinstance(rq, dict) else rq)
+        return plan, ring
 
     def evaluate_form(self, element_index, alpha):
         raise NotImplementedError(

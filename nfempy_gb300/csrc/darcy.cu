@@ -30,6 +30,8 @@
 // no atomics, no zero-fill pass, deterministic sums.  With a record
 // workspace a cell pass first evaluates each cell's metric terms once, and
 // the row pass reads those records instead of the vertices (two-pass form).
+#include <algorithm>
+
 #include "df64.cuh"
 #include "nfem_common.cuh"
 
@@ -76,7 +78,23 @@ struct DarcyParams {
   double qw[32];
   void* rec;  // per-cell records of the two-pass path (NULL: single pass)
   const int64_t* fixed;  // FP64 tetrahedra: nfem_points_fixed64 records (NULL: FP64 edge subtraction)
+  // Work ranges of one launch: the cell pass covers cells [cell_begin,
+  // cell_end); the row pass covers the rows [row_f0, row_f1) and then
+  // [row_q0, row_q1) (flux rows and pressure rows of one cell slice, or all
+  // rows in one range).  ring_shift >= 0: the records live in a ring of
+  // three slices of 2^ring_shift cells (see rec_index).
+  int64_t cell_begin, cell_end;
+  int64_t row_f0, row_f1, row_q0, row_q1;
+  int ring_shift;
 };
+
+// Position of cell c's record: c itself, or its place in the ring of three
+// slices of 2^ring_shift cells that the overlapped assembly keeps in L2.
+__device__ __forceinline__ int64_t rec_index(const DarcyParams& p, int64_t c) {
+  if (p.ring_shift < 0) return c;
+  const int64_t s = c >> p.ring_shift;
+  return ((s % 3) << p.ring_shift) | (c & ((int64_t(1) << p.ring_shift) - 1));
+}
 
 template <typename T, int DIM>
 struct DarcyConst;
@@ -427,15 +445,21 @@ __device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, co
 
 // One cell per thread and iteration (two in flight per thread measured
 // slower: 100.8 against 96.0 us for the whole FP32 assembly at 64^3 x 6).
+// Thread `t` of `nt` takes cells cell_begin + t, + nt, ... (the body of the
+// cell-pass kernel and of the cell-pass blocks of the slice kernel).
 template <typename T, int DIM, int SRC>
-__global__ void __launch_bounds__(256) darcy_records_kernel(const DarcyParams p) {
+__device__ __forceinline__ void records_cells(const DarcyParams& p, int64_t t, int64_t nt) {
   const T u = edge_unit<T>(p);
-  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < p.n_cells;
-       c += int64_t(gridDim.x) * blockDim.x) {
+  for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
     Incidence<T, DIM> x;
     load_incidence<T, DIM, SRC>(p, int32_t(c), true, x);
-    write_record<T, DIM, SRC>(p, c, x, u);
+    write_record<T, DIM, SRC>(p, rec_index(p, c), x, u);
   }
+}
+
+template <typename T, int DIM, int SRC>
+__global__ void __launch_bounds__(256) darcy_records_kernel(const DarcyParams p) {
+  records_cells<T, DIM, SRC>(p, blockIdx.x * int64_t(blockDim.x) + threadIdx.x, int64_t(gridDim.x) * blockDim.x);
 }
 
 // ------------------------------------------------------------------ FP64 tetrahedra
@@ -459,12 +483,11 @@ __host__ __device__ constexpr int final_idx(int a, int b) {
 constexpr int kFinalRp = 10;
 
 template <int SRC>
-__global__ void __launch_bounds__(256) darcy_records_df_kernel(const DarcyParams p) {
+__device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t, int64_t nt) {
   const double* __restrict__ kappa = static_cast<const double*>(p.kappa);
   const double* __restrict__ src = static_cast<const double*>(p.source);
   double* __restrict__ rec = static_cast<double*>(p.rec);
-  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < p.n_cells;
-       c += int64_t(gridDim.x) * blockDim.x) {
+  for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
     const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
     const int vs[3] = {v.y, v.z, v.w};
     dfloat E[3][3];  // E[k][d]: edge k, component d
@@ -555,10 +578,15 @@ __global__ void __launch_bounds__(256) darcy_records_df_kernel(const DarcyParams
       }
     out[kFinalRp] = (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double(df_neg(df_mul(det, F)));
     out[11] = 0.0;
-    double2* o = reinterpret_cast<double2*>(rec + c * 12);
+    double2* o = reinterpret_cast<double2*>(rec + rec_index(p, c) * 12);
 #pragma unroll
     for (int k = 0; k < 6; ++k) o[k] = make_double2(out[2 * k], out[2 * k + 1]);
   }
+}
+
+template <int SRC>
+__global__ void __launch_bounds__(256) darcy_records_df_kernel(const DarcyParams p) {
+  records_df_cells<SRC>(p, blockIdx.x * int64_t(blockDim.x) + threadIdx.x, int64_t(gridDim.x) * blockDim.x);
 }
 
 // Flips the sign of x when neg (a sign-bit operation, no FP64 instruction).
@@ -568,7 +596,7 @@ __device__ __forceinline__ double flip_sign(double x, bool neg) {
 
 // Row a of cell c from a finished FP64 record: the four U_ab with the
 // orientation signs, the divergence column, and the pressure row's r_p.
-__device__ __forceinline__ void final_row(const double* __restrict__ rec, int32_t c, uint32_t m, int a,
+__device__ __forceinline__ void final_row(const double* __restrict__ rec, int64_t c, uint32_t m, int a,
                                           double (&vals)[5], double& rhs_val) {
   using C = DarcyConst<double, 3>;
   const double* r = rec + int64_t(c) * 12;
@@ -721,9 +749,9 @@ struct RowHead {
   uint2 cd;
 };
 
-__device__ __forceinline__ RowHead load_head(const DarcyParams& p, int64_t r) {
+__device__ __forceinline__ RowHead load_head(const DarcyParams& p, int64_t r, int64_t end) {
   RowHead h;
-  if (r < p.n_rows) {
+  if (r < end) {
     h.pr = __ldg(reinterpret_cast<const int2*>(p.pairs) + r);
     h.cd = __ldg(reinterpret_cast<const uint2*>(p.pair_codes) + r);
   } else {
@@ -749,37 +777,54 @@ __device__ __forceinline__ int row_len_from_codes(const RowHead& h) {
   return len;
 }
 
-template <typename T, int DIM, int SRC, bool REC = false>
-__global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_MIN_BLOCKS : 1)
-    darcy_rows_kernel(const DarcyParams p) {
+// Block `rank` of `n_blocks` row blocks (kDarcyWarps warps each) writes the
+// 32-row chunks rank * kDarcyWarps + warp, + n_blocks * kDarcyWarps, ...;
+// st is the warp's staging buffer of 32 * kDarcyMaxRow values.
+template <typename T, int DIM, int SRC, bool REC>
+__device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t rank, int64_t n_blocks) {
   constexpr int NLOC = DIM + 2;
   constexpr int VEC = 16 / int(sizeof(T));  // values per 16 bytes
-  __shared__ __align__(16) T stage[kDarcyWarps][32 * kDarcyMaxRow];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* st = stage[warp];
   T* values = static_cast<T*>(p.values);
   T* rhs = static_cast<T*>(p.rhs);
-  const int64_t stride = int64_t(gridDim.x) * kDarcyWarps * 32;
-
-  int64_t r0 = (int64_t(blockIdx.x) * kDarcyWarps + warp) * 32;
-  // row_ptr of the lane's row and of the row after the chunk (clamped to n_rows)
-  auto rp_at = [&](int64_t r) { return __ldg(p.row_ptr + (r < p.n_rows ? r : p.n_rows)); };
-  RowHead head = load_head(p, r0 + lane);
-  int32_t rp_lane = rp_at(r0 + lane), rp_end = rp_at(r0 + 32);
+  // chunks of 32 rows: first over [row_f0, row_f1), then over [row_q0, row_q1)
+  const int64_t nfc = (p.row_f1 - p.row_f0 + 31) / 32, nqc = (p.row_q1 - p.row_q0 + 31) / 32;
+  const int64_t n_chunks = nfc + nqc;
+  const int64_t jstride = n_blocks * kDarcyWarps;
+  auto chunk_range = [&](int64_t j, int64_t& rb, int64_t& re) {
+    if (j < nfc) {
+      rb = p.row_f0 + 32 * j;
+      re = p.row_f1;
+    } else if (j < n_chunks) {
+      rb = p.row_q0 + 32 * (j - nfc);
+      re = p.row_q1;
+    } else {
+      rb = re = p.n_rows;
+    }
+  };
+  int64_t j = rank * kDarcyWarps + warp;
+  int64_t rb, re;
+  chunk_range(j, rb, re);
+  // row_ptr of the lane's row and of the row after the chunk (clamped to the range end)
+  auto rp_at = [&](int64_t r, int64_t e) { return __ldg(p.row_ptr + (r < e ? r : e)); };
+  RowHead head = load_head(p, rb + lane, re);
+  int32_t rp_lane = rp_at(rb + lane, re), rp_end = rp_at(rb + 32, re);
   const bool bulk = NFEM_DARCY_BULK && !p.accumulate && (reinterpret_cast<uintptr_t>(values) & 15) == 0;
-  for (; r0 < p.n_rows; r0 += stride) {
+  for (; j < n_chunks; j += jstride) {
     if (bulk) {  // the staging buffer is free once the last bulk store has read it
       if (lane == 0) bulk_wait_read();
       __syncwarp();
     }
+    const int64_t r0 = rb;
     const int64_t r = r0 + lane;
-    const bool valid = r < p.n_rows;
+    const bool valid = r < re;
     const RowHead h = head;
     const int32_t rpl = rp_lane, rpe = rp_end;
     // prefetch the next chunk of this warp (overlaps its latency with this one)
-    head = load_head(p, r0 + stride + lane);
-    rp_lane = rp_at(r0 + stride + lane);
-    rp_end = rp_at(r0 + stride + 32);
+    chunk_range(j + jstride, rb, re);
+    head = load_head(p, rb + lane, re);
+    rp_lane = rp_at(rb + lane, re);
+    rp_end = rp_at(rb + 32, re);
     const int32_t base = __shfl_sync(0xffffffffu, rpl, 0);
 
     const int occ[2] = {h.pr.x, h.pr.y};
@@ -827,10 +872,10 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_
       if (on[t]) {
         T v[NLOC];
         if constexpr (REC && sizeof(T) == 8 && DIM == 3) {
-          final_row(static_cast<const double*>(p.rec), c[t], __ldg(p.sign + c[t]), a[t], v, rhs_val);
+          final_row(static_cast<const double*>(p.rec), rec_index(p, c[t]), __ldg(p.sign + c[t]), a[t], v, rhs_val);
         } else if constexpr (REC) {
           T w[RecLayout<T, DIM>::n];
-          load_record<T, DIM>(static_cast<const T*>(p.rec), c[t], a[t] < DIM + 1, w);
+          load_record<T, DIM>(static_cast<const T*>(p.rec), int32_t(rec_index(p, c[t])), a[t] < DIM + 1, w);
           record_row<T, DIM>(w, __ldg(p.sign + c[t]), a[t], v, rhs_val);
         } else {
           Incidence<T, DIM> x;
@@ -881,6 +926,39 @@ __global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_
   if (bulk && lane == 0) bulk_wait_all();
 }
 
+template <typename T, int DIM, int SRC, bool REC = false>
+__global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_MIN_BLOCKS : 1)
+    darcy_rows_kernel(const DarcyParams p) {
+  __shared__ __align__(16) T stage[kDarcyWarps][32 * kDarcyMaxRow];
+  rows_body<T, DIM, SRC, REC>(p, stage[threadIdx.x >> 5], blockIdx.x, gridDim.x);
+}
+
+// ------------------------------------------------------------------ slices
+// One launch of the overlapped assembly of tetrahedra: the blocks of every
+// group of four split into rec_quarters blocks running the cell pass over
+// [cell_begin, cell_end) (the records of a later slice, compute bound) and
+// 4 - rec_quarters blocks writing the rows of the current slice from
+// records made by earlier launches (bandwidth bound), so the two passes run
+// side by side on every SM.  No block waits for another.
+template <typename T, int SRC>
+__global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_MIN_BLOCKS : 1)
+    darcy_slice_kernel(const DarcyParams p, int rec_quarters) {
+  __shared__ __align__(16) T stage[kDarcyWarps][32 * kDarcyMaxRow];
+  const int64_t group = blockIdx.x >> 2, n_groups = gridDim.x >> 2;
+  const int sub = int(blockIdx.x & 3);
+  if (sub < rec_quarters) {
+    const int64_t rank = group * rec_quarters + sub, nb = n_groups * rec_quarters;
+    const int64_t t = rank * blockDim.x + threadIdx.x, nt = nb * blockDim.x;
+    if constexpr (sizeof(T) == 8)
+      records_df_cells<SRC>(p, t, nt);
+    else
+      records_cells<T, 3, SRC>(p, t, nt);
+  } else {
+    const int64_t rank = group * (4 - rec_quarters) + (sub - rec_quarters), nb = n_groups * (4 - rec_quarters);
+    rows_body<T, 3, NFEM_COEF_NONE, true>(p, stage[threadIdx.x >> 5], rank, nb);
+  }
+}
+
 // ------------------------------------------------------------------ cell chunks
 // Cell-chunk variant of the same assembly, one chunk of 32 consecutive cells
 // per warp.  Rows are numbered by first appearance, so the flux rows whose
@@ -926,7 +1004,7 @@ __device__ __forceinline__ void warp_chunk_rows(const DarcyParams& p, WarpChunk<
   for (int64_t r0 = first; r0 < last; r0 += 32) {
     const int64_t r = r0 + lane;
     const bool valid = r < last;
-    const RowHead h = load_head(p, valid ? r : p.n_rows);
+    const RowHead h = load_head(p, valid ? r : p.n_rows, p.n_rows);
     // row lengths and offsets from row_ptr (every lane joins the shuffles)
     const int32_t rpl = __ldg(p.row_ptr + (r < p.n_rows ? r : p.n_rows));
     const int32_t rpe = __ldg(p.row_ptr + (r0 + 32 < last ? r0 + 32 : last));
@@ -1109,7 +1187,8 @@ static int launch_darcy_rows(const DarcyParams& p, cudaStream_t stream) {
       n = 4;
     return n;
   }();
-  const int grid = grid_for(ceil_div(p.n_rows, 32 * kDarcyWarps), 1, per_sm);
+  const int64_t chunks = ceil_div(p.row_f1 - p.row_f0, 32) + ceil_div(p.row_q1 - p.row_q0, 32);
+  const int grid = grid_for(ceil_div(chunks, kDarcyWarps), 1, per_sm);
   darcy_rows_kernel<T, DIM, SRC, REC><<<grid, block, 0, stream>>>(p);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
@@ -1127,6 +1206,49 @@ static int launch_darcy_src(const DarcyParams& p, cudaStream_t stream) {
   }
   NFEM_CHECK_LAUNCH();
   return launch_darcy_rows<T, DIM, NFEM_COEF_NONE, true>(p, stream);
+}
+
+// The overlapped assembly: K = ceil(T / S) slices of S = 2^shift cells,
+// K + 1 launches.  Launch 0 forms the records of slices 0 and 1; launch
+// k + 1 writes the rows of slice k (its flux rows [F_k, F_k+1) and pressure
+// rows) while forming the records of slice k + 2.  A row's cells lie in its
+// slice or the next (the host checks lookahead < S), whose records earlier
+// launches made; records of slice k + 2 take the ring place of slice k - 1,
+// whose rows the previous launch wrote.
+template <typename T, int SRC>
+static int launch_darcy_sliced(DarcyParams p, int shift, const int64_t* flux_begin, int rec_quarters,
+                               cudaStream_t stream) {
+  static const int per_sm = [] {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, darcy_slice_kernel<T, SRC>, 32 * kDarcyWarps, 0) !=
+            cudaSuccess ||
+        n < 1)
+      n = 4;
+    return n;
+  }();
+  const int64_t S = int64_t(1) << shift, T_ = p.n_cells, K = ceil_div(T_, S);
+  int grid = grid_for(int64_t(1) << 40, 1, per_sm);
+  grid = grid < 4 ? 4 : grid & ~3;
+  const int64_t p_base = p.row_q0;
+  for (int64_t l = 0; l <= K; ++l) {
+    const int64_t k = l - 1;  // slice whose rows this launch writes
+    p.cell_begin = l == 0 ? 0 : std::min((l + 1) * S, T_);
+    p.cell_end = std::min((l == 0 ? 2 : l + 2) * S, T_);
+    if (k >= 0) {
+      p.row_f0 = flux_begin[k];
+      p.row_f1 = flux_begin[k + 1];
+      p.row_q0 = p_base + k * S;
+      p.row_q1 = p_base + std::min((k + 1) * S, T_);
+    } else {
+      p.row_f0 = p.row_f1 = p.row_q0 = p.row_q1 = 0;
+    }
+    const bool has_rec = p.cell_end > p.cell_begin, has_rows = k >= 0;
+    if (!has_rec && !has_rows) continue;
+    const int q = !has_rows ? 4 : (!has_rec ? 0 : rec_quarters);
+    darcy_slice_kernel<T, SRC><<<grid, 32 * kDarcyWarps, 0, stream>>>(p, q);
+    NFEM_CHECK_LAUNCH();
+  }
+  return NFEM_OK;
 }
 
 template <typename T, int DIM, int SRC>
@@ -1228,6 +1350,12 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
   p.rec = nullptr;
   p.fixed = nullptr;
+  p.cell_begin = 0;
+  p.cell_end = n_cells;
+  p.row_f0 = 0;
+  p.row_f1 = n_rows;
+  p.row_q0 = p.row_q1 = 0;
+  p.ring_shift = -1;
   if (value_type == NFEM_F64 && points_split) {
     if (reinterpret_cast<uintptr_t>(points_split) & 15) return NFEM_ERR_INVALID_ARG;
     p.fixed = reinterpret_cast<const int64_t*>(points_split);
@@ -1242,6 +1370,93 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   if (value_type == NFEM_F64)
     return dim == 3 ? launch_darcy<double, 3>(p, source_mode, stream) : launch_darcy<double, 2>(p, source_mode, stream);
   return dim == 3 ? launch_darcy<float, 3>(p, source_mode, stream) : launch_darcy<float, 2>(p, source_mode, stream);
+}
+
+extern "C" int nfem_darcy_ring_bytes(int value_type, int slice_shift, size_t* bytes) {
+  if (!bytes || (value_type != NFEM_F64 && value_type != NFEM_F32) || slice_shift < 5 || slice_shift > 30)
+    return NFEM_ERR_INVALID_ARG;
+  // three slices of records: 12 doubles (FP64) or 8 floats (FP32) per tetrahedron
+  *bytes = size_t(3) << slice_shift;
+  *bytes *= value_type == NFEM_F64 ? 12 * sizeof(double) : 8 * sizeof(float);
+  return NFEM_OK;
+}
+
+extern "C" int nfem_darcy_rt1p0_assemble_sliced(int value_type, int64_t n_cells, int64_t n_rows,
+                                                const double* points, const void* point_records,
+                                                const int32_t* cell_vertices, int64_t p_base,
+                                                const uint8_t* sign_mask, const void* kappa, const void* source,
+                                                int source_mode, const double* qweights, int n_qp,
+                                                const int32_t* row_pairs, const uint32_t* pair_codes,
+                                                const int32_t* row_ptr, const nfem_darcy_slices* slices,
+                                                void* values, void* rhs, int accumulate, void* ring,
+                                                size_t ring_bytes, int32_t* dev_status, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n_cells < 0 || n_rows < 0 || !slices) return NFEM_ERR_INVALID_ARG;
+  if (n_rows == 0) return NFEM_OK;
+  if (!cell_vertices || !sign_mask || !kappa || !row_pairs || !pair_codes || !row_ptr || !values || !rhs ||
+      !slices->flux_row_begin || p_base < 0 || p_base + n_cells != n_rows)
+    return NFEM_ERR_INVALID_ARG;
+  if (value_type == NFEM_F32 && (!point_records || (reinterpret_cast<uintptr_t>(point_records) & 15)))
+    return NFEM_ERR_INVALID_ARG;
+  if (value_type == NFEM_F64 && !points && !point_records) return NFEM_ERR_INVALID_ARG;
+  if (point_records && (reinterpret_cast<uintptr_t>(point_records) & 15)) return NFEM_ERR_INVALID_ARG;
+  if (source_mode != NFEM_COEF_NONE && !source) return NFEM_ERR_INVALID_ARG;
+  if (source_mode == NFEM_COEF_QPOINT && (!qweights || n_qp < 1 || n_qp > 32)) return NFEM_ERR_INVALID_ARG;
+  if ((reinterpret_cast<uintptr_t>(cell_vertices) & 15) || (reinterpret_cast<uintptr_t>(row_pairs) & 7) ||
+      (reinterpret_cast<uintptr_t>(pair_codes) & 7))
+    return NFEM_ERR_INVALID_ARG;
+  const int shift = slices->slice_shift;
+  size_t need = 0;
+  if (nfem_darcy_ring_bytes(value_type, shift, &need) != NFEM_OK) return NFEM_ERR_INVALID_ARG;
+  if (!ring || ring_bytes < need || (reinterpret_cast<uintptr_t>(ring) & 15)) return NFEM_ERR_WORKSPACE;
+  // every row's cells must lie in its slice or the next one
+  if (slices->lookahead_cells < 0 || int64_t(slices->lookahead_cells) >= (int64_t(1) << shift))
+    return NFEM_ERR_UNSUPPORTED;
+  const int q = slices->record_quarters;
+  if (q < 1 || q > 3) return NFEM_ERR_INVALID_ARG;
+  const int64_t K = ceil_div(n_cells, int64_t(1) << shift);
+  const int64_t* F = slices->flux_row_begin;
+  if (F[0] != 0 || F[K] != p_base) return NFEM_ERR_INVALID_ARG;
+  for (int64_t k = 0; k < K; ++k)
+    if (F[k + 1] < F[k]) return NFEM_ERR_INVALID_ARG;
+  DarcyParams p;
+  p.n_rows = n_rows;
+  p.n_cells = n_cells;
+  p.p_base = p_base;
+  p.chunk_rows = nullptr;
+  p.points = points;
+  p.split = value_type == NFEM_F32 ? static_cast<const float*>(point_records) : nullptr;
+  p.fixed = value_type == NFEM_F64 ? static_cast<const int64_t*>(point_records) : nullptr;
+  p.cv = cell_vertices;
+  p.sign = sign_mask;
+  p.kappa = kappa;
+  p.source = source;
+  p.pairs = row_pairs;
+  p.pair_codes = pair_codes;
+  p.row_ptr = row_ptr;
+  p.values = values;
+  p.rhs = rhs;
+  p.status = dev_status;
+  p.accumulate = accumulate != 0;
+  p.n_qp = source_mode == NFEM_COEF_QPOINT ? n_qp : 0;
+  for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
+  p.rec = ring;
+  p.ring_shift = shift;
+  p.row_q0 = p_base;  // the launch loop takes p_base from here
+  if (value_type == NFEM_F64) {
+    switch (source_mode) {
+      case NFEM_COEF_NONE: return launch_darcy_sliced<double, NFEM_COEF_NONE>(p, shift, F, q, stream);
+      case NFEM_COEF_CELL: return launch_darcy_sliced<double, NFEM_COEF_CELL>(p, shift, F, q, stream);
+      case NFEM_COEF_QPOINT: return launch_darcy_sliced<double, NFEM_COEF_QPOINT>(p, shift, F, q, stream);
+      default: return NFEM_ERR_INVALID_ARG;
+    }
+  }
+  switch (source_mode) {
+    case NFEM_COEF_NONE: return launch_darcy_sliced<float, NFEM_COEF_NONE>(p, shift, F, q, stream);
+    case NFEM_COEF_CELL: return launch_darcy_sliced<float, NFEM_COEF_CELL>(p, shift, F, q, stream);
+    case NFEM_COEF_QPOINT: return launch_darcy_sliced<float, NFEM_COEF_QPOINT>(p, shift, F, q, stream);
+    default: return NFEM_ERR_INVALID_ARG;
+  }
 }
 
 // ------------------------------------------------------------------ Dirichlet

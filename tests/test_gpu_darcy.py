@@ -22,13 +22,18 @@ def f2d(x, y, z):
     return np.array([2 * PI ** 2 * np.sin(PI * x) * np.sin(PI * y)])
 
 
-def assemble_gpu(m, kappa, rhs, dtype, use_chunks=False, use_records=None):
+def assemble_gpu(m, kappa, rhs, dtype, use_chunks=False, use_records=None, use_slices=True, slice_shift=17,
+                 record_quarters=None):
     sp = product_space(m, DARCY)
     A = nf.CSRMatrix(sp, dtype=dtype)
     res = torch.empty(A.n_rows, dtype=dtype, device="cuda")
     wf = nf.LaplaceDualWeakForm(sp)
     wf.use_chunks = use_chunks
     wf.use_records = use_records
+    wf.use_slices = use_slices
+    wf.min_slice_shift = slice_shift
+    if record_quarters is not None:
+        wf.record_quarters = record_quarters
     wf.functions = {"kappa": kappa, "rhs": rhs}
     asm = nf.SequentialAssembler(sp, A, res)
     asm.form_to_input_list = {"darcy": ["form", range(sp.n_cells), wf, None]}
@@ -44,7 +49,7 @@ def row_scaled_err(Ag, Ao):
     return (abs(d).max(axis=1).toarray().ravel() / scale).max()
 
 
-@pytest.mark.parametrize("kernel", ["cell_chunks", "row_records", "row_one_pass"])
+@pytest.mark.parametrize("kernel", ["cell_chunks", "row_records", "row_records_unsliced", "row_one_pass"])
 @pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
 @pytest.mark.parametrize("gen,n", [("square", 4), ("square", 32), ("cube", 2), ("cube", 6), ("cube", 12)])
 def test_darcy_matrix_matches_oracle(cuda_lib, dtype, tol, gen, n, kernel):
@@ -54,7 +59,8 @@ def test_darcy_matrix_matches_oracle(cuda_lib, dtype, tol, gen, n, kernel):
     T = m["blocks"][-1][1].shape[0]
     kappa = np.exp(np.sin(np.arange(T) * 0.37))
     f_cell = np.cos(np.arange(T) * 0.11)
-    sp, A, res = assemble_gpu(m, kappa, f_cell, dtype, kernel == "cell_chunks", kernel == "row_records")
+    sp, A, res = assemble_gpu(m, kappa, f_cell, dtype, kernel == "cell_chunks", kernel.startswith("row_records"),
+                              use_slices=kernel != "row_records_unsliced", slice_shift=5)
     assert (A.chunk_rows is not None) == (sp.dof_shift == 0)
     Ao, ro, cd, nd, topo = darcy_oracle(m, kappa, f_cell=f_cell)
     Ag = A.to_scipy()
@@ -264,3 +270,25 @@ def test_darcy_records_equal_one_pass(cuda_lib, dtype, gen, n, qpoint):
     tol = 1e-6 if dtype == torch.float32 else (1e-13 if gen == "cube" else 1e-14)
     assert row_scaled_err(A1.to_scipy(), A2.to_scipy()) <= tol
     assert ((r1 - r2).abs().max() / r1.abs().max()).item() <= tol
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("n,shift,quarters", [(12, 10, 1), (16, 11, 2), (16, 13, 3), (6, 17, 2)])
+def test_darcy_sliced_equals_two_pass(cuda_lib, dtype, n, shift, quarters):
+    """The overlapped assembly (cell slices of 2^shift cells, records in a
+    ring of three slices, cell pass and row pass in the same launches) writes
+    exactly the values and residual of the two-pass assembly: the same
+    record and row arithmetic, only scheduled differently.  The sizes give
+    1 to 15 slices, so the ring wraps several times."""
+    m = mesh_gen.cube(n)
+    T = m["blocks"][-1][1].shape[0]
+    rng = np.random.default_rng(n + shift)
+    kappa = np.exp(rng.normal(0.0, 2.0, T))
+    f_cell = rng.normal(0.0, 1.0, T)
+    sp, A1, r1 = assemble_gpu(m, kappa, f_cell, dtype, use_records=True, use_slices=False)
+    _, A2, r2 = assemble_gpu(m, kappa, f_cell, dtype, use_records=True, use_slices=True, slice_shift=shift,
+                             record_quarters=quarters)
+    A2.check_status("sliced")
+    assert A2.lookahead_cells < 2 ** shift
+    assert torch.equal(A1.values, A2.values)
+    assert torch.equal(r1, r2)
