@@ -436,6 +436,11 @@ def assembly_only(args):
     wf = nf.LaplaceDualWeakForm(sp)
     wf.use_chunks = args.kernel == "chunks"
     wf.use_records = args.kernel == "records"
+    wf.use_slices = args.slices
+    if args.slice_shift:
+        wf.min_slice_shift = args.slice_shift
+    if args.record_quarters:
+        wf.record_quarters = args.record_quarters
     wf.functions = {"kappa": kappa, "rhs": f}
     coefs = wf.coefficients(dtype)
     ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
@@ -655,6 +660,11 @@ def run_ours(args):
     wf = nf.LaplaceDualWeakForm(sp)
     wf.use_chunks = args.kernel == "chunks"
     wf.use_records = args.kernel == "records"
+    wf.use_slices = args.slices
+    if args.slice_shift:
+        wf.min_slice_shift = args.slice_shift
+    if args.record_quarters:
+        wf.record_quarters = args.record_quarters
     wf.functions = {"kappa": kappa, "rhs": f}
     coefs = wf.coefficients(dtype)
     res = torch.empty(A.n_rows, dtype=dtype, device="cuda")
@@ -896,6 +906,11 @@ def main():
                     help="with --only solve: which preconditioners to run")
     ap.add_argument("--kernel", choices=["records", "rows", "chunks"], default="records",
                     help="Darcy assembly: cell records then rows (default), rows alone, or cell chunks")
+    ap.add_argument("--slices", action="store_true",
+                    help="the overlapped Darcy assembly by cell slices (nfem_darcy_rt1p0_assemble_sliced)")
+    ap.add_argument("--slice-shift", type=int, default=0, help="cells per slice = 2^shift (default: the library's)")
+    ap.add_argument("--record-quarters", type=int, default=0,
+                    help="quarters of the blocks forming records in the overlapped assembly (default: the library's)")
     ap.add_argument("--only", choices=["assembly", "elasticity", "cosserat", "batch2d", "solve"], default=None,
                     help="time one secondary assembly workload alone and print its record (profiling runs)")
     args = ap.parse_args()

@@ -86,6 +86,7 @@ struct DarcyParams {
   int64_t cell_begin, cell_end;
   int64_t row_f0, row_f1, row_q0, row_q1;
   int ring_shift;
+  int reverse;  // row pass walks its chunks from the last (records written last are still in L2)
 };
 
 // Position of cell c's record: c itself, or its place in the ring of three
@@ -584,8 +585,11 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
   }
 }
 
+#ifndef NFEM_DF_MIN_BLOCKS
+#define NFEM_DF_MIN_BLOCKS 5
+#endif
 template <int SRC>
-__global__ void __launch_bounds__(256) darcy_records_df_kernel(const DarcyParams p) {
+__global__ void __launch_bounds__(256, NFEM_DF_MIN_BLOCKS) darcy_records_df_kernel(const DarcyParams p) {
   records_df_cells<SRC>(p, blockIdx.x * int64_t(blockDim.x) + threadIdx.x, int64_t(gridDim.x) * blockDim.x);
 }
 
@@ -791,7 +795,8 @@ __device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t r
   const int64_t nfc = (p.row_f1 - p.row_f0 + 31) / 32, nqc = (p.row_q1 - p.row_q0 + 31) / 32;
   const int64_t n_chunks = nfc + nqc;
   const int64_t jstride = n_blocks * kDarcyWarps;
-  auto chunk_range = [&](int64_t j, int64_t& rb, int64_t& re) {
+  auto chunk_range = [&](int64_t jj, int64_t& rb, int64_t& re) {
+    const int64_t j = (p.reverse && jj < n_chunks) ? n_chunks - 1 - jj : jj;
     if (j < nfc) {
       rb = p.row_f0 + 32 * j;
       re = p.row_f1;
@@ -1356,6 +1361,7 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   p.row_f1 = n_rows;
   p.row_q0 = p.row_q1 = 0;
   p.ring_shift = -1;
+  p.reverse = workspace != nullptr && !chunk_rows;
   if (value_type == NFEM_F64 && points_split) {
     if (reinterpret_cast<uintptr_t>(points_split) & 15) return NFEM_ERR_INVALID_ARG;
     p.fixed = reinterpret_cast<const int64_t*>(points_split);
@@ -1442,6 +1448,7 @@ extern "C" int nfem_darcy_rt1p0_assemble_sliced(int value_type, int64_t n_cells,
   for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
   p.rec = ring;
   p.ring_shift = shift;
+  p.reverse = 0;
   p.row_q0 = p_base;  // the launch loop takes p_base from here
   if (value_type == NFEM_F64) {
     switch (source_mode) {
