@@ -86,7 +86,6 @@ struct DarcyParams {
   int64_t cell_begin, cell_end;
   int64_t row_f0, row_f1, row_q0, row_q1;
   int ring_shift;
-  int reverse;  // row pass walks its chunks from the last (records written last are still in L2)
 };
 
 // Position of cell c's record: c itself, or its place in the ring of three
@@ -795,8 +794,7 @@ __device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t r
   const int64_t nfc = (p.row_f1 - p.row_f0 + 31) / 32, nqc = (p.row_q1 - p.row_q0 + 31) / 32;
   const int64_t n_chunks = nfc + nqc;
   const int64_t jstride = n_blocks * kDarcyWarps;
-  auto chunk_range = [&](int64_t jj, int64_t& rb, int64_t& re) {
-    const int64_t j = (p.reverse && jj < n_chunks) ? n_chunks - 1 - jj : jj;
+  auto chunk_range = [&](int64_t j, int64_t& rb, int64_t& re) {
     if (j < nfc) {
       rb = p.row_f0 + 32 * j;
       re = p.row_f1;
@@ -1361,7 +1359,6 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   p.row_f1 = n_rows;
   p.row_q0 = p.row_q1 = 0;
   p.ring_shift = -1;
-  p.reverse = workspace != nullptr && !chunk_rows;
   if (value_type == NFEM_F64 && points_split) {
     if (reinterpret_cast<uintptr_t>(points_split) & 15) return NFEM_ERR_INVALID_ARG;
     p.fixed = reinterpret_cast<const int64_t*>(points_split);
@@ -1448,7 +1445,6 @@ extern "C" int nfem_darcy_rt1p0_assemble_sliced(int value_type, int64_t n_cells,
   for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
   p.rec = ring;
   p.ring_shift = shift;
-  p.reverse = 0;
   p.row_q0 = p_base;  // the launch loop takes p_base from here
   if (value_type == NFEM_F64) {
     switch (source_mode) {
