@@ -412,6 +412,24 @@ int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int
                            void* rhs, int accumulate, void* workspace, size_t workspace_bytes,
                            int32_t* dev_status, void* stream);
 
+/* Replaces LCEScaledRieszMapWeakForm.evaluate_form_vectorized
+ * (src/weak_forms/lce_scaled_riesz_map_weak_form.py:415-598), the
+ * preconditioning operator the Cosserat driver assembles
+ * (examples/cosserat_elasticity/mfe_cosserat_elasticity_example_3.py:189-240),
+ * into the CSR pattern of the dual form (its blocks are a subset): per field
+ * block-diagonal; (s,s) the stress compliance plus (div tau_i, div tau_j) of
+ * every row, (m,m) the couple-stress compliance plus l^2 (div v_i, div v_j)
+ * (a constant length l = params7[6]; a varying l is not supported), (u,u)
+ * and (t,t) the P0 mass.  Arguments as nfem_cosserat_assemble, no load. */
+int nfem_cosserat_riesz_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                                 const double* points, const float* points_split,
+                                 const int32_t* cell_vertices, const uint8_t* sign_mask,
+                                 const double* params7, const double* ref_Psi, const double* ref_mhat,
+                                 const double* ref_divhat, const int32_t* inc_ptr, const int32_t* inc,
+                                 const uint8_t* node_codes, const int32_t* row_ptr, void* values,
+                                 int accumulate, void* workspace, size_t workspace_bytes,
+                                 int32_t* dev_status, void* stream);
+
 /* -------------------------------------------- K5 + K7: Krylov solve (a17)
  * Replaces the PETSc KSP solves of the drivers
  * (examples/md_elliptic_scalar/md_elliptic_scalar.py:343-363,

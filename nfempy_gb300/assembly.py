@@ -740,6 +740,53 @@ class LCEDualWeakForm(WeakForm):
                   _lib.ptr(ws), ws.numel(), _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
 
 
+class LCEScaledRieszMapWeakForm(LCEDualWeakForm):
+    """The Cosserat preconditioning operator of the reference driver
+    (src/weak_forms/lce_scaled_riesz_map_weak_form.py:415-598; assembled as P
+    in mfe_cosserat_elasticity_example_3.py:189-240): block-diagonal by field,
+    compliance + div-div on the stress and couple-stress rows, P0 mass on u
+    and t.  functions: the material of LCEDualWeakForm, "l" (a constant, or a
+    callable constant over the mesh) and optionally "grad_l" (must vanish:
+    only a constant length scale is supported on the device).  Assembles the
+    Jacobian only (the form has no load)."""
+
+    def coefficients(self, dtype):
+        gl = self.functions.get("grad_l")
+        if gl is not None:
+            xq = self.quadrature_points()
+            g = np.asarray(gl(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64)
+            if np.abs(g).max() > 0:
+                raise NotImplementedError("a varying length scale l (grad_l != 0) is not supported on the device")
+        saved = self.functions.get("rhs")
+        self.functions["rhs"] = None
+        try:
+            return super().coefficients(dtype)
+        finally:
+            self.functions["rhs"] = saved
+
+    def assemble(self, jacobian, residual=None, accumulate=False, stream=None, coefficients=None):
+        self._check_space()
+        sp = self.space
+        dtype = jacobian.dtype
+        vt = _lib.NFEM_F64 if dtype == torch.float64 else _lib.NFEM_F32
+        if jacobian.node_codes is None:
+            raise NotImplementedError("matrix built without node codes")
+        par, _, Psi, mhat, divhat = coefficients if coefficients is not None else self.coefficients(dtype)
+        dp = _lib.C.POINTER(_lib.C.c_double)
+        key = ("geom", dtype)
+        if key not in self._cache:
+            nb = _lib.C.c_size_t(0)
+            _lib.call("nfem_cosserat_workspace_bytes", vt, sp.n_cells, _lib.C.byref(nb))
+            self._cache[key] = torch.empty(max(int(nb.value), 16), dtype=torch.uint8, device=sp.device)
+        ws = self._cache[key]
+        _lib.call("nfem_cosserat_riesz_assemble", vt, sp.n_cells, sp.n_dof // 3, sp.dof_shift, _lib.ptr(sp.points),
+                  _lib.ptr(sp.points_split), _lib.ptr(sp.cells), _lib.ptr(sp.rt_sign_mask), par.ctypes.data_as(dp),
+                  Psi.ctypes.data_as(dp), mhat.ctypes.data_as(dp), divhat.ctypes.data_as(dp),
+                  _lib.ptr(jacobian.inc_ptr), _lib.ptr(jacobian.inc), _lib.ptr(jacobian.node_codes),
+                  _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values), int(accumulate), _lib.ptr(ws), ws.numel(),
+                  _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+
+
 # ---------------------------------------------------------------- norms
 _RT1_SIGMA = {2: np.array([-1.0, 1.0, -1.0]), 3: np.array([1.0, -1.0, 1.0, -1.0])}
 

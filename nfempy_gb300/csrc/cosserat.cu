@@ -79,6 +79,11 @@ struct CosParams {
   void* rhs;
   int accumulate;
   int32_t* status;
+  // LCEScaledRieszMapWeakForm instead of the dual form: block-diagonal by
+  // field, compliance without the 1/l of the couple stress, plus the
+  // div-div term of every s row and (times l^2 for a constant l) every m row,
+  // and the P0 mass on u and t; no coupling blocks, no load
+  int riesz;
 };
 
 template <typename T>
@@ -185,6 +190,38 @@ __device__ __forceinline__ void cos_block(const CosParams& p, const CosTables<T>
   const int fa = a & 3, fb = b & 3;
   const T sga = ((m >> fa) & 1u) ? T(-1) : T(1);
   const T sgb = ((m >> fb) & 1u) ? T(-1) : T(1);
+  if (p.riesz) {
+    if ((as && bs) || (am && bm)) {
+      const T* Ps = tb.Psi + (fa * 4 + fb) * 9;
+      T PJ[3][3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+          PJ[k][q] = Ps[k * 3 + 0] * J[q][0] + Ps[k * 3 + 1] * J[q][1] + Ps[k * 3 + 2] * J[q][2];
+      T Phi[3][3];
+      const T sc = sga * sgb / adet;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) Phi[c][d] = sc * (J[c][0] * PJ[0][d] + J[c][1] * PJ[1][d] + J[c][2] * PJ[2][d]);
+      const T tr = Phi[0][0] + Phi[1][1] + Phi[2][2];
+      const T mu = as ? T(p.mu_s) : T(p.mu_o), ka = as ? T(p.kappa_s) : T(p.kappa_o), la = as ? T(p.lam_s) : T(p.lam_o);
+      const T cin = T(0.25) / mu + T(0.25) / ka;
+      const T cout = T(0.25) / mu - T(0.25) / ka;
+      const T vf = la / (T(2) * mu * (T(2) * mu + T(3) * la));
+      // int div psi_a div psi_b = sga sgb divhat_a divhat_b / (|That| |det J|), |That| = 1/6
+      const T dd = (as ? T(1) : T(p.l) * T(p.l)) * sga * sgb * tb.divhat[fa] * tb.divhat[fb] * T(6) / adet;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) K[c][d] = (c == d ? tr * cin + dd : T(0)) + Phi[d][c] * cout - vf * Phi[c][d];
+    } else if ((au && bu) || (at && bt)) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) K[c][c] = adet * T(1.0 / 6.0);
+    }
+    return;
+  }
   if ((as && bs) || (am && bm)) {
     // Phi = sga sgb J Psihat_ab J^T / |det|
     const T* Ps = tb.Psi + (fa * 4 + fb) * 9;
@@ -313,7 +350,7 @@ __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const Cos
     T r[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) r[i] = __shfl_sync(0xffffffffu, rhs_acc[i], 0) + __shfl_sync(0xffffffffu, rhs_acc[i], 10);
-    if (lane < 3) {
+    if (lane < 3 && rhs) {
       const T rv = lane == 0 ? r[0] : (lane == 1 ? r[1] : r[2]);
       if (p.accumulate) rhs[r0 + lane] += rv; else rhs[r0 + lane] = rv;
     }
@@ -331,21 +368,19 @@ extern "C" int nfem_cosserat_workspace_bytes(int value_type, int64_t n_cells, si
   return NFEM_OK;
 }
 
-extern "C" int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
-                                      const double* points, const float* points_split, const int32_t* cell_vertices,
-                                      const uint8_t* sign_mask, const double* params7, const void* force,
-                                      const double* ref_Psi, const double* ref_mhat, const double* ref_divhat,
-                                      const int32_t* inc_ptr, const int32_t* inc, const uint8_t* node_codes,
-                                      const int32_t* row_ptr, void* values, void* rhs, int accumulate,
-                                      void* workspace, size_t workspace_bytes, int32_t* dev_status,
-                                      void* stream_) {
+static int cosserat_launch(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0, const double* points,
+                           const float* points_split, const int32_t* cell_vertices, const uint8_t* sign_mask,
+                           const double* params7, const void* force, const double* ref_Psi, const double* ref_mhat,
+                           const double* ref_divhat, const int32_t* inc_ptr, const int32_t* inc,
+                           const uint8_t* node_codes, const int32_t* row_ptr, void* values, void* rhs, int accumulate,
+                           void* workspace, size_t workspace_bytes, int32_t* dev_status, void* stream_, int riesz){
   cudaStream_t stream = (cudaStream_t)stream_;
   if (n_cells < 0) return NFEM_ERR_INVALID_ARG;
   if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n_nodes < 0 || row0 < 0 || !params7)
     return NFEM_ERR_INVALID_ARG;
   if (n_nodes == 0) return NFEM_OK;
   if (!cell_vertices || !sign_mask || !ref_Psi || !ref_mhat || !ref_divhat || !inc_ptr || !inc || !node_codes ||
-      !row_ptr || !values || !rhs)
+      !row_ptr || !values || (!rhs && !riesz))
     return NFEM_ERR_INVALID_ARG;
   if (value_type == NFEM_F64 && !points) return NFEM_ERR_INVALID_ARG;
   if (value_type == NFEM_F32 && (!points_split || (reinterpret_cast<uintptr_t>(points_split) & 15)))
@@ -383,6 +418,7 @@ extern "C" int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n
   p.rhs = rhs;
   p.accumulate = accumulate != 0;
   p.status = dev_status;
+  p.riesz = riesz;
   const size_t vb = value_type == NFEM_F64 ? sizeof(double) : sizeof(float);
   if (!workspace || workspace_bytes < size_t(n_cells) * 12 * vb || (reinterpret_cast<uintptr_t>(workspace) & 15))
     return NFEM_ERR_WORKSPACE;
@@ -398,4 +434,31 @@ extern "C" int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n
   }
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
+}
+
+
+extern "C" int nfem_cosserat_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                                      const double* points, const float* points_split, const int32_t* cell_vertices,
+                                      const uint8_t* sign_mask, const double* params7, const void* force,
+                                      const double* ref_Psi, const double* ref_mhat, const double* ref_divhat,
+                                      const int32_t* inc_ptr, const int32_t* inc, const uint8_t* node_codes,
+                                      const int32_t* row_ptr, void* values, void* rhs, int accumulate,
+                                      void* workspace, size_t workspace_bytes, int32_t* dev_status,
+                                      void* stream) {
+  return cosserat_launch(value_type, n_cells, n_nodes, row0, points, points_split, cell_vertices, sign_mask, params7,
+                         force, ref_Psi, ref_mhat, ref_divhat, inc_ptr, inc, node_codes, row_ptr, values, rhs,
+                         accumulate, workspace, workspace_bytes, dev_status, stream, 0);
+}
+
+extern "C" int nfem_cosserat_riesz_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                                            const double* points, const float* points_split,
+                                            const int32_t* cell_vertices, const uint8_t* sign_mask,
+                                            const double* params7, const double* ref_Psi, const double* ref_mhat,
+                                            const double* ref_divhat, const int32_t* inc_ptr, const int32_t* inc,
+                                            const uint8_t* node_codes, const int32_t* row_ptr, void* values,
+                                            int accumulate, void* workspace, size_t workspace_bytes,
+                                            int32_t* dev_status, void* stream) {
+  return cosserat_launch(value_type, n_cells, n_nodes, row0, points, points_split, cell_vertices, sign_mask, params7,
+                         nullptr, ref_Psi, ref_mhat, ref_divhat, inc_ptr, inc, node_codes, row_ptr, values, nullptr,
+                         accumulate, workspace, workspace_bytes, dev_status, stream, 1);
 }

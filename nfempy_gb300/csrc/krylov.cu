@@ -626,9 +626,11 @@ __global__ void weights_rows(int64_t n, const int32_t* __restrict__ rp, const in
 }
 
 // c_i^2 = sum over the incidences (c, a) of column i of sum_b (inv[c][b][a] / m_b)^2
-template <int N>
+template <int NT>
 __global__ void weights_blockcols(int64_t n_rows, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
-                                  const int32_t* __restrict__ cd, const float* __restrict__ inv, double* __restrict__ c2) {
+                                  const int32_t* __restrict__ cd, const float* __restrict__ inv, double* __restrict__ c2,
+                                  int n_run = 0) {
+  const int N = NT > 0 ? NT : n_run;
   for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n_rows; r += int64_t(gridDim.x) * blockDim.x) {
     double acc = 0.0;
     for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; ++k) {
@@ -1477,6 +1479,78 @@ __global__ void block_extract_invert(int64_t n_cells, const int32_t* __restrict_
   }
 }
 
+// Cells with more local DoFs (6 .. 32, e.g. 30 for the four-field Cosserat
+// layout): one warp per cell, the block and the identity side by side in
+// shared memory, lane j owning columns j and N + j, Gauss-Jordan with partial
+// pivoting in FP32 (the inverse is stored in FP32 and only preconditions).
+constexpr int kBlkWarps = 4;
+constexpr int kBlkMaxN = 32;
+__global__ void __launch_bounds__(32 * kBlkWarps) block_extract_invert_warp(
+    int64_t n_cells, int N, const int32_t* __restrict__ cd, const int32_t* __restrict__ rp,
+    const int32_t* __restrict__ ci, const double* __restrict__ v, float* __restrict__ inv, int32_t* status) {
+  __shared__ float sm[kBlkWarps][kBlkMaxN][2 * kBlkMaxN + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float(*m)[2 * kBlkMaxN + 1] = sm[warp];
+  for (int64_t c = int64_t(blockIdx.x) * kBlkWarps + warp; c < n_cells; c += int64_t(gridDim.x) * kBlkWarps) {
+    const int32_t dj = lane < N ? __ldg(cd + c * N + lane) : 0;
+    for (int i = 0; i < N; ++i) {
+      const int32_t di = __ldg(cd + c * N + i);
+      const int32_t b0 = __ldg(rp + di), b1 = __ldg(rp + di + 1);
+      if (lane < N) {
+        int32_t lo = b0, hi = b1;
+        while (lo < hi) {  // at most log2(row length) steps
+          const int32_t mid = (lo + hi) >> 1;
+          if (__ldg(ci + mid) < dj) lo = mid + 1; else hi = mid;
+        }
+        m[i][lane] = (lo < b1 && __ldg(ci + lo) == dj) ? float(__ldg(v + lo)) : 0.f;
+        m[i][N + lane] = i == lane ? 1.f : 0.f;
+      }
+    }
+    __syncwarp();
+    bool singular = false;
+    for (int k = 0; k < N; ++k) {
+      float best = (lane >= k && lane < N) ? fabsf(m[lane][k]) : -1.f;
+      int p = lane;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {  // warp arg-max, lowest row on ties
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int op = __shfl_xor_sync(0xffffffffu, p, o);
+        if (ob > best || (ob == best && op < p)) { best = ob; p = op; }
+      }
+      if (!(best > 0.f)) {  // the same value in every lane: a uniform exit
+        singular = true;
+        break;
+      }
+      if (p != k && lane < N) {
+        float t = m[k][lane]; m[k][lane] = m[p][lane]; m[p][lane] = t;
+        t = m[k][N + lane]; m[k][N + lane] = m[p][N + lane]; m[p][N + lane] = t;
+      }
+      __syncwarp();
+      const float ip = 1.f / m[k][k];
+      __syncwarp();
+      if (lane < N) {
+        m[k][lane] *= ip;
+        m[k][N + lane] *= ip;
+      }
+      __syncwarp();
+      for (int i = 0; i < N; ++i) {
+        if (i == k) continue;
+        const float f = m[i][k];
+        __syncwarp();
+        if (lane < N) {
+          m[i][lane] -= f * m[k][lane];
+          m[i][N + lane] -= f * m[k][N + lane];
+        }
+        __syncwarp();
+      }
+    }
+    if (singular && lane == 0) set_status(status, NFEM_ERR_BREAKDOWN);
+    for (int i = 0; i < N; ++i)
+      if (lane < N) inv[(c * N + i) * N + lane] = singular ? 0.f : m[i][N + lane];
+    __syncwarp();
+  }
+}
+
 // z_r = (1 / m_r) sum over the incidences (c, a) of row r of (A_c^-1 v[dofs_c])_a
 // The cell-block smoother as a matrix in A's pattern: row r of
 // omega / m_r sum over the incidences (c, a) of r of row a of A_c^-1, at the
@@ -1488,11 +1562,13 @@ static float pre_omega(const nfem_precond* pc) {
   return w > 0.f ? w : 1.f;
 }
 
-template <int N>
+// NT > 0: N = NT known at compile time; NT == 0: N = n_run (cells of 6..32 DoFs)
+template <int NT>
 __global__ void smoother_fill(int64_t n_rows, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                               const int32_t* __restrict__ cd, const float* __restrict__ inv,
                               const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, float omega,
-                              float* __restrict__ sv, int32_t* status) {
+                              float* __restrict__ sv, int32_t* status, int n_run = 0) {
+  const int N = NT > 0 ? NT : n_run;
   for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n_rows; r += int64_t(gridDim.x) * blockDim.x) {
     const int32_t b0 = rp[r], b1 = rp[r + 1];
     for (int32_t e = b0; e < b1; ++e) sv[e] = 0.f;
@@ -1526,12 +1602,13 @@ __global__ void smoother_fill(int64_t n_rows, const int32_t* __restrict__ inc_pt
 }
 
 // omega scales the result; accumulate adds it into z (a post-smoothing step)
-template <int N>
+template <int NT>
 __global__ void block_apply(int64_t n_rows, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                             const int32_t* __restrict__ cd, const float* __restrict__ inv, const float* __restrict__ v,
                             float* __restrict__ z, const int32_t* __restrict__ gate, float omega = 1.f,
-                            int accumulate = 0) {
+                            int accumulate = 0, int n_run = 0) {
   NFEM_GATE(gate);
+  const int N = NT > 0 ? NT : n_run;
   for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n_rows; r += int64_t(gridDim.x) * blockDim.x) {
     const int32_t kb = inc_ptr[r], ke = inc_ptr[r + 1];
     float acc = 0.f;
@@ -1649,7 +1726,7 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
         return NFEM_ERR_INVALID_ARG;
     }
     // every argument is checked before the first launch
-    if (pc->n_loc != 4 && pc->n_loc != 5) return NFEM_ERR_UNSUPPORTED;
+    if (pc->n_loc < 4 || pc->n_loc > kBlkMaxN) return NFEM_ERR_UNSUPPORTED;
     if (pc->smoother) {
       const nfem_csr* S = pc->smoother;
       if (S->value_type != NFEM_F32 || S->n_rows != A64->n_rows || !S->values || S->row_ptr != A64->row_ptr ||
@@ -1662,7 +1739,10 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
                                                         (const double*)A64->values, pc->block_inv, dev_status); break;
       case 5: block_extract_invert<5><<<g, 128, 0, s>>>(pc->n_cells, pc->cell_dofs, A64->row_ptr, A64->col_idx,
                                                         (const double*)A64->values, pc->block_inv, dev_status); break;
-      default: return NFEM_ERR_UNSUPPORTED;
+      default:
+        block_extract_invert_warp<<<grid_for(ceil_div(pc->n_cells, kBlkWarps), 1, 8), 32 * kBlkWarps, 0, s>>>(
+            pc->n_cells, pc->n_loc, pc->cell_dofs, A64->row_ptr, A64->col_idx, (const double*)A64->values,
+            pc->block_inv, dev_status);
     }
     if (pc->smoother) {
       const nfem_csr* S = pc->smoother;
@@ -1671,10 +1751,14 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
         smoother_fill<5><<<gr, 256, 0, s>>>(A64->n_rows, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv,
                                             A64->row_ptr, A64->col_idx, pre_omega(pc), (float*)S->values,
                                             dev_status);
-      else
+      else if (pc->n_loc == 4)
         smoother_fill<4><<<gr, 256, 0, s>>>(A64->n_rows, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv,
                                             A64->row_ptr, A64->col_idx, pre_omega(pc), (float*)S->values,
                                             dev_status);
+      else
+        smoother_fill<0><<<gr, 256, 0, s>>>(A64->n_rows, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv,
+                                            A64->row_ptr, A64->col_idx, pre_omega(pc), (float*)S->values,
+                                            dev_status, pc->n_loc);
     }
   } else if (pc->kind != NFEM_PC_NONE) {
     return NFEM_ERR_UNSUPPORTED;
@@ -1692,8 +1776,11 @@ extern "C" int nfem_precond_setup(const nfem_precond* pc, const nfem_csr* A64, i
       have_c = true;
       if (pc->n_loc == 5)
         weights_blockcols<5><<<g, 256, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, c2);
-      else
+      else if (pc->n_loc == 4)
         weights_blockcols<4><<<g, 256, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, c2);
+      else
+        weights_blockcols<0><<<g, 256, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, c2,
+                                               pc->n_loc);
     }
     weights_final<<<g, 256, 0, s>>>(n, s2, have_c ? c2 : nullptr, pc->wsqrt, pc->winvsqrt);
     NFEM_CHECK_LAUNCH();
@@ -1756,7 +1843,8 @@ static int smoother(const nfem_precond* pc, int64_t n, const float* v, float* z,
     block_apply<4><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z, gate,
                                                 omega, accumulate);
   else
-    return NFEM_ERR_UNSUPPORTED;
+    block_apply<0><<<grid_for(n, B), B, 0, s>>>(n, pc->inc_ptr, pc->inc, pc->cell_dofs, pc->block_inv, v, z, gate,
+                                                omega, accumulate, pc->n_loc);
   return NFEM_OK;
 }
 

@@ -92,8 +92,8 @@ class KrylovSolver:
                                    None, None, None)
         elif self.pc_kind in ("cell_block", "two_level"):
             n_loc = sp.n_loc
-            if n_loc not in (4, 5):
-                raise NotImplementedError("cell_block preconditioner for 4 or 5 local DoFs")
+            if not 4 <= n_loc <= 32 or (self.pc_kind == "two_level" and n_loc not in (4, 5)):
+                raise NotImplementedError("cell_block for 4 to 32 local DoFs per cell; two_level for mixed Darcy")
             self.block_inv = torch.empty((sp.n_cells, n_loc, n_loc), dtype=torch.float32, device=dev)
             kind = _lib.PC_CELL_BLOCK if self.pc_kind == "cell_block" else _lib.PC_TWO_LEVEL
             self.pc = _lib.Precond(kind, n_loc, sp.n_cells, _lib.ptr(sp.cell_dofs).value,

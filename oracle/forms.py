@@ -328,6 +328,56 @@ def cosserat_batch(X, signs, quad, par, f_q):
     return r, j
 
 
+def cosserat_riesz_element(X, signs, quad, par, l_fn, grad_l_fn):
+    """LCEScaledRieszMapWeakForm.evaluate_form_vectorized
+    (lce_scaled_riesz_map_weak_form.py:415-598), 3-D: block-diagonal by
+    field; (s,s) the stress compliance plus sum over the rows of
+    (div tau_i, div tau_j); (m,m) the couple-stress compliance (no 1/l) plus
+    the rows' (div(l v_i), div(l v_j)) with div(l v) = grad l . v + l div v;
+    (u,u) and (t,t) the P0 mass.  l_fn(x, y, z) -> [Q], grad_l_fn -> [3, Q]."""
+    dim = 3
+    pts, wts = quad
+    x, J, det, pinv = evaluate_mapping(dim, pts, X)
+    s_tab = tabulate_oriented("RT", dim, 1, pts, J, det, pinv, signs)
+    Q = len(wts)
+    wdet = det * wts
+    n = 30
+    j = np.zeros((n, n))
+
+    def compliance(psi, mu_v, kappa_v, lam_v):
+        out = np.zeros((12, 12))
+        vol = (1.0 / (2.0 * mu_v)) * (lam_v / (2.0 * mu_v + dim * lam_v))
+        for q in range(Q):
+            P = psi[q]
+            inner = np.zeros((12, 12))
+            outer = np.zeros((12, 12))
+            tro = np.outer(P.ravel(), P.ravel())
+            for i in range(4):
+                for jj in range(4):
+                    inner[i * 3:(i + 1) * 3, jj * 3:(jj + 1) * 3] = 0.5 * np.dot(P[i], P[jj]) * np.eye(3)
+                    outer[i * 3:(i + 1) * 3, jj * 3:(jj + 1) * 3] = 0.5 * np.outer(P[jj], P[i])
+            out += wdet[q] * ((inner + outer) / (2.0 * mu_v) + (inner - outer) / (2.0 * kappa_v) - vol * tro)
+        return out
+
+    psi = s_tab[0, :, :, 0:dim]
+    j[0:12, 0:12] += compliance(psi, par["mu_s"], par["kappa_s"], par["lambda_s"])
+    j[12:24, 12:24] += compliance(psi, par["mu_o"], par["kappa_o"], par["lambda_o"])
+    grad = s_tab[1:dim + 1, :, :, 0:dim]
+    div = np.trace(grad, axis1=0, axis2=3).T / det  # [4, Q]
+    lv = np.ravel(l_fn(x[:, 0], x[:, 1], x[:, 2])) * np.ones(Q)
+    gl = np.asarray(grad_l_fn(x[:, 0], x[:, 1], x[:, 2]), dtype=np.float64).reshape(-1, Q)[:dim]
+    sdiv = (div * wdet) @ div.T
+    ldiv = np.einsum("dq,qid->iq", gl, psi) + div * lv[None, :]
+    mdiv = (ldiv * wdet) @ ldiv.T
+    for c in range(3):
+        idx = np.arange(4) * 3 + c
+        j[np.ix_(idx, idx)] += sdiv
+        j[np.ix_(12 + idx, 12 + idx)] += mdiv
+    for k in range(24, 30):
+        j[k, k] += np.sum(wdet)
+    return np.zeros(n), j
+
+
 def darcy_dirichlet_facet(Xc, signs_c, local_face, Xf, dim, quad_f, p_D):
     """LaplaceDualWeakFormBCDirichlet.evaluate_form (laplace_dual_weak_form.py:90-154)
     for one boundary facet: r = sum_q |det J_F| w_q p_D(x_q) (psi_f . n), with

@@ -46,6 +46,12 @@ def cosserat_rhs(x, y, z):
                      COSSERAT_RHS[3] * x * y, COSSERAT_RHS[4] + 0.0 * x, COSSERAT_RHS[5] + y * y])
 
 
+# the Riesz map of the scaled Cosserat form with a length scale that varies
+# (its grad l . v term), constant material
+RIESZ_FUNCTIONS = {**{k: _const(v) for k, v in COSSERAT_PARAMS.items() if k != "l"},
+                   "l": lambda x, y, z: 0.8 + 0.3 * x - 0.1 * y * z,
+                   "grad_l": lambda x, y, z: np.array([0.3 + 0.0 * x, -0.1 * z, -0.1 * y])}
+
 FORM_FUNCTIONS = {
     "darcy": {
         "kappa": lambda x, y, z: 1.0 + 0.5 * x + 0.25 * y * y + 0.1 * z,

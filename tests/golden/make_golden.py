@@ -288,9 +288,10 @@ from basis.permute_and_transform import (  # noqa: E402
 from weak_forms.laplace_dual_weak_form import LaplaceDualWeakForm  # noqa: E402
 from weak_forms.le_primal_weak_form import LEPrimalWeakForm  # noqa: E402
 from weak_forms.lce_dual_weak_form import LCEDualWeakForm  # noqa: E402
+from weak_forms.lce_scaled_riesz_map_weak_form import LCEScaledRieszMapWeakForm  # noqa: E402
 
 sys.path.insert(0, os.path.dirname(HERE))
-from cases import FORM_FUNCTIONS  # noqa: E402
+from cases import FORM_FUNCTIONS, RIESZ_FUNCTIONS  # noqa: E402
 
 
 class RecordingMat:
@@ -396,6 +397,12 @@ def make_case(name, mesh, fields):
         out["quad_points"] = pts
         out["quad_weights"] = wts
     out["r_el"], out["j_el"] = element_forms(name, space, n_el)
+    if name.startswith("cosserat"):
+        # LCEScaledRieszMapWeakForm (lce_scaled_riesz_map_weak_form.py:415-598)
+        wf = LCEScaledRieszMapWeakForm(space)
+        wf.functions = RIESZ_FUNCTIONS
+        out["j_riesz"] = np.array([np.asarray(wf.evaluate_form_vectorized(i, np.zeros(dest.shape[1]))[1])
+                                   for i in range(n_el)])
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "cells", n_el, "n_dof", space.n_dof, "nnz", len(keys))
 

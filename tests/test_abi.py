@@ -153,8 +153,10 @@ def test_precond_setup_checks_arguments_before_launching(lib_path):
     pc.smoother = ctypes.pointer(other)
     assert lib.nfem_precond_setup(ctypes.byref(pc), ctypes.byref(A64), None, None) == 1
     pc.smoother = None
-    pc.n_loc = 6
+    pc.n_loc = 33  # cell blocks of 4 to 32 DoFs
     assert lib.nfem_precond_setup(ctypes.byref(pc), ctypes.byref(A64), None, None) == 7  # NFEM_ERR_UNSUPPORTED
+    pc.n_loc = 3
+    assert lib.nfem_precond_setup(ctypes.byref(pc), ctypes.byref(A64), None, None) == 7
     A32 = _lib.Csr(100, fake, fake, fake, _lib.NFEM_F32)
     assert lib.nfem_precond_setup(ctypes.byref(pc), ctypes.byref(A32), None, None) == 1
 

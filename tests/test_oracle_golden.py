@@ -96,3 +96,23 @@ def test_element_forms_match_reference(name):
         np.testing.assert_allclose(j, jr, rtol=0, atol=1e-13 * scale, err_msg=f"{name} cell {c} j_el")
         np.testing.assert_allclose(r, rr, rtol=0, atol=1e-13 * max(np.abs(rr).max(), 1e-300),
                                    err_msg=f"{name} cell {c} r_el")
+
+
+def test_cosserat_riesz_map_matches_reference():
+    """oracle.forms.cosserat_riesz_element against the reference's own
+    LCEScaledRieszMapWeakForm.evaluate_form_vectorized (varying l, so the
+    grad l . v part of the scaled divergence is pinned too), 1e-13 of the
+    cell's largest entry."""
+    from tests.cases import COSSERAT_PARAMS, RIESZ_FUNCTIONS
+    mk, fields = CASES["cosserat3d_n1"]
+    m = mk()
+    g = golden("cosserat3d_n1")
+    topo = topology.Topology(m, physical_tags=[1])
+    X = m["points"][topo.cells]
+    s = topo.rt1_signs()
+    quad = quadrature.make_quadrature(3, 3)
+    for c in range(topo.n_cells):
+        _, j = forms.cosserat_riesz_element(X[c], s[c], quad, COSSERAT_PARAMS, RIESZ_FUNCTIONS["l"],
+                                            RIESZ_FUNCTIONS["grad_l"])
+        jr = g["j_riesz"][c]
+        np.testing.assert_allclose(j, jr, rtol=0, atol=1e-13 * np.abs(jr).max(), err_msg=f"cell {c}")
