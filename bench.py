@@ -322,6 +322,7 @@ def _timed_solve(ksp, b, args, stream, two_level=False):
     ksp.setup()
     ev1.record(stream)
     x, info = ksp.solve(b, rtol=1e-8, inner_rtol=inner_rtol, max_inner=args.max_iters, raise_on_failure=False)
+    ksp.last_x = x
     ev2.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall
@@ -569,11 +570,28 @@ def cosserat_bench(args):
     alg = T * 16 + V * 24 + T + T * 24 + A.nnz * 4 + A.n_rows * 4
     peak, kind = measured_peaks()
     ach = alg / (ms * 1e-3) / 1e9
-    return {"metric": "DoF/s assembled", "value": sp.n_dof / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
-            "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz, "kernel": "cosserat_rows_kernel",
-            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "algorithmic_bytes": alg, "peak_source": kind,
-                         "traffic": profiled_traffic("cosserat_rows_f32_cube24.txt")}}
+    out = {"metric": "DoF/s assembled", "value": sp.n_dof / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
+           "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz, "kernel": "cosserat_rows_kernel",
+           "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                        "algorithmic_bytes": alg, "peak_source": kind,
+                        "traffic": profiled_traffic("cosserat_rows_f32_cube24.txt")}}
+    if not args.no_solve:
+        # the FP64 system solved to 1e-8: FGMRES (FP32 inner iterations, FP64
+        # refinement) with the cell-block Jacobi preconditioner (30 x 30
+        # blocks of the matrix itself), then the P0 errors against the
+        # manufactured solution on the device
+        import nfempy_gb300 as nf
+        from nfempy_gb300.solvers import KrylovSolver
+        A64 = A.with_dtype(torch.float64)
+        r64 = torch.empty(A.n_rows, dtype=torch.float64, device="cuda")
+        wf.assemble(A64, r64, coefficients=wf.coefficients(torch.float64))
+        wf.assemble(A, res, coefficients=coefs)
+        ksp = KrylovSolver(A64, pc="cell_block", A32_values=A.values, restart=args.cos_restart)
+        out["solve"] = _timed_solve(ksp, -r64, args, torch.cuda.current_stream())
+        out["solve"]["preconditioner"] = "cell-block Jacobi (30 x 30 blocks of A, weighted additive Schwarz)"
+        out["solve"]["l2_error_u_t_vs_manufactured"] = nf.l2_error(3, sp, exact, ksp.last_x.cpu().numpy(),
+                                                                   skip_fields=["s", "m"])
+    return out
 
 
 def batch2d_bench(args):
@@ -900,6 +918,7 @@ def main():
                     help="FP32 inner tolerance of the block-Jacobi and point-Jacobi solves (default: the solver's)")
     ap.add_argument("--tl-inner-rtol", type=float, default=None,
                     help="FP32 inner tolerance of the two-level solves (default: the solver's)")
+    ap.add_argument("--cos-restart", type=int, default=30, help="FGMRES restart of the Cosserat solve")
     ap.add_argument("--batch-agg", type=int, default=4,
                     help="aggregate side in squares of the batched 2-D two-level solve")
     ap.add_argument("--solver", choices=["both", "plain", "two_level"], default="both",
