@@ -64,12 +64,18 @@ N_SUB = {2: (3, 3, 1), 3: (4, 6, 4, 1)}
 class Mesh:
     """Points and cell blocks of a conformal simplex mesh (reference: src/mesh/mesh.py).
 
-    Construct from the in-memory gmsh layout produced by nfempy_gb300.meshes
-    (or any dict {"dim", "points", "blocks": [(type, conn, physical_tags)]})."""
+    Mesh(dimension, file_name) reads a gmsh 4.1 ASCII file like the
+    reference (nfempy_gb300.gmsh.read_msh, meshio's conventions);
+    Mesh(dimension, data=...) takes the in-memory layout produced by
+    nfempy_gb300.meshes (any dict {"dim", "points", "blocks": [(type, conn,
+    physical_tags)]})."""
 
     def __init__(self, dimension, file_name=None, data=None):
         if data is None:
-            raise NotImplementedError("reading gmsh files is not part of this package; pass data=")
+            if file_name is None:
+                raise ValueError("Mesh needs a gmsh file name or data=")
+            from .gmsh import read_msh
+            data = read_msh(file_name, dim=dimension)
         self.dimension = int(dimension)
         self.data = data
         self.points = np.asarray(data["points"], dtype=np.float64)

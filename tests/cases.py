@@ -8,6 +8,19 @@ from oracle import mesh_gen
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 DARCY = [("u", "RT", 1, 1, False), ("p", "P", 0, 1, True)]
+def golden_mesh(name):
+    """The gmsh mesh stored in a fixture (read from the reference's .msh by
+    tests/golden/make_golden.py)."""
+    g = golden(name)
+    blocks = []
+    i = 0
+    while f"block{i}_type" in g:
+        blocks.append((str(g[f"block{i}_type"]), g[f"block{i}_conn"], g[f"block{i}_phys"]))
+        i += 1
+    return {"dim": int(g["mesh_dim"]), "points": g["points"], "blocks": blocks}
+
+
+COSSERAT_FIELDS = [("s", "RT", 1, 3, False), ("m", "RT", 1, 3, False), ("u", "P", 0, 3, True), ("t", "P", 0, 3, True)]
 CASES = {
     "darcy2d_n4": (lambda: mesh_gen.square(4), DARCY),
     "darcy3d_n2": (lambda: mesh_gen.cube(2), DARCY),
@@ -15,6 +28,8 @@ CASES = {
     "elast2d_n3": (lambda: mesh_gen.square(3), [("u", "P", 2, 2, False)]),
     "cosserat3d_n1": (lambda: mesh_gen.cube(1), [("s", "RT", 1, 3, False), ("m", "RT", 1, 3, False),
                                                  ("u", "P", 0, 3, True), ("t", "P", 0, 3, True)]),
+    "darcy3d_msh0": (lambda: golden_mesh("darcy3d_msh0"), DARCY),
+    "cosserat3d_msh0": (lambda: golden_mesh("cosserat3d_msh0"), COSSERAT_FIELDS),
 }
 
 

@@ -403,6 +403,12 @@ def make_case(name, mesh, fields):
         wf.functions = RIESZ_FUNCTIONS
         out["j_riesz"] = np.array([np.asarray(wf.evaluate_form_vectorized(i, np.zeros(dest.shape[1]))[1])
                                    for i in range(n_el)])
+    if "msh" in name:  # the parsed gmsh mesh travels inside the fixture
+        out["mesh_dim"] = np.int64(dim)
+        for i, (typ, conn, phys) in enumerate(mesh["blocks"]):
+            out[f"block{i}_type"] = np.array(typ)
+            out[f"block{i}_conn"] = np.asarray(conn, dtype=np.int64)
+            out[f"block{i}_phys"] = np.asarray(phys, dtype=np.int64)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "cells", n_el, "n_dof", space.n_dof, "nnz", len(keys))
 
@@ -413,6 +419,17 @@ def main():
     make_case("darcy3d_n2", mesh_gen.cube(2), darcy)
     make_case("elast3d_n2", mesh_gen.cube(2), [("u", "Lagrange", 2, 3, False)])
     make_case("elast2d_n3", mesh_gen.square(3), [("u", "Lagrange", 2, 2, False)])
+    # a mesh gmsh made (the reference's own fixture), read with this
+    # package's gmsh 4.1 reader; the reference's mesh / DoF-map code then
+    # numbers it through the meshio stand-in
+    from nfempy_gb300.gmsh import read_msh
+    msh = read_msh(os.path.join(os.path.dirname(REF_SRC), "examples", "cosserat_elasticity", "gmsh_files", "ex_3",
+                                "example_3_3d_l_0.msh"))
+    msh = {"dim": 3, "points": msh["points"], "blocks": msh["blocks"]}
+    make_case("darcy3d_msh0", msh, darcy)
+    make_case("cosserat3d_msh0", msh,
+              [("s", "RT", 1, 3, False), ("m", "RT", 1, 3, False),
+               ("u", "Lagrange", 0, 3, True), ("t", "Lagrange", 0, 3, True)])
     make_case("cosserat3d_n1", mesh_gen.cube(1),
               [("s", "RT", 1, 3, False), ("m", "RT", 1, 3, False),
                ("u", "Lagrange", 0, 3, True), ("t", "Lagrange", 0, 3, True)])
