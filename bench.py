@@ -523,12 +523,20 @@ def elasticity_bench(args):
     coefs = wf.coefficients(torch.float32)
     ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
     A.check_status("elasticity bench")
+    from nfempy_gb300 import autotune
+    best, best_ms, tried = autotune.tune(f"elasticity_p2_f32_cells{sp.n_cells}",
+                                         lambda: wf.assemble(A, res, coefficients=coefs),
+                                         autotune.elasticity_candidates(), reps=max(3, args.steps // 4))
+    tuned_ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
+    A.check_status("elasticity tuned")
+    autotune.reset_knobs()
     V = m["points"].shape[0]
     alg = T * 16 + V * 24 + T * 4 * 2 + T * 12 + A.nnz * 4 + A.n_rows * 4
     peak, kind = measured_peaks()
     ach = alg / (ms * 1e-3) / 1e9
     out = {"metric": "DoF/s assembled", "value": sp.n_dof / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
            "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz, "kernel": "elasticity_rows_kernel",
+           "autotuned": {"config": best, "ms_per_step": tuned_ms, "candidates": len(tried)},
            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                         "algorithmic_bytes": alg, "peak_source": kind,
                         "traffic": profiled_traffic("elasticity_rows_f32_cube40.txt")}}
@@ -617,6 +625,15 @@ def batch2d_bench(args):
         wf.assemble(A, res, coefficients=coefs)
     graph_ms = _time_assembly(graph.replay, args.steps, args.warmup)
     A.check_status("batch2d graph")
+    # autotuned form and launch shape (nfempy_gb300.autotune, cached per GPU)
+    from nfempy_gb300 import autotune
+    import tempfile as _tf
+    os.environ.setdefault("NFEM_TUNING_CACHE", os.path.join(_tf.gettempdir(), "nfempy_gb300_tuning.json"))
+    best, best_ms, tried = autotune.tune(autotune.darcy_key(sp, torch.float32),
+                                         lambda: wf.assemble(A, res, coefficients=coefs),
+                                         autotune.darcy_candidates(2), form=wf, reps=max(3, args.steps // 4))
+    tuned_ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
+    A.check_status("batch2d tuned")
     T = sp.n_cells
     V = m["points"].shape[0]
     alg = algorithmic_bytes(T, V, A.nnz, sp.n_dof, 4, verts_per_cell=3)
@@ -626,6 +643,8 @@ def batch2d_bench(args):
            "problems": len(sides), "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz,
            "kernel": "darcy_rows_kernel (one pass: triangles, FP32)",
            "graph_replay_ms_per_step": graph_ms,
+           "autotuned": {"config": best, "ms_per_step": tuned_ms, "candidates": len(tried),
+                         "value": sp.n_dof / (tuned_ms * 1e-3), "cache": autotune.cache_path()},
            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                         "algorithmic_bytes": alg, "peak_source": kind,
                         "traffic": profiled_traffic("darcy_rows_f32_batch512.txt")}}
@@ -649,6 +668,44 @@ def batch2d_bench(args):
                              "aggregates": tl.n_agg, "largest_block": int(np.diff(bp).max()),
                              "host_structure_s": t_struct,
                              "time_to_solve_incl_host_structure_ms": out["solve"]["time_to_solve_ms"] + 1e3 * t_struct})
+        # one CUDA graph per step: both assemblies, the preconditioner setup
+        # and the solve replaying the schedule a first solve recorded (no host
+        # synchronisation inside); the FP64 residual is checked on the device
+        c32, c64 = coefs, wf.coefficients(torch.float64)
+        b = torch.empty_like(r64)
+        torch.neg(r64, out=b)
+        _, info_rec = ksp.solve(b.clone(), record_schedule=True, inner_rtol=args.tl_inner_rtol)
+        xg = torch.zeros_like(r64)
+        rel = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+        def step():
+            wf.assemble(A, res, coefficients=c32)
+            wf.assemble(A64, r64, coefficients=c64)
+            torch.neg(r64, out=b)
+            xg.zero_()
+            ksp.refresh()
+            ksp.solve(b, xg, inner_rtol=args.tl_inner_rtol, replay=True, relres_out=rel)
+
+        step()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            step()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g.replay()
+        n_rep = max(3, args.steps // 4)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(n_rep):
+            g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        out["graph_step"] = {"ms_per_step": e0.elapsed_time(e1) / n_rep, "replays": n_rep,
+                             "final_relres_fp64": float(rel.item()),
+                             "contents": "FP32 + FP64 assembly, two-level setup, FGMRES replaying a recorded schedule "
+                                         f"({info_rec.inner_iterations} inner iterations, {info_rec.outer_iterations} "
+                                         "refinement steps)"}
+    autotune.reset_knobs()
     return out
 
 

@@ -55,6 +55,25 @@ typedef enum {
 int nfem_abi_version(void);
 const char* nfem_status_string(int status);
 
+/* Launch knobs: process-wide launch shapes that an autotuner may set
+ * (nfempy_gb300.autotune times candidates and caches the best per GPU and
+ * workload).  No reference counterpart.  0 restores the built-in choice.
+ *   NFEM_KNOB_DARCY_ROWS_BLOCKS_PER_SM   resident blocks per SM of the Darcy
+ *                                        row pass (0: the occupancy maximum)
+ *   NFEM_KNOB_DARCY_CELLS_BLOCK          threads per block of the Darcy cell
+ *                                        pass: 128, 256 (0) or 512
+ *   NFEM_KNOB_ELAS_WARPS                 warps per block of the elasticity
+ *                                        node rows: 2, 4 (0) or 8
+ * nfem_knob_set returns NFEM_ERR_INVALID_ARG for an unknown key or value. */
+typedef enum {
+  NFEM_KNOB_DARCY_ROWS_BLOCKS_PER_SM = 0,
+  NFEM_KNOB_DARCY_CELLS_BLOCK = 1,
+  NFEM_KNOB_ELAS_WARPS = 2,
+  NFEM_KNOB_COUNT = 3
+} nfem_knob;
+int nfem_knob_set(int key, int value);
+int nfem_knob_get(int key, int* value);
+
 /* Exclusive prefix sum of n int32 counts into n + 1 int64 offsets. */
 int nfem_scan_workspace_bytes(int64_t n, size_t* bytes);
 int nfem_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offsets,
@@ -557,6 +576,22 @@ typedef struct {
   int max_snapshots;
   int no_graphs;      /* 0: from the second restart cycle on, the cycle's steps
                          are replayed as one CUDA graph; 1: launched one by one */
+  /* Schedule (no reference counterpart).  schedule_mode 1 records, into the
+   * host array schedule [schedule_capacity], the launch schedule this solve
+   * took: {n_outer, then per refinement step: n_cycles, then the steps of
+   * each cycle}; schedule[0] = -1 when it did not fit.  schedule_mode 2
+   * replays a recorded schedule without any host synchronisation (the call
+   * can be captured into a CUDA graph with the assembly before it): the same
+   * launches, the step counts taken from the schedule rather than from the
+   * device, no nested cycle graphs; the FP64 relative residual
+   * ||b - A x|| / ||b|| after the last step is written to the device double
+   * relres_out, which the caller checks (a system whose solve needs more
+   * steps than recorded ends above rtol there).  info then holds the
+   * recorded counts. */
+  int32_t* schedule;
+  int schedule_capacity;
+  int schedule_mode;
+  double* relres_out;
 } nfem_solve_params;
 
 typedef struct {

@@ -69,7 +69,8 @@ class Precond(C.Structure):
 class SolveParams(C.Structure):
     _fields_ = [("rtol", C.c_double), ("inner_rtol", C.c_double), ("restart", C.c_int), ("max_inner", C.c_int),
                 ("max_outer", C.c_int), ("snapshots", C.c_void_p), ("max_snapshots", C.c_int),
-                ("no_graphs", C.c_int)]
+                ("no_graphs", C.c_int), ("schedule", C.c_void_p), ("schedule_capacity", C.c_int),
+                ("schedule_mode", C.c_int), ("relres_out", C.c_void_p)]
 
 
 class SolveInfo(C.Structure):
@@ -101,6 +102,8 @@ _SIGS = {
     "nfem_pattern_local_codes": ([_P, _I64, _I, _I, _I64, _P, _P, _P, _P, _P, _P, _P], _I),
     "nfem_points_split": ([_P, _I64, _P, _P], _I),
     "nfem_points_fixed64": ([_P, _I64, _P, _P], _I),
+    "nfem_knob_set": ([_I, _I], _I),
+    "nfem_knob_get": ([_I, C.POINTER(_I)], _I),
     "nfem_field_error_workspace_bytes": ([_P], _I),
     "nfem_field_error": ([_I, _I, _I, _I64, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _I,
                           _P, _P, _SZ, _P], _I),

@@ -1,4 +1,5 @@
-// ABI helpers, device prefix scan, coordinate split.
+// ABI helpers, device prefix scan, coordinate split, launch knobs.
+#include <atomic>
 #include <mutex>
 
 #include "nfem_common.cuh"
@@ -6,6 +7,10 @@
 namespace nfem {
 
 static int g_num_sms = 0;
+
+static std::atomic<int> g_knobs[NFEM_KNOB_COUNT];
+
+int knob(int key) { return (key >= 0 && key < NFEM_KNOB_COUNT) ? g_knobs[key].load(std::memory_order_relaxed) : 0; }
 
 int grid_for(int64_t n_items, int block, int blocks_per_sm) {
   if (g_num_sms == 0) {
@@ -338,6 +343,30 @@ extern "C" int nfem_copy_bytes(const void* src_, void* dst_, size_t bytes, void*
 }
 
 extern "C" int nfem_abi_version(void) { return 1; }
+
+extern "C" int nfem_knob_set(int key, int value) {
+  switch (key) {
+    case NFEM_KNOB_DARCY_ROWS_BLOCKS_PER_SM:
+      if (value < 0 || value > 32) return NFEM_ERR_INVALID_ARG;
+      break;
+    case NFEM_KNOB_DARCY_CELLS_BLOCK:
+      if (value != 0 && value != 128 && value != 256 && value != 512) return NFEM_ERR_INVALID_ARG;
+      break;
+    case NFEM_KNOB_ELAS_WARPS:
+      if (value != 0 && value != 2 && value != 4 && value != 8) return NFEM_ERR_INVALID_ARG;
+      break;
+    default:
+      return NFEM_ERR_INVALID_ARG;
+  }
+  g_knobs[key].store(value, std::memory_order_relaxed);
+  return NFEM_OK;
+}
+
+extern "C" int nfem_knob_get(int key, int* value) {
+  if (!value || key < 0 || key >= NFEM_KNOB_COUNT) return NFEM_ERR_INVALID_ARG;
+  *value = g_knobs[key].load(std::memory_order_relaxed);
+  return NFEM_OK;
+}
 
 extern "C" const char* nfem_status_string(int s) {
   switch (s) {

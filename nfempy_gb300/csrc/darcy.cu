@@ -458,7 +458,7 @@ __device__ __forceinline__ void records_cells(const DarcyParams& p, int64_t t, i
 }
 
 template <typename T, int DIM, int SRC>
-__global__ void __launch_bounds__(256) darcy_records_kernel(const DarcyParams p) {
+__global__ void __launch_bounds__(512) darcy_records_kernel(const DarcyParams p) {
   records_cells<T, DIM, SRC>(p, blockIdx.x * int64_t(blockDim.x) + threadIdx.x, int64_t(gridDim.x) * blockDim.x);
 }
 
@@ -1191,7 +1191,8 @@ static int launch_darcy_rows(const DarcyParams& p, cudaStream_t stream) {
     return n;
   }();
   const int64_t chunks = ceil_div(p.row_f1 - p.row_f0, 32) + ceil_div(p.row_q1 - p.row_q0, 32);
-  const int grid = grid_for(ceil_div(chunks, kDarcyWarps), 1, per_sm);
+  const int tuned = knob(NFEM_KNOB_DARCY_ROWS_BLOCKS_PER_SM);
+  const int grid = grid_for(ceil_div(chunks, kDarcyWarps), 1, tuned > 0 && tuned < per_sm ? tuned : per_sm);
   darcy_rows_kernel<T, DIM, SRC, REC><<<grid, block, 0, stream>>>(p);
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
@@ -1202,10 +1203,13 @@ static int launch_darcy_rows(const DarcyParams& p, cudaStream_t stream) {
 template <typename T, int DIM, int SRC>
 static int launch_darcy_src(const DarcyParams& p, cudaStream_t stream) {
   if (!p.rec) return launch_darcy_rows<T, DIM, SRC, false>(p, stream);
+  const int cb = knob(NFEM_KNOB_DARCY_CELLS_BLOCK) > 0 ? knob(NFEM_KNOB_DARCY_CELLS_BLOCK) : 256;
+  const int cg = grid_for(p.n_cells, cb, 8 * 256 / cb);
   if constexpr (sizeof(T) == 8 && DIM == 3) {
-    if (p.n_cells > 0) darcy_records_df_kernel<SRC><<<grid_for(p.n_cells, 256), 256, 0, stream>>>(p);
+    const int cbd = cb < 256 ? cb : 256;  // the double-float kernel is built for blocks of at most 256
+    if (p.n_cells > 0) darcy_records_df_kernel<SRC><<<grid_for(p.n_cells, cbd, 8 * 256 / cbd), cbd, 0, stream>>>(p);
   } else {
-    if (p.n_cells > 0) darcy_records_kernel<T, DIM, SRC><<<grid_for(p.n_cells, 256), 256, 0, stream>>>(p);
+    if (p.n_cells > 0) darcy_records_kernel<T, DIM, SRC><<<cg, cb, 0, stream>>>(p);
   }
   NFEM_CHECK_LAUNCH();
   return launch_darcy_rows<T, DIM, NFEM_COEF_NONE, true>(p, stream);

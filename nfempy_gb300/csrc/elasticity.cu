@@ -485,7 +485,15 @@ extern "C" int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int6
   if (value_type == NFEM_F64) {
     rc = launch_elasticity<double, kElasWarps64>(p, stream);
   } else {
-    rc = launch_elasticity<float, kElasWarps32>(p, stream);
+    const int w = knob(NFEM_KNOB_ELAS_WARPS);
+    if (w == 2)
+      rc = launch_elasticity<float, 2>(p, stream);
+    else if (w == 8)
+      rc = launch_elasticity<float, 8>(p, stream);
+    else if (w == 4)
+      rc = launch_elasticity<float, 4>(p, stream);
+    else
+      rc = launch_elasticity<float, kElasWarps32>(p, stream);
   }
   if (rc) return rc;
   NFEM_CHECK_LAUNCH();

@@ -2088,6 +2088,68 @@ extern "C" int nfem_solve_workspace_bytes(int64_t n, int restart, size_t* bytes)
 }
 
 
+// device scalars of the replayed schedule (no host round trip)
+__global__ void set_inner_target(double* __restrict__ target, const double* __restrict__ wr0, double rtol) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *target = rtol * *wr0;
+}
+__global__ void final_relres(double* __restrict__ out, const double* __restrict__ scal) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *out = scal[1] / (scal[0] > 0.0 ? scal[0] : 1.0);
+}
+
+// The solve's launches in a recorded schedule, with no host synchronisation
+// (capturable); see nfem_solve_params.schedule_mode.
+static int solve_replay(const nfem_csr* A64, const nfem_csr* A32, const nfem_precond* pc, const double* b,
+                        double* x, const nfem_solve_params* prm, SolveWs& w, bool weighted, int64_t n, int64_t ld,
+                        int m, int ldh, int gv, cudaStream_t s, nfem_solve_info* info) {
+  const int B = 256;
+  const int32_t* sch = prm->schedule;
+  const int cap = prm->schedule_capacity;
+  if (!sch || cap < 1 || sch[0] < 0 || !prm->relres_out) return NFEM_ERR_INVALID_ARG;
+  NFEM_RC(multidot<double>(n, 1, b, n, b, w.partial, w.scal + 0, 1, s));
+  NFEM_RC(spmv<double, double, double>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, x, w.r64, b, 1, s));
+  NFEM_RC(multidot<double>(n, 1, w.r64, n, w.r64, w.partial, w.scal + 1, 1, s));
+  int pos = 1;
+  const int n_outer = sch[0];
+  for (int o = 0; o < n_outer; ++o) {
+    if (pos >= cap) return NFEM_ERR_INVALID_ARG;
+    const int n_cycles = sch[pos++];
+    info->outer_iterations++;
+    cast_f64_f32<<<gv, B, 0, s>>>(n, w.r64, w.r32);
+    fill_f32<<<gv, B, 0, s>>>(n, w.d32, 0.f);
+    if (weighted)
+      scale_vec<<<gv, B, 0, s>>>(n, pc->wsqrt, w.r32, w.V, nullptr);
+    else
+      NFEM_TRY_CUDA(cudaMemcpyAsync(w.V, w.r32, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    NFEM_RC(multidot<float>(ld, 1, w.V, ld, w.V, w.partial, w.scal + 3, 1, s, nullptr, w.counter));
+    set_inner_target<<<1, 1, 0, s>>>(w.scal + 4, w.scal + 3, prm->inner_rtol);
+    for (int c = 0; c < n_cycles; ++c) {
+      if (pos >= cap) return NFEM_ERR_INVALID_ARG;
+      const int k = sch[pos++];
+      if (k < 1 || k > m) return NFEM_ERR_INVALID_ARG;
+      if (c > 0)
+        NFEM_RC(spmv<float, float, float>(n, A32->row_ptr, A32->col_idx, (const float*)A32->values, w.d32, w.V,
+                                          w.r32, 1, s, weighted ? pc->wsqrt : nullptr));
+      NFEM_RC(multidot<float>(ld, 1, w.V, ld, w.V, w.partial, w.scal + 2, 1, s, nullptr, w.counter));
+      scale_by_inv_w<<<gv, B, 0, s>>>(n, w.V, w.scal + 2, w.V, weighted ? pc->winvsqrt : nullptr, w.t32, nullptr);
+      init_cycle<<<1, 128, 0, s>>>(w.g, m, w.scal + 2, w.gate);
+      NFEM_CHECK_LAUNCH();
+      NFEM_RC(arnoldi_steps(pc, A32, n, ld, m, ldh, w, weighted, gv, s));
+      info->inner_iterations += k;
+      upper_solve<<<1, 32, 0, s>>>(w.H, ldh, w.g, k, w.y);
+      multi_axpy_f32(ld, k, w.Z, ld, w.y, w.d32, -1.0, s);
+      NFEM_CHECK_LAUNCH();
+    }
+    add_f32_to_f64<<<gv, B, 0, s>>>(n, w.d32, x);
+    NFEM_RC(spmv<double, double, double>(n, A64->row_ptr, A64->col_idx, (const double*)A64->values, x, w.r64, b, 1,
+                                         s));
+    NFEM_RC(multidot<double>(n, 1, w.r64, n, w.r64, w.partial, w.scal + 1, 1, s));
+  }
+  final_relres<<<1, 1, 0, s>>>(prm->relres_out, w.scal);
+  NFEM_CHECK_LAUNCH();
+  info->final_relres = -1.0;  // on the device (relres_out)
+  return NFEM_OK;
+}
+
 extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, const nfem_precond* pc,
                                     const double* b, double* x, const nfem_solve_params* prm, void* workspace,
                                     size_t workspace_bytes, nfem_solve_info* info, void* stream) {
@@ -2123,6 +2185,16 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
   info->outer_iterations = 0;
   info->n_snapshots = 0;
   info->status = NFEM_OK;
+  if (prm->schedule_mode == 2) return solve_replay(A64, A32, pc, b, x, prm, w, weighted, n, ld, m, ldh, gv, s, info);
+  // schedule recording: {n_outer, then per step n_cycles and the cycles' steps}
+  const bool record = prm->schedule_mode == 1 && prm->schedule && prm->schedule_capacity > 0;
+  int rec_pos = 1, rec_cycles_at = -1;
+  bool rec_ok = record;
+  auto rec_push = [&](int v) {
+    if (!rec_ok) return;
+    if (rec_pos >= prm->schedule_capacity) { rec_ok = false; return; }
+    prm->schedule[rec_pos++] = v;
+  };
   double hb[2];
   // ||b||
   NFEM_RC(multidot<double>(n, 1, b, n, b, w.partial, w.scal + 0, 1, s));
@@ -2140,6 +2212,8 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
   while (rel > prm->rtol && info->outer_iterations < prm->max_outer &&
          info->inner_iterations < prm->max_inner) {
     info->outer_iterations++;
+    rec_cycles_at = rec_pos;
+    rec_push(0);
     // inner problem A32 d = r32, d0 = 0
     cast_f64_f32<<<gv, B, 0, s>>>(n, w.r64, w.r32);
     fill_f32<<<gv, B, 0, s>>>(n, w.d32, 0.f);
@@ -2194,6 +2268,8 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       }
       info->inner_iterations += k;
       inner_res = hist[k - 1];
+      rec_push(k);
+      if (rec_ok) prm->schedule[rec_cycles_at]++;
       upper_solve<<<1, 32, 0, s>>>(w.H, ldh, w.g, k, w.y);
       // d += Z y   (multi_axpy subtracts: pass -1 via hsign)
       multi_axpy_f32(ld, k, w.Z, ld, w.y, w.d32, -1.0, s);
@@ -2222,6 +2298,7 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
     }
   }
   info->final_relres = rel;
+  if (record) prm->schedule[0] = rec_ok ? info->outer_iterations : -1;
   int32_t st = 0;
   NFEM_TRY_CUDA(cudaMemcpyAsync(&st, w.status, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   NFEM_TRY_CUDA(cudaStreamSynchronize(s));

@@ -27,6 +27,9 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // times the resident blocks per SM, capped by the work.
 int grid_for(int64_t n_items, int block, int blocks_per_sm = 8);
 
+// Current value of a launch knob (nfem_knob_set; 0 = built-in choice).
+int knob(int key);
+
 // Device-side status word: the first nonzero code written wins.
 __device__ __forceinline__ void set_status(int32_t* status, int32_t code) {
   if (status) atomicCAS(status, 0, code);

@@ -114,10 +114,11 @@ class KrylovSolver:
         if self.weighted:
             self.wsqrt = torch.empty(A.n_rows, dtype=torch.float32, device=dev)
             self.winvsqrt = torch.empty(A.n_rows, dtype=torch.float32, device=dev)
-            scratch = torch.empty(2 * A.n_rows, dtype=torch.float64, device=dev)
+            # kept with the solver: every preconditioner setup writes it
+            self._setup_scratch = torch.empty(2 * A.n_rows, dtype=torch.float64, device=dev)
             self.pc.wsqrt = _lib.ptr(self.wsqrt).value
             self.pc.winvsqrt = _lib.ptr(self.winvsqrt).value
-            self.pc.setup_scratch = _lib.ptr(scratch).value
+            self.pc.setup_scratch = _lib.ptr(self._setup_scratch).value
         a64 = _csr(A)
         _lib.call("nfem_precond_setup", _lib.C.byref(self.pc), _lib.C.byref(a64), _lib.ptr(self.status), st)
         ws_b = _lib.C.c_size_t(0)
@@ -129,15 +130,31 @@ class KrylovSolver:
             self.status.zero_()
             raise _lib.NfemError(s, "preconditioner setup")
 
+    def refresh(self, stream=None):
+        """Preconditioner setup again for new values of A (and of the FP32
+        copy), in place: no allocation and no host synchronisation, so it can
+        be captured in a CUDA graph.  setup() must have run once."""
+        if not self._setup_done:
+            raise RuntimeError("refresh() needs a first setup()")
+        a64 = _csr(self.A)
+        _lib.call("nfem_precond_setup", _lib.C.byref(self.pc), _lib.C.byref(a64), _lib.ptr(self.status),
+                  _lib.stream_ptr(stream))
+
     def solve(self, b, x=None, rtol=1e-8, inner_rtol=None, max_inner=100000, max_outer=20, stream=None,
-              raise_on_failure=True, snapshots=None):
+              raise_on_failure=True, snapshots=None, record_schedule=False, replay=False, relres_out=None):
         """Solve A x = b (FP64 device tensors) to ||b - A x|| / ||b|| <= rtol.
 
         inner_rtol: reduction of the weighted residual each FP32 inner solve
         aims for (None: the preconditioner's entry of INNER_RTOL).
 
         snapshots: optional FP32 tensor [S, n] that receives the iterate after
-        each restart cycle (res.n_snapshots of them)."""
+        each restart cycle (res.n_snapshots of them).
+
+        record_schedule: keep the launch schedule this solve took
+        (self.schedule).  replay: launch that schedule again with no host
+        synchronisation (capturable in a CUDA graph); relres_out, a device
+        double, receives the final FP64 relative residual, which the caller
+        checks: x is a solution only where it is <= rtol."""
         if not self._setup_done:
             self.setup(stream)
         A = self.A
@@ -147,6 +164,18 @@ class KrylovSolver:
             inner_rtol = INNER_RTOL.get(self.pc_kind, 1e-4)
         prm = _lib.SolveParams(float(rtol), float(inner_rtol), self.restart, int(max_inner), int(max_outer))
         prm.no_graphs = 0 if self.graphs else 1
+        if record_schedule:
+            self.schedule = np.full(1 << 14, -1, dtype=np.int32)
+            prm.schedule = self.schedule.ctypes.data
+            prm.schedule_capacity = self.schedule.size
+            prm.schedule_mode = 1
+        if replay:
+            if getattr(self, "schedule", None) is None or self.schedule[0] < 0 or relres_out is None:
+                raise ValueError("replay needs a recorded schedule and relres_out")
+            prm.schedule = self.schedule.ctypes.data
+            prm.schedule_capacity = self.schedule.size
+            prm.schedule_mode = 2
+            prm.relres_out = _lib.ptr(relres_out).value
         if snapshots is not None:
             prm.snapshots = _lib.ptr(snapshots).value
             prm.max_snapshots = int(snapshots.shape[0])
@@ -204,69 +233,68 @@ class TwoLevelCoarse:
         self.A = A
         dim = sp.dim
         dev = A.values.device
+        # the aggregate structure is built on the device: sorts, scans and
+        # scatters over the cells and rows, no host round trip of the mesh
         if cell_agg is not None:
-            agg = np.asarray(cell_agg, dtype=np.int64)
-            if agg.shape != (sp.n_cells,) or agg.min() < 0:
+            agg = torch.as_tensor(np.asarray(cell_agg) if not torch.is_tensor(cell_agg) else cell_agg,
+                                  device=dev).long()
+            if agg.shape != (sp.n_cells,) or int(agg.min().item()) < 0:
                 raise ValueError("cell_agg needs one aggregate index >= 0 per cell")
-            self.n_agg = int(agg.max()) + 1
+            self.n_agg = int(agg.max().item()) + 1
         else:
-            X = sp.mesh.points[sp.cells_host]
-            cent = X.mean(axis=1)[:, :dim]
-            lo, hi = cent.min(axis=0), cent.max(axis=0)
-            idx = np.clip(np.floor((cent - lo) / np.maximum(hi - lo, 1e-300) * n_c).astype(np.int64), 0, n_c - 1)
-            agg = np.zeros(sp.n_cells, dtype=np.int64)
+            cent = sp.points[sp.cells.long()].mean(dim=1)[:, :dim]
+            lo, hi = cent.min(dim=0).values, cent.max(dim=0).values
+            idx = ((cent - lo) / (hi - lo).clamp_min(1e-300) * n_c).floor().long().clamp_(0, n_c - 1)
+            agg = torch.zeros(sp.n_cells, dtype=torch.int64, device=dev)
             for d in range(dim):
                 agg = agg * n_c + idx[:, d]
             self.n_agg = int(n_c ** dim)
-        self.cell_agg_host = agg
-        self.counts_host = np.bincount(agg, minlength=self.n_agg)
-        if np.any(self.counts_host == 0):
+        counts = torch.bincount(agg, minlength=self.n_agg)
+        if bool((counts == 0).any().item()):
             raise ValueError("empty aggregate: choose a coarser grid")
+        self._agg = agg
+        self._counts = counts
         n = A.n_rows
         pb = sp.field_offsets["p"]
         self.p_base = pb
-        cd = sp.all_destination_indexes()
         nf = sp.dim + 1
-        p_agg = np.full((n, 2), -1, dtype=np.int64)
+        p_agg = torch.full((n, 2), -1, dtype=torch.int64, device=dev)
         p_agg[pb:pb + sp.n_cells, 0] = agg
         # flux rows: aggregates of the cells on either side of the face
-        faces = cd[:, :nf].ravel()
-        fagg = np.repeat(agg, nf)
-        order = np.lexsort((fagg, faces))
+        faces = sp.cell_dofs[:, :nf].reshape(-1).long()
+        fagg = agg.repeat_interleave(nf)
+        order = torch.sort(faces * self.n_agg + fagg).indices
         faces, fagg = faces[order], fagg[order]
-        first = np.ones(faces.size, dtype=bool)
+        first = torch.ones(faces.numel(), dtype=torch.bool, device=dev)
         first[1:] = faces[1:] != faces[:-1]
-        cnt = np.bincount(faces, minlength=n)
-        start = np.flatnonzero(first)
+        cnt = torch.bincount(faces, minlength=n)
+        start = torch.nonzero(first).squeeze(1)
         f0 = faces[start]
         a0 = fagg[start]
         two = cnt[f0] == 2
-        a1 = np.where(two, fagg[np.minimum(start + 1, faces.size - 1)], -1)
+        a1 = torch.where(two, fagg[(start + 1).clamp_max(faces.numel() - 1)], torch.full_like(a0, -1))
         boundary = cnt[f0] == 1
         differ = two & (a1 != a0)
         keep0 = boundary | differ
         p_agg[f0[keep0], 0] = a0[keep0]
         p_agg[f0[differ], 1] = a1[differ]
-        self.p_agg_host = p_agg
-        rows = np.repeat(np.arange(n), 2)
-        slots = np.arange(2 * n)
-        aa = p_agg.ravel()
-        m = aa >= 0
-        key = np.lexsort((rows[m], aa[m]))
-        pt_agg = aa[m][key]
-        self.pt_row_host = rows[m][key]
-        pt_slot = slots[m][key]
-        pt_ptr = np.zeros(self.n_agg + 1, dtype=np.int64)
-        np.add.at(pt_ptr, pt_agg + 1, 1)
-        pt_ptr = np.cumsum(pt_ptr)
-        i32 = lambda a: torch.as_tensor(np.ascontiguousarray(a).astype(np.int32), device=dev)
+        self._p_agg = p_agg
+        # P^T lists: the (row, slot) entries of every aggregate, rows ascending
+        aa = p_agg.reshape(-1)
+        slots = torch.nonzero(aa >= 0).squeeze(1)
+        key_order = torch.sort(aa[slots] * (2 * n) + slots).indices
+        pt_slot = slots[key_order]
+        pt_agg = aa[pt_slot]
+        pt_ptr = torch.zeros(self.n_agg + 1, dtype=torch.int64, device=dev)
+        pt_ptr[1:] = torch.cumsum(torch.bincount(pt_agg, minlength=self.n_agg), 0)
+        i32 = lambda a: a.to(torch.int32).contiguous()
         self.cell_agg = i32(agg)
-        self.p_agg = i32(p_agg.ravel())
+        self.p_agg = i32(p_agg.reshape(-1))
         self.p_val = torch.zeros(2 * n, dtype=torch.float32, device=dev)
         self.pt_ptr = i32(pt_ptr)
-        self.pt_row = i32(self.pt_row_host)
+        self.pt_row = i32(pt_slot // 2)
         self.pt_slot = i32(pt_slot)
-        self.pt_val = torch.zeros(max(1, pt_slot.size), dtype=torch.float32, device=dev)
+        self.pt_val = torch.zeros(max(1, pt_slot.numel()), dtype=torch.float32, device=dev)
         na = self.n_agg
         self.n_blocks = 0
         if blocks is not None:
@@ -297,7 +325,7 @@ class TwoLevelCoarse:
                _lib.ptr(self.blk_off).value if self.n_blocks else None,
                _lib.ptr(self.agg_blk).value if self.n_blocks else None)
         self.struct = _lib.TwoLevel(pb, na, _lib.ptr(self.cell_agg).value, _lib.ptr(self.w).value,
-                                    _lib.ptr(self.p_agg).value, _lib.ptr(self.p_val).value, int(pt_slot.size),
+                                    _lib.ptr(self.p_agg).value, _lib.ptr(self.p_val).value, int(pt_slot.numel()),
                                     _lib.ptr(self.pt_ptr).value, _lib.ptr(self.pt_row).value,
                                     _lib.ptr(self.pt_slot).value, _lib.ptr(self.pt_val).value,
                                     _lib.ptr(self.ac).value, _lib.ptr(self.gj).value, _lib.ptr(self.ac_inv).value,
@@ -306,6 +334,19 @@ class TwoLevelCoarse:
         self.struct.post_smooth = 1 if post_smooth else 0
         if fuse_ap:
             self._build_ap()
+
+    # host copies of the structure, for the learned preconditioner's features
+    @property
+    def cell_agg_host(self):
+        return self._agg.cpu().numpy()
+
+    @property
+    def counts_host(self):
+        return self._counts.cpu().numpy()
+
+    @property
+    def p_agg_host(self):
+        return self._p_agg.cpu().numpy()
 
     def _build_ap(self):
         A = self.A

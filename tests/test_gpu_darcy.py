@@ -292,3 +292,30 @@ def test_darcy_sliced_equals_two_pass(cuda_lib, dtype, n, shift, quarters):
     assert A2.lookahead_cells < 2 ** shift
     assert torch.equal(A1.values, A2.values)
     assert torch.equal(r1, r2)
+
+
+def test_autotune_keeps_values(cuda_lib, tmp_path, monkeypatch):
+    """The autotuner times the Darcy forms and launch shapes on a small mesh,
+    applies and caches the fastest; the tuned assembly writes the values of
+    the default one (FP32: to rounding, the forms differ in fusion)."""
+    from nfempy_gb300 import autotune
+    monkeypatch.setenv("NFEM_TUNING_CACHE", str(tmp_path / "t.json"))
+    m = mesh_gen.cube(10)
+    T = m["blocks"][-1][1].shape[0]
+    kappa = np.exp(np.sin(np.arange(T)))
+    sp, A, res = assemble_gpu(m, kappa, 1.0, torch.float32)
+    ref = A.values.clone()
+    wf = nf.LaplaceDualWeakForm(sp)
+    wf.functions = {"kappa": kappa, "rhs": 1.0}
+    key = autotune.darcy_key(sp, torch.float32)
+    try:
+        best, ms, times = autotune.tune(key, lambda: wf.assemble(A, res), autotune.darcy_candidates(3), form=wf,
+                                        reps=2)
+        assert len(times) == len(autotune.darcy_candidates(3)) and ms > 0
+        wf.assemble(A, res)
+        torch.cuda.synchronize()
+        A.check_status("tuned")
+        assert ((A.values - ref).abs().max() / ref.abs().max()).item() <= 2e-6
+        assert autotune.apply_cached(key, wf)["config"] == best
+    finally:
+        autotune.reset_knobs()

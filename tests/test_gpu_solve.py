@@ -280,3 +280,51 @@ def test_smoother_matrix_matches_cell_blocks(cuda_lib, pc):
     # iteration count (hundreds of iterations here); the two-level one is not
     slack = out[False][1] // 4 if pc == "cell_block" else max(3, out[False][1] // 20)
     assert abs(out[False][1] - out[True][1]) <= slack
+
+
+def test_recorded_schedule_replays_in_a_graph(cuda_lib):
+    """A two-level solve records its launch schedule; assembly + setup +
+    the replayed solve are then captured as one CUDA graph.  Each replay
+    reaches the same FP64 relative residual (below 1e-8) on the device and
+    the same solution as the first solve, with new coefficients between
+    replays picked up by the graph (same values -> same answer)."""
+    import nfempy_gb300 as nf
+    from nfempy_gb300 import workloads as wl
+    from nfempy_gb300.solvers import KrylovSolver, TwoLevelCoarse
+    m, sp, kappa, f = wl.darcy3d(12)
+    A32 = nf.CSRMatrix(sp, dtype=torch.float32)
+    A64 = A32.with_dtype(torch.float64)
+    r32 = torch.empty(A32.n_rows, dtype=torch.float32, device="cuda")
+    r64 = torch.empty(A32.n_rows, dtype=torch.float64, device="cuda")
+    wf = nf.LaplaceDualWeakForm(sp)
+    wf.functions = {"kappa": kappa, "rhs": f}
+    c32, c64 = wf.coefficients(torch.float32), wf.coefficients(torch.float64)
+    wf.assemble(A32, r32, coefficients=c32)
+    wf.assemble(A64, r64, coefficients=c64)
+    b = -r64
+    tl = TwoLevelCoarse(A64, 3)
+    ksp = KrylovSolver(A64, pc="two_level", A32_values=A32.values, restart=15, two_level=tl)
+    x0, info0 = ksp.solve(b.clone(), record_schedule=True)
+    assert info0.final_relres <= 1e-8 and ksp.schedule[0] == info0.outer_iterations
+    x = torch.zeros_like(b)
+    rel = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+    def step():
+        wf.assemble(A32, r32, coefficients=c32)
+        wf.assemble(A64, r64, coefficients=c64)
+        torch.neg(r64, out=b)
+        x.zero_()
+        ksp.refresh()
+        ksp.solve(b, x, replay=True, relres_out=rel)
+
+    step()  # eager once (allocations of the first call happen outside the capture)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        step()
+    for _ in range(3):
+        x.fill_(123.0)
+        g.replay()
+        torch.cuda.synchronize()
+        assert float(rel.item()) <= 1e-8
+        assert torch.allclose(x, x0, rtol=0, atol=1e-10 * x0.abs().max().item())
