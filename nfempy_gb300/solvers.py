@@ -287,7 +287,7 @@ class TwoLevelCoarse:
         pt_agg = aa[pt_slot]
         pt_ptr = torch.zeros(self.n_agg + 1, dtype=torch.int64, device=dev)
         pt_ptr[1:] = torch.cumsum(torch.bincount(pt_agg, minlength=self.n_agg), 0)
-        i32 = lambda a: a.to(torch.int32).contiguous()
+        i32 = lambda a: torch.as_tensor(a, device=dev).to(torch.int32).contiguous()
         self.cell_agg = i32(agg)
         self.p_agg = i32(p_agg.reshape(-1))
         self.p_val = torch.zeros(2 * n, dtype=torch.float32, device=dev)
