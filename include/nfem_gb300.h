@@ -332,6 +332,18 @@ int nfem_darcy_rt1_dirichlet(int dim, int value_type, int64_t n_facets, const in
                              const void* pd_q, const double* qweights, int n_qp, void* rhs,
                              void* stream);
 
+/* The same facet term for one row of an RT1 field inside a larger layout:
+ * the face DoF of local face i is cell_dofs[c * ld + dof_offset + i *
+ * dof_stride], and scale multiplies the term.  Replaces
+ * LCEDualWeakFormBCDirichlet.evaluate_form
+ * (src/weak_forms/lce_dual_weak_form.py:651-756): per component c of the
+ * stress (couple stress) field, dof_offset = field start + c, dof_stride = 3,
+ * scale = -1, pd_q = the c-th component of u_D (t_D). */
+int nfem_rt1_dirichlet_rows(int dim, int value_type, int64_t n_facets, const int32_t* facet_occ,
+                            const uint8_t* sign_mask, const int32_t* cell_dofs, int ld, int dof_offset,
+                            int dof_stride, double scale, const void* pd_q, const double* qweights, int n_qp,
+                            void* rhs, void* stream);
+
 /* Replaces l2_error (src/postprocess/l2_error_post_processor.py:7-63) for a
  * mixed Darcy RT1 x P0 solution alpha (FP64): errors[0] = ||u - u_h||_L2,
  * errors[1] = ||p - p_h||_L2 (device doubles), with the exact fields sampled

@@ -103,6 +103,8 @@ _SIGS = {
     "nfem_points_split": ([_P, _I64, _P, _P], _I),
     "nfem_points_fixed64": ([_P, _I64, _P, _P], _I),
     "nfem_knob_set": ([_I, _I], _I),
+    "nfem_rt1_dirichlet_rows": ([_I, _I, _I64, _P, _P, _P, _I, _I, _I, C.c_double, _P, C.POINTER(C.c_double), _I,
+                                 _P, _P], _I),
     "nfem_knob_get": ([_I, C.POINTER(_I)], _I),
     "nfem_field_error_workspace_bytes": ([_P], _I),
     "nfem_field_error": ([_I, _I, _I, _I64, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _I,

@@ -440,6 +440,47 @@ class LaplaceDualWeakFormBCDirichlet(WeakForm):
         self._keep = [pd, occ_t]
 
 
+class LCEDualWeakFormBCDirichlet(LaplaceDualWeakFormBCDirichlet):
+    """Displacement and rotation data on boundary facets for the mixed
+    Cosserat form (src/weak_forms/lce_dual_weak_form.py:651-756): for every
+    component c, adds -int_F u_D[c] (tau . n) to the stress row c of the
+    facet's flux DoF and -int_F t_D[c] (v . n) to its couple-stress row c.
+    functions: {"u": f(x, y, z) -> [3, N], "t": f(x, y, z) -> [3, N]} (or
+    3-vectors).  Facets whose tag is in bc_physical_tags (default: the
+    space's b_physical_tags["s"], or every tagged facet).  Residual only."""
+
+    def __init__(self, space, bc_physical_tags=None):
+        super().__init__(space, bc_physical_tags if bc_physical_tags is not None
+                         else (space.b_physical_tags.get("s") or None))
+
+    def assemble(self, jacobian, residual, accumulate=True, stream=None):
+        sp = self.space
+        dim = sp.dim
+        occ, fverts = self.facets()
+        dtype = residual.dtype
+        vt = _lib.NFEM_F64 if dtype == torch.float64 else _lib.NFEM_F32
+        pts, wts = sp.bc_quadrature[dim - 1]
+        lam = lagrange_p1_values(dim - 1, pts)
+        xq = np.einsum("qv,fvg->fqg", lam, sp.mesh.points[fverts])
+        occ_t = torch.as_tensor(occ, device=sp.device)
+        qw = np.ascontiguousarray(wts, dtype=np.float64)
+        keep = [occ_t]
+        for field, name in (("s", "u"), ("m", "t")):
+            fn = self.functions[name]
+            if callable(fn):
+                v = np.asarray(fn(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).reshape(3, *xq.shape[:2])
+            else:
+                v = np.broadcast_to(np.asarray(fn, dtype=np.float64).reshape(3, 1, 1), (3,) + xq.shape[:2])
+            for c in range(3):
+                pd = torch.as_tensor(np.ascontiguousarray(v[c]), dtype=dtype, device=sp.device)
+                keep.append(pd)
+                _lib.call("nfem_rt1_dirichlet_rows", dim, vt, len(occ), _lib.ptr(occ_t), _lib.ptr(sp.rt_sign_mask),
+                          _lib.ptr(sp.cell_dofs), sp.n_loc, sp.field_slices[field].start + c, 3, -1.0, _lib.ptr(pd),
+                          qw.ctypes.data_as(_lib.C.POINTER(_lib.C.c_double)), len(wts), _lib.ptr(residual),
+                          _lib.stream_ptr(stream))
+        self._keep = keep
+
+
 class SequentialAssembler:
     """Drop-in for src/assembly/SequentialAssembler.py:13-86 with device forms.
 

@@ -1476,6 +1476,7 @@ namespace nfem {
 template <typename T, int DIM>
 __global__ void darcy_dirichlet_kernel(int64_t n_facets, const int32_t* __restrict__ focc,
                                        const uint8_t* __restrict__ sign, const int32_t* __restrict__ cd, int ld,
+                                       int dof_offset, int dof_stride, T scale,
                                        const T* __restrict__ pd, int nq, const double qw0, const double qw1,
                                        const double qw2, const double qw3, T* __restrict__ rhs) {
   using C = DarcyConst<T, DIM>;
@@ -1490,45 +1491,52 @@ __global__ void darcy_dirichlet_kernel(int64_t n_facets, const int32_t* __restri
     T acc = T(0);
     for (int q = 0; q < nq; ++q) acc += T(qw[q]) * pd[f * nq + q];
     const T inv_ref = DIM == 3 ? T(2) : T(1);
-    rhs[cd[int64_t(c) * ld + i]] += sg * inv_ref * acc;
+    rhs[cd[int64_t(c) * ld + dof_offset + i * dof_stride]] += scale * sg * inv_ref * acc;
   }
 }
 }  // namespace nfem
 
-extern "C" int nfem_darcy_rt1_dirichlet(int dim, int value_type, int64_t n_facets, const int32_t* facet_occ,
-                                        const uint8_t* sign_mask, const int32_t* cell_dofs, int ld,
-                                        const void* pd_q, const double* qweights, int n_qp, void* rhs,
-                                        void* stream_) {
-  cudaStream_t stream = (cudaStream_t)stream_;
+static int rt1_dirichlet(int dim, int value_type, int64_t n_facets, const int32_t* facet_occ,
+                         const uint8_t* sign_mask, const int32_t* cell_dofs, int ld, int dof_offset, int dof_stride,
+                         double scale, const void* pd_q, const double* qweights, int n_qp, void* rhs,
+                         cudaStream_t stream) {
   if ((dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_facets < 0 ||
-      n_qp < 1 || n_qp > 4 || !qweights || ld < dim + 1)
+      n_qp < 1 || n_qp > 4 || !qweights || dof_offset < 0 || dof_stride < 1 ||
+      ld < dof_offset + dim * dof_stride + 1)
     return NFEM_ERR_INVALID_ARG;
   if (n_facets == 0) return NFEM_OK;
   if (!facet_occ || !sign_mask || !cell_dofs || !pd_q || !rhs) return NFEM_ERR_INVALID_ARG;
   double w[4] = {0, 0, 0, 0};
   for (int q = 0; q < n_qp; ++q) w[q] = qweights[q];
   const int g = grid_for(n_facets, 256);
+#define NFEM_DIRICHLET(T, D)                                                                                        \
+  darcy_dirichlet_kernel<T, D><<<g, 256, 0, stream>>>(n_facets, facet_occ, sign_mask, cell_dofs, ld, dof_offset,   \
+                                                      dof_stride, T(scale), (const T*)pd_q, n_qp, w[0], w[1],      \
+                                                      w[2], w[3], (T*)rhs)
   if (value_type == NFEM_F64) {
-    if (dim == 3)
-      darcy_dirichlet_kernel<double, 3><<<g, 256, 0, stream>>>(n_facets, facet_occ, sign_mask, cell_dofs, ld,
-                                                               (const double*)pd_q, n_qp, w[0], w[1], w[2], w[3],
-                                                               (double*)rhs);
-    else
-      darcy_dirichlet_kernel<double, 2><<<g, 256, 0, stream>>>(n_facets, facet_occ, sign_mask, cell_dofs, ld,
-                                                               (const double*)pd_q, n_qp, w[0], w[1], w[2], w[3],
-                                                               (double*)rhs);
+    if (dim == 3) NFEM_DIRICHLET(double, 3); else NFEM_DIRICHLET(double, 2);
   } else {
-    if (dim == 3)
-      darcy_dirichlet_kernel<float, 3><<<g, 256, 0, stream>>>(n_facets, facet_occ, sign_mask, cell_dofs, ld,
-                                                              (const float*)pd_q, n_qp, w[0], w[1], w[2], w[3],
-                                                              (float*)rhs);
-    else
-      darcy_dirichlet_kernel<float, 2><<<g, 256, 0, stream>>>(n_facets, facet_occ, sign_mask, cell_dofs, ld,
-                                                              (const float*)pd_q, n_qp, w[0], w[1], w[2], w[3],
-                                                              (float*)rhs);
+    if (dim == 3) NFEM_DIRICHLET(float, 3); else NFEM_DIRICHLET(float, 2);
   }
+#undef NFEM_DIRICHLET
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
+}
+
+extern "C" int nfem_darcy_rt1_dirichlet(int dim, int value_type, int64_t n_facets, const int32_t* facet_occ,
+                                        const uint8_t* sign_mask, const int32_t* cell_dofs, int ld,
+                                        const void* pd_q, const double* qweights, int n_qp, void* rhs,
+                                        void* stream_) {
+  return rt1_dirichlet(dim, value_type, n_facets, facet_occ, sign_mask, cell_dofs, ld, 0, 1, 1.0, pd_q, qweights,
+                       n_qp, rhs, (cudaStream_t)stream_);
+}
+
+extern "C" int nfem_rt1_dirichlet_rows(int dim, int value_type, int64_t n_facets, const int32_t* facet_occ,
+                                       const uint8_t* sign_mask, const int32_t* cell_dofs, int ld, int dof_offset,
+                                       int dof_stride, double scale, const void* pd_q, const double* qweights,
+                                       int n_qp, void* rhs, void* stream_) {
+  return rt1_dirichlet(dim, value_type, n_facets, facet_occ, sign_mask, cell_dofs, ld, dof_offset, dof_stride, scale,
+                       pd_q, qweights, n_qp, rhs, (cudaStream_t)stream_);
 }
 
 // ------------------------------------------------------------------ L2 error

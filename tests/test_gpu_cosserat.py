@@ -121,3 +121,38 @@ def test_cosserat_solve_matches_superlu_and_converges(cuda_lib):
     errs = np.array(errs)
     rates = errs[0] / errs[1]
     assert np.all(rates > 1.6), (errs, rates)
+
+
+def test_cosserat_dirichlet_matches_oracle(cuda_lib):
+    """LCEDualWeakFormBCDirichlet: -int_F u_D[c] (tau . n) on the stress rows
+    and -int_F t_D[c] (v . n) on the couple-stress rows of every boundary
+    facet's flux DoF, against the oracle's facet restatement (normal from
+    compute_normal, basis traced from the neighbour cell), FP64 1e-12."""
+    from nfempy_gb300.assembly import LCEDualWeakFormBCDirichlet
+    m = mesh_gen.cube(2)
+    sp = product_space(m, FIELDS)
+    A = nf.CSRMatrix(sp, dtype=torch.float64)
+    res = torch.zeros(A.n_rows, dtype=torch.float64, device="cuda")
+    uD = lambda x, y, z: np.array([1 + x, y * z, np.sin(z) + 0 * x])
+    tD = lambda x, y, z: np.array([0.5 + 0 * x, x * x, y - z])
+    bc = LCEDualWeakFormBCDirichlet(sp)
+    bc.functions = {"u": uD, "t": tD}
+    bc.assemble(A, res)
+    torch.cuda.synchronize()
+    rg = res.cpu().numpy()
+    topo = topology.Topology(m)
+    cd, nd = topology.cell_dofs(topo, [topology.FieldSpec(*f) for f in FIELDS])
+    X = m["points"][topo.cells]
+    s = topo.rt1_signs()
+    qf = quadrature.make_quadrature(2, 3)
+    ro = np.zeros(nd)
+    occ, fverts = bc.facets()
+    assert len(occ) == 6 * 2 * 2 * 2
+    for o, fv in zip(occ, fverts):
+        c, i = divmod(int(o), 4)
+        for off, fn in ((0, uD), (12, tD)):
+            for comp in range(3):
+                val = forms.darcy_dirichlet_facet(X[c], s[c], i, m["points"][fv], 3, qf,
+                                                  lambda x, y, z: np.array([fn(x, y, z)[comp]]))
+                ro[cd[c, off + i * 3 + comp]] -= val
+    np.testing.assert_allclose(rg, ro, rtol=1e-12, atol=1e-13 * np.abs(ro).max())
