@@ -39,7 +39,8 @@ typedef enum {
   NFEM_ERR_BREAKDOWN = 9,     /* Krylov breakdown (zero or non-finite denominator) */
   NFEM_ERR_NONFINITE = 10,    /* NaN / Inf detected in an input or residual */
   NFEM_ERR_DEGENERATE = 11,   /* a cell with |det J| == 0 */
-  NFEM_ERR_DOMAIN = 12        /* a coefficient outside its domain (kappa <= 0, mu <= 0) */
+  NFEM_ERR_DOMAIN = 12,       /* a coefficient outside its domain (kappa <= 0, mu <= 0) */
+  NFEM_ERR_TIMEOUT = 13       /* a bounded device-side wait ran out */
 } nfem_status;
 
 typedef enum { NFEM_F64 = 0, NFEM_F32 = 1, NFEM_BF16 = 2 } nfem_value_type;
@@ -198,6 +199,20 @@ int nfem_pattern_pairs(const int32_t* inc_ptr, const int32_t* inc, const uint32_
  * double-float values with integer operations.  No reference counterpart
  * (device data layout). */
 int nfem_points_fixed64(const double* points, int64_t n_points, int64_t* records, void* stream);
+
+/* Adds element matrices j_el [n_el, n_loc, n_loc] and residuals r_el
+ * [n_el, n_loc] (either may be NULL) of value_type into the CSR values and
+ * rhs at the rows / columns dofs [n_el, n_loc]: the generic path of
+ * scatter_form_data / scatter_interface_form_data /
+ * scatter_time_dependent_form_data (src/assembly/ScatterFormData.py:5-79)
+ * for weak forms evaluated outside the library.  Atomic additions (the
+ * order of the additions into one entry may vary); an entry outside the
+ * pattern sets NFEM_ERR_PATTERN, a DoF outside [0, n_rows)
+ * NFEM_ERR_INVALID_ARG, in dev_status. */
+int nfem_scatter_elements(int value_type, int64_t n_el, int n_loc, const int32_t* dofs,
+                          const void* j_el, const void* r_el, const int32_t* row_ptr,
+                          const int32_t* col_idx, int64_t n_rows, void* values, void* rhs,
+                          int32_t* dev_status, void* stream);
 
 /* Copies `bytes` from src to dst with a kernel (16-byte vectors when both are
  * 16-byte aligned).  Either pointer may be pinned host memory mapped into the
@@ -651,6 +666,14 @@ int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, const nfem_pr
  * W_l [out, in] row-major; activations batch-major.  weight_type NFEM_BF16
  * reads BF16 weights (and biases from params_f32), FP32 accumulation. */
 int nfem_mlp_param_count(const int32_t* dims, int64_t* count);
+/* Inference of the same network on the tensor cores (tcgen05.mma, BF16 x
+ * BF16 -> FP32 accumulators in tensor memory): y [batch] = the network's
+ * output for x [batch, dims[0]], one fused persistent kernel.  params = the
+ * BF16 copy, params_f32 = the FP32 master (biases).  The hidden activations
+ * after layer 1 are rounded to BF16 (the MMA operand type).  Shapes other
+ * than dims = {<= 16, 256, 256, 1} return NFEM_ERR_UNSUPPORTED. */
+int nfem_mlp_infer_tc(const int32_t* dims, const void* params, const float* params_f32, int64_t batch,
+                      const float* x, float* y, int32_t* dev_status, void* stream);
 int nfem_mlp_forward(const int32_t* dims, int weight_type, const void* params,
                      const float* params_f32, int64_t batch, const float* x, float* h1,
                      float* h2, float* y, void* stream);

@@ -24,7 +24,7 @@ STATUS_NAMES = {
     0: "NFEM_OK", 1: "NFEM_ERR_INVALID_ARG", 2: "NFEM_ERR_CUDA", 3: "NFEM_ERR_WORKSPACE",
     4: "NFEM_ERR_OVERFLOW", 5: "NFEM_ERR_CAPACITY", 6: "NFEM_ERR_PATTERN", 7: "NFEM_ERR_UNSUPPORTED",
     8: "NFEM_ERR_NOT_CONVERGED", 9: "NFEM_ERR_BREAKDOWN", 10: "NFEM_ERR_NONFINITE",
-    11: "NFEM_ERR_DEGENERATE", 12: "NFEM_ERR_DOMAIN",
+    11: "NFEM_ERR_DEGENERATE", 12: "NFEM_ERR_DOMAIN", 13: "NFEM_ERR_TIMEOUT",
 }
 
 
@@ -103,6 +103,8 @@ _SIGS = {
     "nfem_points_split": ([_P, _I64, _P, _P], _I),
     "nfem_points_fixed64": ([_P, _I64, _P, _P], _I),
     "nfem_knob_set": ([_I, _I], _I),
+    "nfem_mlp_infer_tc": ([_P, _P, _P, _I64, _P, _P, _P, _P], _I),
+    "nfem_scatter_elements": ([_I, _I64, _I, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P], _I),
     "nfem_rt1_dirichlet_rows": ([_I, _I, _I64, _P, _P, _P, _I, _I, _I, C.c_double, _P, C.POINTER(C.c_double), _I,
                                  _P, _P], _I),
     "nfem_knob_get": ([_I, C.POINTER(_I)], _I),

@@ -28,7 +28,12 @@ from .elements import lagrange_p1_values
 class CSRMatrix:
     """Global sparse matrix on the device with the pattern of a space's element cliques."""
 
-    def __init__(self, space, dtype=torch.float64, codes=True, stream=None):
+    def __init__(self, space, dtype=torch.float64, codes=True, stream=None, extra_cliques=None):
+        """extra_cliques: optional list of int arrays [n, k] of global DoFs
+        whose (row, column) pairs join the pattern (the couplings of an
+        interface form, whose two cells' DoFs meet in one element matrix).
+        A matrix with extra cliques is filled by host-evaluated forms only:
+        the device forms need the cell-clique pattern."""
         if space.cell_dofs is None:
             raise ValueError("build_structures() the space first")
         self.space = space
@@ -53,6 +58,10 @@ class CSRMatrix:
         _lib.call("nfem_pattern_cols", _lib.ptr(space.cell_dofs), T, n_loc, n_loc, self.n_rows,
                   _lib.ptr(self.inc_ptr), _lib.ptr(self.inc), _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
                   _lib.ptr(self.status), st)
+        self.extended = False
+        if extra_cliques:
+            self._merge_cliques(extra_cliques)
+            codes = False
         self.codes = None
         if codes and n_loc <= 8:
             self.codes = torch.empty(T * n_loc, dtype=torch.int32, device=dev)
@@ -62,7 +71,7 @@ class CSRMatrix:
         self.node_codes = None
         vec = [space.discrete_spaces[n] for n in space.names]
         ncs = {f.n_comp for f in vec}
-        if (self.codes is None and len(ncs) == 1 and vec[0].n_comp > 1 and n_loc % vec[0].n_comp == 0
+        if (codes and self.codes is None and len(ncs) == 1 and vec[0].n_comp > 1 and n_loc % vec[0].n_comp == 0
                 and n_loc // vec[0].n_comp <= 16 and space.dof_shift % vec[0].n_comp == 0):
             self.n_comp = vec[0].n_comp
             self.node_codes = torch.empty((T * n_loc, 16), dtype=torch.uint8, device=dev)
@@ -97,6 +106,37 @@ class CSRMatrix:
         self.values = torch.zeros(max(self.nnz, 1), dtype=dtype, device=dev)
         self.fresh = True
         self.check_status("pattern")
+
+    def _merge_cliques(self, cliques):
+        """Union of the cell-clique pattern and the (row, column) pairs of
+        extra cliques, built on the device (sorted unique pair keys)."""
+        dev = self.row_ptr.device
+        n = self.n_rows
+        rp = self.row_ptr.long()
+        rows = torch.repeat_interleave(torch.arange(n, device=dev), rp[1:] - rp[:-1])
+        keys = [rows * n + self.col_idx[: self.nnz].long()]
+        for q in cliques:
+            q = torch.as_tensor(np.asarray(q, dtype=np.int64), device=dev)
+            if q.numel() == 0:
+                continue
+            if q.dim() != 2 or int(q.min().item()) < 0 or int(q.max().item()) >= n:
+                raise ValueError("extra cliques must be [n, k] arrays of DoFs in [0, n_rows)")
+            keys.append((q[:, :, None] * n + q[:, None, :]).reshape(-1))
+        key = torch.unique(torch.cat(keys))
+        r = key // n
+        self.col_idx = (key % n).to(torch.int32).contiguous()
+        self.row_ptr = torch.zeros(n + 1, dtype=torch.int32, device=dev)
+        self.row_ptr[1:] = torch.cumsum(torch.bincount(r, minlength=n), 0).to(torch.int32)
+        self.nnz = int(key.numel())
+        self.extended = True
+
+    def createVecLeft(self):
+        """A zero device vector of the row space (PETSc Mat.createVecLeft)."""
+        return torch.zeros(self.n_rows, dtype=self.dtype, device=self.values.device)
+
+    def createVecRight(self):
+        """A zero device vector of the column space (PETSc Mat.createVecRight)."""
+        return torch.zeros(self.n_rows, dtype=self.dtype, device=self.values.device)
 
     def max_node_degree(self):
         """Largest number of node columns in a node row (row length / n_comp),
@@ -482,24 +522,43 @@ class LCEDualWeakFormBCDirichlet(LaplaceDualWeakFormBCDirichlet):
 
 
 class SequentialAssembler:
-    """Drop-in for src/assembly/SequentialAssembler.py:13-86 with device forms.
+    """Drop-in for src/assembly/SequentialAssembler.py:13-86.
 
     `jacobian` is a CSRMatrix; `residual` a device tensor (or a host numpy
     array, updated in place with a device->host copy at the end).  A call to
     scatter_forms() is one assembly pass: the first form overwrites the
     matrix values and the residual (they are treated as zeroed, as every
     reference driver creates them), later forms of the pass add to them.
+
+    The six form types of the reference (SequentialAssembler.py:20-30) are
+    accepted with its input lists:
+      "form" / "bc_form":               [type, sequence, form, alpha]
+      "interface_form":                 [type, [(idx, (idx_p, idx_n)), ...], form, alpha]
+      "bc_interface_form":              [type, [(idx, idx_p), ...], form, alpha]
+      "time_dependent_form" / "..._bc_form": [type, sequence, form, (alpha_n, alpha), t]
+    A device form (LaplaceDualWeakForm, LEPrimalWeakForm, LCEDualWeakForm,
+    their boundary forms, ...) assembles every cell in one launch.  Any
+    other form object is evaluated on the host element by element exactly
+    as the reference calls it (ScatterFormData.py:28-79: evaluate_form on
+    the element's slice of alpha, with the same arguments; a form may offer
+    evaluate_forms(indices, alphas) returning batched (r [n, k], j [n, k, k])
+    instead), and the batch is added into the device CSR and residual by
+    one scatter kernel (nfem_scatter_elements).
     """
+
+    _GENERIC = ("form", "bc_form", "interface_form", "bc_interface_form", "time_dependent_form",
+                "time_dependent_bc_form")
 
     def __init__(self, space, jacobian, residual):
         self.space = space
         self.jacobian = jacobian
         self.residual = residual
         self._form_to_input_list = None
+        self._dest = None
 
     @property
     def form_type_to_callable_map(self):
-        return {"form": self._scatter_form, "bc_form": self._scatter_bc_form}
+        return {t: (lambda *a, _t=t: self._scatter(_t, *a)) for t in self._GENERIC}
 
     @property
     def form_to_input_list(self):
@@ -509,6 +568,11 @@ class SequentialAssembler:
     def form_to_input_list(self, v):
         self._form_to_input_list = v
 
+    @staticmethod
+    def _is_device_form(form):
+        return isinstance(form, WeakForm) and callable(getattr(form, "assemble", None))
+
+    # ------------------------------------------------------------ device forms
     def _scatter_form(self, form, sequence, alpha, residual, accumulate):
         n = self.space.n_cells
         seq = range(n) if sequence is None else sequence
@@ -524,23 +588,138 @@ class SequentialAssembler:
             raise NotImplementedError("a boundary form adds to a pass that starts with a cell form")
         form.assemble(self.jacobian, residual, accumulate=True)
 
+    # ------------------------------------------------------------ host-evaluated forms
+    def _cell_dest(self):
+        if self._dest is None:
+            self._dest = self.space.all_destination_indexes()
+        return self._dest
+
+    @staticmethod
+    def _host(a):
+        if a is None:
+            return None
+        if torch.is_tensor(a):
+            return a.detach().double().cpu().numpy()
+        return np.asarray(a)
+
+    def _evaluate(self, form_type, form, items, alpha, alpha_n, t):
+        """Element data of a host-evaluated form: (dest list, r list, j list),
+        with the reference's arguments per element."""
+        sp = self.space
+        dest_all = self._cell_dest()
+        dests, rs, js = [], [], []
+        batched = getattr(form, "evaluate_forms", None)
+        if form_type == "form":
+            idx = np.asarray(list(items), dtype=np.int64)
+            d = dest_all[idx]
+            if batched is not None:
+                r, j = batched(idx, alpha[d])
+                return list(d), list(np.asarray(r)), list(np.asarray(j))
+            for i, di in zip(idx, d):
+                r, j = form.evaluate_form(int(i), alpha[di])
+                dests.append(di), rs.append(r), js.append(j)
+        elif form_type == "time_dependent_form":
+            for i in items:
+                di = dest_all[int(i)]
+                r, j = form.evaluate_form(int(i), alpha_n[di], alpha[di], t)
+                dests.append(di), rs.append(r), js.append(j)
+        elif form_type == "bc_form":
+            for i in items:
+                di = sp.bc_destination_indexes(int(i))
+                r, j = form.evaluate_form(int(i), alpha[di])
+                dests.append(di), rs.append(r), js.append(j)
+        elif form_type == "time_dependent_bc_form":
+            for i in items:
+                di = sp.bc_destination_indexes(int(i))
+                # the reference takes this slice from alpha_n (ScatterFormData.py:43-49)
+                r, j = form.evaluate_form(int(i), alpha_n[di], t)
+                dests.append(di), rs.append(r), js.append(j)
+        elif form_type == "interface_form":
+            for idx, pair in items:
+                p, n = pair
+                dp, dn = dest_all[int(p)], dest_all[int(n)]
+                r, j = form.evaluate_form(idx, pair, (alpha[dp], alpha[dn]))
+                dests.append(np.concatenate((dp, dn))), rs.append(r), js.append(j)
+        elif form_type == "bc_interface_form":
+            for idx, p in items:
+                dp = dest_all[int(p)]
+                r, j = form.evaluate_form(idx, p, alpha[dp])
+                dests.append(dp), rs.append(r), js.append(j)
+        else:
+            raise NotImplementedError(f"form type {form_type}")
+        return dests, rs, js
+
+    def _scatter_host(self, form_type, form, items, alpha, alpha_n, t, residual):
+        A = self.jacobian
+        n = A.n_rows
+        alpha = self._host(alpha) if alpha is not None else np.zeros(n)
+        alpha_n = self._host(alpha_n) if alpha_n is not None else alpha
+        dests, rs, js = self._evaluate(form_type, form, items, alpha, alpha_n, t)
+        if not dests:
+            return
+        vt = _lib.NFEM_F64 if A.dtype == torch.float64 else _lib.NFEM_F32
+        npdt = np.float64 if A.dtype == torch.float64 else np.float32
+        dev = A.values.device
+        groups = {}
+        for k, d in enumerate(dests):
+            groups.setdefault(len(d), []).append(k)
+        for k_loc, ks in groups.items():
+            if k_loc == 0:
+                continue
+            d = np.stack([np.asarray(dests[k], dtype=np.int64) for k in ks])
+            if d.min() < 0 or d.max() >= n or d.max() >= 2 ** 31:
+                raise ValueError("destination index outside the matrix")
+            r = np.stack([np.asarray(rs[k], dtype=np.float64).reshape(k_loc) for k in ks]).astype(npdt)
+            j = np.stack([np.asarray(js[k], dtype=np.float64).reshape(k_loc, k_loc) for k in ks]).astype(npdt)
+            d_t = torch.as_tensor(d.astype(np.int32), device=dev)
+            r_t = torch.as_tensor(r, device=dev)
+            j_t = torch.as_tensor(j, device=dev)
+            _lib.call("nfem_scatter_elements", vt, len(ks), k_loc, _lib.ptr(d_t), _lib.ptr(j_t), _lib.ptr(r_t),
+                      _lib.ptr(A.row_ptr), _lib.ptr(A.col_idx), n, _lib.ptr(A.values), _lib.ptr(residual),
+                      _lib.ptr(A.status), _lib.stream_ptr(None))
+        A.check_status(f"scatter of a {form_type}")
+
+    def _scatter(self, form_type, input_list, residual, accumulate):
+        if "time_dependent" in form_type:
+            _, sequence, form, alphas, t = input_list
+            alpha_n, alpha = alphas
+        else:
+            _, sequence, form, alpha = input_list[:4]
+            alpha_n, t = None, None
+        if self._is_device_form(form):
+            if form_type == "form":
+                return self._scatter_form(form, sequence, alpha, residual, accumulate)
+            if form_type == "bc_form":
+                return self._scatter_bc_form(form, sequence, alpha, residual, accumulate)
+            raise NotImplementedError(f"a device form in a {form_type} entry")
+        return self._scatter_host(form_type, form, sequence, alpha, alpha_n, t, residual)
+
     def scatter_forms(self, measure_time_q=False):
+        items = list(self.form_to_input_list.items())
+        for name, input_list in items:
+            if input_list[0] not in self._GENERIC:
+                raise NotImplementedError(f"form type {input_list[0]}")
+            want = 5 if "time_dependent" in input_list[0] else 4
+            if len(input_list) != want:
+                raise ValueError(f"{name}: a {input_list[0]} entry has {want} items")
         host_res = None
         residual = self.residual
         if not torch.is_tensor(residual):
             host_res = residual
             residual = torch.zeros(self.jacobian.n_rows, dtype=self.jacobian.dtype, device=self.space.device)
         accumulate = not self.jacobian.fresh
+        first_device = bool(items) and self._is_device_form(items[0][1][2])
+        if not accumulate and not first_device:
+            # a pass that starts with a host-evaluated form adds into zeros
+            self.jacobian.values.zero_()
+            residual.zero_()
+            accumulate = True
         first = True
-        for name, input_list in self.form_to_input_list.items():
+        for name, input_list in items:
             if measure_time_q:
                 torch.cuda.synchronize()
                 st = time.time()
-            form_type = input_list[0]
-            if form_type not in self.form_type_to_callable_map:
-                raise NotImplementedError(f"form type {form_type}")
-            _, sequence, form, alpha = input_list[:4]
-            self.form_type_to_callable_map[form_type](form, sequence, alpha, residual, accumulate or not first)
+            self._scatter(input_list[0], input_list, residual, accumulate or not first)
             first = False
             if measure_time_q:
                 torch.cuda.synchronize()

@@ -383,6 +383,7 @@ extern "C" const char* nfem_status_string(int s) {
     case NFEM_ERR_NONFINITE: return "non-finite value";
     case NFEM_ERR_DEGENERATE: return "degenerate cell (|det J| == 0)";
     case NFEM_ERR_DOMAIN: return "coefficient outside its domain (kappa <= 0 or mu <= 0)";
+    case NFEM_ERR_TIMEOUT: return "a bounded device-side wait ran out";
     default: return "unknown status";
   }
 }

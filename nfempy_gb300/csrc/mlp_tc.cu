@@ -1,0 +1,295 @@
+// K6b: inference of the learned preconditioner's network on the 5th-generation
+// tensor cores (tcgen05 + TMEM), one fused kernel for the three layers.
+//
+// No reference counterpart: nfempy has no learned component.  Network and
+// parameter layout as in mlp.cu: y = W3 relu(W2 relu(W1 x + b1) + b2) + b3,
+// weights [out, in] row-major in one flat vector [W1 | b1 | W2 | b2 | W3 | b3],
+// BF16 weights (the inference copy), FP32 biases.  This kernel covers the
+// shape the preconditioner uses: in <= 16 features, two hidden layers of
+// width 256, one output.
+//
+// Per tile of 128 rows (faces):
+//   1. layer 1 on the CUDA cores (K = in is too short for an MMA): each of
+//      the 256 threads computes 128 of the 256 hidden values of one row,
+//      applies the ReLU and stores BF16 into the A tile in shared memory;
+//   2. layer 2 on the tensor cores: one thread issues 16 tcgen05.mma
+//      (kind::f16, BF16 x BF16 -> FP32, M = 128, N = 256, K = 16 each) from
+//      the A tile and the resident W2 tile, accumulating the 128 x 256 block
+//      in tensor memory (256 of the SM's 512 TMEM columns), and commits them
+//      to an mbarrier;
+//   3. epilogue: each warp reads its 32 TMEM lanes (rows) and 128 columns
+//      with tcgen05.ld, adds b2, applies the ReLU and contracts with W3; the
+//      two column halves of a row meet in shared memory and the row's output
+//      is written once.
+// The grid is persistent (one CTA per SM, W2 loaded once per CTA).
+//
+// Shared-memory operands use the canonical no-swizzle K-major layout of the
+// UMMA descriptors: 8-row x 16-byte core matrices, the 16-byte K chunks of
+// a row group adjacent (leading byte offset 128 B), row groups 4096 B apart
+// (stride byte offset), so element (row, k) of a 256-wide BF16 operand lives
+// at (row % 8) * 16 + (row / 8) * 4096 + (k % 8) * 2 + (k / 8) * 128.
+#include <cuda_bf16.h>
+
+#include "nfem_common.cuh"
+
+namespace nfem {
+namespace {
+
+constexpr int kTM = 128;        // rows per tile (MMA M)
+constexpr int kH = 256;         // hidden width (MMA N and K extent)
+constexpr int kInMax = 16;      // input features
+constexpr int kThreads = 256;
+constexpr uint32_t kTmemCols = 256;
+constexpr uint32_t kRowGroupBytes = (kH / 8) * 128;  // 4096: stride between 8-row groups
+
+constexpr size_t kOffA = 0;
+constexpr size_t kOffB = kOffA + size_t(kTM) * kH * 2;        // 65536
+constexpr size_t kOffW1 = kOffB + size_t(kH) * kH * 2;        // 196608
+constexpr size_t kOffB1 = kOffW1 + size_t(kH) * kInMax * 4;   // 212992
+constexpr size_t kOffB2 = kOffB1 + kH * 4;
+constexpr size_t kOffW3 = kOffB2 + kH * 4;
+constexpr size_t kOffPart = kOffW3 + kH * 4;
+constexpr size_t kOffBar = kOffPart + kTM * 4;
+constexpr size_t kOffSlot = kOffBar + 8;
+constexpr size_t kOffFlag = kOffSlot + 4;
+constexpr size_t kSmemBytes = kOffFlag + 4 + 1024;  // + alignment slack
+
+// Instruction descriptor of tcgen05.mma kind::f16: D FP32 (bits 4-5 = 1),
+// A and B BF16 (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0),
+// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kH >> 3) << 17) |
+                            (uint32_t(kTM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading
+// byte offset >> 4 (bits 16-29), stride byte offset >> 4 (bits 32-45), the
+// fixed value 0b001 at bits 46-48, base offset 0, no swizzle (bits 61-63).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return uint64_t((saddr & 0x3FFFFu) >> 4) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
+         (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
+}
+
+__device__ __forceinline__ uint32_t operand_offset(int row, int k) {
+  return uint32_t((row & 7) * 16 + (row >> 3) * kRowGroupBytes + (k & 7) * 2 + (k >> 3) * 128);
+}
+
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool bar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Bounded wait for the MMA commit: about a second of polling at most.
+constexpr uint32_t kWaitPolls = 1u << 22;
+
+template <int KIN>
+__global__ void __launch_bounds__(kThreads, 1)
+    mlp_infer_tc_kernel(int64_t n_rows, int n_in, const __nv_bfloat16* __restrict__ W1,
+                        const float* __restrict__ b1, const __nv_bfloat16* __restrict__ W2,
+                        const float* __restrict__ b2, const __nv_bfloat16* __restrict__ W3,
+                        const float* __restrict__ b3p, const float* __restrict__ x, float* __restrict__ y,
+                        int32_t* status) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sA = smem + kOffA;
+  uint8_t* sB = smem + kOffB;
+  float* sW1 = reinterpret_cast<float*>(smem + kOffW1);
+  float* sb1 = reinterpret_cast<float*>(smem + kOffB1);
+  float* sb2 = reinterpret_cast<float*>(smem + kOffB2);
+  float* sw3 = reinterpret_cast<float*>(smem + kOffW3);
+  float* spart = reinterpret_cast<float*>(smem + kOffPart);
+  uint64_t* sbar = reinterpret_cast<uint64_t*>(smem + kOffBar);
+  uint32_t* sslot = reinterpret_cast<uint32_t*>(smem + kOffSlot);
+  volatile int32_t* sflag = reinterpret_cast<volatile int32_t*>(smem + kOffFlag);
+  const int t = threadIdx.x, warp = t >> 5;
+
+  // resident operands: W2 in the canonical layout, W1 / biases / W3 in FP32
+  const bool w2_aligned = (reinterpret_cast<uintptr_t>(W2) & 15) == 0;
+  for (int idx = t; idx < kH * (kH / 8); idx += kThreads) {
+    const int n = idx >> 5, kc = idx & 31;
+    uint4 v;
+    if (w2_aligned) {
+      v = *reinterpret_cast<const uint4*>(W2 + size_t(n) * kH + kc * 8);
+    } else {
+      uint16_t e[8];
+      for (int q = 0; q < 8; ++q) e[q] = reinterpret_cast<const uint16_t*>(W2)[size_t(n) * kH + kc * 8 + q];
+      v.x = e[0] | (uint32_t(e[1]) << 16); v.y = e[2] | (uint32_t(e[3]) << 16);
+      v.z = e[4] | (uint32_t(e[5]) << 16); v.w = e[6] | (uint32_t(e[7]) << 16);
+    }
+    *reinterpret_cast<uint4*>(sB + operand_offset(n, kc * 8)) = v;
+  }
+  for (int idx = t; idx < kH * KIN; idx += kThreads) {
+    const int j = idx / KIN, k = idx % KIN;
+    sW1[idx] = k < n_in ? __bfloat162float(W1[size_t(j) * n_in + k]) : 0.f;
+  }
+  const float b3 = *b3p;
+  for (int j = t; j < kH; j += kThreads) {
+    sb1[j] = b1[j];
+    sb2[j] = b2[j];
+    sw3[j] = __bfloat162float(W3[j]);
+  }
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(sbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *sflag = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(sslot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = *sslot;
+  const uint32_t bar = smem_u32(sbar);
+  const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
+
+  const int r = t & (kTM - 1), half = t >> 7;
+  const int64_t n_tiles = (n_rows + kTM - 1) / kTM;
+  uint32_t parity = 0;
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t row = tile * kTM + r;
+    // ---- layer 1 (CUDA cores) -> BF16 A tile
+    float xr[KIN];
+#pragma unroll
+    for (int k = 0; k < KIN; ++k) xr[k] = (row < n_rows && k < n_in) ? x[row * n_in + k] : 0.f;
+    for (int j0 = half * (kH / 2); j0 < (half + 1) * (kH / 2); j0 += 8) {
+      uint32_t packed[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float v[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int j = j0 + 2 * q + e;
+          float s = sb1[j];
+#pragma unroll
+          for (int k = 0; k < KIN; ++k) s = fmaf(sW1[j * KIN + k], xr[k], s);
+          v[e] = fmaxf(s, 0.f);
+        }
+        const __nv_bfloat162 h = __floats2bfloat162_rn(v[0], v[1]);
+        packed[q] = *reinterpret_cast<const uint32_t*>(&h);
+      }
+      *reinterpret_cast<uint4*>(sA + operand_offset(r, j0)) = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    }
+    // generic-proxy stores -> visible to the tensor cores (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    // ---- layer 2 (tensor cores): 16 MMAs of K = 16 (two 16-byte K chunks each)
+    if (t == 0) {
+#pragma unroll 1
+      for (int ks = 0; ks < kH / 16; ++ks) {
+        const uint64_t ad = smem_desc(a_base + ks * 256, 128, kRowGroupBytes);
+        const uint64_t bd = smem_desc(b_base + ks * 256, 128, kRowGroupBytes);
+        mma_bf16(tmem, ad, bd, ks > 0 ? 1u : 0u);
+      }
+      mma_commit(bar);
+      uint32_t polls = 0;
+      while (!bar_try_wait(bar, parity)) {
+        if (++polls >= kWaitPolls) {
+          set_status(status, NFEM_ERR_TIMEOUT);
+          *sflag = 1;
+          break;
+        }
+      }
+    }
+    parity ^= 1u;
+    __syncthreads();
+    if (*sflag) break;
+    fence_after_sync();
+    // ---- epilogue: + b2, ReLU, . W3 (warp w reads TMEM lanes 32 (w % 4) ...)
+    const int quarter = warp & 3, chalf = warp >> 2;
+    float acc = 0.f;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kH / 2; c0 += 32) {
+      uint32_t v[32];
+      const int cb = chalf * (kH / 2) + c0;
+      tmem_ld32(tmem + (uint32_t(quarter * 32) << 16) + uint32_t(cb), v);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) acc = fmaf(fmaxf(__uint_as_float(v[i]) + sb2[cb + i], 0.f), sw3[cb + i], acc);
+    }
+    if (chalf == 1) spart[r] = acc;
+    fence_before_sync();
+    __syncthreads();
+    if (chalf == 0 && row < n_rows) y[row] = acc + spart[r] + b3;
+  }
+  // free the tensor memory (every MMA has completed: its commit was waited for)
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after_sync();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+}  // namespace
+}  // namespace nfem
+
+using namespace nfem;
+
+extern "C" int nfem_mlp_infer_tc(const int32_t* dims, const void* params, const float* params_f32, int64_t batch,
+                                 const float* x, float* y, int32_t* dev_status, void* stream) {
+  if (!dims || !params || !params_f32 || batch < 0 || (batch > 0 && (!x || !y))) return NFEM_ERR_INVALID_ARG;
+  const int n_in = dims[0], h1 = dims[1], h2 = dims[2], n_out = dims[3];
+  if (n_in < 1 || h1 < 1 || h2 < 1 || n_out < 1) return NFEM_ERR_INVALID_ARG;
+  if (n_in > kInMax || h1 != kH || h2 != kH || n_out != 1) return NFEM_ERR_UNSUPPORTED;
+  if (batch == 0) return NFEM_OK;
+  const int64_t oW1 = 0, ob1 = oW1 + int64_t(h1) * n_in, oW2 = ob1 + h1, ob2 = oW2 + int64_t(h2) * h1;
+  const int64_t oW3 = ob2 + h2, ob3 = oW3 + h2;
+  cudaStream_t s = (cudaStream_t)stream;
+  auto kern = n_in <= 8 ? mlp_infer_tc_kernel<8> : mlp_infer_tc_kernel<kInMax>;
+  NFEM_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes)));
+  int dev = 0, n_sm = 0;
+  NFEM_TRY_CUDA(cudaGetDevice(&dev));
+  NFEM_TRY_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t n_tiles = (batch + kTM - 1) / kTM;
+  const int grid = int(n_tiles < n_sm ? n_tiles : n_sm);
+  const __nv_bfloat16* P = reinterpret_cast<const __nv_bfloat16*>(params);
+  kern<<<grid, kThreads, kSmemBytes, s>>>(batch, n_in, P + oW1, params_f32 + ob1, P + oW2, params_f32 + ob2,
+                                          P + oW3, params_f32 + ob3, x, y, dev_status);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}

@@ -404,3 +404,67 @@ extern "C" int nfem_pattern_slots(const int32_t* cd, int64_t n_cells, int n_loc,
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }
+
+// ------------------------------------------------------------ generic scatter
+// Element matrices and residuals evaluated elsewhere (a weak form the device
+// does not implement, evaluated cell by cell on the host like the
+// reference's scatter_form_data) added into the CSR pattern: one thread per
+// (element, a, b) entry, the column found by binary search in the row, an
+// atomic add (the order of the additions into one entry may vary).
+namespace nfem {
+template <typename T>
+__global__ void scatter_elements_kernel(int64_t n_el, int n_loc, const int32_t* __restrict__ dofs,
+                                        const T* __restrict__ jel, const T* __restrict__ rel,
+                                        const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                        int64_t n_rows, T* __restrict__ values, T* __restrict__ rhs,
+                                        int32_t* status) {
+  const int64_t nn = int64_t(n_loc) * n_loc;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < n_el * nn;
+       e += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t el = e / nn;
+    const int a = int((e / n_loc) % n_loc), b = int(e % n_loc);
+    const int32_t row = dofs[el * n_loc + a], col = dofs[el * n_loc + b];
+    if (row < 0 || col < 0 || row >= n_rows || col >= n_rows) {
+      set_status(status, NFEM_ERR_INVALID_ARG);
+      continue;
+    }
+    if (jel) {
+      int32_t lo = rp[row], hi = rp[row + 1];
+      const int32_t end = hi;
+      while (lo < hi) {  // at most log2(row length) steps
+        const int32_t mid = (lo + hi) >> 1;
+        if (ci[mid] < col) lo = mid + 1; else hi = mid;
+      }
+      if (lo < end && ci[lo] == col)
+        atomicAdd(values + lo, jel[e]);
+      else
+        set_status(status, NFEM_ERR_PATTERN);
+    }
+    if (rel && b == 0) atomicAdd(rhs + row, rel[el * n_loc + a]);
+  }
+}
+}  // namespace nfem
+
+extern "C" int nfem_scatter_elements(int value_type, int64_t n_el, int n_loc, const int32_t* dofs,
+                                     const void* j_el, const void* r_el, const int32_t* row_ptr,
+                                     const int32_t* col_idx, int64_t n_rows, void* values, void* rhs,
+                                     int32_t* dev_status, void* stream) {
+  using namespace nfem;
+  if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n_el < 0 || n_loc < 1 || n_rows < 0)
+    return NFEM_ERR_INVALID_ARG;
+  if (n_el == 0) return NFEM_OK;
+  if (!dofs || (j_el && (!row_ptr || !col_idx || !values)) || (r_el && !rhs)) return NFEM_ERR_INVALID_ARG;
+  const int64_t work = n_el * int64_t(n_loc) * n_loc;
+  const int g = grid_for(work, 256);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (value_type == NFEM_F64)
+    scatter_elements_kernel<double><<<g, 256, 0, s>>>(n_el, n_loc, dofs, (const double*)j_el, (const double*)r_el,
+                                                      row_ptr, col_idx, n_rows, (double*)values, (double*)rhs,
+                                                      dev_status);
+  else
+    scatter_elements_kernel<float><<<g, 256, 0, s>>>(n_el, n_loc, dofs, (const float*)j_el, (const float*)r_el,
+                                                     row_ptr, col_idx, n_rows, (float*)values, (float*)rhs,
+                                                     dev_status);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}

@@ -79,7 +79,28 @@ class MLP:
                   _lib.stream_ptr())
         return h1, h2, y
 
+    def tensor_core_shape(self):
+        """True when nfem_mlp_infer_tc covers the network (<= 16 inputs, two
+        hidden layers of 256, one output)."""
+        d = self.dims
+        return int(d[0]) <= 16 and int(d[1]) == 256 and int(d[2]) == 256 and int(d[3]) == 1
+
+    def infer_tc(self, x, status=None):
+        """Network output [B, 1] from the fused tensor-core kernel."""
+        x = x.contiguous().float()
+        y = torch.empty((x.shape[0], 1), device=x.device)
+        st = status if status is not None else torch.zeros(1, dtype=torch.int32, device=x.device)
+        _lib.call("nfem_mlp_infer_tc", self._dims_ptr(), _lib.ptr(self.params_bf16), _lib.ptr(self.params),
+                  x.shape[0], _lib.ptr(x), _lib.ptr(y), _lib.ptr(st), _lib.stream_ptr())
+        if status is None and int(st.item()):
+            raise _lib.NfemError(int(st.item()), "nfem_mlp_infer_tc")
+        return y
+
     def predict(self, x, chunk=1 << 16):
+        """Inference: the tensor-core kernel for the preconditioner's shape,
+        else the tiled CUDA-core GEMMs in chunks."""
+        if self.tensor_core_shape():
+            return self.infer_tc(x)
         out = torch.empty((x.shape[0], int(self.dims[3])), device=x.device)
         for s in range(0, x.shape[0], chunk):
             out[s:s + chunk] = self.forward(x[s:s + chunk])[2]

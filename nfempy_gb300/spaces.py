@@ -98,6 +98,21 @@ class DiscreteSpace:
         self.discontinuous = False
         self.name = "Unnamed"
         self.n_dof = 0
+        self._product = None
+
+    @property
+    def elements(self):
+        """One entry per cell (len() is the number of elements, as for the
+        reference's FiniteElement list)."""
+        return range(self._product.n_cells) if self._product is not None else range(0)
+
+    @property
+    def bc_elements(self):
+        """One entry per boundary element (the facet's entity number), in the
+        reference's order (src/spaces/discrete_space.py:163-207)."""
+        if self._product is None:
+            return np.zeros(0, dtype=np.int64)
+        return self._product._bc_facets(self.name)["rank"]
 
     def make_discontinuous(self):
         self.discontinuous = True
@@ -124,6 +139,7 @@ class ProductSpace:
         for name, (dim, nc, family, k, mesh) in discrete_spaces_data.items():
             s = DiscreteSpace(dim, nc, family, k, mesh, self.integration_order)
             s.name = name
+            s._product = self
             self.discrete_spaces[name] = s
         self._dof_shift = 0
         self.n_dof = 0
@@ -161,6 +177,7 @@ class ProductSpace:
             raise NotImplementedError("all fields must use the same physical tags")
         self.physical_tags = list(tags[0])
         self.b_physical_tags = b_physical_tags or {}
+        self._bc_cache = {}
         self.dim = dim
         self.mesh = mesh
         cells, _ = cells_of_dim(mesh.data, dim, self.physical_tags)
@@ -237,17 +254,20 @@ class ProductSpace:
         offset = self._dof_shift
         self.field_offsets = {}
         self.field_slices = {}
+        self.entity_blocks = {}
         col = 0
         for name in self.names:
             s = self.discrete_spaces[name]
             e = s.entity_dofs()
             start = offset
             self.field_offsets[name] = start
+            self.entity_blocks[name] = {}
             c0 = col
             for d in range(dim + 1):
                 w = e[d] * s.n_comp
                 if w == 0:
                     continue
+                self.entity_blocks[name][d] = (offset, w)
                 n_ent = N_SUB[dim][d]
                 blocks.append(_lib.DofBlock(
                     _lib.ptr(self.occ_rank[d]).value if d < dim else None, n_ent, w, offset))
@@ -274,3 +294,147 @@ class ProductSpace:
 
     def all_destination_indexes(self):
         return self.cell_dofs.cpu().numpy().astype(np.int64)
+
+    # ------------------------------------------------------------ boundary elements
+    def _facet_records(self):
+        """Facets of the mesh file, one record per distinct facet: sorted
+        vertices, node order at creation and physical tag.
+
+        The reference inserts the file's blocks in order
+        (src/mesh/mesh.py:221-237, 335-336): a facet is created by its first
+        insertion (a facet block, keeping the file's node order, or the first
+        cell that holds it: a tetrahedron's face i keeps the cell's node order
+        of vertices (1,2,3), (0,2,3), (0,1,3), (0,1,2) (mesh.py:180-215), a
+        triangle's edges are sorted (mesh.py:153-175)), and every insertion
+        with a tag sets its material id, so the last tagged block wins."""
+        if "records" in self._bc_cache:
+            return self._bc_cache["records"]
+        dim = self.dim
+        conns, tags, before = [], [], []
+        seen_cells = False
+        for typ, conn, phys in self.mesh.data["blocks"]:
+            bd = BLOCK_DIM[typ]
+            if bd == dim:
+                seen_cells = True
+            elif bd == dim - 1:
+                c = np.asarray(conn, dtype=np.int64).reshape(-1, dim)
+                conns.append(c)
+                tags.append(np.asarray(phys, dtype=np.int64).reshape(-1))
+                before.append(np.full(c.shape[0], not seen_cells))
+        if not conns:
+            rec = (np.zeros((0, dim), np.int64), np.zeros((0, dim), np.int64), np.zeros(0, np.int64),
+                   np.zeros(0, bool))
+            self._bc_cache["records"] = rec
+            return rec
+        conn = np.concatenate(conns)
+        tag = np.concatenate(tags)
+        before = np.concatenate(before)
+        srt = np.sort(conn, axis=1)
+        _, first, inv = np.unique(srt, axis=0, return_index=True, return_inverse=True)
+        inv = inv.reshape(-1)
+        last = np.zeros(len(first), dtype=np.int64)
+        last[inv] = np.arange(len(inv))  # the last write of each facet wins
+        rec = (srt[first], conn[first], tag[last], before[first])
+        self._bc_cache["records"] = rec
+        return rec
+
+    def _bc_facets(self, name):
+        """Boundary elements of field `name`: the file's facets whose tag is in
+        b_physical_tags[name], ordered by entity number (first appearance
+        over cells x local facets: src/mesh/mesh_topology.py:28-35 and
+        src/spaces/discrete_space.py:163-207).  Each gets the first cell
+        holding it (the first predecessor of product_space.py:132-145), its
+        local facet index and its vertices in the reference's node order."""
+        key = ("facets", name)
+        if key in self._bc_cache:
+            return self._bc_cache[key]
+        dim = self.dim
+        tags = list(self.b_physical_tags.get(name, []) or [])
+        srt, node_order, tag, before = self._facet_records()
+        keep = np.isin(tag, np.asarray(tags, dtype=np.int64)) if tags else np.zeros(len(tag), bool)
+        srt, node_order, before = srt[keep], node_order[keep], before[keep]
+        sub = np.array(((1, 2), (0, 2), (0, 1)) if dim == 2 else ((1, 2, 3), (0, 2, 3), (0, 1, 3), (0, 1, 2)))
+        cells = self.cells_host
+        occ = np.sort(cells[:, sub], axis=2).reshape(-1, dim)  # [T * (dim + 1), dim], flat = c * (dim + 1) + i
+        V = int(max(self.mesh.points.shape[0], 1))
+        if float(V) ** dim >= 2.0 ** 62:
+            raise NotImplementedError("too many vertices for the facet keys")
+
+        def keys(a):
+            k = np.zeros(a.shape[0], dtype=np.int64)
+            for j in range(dim):
+                k = k * V + a[:, j]
+            return k
+        ok = keys(occ)
+        order = np.argsort(ok, kind="stable")
+        fk = keys(srt)
+        pos = np.searchsorted(ok[order], fk)
+        if len(fk) and (np.any(pos >= len(ok)) or np.any(ok[order][np.minimum(pos, len(ok) - 1)] != fk)):
+            raise ValueError("a tagged boundary facet belongs to no cell of the space")
+        flat = order[pos]  # the first (lowest) cell holding the facet
+        c, i = flat // (dim + 1), flat % (dim + 1)
+        if dim - 1 not in self.occ_rank:  # facets carry no DoF of any field: number them now for the order
+            self._number(dim - 1, _lib.stream_ptr(None))
+        rank = self.occ_rank[dim - 1].cpu().numpy()[c, i].astype(np.int64) if len(c) else np.zeros(0, np.int64)
+        o = np.argsort(rank, kind="stable")
+        c, i, rank, node_order, before = c[o], i[o], rank[o], node_order[o], before[o]
+        verts = node_order.copy()
+        if dim == 3:
+            from_cell = cells[c[:, None], sub[i]] if len(c) else np.zeros((0, 3), np.int64)
+        else:
+            from_cell = np.sort(cells[c[:, None], sub[i]], axis=1) if len(c) else np.zeros((0, 2), np.int64)
+        verts[~before] = from_cell[~before]
+        out = {"cell": c, "local": i, "rank": rank, "vertices": verts}
+        self._bc_cache[key] = out
+        return out
+
+    def _field_bc_dofs(self, name):
+        """[n_bc, k] DoFs of field `name` on its boundary elements
+        (src/spaces/dof_map.py:148-170): per dimension d < dim with entity
+        DoFs, the facet's sub-entities in the facet's own order (vertices,
+        then edges (v1,v2), (v0,v2), (v0,v1), then the facet), each entity's
+        DoFs in the cell numbering."""
+        key = ("dofs", name)
+        if key in self._bc_cache:
+            return self._bc_cache[key]
+        dim = self.dim
+        f = self._bc_facets(name)
+        c, verts = f["cell"], f["vertices"]
+        n = len(c)
+        cols = []
+        blocks = self.entity_blocks[name]
+        cell_pos = None
+        if n:
+            # position of each facet vertex in its cell
+            cell_pos = np.argmax(self.cells_host[c][:, None, :] == verts[:, :, None], axis=2)
+        for d in range(dim):
+            if d not in blocks or n == 0:
+                continue
+            off, w = blocks[d]
+            rank = self.occ_rank[d].cpu().numpy()
+            if d == dim - 1:
+                ents = [f["local"]]
+            elif d == 0:
+                ents = [cell_pos[:, k] for k in range(dim)]
+            else:  # d == 1 in 3D: the face's edges in its own order
+                cell_edges = {frozenset(e): j for j, e in enumerate(((2, 3), (1, 3), (1, 2), (0, 3), (0, 2), (0, 1)))}
+                table = np.full((4, 4), -1, dtype=np.int64)
+                for e, j in cell_edges.items():
+                    a, b = tuple(e)
+                    table[a, b] = table[b, a] = j
+                ents = [table[cell_pos[:, a], cell_pos[:, b]] for a, b in ((1, 2), (0, 2), (0, 1))]
+            for le in ents:
+                r = rank[c, le].astype(np.int64)
+                cols.append(off + r[:, None] * w + np.arange(w)[None, :])
+        out = np.concatenate(cols, axis=1) if cols else np.zeros((n, 0), dtype=np.int64)
+        self._bc_cache[key] = out
+        return out
+
+    def bc_destination_indexes(self, bc_index, field_name=None):
+        """Global DoFs of one boundary element (product_space.py:172-201):
+        the fields with boundary elements in order, or one field."""
+        if field_name is not None:
+            return self._field_bc_dofs(field_name)[int(bc_index)]
+        parts = [self._field_bc_dofs(n)[int(bc_index)] for n in self.names
+                 if len(self._bc_facets(n)["rank"]) > 0]
+        return np.concatenate(parts) if parts else np.zeros(0, dtype=np.int64)

@@ -350,7 +350,10 @@ def make_case(name, mesh, fields):
         disc[fname] = dsc
     space = ProductSpace(data)
     space.make_subspaces_discontinuous(disc)
-    space.build_structures({f[0]: [1] for f in fields}, {})
+    # every tagged facet of the mesh is a boundary element of every field
+    b_tags = sorted({int(t) for typ, conn, phys in mesh["blocks"] if mesh_gen.BLOCK_DIM[typ] == dim - 1
+                     for t in np.unique(phys)})
+    space.build_structures({f[0]: [1] for f in fields}, {f[0]: b_tags for f in fields})
     first = fields[0][0]
     n_el = len(space.discrete_spaces[first].elements)
     dest = np.array([space.destination_indexes(i) for i in range(n_el)], dtype=np.int64)
@@ -396,6 +399,13 @@ def make_case(name, mesh, fields):
         out["rt_basis"] = np.array(tabs)
         out["quad_points"] = pts
         out["quad_weights"] = wts
+    # boundary elements: DoFs of each (product_space.py:172-201) and the
+    # facet's vertices in the reference's node order
+    n_bc = len(space.discrete_spaces[first].bc_elements)
+    out["bc_tags"] = np.array(b_tags, dtype=np.int64)
+    out["bc_dest"] = np.array([space.bc_destination_indexes(i) for i in range(n_bc)], dtype=np.int64)
+    out["bc_vertices"] = np.array(
+        [space.discrete_spaces[first].bc_elements[i].data.cell.node_tags for i in range(n_bc)], dtype=np.int64)
     out["r_el"], out["j_el"] = element_forms(name, space, n_el)
     if name.startswith("cosserat"):
         # LCEScaledRieszMapWeakForm (lce_scaled_riesz_map_weak_form.py:415-598)

@@ -6,13 +6,13 @@ import nfempy_gb300 as nf
 from oracle import elements, forms, mesh_gen, quadrature, topology
 
 
-def product_space(mesh_dict, fields, tags=(1,)):
+def product_space(mesh_dict, fields, tags=(1,), b_tags=()):
     mesh = nf.Mesh(mesh_dict["dim"], data=mesh_dict)
     dim = mesh_dict["dim"]
     data = {n: (dim, nc, "Lagrange" if f == "P" else f, k, mesh) for n, f, k, nc, d in fields}
     sp = nf.ProductSpace(data)
     sp.make_subspaces_discontinuous({n: d for n, f, k, nc, d in fields})
-    sp.build_structures({n: list(tags) for n, *_ in fields}, {})
+    sp.build_structures({n: list(tags) for n, *_ in fields}, {n: list(b_tags) for n, *_ in fields} if b_tags else {})
     return sp
 
 

@@ -114,3 +114,59 @@ def test_bf16_forward_and_adam(cuda_lib):
     torch.cuda.synchronize()
     np.testing.assert_allclose(P.double().cpu().numpy(), flat(po), rtol=1e-5, atol=1e-6)
     np.testing.assert_array_equal(Pb.float().cpu().numpy(), P.cpu().to(torch.bfloat16).float().numpy())
+
+
+def torch_reference_tc(P32, Pb, dims, x):
+    """Plain PyTorch FP32 restatement of nfem_mlp_infer_tc: BF16 weights,
+    FP32 biases, the layer-1 activations rounded to BF16 (the MMA operand
+    type), FP32 accumulation."""
+    i, h1, h2, o = dims
+    W = Pb.float()
+    k = 0
+    W1 = W[k:k + h1 * i].view(h1, i); k += h1 * i
+    b1 = P32[k:k + h1]; k += h1
+    W2 = W[k:k + h2 * h1].view(h2, h1); k += h2 * h1
+    b2 = P32[k:k + h2]; k += h2
+    W3 = W[k:k + o * h2].view(o, h2); k += o * h2
+    b3 = P32[k:k + o]
+    a1 = torch.relu(x @ W1.T + b1).to(torch.bfloat16).float()
+    a2 = torch.relu(a1 @ W2.T + b2)
+    return a2 @ W3.T + b3
+
+
+@pytest.mark.parametrize("n_in", [8, 13])
+@pytest.mark.parametrize("B", [1, 127, 128, 129, 5000, 152 * 128 * 3 + 77])
+def test_tensor_core_inference_matches_torch(cuda_lib, n_in, B):
+    """The tcgen05 kernel against a PyTorch FP32 reference of the same op.
+    Tolerance: 2e-3 of max |y| entrywise (a BF16 rounding of one layer-1
+    activation may fall on the other side when the FP32 sums differ in
+    order), 1e-4 of max |y| on average."""
+    dims = (n_in, 256, 256, 1)
+    rng = np.random.default_rng(11 + n_in)
+    p = params_np(rng, dims)
+    P = torch.tensor(flat(p), dtype=torch.float32, device="cuda")
+    Pb = torch.empty(P.numel(), dtype=torch.bfloat16, device="cuda")
+    _lib.call("nfem_to_bf16", P.numel(), _lib.ptr(P), _lib.ptr(Pb), _lib.stream_ptr())
+    x = torch.tensor(rng.normal(size=(B, n_in)), dtype=torch.float32, device="cuda")
+    y = torch.full((B, 1), float("nan"), device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    d = torch.tensor(dims, dtype=torch.int32)
+    _lib.call("nfem_mlp_infer_tc", _lib.C.c_void_p(d.data_ptr()), _lib.ptr(Pb), _lib.ptr(P), B, _lib.ptr(x),
+              _lib.ptr(y), _lib.ptr(st), _lib.stream_ptr())
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    ref = torch_reference_tc(P, Pb, dims, x)
+    err = (y - ref).abs()
+    scale = ref.abs().max().item()
+    assert torch.isfinite(y).all()
+    assert err.max().item() <= 2e-3 * scale, (err.max().item(), scale)
+    assert err.mean().item() <= 1e-4 * scale
+
+
+def test_tensor_core_inference_refuses_other_shapes(cuda_lib):
+    P = torch.zeros(10, device="cuda")
+    for dims in ((8, 128, 256, 1), (8, 256, 256, 2), (17, 256, 256, 1)):
+        d = torch.tensor(dims, dtype=torch.int32)
+        rc = _lib.lib().nfem_mlp_infer_tc(_lib.C.c_void_p(d.data_ptr()), _lib.ptr(P), _lib.ptr(P), 4, _lib.ptr(P),
+                                          _lib.ptr(P), None, None)
+        assert _lib.STATUS_NAMES[rc] == "NFEM_ERR_UNSUPPORTED"

@@ -20,6 +20,21 @@ def test_cell_dofs_match_reference(cuda_lib, name):
     np.testing.assert_array_equal(sp.destination_indexes(3), g["cell_dofs"][3])
 
 
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_bc_dofs_match_reference(cuda_lib, name):
+    """Boundary elements (order, node order) and their DoFs against the
+    reference's bc_destination_indexes on the same mesh and tags."""
+    mk, fields = CASES[name]
+    g = golden(name)
+    sp = product_space(mk(), fields, b_tags=tuple(int(t) for t in g["bc_tags"]))
+    first = fields[0][0]
+    n_bc = len(sp.discrete_spaces[first].bc_elements)
+    assert n_bc == g["bc_dest"].shape[0]
+    got = np.array([sp.bc_destination_indexes(i) for i in range(n_bc)], dtype=np.int64).reshape(g["bc_dest"].shape)
+    np.testing.assert_array_equal(got, g["bc_dest"])
+    np.testing.assert_array_equal(sp._bc_facets(first)["vertices"], g["bc_vertices"])
+
+
 @pytest.mark.parametrize("gen,n", [("square", 1), ("square", 7), ("square", 32), ("cube", 1), ("cube", 5),
                                    ("cube", 12)])
 def test_numbering_and_flags_match_oracle(cuda_lib, gen, n):
