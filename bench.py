@@ -367,9 +367,11 @@ def solve_bench(args, A, wf, coefs, res, stream):
         kappa = wf.functions["kappa"]
         tl2 = TwoLevelCoarse(A64, nc)
         tl2.set_weights(learned.learned_weights(tl2, model, kappa, alpha))
+        inference = mlp_inference_timing(model, learned.FaceData(tl2).features(kappa))
         ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.tl_restart, two_level=tl2)
         out["learned"] = _timed_solve(ksp, b, args, stream, two_level=True)
         out["learned"]["alpha"] = alpha
+        out["learned"]["network_inference"] = inference
         out["learned"]["training"] = {k: ck["record"][k] for k in ("n", "fields", "solves_used", "pairs",
                                                                    "data_seconds", "train_seconds")}
         plain = out["plain_block_jacobi"]["time_to_solve_ms"]
@@ -388,6 +390,73 @@ def solve_bench(args, A, wf, coefs, res, stream):
     tl["time_to_solve_incl_host_structure_ms"] = tl["time_to_solve_ms"] + 1e3 * tl["host_structure_s"]
     tl["speedup_vs_plain_incl_host_structure"] = (out["plain_block_jacobi"]["time_to_solve_ms"]
                                                   / tl["time_to_solve_incl_host_structure_ms"])
+    return out
+
+
+def mlp_inference_timing(model, x, reps=20, warmup=3):
+    """The network's inference over the faces of the benchmark mesh: the
+    fused tcgen05 kernel against the tiled CUDA-core GEMMs (same BF16
+    weights), CUDA events on the current stream, inputs resident."""
+    import torch
+    rows = int(x.shape[0])
+    flops_row = 2 * (int(model.dims[0]) * int(model.dims[1]) + int(model.dims[1]) * int(model.dims[2])
+                     + int(model.dims[2]) * int(model.dims[3]))
+    out = {"rows": rows, "flops_per_row": flops_row,
+           "network": "x[8] -> 256 -> 256 -> 1, BF16 weights, FP32 accumulation"}
+
+    def timeit(fn):
+        for _ in range(warmup):
+            fn()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s.record()
+        for _ in range(reps):
+            fn()
+        e.record()
+        torch.cuda.synchronize()
+        return s.elapsed_time(e) / reps
+    if model.tensor_core_shape():
+        y_tc = model.infer_tc(x)
+        ms = timeit(lambda: model.infer_tc(x))
+        peak = measured_peaks()
+        pk = peak.get("bf16_tflops") if peak else None
+        ach = rows * flops_row / (ms * 1e-3) / 1e12
+        out["tensor_core"] = {"kernel": "mlp_infer_tc_kernel (tcgen05.mma kind::f16, M128 N256 K16, TMEM accumulators)",
+                              "ms": ms, "tflops": ach,
+                              "frac_of_measured_bf16_peak": (ach / pk) if pk else None}
+    chunk = 1 << 16
+
+    def cuda_core():
+        for s0 in range(0, rows, chunk):
+            model.forward(x[s0:s0 + chunk])
+    ms_cc = timeit(cuda_core)
+    out["cuda_core"] = {"kernel": "gemm_kernel x3 (64x64 tiles, FP32 FMA)", "ms": ms_cc,
+                        "tflops": rows * flops_row / (ms_cc * 1e-3) / 1e12}
+    if "tensor_core" in out:
+        y_cc = torch.cat([model.forward(x[s0:s0 + chunk])[2] for s0 in range(0, rows, chunk)])
+        out["tensor_core"]["speedup_vs_cuda_core"] = ms_cc / out["tensor_core"]["ms"]
+        out["tensor_core"]["max_abs_diff_vs_cuda_core"] = float((y_tc - y_cc).abs().max().item())
+        out["tensor_core"]["max_abs_output"] = float(y_cc.abs().max().item())
+    return out
+
+
+def mlp_only(args):
+    """The learned network's inference alone on --mlp-rows synthetic feature
+    rows (seeded normal features, the shipped checkpoint's weights, or a
+    seeded network of the same shape when no checkpoint is present)."""
+    import torch
+    from nfempy_gb300 import learned
+    try:
+        from nfempy_gb300 import train_learned
+        model, _ = train_learned.load()
+        src = "checkpoint"
+    except (OSError, FileNotFoundError, KeyError):
+        model = learned.MLP(learned.N_FEAT, width=256, n_out=1, seed=0)
+        src = "seeded"
+    g = torch.Generator(device="cuda").manual_seed(20261204)
+    x = torch.randn((args.mlp_rows, int(model.dims[0])), device="cuda", generator=g)
+    out = mlp_inference_timing(model, x, reps=args.steps, warmup=args.warmup)
+    out["weights"] = src
     return out
 
 
@@ -551,9 +620,16 @@ def elasticity_bench(args):
         bc = LEPrimalWeakFormBCDirichlet(sp)
         bc.functions = {"u": None}
         bc.assemble(A64)
-        ksp = KrylovSolver(A64, pc="jacobi", A32_values=A64.values.to(torch.float32), restart=args.restart)
+        A32v = A64.values.to(torch.float32)
+        ksp = KrylovSolver(A64, pc="jacobi", A32_values=A32v, restart=args.restart)
         out["solve"] = _timed_solve(ksp, -r64, args, torch.cuda.current_stream())
         out["solve"]["preconditioner"] = "point Jacobi"
+        # the cell cliques' 30 x 30 blocks (weighted additive Schwarz)
+        ksp = KrylovSolver(A64, pc="cell_block", A32_values=A32v, restart=args.restart)
+        out["solve_cell_block"] = _timed_solve(ksp, -r64, args, torch.cuda.current_stream())
+        out["solve_cell_block"]["preconditioner"] = "cell-block Jacobi (30 x 30 cell blocks)"
+        out["solve_cell_block"]["speedup_vs_point_jacobi"] = (out["solve"]["time_to_solve_ms"]
+                                                              / out["solve_cell_block"]["time_to_solve_ms"])
     return out
 
 
@@ -987,14 +1063,16 @@ def main():
     ap.add_argument("--slice-shift", type=int, default=0, help="cells per slice = 2^shift (default: the library's)")
     ap.add_argument("--record-quarters", type=int, default=0,
                     help="quarters of the blocks forming records in the overlapped assembly (default: the library's)")
-    ap.add_argument("--only", choices=["assembly", "elasticity", "cosserat", "batch2d", "solve"], default=None,
+    ap.add_argument("--mlp-rows", type=int, default=3_200_000,
+                    help="rows (faces) of --only mlp: synthetic features through the learned network")
+    ap.add_argument("--only", choices=["assembly", "elasticity", "cosserat", "batch2d", "solve", "mlp"], default=None,
                     help="time one secondary assembly workload alone and print its record (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.only:
         fn = {"assembly": assembly_only, "elasticity": elasticity_bench, "cosserat": cosserat_bench, "batch2d": batch2d_bench,
-              "solve": solve_only}[args.only]
+              "solve": solve_only, "mlp": mlp_only}[args.only]
         print(json.dumps({"workload": args.only, **fn(args)}), flush=True)
         return
     if args.impl == "reference":

@@ -214,6 +214,15 @@ int nfem_scatter_elements(int value_type, int64_t n_el, int n_loc, const int32_t
                           const int32_t* col_idx, int64_t n_rows, void* values, void* rhs,
                           int32_t* dev_status, void* stream);
 
+/* Adds n (row, col, value) triples (values FP64, converted to value_type)
+ * into the CSR values: Mat.setValue(row, col, value, addv=True) batched
+ * (src/assembly/ScatterFormData.py:5-11).  Atomic; an entry outside the
+ * pattern sets NFEM_ERR_PATTERN, a row or column outside [0, n_rows)
+ * NFEM_ERR_INVALID_ARG, in dev_status. */
+int nfem_csr_add_entries(int value_type, int64_t n, const int32_t* rows, const int32_t* cols,
+                         const double* vals, const int32_t* row_ptr, const int32_t* col_idx,
+                         int64_t n_rows, void* values, int32_t* dev_status, void* stream);
+
 /* Copies `bytes` from src to dst with a kernel (16-byte vectors when both are
  * 16-byte aligned).  Either pointer may be pinned host memory mapped into the
  * device address space (cudaHostAlloc), so results reach the host without a

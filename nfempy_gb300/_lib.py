@@ -104,6 +104,7 @@ _SIGS = {
     "nfem_points_fixed64": ([_P, _I64, _P, _P], _I),
     "nfem_knob_set": ([_I, _I], _I),
     "nfem_mlp_infer_tc": ([_P, _P, _P, _I64, _P, _P, _P, _P], _I),
+    "nfem_csr_add_entries": ([_I, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P], _I),
     "nfem_scatter_elements": ([_I, _I64, _I, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P], _I),
     "nfem_rt1_dirichlet_rows": ([_I, _I, _I64, _P, _P, _P, _I, _I, _I, C.c_double, _P, C.POINTER(C.c_double), _I,
                                  _P, _P], _I),

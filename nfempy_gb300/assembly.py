@@ -186,9 +186,49 @@ class CSRMatrix:
     # PETSc-like surface used by the drivers
     def zeroEntries(self):
         self.fresh = True
+        self._pending = []
+
+    def setValue(self, row, col, value, addv=True):
+        """Mat.setValue: the entry is buffered on the host and added on the
+        device at the next assemble() (addv=False is not supported: the
+        reference's scatter always adds).  An entry outside the pattern is
+        an error at assemble()."""
+        if not addv:
+            raise NotImplementedError("setValue(addv=False)")
+        if getattr(self, "_pending", None) is None:
+            self._pending = []
+        self._pending.append((int(row), int(col), float(value)))
+
+    def _flush(self):
+        pend = getattr(self, "_pending", None)
+        if not pend:
+            return
+        if self.fresh:  # the first additions of a pass go into zeros
+            self.values.zero_()
+            self.fresh = False
+        a = np.asarray(pend, dtype=np.float64)
+        dev = self.values.device
+        rows = torch.as_tensor(a[:, 0].astype(np.int32), device=dev)
+        cols = torch.as_tensor(a[:, 1].astype(np.int32), device=dev)
+        vals = torch.as_tensor(a[:, 2], device=dev)
+        vt = _lib.NFEM_F64 if self.dtype == torch.float64 else _lib.NFEM_F32
+        _lib.call("nfem_csr_add_entries", vt, len(pend), _lib.ptr(rows), _lib.ptr(cols), _lib.ptr(vals),
+                  _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx), self.n_rows, _lib.ptr(self.values),
+                  _lib.ptr(self.status), _lib.stream_ptr(None))
+        self._pending = []
 
     def assemble(self):
+        """Mat.assemble(): adds the buffered setValue entries and checks the
+        device status word."""
+        self._flush()
         self.check_status("assemble")
+
+    def getValue(self, row, col):
+        """One entry (0 where the pattern has none)."""
+        rp0, rp1 = int(self.row_ptr[row].item()), int(self.row_ptr[row + 1].item())
+        cols = self.col_idx[rp0:rp1]
+        hit = (cols == int(col)).nonzero()
+        return float(self.values[rp0 + int(hit[0, 0])].item()) if hit.numel() else 0.0
 
     def getSize(self):
         return (self.n_rows, self.n_rows)
@@ -224,8 +264,66 @@ def _to_device(x, dtype, device, n):
     return t
 
 
+def element_view(space, indices):
+    """The cells `indices` of a space with disjoint DoFs: every selected cell
+    gets its own copy of its DoFs, each field's block kept contiguous and in
+    the space's local column order (field offset + cell * width + column).
+    A device form assembled over the view gives a block-diagonal matrix
+    whose row r holds exactly its cell's n_loc columns in local order: the
+    element matrices, with the cells' own geometry and orientation signs."""
+    idx = np.asarray(indices, dtype=np.int64).reshape(-1)
+    if idx.size and (idx.min() < 0 or idx.max() >= space.n_cells):
+        raise IndexError("cell index outside the space")
+    view = object.__new__(type(space))
+    view.__dict__.update(space.__dict__)
+    T = int(idx.size)
+    dev = space.device
+    idx_t = torch.as_tensor(idx, device=dev)
+    view.view_of = space
+    view.view_indices = idx
+    view.n_cells = T
+    view.cells = space.cells[idx_t].contiguous()
+    view.cells_host = space.cells_host[idx]
+    if getattr(space, "rt_sign_mask", None) is not None:
+        view.rt_sign_mask = space.rt_sign_mask[idx_t].contiguous()
+    view._dof_shift = 0
+    cd = np.empty((T, space.n_loc), dtype=np.int64)
+    off = 0
+    view.field_offsets = {}
+    for name in space.names:
+        sl = space.field_slices[name]
+        w = sl.stop - sl.start
+        view.field_offsets[name] = off
+        cd[:, sl] = off + np.arange(T)[:, None] * w + np.arange(w)[None, :]
+        off += T * w
+    if off >= 2 ** 31 - 1:
+        raise _lib.NfemError(4, "element_view (DoF count)")
+    view.n_dof = off
+    view.cell_dofs = torch.as_tensor(cd.astype(np.int32), device=dev)
+    view._bc_cache = {}
+    return view
+
+
+def _slice_cells(v, idx, T):
+    """A coefficient restricted to the cells idx: per-cell arrays (first
+    dimension = number of cells) are sliced, scalars and callables kept."""
+    if v is None or callable(v) or np.isscalar(v):
+        return v
+    if torch.is_tensor(v):
+        return v[torch.as_tensor(idx, device=v.device)] if v.dim() and v.shape[0] == T else v
+    a = np.asarray(v)
+    return a[idx] if a.ndim and a.shape[0] == T else v
+
+
 class WeakForm:
-    """Base with the reference's attributes (src/weak_forms/weak_from.py:6-29)."""
+    """Base with the reference's attributes (src/weak_forms/weak_from.py:6-29).
+
+    Cell forms (cell_form = True) also offer the reference's per-element
+    evaluate_form(i, alpha) and a batched evaluate_forms(indices, alphas),
+    both computed on the device by the form's own assembly kernel over an
+    element_view of the cells."""
+
+    cell_form = False
 
     def __init__(self, space):
         self.space = space
@@ -239,6 +337,50 @@ class WeakForm:
     def functions(self, functions):
         self._functions = functions
         self._cache = {}
+
+    def evaluate_forms(self, indices, alphas=None, dtype=torch.float64):
+        """Element data of the cells `indices` on the device:
+        (r [n, n_loc], j [n, n_loc, n_loc]) in the space's local DoF order,
+        as the reference's evaluate_form returns them cell by cell.  alphas
+        [n, n_loc] (the cells' slices of alpha) adds j @ alpha_l to r: the
+        forms are linear in alpha, so r(alpha) = r(0) + j alpha_l with
+        j = dr/dalpha."""
+        if not self.cell_form:
+            raise NotImplementedError(f"{type(self).__name__} is not a cell form")
+        sp = self.space
+        idx = np.asarray(indices, dtype=np.int64).reshape(-1)
+        n_loc = sp.n_loc
+        if idx.size == 0:
+            return (torch.zeros((0, n_loc), dtype=dtype, device=sp.device),
+                    torch.zeros((0, n_loc, n_loc), dtype=dtype, device=sp.device))
+        view = element_view(sp, idx)
+        vf = object.__new__(type(self))
+        vf.__dict__.update(self.__dict__)
+        vf.space = view
+        vf.functions = {k: _slice_cells(v, idx, sp.n_cells) for k, v in (self.functions or {}).items()}
+        if hasattr(vf, "use_slices"):
+            vf.use_slices = False
+        A = CSRMatrix(view, dtype=dtype)
+        res = torch.zeros(A.n_rows, dtype=dtype, device=sp.device)
+        vf.assemble(A, res, accumulate=False)
+        A.check_status("evaluate_forms")
+        cd = view.cell_dofs.long()
+        if A.nnz != view.n_dof * n_loc:
+            raise _lib.NfemError(6, "evaluate_forms (view pattern)")
+        j = A.values[: A.nnz].view(view.n_dof, n_loc)[cd]  # [n, n_loc (row a), n_loc (column b)]
+        r = res[cd]
+        if alphas is not None:
+            al = torch.as_tensor(np.asarray(alphas.cpu() if torch.is_tensor(alphas) else alphas),
+                                 dtype=dtype, device=sp.device).reshape(len(idx), n_loc)
+            r = r + torch.einsum("nab,nb->na", j, al)
+        return r, j
+
+    def evaluate_form(self, element_index, alpha):
+        """(r_el, j_el) of one cell as host arrays, the reference's
+        per-element call (e.g. laplace_dual_weak_form.py:18-86)."""
+        a = None if alpha is None else np.asarray(alpha.cpu() if torch.is_tensor(alpha) else alpha)[None, :]
+        r, j = self.evaluate_forms([int(element_index)], a)
+        return r[0].cpu().numpy(), j[0].cpu().numpy()
 
     def quadrature_points(self):
         """Physical quadrature points [T, Q, 3] (host float64)."""
@@ -270,6 +412,8 @@ class LaplaceDualWeakForm(WeakForm):
     per cell instead of once per incidence); the 512-problem triangle batch
     FP32 0.280 ms against 0.250 ms (a triangle's geometry is cheap).
     """
+
+    cell_form = True
 
     use_chunks = False
     use_records = None
@@ -400,9 +544,6 @@ class LaplaceDualWeakForm(WeakForm):
         plan.record_quarters = int(rq[dtype] if isinstance(rq, dict) else rq)
         return plan, ring
 
-    def evaluate_form(self, element_index, alpha):
-        raise NotImplementedError(
-            "per-cell evaluation is not offered on the device; assemble with SequentialAssembler")
 
 
 class LaplaceDualWeakFormBCDirichlet(WeakForm):
@@ -412,6 +553,8 @@ class LaplaceDualWeakFormBCDirichlet(WeakForm):
     `bc_physical_tags` (default: the space's b_physical_tags["u"], or every
     tagged facet).  functions: {"p": f(x, y, z) -> [1, N]} or a scalar.
     Only the residual changes (the form's Jacobian is zero)."""
+
+    residual_only = True  # zero Jacobian: the residual does not depend on alpha
 
     def __init__(self, space, bc_physical_tags=None):
         super().__init__(space)
@@ -574,18 +717,37 @@ class SequentialAssembler:
 
     # ------------------------------------------------------------ device forms
     def _scatter_form(self, form, sequence, alpha, residual, accumulate):
+        """All cells at alpha = 0: the form's one-launch row-owner assembly.
+        A subset of the cells or alpha != 0: the form's element data of those
+        cells (evaluate_forms, on the device) added by the scatter kernel."""
         n = self.space.n_cells
         seq = range(n) if sequence is None else sequence
-        if not (isinstance(seq, range) and seq.start == 0 and seq.stop == n and seq.step == 1):
-            if not np.array_equal(np.asarray(list(seq)), np.arange(n)):
-                raise NotImplementedError("device assembly covers all cells of the space in one pass")
-        if alpha is not None and np.any(np.asarray(alpha.cpu() if torch.is_tensor(alpha) else alpha) != 0):
-            raise NotImplementedError("linear forms are assembled at alpha = 0 (one Newton step)")
-        form.assemble(self.jacobian, residual, accumulate=accumulate)
+        full = isinstance(seq, range) and seq.start == 0 and seq.stop == n and seq.step == 1
+        if not full:
+            full = np.array_equal(np.asarray(list(seq)), np.arange(n))
+        zero = alpha is None or not np.any(self._host(alpha) != 0)
+        if full and zero:
+            form.assemble(self.jacobian, residual, accumulate=accumulate)
+            return
+        A = self.jacobian
+        if not accumulate:
+            A.values.zero_()
+            residual.zero_()
+        idx = np.asarray(list(seq), dtype=np.int64)
+        al = None if zero else self._host(alpha)[self._cell_dest()[idx]]
+        r, j = form.evaluate_forms(idx, al, dtype=A.dtype)
+        d_t = torch.as_tensor(self._cell_dest()[idx].astype(np.int32), device=A.values.device)
+        vt = _lib.NFEM_F64 if A.dtype == torch.float64 else _lib.NFEM_F32
+        _lib.call("nfem_scatter_elements", vt, len(idx), r.shape[1], _lib.ptr(d_t), _lib.ptr(j.contiguous()),
+                  _lib.ptr(r.contiguous()), _lib.ptr(A.row_ptr), _lib.ptr(A.col_idx), A.n_rows, _lib.ptr(A.values),
+                  _lib.ptr(residual), _lib.ptr(A.status), _lib.stream_ptr(None))
+        A.check_status("scatter of a device form's element data")
 
     def _scatter_bc_form(self, form, sequence, alpha, residual, accumulate):
         if not accumulate:
             raise NotImplementedError("a boundary form adds to a pass that starts with a cell form")
+        if not getattr(form, "residual_only", False) and alpha is not None and np.any(self._host(alpha) != 0):
+            raise NotImplementedError("this boundary form is assembled at alpha = 0")
         form.assemble(self.jacobian, residual, accumulate=True)
 
     # ------------------------------------------------------------ host-evaluated forms
@@ -750,6 +912,8 @@ class LEPrimalWeakForm(WeakForm):
                per cell; "rhs" - None, a 3-vector, per-cell array [T, 3], or
                f(x, y, z) -> [3, N] constant per cell.  r = +int f . phi."""
 
+    cell_form = True
+
     def _check_space(self):
         sp = self.space
         if sp is None or self.functions is None:
@@ -779,7 +943,7 @@ class LEPrimalWeakForm(WeakForm):
             else:
                 fv = np.asarray(f, dtype=np.float64)
                 fv = np.broadcast_to(fv.reshape(-1, 3) if fv.size != 3 else fv.reshape(1, 3), (T, 3))
-            ft = torch.as_tensor(np.ascontiguousarray(fv), dtype=dtype, device=sp.device)
+            ft = torch.as_tensor(np.array(fv, dtype=np.float64, order="C"), dtype=dtype, device=sp.device)
         from .elements import p2_reference_tables
         S, m, Mf = p2_reference_tables(3)
         out = (torch.as_tensor(lam, dtype=dtype, device=sp.device), torch.as_tensor(mu, dtype=dtype, device=sp.device),
@@ -883,6 +1047,8 @@ class LCEDualWeakForm(WeakForm):
     -sum_q |det J| w_q f(x_q) (lce_dual_weak_form.py:490-502) is exactly the
     cell's quadrature-weighted mean of f times -|T|: that mean is what goes
     to the device."""
+
+    cell_form = True
 
     NAMES = ("lambda_s", "mu_s", "kappa_s", "lambda_o", "mu_o", "kappa_o", "l")
 

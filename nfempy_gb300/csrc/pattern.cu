@@ -468,3 +468,52 @@ extern "C" int nfem_scatter_elements(int value_type, int64_t n_el, int n_loc, co
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }
+
+// ------------------------------------------------------------ single entries
+// (row, col, value) triples added into the CSR pattern: the batched form of
+// PETSc's Mat.setValue(row, col, value, addv=True) that the reference's
+// scatter calls once per entry (src/assembly/ScatterFormData.py:5-11).
+namespace nfem {
+template <typename T>
+__global__ void csr_add_coo_kernel(int64_t n, const int32_t* __restrict__ rows, const int32_t* __restrict__ cols,
+                                   const double* __restrict__ vals, const int32_t* __restrict__ rp,
+                                   const int32_t* __restrict__ ci, int64_t n_rows, T* __restrict__ values,
+                                   int32_t* status) {
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < n; e += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t row = rows[e], col = cols[e];
+    if (row < 0 || col < 0 || row >= n_rows || col >= n_rows) {
+      set_status(status, NFEM_ERR_INVALID_ARG);
+      continue;
+    }
+    int32_t lo = rp[row], hi = rp[row + 1];
+    const int32_t end = hi;
+    while (lo < hi) {
+      const int32_t mid = (lo + hi) >> 1;
+      if (ci[mid] < col) lo = mid + 1; else hi = mid;
+    }
+    if (lo < end && ci[lo] == col)
+      atomicAdd(values + lo, T(vals[e]));
+    else
+      set_status(status, NFEM_ERR_PATTERN);
+  }
+}
+}  // namespace nfem
+
+extern "C" int nfem_csr_add_entries(int value_type, int64_t n, const int32_t* rows, const int32_t* cols,
+                                    const double* vals, const int32_t* row_ptr, const int32_t* col_idx,
+                                    int64_t n_rows, void* values, int32_t* dev_status, void* stream) {
+  using namespace nfem;
+  if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n < 0 || n_rows < 0) return NFEM_ERR_INVALID_ARG;
+  if (n == 0) return NFEM_OK;
+  if (!rows || !cols || !vals || !row_ptr || !col_idx || !values) return NFEM_ERR_INVALID_ARG;
+  const int g = grid_for(n, 256);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (value_type == NFEM_F64)
+    csr_add_coo_kernel<double><<<g, 256, 0, s>>>(n, rows, cols, vals, row_ptr, col_idx, n_rows, (double*)values,
+                                                 dev_status);
+  else
+    csr_add_coo_kernel<float><<<g, 256, 0, s>>>(n, rows, cols, vals, row_ptr, col_idx, n_rows, (float*)values,
+                                                dev_status);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}

@@ -82,3 +82,19 @@ FORM_FUNCTIONS = {
         "rhs": cosserat_rhs,
     },
 }
+
+# coefficients the device forms take as they are: kappa, lambda and mu
+# constant on each cell (here constant), the Darcy source sampled at the
+# quadrature points, a constant elasticity load (the Cosserat case above
+# already fits: constant material, a load the device integrates exactly)
+FORM_FUNCTIONS_DEVICE = {
+    "darcy": {
+        "kappa": _const(2.5),
+        "rhs": FORM_FUNCTIONS["darcy"]["rhs"],
+    },
+    "elast": {
+        "lambda": _const(1.3),
+        "mu": _const(0.8),
+        "rhs": lambda x, y, z: np.array([1.0 + 0.0 * x, -0.5 + 0.0 * x, 0.25 + 0.0 * x]),
+    },
+}

@@ -291,7 +291,7 @@ from weak_forms.lce_dual_weak_form import LCEDualWeakForm  # noqa: E402
 from weak_forms.lce_scaled_riesz_map_weak_form import LCEScaledRieszMapWeakForm  # noqa: E402
 
 sys.path.insert(0, os.path.dirname(HERE))
-from cases import FORM_FUNCTIONS, RIESZ_FUNCTIONS  # noqa: E402
+from cases import FORM_FUNCTIONS, FORM_FUNCTIONS_DEVICE, RIESZ_FUNCTIONS  # noqa: E402
 
 
 class RecordingMat:
@@ -316,7 +316,7 @@ class CountingForm:
         return np.zeros(n), np.ones((n, n))
 
 
-def element_forms(name, space, n_el):
+def element_forms(name, space, n_el, functions=None):
     """r_el, j_el of every cell from the reference's own weak form (alpha = 0)."""
     kind = name.split("_")[0].rstrip("23d")
     if kind == "darcy":
@@ -328,7 +328,7 @@ def element_forms(name, space, n_el):
     else:
         wf = LCEDualWeakForm(space)
         ev = wf.evaluate_form_vectorized
-    wf.functions = FORM_FUNCTIONS[kind]
+    wf.functions = (functions or FORM_FUNCTIONS)[kind]
     rs, js = [], []
     for i in range(n_el):
         n = len(space.destination_indexes(i))
@@ -407,6 +407,9 @@ def make_case(name, mesh, fields):
     out["bc_vertices"] = np.array(
         [space.discrete_spaces[first].bc_elements[i].data.cell.node_tags for i in range(n_bc)], dtype=np.int64)
     out["r_el"], out["j_el"] = element_forms(name, space, n_el)
+    kind = name.split("_")[0].rstrip("23d")
+    if kind in FORM_FUNCTIONS_DEVICE:
+        out["r_el_dev"], out["j_el_dev"] = element_forms(name, space, n_el, FORM_FUNCTIONS_DEVICE)
     if name.startswith("cosserat"):
         # LCEScaledRieszMapWeakForm (lce_scaled_riesz_map_weak_form.py:415-598)
         wf = LCEScaledRieszMapWeakForm(space)

@@ -236,3 +236,29 @@ def test_time_dependent_forms(cuda_lib):
     asm2.form_to_input_list = asm.form_to_input_list
     asm2.scatter_forms()
     np.testing.assert_allclose(host, ro, rtol=0, atol=1e-12)
+
+
+def test_set_value_like_the_reference_scatter(cuda_lib):
+    """The reference's own scatter loop (ScatterFormData.py:5-11: one
+    Mat.setValue(addv=True) per entry) against a CSRMatrix: buffered on the
+    host, added on the device at assemble()."""
+    mk, fields = CASES["darcy2d_n4"]
+    g = golden("darcy2d_n4")
+    sp = product_space(mk(), fields)
+    A = nf.CSRMatrix(sp)
+    for i in range(sp.n_cells):
+        d = g["cell_dofs"][i]
+        data = g["j_el"][i].ravel()
+        row = np.repeat(d, len(d))
+        col = np.tile(d, len(d))
+        for k in range(len(data)):
+            A.setValue(row=row[k], col=col[k], value=data[k], addv=True)
+    A.assemble()
+    O, _ = assembly.assemble_csr(g["cell_dofs"], g["j_el"], g["r_el"], int(g["n_dof"]))
+    np.testing.assert_allclose(dense_of(A), O.toarray(), rtol=0, atol=1e-14 * np.abs(O.data).max())
+    assert A.getValue(int(g["cell_dofs"][0][0]), int(g["cell_dofs"][0][1])) == pytest.approx(
+        O[int(g["cell_dofs"][0][0]), int(g["cell_dofs"][0][1])], abs=1e-14)
+    # a coupling outside the pattern is reported at assemble()
+    A.setValue(0, sp.n_dof - 1, 1.0)
+    with pytest.raises(_lib.NfemError):
+        A.assemble()
