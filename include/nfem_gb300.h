@@ -64,13 +64,19 @@ const char* nfem_status_string(int status);
  *   NFEM_KNOB_DARCY_CELLS_BLOCK          threads per block of the Darcy cell
  *                                        pass: 128, 256 (0) or 512
  *   NFEM_KNOB_ELAS_WARPS                 warps per block of the elasticity
- *                                        node rows: 2, 4 (0) or 8
+ *                                        node rows with shared images: 2, 4 (0) or 8
+ *   NFEM_KNOB_ELAS_ROWS                  elasticity and Cosserat node rows: 1
+ *                                        shared-memory row images, 2 register
+ *                                        accumulation by warp shuffles; 0 the
+ *                                        built-in choice (elasticity: images,
+ *                                        Cosserat: registers)
  * nfem_knob_set returns NFEM_ERR_INVALID_ARG for an unknown key or value. */
 typedef enum {
   NFEM_KNOB_DARCY_ROWS_BLOCKS_PER_SM = 0,
   NFEM_KNOB_DARCY_CELLS_BLOCK = 1,
   NFEM_KNOB_ELAS_WARPS = 2,
-  NFEM_KNOB_COUNT = 3
+  NFEM_KNOB_ELAS_ROWS = 3,
+  NFEM_KNOB_COUNT = 4
 } nfem_knob;
 int nfem_knob_set(int key, int value);
 int nfem_knob_get(int key, int* value);

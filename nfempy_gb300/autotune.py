@@ -18,7 +18,7 @@ import torch
 
 from . import _lib
 
-KNOBS = {"darcy_rows_blocks_per_sm": 0, "darcy_cells_block": 1, "elas_warps": 2}
+KNOBS = {"darcy_rows_blocks_per_sm": 0, "darcy_cells_block": 1, "elas_warps": 2, "elas_rows": 3}
 
 
 def cache_path():
@@ -117,7 +117,8 @@ def darcy_candidates(dim):
 
 
 def elasticity_candidates():
-    return [{"form": {}, "knobs": {"elas_warps": w}} for w in (2, 4, 8)]
+    return ([{"form": {}, "knobs": {"elas_rows": 2}}]
+            + [{"form": {}, "knobs": {"elas_rows": 1, "elas_warps": w}} for w in (2, 4, 8)])
 
 
 def darcy_key(space, dtype):

@@ -355,6 +355,9 @@ extern "C" int nfem_knob_set(int key, int value) {
     case NFEM_KNOB_ELAS_WARPS:
       if (value != 0 && value != 2 && value != 4 && value != 8) return NFEM_ERR_INVALID_ARG;
       break;
+    case NFEM_KNOB_ELAS_ROWS:
+      if (value < 0 || value > 2) return NFEM_ERR_INVALID_ARG;
+      break;
     default:
       return NFEM_ERR_INVALID_ARG;
   }

@@ -358,6 +358,99 @@ __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const Cos
   }
 }
 
+// Register form of the node rows (as elasticity_rows_reg_kernel): lane L
+// owns node column L of the row (deg <= 32), the two groups evaluate the
+// blocks of the row's (at most two) incidences, and each block reaches the
+// owner of its column by nine warp shuffles.  No shared-memory image; every
+// block added by its owner in incidence order (bitwise deterministic).
+__device__ __forceinline__ int cos_code_match(uint4 cw, int col) {
+  const uint32_t rep = 0x01010101u * uint32_t(col);
+  const uint32_t m0 = __vcmpeq4(cw.x, rep), m1 = __vcmpeq4(cw.y, rep), m2 = __vcmpeq4(cw.z, rep) & 0x0000ffffu;
+  if (m0) return (__ffs(m0) - 1) >> 3;
+  if (m1) return 4 + ((__ffs(m1) - 1) >> 3);
+  if (m2) return 8 + ((__ffs(m2) - 1) >> 3);
+  return -1;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_reg_kernel(const CosParams p) {
+  __shared__ CosTables<T> tb;
+  for (int i = threadIdx.x; i < 144; i += blockDim.x) tb.Psi[i] = T(c_Psi[i]);
+  if (threadIdx.x < 12) tb.mhat[threadIdx.x] = T(c_mhat[threadIdx.x]);
+  if (threadIdx.x < 4) tb.divhat[threadIdx.x] = T(c_divhat[threadIdx.x]);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane / 10, b = lane - 10 * (lane / 10);
+  const T* force = static_cast<const T*>(p.force);
+  T* values = static_cast<T*>(p.values);
+  T* rhs = static_cast<T*>(p.rhs);
+  const uint4* codes4 = reinterpret_cast<const uint4*>(p.codes);
+  for (int64_t v = int64_t(blockIdx.x) * kCosWarps + warp; v < p.n_nodes; v += int64_t(gridDim.x) * kCosWarps) {
+    const int64_t r0 = p.row0 + 3 * v;
+    const int32_t base = __ldg(p.row_ptr + r0);
+    const int len = __ldg(p.row_ptr + r0 + 1) - base;
+    const int32_t kb = __ldg(p.inc_ptr + r0), ke = __ldg(p.inc_ptr + r0 + 1);
+    if (len > 3 * kCosDegMax || len < 3 || len % 3 != 0 || ke - kb > 2) {
+      if (lane == 0) set_status(p.status, NFEM_ERR_UNSUPPORTED);
+      continue;
+    }
+    const int deg = len / 3;
+    T K[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) K[i][j] = T(0);
+    T rhs_acc[3] = {T(0), T(0), T(0)};
+    const int32_t k = kb + g;
+    if (lane < 20 && k < ke) {
+      const int32_t occ = __ldg(p.inc + k);
+      const int32_t c = occ / 30;
+      const int a = (occ - c * 30) / 3;
+      T J[3][3], adet;
+      uint32_t m;
+      cos_load_geom<T>(p, c, J, adet, m);
+      cos_block<T>(p, tb, J, adet, m, a, b, K);
+      if (b == 0 && force && (a == 8 || a == 9)) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+          rhs_acc[i] = -adet * T(1.0 / 6.0) * __ldg(force + int64_t(c) * 6 + (a == 8 ? 0 : 3) + i);
+      }
+    }
+    T acc[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) acc[e] = T(0);
+#pragma unroll
+    for (int gg = 0; gg < 2; ++gg) {
+      if (kb + gg >= ke) break;  // warp-uniform
+      const uint4 cw = __ldg(codes4 + (kb + gg));
+      const int src = lane < deg ? cos_code_match(cw, lane) : -1;
+      const int from = src >= 0 ? 10 * gg + src : lane;
+#pragma unroll
+      for (int e = 0; e < 9; ++e) {
+        const T val = __shfl_sync(0xffffffffu, K[e / 3][e % 3], from);
+        if (src >= 0) acc[e] += val;
+      }
+    }
+    if (lane < deg) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        T* out = values + int64_t(base) + i * len + 3 * lane;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          if (p.accumulate) out[j] += acc[i * 3 + j]; else out[j] = acc[i * 3 + j];
+        }
+      }
+    }
+    T r[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) r[i] = __shfl_sync(0xffffffffu, rhs_acc[i], 0) + __shfl_sync(0xffffffffu, rhs_acc[i], 10);
+    if (lane < 3 && rhs) {
+      const T rv = lane == 0 ? r[0] : (lane == 1 ? r[1] : r[2]);
+      if (p.accumulate) rhs[r0 + lane] += rv; else rhs[r0 + lane] = rv;
+    }
+  }
+}
+
 }  // namespace nfem
 
 using namespace nfem;
@@ -425,12 +518,19 @@ static int cosserat_launch(int value_type, int64_t n_cells, int64_t n_nodes, int
   p.n_cells = n_cells;
   p.geom = workspace;
   const int grid = grid_for(ceil_div(n_nodes, kCosWarps), 1, 8);
+  const bool reg = knob(NFEM_KNOB_ELAS_ROWS) != 1;  // register accumulation (default) or shared images (1)
   if (value_type == NFEM_F64) {
     cos_geom_kernel<double><<<grid_for(n_cells, 256), 256, 0, stream>>>(p);
-    cosserat_rows_kernel<double><<<grid, 32 * kCosWarps, 0, stream>>>(p);
+    if (reg)
+      cosserat_rows_reg_kernel<double><<<grid, 32 * kCosWarps, 0, stream>>>(p);
+    else
+      cosserat_rows_kernel<double><<<grid, 32 * kCosWarps, 0, stream>>>(p);
   } else {
     cos_geom_kernel<float><<<grid_for(n_cells, 256), 256, 0, stream>>>(p);
-    cosserat_rows_kernel<float><<<grid, 32 * kCosWarps, 0, stream>>>(p);
+    if (reg)
+      cosserat_rows_reg_kernel<float><<<grid, 32 * kCosWarps, 0, stream>>>(p);
+    else
+      cosserat_rows_kernel<float><<<grid, 32 * kCosWarps, 0, stream>>>(p);
   }
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;

@@ -82,6 +82,8 @@ class KrylovSolver:
         dev = A.values.device
         if self.values32 is None or self.values32.data_ptr() == 0:
             self.values32 = A.values.to(torch.float32)
+        if self.values32.dtype != torch.float32 or self.values32.numel() < A.nnz:
+            raise ValueError("A32_values must be the FP32 values of A's pattern")
         st = _lib.stream_ptr(stream)
         sp = A.space
         if self.pc_kind == "none":

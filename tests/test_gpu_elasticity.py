@@ -33,9 +33,21 @@ def row_scaled_err(Ag, Ao):
     return (abs(d).max(axis=1).toarray().ravel() / scale).max()
 
 
+@pytest.mark.parametrize("rows", [1, 2])
 @pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
 @pytest.mark.parametrize("n", [1, 2, 4])
-def test_elasticity_matches_oracle(cuda_lib, dtype, tol, n):
+def test_elasticity_matches_oracle(cuda_lib, dtype, tol, n, rows):
+    """rows: the node-row kernel (2 register accumulation, 1 shared-memory
+    row images), chosen by the NFEM_KNOB_ELAS_ROWS launch knob."""
+    from nfempy_gb300 import autotune
+    autotune.set_knobs({"elas_rows": rows})
+    try:
+        _check_elasticity(dtype, tol, n)
+    finally:
+        autotune.reset_knobs()
+
+
+def _check_elasticity(dtype, tol, n):
     m = mesh_gen.cube(n)
     T = m["blocks"][-1][1].shape[0]
     rng = np.random.default_rng(n)
