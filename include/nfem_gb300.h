@@ -684,9 +684,10 @@ int nfem_mlp_param_count(const int32_t* dims, int64_t* count);
 /* Inference of the same network on the tensor cores (tcgen05.mma, BF16 x
  * BF16 -> FP32 accumulators in tensor memory): y [batch] = the network's
  * output for x [batch, dims[0]], one fused persistent kernel.  params = the
- * BF16 copy, params_f32 = the FP32 master (biases).  The hidden activations
- * after layer 1 are rounded to BF16 (the MMA operand type).  Shapes other
- * than dims = {<= 16, 256, 256, 1} return NFEM_ERR_UNSUPPORTED. */
+ * BF16 copy, params_f32 = the FP32 master (biases).  The inputs and the
+ * hidden activations after layer 1 are rounded to BF16 (the MMA operand
+ * type).  Shapes other than dims = {<= 16, 256, 256, 1} return
+ * NFEM_ERR_UNSUPPORTED. */
 int nfem_mlp_infer_tc(const int32_t* dims, const void* params, const float* params_f32, int64_t batch,
                       const float* x, float* y, int32_t* dev_status, void* stream);
 int nfem_mlp_forward(const int32_t* dims, int weight_type, const void* params,

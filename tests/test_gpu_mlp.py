@@ -118,8 +118,8 @@ def test_bf16_forward_and_adam(cuda_lib):
 
 def torch_reference_tc(P32, Pb, dims, x):
     """Plain PyTorch FP32 restatement of nfem_mlp_infer_tc: BF16 weights,
-    FP32 biases, the layer-1 activations rounded to BF16 (the MMA operand
-    type), FP32 accumulation."""
+    FP32 biases, the inputs and the layer-1 activations rounded to BF16 (the
+    MMA operand type), FP32 accumulation."""
     i, h1, h2, o = dims
     W = Pb.float()
     k = 0
@@ -129,7 +129,8 @@ def torch_reference_tc(P32, Pb, dims, x):
     b2 = P32[k:k + h2]; k += h2
     W3 = W[k:k + o * h2].view(o, h2); k += o * h2
     b3 = P32[k:k + o]
-    a1 = torch.relu(x @ W1.T + b1).to(torch.bfloat16).float()
+    xb = x.to(torch.bfloat16).float()
+    a1 = torch.relu(xb @ W1.T + b1).to(torch.bfloat16).float()
     a2 = torch.relu(a1 @ W2.T + b2)
     return a2 @ W3.T + b3
 
