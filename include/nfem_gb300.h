@@ -688,6 +688,24 @@ int nfem_mlp_param_count(const int32_t* dims, int64_t* count);
  * hidden activations after layer 1 are rounded to BF16 (the MMA operand
  * type).  Shapes other than dims = {<= 16, 256, 256, 1} return
  * NFEM_ERR_UNSUPPORTED. */
+/* Replaces LERieszMapWeakForm.evaluate_form_vectorized
+ * (src/weak_forms/le_riesz_map_weak_form.py:245-360): the Riesz map of the
+ * mixed linear-elastic space s (RT1 x 3), u (P0 x 3), t (P0 x 3), 18 local
+ * DoFs, DoF = row0 + 3 * node + component; per stress row c the compliance
+ * 1/(2 mu) int psi_i . psi_j plus int div psi_i div psi_j, minus
+ * lambda / (2 mu (2 mu + 3 lambda)) int psi_i[c] psi_j[d] across rows, and
+ * the P0 mass on u and t.  Constant lambda, mu (host); the Cosserat node-row
+ * kernel in its Riesz mode over the 18-DoF layout.  Arguments otherwise as
+ * nfem_cosserat_riesz_assemble. */
+int nfem_le_riesz_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                           const double* points, const float* points_split,
+                           const int32_t* cell_vertices, const uint8_t* sign_mask, double lambda_,
+                           double mu, const double* ref_Psi, const double* ref_mhat,
+                           const double* ref_divhat, const int32_t* inc_ptr, const int32_t* inc,
+                           const uint8_t* node_codes, const int32_t* row_ptr, void* values,
+                           int accumulate, void* workspace, size_t workspace_bytes,
+                           int32_t* dev_status, void* stream);
+
 int nfem_mlp_infer_tc(const int32_t* dims, const void* params, const float* params_f32, int64_t batch,
                       const float* x, float* y, int32_t* dev_status, void* stream);
 int nfem_mlp_forward(const int32_t* dims, int weight_type, const void* params,

@@ -1173,6 +1173,78 @@ class LCEScaledRieszMapWeakForm(LCEDualWeakForm):
                   _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
 
 
+class LERieszMapWeakForm(WeakForm):
+    """Riesz map of the mixed linear-elastic space s (RT1^3), u (P0^3),
+    t (P0^3) on tetrahedra (src/weak_forms/le_riesz_map_weak_form.py:245-360,
+    the preconditioning operator of the mixed elasticity drivers): per stress
+    row the compliance 1/(2 mu) int psi_i . psi_j plus int div psi_i div psi_j,
+    minus lambda / (2 mu (2 mu + 3 lambda)) int tr(psi) tr(psi) across the
+    rows, and the P0 mass on u and t.  functions: "lambda", "mu" (constants
+    or callables constant over the mesh; "rhs" is read by the reference but
+    does not enter the operator).  Jacobian only."""
+
+    cell_form = True
+    NAMES = ("lambda", "mu")
+
+    def _check_space(self):
+        sp = self.space
+        if sp is None or self.functions is None:
+            raise ValueError
+        if sp.names != ["s", "u", "t"] or sp.dim != 3:
+            raise NotImplementedError("LERieszMapWeakForm expects fields ('s', 'u', 't') on tetrahedra")
+        d = sp.discrete_spaces
+        ok = (d["s"].family == "RT" and d["s"].k_order == 1 and d["u"].family == "Lagrange" and d["u"].k_order == 0
+              and d["t"].family == "Lagrange" and d["t"].k_order == 0 and all(d[n].n_comp == 3 for n in sp.names))
+        if not ok:
+            raise NotImplementedError("LERieszMapWeakForm expects RT1^3 x P0^3 x P0^3")
+
+    def coefficients(self, dtype):
+        key = ("coef", dtype)
+        if key in self._cache:
+            return self._cache[key]
+        par = []
+        for k in self.NAMES:
+            v = self.functions[k]
+            if callable(v):
+                xq = self.quadrature_points()
+                vals = np.asarray(v(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).ravel()
+                if vals.size == 0 or np.abs(vals - vals[0]).max() > 1e-14 * max(1.0, np.abs(vals).max()):
+                    raise NotImplementedError(f"{k} must be constant over the mesh (the device form takes one material)")
+                par.append(float(vals[0]))
+            else:
+                par.append(float(np.ravel(v)[0]))
+        from .elements import rt1_tet_tables
+        Psi, mhat, divhat = rt1_tet_tables()
+        out = (par[0], par[1], np.ascontiguousarray(Psi.reshape(-1)), np.ascontiguousarray(mhat.reshape(-1)),
+               np.ascontiguousarray(divhat))
+        self._cache[key] = out
+        return out
+
+    def assemble(self, jacobian, residual=None, accumulate=False, stream=None, coefficients=None):
+        self._check_space()
+        sp = self.space
+        dtype = jacobian.dtype
+        vt = _lib.NFEM_F64 if dtype == torch.float64 else _lib.NFEM_F32
+        if jacobian.node_codes is None:
+            raise NotImplementedError("matrix built without node codes")
+        lam, mu, Psi, mhat, divhat = coefficients if coefficients is not None else self.coefficients(dtype)
+        dp = _lib.C.POINTER(_lib.C.c_double)
+        key = ("geom", dtype)
+        if key not in self._cache:
+            nb = _lib.C.c_size_t(0)
+            _lib.call("nfem_cosserat_workspace_bytes", vt, sp.n_cells, _lib.C.byref(nb))
+            self._cache[key] = torch.empty(max(int(nb.value), 16), dtype=torch.uint8, device=sp.device)
+        ws = self._cache[key]
+        _lib.call("nfem_le_riesz_assemble", vt, sp.n_cells, sp.n_dof // 3, sp.dof_shift, _lib.ptr(sp.points),
+                  _lib.ptr(sp.points_split), _lib.ptr(sp.cells), _lib.ptr(sp.rt_sign_mask), float(lam), float(mu),
+                  Psi.ctypes.data_as(dp), mhat.ctypes.data_as(dp), divhat.ctypes.data_as(dp),
+                  _lib.ptr(jacobian.inc_ptr), _lib.ptr(jacobian.inc), _lib.ptr(jacobian.node_codes),
+                  _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values), int(accumulate), _lib.ptr(ws), ws.numel(),
+                  _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+        if residual is not None and not accumulate:
+            residual.zero_()
+
+
 # ---------------------------------------------------------------- norms
 _RT1_SIGMA = {2: np.array([-1.0, 1.0, -1.0]), 3: np.array([1.0, -1.0, 1.0, -1.0])}
 

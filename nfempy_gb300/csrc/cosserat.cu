@@ -84,7 +84,13 @@ struct CosParams {
   // div-div term of every s row and (times l^2 for a constant l) every m row,
   // and the P0 mass on u and t; no coupling blocks, no load
   int riesz;
+  // local DoFs per cell: 30 (s, m, u, t) or 18 (s, u, t: the linear
+  // elasticity layout of LERieszMapWeakForm, no couple stress)
+  int n_loc;
 };
+
+// block kind of local node x: 0..3 s faces, 4..7 m faces, 8 u, 9 t
+__device__ __forceinline__ int cos_kind(int n_loc, int x) { return n_loc == 30 ? x : (x < 4 ? x : x + 4); }
 
 template <typename T>
 __device__ __forceinline__ void cos_edges(const CosParams& p, int32_t c, T (&J)[3][3]);
@@ -305,10 +311,10 @@ __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const Cos
     __syncwarp();
     T rhs_acc[3] = {T(0), T(0), T(0)};
     const int32_t k = kb + g;
-    if (lane < 20 && k < ke) {
+    if (lane < 20 && k < ke && b < p.n_loc / 3) {
       const int32_t occ = __ldg(p.inc + k);
-      const int32_t c = occ / 30;
-      const int a = (occ - c * 30) / 3;
+      const int32_t c = occ / p.n_loc;
+      const int a = cos_kind(p.n_loc, (occ - c * p.n_loc) / 3);
       // node position inside the row; the clamp keeps a corrupted code in
       // this node's image (a valid one is < deg)
       const int pos = min(int(__ldg(p.codes + int64_t(k) * 16 + b)), deg - 1);
@@ -316,7 +322,7 @@ __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_kernel(const Cos
       uint32_t m;
       cos_load_geom<T>(p, c, J, adet, m);
       T K[3][3];
-      cos_block<T>(p, tb, J, adet, m, a, b, K);
+      cos_block<T>(p, tb, J, adet, m, a, cos_kind(p.n_loc, b), K);
       T* im = img[warp][g];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
@@ -402,14 +408,14 @@ __global__ void __launch_bounds__(32 * kCosWarps) cosserat_rows_reg_kernel(const
       for (int j = 0; j < 3; ++j) K[i][j] = T(0);
     T rhs_acc[3] = {T(0), T(0), T(0)};
     const int32_t k = kb + g;
-    if (lane < 20 && k < ke) {
+    if (lane < 20 && k < ke && b < p.n_loc / 3) {
       const int32_t occ = __ldg(p.inc + k);
-      const int32_t c = occ / 30;
-      const int a = (occ - c * 30) / 3;
+      const int32_t c = occ / p.n_loc;
+      const int a = cos_kind(p.n_loc, (occ - c * p.n_loc) / 3);
       T J[3][3], adet;
       uint32_t m;
       cos_load_geom<T>(p, c, J, adet, m);
-      cos_block<T>(p, tb, J, adet, m, a, b, K);
+      cos_block<T>(p, tb, J, adet, m, a, cos_kind(p.n_loc, b), K);
       if (b == 0 && force && (a == 8 || a == 9)) {
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -466,7 +472,8 @@ static int cosserat_launch(int value_type, int64_t n_cells, int64_t n_nodes, int
                            const double* params7, const void* force, const double* ref_Psi, const double* ref_mhat,
                            const double* ref_divhat, const int32_t* inc_ptr, const int32_t* inc,
                            const uint8_t* node_codes, const int32_t* row_ptr, void* values, void* rhs, int accumulate,
-                           void* workspace, size_t workspace_bytes, int32_t* dev_status, void* stream_, int riesz){
+                           void* workspace, size_t workspace_bytes, int32_t* dev_status, void* stream_, int riesz,
+                           int n_loc = 30) {
   cudaStream_t stream = (cudaStream_t)stream_;
   if (n_cells < 0) return NFEM_ERR_INVALID_ARG;
   if ((value_type != NFEM_F64 && value_type != NFEM_F32) || n_nodes < 0 || row0 < 0 || !params7)
@@ -512,6 +519,7 @@ static int cosserat_launch(int value_type, int64_t n_cells, int64_t n_nodes, int
   p.accumulate = accumulate != 0;
   p.status = dev_status;
   p.riesz = riesz;
+  p.n_loc = n_loc;
   const size_t vb = value_type == NFEM_F64 ? sizeof(double) : sizeof(float);
   if (!workspace || workspace_bytes < size_t(n_cells) * 12 * vb || (reinterpret_cast<uintptr_t>(workspace) & 15))
     return NFEM_ERR_WORKSPACE;
@@ -561,4 +569,22 @@ extern "C" int nfem_cosserat_riesz_assemble(int value_type, int64_t n_cells, int
   return cosserat_launch(value_type, n_cells, n_nodes, row0, points, points_split, cell_vertices, sign_mask, params7,
                          nullptr, ref_Psi, ref_mhat, ref_divhat, inc_ptr, inc, node_codes, row_ptr, values, nullptr,
                          accumulate, workspace, workspace_bytes, dev_status, stream, 1);
+}
+
+extern "C" int nfem_le_riesz_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                                      const double* points, const float* points_split,
+                                      const int32_t* cell_vertices, const uint8_t* sign_mask, double lambda_,
+                                      double mu, const double* ref_Psi, const double* ref_mhat,
+                                      const double* ref_divhat, const int32_t* inc_ptr, const int32_t* inc,
+                                      const uint8_t* node_codes, const int32_t* row_ptr, void* values,
+                                      int accumulate, void* workspace, size_t workspace_bytes,
+                                      int32_t* dev_status, void* stream) {
+  // the stress block of the Cosserat Riesz map with kappa = mu (equal weights
+  // 1/(2 mu) on the symmetric and skew parts: 1/(4 mu) + 1/(4 kappa) = 1/(2 mu),
+  // 1/(4 mu) - 1/(4 kappa) = 0) is the linear-elastic compliance; the
+  // couple-stress parameters are unused by the 18-DoF layout
+  const double par[7] = {lambda_, mu, mu, lambda_, mu, mu, 1.0};
+  return cosserat_launch(value_type, n_cells, n_nodes, row0, points, points_split, cell_vertices, sign_mask, par,
+                         nullptr, ref_Psi, ref_mhat, ref_divhat, inc_ptr, inc, node_codes, row_ptr, values, nullptr,
+                         accumulate, workspace, workspace_bytes, dev_status, stream, 1, 18);
 }

@@ -378,6 +378,38 @@ def cosserat_riesz_element(X, signs, quad, par, l_fn, grad_l_fn):
     return np.zeros(n), j
 
 
+def le_riesz_element(X, signs, quad, lam_fn, mu_fn):
+    """LERieszMapWeakForm.evaluate_form_vectorized
+    (le_riesz_map_weak_form.py:245-360), 3-D, fields s (RT1 x 3), u, t
+    (P0 x 3), 18 local DoFs, s DoF (i, c) at 3 i + c: per stress row c the
+    (1/(2 mu)) psi_i . psi_j mass and the (div psi_i, div psi_j) term; across
+    the rows -(1/(2 mu)) lambda / (2 mu + 3 lambda) psi_i[c] psi_j[d]; the P0
+    mass on u and t.  lam_fn, mu_fn(x, y, z) -> [Q] at the quadrature
+    points."""
+    dim = 3
+    pts, wts = quad
+    x, J, det, pinv = evaluate_mapping(dim, pts, X)
+    s_tab = tabulate_oriented("RT", dim, 1, pts, J, det, pinv, signs)
+    Q = len(wts)
+    wdet = det * wts
+    lam = np.ravel(lam_fn(x[:, 0], x[:, 1], x[:, 2])) * np.ones(Q)
+    mu = np.ravel(mu_fn(x[:, 0], x[:, 1], x[:, 2])) * np.ones(Q)
+    psi = s_tab[0, :, :, 0:dim]  # [Q, 4, 3]
+    j = np.zeros((18, 18))
+    mass = np.einsum("q,qid,qjd->ij", wdet / (2.0 * mu), psi, psi)
+    div = np.trace(s_tab[1:dim + 1, :, :, 0:dim], axis1=0, axis2=3).T / det  # [4, Q]
+    ddiv = (div * wdet) @ div.T
+    for c in range(3):
+        idx = np.arange(4) * 3 + c
+        j[np.ix_(idx, idx)] += mass + ddiv
+    vf = (1.0 / (2.0 * mu)) * (lam / (2.0 * mu + dim * lam))
+    flat = psi.reshape(Q, 12)
+    j[:12, :12] -= np.einsum("q,qa,qb->ab", vf * wdet, flat, flat)
+    for k in range(12, 18):
+        j[k, k] += np.sum(wdet)
+    return np.zeros(18), j
+
+
 def darcy_dirichlet_facet(Xc, signs_c, local_face, Xf, dim, quad_f, p_D):
     """LaplaceDualWeakFormBCDirichlet.evaluate_form (laplace_dual_weak_form.py:90-154)
     for one boundary facet: r = sum_q |det J_F| w_q p_D(x_q) (psi_f . n), with

@@ -20,6 +20,7 @@ def golden_mesh(name):
     return {"dim": int(g["mesh_dim"]), "points": g["points"], "blocks": blocks}
 
 
+LE_FIELDS = [("s", "RT", 1, 3, False), ("u", "P", 0, 3, True), ("t", "P", 0, 3, True)]
 COSSERAT_FIELDS = [("s", "RT", 1, 3, False), ("m", "RT", 1, 3, False), ("u", "P", 0, 3, True), ("t", "P", 0, 3, True)]
 CASES = {
     "darcy2d_n4": (lambda: mesh_gen.square(4), DARCY),
@@ -30,6 +31,8 @@ CASES = {
                                                  ("u", "P", 0, 3, True), ("t", "P", 0, 3, True)]),
     "darcy3d_msh0": (lambda: golden_mesh("darcy3d_msh0"), DARCY),
     "cosserat3d_msh0": (lambda: golden_mesh("cosserat3d_msh0"), COSSERAT_FIELDS),
+    "le3d_n1": (lambda: mesh_gen.cube(1), LE_FIELDS),
+    "le3d_msh0": (lambda: golden_mesh("le3d_msh0"), LE_FIELDS),
 }
 
 
@@ -66,6 +69,11 @@ def cosserat_rhs(x, y, z):
 RIESZ_FUNCTIONS = {**{k: _const(v) for k, v in COSSERAT_PARAMS.items() if k != "l"},
                    "l": lambda x, y, z: 0.8 + 0.3 * x - 0.1 * y * z,
                    "grad_l": lambda x, y, z: np.array([0.3 + 0.0 * x, -0.1 * z, -0.1 * y])}
+
+# the mixed linear-elastic Riesz map (LERieszMapWeakForm): constant
+# material; the reference reads "rhs" but the operator does not use it
+LE_RIESZ_FUNCTIONS = {"lambda": _const(1.3), "mu": _const(0.7),
+                      "rhs": lambda x, y, z: np.zeros((3,) + np.shape(x))}
 
 FORM_FUNCTIONS = {
     "darcy": {

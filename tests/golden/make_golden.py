@@ -289,9 +289,10 @@ from weak_forms.laplace_dual_weak_form import LaplaceDualWeakForm  # noqa: E402
 from weak_forms.le_primal_weak_form import LEPrimalWeakForm  # noqa: E402
 from weak_forms.lce_dual_weak_form import LCEDualWeakForm  # noqa: E402
 from weak_forms.lce_scaled_riesz_map_weak_form import LCEScaledRieszMapWeakForm  # noqa: E402
+from weak_forms.le_riesz_map_weak_form import LERieszMapWeakForm  # noqa: E402
 
 sys.path.insert(0, os.path.dirname(HERE))
-from cases import FORM_FUNCTIONS, FORM_FUNCTIONS_DEVICE, RIESZ_FUNCTIONS  # noqa: E402
+from cases import FORM_FUNCTIONS, FORM_FUNCTIONS_DEVICE, LE_RIESZ_FUNCTIONS, RIESZ_FUNCTIONS  # noqa: E402
 
 
 class RecordingMat:
@@ -314,6 +315,10 @@ class CountingForm:
     def evaluate_form(self, i, alpha):
         n = len(alpha)
         return np.zeros(n), np.ones((n, n))
+
+
+def kind_of(name):
+    return name.split("_")[0].rstrip("23d")
 
 
 def element_forms(name, space, n_el, functions=None):
@@ -406,10 +411,17 @@ def make_case(name, mesh, fields):
     out["bc_dest"] = np.array([space.bc_destination_indexes(i) for i in range(n_bc)], dtype=np.int64)
     out["bc_vertices"] = np.array(
         [space.discrete_spaces[first].bc_elements[i].data.cell.node_tags for i in range(n_bc)], dtype=np.int64)
-    out["r_el"], out["j_el"] = element_forms(name, space, n_el)
-    kind = name.split("_")[0].rstrip("23d")
+    if kind_of(name) in FORM_FUNCTIONS:
+        out["r_el"], out["j_el"] = element_forms(name, space, n_el)
+    kind = kind_of(name)
     if kind in FORM_FUNCTIONS_DEVICE:
         out["r_el_dev"], out["j_el_dev"] = element_forms(name, space, n_el, FORM_FUNCTIONS_DEVICE)
+    if name.startswith("le3d"):
+        # LERieszMapWeakForm (le_riesz_map_weak_form.py:245-360)
+        wf = LERieszMapWeakForm(space)
+        wf.functions = LE_RIESZ_FUNCTIONS
+        out["j_riesz"] = np.array([np.asarray(wf.evaluate_form_vectorized(i, np.zeros(dest.shape[1]))[1])
+                                   for i in range(n_el)])
     if name.startswith("cosserat"):
         # LCEScaledRieszMapWeakForm (lce_scaled_riesz_map_weak_form.py:415-598)
         wf = LCEScaledRieszMapWeakForm(space)
@@ -443,6 +455,9 @@ def main():
     make_case("cosserat3d_msh0", msh,
               [("s", "RT", 1, 3, False), ("m", "RT", 1, 3, False),
                ("u", "Lagrange", 0, 3, True), ("t", "Lagrange", 0, 3, True)])
+    le = [("s", "RT", 1, 3, False), ("u", "Lagrange", 0, 3, True), ("t", "Lagrange", 0, 3, True)]
+    make_case("le3d_n1", mesh_gen.cube(1), le)
+    make_case("le3d_msh0", msh, le)
     make_case("cosserat3d_n1", mesh_gen.cube(1),
               [("s", "RT", 1, 3, False), ("m", "RT", 1, 3, False),
                ("u", "Lagrange", 0, 3, True), ("t", "Lagrange", 0, 3, True)])

@@ -79,3 +79,29 @@ def test_device_form_on_a_cell_subset_at_nonzero_alpha(cuda_lib, name):
     scale = np.abs(j_ref).max()
     np.testing.assert_allclose(got, O.toarray(), rtol=0, atol=1e-12 * scale)
     np.testing.assert_allclose(res.cpu().numpy(), ro, rtol=0, atol=1e-11 * max(scale, np.abs(ro).max()))
+
+
+@pytest.mark.parametrize("name", ["le3d_n1", "le3d_msh0"])
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
+def test_le_riesz_map_equals_reference(cuda_lib, name, dtype, tol):
+    """LERieszMapWeakForm on the device (the Cosserat node-row kernel over
+    the 18-DoF layout) against the reference's own
+    LERieszMapWeakForm.evaluate_form_vectorized; the assembled operator
+    against the oracle's."""
+    from tests.cases import LE_RIESZ_FUNCTIONS
+    mk, fields = CASES[name]
+    g = golden(name)
+    sp = product_space(mk(), fields)
+    wf = nf.LERieszMapWeakForm(sp)
+    wf.functions = LE_RIESZ_FUNCTIONS
+    r, j = wf.evaluate_forms(np.arange(sp.n_cells), dtype=dtype)
+    scale = np.abs(g["j_riesz"]).max()
+    np.testing.assert_allclose(j.double().cpu().numpy(), g["j_riesz"], rtol=0, atol=tol * scale)
+    assert float(r.abs().max().item()) == 0.0
+    A = nf.CSRMatrix(sp, dtype=dtype)
+    wf.assemble(A)
+    A.assemble()
+    O, _ = assembly.assemble_csr(g["cell_dofs"], g["j_riesz"], np.zeros(g["cell_dofs"].shape), int(g["n_dof"]))
+    Ag = A.to_scipy()
+    np.testing.assert_array_equal(Ag.indptr, O.indptr)
+    np.testing.assert_allclose(Ag.toarray(), O.toarray(), rtol=0, atol=tol * scale)
