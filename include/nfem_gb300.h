@@ -697,6 +697,21 @@ int nfem_mlp_param_count(const int32_t* dims, int64_t* count);
  * the P0 mass on u and t.  Constant lambda, mu (host); the Cosserat node-row
  * kernel in its Riesz mode over the 18-DoF layout.  Arguments otherwise as
  * nfem_cosserat_riesz_assemble. */
+/* Replaces LEDualWeakForm.evaluate_form_vectorized
+ * (src/weak_forms/le_dual_weak_form.py:354-515), the mixed linear-elastic
+ * form with weakly imposed symmetry, with the scatter: the same 18-DoF
+ * layout; per stress row the compliance 1/(2 mu) (psi_i . psi_j) minus
+ * lambda / (2 mu (2 mu + 3 lambda)) psi_i[c] psi_j[d], the rotation
+ * coupling (t, s) = the skew moments of the stress basis, the displacement
+ * coupling (u, s) = int div psi_j per component, and r = -int f_u, -int f_t
+ * (force [n_cells, 6] of cell means, or NULL).  Constant lambda, mu. */
+int nfem_le_dual_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                          const double* points, const float* points_split, const int32_t* cell_vertices,
+                          const uint8_t* sign_mask, double lambda_, double mu, const void* force,
+                          const double* ref_Psi, const double* ref_mhat, const double* ref_divhat,
+                          const int32_t* inc_ptr, const int32_t* inc, const uint8_t* node_codes,
+                          const int32_t* row_ptr, void* values, void* rhs, int accumulate,
+                          void* workspace, size_t workspace_bytes, int32_t* dev_status, void* stream);
 int nfem_le_riesz_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
                            const double* points, const float* points_split,
                            const int32_t* cell_vertices, const uint8_t* sign_mask, double lambda_,

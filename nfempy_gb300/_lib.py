@@ -150,6 +150,9 @@ _SIGS = {
                                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), _P, _P, _P,
                                       _P, _P, _I, _P, _SZ, _P, _P], _I),
     "nfem_cosserat_workspace_bytes": ([_I, _I64, C.POINTER(C.c_size_t)], _I),
+    "nfem_le_dual_assemble": ([_I, _I64, _I64, _I64, _P, _P, _P, _P, C.c_double, C.c_double, _P,
+                               C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), _P, _P, _P, _P,
+                               _P, _P, _I, _P, _SZ, _P, _P], _I),
     "nfem_le_riesz_assemble": ([_I, _I64, _I64, _I64, _P, _P, _P, _P, C.c_double, C.c_double, C.POINTER(C.c_double),
                                 C.POINTER(C.c_double), C.POINTER(C.c_double), _P, _P, _P, _P, _P, _I, _P, _SZ, _P,
                                 _P], _I),

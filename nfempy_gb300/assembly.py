@@ -1173,6 +1173,66 @@ class LCEScaledRieszMapWeakForm(LCEDualWeakForm):
                   _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
 
 
+class LEDualWeakForm(WeakForm):
+    """Mixed linear elasticity with weakly imposed symmetry, 3-D
+    (src/weak_forms/le_dual_weak_form.py:354-515): fields s (RT1^3), u (P0^3),
+    t (P0^3).  functions: "lambda", "mu" (constants or callables constant
+    over the mesh) and "rhs" (f_u then f_t, a 6-vector, per-cell [T, 6] or
+    f(x, y, z) -> [6, N]: its quadrature-weighted cell mean is exact for the
+    P0 test functions).  r = -int f . v at alpha = 0."""
+
+    cell_form = True
+    NAMES = ("lambda", "mu")
+
+    def _check_space(self):
+        LERieszMapWeakForm._check_space(self)
+
+    def coefficients(self, dtype):
+        key = ("coef", dtype)
+        if key in self._cache:
+            return self._cache[key]
+        sp = self.space
+        T = sp.n_cells
+        lam, mu, Psi, mhat, divhat = LERieszMapWeakForm.coefficients(self, dtype)
+        f = self.functions.get("rhs")
+        ft = None
+        if f is not None:
+            if callable(f):
+                xq = self.quadrature_points()
+                _, wts = sp.quadrature[sp.dim]
+                fq = np.asarray(f(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).reshape(6, T, -1)
+                fv = np.einsum("ktq,q->tk", fq, np.asarray(wts)) / float(np.sum(wts))
+            else:
+                fv = np.asarray(f, dtype=np.float64)
+                fv = np.broadcast_to(fv.reshape(1, 6) if fv.size == 6 else fv.reshape(T, 6), (T, 6))
+            ft = torch.as_tensor(np.array(fv, dtype=np.float64, order="C"), dtype=dtype, device=sp.device)
+        out = (lam, mu, ft, Psi, mhat, divhat)
+        self._cache[key] = out
+        return out
+
+    def assemble(self, jacobian, residual, accumulate=False, stream=None, coefficients=None):
+        self._check_space()
+        sp = self.space
+        dtype = jacobian.dtype
+        vt = _lib.NFEM_F64 if dtype == torch.float64 else _lib.NFEM_F32
+        if jacobian.node_codes is None:
+            raise NotImplementedError("matrix built without node codes")
+        lam, mu, f, Psi, mhat, divhat = coefficients if coefficients is not None else self.coefficients(dtype)
+        dp = _lib.C.POINTER(_lib.C.c_double)
+        key = ("geom", dtype)
+        if key not in self._cache:
+            nb = _lib.C.c_size_t(0)
+            _lib.call("nfem_cosserat_workspace_bytes", vt, sp.n_cells, _lib.C.byref(nb))
+            self._cache[key] = torch.empty(max(int(nb.value), 16), dtype=torch.uint8, device=sp.device)
+        ws = self._cache[key]
+        _lib.call("nfem_le_dual_assemble", vt, sp.n_cells, sp.n_dof // 3, sp.dof_shift, _lib.ptr(sp.points),
+                  _lib.ptr(sp.points_split), _lib.ptr(sp.cells), _lib.ptr(sp.rt_sign_mask), float(lam), float(mu),
+                  _lib.ptr(f), Psi.ctypes.data_as(dp), mhat.ctypes.data_as(dp), divhat.ctypes.data_as(dp),
+                  _lib.ptr(jacobian.inc_ptr), _lib.ptr(jacobian.inc), _lib.ptr(jacobian.node_codes),
+                  _lib.ptr(jacobian.row_ptr), _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate),
+                  _lib.ptr(ws), ws.numel(), _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+
+
 class LERieszMapWeakForm(WeakForm):
     """Riesz map of the mixed linear-elastic space s (RT1^3), u (P0^3),
     t (P0^3) on tetrahedra (src/weak_forms/le_riesz_map_weak_form.py:245-360,

@@ -571,6 +571,22 @@ extern "C" int nfem_cosserat_riesz_assemble(int value_type, int64_t n_cells, int
                          accumulate, workspace, workspace_bytes, dev_status, stream, 1);
 }
 
+extern "C" int nfem_le_dual_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
+                                     const double* points, const float* points_split, const int32_t* cell_vertices,
+                                     const uint8_t* sign_mask, double lambda_, double mu, const void* force,
+                                     const double* ref_Psi, const double* ref_mhat, const double* ref_divhat,
+                                     const int32_t* inc_ptr, const int32_t* inc, const uint8_t* node_codes,
+                                     const int32_t* row_ptr, void* values, void* rhs, int accumulate,
+                                     void* workspace, size_t workspace_bytes, int32_t* dev_status, void* stream) {
+  // the Cosserat dual form over the 18-DoF layout with kappa = mu: the
+  // compliance weighs the symmetric and skew parts alike (1/(2 mu)), and the
+  // (t, s) and (u, s) couplings are the same operators
+  const double par[7] = {lambda_, mu, mu, lambda_, mu, mu, 1.0};
+  return cosserat_launch(value_type, n_cells, n_nodes, row0, points, points_split, cell_vertices, sign_mask, par,
+                         force, ref_Psi, ref_mhat, ref_divhat, inc_ptr, inc, node_codes, row_ptr, values, rhs,
+                         accumulate, workspace, workspace_bytes, dev_status, stream, 0, 18);
+}
+
 extern "C" int nfem_le_riesz_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int64_t row0,
                                       const double* points, const float* points_split,
                                       const int32_t* cell_vertices, const uint8_t* sign_mask, double lambda_,

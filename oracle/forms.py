@@ -378,6 +378,24 @@ def cosserat_riesz_element(X, signs, quad, par, l_fn, grad_l_fn):
     return np.zeros(n), j
 
 
+LE_OF_COSSERAT = np.r_[0:12, 24:30]  # s, u, t inside the Cosserat layout s, m, u, t
+
+
+def le_dual_element(X, signs, quad, lam, mu, f_fn):
+    """LEDualWeakForm.evaluate_form_vectorized (le_dual_weak_form.py:354-515),
+    3-D, fields s (RT1 x 3), u, t (P0 x 3), 18 local DoFs: the mixed Cosserat
+    element with kappa = mu (the compliance 1/(2 mu) on the symmetric and the
+    skew part alike) restricted to the s, u and t DoFs.  The reference's
+    blocks are the same operators: (s, s) 1/(2 mu) psi_i . psi_j minus the
+    volumetric term, (t, s) the skew moments of the stress basis, (u, s)
+    int div psi_j per component, r = -int f.  lam, mu constants; f_fn(x, y,
+    z) -> [6, Q] (f_u then f_t)."""
+    par = dict(lambda_s=lam, mu_s=mu, kappa_s=mu, lambda_o=lam, mu_o=mu, kappa_o=mu, l=1.0)
+    r, j = cosserat_element(X, signs, quad, par, f_fn, None)
+    idx = LE_OF_COSSERAT
+    return r[idx], j[np.ix_(idx, idx)]
+
+
 def le_riesz_element(X, signs, quad, lam_fn, mu_fn):
     """LERieszMapWeakForm.evaluate_form_vectorized
     (le_riesz_map_weak_form.py:245-360), 3-D, fields s (RT1 x 3), u, t

@@ -89,6 +89,9 @@ FORM_FUNCTIONS = {
         **{k: _const(v) for k, v in COSSERAT_PARAMS.items()},
         "rhs": cosserat_rhs,
     },
+    # LEDualWeakForm: constant material (the device form takes one), a load
+    # that varies inside the cells
+    "le": {"lambda": _const(1.3), "mu": _const(0.7), "rhs": cosserat_rhs},
 }
 
 # coefficients the device forms take as they are: kappa, lambda and mu

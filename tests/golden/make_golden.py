@@ -290,6 +290,7 @@ from weak_forms.le_primal_weak_form import LEPrimalWeakForm  # noqa: E402
 from weak_forms.lce_dual_weak_form import LCEDualWeakForm  # noqa: E402
 from weak_forms.lce_scaled_riesz_map_weak_form import LCEScaledRieszMapWeakForm  # noqa: E402
 from weak_forms.le_riesz_map_weak_form import LERieszMapWeakForm  # noqa: E402
+from weak_forms.le_dual_weak_form import LEDualWeakForm  # noqa: E402
 
 sys.path.insert(0, os.path.dirname(HERE))
 from cases import FORM_FUNCTIONS, FORM_FUNCTIONS_DEVICE, LE_RIESZ_FUNCTIONS, RIESZ_FUNCTIONS  # noqa: E402
@@ -330,6 +331,9 @@ def element_forms(name, space, n_el, functions=None):
     elif kind == "elast":
         wf = LEPrimalWeakForm(space)
         ev = wf.evaluate_form
+    elif kind == "le":
+        wf = LEDualWeakForm(space)
+        ev = wf.evaluate_form_vectorized
     else:
         wf = LCEDualWeakForm(space)
         ev = wf.evaluate_form_vectorized

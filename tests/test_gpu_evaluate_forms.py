@@ -14,7 +14,8 @@ from tests.gpu_helpers import product_space
 
 pytestmark = pytest.mark.gpu
 
-FORMS = {"darcy": nf.LaplaceDualWeakForm, "elast": nf.LEPrimalWeakForm, "cosserat": nf.LCEDualWeakForm}
+FORMS = {"darcy": nf.LaplaceDualWeakForm, "elast": nf.LEPrimalWeakForm, "cosserat": nf.LCEDualWeakForm,
+         "le": nf.LEDualWeakForm}
 
 
 def kind_of(name):
@@ -24,12 +25,13 @@ def kind_of(name):
 def reference_arrays(name):
     g = golden(name)
     kind = kind_of(name)
-    if kind == "cosserat":
-        return g["r_el"], g["j_el"], FORM_FUNCTIONS["cosserat"]
+    if kind in ("cosserat", "le"):
+        return g["r_el"], g["j_el"], FORM_FUNCTIONS[kind]
     return g["r_el_dev"], g["j_el_dev"], FORM_FUNCTIONS_DEVICE[kind]
 
 
-CELL_CASES = ["darcy2d_n4", "darcy3d_n2", "darcy3d_msh0", "elast3d_n2", "cosserat3d_n1", "cosserat3d_msh0"]
+CELL_CASES = ["darcy2d_n4", "darcy3d_n2", "darcy3d_msh0", "elast3d_n2", "cosserat3d_n1", "cosserat3d_msh0",
+              "le3d_n1", "le3d_msh0"]
 
 
 @pytest.mark.parametrize("name", CELL_CASES)

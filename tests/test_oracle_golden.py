@@ -63,7 +63,7 @@ def test_pattern_b_filter():
     assert list(zip(rows.tolist(), ix.tolist())) == [(0, 0), (0, 2), (1, 1), (1, 2), (2, 2)]
 
 
-@pytest.mark.parametrize("name", [n for n in sorted(CASES) if not n.startswith("le3d")])
+@pytest.mark.parametrize("name", sorted(CASES))
 def test_element_forms_match_reference(name):
     """The oracle's element residuals and Jacobians against the ones the
     reference's own weak forms computed (LaplaceDualWeakForm, LEPrimalWeakForm
@@ -88,6 +88,8 @@ def test_element_forms_match_reference(name):
             r, j = forms.darcy_element(X[c], signs[c], dim, quad, F["kappa"], F["rhs"])
         elif kind == "elast":
             r, j = forms.elasticity_element(X[c], dim, quad, F["lambda"], F["mu"], F["rhs"])
+        elif kind == "le":
+            r, j = forms.le_dual_element(X[c], signs[c], quad, 1.3, 0.7, F["rhs"])
         else:
             r, j = forms.cosserat_element(X[c], signs[c], quad, COSSERAT_PARAMS, F["rhs"], None)
         jr, rr = g["j_el"][c], g["r_el"][c]
