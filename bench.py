@@ -655,6 +655,28 @@ def elasticity_bench(args):
         out["solve_cell_block"]["preconditioner"] = "cell-block Jacobi (30 x 30 cell blocks)"
         out["solve_cell_block"]["speedup_vs_point_jacobi"] = (out["solve"]["time_to_solve_ms"]
                                                               / out["solve_cell_block"]["time_to_solve_ms"])
+        # the driver's own solver family: CG (ICC replaced by 3 x 3 node blocks)
+        from nfempy_gb300.solvers import CGSolver
+        for pc in ("node_block", "jacobi"):
+            cg = CGSolver(A64, pc=pc, A32_values=A32v)
+            torch.cuda.synchronize()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record()
+            cg.setup()
+            e1.record()
+            xcg, info = cg.solve(-r64, rtol=1e-8, raise_on_failure=False)
+            e2.record()
+            torch.cuda.synchronize()
+            rel = float(cg.residual(xcg, -r64).norm() / r64.norm())
+            out[f"solve_cg_{pc}"] = {"setup_ms": e0.elapsed_time(e1), "solve_ms": e1.elapsed_time(e2),
+                                     "time_to_solve_ms": e0.elapsed_time(e2), "inner_iterations": info.inner_iterations,
+                                     "outer_iterations": info.outer_iterations, "final_relres_fp64": rel,
+                                     "status": info.status,
+                                     "ms_per_inner_iteration": e1.elapsed_time(e2) / max(1, info.inner_iterations),
+                                     "preconditioner": ("3 x 3 node-block Jacobi" if pc == "node_block"
+                                                        else "point Jacobi"),
+                                     "speedup_vs_fgmres_point_jacobi": out["solve"]["time_to_solve_ms"]
+                                     / e0.elapsed_time(e2)}
     return out
 
 

@@ -513,8 +513,10 @@ typedef enum {
   NFEM_PC_CELL_BLOCK = 2,  /* cell-patch block Jacobi (weighted additive Schwarz over
                               the element cliques): cell_dofs [n_cells, n_loc],
                               block_inv [n_cells, n_loc, n_loc], row incidences */
-  NFEM_PC_TWO_LEVEL = 3    /* NFEM_PC_CELL_BLOCK smoother followed by a Galerkin coarse
+  NFEM_PC_TWO_LEVEL = 3,   /* NFEM_PC_CELL_BLOCK smoother followed by a Galerkin coarse
                               correction (see nfem_two_level) */
+  NFEM_PC_NODE_BLOCK = 4   /* nfem_solve_ir_pcg only: inverses of the 3 x 3 diagonal
+                              blocks of the nodes of a vector field (DoF = 3 node + c) */
 } nfem_pc_kind;
 
 /* Two-level preconditioner: z = B v, then z += P Ac^-1 P^T (v - A z), with B
@@ -674,20 +676,7 @@ int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, const nfem_pr
                          void* workspace, size_t workspace_bytes, nfem_solve_info* info,
                          void* stream);
 
-/* ----------------------------------- K6: learned preconditioner network
- * No counterpart in the reference (nfempy has no learned component).
- * Network x -> relu(W1 x + b1) -> relu(W2 h1 + b2) -> W3 h2 + b3, dims =
- * {in, h1, h2, out}, parameters flat [W1 | b1 | W2 | b2 | W3 | b3] with
- * W_l [out, in] row-major; activations batch-major.  weight_type NFEM_BF16
- * reads BF16 weights (and biases from params_f32), FP32 accumulation. */
-int nfem_mlp_param_count(const int32_t* dims, int64_t* count);
-/* Inference of the same network on the tensor cores (tcgen05.mma, BF16 x
- * BF16 -> FP32 accumulators in tensor memory): y [batch] = the network's
- * output for x [batch, dims[0]], one fused persistent kernel.  params = the
- * BF16 copy, params_f32 = the FP32 master (biases).  The inputs and the
- * hidden activations after layer 1 are rounded to BF16 (the MMA operand
- * type).  Shapes other than dims = {<= 16, 256, 256, 1} return
- * NFEM_ERR_UNSUPPORTED. */
+/* ------------------------- mixed linear elasticity (s, u, t), 3-D */
 /* Replaces LERieszMapWeakForm.evaluate_form_vectorized
  * (src/weak_forms/le_riesz_map_weak_form.py:245-360): the Riesz map of the
  * mixed linear-elastic space s (RT1 x 3), u (P0 x 3), t (P0 x 3), 18 local
@@ -721,6 +710,39 @@ int nfem_le_riesz_assemble(int value_type, int64_t n_cells, int64_t n_nodes, int
                            int accumulate, void* workspace, size_t workspace_bytes,
                            int32_t* dev_status, void* stream);
 
+
+/* Conjugate gradients for symmetric positive definite systems (the
+ * driver's PETSc CG, examples/cauchy_elasticity/cg_elasticity_example_1.py:
+ * 159-170, with a block-diagonal preconditioner in place of ICC): FP32 CG on
+ * A32 inside FP64 iterative refinement on A64 until ||b - A x|| / ||b|| <=
+ * rtol; each inner solve stops at inner_rtol (relative, on its own start).
+ * x is overwritten (start 0 is not assumed: the first residual uses x).
+ * pc_kind NFEM_PC_JACOBI (inv [n_rows] = 1 / a_ii) or NFEM_PC_NODE_BLOCK
+ * (inv [n_rows / 3][9]), filled by nfem_pcg_setup from the FP64 matrix.
+ * Reductions in a fixed order (deterministic).  Synchronises on `stream`
+ * every 16 inner iterations and per refinement step.  A non-positive p.Ap
+ * sets NFEM_ERR_BREAKDOWN. */
+int nfem_pcg_setup(int pc_kind, const nfem_csr* A64, float* inv, int32_t* dev_status, void* stream);
+int nfem_pcg_workspace_bytes(int64_t n_rows, size_t* bytes);
+int nfem_solve_ir_pcg(const nfem_csr* A64, const nfem_csr* A32, int pc_kind, const float* inv,
+                      const double* b, double* x, double rtol, double inner_rtol, int max_inner,
+                      int max_outer, void* workspace, size_t workspace_bytes, nfem_solve_info* info,
+                      int32_t* dev_status, void* stream);
+
+/* ----------------------------------- K6: learned preconditioner network
+ * No counterpart in the reference (nfempy has no learned component).
+ * Network x -> relu(W1 x + b1) -> relu(W2 h1 + b2) -> W3 h2 + b3, dims =
+ * {in, h1, h2, out}, parameters flat [W1 | b1 | W2 | b2 | W3 | b3] with
+ * W_l [out, in] row-major; activations batch-major.  weight_type NFEM_BF16
+ * reads BF16 weights (and biases from params_f32), FP32 accumulation. */
+int nfem_mlp_param_count(const int32_t* dims, int64_t* count);
+/* Inference of the same network on the tensor cores (tcgen05.mma, BF16 x
+ * BF16 -> FP32 accumulators in tensor memory): y [batch] = the network's
+ * output for x [batch, dims[0]], one fused persistent kernel.  params = the
+ * BF16 copy, params_f32 = the FP32 master (biases).  The inputs and the
+ * hidden activations after layer 1 are rounded to BF16 (the MMA operand
+ * type).  Shapes other than dims = {<= 16, 256, 256, 1} return
+ * NFEM_ERR_UNSUPPORTED. */
 int nfem_mlp_infer_tc(const int32_t* dims, const void* params, const float* params_f32, int64_t batch,
                       const float* x, float* y, int32_t* dev_status, void* stream);
 int nfem_mlp_forward(const int32_t* dims, int weight_type, const void* params,

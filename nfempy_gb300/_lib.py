@@ -78,7 +78,7 @@ class SolveInfo(C.Structure):
                 ("final_relres", C.c_double), ("status", C.c_int), ("n_snapshots", C.c_int)]
 
 
-PC_NONE, PC_JACOBI, PC_CELL_BLOCK, PC_TWO_LEVEL = 0, 1, 2, 3
+PC_NONE, PC_JACOBI, PC_CELL_BLOCK, PC_TWO_LEVEL, PC_NODE_BLOCK = 0, 1, 2, 3, 4
 
 _P = C.c_void_p
 _I = C.c_int
@@ -105,6 +105,9 @@ _SIGS = {
     "nfem_knob_set": ([_I, _I], _I),
     "nfem_mlp_infer_tc": ([_P, _P, _P, _I64, _P, _P, _P, _P], _I),
     "nfem_csr_add_entries": ([_I, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P], _I),
+    "nfem_pcg_setup": ([_I, _P, _P, _P, _P], _I),
+    "nfem_pcg_workspace_bytes": ([_I64, C.POINTER(_SZ)], _I),
+    "nfem_solve_ir_pcg": ([_P, _P, _I, _P, _P, _P, C.c_double, C.c_double, _I, _I, _P, _SZ, _P, _P, _P], _I),
     "nfem_scatter_elements": ([_I, _I64, _I, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P], _I),
     "nfem_rt1_dirichlet_rows": ([_I, _I, _I64, _P, _P, _P, _I, _I, _I, C.c_double, _P, C.POINTER(C.c_double), _I,
                                  _P, _P], _I),

@@ -632,6 +632,8 @@ class LCEDualWeakFormBCDirichlet(LaplaceDualWeakFormBCDirichlet):
     3-vectors).  Facets whose tag is in bc_physical_tags (default: the
     space's b_physical_tags["s"], or every tagged facet).  Residual only."""
 
+    FIELD_DATA = (("s", "u"), ("m", "t"))  # (RT1 field, its Dirichlet datum)
+
     def __init__(self, space, bc_physical_tags=None):
         super().__init__(space, bc_physical_tags if bc_physical_tags is not None
                          else (space.b_physical_tags.get("s") or None))
@@ -648,7 +650,7 @@ class LCEDualWeakFormBCDirichlet(LaplaceDualWeakFormBCDirichlet):
         occ_t = torch.as_tensor(occ, device=sp.device)
         qw = np.ascontiguousarray(wts, dtype=np.float64)
         keep = [occ_t]
-        for field, name in (("s", "u"), ("m", "t")):
+        for field, name in self.FIELD_DATA:
             fn = self.functions[name]
             if callable(fn):
                 v = np.asarray(fn(xq[..., 0], xq[..., 1], xq[..., 2]), dtype=np.float64).reshape(3, *xq.shape[:2])
@@ -662,6 +664,16 @@ class LCEDualWeakFormBCDirichlet(LaplaceDualWeakFormBCDirichlet):
                           qw.ctypes.data_as(_lib.C.POINTER(_lib.C.c_double)), len(wts), _lib.ptr(residual),
                           _lib.stream_ptr(stream))
         self._keep = keep
+
+
+class LEDualWeakFormBCDirichlet(LCEDualWeakFormBCDirichlet):
+    """Displacement data on boundary facets for the mixed linear-elastic form
+    (src/weak_forms/le_dual_weak_form.py:518-595): for every component c,
+    adds -int_F u_D[c] (tau . n) to the stress row c of the facet's flux
+    DoF.  functions: {"u": f(x, y, z) -> [3, N]} (or a 3-vector).  Residual
+    only."""
+
+    FIELD_DATA = (("s", "u"),)
 
 
 class SequentialAssembler:

@@ -200,6 +200,78 @@ class KrylovSolver:
         return r
 
 
+class CGSolver:
+    """Conjugate gradients for symmetric positive definite systems (the P2
+    elasticity driver's PETSc CG, cg_elasticity_example_1.py:159-170): FP32
+    CG on the FP32 copy of A inside FP64 iterative refinement on A, with
+    point Jacobi (pc="jacobi") or the inverses of the 3 x 3 diagonal node
+    blocks of a vector field (pc="node_block", DoF = 3 node + component) in
+    place of the driver's incomplete Cholesky."""
+
+    def __init__(self, A, pc="node_block", A32_values=None):
+        if A.dtype != torch.float64:
+            raise ValueError("A must be the FP64 matrix (the residual is measured in FP64)")
+        if pc not in ("jacobi", "node_block"):
+            raise ValueError(f"unknown preconditioner {pc}")
+        self.A = A
+        self.pc_kind = pc
+        self.values32 = A32_values
+        self.status = torch.zeros(1, dtype=torch.int32, device=A.values.device)
+        self._setup_done = False
+
+    def setup(self, stream=None):
+        A = self.A
+        dev = A.values.device
+        if self.values32 is None:
+            self.values32 = A.values.to(torch.float32)
+        if self.values32.dtype != torch.float32 or self.values32.numel() < A.nnz:
+            raise ValueError("A32_values must be the FP32 values of A's pattern")
+        kind = _lib.PC_JACOBI if self.pc_kind == "jacobi" else _lib.PC_NODE_BLOCK
+        if kind == _lib.PC_NODE_BLOCK and A.n_rows % 3:
+            raise NotImplementedError("node blocks need 3 DoFs per node")
+        self.inv = torch.empty(A.n_rows * (1 if kind == _lib.PC_JACOBI else 3), dtype=torch.float32, device=dev)
+        a64 = _csr(A)
+        _lib.call("nfem_pcg_setup", kind, _lib.C.byref(a64), _lib.ptr(self.inv), _lib.ptr(self.status),
+                  _lib.stream_ptr(stream))
+        wsb = _lib.C.c_size_t(0)
+        _lib.call("nfem_pcg_workspace_bytes", A.n_rows, _lib.C.byref(wsb))
+        self.ws = torch.empty(int(wsb.value), dtype=torch.uint8, device=dev)
+        self._kind = kind
+        self._setup_done = True
+        s = int(self.status.item())
+        if s:
+            self.status.zero_()
+            raise _lib.NfemError(s, "CG preconditioner setup")
+
+    def solve(self, b, rtol=1e-8, inner_rtol=1e-3, max_inner=20000, max_outer=50, x=None, stream=None,
+              raise_on_failure=True):
+        if not self._setup_done:
+            self.setup(stream)
+        A = self.A
+        b = b.to(torch.float64).contiguous()
+        x = torch.zeros_like(b) if x is None else x
+        info = _lib.SolveInfo()
+        a64 = _csr(A)
+        a32 = _csr(A, self.values32)
+        rc = _lib.lib().nfem_solve_ir_pcg(_lib.C.byref(a64), _lib.C.byref(a32), self._kind, _lib.ptr(self.inv),
+                                           _lib.ptr(b), _lib.ptr(x), float(rtol), float(inner_rtol), int(max_inner),
+                                           int(max_outer), _lib.ptr(self.ws), self.ws.numel(), _lib.C.byref(info),
+                                           _lib.ptr(self.status), _lib.stream_ptr(stream))
+        res = SolveResult(info)
+        if rc != 0:
+            self.status.zero_()
+            if raise_on_failure:
+                raise _lib.NfemError(rc, f"CG solve ({res.as_dict()})")
+        return x, res
+
+    def residual(self, x, b, stream=None):
+        r = torch.empty_like(b)
+        A = self.A
+        _lib.call("nfem_residual_f64", A.n_rows, _lib.ptr(A.row_ptr), _lib.ptr(A.col_idx), _lib.ptr(A.values),
+                  _lib.ptr(x), _lib.ptr(b), _lib.ptr(r), _lib.stream_ptr(stream))
+        return r
+
+
 class TwoLevelCoarse:
     """Aggregates and prolongation structure of the two-level preconditioner.
 

@@ -168,3 +168,36 @@ def test_cosserat_dirichlet_matches_oracle(cuda_lib):
                                                   lambda x, y, z: np.array([fn(x, y, z)[comp]]))
                 ro[cd[c, off + i * 3 + comp]] -= val
     np.testing.assert_allclose(rg, ro, rtol=1e-12, atol=1e-13 * np.abs(ro).max())
+
+
+def test_le_dual_dirichlet_matches_oracle(cuda_lib):
+    """LEDualWeakFormBCDirichlet (le_dual_weak_form.py:518-595): -int_F u_D[c]
+    (tau . n) on the stress rows of every boundary facet's flux DoF of the
+    mixed linear-elastic space (s, u, t), against the oracle's facet
+    restatement, FP64 1e-12."""
+    from nfempy_gb300.assembly import LEDualWeakFormBCDirichlet
+    from tests.cases import LE_FIELDS
+    m = mesh_gen.cube(2)
+    sp = product_space(m, LE_FIELDS)
+    A = nf.CSRMatrix(sp, dtype=torch.float64)
+    res = torch.zeros(A.n_rows, dtype=torch.float64, device="cuda")
+    uD = lambda x, y, z: np.array([1 + x, y * z, np.sin(z) + 0 * x])
+    bc = LEDualWeakFormBCDirichlet(sp)
+    bc.functions = {"u": uD}
+    bc.assemble(A, res)
+    torch.cuda.synchronize()
+    rg = res.cpu().numpy()
+    topo = topology.Topology(m)
+    cd, nd = topology.cell_dofs(topo, [topology.FieldSpec(*f) for f in LE_FIELDS])
+    X = m["points"][topo.cells]
+    s = topo.rt1_signs()
+    qf = quadrature.make_quadrature(2, 3)
+    ro = np.zeros(nd)
+    occ, fverts = bc.facets()
+    for o, fv in zip(occ, fverts):
+        c, i = divmod(int(o), 4)
+        for comp in range(3):
+            val = forms.darcy_dirichlet_facet(X[c], s[c], i, m["points"][fv], 3, qf,
+                                              lambda x, y, z: np.array([uD(x, y, z)[comp]]))
+            ro[cd[c, i * 3 + comp]] -= val
+    np.testing.assert_allclose(rg, ro, rtol=1e-12, atol=1e-13 * np.abs(ro).max())

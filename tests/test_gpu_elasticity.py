@@ -141,3 +141,58 @@ def test_elasticity_clamped_solve(cuda_lib):
     xo = solve.solve_newton_step(Ag, res.cpu().numpy())
     xg = x.cpu().numpy()
     assert np.linalg.norm(xg - xo) <= 1e-5 * np.linalg.norm(xo)
+
+
+@pytest.mark.parametrize("pc", ["jacobi", "node_block"])
+def test_elasticity_clamped_solve_cg(cuda_lib, pc):
+    """The driver's own solver family (cg_elasticity_example_1.py:159-170:
+    CG on the SPD penalised system): CGSolver with point Jacobi or 3 x 3 node
+    blocks in place of ICC, FP32 CG inside FP64 refinement, to 1e-8 FP64
+    relative residual; equal to SuperLU's solution; twice the same solve
+    gives bitwise the same iterate (fixed-order reductions)."""
+    from nfempy_gb300.solvers import CGSolver
+    from oracle import solve
+    m = mesh_gen.cube(3)
+    T = m["blocks"][-1][1].shape[0]
+    rng = np.random.default_rng(5)
+    sp = product_space(m, FIELD)
+    A = nf.CSRMatrix(sp, dtype=torch.float64)
+    res = torch.zeros(A.n_rows, dtype=torch.float64, device="cuda")
+    wf = LEPrimalWeakForm(sp)
+    wf.functions = {"lambda": np.exp(rng.normal(0, 0.5, T)), "mu": np.exp(rng.normal(0, 0.5, T)),
+                    "rhs": np.array([1.0, 1.0, 1.0])}
+    wf.assemble(A, res)
+    bc = LEPrimalWeakFormBCDirichlet(sp)
+    bc.functions = {"u": None}
+    bc.assemble(A)
+    torch.cuda.synchronize()
+    cg = CGSolver(A, pc=pc)
+    x, info = cg.solve(-res, rtol=1e-8)
+    assert info.status == 0 and info.final_relres <= 1e-8, info.as_dict()
+    rel = float(cg.residual(x, -res).norm() / res.norm())
+    assert rel <= 1e-8
+    x2, info2 = cg.solve(-res, rtol=1e-8)
+    assert torch.equal(x, x2) and info2.inner_iterations == info.inner_iterations
+    Ag = A.to_scipy()
+    xo = solve.solve_newton_step(Ag, res.cpu().numpy())
+    assert np.linalg.norm(x.cpu().numpy() - xo) <= 1e-5 * np.linalg.norm(xo)
+
+
+def test_cg_refuses_a_zero_diagonal(cuda_lib):
+    """The mixed Darcy saddle point (zero pressure block) is not a CG system:
+    its point-Jacobi setup finds the zero diagonal and reports
+    NFEM_ERR_DEGENERATE instead of dividing by it."""
+    from nfempy_gb300 import _lib
+    from nfempy_gb300.solvers import CGSolver
+    from tests.cases import DARCY
+    m = mesh_gen.cube(2)
+    sp = product_space(m, DARCY)
+    A = nf.CSRMatrix(sp, dtype=torch.float64)
+    res = torch.zeros(A.n_rows, dtype=torch.float64, device="cuda")
+    wf = nf.LaplaceDualWeakForm(sp)
+    wf.functions = {"kappa": 1.0, "rhs": 1.0}
+    wf.assemble(A, res)
+    cg = CGSolver(A, pc="jacobi")
+    with pytest.raises(_lib.NfemError) as e:
+        cg.setup()
+    assert _lib.STATUS_NAMES[e.value.status] == "NFEM_ERR_DEGENERATE"
