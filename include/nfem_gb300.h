@@ -70,13 +70,18 @@ const char* nfem_status_string(int status);
  *                                        accumulation by warp shuffles; 0 the
  *                                        built-in choice (elasticity: images,
  *                                        Cosserat: registers)
+ *   NFEM_KNOB_COARSE_TC                  trailing updates of the dense coarse
+ *                                        inverse: 0 tensor cores (3xTF32) from
+ *                                        512 aggregates on, 1 CUDA cores, 2
+ *                                        tensor cores from 128 on
  * nfem_knob_set returns NFEM_ERR_INVALID_ARG for an unknown key or value. */
 typedef enum {
   NFEM_KNOB_DARCY_ROWS_BLOCKS_PER_SM = 0,
   NFEM_KNOB_DARCY_CELLS_BLOCK = 1,
   NFEM_KNOB_ELAS_WARPS = 2,
   NFEM_KNOB_ELAS_ROWS = 3,
-  NFEM_KNOB_COUNT = 4
+  NFEM_KNOB_COARSE_TC = 4,
+  NFEM_KNOB_COUNT = 5
 } nfem_knob;
 int nfem_knob_set(int key, int value);
 int nfem_knob_get(int key, int* value);

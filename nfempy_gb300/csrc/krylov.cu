@@ -33,7 +33,10 @@
 #include <algorithm>
 #include <vector>
 
+#include <type_traits>
+
 #include "nfem_common.cuh"
+#include "tc_common.cuh"
 
 #define NFEM_RC(...)                \
   do {                              \
@@ -960,6 +963,123 @@ __global__ void __launch_bounds__(256) bgj_trailing(T* __restrict__ m, int N, in
     }
 }
 
+// The trailing update on the tensor cores (FP32 trailing matrix): a tile of
+// 128 rows x 256 columns of A_IJ -= A_IK A_KJ per CTA, as one 128 x 256 x 64
+// product in tensor memory.  The operands are split into TF32 high and low
+// parts (x = hi + lo, both TF32) and the product taken as hi.hi + hi.lo +
+// lo.hi (24 tcgen05.mma kind::tf32, M 128, N 256, K 8), which keeps FP32
+// accuracy (the dropped lo.lo term is below 2^-22 relative).  A_IK is staged
+// K-major as it lies in memory; A_KJ is staged transposed (column n of the
+// tile as row n of the B operand).  Rows and columns of the pivot block K
+// and beyond N are left alone.
+constexpr int kTcTM = 128, kTcTN = 256;
+constexpr uint32_t kTcSbo = (kGjB / 4) * 128;  // 2048: row-group stride of the K = 64 operands
+constexpr size_t kTcA = size_t(kTcTM) * kGjB * 4;   // 32 KB per part
+constexpr size_t kTcB = size_t(kTcTN) * kGjB * 4;   // 64 KB per part
+constexpr size_t kTcSmem = 2 * kTcA + 2 * kTcB + 64 + 1024;
+
+__device__ __forceinline__ uint32_t tc_off(int row, int k) {
+  return uint32_t((row & 7) * 16 + (row >> 3) * kTcSbo + (k & 3) * 4 + (k >> 2) * 128);
+}
+
+__global__ void __launch_bounds__(256, 1) bgj_trailing_tc(float* __restrict__ m, int N, int k0, int32_t* status) {
+  extern __shared__ uint8_t tc_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sAh = sm;
+  uint8_t* sAl = sAh + kTcA;
+  uint8_t* sBh = sAl + kTcA;
+  uint8_t* sBl = sBh + kTcB;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sBl + kTcB);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
+  volatile int32_t* flag = reinterpret_cast<volatile int32_t*>(slot + 1);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int i0 = blockIdx.y * kTcTM, j0 = blockIdx.x * kTcTN;
+  // A = A_IK: 128 rows x 64, 16-byte chunks; eight consecutive lanes take
+  // eight rows of one chunk (one 128-byte core-matrix line)
+  for (int q = t; q < kTcTM * (kGjB / 4); q += 256) {
+    const int r = (q & 7) + 8 * (q >> 7), c = (q >> 3) & 15;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i0 + r < N) v = *reinterpret_cast<const float4*>(m + int64_t(i0 + r) * N + k0 + 4 * c);
+    const float e[4] = {v.x, v.y, v.z, v.w};
+    float h[4], l[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      h[u] = tc::to_tf32(e[u]);
+      l[u] = tc::to_tf32(e[u] - h[u]);
+    }
+    *reinterpret_cast<float4*>(sAh + tc_off(r, 4 * c)) = make_float4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<float4*>(sAl + tc_off(r, 4 * c)) = make_float4(l[0], l[1], l[2], l[3]);
+  }
+  // B = A_KJ transposed: row n of B = column j0 + n of the 64 pivot rows
+  for (int q = t; q < kGjB * (kTcTN / 4); q += 256) {
+    const int k = q >> 6, n4 = q & 63;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (j0 + 4 * n4 < N) v = *reinterpret_cast<const float4*>(m + int64_t(k0 + k) * N + j0 + 4 * n4);
+    const float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float h = tc::to_tf32(e[u]);
+      *reinterpret_cast<float*>(sBh + tc_off(4 * n4 + u, k)) = h;
+      *reinterpret_cast<float*>(sBl + tc_off(4 * n4 + u, k)) = tc::to_tf32(e[u] - h);
+    }
+  }
+  if (t == 0) {
+    tc::bar_init(tc::smem_u32(bar));
+    *flag = 0;
+  }
+  if (warp == 0) tc::tmem_alloc(tc::smem_u32(slot), kTcTN);
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *slot;
+  if (t == 0) {
+    constexpr uint32_t id = tc::idesc(tc::kTypeTF32, kTcTM, kTcTN);
+    const uint32_t ah = tc::smem_u32(sAh), al = tc::smem_u32(sAl), bh = tc::smem_u32(sBh), bl = tc::smem_u32(sBl);
+#pragma unroll 1
+    for (int ks = 0; ks < kGjB / 8; ++ks) {  // K = 8 per MMA: two 16-byte chunks
+      const uint32_t o = uint32_t(ks) * 256;
+      tc::mma_tf32(tmem, tc::smem_desc(ah + o, 128, kTcSbo), tc::smem_desc(bh + o, 128, kTcSbo), id, ks > 0);
+      tc::mma_tf32(tmem, tc::smem_desc(ah + o, 128, kTcSbo), tc::smem_desc(bl + o, 128, kTcSbo), id, 1u);
+      tc::mma_tf32(tmem, tc::smem_desc(al + o, 128, kTcSbo), tc::smem_desc(bh + o, 128, kTcSbo), id, 1u);
+    }
+    tc::commit(tc::smem_u32(bar));
+    if (!tc::wait_commit(tc::smem_u32(bar), 0, status)) *flag = 1;
+  }
+  __syncthreads();
+  tc::fence_after_sync();
+  if (!*flag) {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. and columns 128 (w / 4) ..
+    const int row = i0 + 32 * (warp & 3) + lane;
+    const bool row_ok = row < N && (row < k0 || row >= k0 + kGjB);
+#pragma unroll 1
+    for (int c0 = 0; c0 < kTcTN / 2; c0 += 32) {
+      uint32_t v[32];
+      const int cb = (warp >> 2) * (kTcTN / 2) + c0;
+      tc::tmem_ld32(tmem + (uint32_t(32 * (warp & 3)) << 16) + uint32_t(cb), v);
+      const int col0 = j0 + cb;
+      if (row_ok && col0 < N && (col0 + 32 <= k0 || col0 >= k0 + kGjB)) {
+        float4* dst = reinterpret_cast<float4*>(m + int64_t(row) * N + col0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          float4 x = dst[u];
+          x.x -= __uint_as_float(v[4 * u]);
+          x.y -= __uint_as_float(v[4 * u + 1]);
+          x.z -= __uint_as_float(v[4 * u + 2]);
+          x.w -= __uint_as_float(v[4 * u + 3]);
+          dst[u] = x;
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, kTcTN);
+  }
+}
+
 template <typename T>
 __global__ void bgj_put_diag(T* __restrict__ m, int N, int k0, const T* __restrict__ dblk) {
   for (int e = threadIdx.x; e < kGjB * kGjB; e += blockDim.x)
@@ -988,12 +1108,30 @@ static int blocked_inverse(const double* ac, int n, T* m, T* dblk, float* inv, i
            cudaFuncSetAttribute(bgj_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) == cudaSuccess;
   }();
   if (!attr) return NFEM_ERR_CUDA;
+  // trailing updates on the tensor cores (FP32 trailing matrix) from N = 512
+  // on, or from 128 with the knob at 2; 1 keeps the CUDA-core tiles
+  const int tck = knob(NFEM_KNOB_COARSE_TC);
+  bool tc = false;
+  if constexpr (std::is_same<T, float>::value) tc = tck != 1 && N >= (tck == 2 ? 128 : 512);
+  if (tc) {
+    static const bool tc_attr = cudaFuncSetAttribute(bgj_trailing_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     int(kTcSmem)) == cudaSuccess;
+    if (!tc_attr) return NFEM_ERR_CUDA;
+  }
   bgj_pad<T><<<grid_for(int64_t(N) * N, 256), 256, 0, s>>>(ac, n, N, m);
   for (int kb = 0; kb < nt; ++kb) {
     const int k0 = kb * kGjB;
     bgj_inv_diag<T><<<1, 1024, 0, s>>>(m, N, k0, dblk, status);
     bgj_panel<T><<<nt, 256, smem, s>>>(m, N, k0, dblk, 0);
-    bgj_trailing<T><<<dim3(nt, nt), 256, smem, s>>>(m, N, k0);
+    if constexpr (std::is_same<T, float>::value) {
+      if (tc)
+        bgj_trailing_tc<<<dim3(unsigned(ceil_div(N, kTcTN)), unsigned(ceil_div(N, kTcTM))), 256, kTcSmem, s>>>(
+            m, N, k0, status);
+      else
+        bgj_trailing<T><<<dim3(nt, nt), 256, smem, s>>>(m, N, k0);
+    } else {
+      bgj_trailing<T><<<dim3(nt, nt), 256, smem, s>>>(m, N, k0);
+    }
     bgj_panel<T><<<nt, 256, smem, s>>>(m, N, k0, dblk, 1);
     bgj_put_diag<T><<<1, 256, 0, s>>>(m, N, k0, dblk);
   }

@@ -226,15 +226,29 @@ def test_two_level_ap_product_and_fused_solve(cuda_lib):
     assert abs(out[True][3].inner_iterations - out[False][3].inner_iterations) <= 3
 
 
-@pytest.mark.parametrize("n_c", [4, 7])
-def test_dense_coarse_inverse(cuda_lib, n_c):
+@pytest.mark.parametrize("n_c,coarse_tc", [(4, 0), (7, 0), (7, 2), (8, 0), (8, 1), (9, 0)])
+def test_dense_coarse_inverse(cuda_lib, n_c, coarse_tc):
     """The stored FP32 inverse of the Galerkin coarse matrix: 64 aggregates
     (one tile) and 343 (tiles clipped at the padded edge, 128-wide trailing
     tiles straddling the pivot block) both give ||X A_c - I|| within FP32
-    round-off times the conditioning."""
+    round-off times the conditioning.  512 and 729 aggregates take the
+    trailing updates on the tensor cores (3xTF32 tcgen05 MMAs, tiles of
+    128 x 256 straddling the pivot block and the padded edge); the knob
+    NFEM_KNOB_COARSE_TC forces them at 343 (2) or keeps the CUDA cores at 512
+    (1), and both reach the same bound."""
+    from nfempy_gb300 import autotune, meshes
+    from nfempy_gb300.solvers import TwoLevelCoarse
+    autotune.set_knobs({"coarse_tc": coarse_tc})
+    try:
+        _check_dense_coarse_inverse(n_c)
+    finally:
+        autotune.reset_knobs()
+
+
+def _check_dense_coarse_inverse(n_c):
     from nfempy_gb300 import meshes
     from nfempy_gb300.solvers import TwoLevelCoarse
-    m = mesh_gen.cube(14)
+    m = mesh_gen.cube(max(14, 2 * n_c))
     cent = m["points"][m["blocks"][-1][1]].mean(axis=1)
     kappa = np.exp(meshes.grf_log_field(cent, 0.1, 1.0, 3))
     sp, A, res = assembled(m, kappa, 1.0)
