@@ -1010,18 +1010,25 @@ __global__ void __launch_bounds__(256, 1) bgj_trailing_tc(float* __restrict__ m,
     *reinterpret_cast<float4*>(sAh + tc_off(r, 4 * c)) = make_float4(h[0], h[1], h[2], h[3]);
     *reinterpret_cast<float4*>(sAl + tc_off(r, 4 * c)) = make_float4(l[0], l[1], l[2], l[3]);
   }
-  // B = A_KJ transposed: row n of B = column j0 + n of the 64 pivot rows
-  for (int q = t; q < kGjB * (kTcTN / 4); q += 256) {
-    const int k = q >> 6, n4 = q & 63;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (j0 + 4 * n4 < N) v = *reinterpret_cast<const float4*>(m + int64_t(k0 + k) * N + j0 + 4 * n4);
-    const float e[4] = {v.x, v.y, v.z, v.w};
+  // B = A_KJ transposed: row n of B = column j0 + n of the 64 pivot rows.
+  // Lane n takes the 16-byte chunk of four pivot rows of its column: the
+  // global loads of a warp are 32 consecutive columns, its shared stores
+  // whole 128-byte core-matrix lines
+  for (int q = t; q < kTcTN * (kGjB / 4); q += 256) {
+    const int n = q & (kTcTN - 1), c = q >> 8;
+    float e[4] = {0.f, 0.f, 0.f, 0.f};
+    if (j0 + n < N) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) e[u] = m[int64_t(k0 + 4 * c + u) * N + j0 + n];
+    }
+    float h[4], l[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const float h = tc::to_tf32(e[u]);
-      *reinterpret_cast<float*>(sBh + tc_off(4 * n4 + u, k)) = h;
-      *reinterpret_cast<float*>(sBl + tc_off(4 * n4 + u, k)) = tc::to_tf32(e[u] - h);
+      h[u] = tc::to_tf32(e[u]);
+      l[u] = tc::to_tf32(e[u] - h[u]);
     }
+    *reinterpret_cast<float4*>(sBh + tc_off(n, 4 * c)) = make_float4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<float4*>(sBl + tc_off(n, 4 * c)) = make_float4(l[0], l[1], l[2], l[3]);
   }
   if (t == 0) {
     tc::bar_init(tc::smem_u32(bar));

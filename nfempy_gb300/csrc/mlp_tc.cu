@@ -33,6 +33,7 @@
 #include <cuda_bf16.h>
 
 #include "nfem_common.cuh"
+#include "tc_common.cuh"
 
 namespace nfem {
 namespace {
@@ -58,23 +59,8 @@ constexpr size_t kOffSlot = kOffBar + 8;
 constexpr size_t kOffFlag = kOffSlot + 4;
 constexpr size_t kSmemBytes = kOffFlag + 4 + 1024;  // + alignment slack
 
-// Instruction descriptor of tcgen05.mma kind::f16: D FP32 (bits 4-5 = 1),
-// A and B BF16 (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0),
-// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kH >> 3) << 17) |
-                            (uint32_t(kTM >> 4) << 24);
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-// Shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading
-// byte offset >> 4 (bits 16-29), stride byte offset >> 4 (bits 32-45), the
-// fixed value 0b001 at bits 46-48, base offset 0, no swizzle (bits 61-63).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  return uint64_t((saddr & 0x3FFFFu) >> 4) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
-         (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
-}
+// Instruction descriptor: BF16 x BF16 -> FP32, M 128, N 256, both K-major.
+constexpr uint32_t kIdesc = tc::idesc(tc::kTypeBF16, 128, 256);
 
 __device__ __forceinline__ uint32_t operand_offset(int row, int k) {
   return uint32_t((row & 7) * 16 + (row >> 3) * kRowGroupBytes + (k & 7) * 2 + (k >> 3) * 128);
@@ -83,63 +69,10 @@ __device__ __forceinline__ uint32_t operand1_offset(int row, int k) {
   return uint32_t((row & 7) * 16 + (row >> 3) * kRowGroupBytes1 + (k & 7) * 2 + (k >> 3) * 128);
 }
 
-__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ bool bar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(done)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-
-// 32 consecutive FP32 columns of this thread's TMEM lane.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr)
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
-// Bounded wait for the MMA commit: about a second of polling at most.
-constexpr uint32_t kWaitPolls = 1u << 22;
-
 // Thread 0 issues nothing else while it waits: a bounded poll of the
 // mbarrier phase, NFEM_ERR_TIMEOUT and the flag when it runs out.
 __device__ __forceinline__ void wait_commit(uint32_t bar, uint32_t parity, int32_t* status, volatile int32_t* flag) {
-  uint32_t polls = 0;
-  while (!bar_try_wait(bar, parity)) {
-    if (++polls >= kWaitPolls) {
-      set_status(status, NFEM_ERR_TIMEOUT);
-      *flag = 1;
-      return;
-    }
-  }
+  if (!tc::wait_commit(bar, parity, status)) *flag = 1;
 }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
@@ -209,23 +142,19 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   const float b3 = *b3p;
   if (t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(sbar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    tc::bar_init(tc::smem_u32(sbar));
     *sflag = 0;
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(sslot)),
-                 "r"(kTmemCols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    tc::tmem_alloc(tc::smem_u32(sslot), kTmemCols);
   }
-  fence_before_sync();
+  tc::fence_before_sync();
   __syncthreads();
-  fence_after_sync();
+  tc::fence_after_sync();
   const uint32_t tmem = *sslot;
-  const uint32_t bar = smem_u32(sbar);
-  const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
-  const uint32_t a1_base = smem_u32(sA1), w1_base = smem_u32(sW1);
+  const uint32_t bar = tc::smem_u32(sbar);
+  const uint32_t a_base = tc::smem_u32(sA), b_base = tc::smem_u32(sB);
+  const uint32_t a1_base = tc::smem_u32(sA1), w1_base = tc::smem_u32(sW1);
 
   const int r = t & (kTM - 1), half = t >> 7;
   const int quarter = warp & 3, chalf = warp >> 2;  // TMEM lanes 32 quarter.., columns 128 chalf..
@@ -246,26 +175,27 @@ __global__ void __launch_bounds__(kThreads, 1)
           make_uint4(pack_bf16x2(xv[0], xv[1]), pack_bf16x2(xv[2], xv[3]), pack_bf16x2(xv[4], xv[5]),
                      pack_bf16x2(xv[6], xv[7]));
     }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    fence_before_sync();
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
     __syncthreads();
-    fence_after_sync();
+    tc::fence_after_sync();
     // ---- layer 1 (tensor cores): one MMA, K = 16
     if (t == 0) {
-      mma_bf16(tmem, smem_desc(a1_base, 128, kRowGroupBytes1), smem_desc(w1_base, 128, kRowGroupBytes1), 0u);
-      mma_commit(bar);
+      tc::mma_f16(tmem, tc::smem_desc(a1_base, 128, kRowGroupBytes1), tc::smem_desc(w1_base, 128, kRowGroupBytes1), kIdesc,
+                  0u);
+      tc::commit(bar);
       wait_commit(bar, parity, status, sflag);
     }
     parity ^= 1u;
     __syncthreads();
     if (*sflag) break;
-    fence_after_sync();
+    tc::fence_after_sync();
     // ---- epilogue 1: + b1, ReLU, BF16 -> A2
 #pragma unroll 1
     for (int c0 = 0; c0 < kH / 2; c0 += 32) {
       uint32_t v[32];
       const int cb = chalf * (kH / 2) + c0;
-      tmem_ld32(tmem + lane_base + uint32_t(cb), v);
+      tc::tmem_ld32(tmem + lane_base + uint32_t(cb), v);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         uint32_t pk[4];
@@ -278,46 +208,46 @@ __global__ void __launch_bounds__(kThreads, 1)
         *reinterpret_cast<uint4*>(sA + operand_offset(r, cb + q * 8)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
     }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    fence_before_sync();
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
     __syncthreads();
-    fence_after_sync();
+    tc::fence_after_sync();
     // ---- layer 2 (tensor cores): 16 MMAs of K = 16 (two 16-byte K chunks each)
     if (t == 0) {
 #pragma unroll 1
       for (int ks = 0; ks < kH / 16; ++ks) {
-        const uint64_t ad = smem_desc(a_base + ks * 256, 128, kRowGroupBytes);
-        const uint64_t bd = smem_desc(b_base + ks * 256, 128, kRowGroupBytes);
-        mma_bf16(tmem + uint32_t(kH), ad, bd, ks > 0 ? 1u : 0u);
+        const uint64_t ad = tc::smem_desc(a_base + ks * 256, 128, kRowGroupBytes);
+        const uint64_t bd = tc::smem_desc(b_base + ks * 256, 128, kRowGroupBytes);
+        tc::mma_f16(tmem + uint32_t(kH), ad, bd, kIdesc, ks > 0 ? 1u : 0u);
       }
-      mma_commit(bar);
+      tc::commit(bar);
       wait_commit(bar, parity, status, sflag);
     }
     parity ^= 1u;
     __syncthreads();
     if (*sflag) break;
-    fence_after_sync();
+    tc::fence_after_sync();
     // ---- epilogue 2: + b2, ReLU, . W3
     float acc = 0.f;
 #pragma unroll 1
     for (int c0 = 0; c0 < kH / 2; c0 += 32) {
       uint32_t v[32];
       const int cb = chalf * (kH / 2) + c0;
-      tmem_ld32(tmem + lane_base + uint32_t(kH + cb), v);
+      tc::tmem_ld32(tmem + lane_base + uint32_t(kH + cb), v);
 #pragma unroll
       for (int i = 0; i < 32; ++i) acc = fmaf(fmaxf(__uint_as_float(v[i]) + sb2[cb + i], 0.f), sw3[cb + i], acc);
     }
     if (chalf == 1) spart[r] = acc;
-    fence_before_sync();
+    tc::fence_before_sync();
     __syncthreads();
     if (chalf == 0 && row < n_rows) y[row] = acc + spart[r] + b3;
   }
   // free the tensor memory (every MMA has completed: its commit was waited for)
-  fence_before_sync();
+  tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) {
-    fence_after_sync();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, kTmemCols);
   }
 }
 
