@@ -850,7 +850,7 @@ __global__ void __launch_bounds__(1024) bgj_inv_diag(T* __restrict__ m, int N, i
                                                      int32_t* status) {
   using D = NFEM_COARSE_DIAG_T;
   static_assert(kGjB == 64, "16 threads x 4 entries per row");
-  __shared__ D rowb[2][kGjB], colb[2][kGjB];
+  __shared__ D rowb[2][kGjB], colb[2][kGjB], ipb[2];
   const int r = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
   D a[4];
 #pragma unroll
@@ -866,10 +866,12 @@ __global__ void __launch_bounds__(1024) bgj_inv_diag(T* __restrict__ m, int N, i
 #pragma unroll
       for (int q = 1; q < 4; ++q) v = (k - c0 == q) ? a[q] : v;
       colb[b][r] = v;
+      // the pivot's reciprocal, once per step (the one division of the step)
+      if (r == k) ipb[b] = v != D(0) ? D(1) / v : D(0);
     }
     __syncthreads();
     const D p = rowb[b][k];
-    const D ip = p != D(0) ? D(1) / p : D(0);
+    const D ip = ipb[b];
     if (threadIdx.x == 0 && !(fabs(p) > 0.0)) set_status(status, NFEM_ERR_BREAKDOWN);
     const D cr = colb[b][r];
 #pragma unroll
@@ -995,40 +997,61 @@ __global__ void __launch_bounds__(256, 1) bgj_trailing_tc(float* __restrict__ m,
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int i0 = blockIdx.y * kTcTM, j0 = blockIdx.x * kTcTN;
   // A = A_IK: 128 rows x 64, 16-byte chunks; eight consecutive lanes take
-  // eight rows of one chunk (one 128-byte core-matrix line)
-  for (int q = t; q < kTcTM * (kGjB / 4); q += 256) {
-    const int r = (q & 7) + 8 * (q >> 7), c = (q >> 3) & 15;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (i0 + r < N) v = *reinterpret_cast<const float4*>(m + int64_t(i0 + r) * N + k0 + 4 * c);
-    const float e[4] = {v.x, v.y, v.z, v.w};
-    float h[4], l[4];
+  // eight rows of one chunk (one 128-byte core-matrix line).  Every load of
+  // the thread is issued before the first is used (eight in flight)
+  {
+    constexpr int kIt = kTcTM * (kGjB / 4) / 256;  // 8
+    float4 v[kIt];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      h[u] = tc::to_tf32(e[u]);
-      l[u] = tc::to_tf32(e[u] - h[u]);
+    for (int it = 0; it < kIt; ++it) {
+      const int q = t + 256 * it;
+      const int r = (q & 7) + 8 * (q >> 7), c = (q >> 3) & 15;
+      v[it] = i0 + r < N ? __ldg(reinterpret_cast<const float4*>(m + int64_t(i0 + r) * N + k0 + 4 * c))
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    *reinterpret_cast<float4*>(sAh + tc_off(r, 4 * c)) = make_float4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<float4*>(sAl + tc_off(r, 4 * c)) = make_float4(l[0], l[1], l[2], l[3]);
+#pragma unroll
+    for (int it = 0; it < kIt; ++it) {
+      const int q = t + 256 * it;
+      const int r = (q & 7) + 8 * (q >> 7), c = (q >> 3) & 15;
+      const float e[4] = {v[it].x, v[it].y, v[it].z, v[it].w};
+      float h[4], l[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        h[u] = tc::to_tf32(e[u]);
+        l[u] = tc::to_tf32(e[u] - h[u]);
+      }
+      *reinterpret_cast<float4*>(sAh + tc_off(r, 4 * c)) = make_float4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<float4*>(sAl + tc_off(r, 4 * c)) = make_float4(l[0], l[1], l[2], l[3]);
+    }
   }
   // B = A_KJ transposed: row n of B = column j0 + n of the 64 pivot rows.
   // Lane n takes the 16-byte chunk of four pivot rows of its column: the
   // global loads of a warp are 32 consecutive columns, its shared stores
   // whole 128-byte core-matrix lines
-  for (int q = t; q < kTcTN * (kGjB / 4); q += 256) {
-    const int n = q & (kTcTN - 1), c = q >> 8;
-    float e[4] = {0.f, 0.f, 0.f, 0.f};
-    if (j0 + n < N) {
+  // (sixteen chunks per thread, in two batches of eight: 32 loads in flight)
+  const int n = t & (kTcTN - 1);
+  const bool n_ok = j0 + n < N;
 #pragma unroll
-      for (int u = 0; u < 4; ++u) e[u] = m[int64_t(k0 + 4 * c + u) * N + j0 + n];
-    }
-    float h[4], l[4];
+  for (int batch = 0; batch < 2; ++batch) {
+    float e[8][4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      h[u] = tc::to_tf32(e[u]);
-      l[u] = tc::to_tf32(e[u] - h[u]);
+    for (int it = 0; it < 8; ++it) {
+      const int c = batch * 8 + it;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) e[it][u] = n_ok ? __ldg(m + int64_t(k0 + 4 * c + u) * N + j0 + n) : 0.f;
     }
-    *reinterpret_cast<float4*>(sBh + tc_off(n, 4 * c)) = make_float4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<float4*>(sBl + tc_off(n, 4 * c)) = make_float4(l[0], l[1], l[2], l[3]);
+#pragma unroll
+    for (int it = 0; it < 8; ++it) {
+      const int c = batch * 8 + it;
+      float h[4], l[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        h[u] = tc::to_tf32(e[it][u]);
+        l[u] = tc::to_tf32(e[it][u] - h[u]);
+      }
+      *reinterpret_cast<float4*>(sBh + tc_off(n, 4 * c)) = make_float4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<float4*>(sBl + tc_off(n, 4 * c)) = make_float4(l[0], l[1], l[2], l[3]);
+    }
   }
   if (t == 0) {
     tc::bar_init(tc::smem_u32(bar));
@@ -1067,14 +1090,16 @@ __global__ void __launch_bounds__(256, 1) bgj_trailing_tc(float* __restrict__ m,
       const int col0 = j0 + cb;
       if (row_ok && col0 < N && (col0 + 32 <= k0 || col0 >= k0 + kGjB)) {
         float4* dst = reinterpret_cast<float4*>(m + int64_t(row) * N + col0);
+        float4 x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x[u] = dst[u];  // eight loads in flight
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          float4 x = dst[u];
-          x.x -= __uint_as_float(v[4 * u]);
-          x.y -= __uint_as_float(v[4 * u + 1]);
-          x.z -= __uint_as_float(v[4 * u + 2]);
-          x.w -= __uint_as_float(v[4 * u + 3]);
-          dst[u] = x;
+          x[u].x -= __uint_as_float(v[4 * u]);
+          x[u].y -= __uint_as_float(v[4 * u + 1]);
+          x[u].z -= __uint_as_float(v[4 * u + 2]);
+          x[u].w -= __uint_as_float(v[4 * u + 3]);
+          dst[u] = x[u];
         }
       }
     }
