@@ -67,9 +67,10 @@ const char* nfem_status_string(int status);
  *                                        node rows with shared images: 2, 4 (0) or 8
  *   NFEM_KNOB_ELAS_ROWS                  elasticity and Cosserat node rows: 1
  *                                        shared-memory row images, 2 register
- *                                        accumulation by warp shuffles; 0 the
- *                                        built-in choice (elasticity: images,
- *                                        Cosserat: registers)
+ *                                        accumulation by warp shuffles, 3
+ *                                        (elasticity) registers for rows of at
+ *                                        most 32 node columns and images for
+ *                                        longer rows; 0 the built-in choice
  *   NFEM_KNOB_COARSE_TC                  trailing updates of the dense coarse
  *                                        inverse: 0 tensor cores (3xTF32) from
  *                                        512 aggregates on, 1 CUDA cores, 2

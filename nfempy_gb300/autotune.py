@@ -117,7 +117,7 @@ def darcy_candidates(dim):
 
 
 def elasticity_candidates():
-    return ([{"form": {}, "knobs": {"elas_rows": 2}}]
+    return ([{"form": {}, "knobs": {"elas_rows": 2}}, {"form": {}, "knobs": {"elas_rows": 3}}]
             + [{"form": {}, "knobs": {"elas_rows": 1, "elas_warps": w}} for w in (2, 4, 8)])
 
 

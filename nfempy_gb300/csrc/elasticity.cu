@@ -65,6 +65,10 @@ static int upload_tables(const double* S, const double* m, const double* Mf, cud
 struct ElasParams {
   int64_t n_nodes;
   int deg_max;  // largest node degree (columns / 3) of any node row
+  // rows a kernel takes by node degree: 0 every row, 1 degree <= 32 only,
+  // 2 degree > 32 only (the split form: register rows for the short edge
+  // rows, shared-memory images for the long vertex rows)
+  int deg_filter;
   int64_t n_cells;
   void* geom;  // [n_cells][12]: J^-1 (row-major, 9), lambda |det J|, mu |det J|, |det J|
   int64_t row0;  // first row of the space (dof_shift)
@@ -218,6 +222,7 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
       if (lane == 0) set_status(p.status, NFEM_ERR_UNSUPPORTED);
       continue;
     }
+    if ((p.deg_filter == 1 && deg > 32) || (p.deg_filter == 2 && deg <= 32)) continue;  // the other kernel's row
     // the group images of this node: [images][3 rows][deg][4]
     const int gstride = kElasImages == 3 ? 3 * deg * 4 : 0;
     for (int q = lane; q < kElasImages * 3 * deg; q += 32) {
@@ -363,6 +368,7 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_reg_kernel(const E
       if (lane == 0) set_status(p.status, NFEM_ERR_UNSUPPORTED);
       continue;
     }
+    if ((p.deg_filter == 1 && deg > 32) || (p.deg_filter == 2 && deg <= 32)) continue;  // the other kernel's row
     const int np = (deg + 31) >> 5;  // columns per lane
     T acc[3][9];
 #pragma unroll
@@ -640,7 +646,21 @@ extern "C" int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int6
     elas_geom_kernel<float><<<grid_for(n_cells, 256), 256, 0, stream>>>(p);
   p.deg_max = max_node_degree > 0 ? max_node_degree : kElasDegMax;
   if (p.deg_max > 255) return NFEM_ERR_UNSUPPORTED;  // node codes are bytes
-  if (knob(NFEM_KNOB_ELAS_ROWS) == 2 && p.deg_max <= 96) {
+  p.deg_filter = 0;
+  if (knob(NFEM_KNOB_ELAS_ROWS) == 3 && p.deg_max <= 96) {
+    // split: rows of at most 32 node columns in registers, longer rows in images
+    p.deg_filter = 2;
+    if (value_type == NFEM_F64)
+      rc = launch_elasticity<double, kElasWarps64>(p, stream);
+    else
+      rc = launch_elasticity<float, kElasWarps32>(p, stream);
+    if (rc) return rc;
+    p.deg_filter = 1;
+    if (value_type == NFEM_F64)
+      rc = launch_elasticity_reg<double, 4>(p, stream);
+    else
+      rc = launch_elasticity_reg<float, 8>(p, stream);
+  } else if (knob(NFEM_KNOB_ELAS_ROWS) == 2 && p.deg_max <= 96) {
     // register accumulation (opt-in: measured at 40^3 x 6 FP32 1.08 ms
     // against 0.61 ms for the shared-memory images)
     if (value_type == NFEM_F64)

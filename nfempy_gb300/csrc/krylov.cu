@@ -842,29 +842,32 @@ __global__ void __launch_bounds__(256) bgj_pad(const double* __restrict__ ac, in
 #ifndef NFEM_COARSE_DIAG_T
 #define NFEM_COARSE_DIAG_T float
 #endif
-// One 64 x 64 diagonal block inverted by 1024 threads, four entries of a
+// One 64 x 64 diagonal block inverted by 256 threads, sixteen entries of a
 // row in each thread's registers; per step the pivot row and column go
-// through double-buffered shared memory (one barrier a step).
+// through double-buffered shared memory (one barrier a step, of 8 warps:
+// the 64 barriers are the kernel's critical path, 1,024 threads made each
+// one slower).
+constexpr int kDiagThreads = 256, kDiagE = kGjB * kGjB / kDiagThreads;  // 16 entries per thread
 template <typename T>
-__global__ void __launch_bounds__(1024) bgj_inv_diag(T* __restrict__ m, int N, int k0, T* __restrict__ dblk,
-                                                     int32_t* status) {
+__global__ void __launch_bounds__(kDiagThreads) bgj_inv_diag(T* __restrict__ m, int N, int k0, T* __restrict__ dblk,
+                                                             int32_t* status) {
   using D = NFEM_COARSE_DIAG_T;
-  static_assert(kGjB == 64, "16 threads x 4 entries per row");
+  static_assert(kGjB == 64 && kDiagE == 16, "4 threads x 16 entries per row");
   __shared__ D rowb[2][kGjB], colb[2][kGjB], ipb[2];
-  const int r = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
-  D a[4];
+  const int r = threadIdx.x >> 2, c0 = (threadIdx.x & 3) * kDiagE;
+  D a[kDiagE];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) a[q] = D(m[int64_t(k0 + r) * N + k0 + c0 + q]);
+  for (int q = 0; q < kDiagE; ++q) a[q] = D(m[int64_t(k0 + r) * N + k0 + c0 + q]);
   for (int k = 0; k < kGjB; ++k) {
     const int b = k & 1;
     if (r == k) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) rowb[b][c0 + q] = a[q];
+      for (int q = 0; q < kDiagE; ++q) rowb[b][c0 + q] = a[q];
     }
-    if (k >= c0 && k < c0 + 4) {
+    if (k >= c0 && k < c0 + kDiagE) {
       D v = a[0];
 #pragma unroll
-      for (int q = 1; q < 4; ++q) v = (k - c0 == q) ? a[q] : v;
+      for (int q = 1; q < kDiagE; ++q) v = (k - c0 == q) ? a[q] : v;
       colb[b][r] = v;
       // the pivot's reciprocal, once per step (the one division of the step)
       if (r == k) ipb[b] = v != D(0) ? D(1) / v : D(0);
@@ -875,7 +878,7 @@ __global__ void __launch_bounds__(1024) bgj_inv_diag(T* __restrict__ m, int N, i
     if (threadIdx.x == 0 && !(fabs(p) > 0.0)) set_status(status, NFEM_ERR_BREAKDOWN);
     const D cr = colb[b][r];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < kDiagE; ++q) {
       const int c = c0 + q;
       const D rc = rowb[b][c] * ip;
       if (r == k && c == k) a[q] = ip;
@@ -885,7 +888,7 @@ __global__ void __launch_bounds__(1024) bgj_inv_diag(T* __restrict__ m, int N, i
     }
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) dblk[r * kGjB + c0 + q] = T(a[q]);
+  for (int q = 0; q < kDiagE; ++q) dblk[r * kGjB + c0 + q] = T(a[q]);
 }
 
 // 64 x 64 product of two shared-memory tiles, 4 x 4 outputs per thread
@@ -1153,7 +1156,7 @@ static int blocked_inverse(const double* ac, int n, T* m, T* dblk, float* inv, i
   bgj_pad<T><<<grid_for(int64_t(N) * N, 256), 256, 0, s>>>(ac, n, N, m);
   for (int kb = 0; kb < nt; ++kb) {
     const int k0 = kb * kGjB;
-    bgj_inv_diag<T><<<1, 1024, 0, s>>>(m, N, k0, dblk, status);
+    bgj_inv_diag<T><<<1, kDiagThreads, 0, s>>>(m, N, k0, dblk, status);
     bgj_panel<T><<<nt, 256, smem, s>>>(m, N, k0, dblk, 0);
     if constexpr (std::is_same<T, float>::value) {
       if (tc)

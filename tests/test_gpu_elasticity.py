@@ -33,7 +33,7 @@ def row_scaled_err(Ag, Ao):
     return (abs(d).max(axis=1).toarray().ravel() / scale).max()
 
 
-@pytest.mark.parametrize("rows", [1, 2])
+@pytest.mark.parametrize("rows", [1, 2, 3])
 @pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
 @pytest.mark.parametrize("n", [1, 2, 4])
 def test_elasticity_matches_oracle(cuda_lib, dtype, tol, n, rows):
