@@ -842,19 +842,21 @@ __global__ void __launch_bounds__(256) bgj_pad(const double* __restrict__ ac, in
 #ifndef NFEM_COARSE_DIAG_T
 #define NFEM_COARSE_DIAG_T float
 #endif
-// One 64 x 64 diagonal block inverted by 256 threads, sixteen entries of a
+// One 64 x 64 diagonal block inverted by 1,024 threads, four entries of a
 // row in each thread's registers; per step the pivot row and column go
-// through double-buffered shared memory (one barrier a step, of 8 warps:
-// the 64 barriers are the kernel's critical path, 1,024 threads made each
-// one slower).
-constexpr int kDiagThreads = 256, kDiagE = kGjB * kGjB / kDiagThreads;  // 16 entries per thread
+// through double-buffered shared memory (one barrier a step).  Measured at
+// 4,096 aggregates: 1,024 threads 40 us per block, 256 threads (sixteen
+// entries each) 47 us: the per-thread work of a step outweighs the cheaper
+// barrier.
+constexpr int kDiagThreads = 1024, kDiagE = kGjB * kGjB / kDiagThreads;  // 4 entries per thread
 template <typename T>
 __global__ void __launch_bounds__(kDiagThreads) bgj_inv_diag(T* __restrict__ m, int N, int k0, T* __restrict__ dblk,
                                                              int32_t* status) {
   using D = NFEM_COARSE_DIAG_T;
-  static_assert(kGjB == 64 && kDiagE == 16, "4 threads x 16 entries per row");
+  static_assert(kGjB == 64 && kDiagE * kDiagThreads == kGjB * kGjB && kGjB % kDiagE == 0,
+                "whole rows of kDiagE entries per thread");
   __shared__ D rowb[2][kGjB], colb[2][kGjB], ipb[2];
-  const int r = threadIdx.x >> 2, c0 = (threadIdx.x & 3) * kDiagE;
+  const int r = threadIdx.x / (kGjB / kDiagE), c0 = (threadIdx.x % (kGjB / kDiagE)) * kDiagE;
   D a[kDiagE];
 #pragma unroll
   for (int q = 0; q < kDiagE; ++q) a[q] = D(m[int64_t(k0 + r) * N + k0 + c0 + q]);
