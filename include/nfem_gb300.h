@@ -71,6 +71,7 @@ const char* nfem_status_string(int status);
  *                                        (elasticity) registers for rows of at
  *                                        most 32 node columns and images for
  *                                        longer rows; 0 the built-in choice
+ *                                        (shared-memory images)
  *   NFEM_KNOB_COARSE_TC                  trailing updates of the dense coarse
  *                                        inverse: 0 tensor cores (3xTF32) from
  *                                        512 aggregates on, 1 CUDA cores, 2

@@ -526,7 +526,9 @@ static int cosserat_launch(int value_type, int64_t n_cells, int64_t n_nodes, int
   p.n_cells = n_cells;
   p.geom = workspace;
   const int grid = grid_for(ceil_div(n_nodes, kCosWarps), 1, 8);
-  const bool reg = knob(NFEM_KNOB_ELAS_ROWS) != 1;  // register accumulation (default) or shared images (1)
+  // shared-memory images (the default: 0.346 against 0.353 ms at 24^3 x 6) or
+  // register accumulation (knob 2)
+  const bool reg = knob(NFEM_KNOB_ELAS_ROWS) == 2;
   if (value_type == NFEM_F64) {
     cos_geom_kernel<double><<<grid_for(n_cells, 256), 256, 0, stream>>>(p);
     if (reg)
