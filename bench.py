@@ -532,6 +532,7 @@ def assembly_only(args):
     wf.use_chunks = args.kernel == "chunks"
     wf.use_records = args.kernel == "records"
     wf.use_slices = args.slices
+    wf.use_streams = args.streams
     if args.slice_shift:
         wf.min_slice_shift = args.slice_shift
     if args.record_quarters:
@@ -865,6 +866,7 @@ def run_ours(args):
     wf.use_chunks = args.kernel == "chunks"
     wf.use_records = args.kernel == "records"
     wf.use_slices = args.slices
+    wf.use_streams = args.streams
     if args.slice_shift:
         wf.min_slice_shift = args.slice_shift
     if args.record_quarters:
@@ -1116,6 +1118,8 @@ def main():
     ap.add_argument("--slice-shift", type=int, default=0, help="cells per slice = 2^shift (default: the library's)")
     ap.add_argument("--record-quarters", type=int, default=0,
                     help="quarters of the blocks forming records in the overlapped assembly (default: the library's)")
+    ap.add_argument("--streams", type=int, default=0,
+                    help="K > 0: the headline's two passes over K cell slices on two streams")
     ap.add_argument("--mlp-rows", type=int, default=3_200_000,
                     help="rows (faces) of --only mlp: synthetic features through the learned network")
     ap.add_argument("--only", choices=["assembly", "elasticity", "cosserat", "batch2d", "solve", "mlp"], default=None,

@@ -319,6 +319,24 @@ int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t 
  * vertices.  The workspace is 16-byte aligned, of at least this size. */
 int nfem_darcy_workspace_bytes(int dim, int value_type, int64_t n_cells, size_t* bytes);
 
+/* One pass of the two-pass assembly over a range (workspace required):
+ * pass 1 forms the cell records of [cell_begin, cell_end); pass 2 writes the
+ * rows [row_f0, row_f1) and [row_q0, row_q1) from records already formed.
+ * The caller orders the passes, e.g. the records of consecutive cell slices
+ * on one stream and the rows of each slice on a second stream once the
+ * records of every cell its rows touch are done (each row written once, as
+ * by nfem_darcy_rt1p0_assemble). */
+int nfem_darcy_rt1p0_assemble_pass(int dim, int value_type, int64_t n_cells, int64_t n_rows,
+                                   const double* points, const float* points_split,
+                                   const int32_t* cell_vertices, int64_t p_base, const uint8_t* sign_mask,
+                                   const void* kappa, const void* source, int source_mode,
+                                   const double* qweights, int n_qp, const int32_t* row_pairs,
+                                   const uint32_t* pair_codes, const int32_t* row_ptr, void* values,
+                                   void* rhs, int accumulate, void* workspace, size_t workspace_bytes,
+                                   int pass, int64_t cell_begin, int64_t cell_end, int64_t row_f0,
+                                   int64_t row_f1, int64_t row_q0, int64_t row_q1, int32_t* dev_status,
+                                   void* stream);
+
 /* Overlapped form of nfem_darcy_rt1p0_assemble for tetrahedra (same
  * reference interface, same values up to rounding): the mesh is cut into
  * K = ceil(n_cells / 2^slice_shift) slices of consecutive cells and the

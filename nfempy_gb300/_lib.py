@@ -108,6 +108,8 @@ _SIGS = {
     "nfem_pcg_setup": ([_I, _P, _P, _P, _P], _I),
     "nfem_pcg_workspace_bytes": ([_I64, C.POINTER(_SZ)], _I),
     "nfem_solve_ir_pcg": ([_P, _P, _I, _P, _P, _P, C.c_double, C.c_double, _I, _I, _P, _SZ, _P, _P, _P], _I),
+    "nfem_darcy_rt1p0_assemble_pass": ([_I, _I, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _I, C.c_void_p, _I, _P, _P,
+                                        _P, _P, _P, _I, _P, _SZ, _I, _I64, _I64, _I64, _I64, _I64, _I64, _P, _P], _I),
     "nfem_scatter_elements": ([_I, _I64, _I, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P], _I),
     "nfem_rt1_dirichlet_rows": ([_I, _I, _I64, _P, _P, _P, _I, _I, _I, C.c_double, _P, C.POINTER(C.c_double), _I,
                                  _P, _P], _I),

@@ -423,6 +423,7 @@ class LaplaceDualWeakForm(WeakForm):
     # default: at 64^3 x 6 it measured 0.31-0.53 ms (FP64) and 0.12-0.34 ms
     # (FP32) against 0.23 / 0.10 ms for the two passes one after the other.
     use_slices = False
+    use_streams = 0  # K > 0: the two passes over K cell slices on two streams
     min_slice_shift = 17
     record_quarters = {torch.float64: 2, torch.float32: 1}
 
@@ -513,6 +514,9 @@ class LaplaceDualWeakForm(WeakForm):
                 _lib.call("nfem_darcy_workspace_bytes", sp.dim, vt, sp.n_cells, _lib.C.byref(nb))
                 self._cache[key] = torch.empty(max(int(nb.value), 16), dtype=torch.uint8, device=sp.device)
             ws = self._cache[key]
+            if self.use_streams and getattr(jacobian, "chunk_rows_host", None) is not None:
+                return self._assemble_two_streams(jacobian, residual, accumulate, stream, kt, st, mode, qw, len(wts),
+                                                  split, ws, vt)
         _lib.call("nfem_darcy_rt1p0_assemble", sp.dim, vt, sp.n_cells, jacobian.n_rows,
                   _lib.ptr(sp.points), _lib.ptr(split), _lib.ptr(sp.cells), None,
                   sp.field_offsets["p"], _lib.ptr(sp.rt_sign_mask), _lib.ptr(kt), _lib.ptr(st), mode,
@@ -521,6 +525,48 @@ class LaplaceDualWeakForm(WeakForm):
                   _lib.ptr(jacobian.chunk_rows if self.use_chunks else None), _lib.ptr(jacobian.values),
                   _lib.ptr(residual), int(accumulate), _lib.ptr(ws), 0 if ws is None else ws.numel(),
                   _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+
+    def _assemble_two_streams(self, jacobian, residual, accumulate, stream, kt, st, mode, qw, n_qp, split, ws, vt):
+        """The two passes over K cell slices on two streams: the records of
+        slice k on the launching stream, the rows of slice k on a second
+        stream once the records of every cell its rows touch are done
+        (slice k + ceil(lookahead / S)), so the cell pass of later slices
+        runs beside the row pass of earlier ones.  Same values as the
+        one-stream form (the same kernels, each row written once)."""
+        sp = self.space
+        T = sp.n_cells
+        K = int(self.use_streams)
+        S = -(-T // K)
+        S = -(-S // 32) * 32  # slice starts on the chunk table's 32-cell grid
+        K = -(-T // S)
+        cr = jacobian.chunk_rows_host
+        p_base = sp.field_offsets["p"]
+        F = [int(cr[k * S // 32]) for k in range(K)] + [p_base]
+        ahead = -(-int(jacobian.lookahead_cells) // S)
+        main = stream if stream is not None else torch.cuda.current_stream()
+        key = ("side_stream", main.device)
+        if key not in self._cache:
+            self._cache[key] = (torch.cuda.Stream(device=main.device),
+                                [torch.cuda.Event() for _ in range(K + 1)])
+        side, events = self._cache[key]
+        if len(events) < K + 1:
+            events.extend(torch.cuda.Event() for _ in range(K + 1 - len(events)))
+        common = (sp.dim, vt, T, jacobian.n_rows, _lib.ptr(sp.points), _lib.ptr(split), _lib.ptr(sp.cells), p_base,
+                  _lib.ptr(sp.rt_sign_mask), _lib.ptr(kt), _lib.ptr(st), mode, _lib.C.cast(qw, _lib.C.c_void_p), n_qp,
+                  _lib.ptr(jacobian.pairs), _lib.ptr(jacobian.pair_codes), _lib.ptr(jacobian.row_ptr),
+                  _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate), _lib.ptr(ws), ws.numel())
+        events[K].record(main)
+        side.wait_event(events[K])  # the side stream starts after the caller's earlier work
+        for k in range(K):
+            _lib.call("nfem_darcy_rt1p0_assemble_pass", *common, 1, k * S, min((k + 1) * S, T), 0, 0, 0, 0,
+                      _lib.ptr(jacobian.status), _lib.stream_ptr(main))
+            events[k].record(main)
+        for k in range(K):
+            side.wait_event(events[min(K - 1, k + ahead)])
+            _lib.call("nfem_darcy_rt1p0_assemble_pass", *common, 2, 0, 0, F[k], F[k + 1], p_base + k * S,
+                      p_base + min((k + 1) * S, T), _lib.ptr(jacobian.status), _lib.stream_ptr(side))
+        events[K].record(side)
+        main.wait_event(events[K])
 
     def _slice_plan(self, jacobian, dtype, vt):
         """(nfem_darcy_slices, ring workspace) of the overlapped assembly,

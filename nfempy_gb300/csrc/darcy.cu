@@ -1215,6 +1215,29 @@ static int launch_darcy_src(const DarcyParams& p, cudaStream_t stream) {
   return launch_darcy_rows<T, DIM, NFEM_COEF_NONE, true>(p, stream);
 }
 
+// One pass of the two-pass assembly over a range: pass 1 the cell records of
+// [cell_begin, cell_end); pass 2 the rows [row_f0, row_f1) and [row_q0,
+// row_q1) from records already formed (the caller orders the passes, e.g.
+// records and rows of consecutive cell slices on two streams).
+template <typename T, int DIM, int SRC>
+static int launch_darcy_pass(const DarcyParams& p, int pass, cudaStream_t stream) {
+  if (pass == 1) {
+    const int64_t nc = p.cell_end - p.cell_begin;
+    if (nc <= 0) return NFEM_OK;
+    const int cb = knob(NFEM_KNOB_DARCY_CELLS_BLOCK) > 0 ? knob(NFEM_KNOB_DARCY_CELLS_BLOCK) : 256;
+    if constexpr (sizeof(T) == 8 && DIM == 3) {
+      const int cbd = cb < 256 ? cb : 256;
+      darcy_records_df_kernel<SRC><<<grid_for(nc, cbd, 8 * 256 / cbd), cbd, 0, stream>>>(p);
+    } else {
+      darcy_records_kernel<T, DIM, SRC><<<grid_for(nc, cb, 8 * 256 / cb), cb, 0, stream>>>(p);
+    }
+    NFEM_CHECK_LAUNCH();
+    return NFEM_OK;
+  }
+  if (p.row_f1 <= p.row_f0 && p.row_q1 <= p.row_q0) return NFEM_OK;
+  return launch_darcy_rows<T, DIM, NFEM_COEF_NONE, true>(p, stream);
+}
+
 // The overlapped assembly: K = ceil(T / S) slices of S = 2^shift cells,
 // K + 1 launches.  Launch 0 forms the records of slices 0 and 1; launch
 // k + 1 writes the rows of slice k (its flux rows [F_k, F_k+1) and pressure
@@ -1310,7 +1333,7 @@ extern "C" int nfem_darcy_workspace_bytes(int dim, int value_type, int64_t n_cel
   return NFEM_OK;
 }
 
-extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t n_rows,
+static int darcy_build(DarcyParams& p, int dim, int value_type, int64_t n_cells, int64_t n_rows,
                                          const double* points, const float* points_split,
                                          const int32_t* cell_vertices, const int32_t* flux_dofs, int64_t p_base,
                                          const uint8_t* sign_mask, const void* kappa, const void* source,
@@ -1318,12 +1341,10 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
                                          const int32_t* row_pairs, const uint32_t* pair_codes,
                                          const int32_t* row_ptr, const int32_t* chunk_rows, void* values,
                                          void* rhs, int accumulate, void* workspace, size_t workspace_bytes,
-                                         int32_t* dev_status, void* stream_) {
+                                         int32_t* dev_status) {
   (void)flux_dofs;
-  cudaStream_t stream = (cudaStream_t)stream_;
   if ((dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_rows < 0)
     return NFEM_ERR_INVALID_ARG;
-  if (n_rows == 0) return NFEM_OK;
   if (!cell_vertices || !sign_mask || !kappa || !row_pairs || !pair_codes || !row_ptr || !values || !rhs)
     return NFEM_ERR_INVALID_ARG;
   if (value_type == NFEM_F64 && !points) return NFEM_ERR_INVALID_ARG;
@@ -1335,7 +1356,6 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
   if ((reinterpret_cast<uintptr_t>(row_pairs) & 7) || (reinterpret_cast<uintptr_t>(pair_codes) & 7))
     return NFEM_ERR_INVALID_ARG;
   if (chunk_rows && (n_cells < 1 || p_base < 0 || p_base + n_cells != n_rows)) return NFEM_ERR_INVALID_ARG;
-  DarcyParams p;
   p.n_rows = n_rows;
   p.n_cells = n_cells;
   p.p_base = p_base;
@@ -1374,9 +1394,78 @@ extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cell
       return NFEM_ERR_WORKSPACE;
     p.rec = workspace;
   }
+  return NFEM_OK;
+}
+
+extern "C" int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t n_rows,
+                                         const double* points, const float* points_split,
+                                         const int32_t* cell_vertices, const int32_t* flux_dofs, int64_t p_base,
+                                         const uint8_t* sign_mask, const void* kappa, const void* source,
+                                         int source_mode, const double* qweights, int n_qp,
+                                         const int32_t* row_pairs, const uint32_t* pair_codes,
+                                         const int32_t* row_ptr, const int32_t* chunk_rows, void* values,
+                                         void* rhs, int accumulate, void* workspace, size_t workspace_bytes,
+                                         int32_t* dev_status, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if ((dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_rows < 0)
+    return NFEM_ERR_INVALID_ARG;
+  if (n_rows == 0) return NFEM_OK;
+  DarcyParams p;
+  const int rc = darcy_build(p, dim, value_type, n_cells, n_rows, points, points_split, cell_vertices, flux_dofs,
+                             p_base, sign_mask, kappa, source, source_mode, qweights, n_qp, row_pairs, pair_codes,
+                             row_ptr, chunk_rows, values, rhs, accumulate, workspace, workspace_bytes, dev_status);
+  if (rc) return rc;
   if (value_type == NFEM_F64)
     return dim == 3 ? launch_darcy<double, 3>(p, source_mode, stream) : launch_darcy<double, 2>(p, source_mode, stream);
   return dim == 3 ? launch_darcy<float, 3>(p, source_mode, stream) : launch_darcy<float, 2>(p, source_mode, stream);
+}
+
+extern "C" int nfem_darcy_rt1p0_assemble_pass(int dim, int value_type, int64_t n_cells, int64_t n_rows,
+                                              const double* points, const float* points_split,
+                                              const int32_t* cell_vertices, int64_t p_base,
+                                              const uint8_t* sign_mask, const void* kappa, const void* source,
+                                              int source_mode, const double* qweights, int n_qp,
+                                              const int32_t* row_pairs, const uint32_t* pair_codes,
+                                              const int32_t* row_ptr, void* values, void* rhs, int accumulate,
+                                              void* workspace, size_t workspace_bytes, int pass, int64_t cell_begin,
+                                              int64_t cell_end, int64_t row_f0, int64_t row_f1, int64_t row_q0,
+                                              int64_t row_q1, int32_t* dev_status, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if ((dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_rows < 0 ||
+      (pass != 1 && pass != 2) || !workspace)
+    return NFEM_ERR_INVALID_ARG;
+  if (cell_begin < 0 || cell_end > n_cells || row_f0 < 0 || row_f1 > n_rows || row_q0 < 0 || row_q1 > n_rows)
+    return NFEM_ERR_INVALID_ARG;
+  if (n_rows == 0) return NFEM_OK;
+  DarcyParams p;
+  const int rc = darcy_build(p, dim, value_type, n_cells, n_rows, points, points_split, cell_vertices, nullptr,
+                             p_base, sign_mask, kappa, source, source_mode, qweights, n_qp, row_pairs, pair_codes,
+                             row_ptr, nullptr, values, rhs, accumulate, workspace, workspace_bytes, dev_status);
+  if (rc) return rc;
+  p.cell_begin = cell_begin;
+  p.cell_end = cell_end;
+  p.row_f0 = row_f0;
+  p.row_f1 = row_f1;
+  p.row_q0 = row_q0;
+  p.row_q1 = row_q1;
+  auto run = [&](auto tag) -> int {
+    using T = decltype(tag);
+    if (dim == 3) {
+      switch (source_mode) {
+        case NFEM_COEF_NONE: return launch_darcy_pass<T, 3, NFEM_COEF_NONE>(p, pass, stream);
+        case NFEM_COEF_CELL: return launch_darcy_pass<T, 3, NFEM_COEF_CELL>(p, pass, stream);
+        case NFEM_COEF_QPOINT: return launch_darcy_pass<T, 3, NFEM_COEF_QPOINT>(p, pass, stream);
+        default: return NFEM_ERR_INVALID_ARG;
+      }
+    }
+    switch (source_mode) {
+      case NFEM_COEF_NONE: return launch_darcy_pass<T, 2, NFEM_COEF_NONE>(p, pass, stream);
+      case NFEM_COEF_CELL: return launch_darcy_pass<T, 2, NFEM_COEF_CELL>(p, pass, stream);
+      case NFEM_COEF_QPOINT: return launch_darcy_pass<T, 2, NFEM_COEF_QPOINT>(p, pass, stream);
+      default: return NFEM_ERR_INVALID_ARG;
+    }
+  };
+  return value_type == NFEM_F64 ? run(double(0)) : run(float(0));
 }
 
 extern "C" int nfem_darcy_ring_bytes(int value_type, int slice_shift, size_t* bytes) {

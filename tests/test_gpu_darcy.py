@@ -23,7 +23,7 @@ def f2d(x, y, z):
 
 
 def assemble_gpu(m, kappa, rhs, dtype, use_chunks=False, use_records=None, use_slices=True, slice_shift=17,
-                 record_quarters=None):
+                 record_quarters=None, use_streams=0):
     sp = product_space(m, DARCY)
     A = nf.CSRMatrix(sp, dtype=dtype)
     res = torch.empty(A.n_rows, dtype=dtype, device="cuda")
@@ -32,6 +32,7 @@ def assemble_gpu(m, kappa, rhs, dtype, use_chunks=False, use_records=None, use_s
     wf.use_records = use_records
     wf.use_slices = use_slices
     wf.min_slice_shift = slice_shift
+    wf.use_streams = use_streams
     if record_quarters is not None:
         wf.record_quarters = record_quarters
     wf.functions = {"kappa": kappa, "rhs": rhs}
@@ -290,6 +291,25 @@ def test_darcy_sliced_equals_two_pass(cuda_lib, dtype, n, shift, quarters):
                              record_quarters=quarters)
     A2.check_status("sliced")
     assert A2.lookahead_cells < 2 ** shift
+    assert torch.equal(A1.values, A2.values)
+    assert torch.equal(r1, r2)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("n,K", [(3, 1), (6, 4), (10, 7), (12, 16)])
+def test_darcy_two_streams_equal_two_pass(cuda_lib, dtype, n, K):
+    """The two passes over K cell slices on two streams (records of slice k
+    on one stream, rows of slice k on the other once the records its rows
+    need are done) write exactly the values and residual of the two passes
+    in turn."""
+    m = mesh_gen.cube(n)
+    T = m["blocks"][-1][1].shape[0]
+    rng = np.random.default_rng(n + K)
+    kappa = np.exp(rng.normal(0.0, 2.0, T))
+    f_cell = rng.normal(0.0, 1.0, T)
+    sp, A1, r1 = assemble_gpu(m, kappa, f_cell, dtype, use_records=True, use_slices=False)
+    _, A2, r2 = assemble_gpu(m, kappa, f_cell, dtype, use_records=True, use_slices=False, use_streams=K)
+    A2.check_status("two streams")
     assert torch.equal(A1.values, A2.values)
     assert torch.equal(r1, r2)
 
