@@ -423,7 +423,13 @@ class LaplaceDualWeakForm(WeakForm):
     # default: at 64^3 x 6 it measured 0.31-0.53 ms (FP64) and 0.12-0.34 ms
     # (FP32) against 0.23 / 0.10 ms for the two passes one after the other.
     use_slices = False
-    use_streams = 0  # K > 0: the two passes over K cell slices on two streams
+    # K > 0: the two passes over K cell slices on two streams.  Off by
+    # default: at 64^3 x 6 it measured FP64 0.246 / 0.236 / 0.284 ms (K = 4,
+    # 8, 16) and FP32 0.124 / 0.143 / 0.203 ms against 0.228 / 0.102 ms in
+    # turn: each cell-pass launch fills the GPU, so the row launches queue
+    # behind it instead of running beside it, and every slice adds a fill
+    # and a drain
+    use_streams = 0
     min_slice_shift = 17
     record_quarters = {torch.float64: 2, torch.float32: 1}
 
