@@ -76,6 +76,12 @@ const char* nfem_status_string(int status);
  *                                        inverse: 0 tensor cores (3xTF32) from
  *                                        512 aggregates on, 1 CUDA cores, 2
  *                                        tensor cores from 128 on
+ *   NFEM_KNOB_DARCY_F64_RECORDS          FP64 Darcy records of tetrahedra: 0
+ *                                        exact integer arithmetic for lattice
+ *                                        cells (edges that are multiples of a
+ *                                        common power of two with quotients
+ *                                        below 2^20) and double-float for the
+ *                                        others, 1 double-float for every cell
  * nfem_knob_set returns NFEM_ERR_INVALID_ARG for an unknown key or value. */
 typedef enum {
   NFEM_KNOB_DARCY_ROWS_BLOCKS_PER_SM = 0,
@@ -83,7 +89,8 @@ typedef enum {
   NFEM_KNOB_ELAS_WARPS = 2,
   NFEM_KNOB_ELAS_ROWS = 3,
   NFEM_KNOB_COARSE_TC = 4,
-  NFEM_KNOB_COUNT = 5
+  NFEM_KNOB_DARCY_F64_RECORDS = 5,
+  NFEM_KNOB_COUNT = 6
 } nfem_knob;
 int nfem_knob_set(int key, int value);
 int nfem_knob_get(int key, int* value);

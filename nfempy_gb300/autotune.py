@@ -18,7 +18,7 @@ import torch
 
 from . import _lib
 
-KNOBS = {"darcy_rows_blocks_per_sm": 0, "darcy_cells_block": 1, "elas_warps": 2, "elas_rows": 3, "coarse_tc": 4}
+KNOBS = {"darcy_rows_blocks_per_sm": 0, "darcy_cells_block": 1, "elas_warps": 2, "elas_rows": 3, "coarse_tc": 4, "darcy_f64_records": 5}
 
 
 def cache_path():

@@ -361,6 +361,9 @@ extern "C" int nfem_knob_set(int key, int value) {
     case NFEM_KNOB_COARSE_TC:
       if (value < 0 || value > 2) return NFEM_ERR_INVALID_ARG;
       break;
+    case NFEM_KNOB_DARCY_F64_RECORDS:
+      if (value < 0 || value > 1) return NFEM_ERR_INVALID_ARG;
+      break;
     default:
       return NFEM_ERR_INVALID_ARG;
   }

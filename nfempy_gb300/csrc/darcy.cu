@@ -78,6 +78,7 @@ struct DarcyParams {
   double qw[32];
   void* rec;  // per-cell records of the two-pass path (NULL: single pass)
   const int64_t* fixed;  // FP64 tetrahedra: nfem_points_fixed64 records (NULL: FP64 edge subtraction)
+  int lattice;           // FP64 tetrahedra: exact integer records for lattice cells (lattice_record)
   // Work ranges of one launch: the cell pass covers cells [cell_begin,
   // cell_end); the row pass covers the rows [row_f0, row_f1) and then
   // [row_q0, row_q1) (flux rows and pressure rows of one cell slice, or all
@@ -482,6 +483,81 @@ __host__ __device__ constexpr int final_idx(int a, int b) {
 }
 constexpr int kFinalRp = 10;
 
+// Lattice cells.  With the fixed-point points, a cell's edge components
+// e (exact 64-bit integers) are often all multiples of a common power of
+// two 2^k with quotients n = e / 2^k below 2^11 in magnitude (every cell of
+// a mesh on a dyadic grid, such as an n^3 cube with n a power of two, or a
+// graded one whose cells span at most 2^11 steps of their own grid).  Then
+// G = n n^T, the row sums, every T120_ab (|T120| < 186 * 2^22 < 2^31) and
+// det (< 3 * 2^34) are exact in integer arithmetic, and the only rounding
+// left is the one factor V = 1 / (30 kappa |det|):
+//   U_ab = T120_ab * V * 2^(shift - k - e_kappa - e_det)
+// with kappa = m_kappa 2^e_kappa, |det| = m_det 2^e_det (m in [1, 2)) and
+// V = 1 / (30 m_kappa m_det) in double-float, turned into the 64-bit
+// fixed-point factor vq = V 2^68 (in [2^61, 2^64)).  Each record word is
+// then one 64 x 64-bit high product packed into FP64 bits (within one ulp
+// of T120_ab V).  The same quantities as the double-float path, with
+// fewer roundings and a fraction of its instructions.
+constexpr int kLatticeBits = 11;
+
+__device__ __forceinline__ bool lattice_cell(const int64_t (&e)[3][3], int& k) {
+  uint64_t m = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) m |= static_cast<uint64_t>(e[i][d] < 0 ? -e[i][d] : e[i][d]);
+  if (m == 0) return false;  // degenerate: the double-float path reports it
+  k = __ffsll(static_cast<long long>(m)) - 1;
+  return (m >> k) < (uint64_t(1) << kLatticeBits);
+}
+
+template <int SRC>
+__device__ __forceinline__ void lattice_record(const DarcyParams& p, int64_t c, const int64_t (&e)[3][3], int k,
+                                               int shift, double kap, dfloat F) {
+  int32_t n[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) n[i][d] = static_cast<int32_t>(e[i][d] >> k);
+  int32_t G[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) G[i][j] = n[i][0] * n[j][0] + n[i][1] * n[j][1] + n[i][2] * n[j][2];
+  const int64_t cr0 = int64_t(n[1][1] * n[2][2] - n[1][2] * n[2][1]);
+  const int64_t cr1 = int64_t(n[1][2] * n[2][0] - n[1][0] * n[2][2]);
+  const int64_t cr2 = int64_t(n[1][0] * n[2][1] - n[1][1] * n[2][0]);
+  const int64_t det = n[0][0] * cr0 + n[0][1] * cr1 + n[0][2] * cr2;
+  const uint64_t adet = static_cast<uint64_t>(det < 0 ? -det : det);
+  if (adet == 0) set_status(p.status, NFEM_ERR_DEGENERATE);
+  const int32_t R[3] = {G[0][0] + G[0][1] + G[0][2], G[0][1] + G[1][1] + G[1][2], G[0][2] + G[1][2] + G[2][2]};
+  const int32_t S = G[0][0] + G[1][1] + G[2][2] + R[0] + R[1] + R[2];
+  // m_det, m_kappa in [1, 2) and their binary exponents
+  const int e_det = 63 - df_clz64(adet);
+  const dfloat mdet = df_from_i64(static_cast<int64_t>(adet), e_det);
+  const uint64_t kb = static_cast<uint64_t>(__double_as_longlong(kap));
+  const int e_kap = int((kb >> 52) & 0x7ff) - 1023;
+  const dfloat mkap = df_from_double(__longlong_as_double(static_cast<long long>((kb & 0xFFFFFFFFFFFFFull) |
+                                                                                  (1023ull << 52))));
+  const uint64_t vq = df_to_u64_scaled(df_recip(df_mul_f(df_mul(mkap, mdet), 30.f)), 68);
+  const int ex = shift - k - e_kap - e_det - 68;
+  // T120 in record order, converted and stored two words at a time
+  auto t120 = [&](int a, int b) -> int64_t {
+    if (a == 0) return b == 0 ? S : S - 5 * R[b - 1];
+    return S - 5 * (R[a - 1] + R[b - 1]) + 20 * G[a - 1][b - 1];
+  };
+  double2* o = reinterpret_cast<double2*>(static_cast<double*>(p.rec) + rec_index(p, c) * 12);
+  o[0] = make_double2(df_i64_times_u64(t120(0, 0), vq, ex), df_i64_times_u64(t120(0, 1), vq, ex));
+  o[1] = make_double2(df_i64_times_u64(t120(0, 2), vq, ex), df_i64_times_u64(t120(0, 3), vq, ex));
+  o[2] = make_double2(df_i64_times_u64(t120(1, 1), vq, ex), df_i64_times_u64(t120(1, 2), vq, ex));
+  o[3] = make_double2(df_i64_times_u64(t120(1, 3), vq, ex), df_i64_times_u64(t120(2, 2), vq, ex));
+  o[4] = make_double2(df_i64_times_u64(t120(2, 3), vq, ex), df_i64_times_u64(t120(3, 3), vq, ex));
+  // r_p = -|det J| F = -(m_det F) 2^(e_det + 3 (k - shift))
+  const double rp =
+      (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double_scaled(df_neg(df_mul(mdet, F)), e_det + 3 * (k - shift));
+  o[5] = make_double2(rp, 0.0);
+}
+
 template <int SRC>
 __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t, int64_t nt) {
   const double* __restrict__ kappa = static_cast<const double*>(p.kappa);
@@ -490,29 +566,6 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
   for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
     const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
     const int vs[3] = {v.y, v.z, v.w};
-    dfloat E[3][3];  // E[k][d]: edge k, component d
-    if (p.fixed) {
-      // exact integer differences of the fixed-point records, converted by
-      // integer operations (no FP64 instruction)
-      const int shift = int(__ldg(p.fixed));
-      const longlong2* R = reinterpret_cast<const longlong2*>(p.fixed);
-      const longlong2 a0 = __ldg(R + 2 * (int64_t(v.x) + 1)), a1 = __ldg(R + 2 * (int64_t(v.x) + 1) + 1);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const longlong2 b0 = __ldg(R + 2 * (int64_t(vs[k]) + 1)), b1 = __ldg(R + 2 * (int64_t(vs[k]) + 1) + 1);
-        E[k][0] = df_from_i64(b0.x - a0.x, shift);
-        E[k][1] = df_from_i64(b0.y - a0.y, shift);
-        E[k][2] = df_from_i64(b1.x - a1.x, shift);
-      }
-    } else {  // exactly rounded FP64 differences
-      double x0[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) x0[d] = __ldg(p.points + int64_t(v.x) * 3 + d);
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) E[k][d] = df_from_double(__ldg(p.points + int64_t(vs[k]) * 3 + d) - x0[d]);
-    }
     // coefficient checks on the bit patterns
     const double kap = __ldg(kappa + c);
     if (!df_bits_positive(kap)) set_status(p.status, df_bits_finite(kap) ? NFEM_ERR_DOMAIN : NFEM_ERR_NONFINITE);
@@ -532,6 +585,39 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
         if (q < p.n_qp) f += p.qw[q] * __ldg(src + c * p.n_qp + q);
       if (!df_bits_finite(f)) set_status(p.status, NFEM_ERR_NONFINITE);
       F = df_from_double(f);
+    }
+    dfloat E[3][3];  // E[k][d]: edge k, component d
+    if (p.fixed) {
+      // exact integer differences of the fixed-point records
+      const int shift = int(__ldg(p.fixed));
+      const longlong2* Rp = reinterpret_cast<const longlong2*>(p.fixed);
+      const longlong2 a0 = __ldg(Rp + 2 * (int64_t(v.x) + 1)), a1 = __ldg(Rp + 2 * (int64_t(v.x) + 1) + 1);
+      int64_t e[3][3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const longlong2 b0 = __ldg(Rp + 2 * (int64_t(vs[k]) + 1)), b1 = __ldg(Rp + 2 * (int64_t(vs[k]) + 1) + 1);
+        e[k][0] = b0.x - a0.x;
+        e[k][1] = b0.y - a0.y;
+        e[k][2] = b1.x - a1.x;
+      }
+      int k2 = 0;
+      if (p.lattice && lattice_cell(e, k2)) {
+        lattice_record<SRC>(p, c, e, k2, shift, kap, F);
+        continue;
+      }
+      // converted by integer operations (no FP64 instruction)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) E[k][d] = df_from_i64(e[k][d], shift);
+    } else {  // exactly rounded FP64 differences
+      double x0[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) x0[d] = __ldg(p.points + int64_t(v.x) * 3 + d);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) E[k][d] = df_from_double(__ldg(p.points + int64_t(vs[k]) * 3 + d) - x0[d]);
     }
     const float one[3] = {1.f, 1.f, 1.f};
     // G = E E^T (edges as rows)
@@ -1377,6 +1463,7 @@ static int darcy_build(DarcyParams& p, int dim, int value_type, int64_t n_cells,
   for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
   p.rec = nullptr;
   p.fixed = nullptr;
+  p.lattice = knob(NFEM_KNOB_DARCY_F64_RECORDS) == 0;
   p.cell_begin = 0;
   p.cell_end = n_cells;
   p.row_f0 = 0;
@@ -1523,6 +1610,7 @@ extern "C" int nfem_darcy_rt1p0_assemble_sliced(int value_type, int64_t n_cells,
   p.points = points;
   p.split = value_type == NFEM_F32 ? static_cast<const float*>(point_records) : nullptr;
   p.fixed = value_type == NFEM_F64 ? static_cast<const int64_t*>(point_records) : nullptr;
+  p.lattice = knob(NFEM_KNOB_DARCY_F64_RECORDS) == 0;
   p.cv = cell_vertices;
   p.sign = sign_mask;
   p.kappa = kappa;

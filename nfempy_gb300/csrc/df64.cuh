@@ -19,6 +19,9 @@
 //   df_to_double    the FP64 bit pattern of hi, plus lo counted in units of
 //                   the FP64 ulp of hi, rounded: the nearest FP64 value to
 //                   hi + lo up to half an ulp.
+// Exact integer products for lattice cells: a 64-bit integer times a 64-bit
+// fixed-point factor through the high half of their 128-bit product, packed
+// into FP64 bits (df_i64_times_u64).
 // The header compiles for the device and for the host (tests check it there
 // against long double).
 #pragma once
@@ -276,6 +279,88 @@ DF_HD double df_to_double(dfloat x) {
   const int64_t step = opposite ? -static_cast<int64_t>(ak) : static_cast<int64_t>(ak);
   const uint64_t mag = (db & 0x7FFFFFFFFFFFFFFFull) + static_cast<uint64_t>(step);
   return df_double((db & 0x8000000000000000ull) | mag);
+}
+
+DF_HD uint64_t df_umulhi64(uint64_t a, uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __umul64hi(a, b);
+#else
+  return static_cast<uint64_t>((static_cast<unsigned __int128>(a) * b) >> 64);
+#endif
+}
+
+// floor(v 2^q) of a positive normalised double-float as a 64-bit integer,
+// by integer operations; needs 2^24 <= hi 2^q < 2^64 (lo's bits below
+// 2^-q are cut, and lo < 0 is subtracted).  Larger values (and inf)
+// saturate, smaller ones give 0.
+DF_HD uint64_t df_to_u64_scaled(dfloat v, int q) {
+  const uint32_t hb = df_bits(v.hi);
+  const int eh = static_cast<int>((hb >> 23) & 0xff);
+  const uint64_t mh = (hb & 0x7fffffu) | 0x800000u;  // hi = mh 2^(eh - 150)
+  const int sh = eh - 150 + q;
+  if (sh > 40) return ~0ull;
+  if (sh < 0) return 0ull;
+  uint64_t r = mh << sh;
+  const uint32_t lb = df_bits(v.lo);
+  const int el = static_cast<int>((lb >> 23) & 0xff);
+  if (el != 0) {
+    const uint64_t ml = (lb & 0x7fffffu) | 0x800000u;
+    const int sl = el - 150 + q;
+    const uint64_t lv = sl >= 0 ? (ml << sl) : (sl > -64 ? (ml >> -sl) : 0u);
+    r = (lb >> 31) ? r - lv : r + lv;
+  }
+  return r;
+}
+
+// The FP64 value of mag 2^e (mag in [2^52, 2^53)) with the given sign, from
+// the bits when the exponent is a normal one; otherwise through ldexp.
+DF_HD double df_pack_double(bool neg, uint64_t mag, int e) {
+  const int be = e + 52 + 1023;
+  if (be >= 1 && be <= 2046)
+    return df_double((neg ? 0x8000000000000000ull : 0ull) | (static_cast<uint64_t>(be) << 52) |
+                     (mag & 0xFFFFFFFFFFFFFull));
+  const double m = static_cast<double>(mag);
+#if defined(__CUDA_ARCH__)
+  return neg ? -ldexp(m, e) : ldexp(m, e);
+#else
+  return neg ? -std::ldexp(m, e) : std::ldexp(m, e);
+#endif
+}
+
+// t vq 2^e as FP64, within one ulp, for an integer t (|t| < 2^63) and a
+// fixed-point factor vq >= 2^56: the high 64 bits of the 128-bit product of
+// the normalised |t| and vq (at least 55 significant bits), rounded to 53.
+DF_HD double df_i64_times_u64(int64_t t, uint64_t vq, int e) {
+  if (t == 0 || vq == 0) return 0.0;
+  const uint64_t a = t < 0 ? static_cast<uint64_t>(-(t + 1)) + 1u : static_cast<uint64_t>(t);
+  const int lz = df_clz64(a);
+  const uint64_t hi = df_umulhi64(a << lz, vq);  // (|t| 2^lz vq) / 2^64, truncated
+  const int lz2 = df_clz64(hi);
+  const uint64_t h = hi << lz2;  // leading bit at 63
+  uint64_t m = (h >> 11) + ((h >> 10) & 1u);
+  int ex = 0;
+  if (m >> 53) {
+    m >>= 1;
+    ex = 1;
+  }
+  // |t| vq 2^e ~ h 2^(64 - lz2 - lz + e) = m 2^(75 + ex - lz2 - lz + e)
+  return df_pack_double(t < 0, m, 75 + ex - lz2 - lz + e);
+}
+
+// x 2^e as FP64 for a normalised double-float x (df_to_double, then the
+// exponent moved on the bits while it stays normal).
+DF_HD double df_to_double_scaled(dfloat x, int e) {
+  const double d = df_to_double(x);
+  const uint64_t b = df_bits64(d);
+  const int be = static_cast<int>((b >> 52) & 0x7ff);
+  if (be == 0 || be == 0x7ff) return d;
+  const int ne = be + e;
+  if (ne >= 1 && ne <= 2046) return df_double((b & 0x800FFFFFFFFFFFFFull) | (static_cast<uint64_t>(ne) << 52));
+#if defined(__CUDA_ARCH__)
+  return ldexp(d, e);
+#else
+  return std::ldexp(d, e);
+#endif
 }
 
 }  // namespace nfem

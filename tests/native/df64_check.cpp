@@ -16,6 +16,8 @@ int main() {
   std::uniform_int_distribution<int> ex(-40, 40);
   auto rnd = [&]() { return std::ldexp(u(g), ex(g)); };
   long double e_split = 0, e_pack = 0, e_add = 0, e_mul = 0, e_rec = 0, e_dot = 0, e_round = 0, e_i64 = 0;
+  long double e_q64 = 0, e_prod = 0, e_scaled = 0;
+  std::uniform_int_distribution<int> tb(1, 62), eo(-1100, 1000);
   std::uniform_int_distribution<int64_t> iq(-(int64_t(1) << 62), int64_t(1) << 62);
   std::uniform_int_distribution<int> sh(0, 120);
   for (int it = 0; it < 200000; ++it) {
@@ -48,6 +50,26 @@ int main() {
       long double want = std::ldexp((long double)qi, -shift);
       e_i64 = std::fmax(e_i64, std::fabs((val(Q) - want) / want));
     }
+    // the lattice records: V 2^68 as a 64-bit integer for V in (1/120, 1/30],
+    // and t vq 2^e as FP64 for integers t of any size and sign
+    {
+      dfloat V = nfem::df_recip(nfem::df_mul_f(nfem::df_from_double(1.0 + std::fabs(u(g)) * 3.0), 30.f));
+      V = nfem::quick_two_sum(V.hi, V.lo);
+      uint64_t vq = nfem::df_to_u64_scaled(V, 68);
+      long double want = std::ldexp(val(V), 68);
+      e_q64 = std::fmax(e_q64, std::fabs(((long double)vq - want) / want));
+      int64_t t = static_cast<int64_t>(g() >> (64 - tb(g)));
+      if (g() & 1) t = -t;
+      int e = eo(g);
+      double r = nfem::df_i64_times_u64(t, vq, e);
+      long double exact = std::ldexp((long double)t * (long double)vq, e);
+      if (t != 0 && std::fabs(exact) > 1e-300L && std::fabs(exact) < 1e300L)
+        e_prod = std::fmax(e_prod, std::fabs(((long double)r - exact) / exact));
+      double rs = nfem::df_to_double_scaled(V, e);
+      long double es = std::ldexp(val(V), e);
+      if (std::fabs(es) > 1e-300L && std::fabs(es) < 1e300L)
+        e_scaled = std::fmax(e_scaled, std::fabs(((long double)rs - es) / es));
+    }
     // packing of a normalised pair whose hi is a power of two and lo points below it
     dfloat q = nfem::quick_two_sum(std::ldexp(1.0f, ex(g)), -std::ldexp((float)std::fabs(u(g)), -30 + ex(g)));
     double qd = nfem::df_to_double(q);
@@ -55,5 +77,6 @@ int main() {
   }
   std::printf("split %.9Le\nround %.9Le\npack %.9Le\nadd %.9Le\nmul %.9Le\nrecip %.9Le\ndot %.9Le\ni64 %.9Le\n",
               e_split, e_round, e_pack, e_add, e_mul, e_rec, e_dot, e_i64);
+  std::printf("q64 %.9Le\nprod %.9Le\nscaled %.9Le\n", e_q64, e_prod, e_scaled);
   return 0;
 }

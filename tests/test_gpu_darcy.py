@@ -339,3 +339,54 @@ def test_autotune_keeps_values(cuda_lib, tmp_path, monkeypatch):
         assert autotune.apply_cached(key, wf)["config"] == best
     finally:
         autotune.reset_knobs()
+
+
+def _lattice_meshes():
+    """Meshes for the FP64 lattice records: a dyadic cube (every cell a
+    lattice cell), the same cube scaled by 3 and moved by (0.5, -2, 1.25)
+    (still dyadic), a cube with a third of its vertices moved by
+    non-dyadic amounts (lattice and double-float cells side by side) and
+    cube(6) (coordinates k/6: no lattice cell)."""
+    m16 = mesh_gen.cube(16)
+    moved = dict(m16, points=m16["points"] * 3.0 + np.array([0.5, -2.0, 1.25]))
+    m8 = mesh_gen.cube(8)
+    rng = np.random.default_rng(8)
+    pts = m8["points"].copy()
+    pick = rng.random(len(pts)) < 0.33
+    pts[pick] += rng.uniform(-0.03, 0.03, (int(pick.sum()), 3))
+    return {"cube16": m16, "moved16": moved, "mixed8": dict(m8, points=pts), "cube6": mesh_gen.cube(6)}
+
+
+@pytest.mark.parametrize("name", ["cube16", "moved16", "mixed8", "cube6"])
+@pytest.mark.parametrize("qpoint", [False, True])
+def test_darcy_f64_lattice_records(cuda_lib, name, qpoint):
+    """FP64 tetrahedra on lattice cells take exact integer records (G, det
+    and the T120 combinations in integers, one rounded factor 1/(30 kappa
+    |det|)): against the FP64 oracle within 1e-12 row-scaled, and against the
+    double-float records of every cell (knob NFEM_KNOB_DARCY_F64_RECORDS = 1)
+    within 1e-13, the double-float path's own accuracy."""
+    from nfempy_gb300 import autotune
+    m = _lattice_meshes()[name]
+    T = m["blocks"][-1][1].shape[0]
+    rng = np.random.default_rng(T)
+    kappa = np.exp(rng.normal(0.0, 2.0, T))
+    f_cell = rng.normal(0.0, 1.0, T)
+    rhs = f2d if qpoint else f_cell
+    sp, A, res = assemble_gpu(m, kappa, rhs, torch.float64, use_records=True, use_slices=False)
+    A.check_status(name)
+    autotune.set_knobs({"darcy_f64_records": 1})
+    try:
+        _, A_df, res_df = assemble_gpu(m, kappa, rhs, torch.float64, use_records=True, use_slices=False)
+    finally:
+        autotune.reset_knobs()
+    Ao, ro, *_ = darcy_oracle(m, kappa, f_callable=f2d) if qpoint else darcy_oracle(m, kappa, f_cell=f_cell)
+    Ag = A.to_scipy()
+    np.testing.assert_array_equal(Ag.indptr, Ao.indptr)
+    np.testing.assert_array_equal(Ag.indices, Ao.indices)
+    assert row_scaled_err(Ag, Ao) <= 1e-12
+    rg = res.cpu().numpy()
+    assert np.abs(rg - ro).max() <= 1e-12 * np.abs(ro).max()
+    assert row_scaled_err(A.to_scipy(), A_df.to_scipy()) <= 1e-13
+    assert ((res - res_df).abs().max() / res_df.abs().max()).item() <= 1e-13
+    if name == "cube6":  # no lattice cell: the same double-float records
+        assert torch.equal(A.values, A_df.values)
