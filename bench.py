@@ -545,9 +545,19 @@ def assembly_only(args):
     alg = algorithmic_bytes(sp.n_cells, m["points"].shape[0], A.nnz, sp.n_dof, vb)
     peak, kind = measured_peaks()
     ach = alg / (ms * 1e-3) / 1e9
-    return {"precision": args.precision, "kernel": args.kernel, "ms_per_step": ms, "value": sp.n_dof / (ms * 1e-3),
-            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "frac": ach / peak, "algorithmic_bytes": alg,
-                         "peak_source": kind}}
+    out = {"precision": args.precision, "kernel": args.kernel, "ms_per_step": ms, "value": sp.n_dof / (ms * 1e-3),
+           "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "frac": ach / peak, "algorithmic_bytes": alg,
+                        "peak_source": kind}}
+    if dtype == torch.float64 and args.kernel == "records":
+        from nfempy_gb300 import autotune
+        autotune.set_knobs({"darcy_f64_records": 1})  # double-float records for every cell
+        try:
+            out["double_float_records_ms"] = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs),
+                                                            args.steps, args.warmup)
+        finally:
+            autotune.set_knobs({"darcy_f64_records": 0})
+        A.check_status("assembly, double-float records")
+    return out
 
 
 def solve_only(args):
@@ -856,7 +866,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import nfempy_gb300 as nf
-    from nfempy_gb300 import _lib, workloads
+    from nfempy_gb300 import _lib, autotune, workloads
 
     dtype = torch.float32 if args.precision == "f32" else torch.float64
     vbytes = 4 if dtype == torch.float32 else 8
@@ -996,6 +1006,16 @@ def run_ours(args):
     ms_o = _time_assembly(lambda: wf.assemble(A_o, res_o, coefficients=coefs_o), args.steps, args.warmup)
     A_o.check_status("bench other precision")
     ms_o = max_over_ranks(ms_o, dist, "cuda")
+    # ---------------- FP64 with double-float records for every cell (the
+    # arithmetic of cells off a dyadic lattice), same mesh and buffers
+    A64, res64, coefs64 = (A, res, coefs) if args.precision == "f64" else (A_o, res_o, coefs_o)
+    autotune.set_knobs({"darcy_f64_records": 1})
+    try:
+        ms_df = _time_assembly(lambda: wf.assemble(A64, res64, coefficients=coefs64), args.steps, args.warmup)
+    finally:
+        autotune.set_knobs({"darcy_f64_records": 0})
+    A64.check_status("bench double-float records")
+    ms_df = max_over_ranks(ms_df, dist, "cuda")
     clk = clocks.stop()
     v32, v64 = (A.values, A_o.values) if other == "f64" else (A_o.values, A.values)
     r32, r64 = (res, res_o) if other == "f64" else (res_o, res)
@@ -1053,6 +1073,13 @@ def run_ours(args):
     legs["f32"]["max_rhs_diff_vs_f64"] = f32_vs_f64_rhs
     legs["f64"]["parity"] = ("FP64 values within 1e-12 of the FP64 oracle, row-scaled, at this size "
                              "(tests/test_gpu_fullsize.py)")
+    legs["f64"]["records"] = ("cell pass: exact integer records for lattice cells (every cell of this dyadic "
+                              "cube), double-float for cells off the lattice")
+    legs["f64"]["double_float_records"] = {
+        "ms_per_step": ms_df, "value": job_rate(n_dof, world, ms_df),
+        "roofline_frac": algorithmic_bytes(T, V, A.nnz, n_dof, 8) / (ms_df * 1e-3) / 1e9 / peak,
+        "what": "the same FP64 assembly with double-float records for every cell (knob "
+                "NFEM_KNOB_DARCY_F64_RECORDS = 1): the cost on meshes off a dyadic lattice"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
