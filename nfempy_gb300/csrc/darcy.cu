@@ -79,6 +79,7 @@ struct DarcyParams {
   void* rec;  // per-cell records of the two-pass path (NULL: single pass)
   const int64_t* fixed;  // FP64 tetrahedra: nfem_points_fixed64 records (NULL: FP64 edge subtraction)
   int lattice;           // FP64 tetrahedra: exact integer records for lattice cells (lattice_record)
+  int prow;              // the cell pass writes each cell's pressure row (pressure_row); the row pass skips them
   // Work ranges of one launch: the cell pass covers cells [cell_begin,
   // cell_end); the row pass covers the rows [row_f0, row_f1) and then
   // [row_q0, row_q1) (flux rows and pressure rows of one cell slice, or all
@@ -381,7 +382,46 @@ struct RecLayout {
   static constexpr int g0 = sums ? (DIM == 3 ? 4 : 3) : 0;  // first G word
 };
 
-// Record of one cell from its loaded incidence (see the layout above).
+// Pressure row p_base + c of cell c, written by the cell pass when p.prow
+// is set: its one incidence is the cell's local DoF NF, its values are the
+// orientation signs of the flux columns and 0 on the diagonal (record_row /
+// final_row for a == NF), its residual entry r_p.  Consecutive cells own
+// consecutive rows, so a warp's stores cover one contiguous stretch, and
+// the row pass then covers the flux rows only (it no longer reads every
+// record a second time for r_p).  A row other than the one incidence of
+// NLOC columns that nfem_pattern_pairs makes sets NFEM_ERR_PATTERN.
+template <typename T, int DIM>
+__device__ __forceinline__ void pressure_row(const DarcyParams& p, int64_t c, T rp) {
+  constexpr int NF = DIM + 1, NLOC = DIM + 2;
+  using C = DarcyConst<T, DIM>;
+  const int64_t r = p.p_base + c;
+  const int2 pr = __ldg(reinterpret_cast<const int2*>(p.pairs) + r);
+  const uint32_t code = __ldg(reinterpret_cast<const uint2*>(p.pair_codes) + r).x;
+  const int32_t b0 = __ldg(p.row_ptr + r), b1 = __ldg(p.row_ptr + r + 1);
+  if (pr.x != int32_t(c) * NLOC + NF || pr.y >= 0 || b1 - b0 != NLOC) {
+    set_status(p.status, NFEM_ERR_PATTERN);
+    return;
+  }
+  const uint32_t m = __ldg(p.sign + c);
+  T* v = static_cast<T*>(p.values) + b0;
+  T* rhs = static_cast<T*>(p.rhs);
+#pragma unroll
+  for (int b = 0; b < NLOC; ++b) {
+    const T val = b < NF ? (((m >> b) & 1u) ? -C::sigma(b) : C::sigma(b)) : T(0);
+    const int pos = min(int((code >> (4 * b)) & 15u), NLOC - 1);
+    if (p.accumulate)
+      v[pos] += val;
+    else
+      v[pos] = val;
+  }
+  if (p.accumulate)
+    rhs[r] += rp;
+  else
+    rhs[r] = rp;
+}
+
+// Record of cell c from its loaded incidence (see the layout above), and
+// its pressure row when p.prow is set.
 template <typename T, int DIM, int SRC>
 __device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, const Incidence<T, DIM>& x, T u) {
   using L = RecLayout<T, DIM>;
@@ -433,15 +473,17 @@ __device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, co
   w[L::scale] = scale;
   w[L::rp] = rp;
   // 16-byte stores: a record never straddles a 32-byte sector per store
+  const int64_t ri = rec_index(p, c);
   if constexpr (sizeof(T) == 4) {
-    float4* out = reinterpret_cast<float4*>(rec + c * NW);
+    float4* out = reinterpret_cast<float4*>(rec + ri * NW);
 #pragma unroll
     for (int k = 0; k < NW / 4; ++k) out[k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
   } else {
-    double2* out = reinterpret_cast<double2*>(rec + c * NW);
+    double2* out = reinterpret_cast<double2*>(rec + ri * NW);
 #pragma unroll
     for (int k = 0; k < NW / 2; ++k) out[k] = make_double2(w[2 * k], w[2 * k + 1]);
   }
+  if (p.prow) pressure_row<T, DIM>(p, c, rp);
 }
 
 // One cell per thread and iteration (two in flight per thread measured
@@ -454,7 +496,7 @@ __device__ __forceinline__ void records_cells(const DarcyParams& p, int64_t t, i
   for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
     Incidence<T, DIM> x;
     load_incidence<T, DIM, SRC>(p, int32_t(c), true, x);
-    write_record<T, DIM, SRC>(p, rec_index(p, c), x, u);
+    write_record<T, DIM, SRC>(p, c, x, u);
   }
 }
 
@@ -556,6 +598,7 @@ __device__ __forceinline__ void lattice_record(const DarcyParams& p, int64_t c, 
   const double rp =
       (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double_scaled(df_neg(df_mul(mdet, F)), e_det + 3 * (k - shift));
   o[5] = make_double2(rp, 0.0);
+  if (p.prow) pressure_row<double, 3>(p, c, rp);
 }
 
 template <int SRC>
@@ -667,6 +710,7 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
     double2* o = reinterpret_cast<double2*>(rec + rec_index(p, c) * 12);
 #pragma unroll
     for (int k = 0; k < 6; ++k) o[k] = make_double2(out[2 * k], out[2 * k + 1]);
+    if (p.prow) pressure_row<double, 3>(p, c, out[kFinalRp]);
   }
 }
 
@@ -1285,10 +1329,20 @@ static int launch_darcy_rows(const DarcyParams& p, cudaStream_t stream) {
 }
 
 // Single pass (the row kernel evaluates every incidence from the vertices)
-// or, with the record workspace, the cell pass followed by the row pass.
+// or, with the record workspace, the cell pass (records and the pressure
+// rows) followed by the row pass over the flux rows and any rows after the
+// pressure rows.
 template <typename T, int DIM, int SRC>
-static int launch_darcy_src(const DarcyParams& p, cudaStream_t stream) {
-  if (!p.rec) return launch_darcy_rows<T, DIM, SRC, false>(p, stream);
+static int launch_darcy_src(const DarcyParams& p_in, cudaStream_t stream) {
+  if (!p_in.rec) return launch_darcy_rows<T, DIM, SRC, false>(p_in, stream);
+  DarcyParams p = p_in;
+  if (p.p_base >= 0 && p.p_base + p.n_cells <= p.n_rows) {
+    p.prow = 1;
+    p.row_f0 = 0;
+    p.row_f1 = p.p_base;
+    p.row_q0 = p.p_base + p.n_cells;
+    p.row_q1 = p.n_rows;
+  }
   const int cb = knob(NFEM_KNOB_DARCY_CELLS_BLOCK) > 0 ? knob(NFEM_KNOB_DARCY_CELLS_BLOCK) : 256;
   const int cg = grid_for(p.n_cells, cb, 8 * 256 / cb);
   if constexpr (sizeof(T) == 8 && DIM == 3) {
@@ -1346,6 +1400,7 @@ static int launch_darcy_sliced(DarcyParams p, int shift, const int64_t* flux_beg
   int grid = grid_for(int64_t(1) << 40, 1, per_sm);
   grid = grid < 4 ? 4 : grid & ~3;
   const int64_t p_base = p.row_q0;
+  p.prow = 1;  // the cell blocks write the pressure rows of their cells
   for (int64_t l = 0; l <= K; ++l) {
     const int64_t k = l - 1;  // slice whose rows this launch writes
     p.cell_begin = l == 0 ? 0 : std::min((l + 1) * S, T_);
@@ -1353,8 +1408,7 @@ static int launch_darcy_sliced(DarcyParams p, int shift, const int64_t* flux_beg
     if (k >= 0) {
       p.row_f0 = flux_begin[k];
       p.row_f1 = flux_begin[k + 1];
-      p.row_q0 = p_base + k * S;
-      p.row_q1 = p_base + std::min((k + 1) * S, T_);
+      p.row_q0 = p.row_q1 = 0;
     } else {
       p.row_f0 = p.row_f1 = p.row_q0 = p.row_q1 = 0;
     }
@@ -1464,6 +1518,7 @@ static int darcy_build(DarcyParams& p, int dim, int value_type, int64_t n_cells,
   p.rec = nullptr;
   p.fixed = nullptr;
   p.lattice = knob(NFEM_KNOB_DARCY_F64_RECORDS) == 0;
+  p.prow = 0;
   p.cell_begin = 0;
   p.cell_end = n_cells;
   p.row_f0 = 0;
@@ -1611,6 +1666,7 @@ extern "C" int nfem_darcy_rt1p0_assemble_sliced(int value_type, int64_t n_cells,
   p.split = value_type == NFEM_F32 ? static_cast<const float*>(point_records) : nullptr;
   p.fixed = value_type == NFEM_F64 ? static_cast<const int64_t*>(point_records) : nullptr;
   p.lattice = knob(NFEM_KNOB_DARCY_F64_RECORDS) == 0;
+  p.prow = 0;
   p.cv = cell_vertices;
   p.sign = sign_mask;
   p.kappa = kappa;
