@@ -543,18 +543,25 @@ constexpr int kFinalRp = 10;
 constexpr int kLatticeBits = 11;
 
 __device__ __forceinline__ bool lattice_cell(const int64_t (&e)[3][3], int& k) {
-  uint64_t m = 0;
+  // trailing zeros of |x| and x agree; x ^ (x >> 63) is |x| or |x| - 1
+  uint64_t o = 0, m = 0;
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int d = 0; d < 3; ++d) m |= static_cast<uint64_t>(e[i][d] < 0 ? -e[i][d] : e[i][d]);
-  if (m == 0) return false;  // degenerate: the double-float path reports it
-  k = __ffsll(static_cast<long long>(m)) - 1;
+    for (int d = 0; d < 3; ++d) {
+      o |= static_cast<uint64_t>(e[i][d]);
+      m |= static_cast<uint64_t>(e[i][d] ^ (e[i][d] >> 63));
+    }
+  if (o == 0) return false;  // degenerate: the double-float path reports it
+  k = __ffsll(static_cast<long long>(o)) - 1;
   return (m >> k) < (uint64_t(1) << kLatticeBits);
 }
 
+// Writes the record (and pressure row) of lattice cell c and returns true,
+// or returns false without writing when a record word would leave the
+// normal FP64 range (the double-float path then takes the cell).
 template <int SRC>
-__device__ __forceinline__ void lattice_record(const DarcyParams& p, int64_t c, const int64_t (&e)[3][3], int k,
+__device__ __forceinline__ bool lattice_record(const DarcyParams& p, int64_t c, const int64_t (&e)[3][3], int k,
                                                int shift, double kap, dfloat F) {
   int32_t n[3][3];
 #pragma unroll
@@ -571,34 +578,40 @@ __device__ __forceinline__ void lattice_record(const DarcyParams& p, int64_t c, 
   const int64_t cr2 = int64_t(n[1][0] * n[2][1] - n[1][1] * n[2][0]);
   const int64_t det = n[0][0] * cr0 + n[0][1] * cr1 + n[0][2] * cr2;
   const uint64_t adet = static_cast<uint64_t>(det < 0 ? -det : det);
+  // m_det, m_kappa in [1, 2) and their binary exponents
+  const int e_det = 63 - df_clz64(adet);
+  const uint64_t kb = static_cast<uint64_t>(__double_as_longlong(kap));
+  const int e_kap = int((kb >> 52) & 0x7ff) - 1023;
+  // V = 1 / (30 m_kappa m_det) as the normalised 64-bit factor vq in [2^63, 2^64)
+  const dfloat mdet = df_from_i64(static_cast<int64_t>(adet), e_det);
+  const dfloat mkap = df_from_double(__longlong_as_double(static_cast<long long>((kb & 0xFFFFFFFFFFFFFull) |
+                                                                                  (1023ull << 52))));
+  const uint64_t vq0 = df_to_u64_scaled(df_recip(df_mul_f(df_mul(mkap, mdet), 30.f)), 68);
+  const int lzv = df_clz64(vq0);
+  const uint64_t vq = vq0 << (lzv & 63);
+  const int ex = shift - k - e_kap - e_det - 68 - lzv;
+  if (adet != 0 && (ex < -1080 || ex > 920)) return false;
   if (adet == 0) set_status(p.status, NFEM_ERR_DEGENERATE);
   const int32_t R[3] = {G[0][0] + G[0][1] + G[0][2], G[0][1] + G[1][1] + G[1][2], G[0][2] + G[1][2] + G[2][2]};
   const int32_t S = G[0][0] + G[1][1] + G[2][2] + R[0] + R[1] + R[2];
-  // m_det, m_kappa in [1, 2) and their binary exponents
-  const int e_det = 63 - df_clz64(adet);
-  const dfloat mdet = df_from_i64(static_cast<int64_t>(adet), e_det);
-  const uint64_t kb = static_cast<uint64_t>(__double_as_longlong(kap));
-  const int e_kap = int((kb >> 52) & 0x7ff) - 1023;
-  const dfloat mkap = df_from_double(__longlong_as_double(static_cast<long long>((kb & 0xFFFFFFFFFFFFFull) |
-                                                                                  (1023ull << 52))));
-  const uint64_t vq = df_to_u64_scaled(df_recip(df_mul_f(df_mul(mkap, mdet), 30.f)), 68);
-  const int ex = shift - k - e_kap - e_det - 68;
   // T120 in record order, converted and stored two words at a time
-  auto t120 = [&](int a, int b) -> int64_t {
+  auto t120 = [&](int a, int b) -> int32_t {
     if (a == 0) return b == 0 ? S : S - 5 * R[b - 1];
     return S - 5 * (R[a - 1] + R[b - 1]) + 20 * G[a - 1][b - 1];
   };
+  auto word = [&](int a, int b) { return df_i32_times_q63(t120(a, b), vq, ex); };
   double2* o = reinterpret_cast<double2*>(static_cast<double*>(p.rec) + rec_index(p, c) * 12);
-  o[0] = make_double2(df_i64_times_u64(t120(0, 0), vq, ex), df_i64_times_u64(t120(0, 1), vq, ex));
-  o[1] = make_double2(df_i64_times_u64(t120(0, 2), vq, ex), df_i64_times_u64(t120(0, 3), vq, ex));
-  o[2] = make_double2(df_i64_times_u64(t120(1, 1), vq, ex), df_i64_times_u64(t120(1, 2), vq, ex));
-  o[3] = make_double2(df_i64_times_u64(t120(1, 3), vq, ex), df_i64_times_u64(t120(2, 2), vq, ex));
-  o[4] = make_double2(df_i64_times_u64(t120(2, 3), vq, ex), df_i64_times_u64(t120(3, 3), vq, ex));
+  o[0] = make_double2(word(0, 0), word(0, 1));
+  o[1] = make_double2(word(0, 2), word(0, 3));
+  o[2] = make_double2(word(1, 1), word(1, 2));
+  o[3] = make_double2(word(1, 3), word(2, 2));
+  o[4] = make_double2(word(2, 3), word(3, 3));
   // r_p = -|det J| F = -(m_det F) 2^(e_det + 3 (k - shift))
   const double rp =
       (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double_scaled(df_neg(df_mul(mdet, F)), e_det + 3 * (k - shift));
   o[5] = make_double2(rp, 0.0);
   if (p.prow) pressure_row<double, 3>(p, c, rp);
+  return true;
 }
 
 template <int SRC>
@@ -644,10 +657,7 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
         e[k][2] = b1.x - a1.x;
       }
       int k2 = 0;
-      if (p.lattice && lattice_cell(e, k2)) {
-        lattice_record<SRC>(p, c, e, k2, shift, kap, F);
-        continue;
-      }
+      if (p.lattice && lattice_cell(e, k2) && lattice_record<SRC>(p, c, e, k2, shift, kap, F)) continue;
       // converted by integer operations (no FP64 instruction)
 #pragma unroll
       for (int k = 0; k < 3; ++k)
@@ -1019,16 +1029,17 @@ __device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t r
         const int at = a[t];
         if (direct) {
           // the first incidence stores all its entries; the second stores its
-          // own and overwrites the shared diagonal with the sum
+          // own and overwrites the shared diagonal with the sum (one add)
           T d = T(0);
 #pragma unroll
           for (int b = 0; b < NLOC; ++b) d = (b == at) ? v[b] : d;
+          const T dsum = t == 1 ? d + diag : d;
 #pragma unroll
           for (int b = 0; b < NLOC; ++b) {
             // codes index inside the row (< 16 entries); the clamp keeps a
             // corrupted code inside this warp's staging buffer
             const int idx = min(off + int((cd >> (4 * b)) & 15u), kCap);
-            st[idx] = (t == 1 && b == at) ? v[b] + diag : v[b];
+            st[idx] = (b == at) ? dsum : v[b];
           }
           if (t == 0) diag = d;
         } else {

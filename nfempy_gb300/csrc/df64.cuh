@@ -19,9 +19,9 @@
 //   df_to_double    the FP64 bit pattern of hi, plus lo counted in units of
 //                   the FP64 ulp of hi, rounded: the nearest FP64 value to
 //                   hi + lo up to half an ulp.
-// Exact integer products for lattice cells: a 64-bit integer times a 64-bit
-// fixed-point factor through the high half of their 128-bit product, packed
-// into FP64 bits (df_i64_times_u64).
+// Exact integer products for lattice cells: a 32-bit integer times a 64-bit
+// fixed-point factor through the high 64 bits of their 96-bit product,
+// packed into FP64 bits (df_i32_times_q63).
 // The header compiles for the device and for the host (tests check it there
 // against long double).
 #pragma once
@@ -281,14 +281,6 @@ DF_HD double df_to_double(dfloat x) {
   return df_double((db & 0x8000000000000000ull) | mag);
 }
 
-DF_HD uint64_t df_umulhi64(uint64_t a, uint64_t b) {
-#if defined(__CUDA_ARCH__)
-  return __umul64hi(a, b);
-#else
-  return static_cast<uint64_t>((static_cast<unsigned __int128>(a) * b) >> 64);
-#endif
-}
-
 // floor(v 2^q) of a positive normalised double-float as a 64-bit integer,
 // by integer operations; needs 2^24 <= hi 2^q < 2^64 (lo's bits below
 // 2^-q are cut, and lo < 0 is subtracted).  Larger values (and inf)
@@ -312,39 +304,38 @@ DF_HD uint64_t df_to_u64_scaled(dfloat v, int q) {
   return r;
 }
 
-// The FP64 value of mag 2^e (mag in [2^52, 2^53)) with the given sign, from
-// the bits when the exponent is a normal one; otherwise through ldexp.
-DF_HD double df_pack_double(bool neg, uint64_t mag, int e) {
-  const int be = e + 52 + 1023;
-  if (be >= 1 && be <= 2046)
-    return df_double((neg ? 0x8000000000000000ull : 0ull) | (static_cast<uint64_t>(be) << 52) |
-                     (mag & 0xFFFFFFFFFFFFFull));
-  const double m = static_cast<double>(mag);
+DF_HD int df_clz32(uint32_t x) {
 #if defined(__CUDA_ARCH__)
-  return neg ? -ldexp(m, e) : ldexp(m, e);
+  return __clz(static_cast<int>(x));
 #else
-  return neg ? -std::ldexp(m, e) : std::ldexp(m, e);
+  return x ? __builtin_clz(x) : 32;
+#endif
+}
+DF_HD uint32_t df_umulhi32(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __umulhi(a, b);
+#else
+  return static_cast<uint32_t>((static_cast<uint64_t>(a) * b) >> 32);
 #endif
 }
 
-// t vq 2^e as FP64, within one ulp, for an integer t (|t| < 2^63) and a
-// fixed-point factor vq >= 2^56: the high 64 bits of the 128-bit product of
-// the normalised |t| and vq (at least 55 significant bits), rounded to 53.
-DF_HD double df_i64_times_u64(int64_t t, uint64_t vq, int e) {
-  if (t == 0 || vq == 0) return 0.0;
-  const uint64_t a = t < 0 ? static_cast<uint64_t>(-(t + 1)) + 1u : static_cast<uint64_t>(t);
-  const int lz = df_clz64(a);
-  const uint64_t hi = df_umulhi64(a << lz, vq);  // (|t| 2^lz vq) / 2^64, truncated
-  const int lz2 = df_clz64(hi);
-  const uint64_t h = hi << lz2;  // leading bit at 63
-  uint64_t m = (h >> 11) + ((h >> 10) & 1u);
-  int ex = 0;
-  if (m >> 53) {
-    m >>= 1;
-    ex = 1;
-  }
-  // |t| vq 2^e ~ h 2^(64 - lz2 - lz + e) = m 2^(75 + ex - lz2 - lz + e)
-  return df_pack_double(t < 0, m, 75 + ex - lz2 - lz + e);
+// t vq 2^e as FP64 for a 32-bit integer t and a normalised fixed-point
+// factor vq in [2^63, 2^64), within one ulp: h = (|t| 2^lz vq) / 2^32 (a
+// 32 x 64-bit product, exact down to the cut low word) rounded to 53 bits
+// m, and the FP64 bits formed as ((biased exponent - 1) << 52) + m, where
+// the leading bit of m carries into the exponent field.  The caller keeps
+// e in [-1080, 920], so every result is a normal FP64 number.
+DF_HD double df_i32_times_q63(int32_t t, uint64_t vq, int e) {
+  const uint32_t a = t < 0 ? 0u - static_cast<uint32_t>(t) : static_cast<uint32_t>(t);
+  const int lz = df_clz32(a);
+  const uint32_t an = a << (lz & 31);
+  const uint64_t h = static_cast<uint64_t>(an) * static_cast<uint32_t>(vq >> 32) +
+                     df_umulhi32(an, static_cast<uint32_t>(vq));  // in [2^62, 2^64)
+  const int top = static_cast<int>(h >> 63);
+  const uint64_t m = (h >> (10 + top)) + ((h >> (9 + top)) & 1u);  // in [2^52, 2^53]
+  const uint64_t bexp = static_cast<uint64_t>(1023 + 94 - 1 + top + e - lz);
+  const uint64_t bits = (bexp << 52) + m;
+  return t == 0 ? 0.0 : df_double(bits | (t < 0 ? 0x8000000000000000ull : 0ull));
 }
 
 // x 2^e as FP64 for a normalised double-float x (df_to_double, then the

@@ -17,7 +17,7 @@ int main() {
   auto rnd = [&]() { return std::ldexp(u(g), ex(g)); };
   long double e_split = 0, e_pack = 0, e_add = 0, e_mul = 0, e_rec = 0, e_dot = 0, e_round = 0, e_i64 = 0;
   long double e_q64 = 0, e_prod = 0, e_scaled = 0;
-  std::uniform_int_distribution<int> tb(1, 62), eo(-1100, 1000);
+  std::uniform_int_distribution<int> tb(1, 31), eo(-1080, 920);
   std::uniform_int_distribution<int64_t> iq(-(int64_t(1) << 62), int64_t(1) << 62);
   std::uniform_int_distribution<int> sh(0, 120);
   for (int it = 0; it < 200000; ++it) {
@@ -58,13 +58,14 @@ int main() {
       uint64_t vq = nfem::df_to_u64_scaled(V, 68);
       long double want = std::ldexp(val(V), 68);
       e_q64 = std::fmax(e_q64, std::fabs(((long double)vq - want) / want));
-      int64_t t = static_cast<int64_t>(g() >> (64 - tb(g)));
+      const uint64_t vqn = vq << __builtin_clzll(vq);  // normalised to [2^63, 2^64)
+      int32_t t = static_cast<int32_t>(g() >> (64 - tb(g)));
       if (g() & 1) t = -t;
       int e = eo(g);
-      double r = nfem::df_i64_times_u64(t, vq, e);
-      long double exact = std::ldexp((long double)t * (long double)vq, e);
-      if (t != 0 && std::fabs(exact) > 1e-300L && std::fabs(exact) < 1e300L)
-        e_prod = std::fmax(e_prod, std::fabs(((long double)r - exact) / exact));
+      double r = nfem::df_i32_times_q63(t, vqn, e);
+      long double exact = std::ldexp((long double)t * (long double)vqn, e);
+      if (t == 0 && r != 0.0) e_prod = 1.0L;
+      if (t != 0) e_prod = std::fmax(e_prod, std::fabs(((long double)r - exact) / exact));
       double rs = nfem::df_to_double_scaled(V, e);
       long double es = std::ldexp(val(V), e);
       if (std::fabs(es) > 1e-300L && std::fabs(es) < 1e300L)
