@@ -390,25 +390,53 @@ struct RecLayout {
 // the row pass then covers the flux rows only (it no longer reads every
 // record a second time for r_p).  A row other than the one incidence of
 // NLOC columns that nfem_pattern_pairs makes sets NFEM_ERR_PATTERN.
+// The pattern words of a pressure row, loaded when its cell's iteration
+// starts so that their latency overlaps the cell's arithmetic.
+struct PRowIn {
+  int2 pr;
+  uint32_t code, m;
+  int32_t b0, b1;
+};
+__device__ __forceinline__ PRowIn load_prow(const DarcyParams& p, int64_t c) {
+  PRowIn in;
+  if (p.prow) {
+    const int64_t r = p.p_base + c;
+    in.pr = __ldg(reinterpret_cast<const int2*>(p.pairs) + r);
+    in.code = __ldg(reinterpret_cast<const uint2*>(p.pair_codes) + r).x;
+    in.b0 = __ldg(p.row_ptr + r);
+    in.b1 = __ldg(p.row_ptr + r + 1);
+    in.m = __ldg(p.sign + c);
+  } else {
+    in.pr = make_int2(-1, -1);
+    in.code = in.m = 0u;
+    in.b0 = in.b1 = 0;
+  }
+  return in;
+}
+// +-1 with the given sign, by bits
+__device__ __forceinline__ double unit_signed(bool neg, double) {
+  return __longlong_as_double(static_cast<long long>(0x3FF0000000000000ull | (static_cast<uint64_t>(neg) << 63)));
+}
+__device__ __forceinline__ float unit_signed(bool neg, float) {
+  return __uint_as_float(0x3F800000u | (static_cast<uint32_t>(neg) << 31));
+}
+
 template <typename T, int DIM>
-__device__ __forceinline__ void pressure_row(const DarcyParams& p, int64_t c, T rp) {
+__device__ __forceinline__ void pressure_row(const DarcyParams& p, int64_t c, T rp, const PRowIn& in) {
   constexpr int NF = DIM + 1, NLOC = DIM + 2;
   using C = DarcyConst<T, DIM>;
   const int64_t r = p.p_base + c;
-  const int2 pr = __ldg(reinterpret_cast<const int2*>(p.pairs) + r);
-  const uint32_t code = __ldg(reinterpret_cast<const uint2*>(p.pair_codes) + r).x;
-  const int32_t b0 = __ldg(p.row_ptr + r), b1 = __ldg(p.row_ptr + r + 1);
-  if (pr.x != int32_t(c) * NLOC + NF || pr.y >= 0 || b1 - b0 != NLOC) {
+  if (in.pr.x != int32_t(c) * NLOC + NF || in.pr.y >= 0 || in.b1 - in.b0 != NLOC) {
     set_status(p.status, NFEM_ERR_PATTERN);
     return;
   }
-  const uint32_t m = __ldg(p.sign + c);
-  T* v = static_cast<T*>(p.values) + b0;
+  T* v = static_cast<T*>(p.values) + in.b0;
   T* rhs = static_cast<T*>(p.rhs);
 #pragma unroll
   for (int b = 0; b < NLOC; ++b) {
-    const T val = b < NF ? (((m >> b) & 1u) ? -C::sigma(b) : C::sigma(b)) : T(0);
-    const int pos = min(int((code >> (4 * b)) & 15u), NLOC - 1);
+    const bool neg = b < NF && ((((in.m >> b) & 1u) != 0) != (C::sigma(b < NF ? b : 0) < T(0)));
+    const T val = b < NF ? unit_signed(neg, T(0)) : T(0);
+    const int pos = min(int((in.code >> (4 * b)) & 15u), NLOC - 1);
     if (p.accumulate)
       v[pos] += val;
     else
@@ -423,7 +451,8 @@ __device__ __forceinline__ void pressure_row(const DarcyParams& p, int64_t c, T 
 // Record of cell c from its loaded incidence (see the layout above), and
 // its pressure row when p.prow is set.
 template <typename T, int DIM, int SRC>
-__device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, const Incidence<T, DIM>& x, T u) {
+__device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, const Incidence<T, DIM>& x, T u,
+                                             const PRowIn& prow) {
   using L = RecLayout<T, DIM>;
   constexpr int NW = L::n;
   using C = DarcyConst<T, DIM>;
@@ -483,7 +512,7 @@ __device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, co
 #pragma unroll
     for (int k = 0; k < NW / 2; ++k) out[k] = make_double2(w[2 * k], w[2 * k + 1]);
   }
-  if (p.prow) pressure_row<T, DIM>(p, c, rp);
+  if (p.prow) pressure_row<T, DIM>(p, c, rp, prow);
 }
 
 // One cell per thread and iteration (two in flight per thread measured
@@ -494,9 +523,10 @@ template <typename T, int DIM, int SRC>
 __device__ __forceinline__ void records_cells(const DarcyParams& p, int64_t t, int64_t nt) {
   const T u = edge_unit<T>(p);
   for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
+    const PRowIn prow = load_prow(p, c);
     Incidence<T, DIM> x;
     load_incidence<T, DIM, SRC>(p, int32_t(c), true, x);
-    write_record<T, DIM, SRC>(p, c, x, u);
+    write_record<T, DIM, SRC>(p, c, x, u, prow);
   }
 }
 
@@ -562,7 +592,7 @@ __device__ __forceinline__ bool lattice_cell(const int64_t (&e)[3][3], int& k) {
 // normal FP64 range (the double-float path then takes the cell).
 template <int SRC>
 __device__ __forceinline__ bool lattice_record(const DarcyParams& p, int64_t c, const int64_t (&e)[3][3], int k,
-                                               int shift, double kap, dfloat F) {
+                                               int shift, double kap, dfloat F, const PRowIn& prow) {
   int32_t n[3][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
@@ -610,7 +640,7 @@ __device__ __forceinline__ bool lattice_record(const DarcyParams& p, int64_t c, 
   const double rp =
       (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double_scaled(df_neg(df_mul(mdet, F)), e_det + 3 * (k - shift));
   o[5] = make_double2(rp, 0.0);
-  if (p.prow) pressure_row<double, 3>(p, c, rp);
+  if (p.prow) pressure_row<double, 3>(p, c, rp, prow);
   return true;
 }
 
@@ -622,6 +652,7 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
   for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
     const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
     const int vs[3] = {v.y, v.z, v.w};
+    const PRowIn prow = load_prow(p, c);
     // coefficient checks on the bit patterns
     const double kap = __ldg(kappa + c);
     if (!df_bits_positive(kap)) set_status(p.status, df_bits_finite(kap) ? NFEM_ERR_DOMAIN : NFEM_ERR_NONFINITE);
@@ -657,7 +688,7 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
         e[k][2] = b1.x - a1.x;
       }
       int k2 = 0;
-      if (p.lattice && lattice_cell(e, k2) && lattice_record<SRC>(p, c, e, k2, shift, kap, F)) continue;
+      if (p.lattice && lattice_cell(e, k2) && lattice_record<SRC>(p, c, e, k2, shift, kap, F, prow)) continue;
       // converted by integer operations (no FP64 instruction)
 #pragma unroll
       for (int k = 0; k < 3; ++k)
@@ -720,12 +751,12 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
     double2* o = reinterpret_cast<double2*>(rec + rec_index(p, c) * 12);
 #pragma unroll
     for (int k = 0; k < 6; ++k) o[k] = make_double2(out[2 * k], out[2 * k + 1]);
-    if (p.prow) pressure_row<double, 3>(p, c, out[kFinalRp]);
+    if (p.prow) pressure_row<double, 3>(p, c, out[kFinalRp], prow);
   }
 }
 
 #ifndef NFEM_DF_MIN_BLOCKS
-#define NFEM_DF_MIN_BLOCKS 5
+#define NFEM_DF_MIN_BLOCKS 4
 #endif
 template <int SRC>
 __global__ void __launch_bounds__(256, NFEM_DF_MIN_BLOCKS) darcy_records_df_kernel(const DarcyParams p) {
@@ -1339,6 +1370,36 @@ static int launch_darcy_rows(const DarcyParams& p, cudaStream_t stream) {
   return NFEM_OK;
 }
 
+// The cell pass over [cell_begin, cell_end): one thread per cell and
+// iteration, the grid sized to the blocks the SMs hold at once (the
+// occupancy of the kernel as built), so a grid-stride launch runs as one
+// wave with no partly filled second one.
+template <typename K>
+static int resident_blocks(K kernel, int block) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, 0) != cudaSuccess || n < 1) n = 1;
+  return n;
+}
+
+template <typename T, int DIM, int SRC>
+static void launch_cell_pass(const DarcyParams& p, cudaStream_t stream) {
+  const int64_t nc = p.cell_end - p.cell_begin;
+  if (nc <= 0) return;
+  const int cb = knob(NFEM_KNOB_DARCY_CELLS_BLOCK) > 0 ? knob(NFEM_KNOB_DARCY_CELLS_BLOCK) : 256;
+  if constexpr (sizeof(T) == 8 && DIM == 3) {
+    const int cbd = cb < 256 ? cb : 256;  // the double-float kernel is built for blocks of at most 256
+    static int per_sm[3] = {0, 0, 0};     // blocks of 64, 128, 256 threads
+    const int slot = cbd == 256 ? 2 : (cbd == 128 ? 1 : 0);
+    if (!per_sm[slot]) per_sm[slot] = resident_blocks(darcy_records_df_kernel<SRC>, cbd);
+    darcy_records_df_kernel<SRC><<<grid_for(nc, cbd, per_sm[slot]), cbd, 0, stream>>>(p);
+  } else {
+    static int per_sm[4] = {0, 0, 0, 0};  // blocks of 64, 128, 256, 512 threads
+    const int slot = cb == 512 ? 3 : (cb == 256 ? 2 : (cb == 128 ? 1 : 0));
+    if (!per_sm[slot]) per_sm[slot] = resident_blocks(darcy_records_kernel<T, DIM, SRC>, cb);
+    darcy_records_kernel<T, DIM, SRC><<<grid_for(nc, cb, per_sm[slot]), cb, 0, stream>>>(p);
+  }
+}
+
 // Single pass (the row kernel evaluates every incidence from the vertices)
 // or, with the record workspace, the cell pass (records and the pressure
 // rows) followed by the row pass over the flux rows and any rows after the
@@ -1354,14 +1415,7 @@ static int launch_darcy_src(const DarcyParams& p_in, cudaStream_t stream) {
     p.row_q0 = p.p_base + p.n_cells;
     p.row_q1 = p.n_rows;
   }
-  const int cb = knob(NFEM_KNOB_DARCY_CELLS_BLOCK) > 0 ? knob(NFEM_KNOB_DARCY_CELLS_BLOCK) : 256;
-  const int cg = grid_for(p.n_cells, cb, 8 * 256 / cb);
-  if constexpr (sizeof(T) == 8 && DIM == 3) {
-    const int cbd = cb < 256 ? cb : 256;  // the double-float kernel is built for blocks of at most 256
-    if (p.n_cells > 0) darcy_records_df_kernel<SRC><<<grid_for(p.n_cells, cbd, 8 * 256 / cbd), cbd, 0, stream>>>(p);
-  } else {
-    if (p.n_cells > 0) darcy_records_kernel<T, DIM, SRC><<<cg, cb, 0, stream>>>(p);
-  }
+  launch_cell_pass<T, DIM, SRC>(p, stream);
   NFEM_CHECK_LAUNCH();
   return launch_darcy_rows<T, DIM, NFEM_COEF_NONE, true>(p, stream);
 }
@@ -1373,15 +1427,7 @@ static int launch_darcy_src(const DarcyParams& p_in, cudaStream_t stream) {
 template <typename T, int DIM, int SRC>
 static int launch_darcy_pass(const DarcyParams& p, int pass, cudaStream_t stream) {
   if (pass == 1) {
-    const int64_t nc = p.cell_end - p.cell_begin;
-    if (nc <= 0) return NFEM_OK;
-    const int cb = knob(NFEM_KNOB_DARCY_CELLS_BLOCK) > 0 ? knob(NFEM_KNOB_DARCY_CELLS_BLOCK) : 256;
-    if constexpr (sizeof(T) == 8 && DIM == 3) {
-      const int cbd = cb < 256 ? cb : 256;
-      darcy_records_df_kernel<SRC><<<grid_for(nc, cbd, 8 * 256 / cbd), cbd, 0, stream>>>(p);
-    } else {
-      darcy_records_kernel<T, DIM, SRC><<<grid_for(nc, cb, 8 * 256 / cb), cb, 0, stream>>>(p);
-    }
+    launch_cell_pass<T, DIM, SRC>(p, stream);
     NFEM_CHECK_LAUNCH();
     return NFEM_OK;
   }

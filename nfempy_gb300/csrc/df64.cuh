@@ -260,7 +260,9 @@ DF_HD double df_to_double(dfloat x) {
   const uint32_t hb = df_bits(x.hi);
   const int32_t he = static_cast<int32_t>((hb >> 23) & 0xff);
   if (he == 0) return 0.0;     // |hi| < 2^-126: treated as zero
-  if (he == 255) return x.hi;  // inf / nan pass through
+  if (he == 255)  // inf / nan pass through (by bits: no conversion instruction)
+    return df_double((static_cast<uint64_t>(hb & 0x80000000u) << 32) | 0x7FF0000000000000ull |
+                     (static_cast<uint64_t>(hb & 0x7fffffu) << 29));
   uint64_t db = (static_cast<uint64_t>(hb & 0x80000000u) << 32) | (static_cast<uint64_t>(he + 896) << 52) |
                 (static_cast<uint64_t>(hb & 0x7fffffu) << 29);
   const uint32_t lb = df_bits(x.lo);
