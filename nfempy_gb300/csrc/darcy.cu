@@ -432,20 +432,23 @@ __device__ __forceinline__ void pressure_row(const DarcyParams& p, int64_t c, T 
   }
   T* v = static_cast<T*>(p.values) + in.b0;
   T* rhs = static_cast<T*>(p.rhs);
+  T val[NLOC];
+  int pos[NLOC];
 #pragma unroll
   for (int b = 0; b < NLOC; ++b) {
     const bool neg = b < NF && ((((in.m >> b) & 1u) != 0) != (C::sigma(b < NF ? b : 0) < T(0)));
-    const T val = b < NF ? unit_signed(neg, T(0)) : T(0);
-    const int pos = min(int((in.code >> (4 * b)) & 15u), NLOC - 1);
-    if (p.accumulate)
-      v[pos] += val;
-    else
-      v[pos] = val;
+    val[b] = b < NF ? unit_signed(neg, T(0)) : T(0);
+    pos[b] = min(int((in.code >> (4 * b)) & 15u), NLOC - 1);
   }
-  if (p.accumulate)
+  if (p.accumulate) {
+#pragma unroll
+    for (int b = 0; b < NLOC; ++b) v[pos[b]] += val[b];
     rhs[r] += rp;
-  else
+  } else {
+#pragma unroll
+    for (int b = 0; b < NLOC; ++b) v[pos[b]] = val[b];
     rhs[r] = rp;
+  }
 }
 
 // Record of cell c from its loaded incidence (see the layout above), and
@@ -566,11 +569,22 @@ constexpr int kFinalRp = 10;
 //   U_ab = T120_ab * V * 2^(shift - k - e_kappa - e_det)
 // with kappa = m_kappa 2^e_kappa, |det| = m_det 2^e_det (m in [1, 2)) and
 // V = 1 / (30 m_kappa m_det) in double-float, turned into the 64-bit
-// fixed-point factor vq = V 2^68 (in [2^61, 2^64)).  Each record word is
-// then one 64 x 64-bit high product packed into FP64 bits (within one ulp
-// of T120_ab V).  The same quantities as the double-float path, with
-// fewer roundings and a fraction of its instructions.
+// fixed-point factor vq = V 2^68, normalised to [2^63, 2^64).  Each FP64
+// word is then one 32 x 64-bit high product packed into FP64 bits (within
+// one ulp of T120_ab V).  The same quantities as the double-float path,
+// with fewer roundings and a fraction of its instructions.
+//
+// The record of a lattice cell keeps the integers instead of the words
+// (64 bytes: two sectors of its 96-byte slot, so a third less record
+// traffic through DRAM each way):
+//   int32  [0] e, [1] kLatticeTag, [2..3] vq, [4..13] T120 in word order,
+//   double [7] r_p
+// and the row pass forms the four words of its row.  A double-float
+// record starts with U00 > 0 (finite, or +inf for a degenerate cell), whose
+// high 32 bits never equal the tag; only invalid coefficients (which set
+// the status word) could produce a NaN that does.
 constexpr int kLatticeBits = 11;
+constexpr uint32_t kLatticeTag = 0xFFFFFFFFu;
 
 __device__ __forceinline__ bool lattice_cell(const int64_t (&e)[3][3], int& k) {
   // trailing zeros of |x| and x agree; x ^ (x >> 63) is |x| or |x| - 1
@@ -629,17 +643,17 @@ __device__ __forceinline__ bool lattice_record(const DarcyParams& p, int64_t c, 
     if (a == 0) return b == 0 ? S : S - 5 * R[b - 1];
     return S - 5 * (R[a - 1] + R[b - 1]) + 20 * G[a - 1][b - 1];
   };
-  auto word = [&](int a, int b) { return df_i32_times_q63(t120(a, b), vq, ex); };
-  double2* o = reinterpret_cast<double2*>(static_cast<double*>(p.rec) + rec_index(p, c) * 12);
-  o[0] = make_double2(word(0, 0), word(0, 1));
-  o[1] = make_double2(word(0, 2), word(0, 3));
-  o[2] = make_double2(word(1, 1), word(1, 2));
-  o[3] = make_double2(word(1, 3), word(2, 2));
-  o[4] = make_double2(word(2, 3), word(3, 3));
+  // the compact lattice record (kLatticeTag): the row pass forms the FP64
+  // words it needs with df_i32_times_q63, the same packing as here
+  int4* o = reinterpret_cast<int4*>(static_cast<double*>(p.rec) + rec_index(p, c) * 12);
+  o[0] = make_int4(ex, int(kLatticeTag), int(uint32_t(vq)), int(uint32_t(vq >> 32)));
+  o[1] = make_int4(t120(0, 0), t120(0, 1), t120(0, 2), t120(0, 3));
+  o[2] = make_int4(t120(1, 1), t120(1, 2), t120(1, 3), t120(2, 2));
   // r_p = -|det J| F = -(m_det F) 2^(e_det + 3 (k - shift))
   const double rp =
       (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double_scaled(df_neg(df_mul(mdet, F)), e_det + 3 * (k - shift));
-  o[5] = make_double2(rp, 0.0);
+  const long long rpb = __double_as_longlong(rp);
+  o[3] = make_int4(t120(2, 3), t120(3, 3), int(uint32_t(rpb)), int(uint32_t(uint64_t(rpb) >> 32)));
   if (p.prow) pressure_row<double, 3>(p, c, rp, prow);
   return true;
 }
@@ -774,6 +788,8 @@ __device__ __forceinline__ void final_row(const double* __restrict__ rec, int64_
                                           double (&vals)[5], double& rhs_val) {
   using C = DarcyConst<double, 3>;
   const double* r = rec + int64_t(c) * 12;
+  const int4 head = __ldg(reinterpret_cast<const int4*>(r));
+  const bool lattice = uint32_t(head.y) == kLatticeTag;
   bool neg[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) neg[i] = (((m >> i) & 1u) != 0) != (C::sigma(i) < 0.0);  // sg_i < 0
@@ -781,20 +797,35 @@ __device__ __forceinline__ void final_row(const double* __restrict__ rec, int64_
     bool na = neg[0];
 #pragma unroll
     for (int i = 1; i < 4; ++i) na = (a == i) ? neg[i] : na;
+    // index of U_ab in the record without local-memory tables
+    int idx[4];
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-      // index of U_ab in the record without local-memory tables
-      int idx = final_idx(0, b);
+      idx[b] = final_idx(0, b);
 #pragma unroll
-      for (int i = 1; i < 4; ++i) idx = (a == i) ? final_idx(i, b) : idx;
-      vals[b] = flip_sign(__ldg(r + idx), na != neg[b]);
+      for (int i = 1; i < 4; ++i) idx[b] = (a == i) ? final_idx(i, b) : idx[b];
     }
+    double u[4];
+    if (lattice) {  // only the record's first two sectors are read
+      const uint64_t vq = (uint64_t(uint32_t(head.w)) << 32) | uint32_t(head.z);
+      const int32_t* t = reinterpret_cast<const int32_t*>(r) + 4;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) u[b] = df_i32_times_q63(__ldg(t + idx[b]), vq, head.x);
+    } else {
+#pragma unroll
+      for (int b = 0; b < 4; ++b) u[b] = __ldg(r + idx[b]);
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) vals[b] = flip_sign(u[b], na != neg[b]);
     vals[4] = na ? 1.0 : -1.0;  // -sg_a
   } else {
 #pragma unroll
     for (int b = 0; b < 4; ++b) vals[b] = neg[b] ? -1.0 : 1.0;
     vals[4] = 0.0;
-    rhs_val += __ldg(r + kFinalRp);
+    if (lattice)
+      rhs_val += __ldg(r + 7);
+    else
+      rhs_val += __ldg(r + kFinalRp);
   }
 }
 

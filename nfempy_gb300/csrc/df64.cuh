@@ -341,19 +341,18 @@ DF_HD double df_i32_times_q63(int32_t t, uint64_t vq, int e) {
 }
 
 // x 2^e as FP64 for a normalised double-float x (df_to_double, then the
-// exponent moved on the bits while it stays normal).
+// exponent moved on the bits): results beyond the FP64 range become +-inf,
+// results below the normal range +-0 (no FP64 instruction).
 DF_HD double df_to_double_scaled(dfloat x, int e) {
   const double d = df_to_double(x);
   const uint64_t b = df_bits64(d);
   const int be = static_cast<int>((b >> 52) & 0x7ff);
   if (be == 0 || be == 0x7ff) return d;
   const int ne = be + e;
-  if (ne >= 1 && ne <= 2046) return df_double((b & 0x800FFFFFFFFFFFFFull) | (static_cast<uint64_t>(ne) << 52));
-#if defined(__CUDA_ARCH__)
-  return ldexp(d, e);
-#else
-  return std::ldexp(d, e);
-#endif
+  const uint64_t sign = b & 0x8000000000000000ull;
+  if (ne > 2046) return df_double(sign | 0x7FF0000000000000ull);
+  if (ne < 1) return df_double(sign);
+  return df_double((b & 0x800FFFFFFFFFFFFFull) | (static_cast<uint64_t>(ne) << 52));
 }
 
 }  // namespace nfem
