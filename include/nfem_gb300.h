@@ -319,10 +319,12 @@ int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t 
  * NULL (and chunk_rows == NULL) a cell pass first evaluates, once per cell,
  * the metric terms all rows of the cell's element matrix are made of
  * (G = J^T J, the scale and the pressure row's residual entry: 8 FP32 words
- * per cell; FP64 adds the row sums of G: 12 words per tetrahedron, 8 per
- * triangle) and the row
- * pass reads them in place of the vertices; the values agree with the one
- * pass to rounding (the same expressions, fused alike or not).  NULL: one pass that evaluates every (row, cell) incidence from the
+ * per cell; FP64 triangles add the row sums of G, 8 words; FP64 tetrahedra
+ * keep the ten distinct entries of the flux block and the residual entry,
+ * 11 words) and the row pass reads them in place of the vertices; the
+ * values agree with the one pass to rounding (the same expressions, fused
+ * alike or not).  The cell pass also writes each cell's pressure row
+ * (row p_base + c).  NULL: one pass that evaluates every (row, cell) incidence from the
  * vertices.  The workspace is 16-byte aligned, of at least this size. */
 int nfem_darcy_workspace_bytes(int dim, int value_type, int64_t n_cells, size_t* bytes);
 

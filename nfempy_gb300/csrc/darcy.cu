@@ -80,6 +80,7 @@ struct DarcyParams {
   const int64_t* fixed;  // FP64 tetrahedra: nfem_points_fixed64 records (NULL: FP64 edge subtraction)
   int lattice;           // FP64 tetrahedra: exact integer records for lattice cells (lattice_record)
   int prow;              // the cell pass writes each cell's pressure row (pressure_row); the row pass skips them
+  int64_t rp_off;        // FP64 tetrahedra: r_p of record slot s at ((double*)rec)[rp_off + s]
   // Work ranges of one launch: the cell pass covers cells [cell_begin,
   // cell_end); the row pass covers the rows [row_f0, row_f1) and then
   // [row_q0, row_q1) (flux rows and pressure rows of one cell slice, or all
@@ -542,8 +543,12 @@ __global__ void __launch_bounds__(512) darcy_records_kernel(const DarcyParams p)
 // FP64 records of tetrahedra hold the finished flux block, evaluated once
 // per cell in double-float arithmetic on the FP32 pipes (df64.cuh) and
 // packed into FP64 words by integer operations; only the nine edge
-// subtractions run on the FP64 units.  Layout (12 doubles, 96 bytes):
-//   [U00, U01, U02, U03, U11, U12, U13, U22, U23, U33, r_p, 0]
+// subtractions run on the FP64 units.  Layout: 10 doubles (80 bytes) per
+// record slot,
+//   [U00, U01, U02, U03, U11, U12, U13, U22, U23, U33],
+// and the pressure row's r_p in a region of its own after all slots
+// (p.rp_off doubles from the start), which the row pass reads only when
+// the cell pass has not written the pressure rows itself.
 // U_ab = T120_ab / (30 kappa |det J|) without the orientation signs, with
 //   T120_ab = (tr G + sum G) - 5 (R_a + R_b) + 20 G_ab,
 // R_0 = 0, G_0b = 0 and R_a, G_ab (a, b >= 1) the row sums and entries of
@@ -556,7 +561,7 @@ __global__ void __launch_bounds__(512) darcy_records_kernel(const DarcyParams p)
 __host__ __device__ constexpr int final_idx(int a, int b) {
   return (a < b ? a : b) * 4 - (a < b ? a : b) * ((a < b ? a : b) - 1) / 2 + (a < b ? b - a : a - b);
 }
-constexpr int kFinalRp = 10;
+constexpr int kFinalWords = 10;
 
 // Lattice cells.  With the fixed-point points, a cell's edge components
 // e (exact 64-bit integers) are often all multiples of a common power of
@@ -572,19 +577,11 @@ constexpr int kFinalRp = 10;
 // fixed-point factor vq = V 2^68, normalised to [2^63, 2^64).  Each FP64
 // word is then one 32 x 64-bit high product packed into FP64 bits (within
 // one ulp of T120_ab V).  The same quantities as the double-float path,
-// with fewer roundings and a fraction of its instructions.
-//
-// The record of a lattice cell keeps the integers instead of the words
-// (64 bytes: two sectors of its 96-byte slot, so a third less record
-// traffic through DRAM each way):
-//   int32  [0] e, [1] kLatticeTag, [2..3] vq, [4..13] T120 in word order,
-//   double [7] r_p
-// and the row pass forms the four words of its row.  A double-float
-// record starts with U00 > 0 (finite, or +inf for a degenerate cell), whose
-// high 32 bits never equal the tag; only invalid coefficients (which set
-// the status word) could produce a NaN that does.
+// with fewer roundings and a fraction of its instructions.  (Keeping the
+// integers in the record and forming the words in the row pass instead
+// measured slower: the row pass needs 16 words per cell against 10 here,
+// and it is the pass bound by memory latency and issue together.)
 constexpr int kLatticeBits = 11;
-constexpr uint32_t kLatticeTag = 0xFFFFFFFFu;
 
 __device__ __forceinline__ bool lattice_cell(const int64_t (&e)[3][3], int& k) {
   // trailing zeros of |x| and x agree; x ^ (x >> 63) is |x| or |x| - 1
@@ -643,18 +640,21 @@ __device__ __forceinline__ bool lattice_record(const DarcyParams& p, int64_t c, 
     if (a == 0) return b == 0 ? S : S - 5 * R[b - 1];
     return S - 5 * (R[a - 1] + R[b - 1]) + 20 * G[a - 1][b - 1];
   };
-  // the compact lattice record (kLatticeTag): the row pass forms the FP64
-  // words it needs with df_i32_times_q63, the same packing as here
-  int4* o = reinterpret_cast<int4*>(static_cast<double*>(p.rec) + rec_index(p, c) * 12);
-  o[0] = make_int4(ex, int(kLatticeTag), int(uint32_t(vq)), int(uint32_t(vq >> 32)));
-  o[1] = make_int4(t120(0, 0), t120(0, 1), t120(0, 2), t120(0, 3));
-  o[2] = make_int4(t120(1, 1), t120(1, 2), t120(1, 3), t120(2, 2));
+  auto word = [&](int a, int b) { return df_i32_times_q63(t120(a, b), vq, ex); };
+  const int64_t slot = rec_index(p, c);
+  double2* o = reinterpret_cast<double2*>(static_cast<double*>(p.rec) + slot * kFinalWords);
+  o[0] = make_double2(word(0, 0), word(0, 1));
+  o[1] = make_double2(word(0, 2), word(0, 3));
+  o[2] = make_double2(word(1, 1), word(1, 2));
+  o[3] = make_double2(word(1, 3), word(2, 2));
+  o[4] = make_double2(word(2, 3), word(3, 3));
   // r_p = -|det J| F = -(m_det F) 2^(e_det + 3 (k - shift))
   const double rp =
       (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double_scaled(df_neg(df_mul(mdet, F)), e_det + 3 * (k - shift));
-  const long long rpb = __double_as_longlong(rp);
-  o[3] = make_int4(t120(2, 3), t120(3, 3), int(uint32_t(rpb)), int(uint32_t(uint64_t(rpb) >> 32)));
-  if (p.prow) pressure_row<double, 3>(p, c, rp, prow);
+  if (p.prow)
+    pressure_row<double, 3>(p, c, rp, prow);
+  else
+    static_cast<double*>(p.rec)[p.rp_off + slot] = rp;
   return true;
 }
 
@@ -749,7 +749,7 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
     dfloat R5[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) R5[i] = df_mul_f(R[i], 5.f);
-    double out[12];
+    double out[kFinalWords];
     out[0] = df_to_double(df_mul(W, S));
 #pragma unroll
     for (int b = 1; b < 4; ++b) out[b] = df_to_double(df_mul(W, df_sub(S, R5[b - 1])));
@@ -760,12 +760,15 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
         const dfloat t = df_add(df_sub(S, df_add(R5[a - 1], R5[b - 1])), df_mul_f(G[a - 1][b - 1], 20.f));
         out[final_idx(a, b)] = df_to_double(df_mul(W, t));
       }
-    out[kFinalRp] = (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double(df_neg(df_mul(det, F)));
-    out[11] = 0.0;
-    double2* o = reinterpret_cast<double2*>(rec + rec_index(p, c) * 12);
+    const double rp = (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double(df_neg(df_mul(det, F)));
+    const int64_t slot = rec_index(p, c);
+    double2* o = reinterpret_cast<double2*>(rec + slot * kFinalWords);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) o[k] = make_double2(out[2 * k], out[2 * k + 1]);
-    if (p.prow) pressure_row<double, 3>(p, c, out[kFinalRp], prow);
+    for (int k = 0; k < kFinalWords / 2; ++k) o[k] = make_double2(out[2 * k], out[2 * k + 1]);
+    if (p.prow)
+      pressure_row<double, 3>(p, c, rp, prow);
+    else
+      rec[p.rp_off + slot] = rp;
   }
 }
 
@@ -782,14 +785,14 @@ __device__ __forceinline__ double flip_sign(double x, bool neg) {
   return __longlong_as_double(__double_as_longlong(x) ^ (static_cast<long long>(neg) << 63));
 }
 
-// Row a of cell c from a finished FP64 record: the four U_ab with the
-// orientation signs, the divergence column, and the pressure row's r_p.
-__device__ __forceinline__ void final_row(const double* __restrict__ rec, int64_t c, uint32_t m, int a,
-                                          double (&vals)[5], double& rhs_val) {
+// Row a of the cell in record slot `slot` from its finished FP64 record:
+// the four U_ab with the orientation signs, the divergence column, and the
+// pressure row's r_p.
+__device__ __forceinline__ void final_row(const DarcyParams& p, int64_t slot, uint32_t m, int a, double (&vals)[5],
+                                          double& rhs_val) {
   using C = DarcyConst<double, 3>;
-  const double* r = rec + int64_t(c) * 12;
-  const int4 head = __ldg(reinterpret_cast<const int4*>(r));
-  const bool lattice = uint32_t(head.y) == kLatticeTag;
+  const double* rec = static_cast<const double*>(p.rec);
+  const double* r = rec + slot * kFinalWords;
   bool neg[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) neg[i] = (((m >> i) & 1u) != 0) != (C::sigma(i) < 0.0);  // sg_i < 0
@@ -797,35 +800,20 @@ __device__ __forceinline__ void final_row(const double* __restrict__ rec, int64_
     bool na = neg[0];
 #pragma unroll
     for (int i = 1; i < 4; ++i) na = (a == i) ? neg[i] : na;
-    // index of U_ab in the record without local-memory tables
-    int idx[4];
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-      idx[b] = final_idx(0, b);
+      // index of U_ab in the record without local-memory tables
+      int idx = final_idx(0, b);
 #pragma unroll
-      for (int i = 1; i < 4; ++i) idx[b] = (a == i) ? final_idx(i, b) : idx[b];
+      for (int i = 1; i < 4; ++i) idx = (a == i) ? final_idx(i, b) : idx;
+      vals[b] = flip_sign(__ldg(r + idx), na != neg[b]);
     }
-    double u[4];
-    if (lattice) {  // only the record's first two sectors are read
-      const uint64_t vq = (uint64_t(uint32_t(head.w)) << 32) | uint32_t(head.z);
-      const int32_t* t = reinterpret_cast<const int32_t*>(r) + 4;
-#pragma unroll
-      for (int b = 0; b < 4; ++b) u[b] = df_i32_times_q63(__ldg(t + idx[b]), vq, head.x);
-    } else {
-#pragma unroll
-      for (int b = 0; b < 4; ++b) u[b] = __ldg(r + idx[b]);
-    }
-#pragma unroll
-    for (int b = 0; b < 4; ++b) vals[b] = flip_sign(u[b], na != neg[b]);
     vals[4] = na ? 1.0 : -1.0;  // -sg_a
   } else {
 #pragma unroll
     for (int b = 0; b < 4; ++b) vals[b] = neg[b] ? -1.0 : 1.0;
     vals[4] = 0.0;
-    if (lattice)
-      rhs_val += __ldg(r + 7);
-    else
-      rhs_val += __ldg(r + kFinalRp);
+    rhs_val += __ldg(rec + p.rp_off + slot);
   }
 }
 
@@ -1077,7 +1065,7 @@ __device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t r
       if (on[t]) {
         T v[NLOC];
         if constexpr (REC && sizeof(T) == 8 && DIM == 3) {
-          final_row(static_cast<const double*>(p.rec), rec_index(p, c[t]), __ldg(p.sign + c[t]), a[t], v, rhs_val);
+          final_row(p, rec_index(p, c[t]), __ldg(p.sign + c[t]), a[t], v, rhs_val);
         } else if constexpr (REC) {
           T w[RecLayout<T, DIM>::n];
           load_record<T, DIM>(static_cast<const T*>(p.rec), int32_t(rec_index(p, c[t])), a[t] < DIM + 1, w);
@@ -1556,8 +1544,8 @@ using namespace nfem;
 extern "C" int nfem_darcy_workspace_bytes(int dim, int value_type, int64_t n_cells, size_t* bytes) {
   if (!bytes || (dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_cells < 0)
     return NFEM_ERR_INVALID_ARG;
-  // FP32: 8 words per cell; FP64: 12 (tetrahedra) or 8 (triangles)
-  *bytes = value_type == NFEM_F64 ? size_t(n_cells) * (dim == 3 ? 12 : 8) * 8 : size_t(n_cells) * 8 * 4;
+  // FP32: 8 words per cell; FP64: 10 + 1 (tetrahedra: the words, then r_p) or 8 (triangles)
+  *bytes = value_type == NFEM_F64 ? size_t(n_cells) * (dim == 3 ? 11 : 8) * 8 : size_t(n_cells) * 8 * 4;
   return NFEM_OK;
 }
 
@@ -1604,6 +1592,7 @@ static int darcy_build(DarcyParams& p, int dim, int value_type, int64_t n_cells,
   p.n_qp = source_mode == NFEM_COEF_QPOINT ? n_qp : 0;
   for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
   p.rec = nullptr;
+  p.rp_off = 0;
   p.fixed = nullptr;
   p.lattice = knob(NFEM_KNOB_DARCY_F64_RECORDS) == 0;
   p.prow = 0;
@@ -1623,6 +1612,7 @@ static int darcy_build(DarcyParams& p, int dim, int value_type, int64_t n_cells,
     if (workspace_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 15) || n_cells < 0)
       return NFEM_ERR_WORKSPACE;
     p.rec = workspace;
+    p.rp_off = kFinalWords * n_cells;
   }
   return NFEM_OK;
 }
@@ -1701,9 +1691,9 @@ extern "C" int nfem_darcy_rt1p0_assemble_pass(int dim, int value_type, int64_t n
 extern "C" int nfem_darcy_ring_bytes(int value_type, int slice_shift, size_t* bytes) {
   if (!bytes || (value_type != NFEM_F64 && value_type != NFEM_F32) || slice_shift < 5 || slice_shift > 30)
     return NFEM_ERR_INVALID_ARG;
-  // three slices of records: 12 doubles (FP64) or 8 floats (FP32) per tetrahedron
+  // three slices of records: 10 + 1 doubles (FP64) or 8 floats (FP32) per tetrahedron
   *bytes = size_t(3) << slice_shift;
-  *bytes *= value_type == NFEM_F64 ? 12 * sizeof(double) : 8 * sizeof(float);
+  *bytes *= value_type == NFEM_F64 ? 11 * sizeof(double) : 8 * sizeof(float);
   return NFEM_OK;
 }
 
@@ -1769,6 +1759,7 @@ extern "C" int nfem_darcy_rt1p0_assemble_sliced(int value_type, int64_t n_cells,
   p.n_qp = source_mode == NFEM_COEF_QPOINT ? n_qp : 0;
   for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
   p.rec = ring;
+  p.rp_off = int64_t(kFinalWords) * (int64_t(3) << shift);
   p.ring_shift = shift;
   p.row_q0 = p_base;  // the launch loop takes p_base from here
   if (value_type == NFEM_F64) {
