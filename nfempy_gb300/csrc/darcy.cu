@@ -663,8 +663,13 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
   const double* __restrict__ kappa = static_cast<const double*>(p.kappa);
   const double* __restrict__ src = static_cast<const double*>(p.source);
   double* __restrict__ rec = static_cast<double*>(p.rec);
+  // the next cell's vertex ids are loaded one iteration ahead, so the point
+  // gathers that depend on them start without waiting for that load
+  const int4* __restrict__ cv4 = reinterpret_cast<const int4*>(p.cv);
+  int4 v_next = p.cell_begin + t < p.cell_end ? __ldg(cv4 + p.cell_begin + t) : make_int4(0, 0, 0, 0);
   for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
-    const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+    const int4 v = v_next;
+    if (c + nt < p.cell_end) v_next = __ldg(cv4 + c + nt);
     const int vs[3] = {v.y, v.z, v.w};
     const PRowIn prow = load_prow(p, c);
     // coefficient checks on the bit patterns
@@ -942,6 +947,11 @@ struct RowHead {
   uint2 cd;
 };
 
+// Fire-and-forget fetch of the line holding ptr into L2 (no register result).
+__device__ __forceinline__ void prefetch_l2(const void* ptr) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+}
+
 __device__ __forceinline__ RowHead load_head(const DarcyParams& p, int64_t r, int64_t end) {
   RowHead h;
   if (r < end) {
@@ -1095,6 +1105,30 @@ __device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t r
         } else {
 #pragma unroll
           for (int b = 0; b < NLOC; ++b) st[min(off + int((cd >> (4 * b)) & 15u), kCap)] += v[b];
+        }
+      }
+    }
+    if constexpr (REC && sizeof(T) == 8 && DIM == 3) {
+      // The next chunk's head has arrived by now: start its record words
+      // (the four of each incidence's row) and signs towards L2 while this
+      // chunk is stored, so its loads find them there.
+      const int occn[2] = {head.pr.x, head.pr.y};
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        if (occn[t] >= 0) {
+          const int32_t cn = occn[t] / NLOC;
+          const int an = occn[t] - cn * NLOC;
+          prefetch_l2(p.sign + cn);
+          if (an < 4) {
+            const double* rn = static_cast<const double*>(p.rec) + rec_index(p, cn) * kFinalWords;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+              int idx = final_idx(0, b);
+#pragma unroll
+              for (int i = 1; i < 4; ++i) idx = (an == i) ? final_idx(i, b) : idx;
+              prefetch_l2(rn + idx);
+            }
+          }
         }
       }
     }
