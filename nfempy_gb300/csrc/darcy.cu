@@ -947,11 +947,6 @@ struct RowHead {
   uint2 cd;
 };
 
-// Fire-and-forget fetch of the line holding ptr into L2 (no register result).
-__device__ __forceinline__ void prefetch_l2(const void* ptr) {
-  asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
-}
-
 __device__ __forceinline__ RowHead load_head(const DarcyParams& p, int64_t r, int64_t end) {
   RowHead h;
   if (r < end) {
@@ -1105,30 +1100,6 @@ __device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t r
         } else {
 #pragma unroll
           for (int b = 0; b < NLOC; ++b) st[min(off + int((cd >> (4 * b)) & 15u), kCap)] += v[b];
-        }
-      }
-    }
-    if constexpr (REC && sizeof(T) == 8 && DIM == 3) {
-      // The next chunk's head has arrived by now: start its record words
-      // (the four of each incidence's row) and signs towards L2 while this
-      // chunk is stored, so its loads find them there.
-      const int occn[2] = {head.pr.x, head.pr.y};
-#pragma unroll
-      for (int t = 0; t < 2; ++t) {
-        if (occn[t] >= 0) {
-          const int32_t cn = occn[t] / NLOC;
-          const int an = occn[t] - cn * NLOC;
-          prefetch_l2(p.sign + cn);
-          if (an < 4) {
-            const double* rn = static_cast<const double*>(p.rec) + rec_index(p, cn) * kFinalWords;
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-              int idx = final_idx(0, b);
-#pragma unroll
-              for (int i = 1; i < 4; ++i) idx = (an == i) ? final_idx(i, b) : idx;
-              prefetch_l2(rn + idx);
-            }
-          }
         }
       }
     }
