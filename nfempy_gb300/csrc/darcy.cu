@@ -658,11 +658,120 @@ __device__ __forceinline__ bool lattice_record(const DarcyParams& p, int64_t c, 
   return true;
 }
 
+// Record (and pressure row) of cell c, whose vertex ids v were loaded.
 template <int SRC>
-__device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t, int64_t nt) {
+__device__ __forceinline__ void record_df_cell(const DarcyParams& p, int64_t c, const int4 v) {
   const double* __restrict__ kappa = static_cast<const double*>(p.kappa);
   const double* __restrict__ src = static_cast<const double*>(p.source);
   double* __restrict__ rec = static_cast<double*>(p.rec);
+  const int vs[3] = {v.y, v.z, v.w};
+  const PRowIn prow = load_prow(p, c);
+  // coefficient checks on the bit patterns
+  const double kap = __ldg(kappa + c);
+  if (!df_bits_positive(kap)) set_status(p.status, df_bits_finite(kap) ? NFEM_ERR_DOMAIN : NFEM_ERR_NONFINITE);
+  dfloat F = df_make(0.f);  // the source integrated over the reference cell
+  if constexpr (SRC == NFEM_COEF_CELL) {
+    const double s = __ldg(src + c);
+    if (!df_bits_finite(s)) set_status(p.status, NFEM_ERR_NONFINITE);
+    // 1/6 as a double-float constant (its FP32 part and the remainder)
+    constexpr float kSixthHi = float(1.0 / 6.0);
+    constexpr float kSixthLo = float(1.0 / 6.0 - double(kSixthHi));
+    F = df_mul(df_from_double(s), dfloat{kSixthHi, kSixthLo});
+  }
+  if constexpr (SRC == NFEM_COEF_QPOINT) {
+    double f = 0.0;
+#pragma unroll 4
+    for (int q = 0; q < 32; ++q)
+      if (q < p.n_qp) f += p.qw[q] * __ldg(src + c * p.n_qp + q);
+    if (!df_bits_finite(f)) set_status(p.status, NFEM_ERR_NONFINITE);
+    F = df_from_double(f);
+  }
+  dfloat E[3][3];  // E[k][d]: edge k, component d
+  if (p.fixed) {
+    // exact integer differences of the fixed-point records
+    const int shift = int(__ldg(p.fixed));
+    const longlong2* Rp = reinterpret_cast<const longlong2*>(p.fixed);
+    const longlong2 a0 = __ldg(Rp + 2 * (int64_t(v.x) + 1)), a1 = __ldg(Rp + 2 * (int64_t(v.x) + 1) + 1);
+    int64_t e[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const longlong2 b0 = __ldg(Rp + 2 * (int64_t(vs[k]) + 1)), b1 = __ldg(Rp + 2 * (int64_t(vs[k]) + 1) + 1);
+      e[k][0] = b0.x - a0.x;
+      e[k][1] = b0.y - a0.y;
+      e[k][2] = b1.x - a1.x;
+    }
+    int k2 = 0;
+    if (p.lattice && lattice_cell(e, k2) && lattice_record<SRC>(p, c, e, k2, shift, kap, F, prow)) return;
+    // converted by integer operations (no FP64 instruction)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) E[k][d] = df_from_i64(e[k][d], shift);
+  } else {  // exactly rounded FP64 differences
+    double x0[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) x0[d] = __ldg(p.points + int64_t(v.x) * 3 + d);
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) E[k][d] = df_from_double(__ldg(p.points + int64_t(vs[k]) * 3 + d) - x0[d]);
+  }
+  const float one[3] = {1.f, 1.f, 1.f};
+  // G = E E^T (edges as rows)
+  dfloat G[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) G[i][j] = df_dot<3>(E[i], E[j], one);
+  // |det J| = |E0 . (E1 x E2)|
+  dfloat cr[3];
+  {
+    const float pm[2] = {1.f, -1.f};
+    const dfloat a0[2] = {E[1][1], E[1][2]}, b0[2] = {E[2][2], E[2][1]};
+    const dfloat a1[2] = {E[1][2], E[1][0]}, b1[2] = {E[2][0], E[2][2]};
+    const dfloat a2[2] = {E[1][0], E[1][1]}, b2[2] = {E[2][1], E[2][0]};
+    cr[0] = df_dot<2>(a0, b0, pm);
+    cr[1] = df_dot<2>(a1, b1, pm);
+    cr[2] = df_dot<2>(a2, b2, pm);
+  }
+  const dfloat det = df_abs(df_dot<3>(E[0], cr, one));
+  if (!(det.hi > 0.f)) set_status(p.status, NFEM_ERR_DEGENERATE);
+  // row sums R_i, S = tr G + sum G
+  dfloat R[3];
+  R[0] = df_add(df_add(G[0][0], G[0][1]), G[0][2]);
+  R[1] = df_add(df_add(G[0][1], G[1][1]), G[1][2]);
+  R[2] = df_add(df_add(G[0][2], G[1][2]), G[2][2]);
+  const dfloat trG = df_add(df_add(G[0][0], G[1][1]), G[2][2]);
+  const dfloat S = df_add(trG, df_add(df_add(R[0], R[1]), R[2]));
+  // W = 1 / (30 kappa |det J|)
+  const dfloat W = df_recip(df_mul_f(df_mul(df_from_double(kap), det), 30.f));
+  dfloat R5[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) R5[i] = df_mul_f(R[i], 5.f);
+  double out[kFinalWords];
+  out[0] = df_to_double(df_mul(W, S));
+#pragma unroll
+  for (int b = 1; b < 4; ++b) out[b] = df_to_double(df_mul(W, df_sub(S, R5[b - 1])));
+#pragma unroll
+  for (int a = 1; a < 4; ++a)
+#pragma unroll
+    for (int b = a; b < 4; ++b) {
+      const dfloat t = df_add(df_sub(S, df_add(R5[a - 1], R5[b - 1])), df_mul_f(G[a - 1][b - 1], 20.f));
+      out[final_idx(a, b)] = df_to_double(df_mul(W, t));
+    }
+  const double rp = (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double(df_neg(df_mul(det, F)));
+  const int64_t slot = rec_index(p, c);
+  double2* o = reinterpret_cast<double2*>(rec + slot * kFinalWords);
+#pragma unroll
+  for (int k = 0; k < kFinalWords / 2; ++k) o[k] = make_double2(out[2 * k], out[2 * k + 1]);
+  if (p.prow)
+    pressure_row<double, 3>(p, c, rp, prow);
+  else
+    rec[p.rp_off + slot] = rp;
+}
+
+template <int SRC>
+__device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t, int64_t nt) {
   // the next cell's vertex ids are loaded one iteration ahead, so the point
   // gathers that depend on them start without waiting for that load
   const int4* __restrict__ cv4 = reinterpret_cast<const int4*>(p.cv);
@@ -670,110 +779,7 @@ __device__ __forceinline__ void records_df_cells(const DarcyParams& p, int64_t t
   for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
     const int4 v = v_next;
     if (c + nt < p.cell_end) v_next = __ldg(cv4 + c + nt);
-    const int vs[3] = {v.y, v.z, v.w};
-    const PRowIn prow = load_prow(p, c);
-    // coefficient checks on the bit patterns
-    const double kap = __ldg(kappa + c);
-    if (!df_bits_positive(kap)) set_status(p.status, df_bits_finite(kap) ? NFEM_ERR_DOMAIN : NFEM_ERR_NONFINITE);
-    dfloat F = df_make(0.f);  // the source integrated over the reference cell
-    if constexpr (SRC == NFEM_COEF_CELL) {
-      const double s = __ldg(src + c);
-      if (!df_bits_finite(s)) set_status(p.status, NFEM_ERR_NONFINITE);
-      // 1/6 as a double-float constant (its FP32 part and the remainder)
-      constexpr float kSixthHi = float(1.0 / 6.0);
-      constexpr float kSixthLo = float(1.0 / 6.0 - double(kSixthHi));
-      F = df_mul(df_from_double(s), dfloat{kSixthHi, kSixthLo});
-    }
-    if constexpr (SRC == NFEM_COEF_QPOINT) {
-      double f = 0.0;
-#pragma unroll 4
-      for (int q = 0; q < 32; ++q)
-        if (q < p.n_qp) f += p.qw[q] * __ldg(src + c * p.n_qp + q);
-      if (!df_bits_finite(f)) set_status(p.status, NFEM_ERR_NONFINITE);
-      F = df_from_double(f);
-    }
-    dfloat E[3][3];  // E[k][d]: edge k, component d
-    if (p.fixed) {
-      // exact integer differences of the fixed-point records
-      const int shift = int(__ldg(p.fixed));
-      const longlong2* Rp = reinterpret_cast<const longlong2*>(p.fixed);
-      const longlong2 a0 = __ldg(Rp + 2 * (int64_t(v.x) + 1)), a1 = __ldg(Rp + 2 * (int64_t(v.x) + 1) + 1);
-      int64_t e[3][3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const longlong2 b0 = __ldg(Rp + 2 * (int64_t(vs[k]) + 1)), b1 = __ldg(Rp + 2 * (int64_t(vs[k]) + 1) + 1);
-        e[k][0] = b0.x - a0.x;
-        e[k][1] = b0.y - a0.y;
-        e[k][2] = b1.x - a1.x;
-      }
-      int k2 = 0;
-      if (p.lattice && lattice_cell(e, k2) && lattice_record<SRC>(p, c, e, k2, shift, kap, F, prow)) continue;
-      // converted by integer operations (no FP64 instruction)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) E[k][d] = df_from_i64(e[k][d], shift);
-    } else {  // exactly rounded FP64 differences
-      double x0[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) x0[d] = __ldg(p.points + int64_t(v.x) * 3 + d);
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) E[k][d] = df_from_double(__ldg(p.points + int64_t(vs[k]) * 3 + d) - x0[d]);
-    }
-    const float one[3] = {1.f, 1.f, 1.f};
-    // G = E E^T (edges as rows)
-    dfloat G[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = i; j < 3; ++j) G[i][j] = df_dot<3>(E[i], E[j], one);
-    // |det J| = |E0 . (E1 x E2)|
-    dfloat cr[3];
-    {
-      const float pm[2] = {1.f, -1.f};
-      const dfloat a0[2] = {E[1][1], E[1][2]}, b0[2] = {E[2][2], E[2][1]};
-      const dfloat a1[2] = {E[1][2], E[1][0]}, b1[2] = {E[2][0], E[2][2]};
-      const dfloat a2[2] = {E[1][0], E[1][1]}, b2[2] = {E[2][1], E[2][0]};
-      cr[0] = df_dot<2>(a0, b0, pm);
-      cr[1] = df_dot<2>(a1, b1, pm);
-      cr[2] = df_dot<2>(a2, b2, pm);
-    }
-    const dfloat det = df_abs(df_dot<3>(E[0], cr, one));
-    if (!(det.hi > 0.f)) set_status(p.status, NFEM_ERR_DEGENERATE);
-    // row sums R_i, S = tr G + sum G
-    dfloat R[3];
-    R[0] = df_add(df_add(G[0][0], G[0][1]), G[0][2]);
-    R[1] = df_add(df_add(G[0][1], G[1][1]), G[1][2]);
-    R[2] = df_add(df_add(G[0][2], G[1][2]), G[2][2]);
-    const dfloat trG = df_add(df_add(G[0][0], G[1][1]), G[2][2]);
-    const dfloat S = df_add(trG, df_add(df_add(R[0], R[1]), R[2]));
-    // W = 1 / (30 kappa |det J|)
-    const dfloat W = df_recip(df_mul_f(df_mul(df_from_double(kap), det), 30.f));
-    dfloat R5[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) R5[i] = df_mul_f(R[i], 5.f);
-    double out[kFinalWords];
-    out[0] = df_to_double(df_mul(W, S));
-#pragma unroll
-    for (int b = 1; b < 4; ++b) out[b] = df_to_double(df_mul(W, df_sub(S, R5[b - 1])));
-#pragma unroll
-    for (int a = 1; a < 4; ++a)
-#pragma unroll
-      for (int b = a; b < 4; ++b) {
-        const dfloat t = df_add(df_sub(S, df_add(R5[a - 1], R5[b - 1])), df_mul_f(G[a - 1][b - 1], 20.f));
-        out[final_idx(a, b)] = df_to_double(df_mul(W, t));
-      }
-    const double rp = (SRC == NFEM_COEF_NONE) ? 0.0 : df_to_double(df_neg(df_mul(det, F)));
-    const int64_t slot = rec_index(p, c);
-    double2* o = reinterpret_cast<double2*>(rec + slot * kFinalWords);
-#pragma unroll
-    for (int k = 0; k < kFinalWords / 2; ++k) o[k] = make_double2(out[2 * k], out[2 * k + 1]);
-    if (p.prow)
-      pressure_row<double, 3>(p, c, rp, prow);
-    else
-      rec[p.rp_off + slot] = rp;
+    record_df_cell<SRC>(p, c, v);
   }
 }
 
@@ -793,6 +799,15 @@ __device__ __forceinline__ double flip_sign(double x, bool neg) {
 // Row a of the cell in record slot `slot` from its finished FP64 record:
 // the four U_ab with the orientation signs, the divergence column, and the
 // pressure row's r_p.
+template <bool COH>
+__device__ __forceinline__ double rec_load(const double* ptr) {
+  if constexpr (COH)
+    return __ldcg(ptr);
+  else
+    return __ldg(ptr);
+}
+
+template <bool COH = false>
 __device__ __forceinline__ void final_row(const DarcyParams& p, int64_t slot, uint32_t m, int a, double (&vals)[5],
                                           double& rhs_val) {
   using C = DarcyConst<double, 3>;
@@ -811,14 +826,14 @@ __device__ __forceinline__ void final_row(const DarcyParams& p, int64_t slot, ui
       int idx = final_idx(0, b);
 #pragma unroll
       for (int i = 1; i < 4; ++i) idx = (a == i) ? final_idx(i, b) : idx;
-      vals[b] = flip_sign(__ldg(r + idx), na != neg[b]);
+      vals[b] = flip_sign(rec_load<COH>(r + idx), na != neg[b]);
     }
     vals[4] = na ? 1.0 : -1.0;  // -sg_a
   } else {
 #pragma unroll
     for (int b = 0; b < 4; ++b) vals[b] = neg[b] ? -1.0 : 1.0;
     vals[4] = 0.0;
-    rhs_val += __ldg(rec + p.rp_off + slot);
+    rhs_val += rec_load<COH>(rec + p.rp_off + slot);
   }
 }
 
@@ -978,13 +993,125 @@ __device__ __forceinline__ int row_len_from_codes(const RowHead& h) {
 // Block `rank` of `n_blocks` row blocks (kDarcyWarps warps each) writes the
 // 32-row chunks rank * kDarcyWarps + warp, + n_blocks * kDarcyWarps, ...;
 // st is the warp's staging buffer of 32 * kDarcyMaxRow values.
-template <typename T, int DIM, int SRC, bool REC>
-__device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t rank, int64_t n_blocks) {
+// One 32-row chunk [rb, re) (rows beyond re idle) with its lanes' head
+// words h, row_ptr of the lane's row rpl and of the row after the chunk
+// rpe; st is the warp's staging buffer.  COH reads the records through L2
+// only (records written by other blocks of the same launch).
+template <typename T, int DIM, int SRC, bool REC, bool COH = false>
+__device__ __forceinline__ void process_chunk(const DarcyParams& p, T* st, int64_t rb, int64_t re, const RowHead h,
+                                              int32_t rpl, int32_t rpe, bool bulk) {
   constexpr int NLOC = DIM + 2;
   constexpr int VEC = 16 / int(sizeof(T));  // values per 16 bytes
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31;
   T* values = static_cast<T*>(p.values);
   T* rhs = static_cast<T*>(p.rhs);
+  const int64_t r0 = rb;
+  const int64_t r = r0 + lane;
+  const bool valid = r < re;
+  const int32_t base = __shfl_sync(0xffffffffu, rpl, 0);
+
+  const int occ[2] = {h.pr.x, h.pr.y};
+  const uint32_t code[2] = {h.cd.x, h.cd.y};
+  int32_t c[2];
+  int a[2];
+  bool on[2], geo[2];
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    on[t] = occ[t] >= 0;
+    c[t] = on[t] ? occ[t] / NLOC : 0;
+    a[t] = on[t] ? occ[t] - c[t] * NLOC : 0;
+    geo[t] = on[t] && ((a[t] < DIM + 1) || (SRC != 0));
+  }
+  // row lengths and offsets inside the chunk straight from row_ptr
+  // every lane takes part in the shuffle; lane 31 then uses the chunk end
+  const int32_t rp_down = __shfl_down_sync(0xffffffffu, rpl, 1);
+  const int32_t rpn = lane == 31 ? rpe : rp_down;
+  const int len = valid ? rpn - rpl : 0;
+  // staging index q of global entry base - sh + q: the bulk store's middle
+  // is 16-byte aligned in both memories
+  const int sh = bulk ? (base & (VEC - 1)) : 0;
+  const int off = rpl - base + sh;
+  const int span = rpe - base;
+  if (span + sh > 32 * kDarcyMaxRow || span < 0) {  // rows of at most 16 entries fit
+    if (lane == 0) set_status(p.status, NFEM_ERR_PATTERN);
+    return;
+  }
+  const bool two = on[0] && on[1];
+  const int pos_a0 = int((code[0] >> (4 * a[0])) & 15u), pos_a1 = int((code[1] >> (4 * a[1])) & 15u);
+  // Two cells of a conforming simplicial mesh share exactly one column of a
+  // face row (the face itself): then the row has 2 NLOC - 1 entries and
+  // each is stored once, the diagonal summed in a register.  A warp with
+  // any other layout zero-fills its image and adds every contribution.
+  const bool simple = !on[0] || (two ? (len == 2 * NLOC - 1 && pos_a0 == pos_a1) : (len == NLOC));
+  const bool direct = __all_sync(0xffffffffu, simple);
+  if (!direct) {
+    for (int i = lane; i < span; i += 32) st[sh + i] = T(0);
+    __syncwarp();
+  }
+  constexpr int kCap = 32 * kDarcyMaxRow - 1;
+  T rhs_val = T(0), diag = T(0);
+#pragma unroll kDarcyIncUnroll
+  for (int t = 0; t < 2; ++t) {
+    if (on[t]) {
+      T v[NLOC];
+      if constexpr (REC && sizeof(T) == 8 && DIM == 3) {
+        final_row<COH>(p, rec_index(p, c[t]), __ldg(p.sign + c[t]), a[t], v, rhs_val);
+      } else if constexpr (REC) {
+        T w[RecLayout<T, DIM>::n];
+        load_record<T, DIM>(static_cast<const T*>(p.rec), int32_t(rec_index(p, c[t])), a[t] < DIM + 1, w);
+        record_row<T, DIM>(w, __ldg(p.sign + c[t]), a[t], v, rhs_val);
+      } else {
+        Incidence<T, DIM> x;
+        load_incidence<T, DIM, SRC>(p, c[t], geo[t], x);
+        element_row<T, DIM, SRC>(p, x, a[t], geo[t], v, rhs_val);
+      }
+      const uint32_t cd = code[t];
+      const int at = a[t];
+      if (direct) {
+        // the first incidence stores all its entries; the second stores its
+        // own and overwrites the shared diagonal with the sum (one add)
+        T d = T(0);
+#pragma unroll
+        for (int b = 0; b < NLOC; ++b) d = (b == at) ? v[b] : d;
+        const T dsum = t == 1 ? d + diag : d;
+#pragma unroll
+        for (int b = 0; b < NLOC; ++b) {
+          // codes index inside the row (< 16 entries); the clamp keeps a
+          // corrupted code inside this warp's staging buffer
+          const int idx = min(off + int((cd >> (4 * b)) & 15u), kCap);
+          st[idx] = (b == at) ? dsum : v[b];
+        }
+        if (t == 0) diag = d;
+      } else {
+#pragma unroll
+        for (int b = 0; b < NLOC; ++b) st[min(off + int((cd >> (4 * b)) & 15u), kCap)] += v[b];
+      }
+    }
+  }
+  __syncwarp();
+  if (p.accumulate) {
+    for (int i = lane; i < span; i += 32) values[int64_t(base) + i] += st[sh + i];
+    if (valid) rhs[r] += rhs_val;
+  } else {
+    const int qe = sh + span;
+    const int q0 = (sh + VEC - 1) & ~(VEC - 1), q1 = qe & ~(VEC - 1);
+    T* gseg = values + (int64_t(base) - sh);  // global address of staging index 0
+    if (bulk && q1 > q0) {
+      if (lane == 0) bulk_store_s2g(gseg + q0, st + q0, uint32_t(q1 - q0) * uint32_t(sizeof(T)));
+      if (lane < q0 - sh) gseg[sh + lane] = st[sh + lane];             // head: < VEC entries
+      if (lane >= 16 && lane - 16 < qe - q1) gseg[q1 + lane - 16] = st[q1 + lane - 16];  // tail
+    } else {
+      for (int i = lane; i < span; i += 32) values[int64_t(base) + i] = st[sh + i];
+    }
+    if (valid) rhs[r] = rhs_val;
+  }
+  __syncwarp();
+}
+
+template <typename T, int DIM, int SRC, bool REC>
+__device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t rank, int64_t n_blocks) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* values = static_cast<T*>(p.values);
   // chunks of 32 rows: first over [row_f0, row_f1), then over [row_q0, row_q1)
   const int64_t nfc = (p.row_f1 - p.row_f0 + 31) / 32, nqc = (p.row_q1 - p.row_q0 + 31) / 32;
   const int64_t n_chunks = nfc + nqc;
@@ -1013,9 +1140,7 @@ __device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t r
       if (lane == 0) bulk_wait_read();
       __syncwarp();
     }
-    const int64_t r0 = rb;
-    const int64_t r = r0 + lane;
-    const bool valid = r < re;
+    const int64_t rbc = rb, rec_ = re;
     const RowHead h = head;
     const int32_t rpl = rp_lane, rpe = rp_end;
     // prefetch the next chunk of this warp (overlaps its latency with this one)
@@ -1023,104 +1148,7 @@ __device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t r
     head = load_head(p, rb + lane, re);
     rp_lane = rp_at(rb + lane, re);
     rp_end = rp_at(rb + 32, re);
-    const int32_t base = __shfl_sync(0xffffffffu, rpl, 0);
-
-    const int occ[2] = {h.pr.x, h.pr.y};
-    const uint32_t code[2] = {h.cd.x, h.cd.y};
-    int32_t c[2];
-    int a[2];
-    bool on[2], geo[2];
-#pragma unroll
-    for (int t = 0; t < 2; ++t) {
-      on[t] = occ[t] >= 0;
-      c[t] = on[t] ? occ[t] / NLOC : 0;
-      a[t] = on[t] ? occ[t] - c[t] * NLOC : 0;
-      geo[t] = on[t] && ((a[t] < DIM + 1) || (SRC != 0));
-    }
-    // row lengths and offsets inside the chunk straight from row_ptr
-    // every lane takes part in the shuffle; lane 31 then uses the chunk end
-    const int32_t rp_down = __shfl_down_sync(0xffffffffu, rpl, 1);
-    const int32_t rpn = lane == 31 ? rpe : rp_down;
-    const int len = valid ? rpn - rpl : 0;
-    // staging index q of global entry base - sh + q: the bulk store's middle
-    // is 16-byte aligned in both memories
-    const int sh = bulk ? (base & (VEC - 1)) : 0;
-    const int off = rpl - base + sh;
-    const int span = rpe - base;
-    if (span + sh > 32 * kDarcyMaxRow || span < 0) {  // rows of at most 16 entries fit
-      if (lane == 0) set_status(p.status, NFEM_ERR_PATTERN);
-      continue;
-    }
-    const bool two = on[0] && on[1];
-    const int pos_a0 = int((code[0] >> (4 * a[0])) & 15u), pos_a1 = int((code[1] >> (4 * a[1])) & 15u);
-    // Two cells of a conforming simplicial mesh share exactly one column of a
-    // face row (the face itself): then the row has 2 NLOC - 1 entries and
-    // each is stored once, the diagonal summed in a register.  A warp with
-    // any other layout zero-fills its image and adds every contribution.
-    const bool simple = !on[0] || (two ? (len == 2 * NLOC - 1 && pos_a0 == pos_a1) : (len == NLOC));
-    const bool direct = __all_sync(0xffffffffu, simple);
-    if (!direct) {
-      for (int i = lane; i < span; i += 32) st[sh + i] = T(0);
-      __syncwarp();
-    }
-    constexpr int kCap = 32 * kDarcyMaxRow - 1;
-    T rhs_val = T(0), diag = T(0);
-#pragma unroll kDarcyIncUnroll
-    for (int t = 0; t < 2; ++t) {
-      if (on[t]) {
-        T v[NLOC];
-        if constexpr (REC && sizeof(T) == 8 && DIM == 3) {
-          final_row(p, rec_index(p, c[t]), __ldg(p.sign + c[t]), a[t], v, rhs_val);
-        } else if constexpr (REC) {
-          T w[RecLayout<T, DIM>::n];
-          load_record<T, DIM>(static_cast<const T*>(p.rec), int32_t(rec_index(p, c[t])), a[t] < DIM + 1, w);
-          record_row<T, DIM>(w, __ldg(p.sign + c[t]), a[t], v, rhs_val);
-        } else {
-          Incidence<T, DIM> x;
-          load_incidence<T, DIM, SRC>(p, c[t], geo[t], x);
-          element_row<T, DIM, SRC>(p, x, a[t], geo[t], v, rhs_val);
-        }
-        const uint32_t cd = code[t];
-        const int at = a[t];
-        if (direct) {
-          // the first incidence stores all its entries; the second stores its
-          // own and overwrites the shared diagonal with the sum (one add)
-          T d = T(0);
-#pragma unroll
-          for (int b = 0; b < NLOC; ++b) d = (b == at) ? v[b] : d;
-          const T dsum = t == 1 ? d + diag : d;
-#pragma unroll
-          for (int b = 0; b < NLOC; ++b) {
-            // codes index inside the row (< 16 entries); the clamp keeps a
-            // corrupted code inside this warp's staging buffer
-            const int idx = min(off + int((cd >> (4 * b)) & 15u), kCap);
-            st[idx] = (b == at) ? dsum : v[b];
-          }
-          if (t == 0) diag = d;
-        } else {
-#pragma unroll
-          for (int b = 0; b < NLOC; ++b) st[min(off + int((cd >> (4 * b)) & 15u), kCap)] += v[b];
-        }
-      }
-    }
-    __syncwarp();
-    if (p.accumulate) {
-      for (int i = lane; i < span; i += 32) values[int64_t(base) + i] += st[sh + i];
-      if (valid) rhs[r] += rhs_val;
-    } else {
-      const int qe = sh + span;
-      const int q0 = (sh + VEC - 1) & ~(VEC - 1), q1 = qe & ~(VEC - 1);
-      T* gseg = values + (int64_t(base) - sh);  // global address of staging index 0
-      if (bulk && q1 > q0) {
-        if (lane == 0) bulk_store_s2g(gseg + q0, st + q0, uint32_t(q1 - q0) * uint32_t(sizeof(T)));
-        if (lane < q0 - sh) gseg[sh + lane] = st[sh + lane];             // head: < VEC entries
-        if (lane >= 16 && lane - 16 < qe - q1) gseg[q1 + lane - 16] = st[q1 + lane - 16];  // tail
-      } else {
-        for (int i = lane; i < span; i += 32) values[int64_t(base) + i] = st[sh + i];
-      }
-      if (valid) rhs[r] = rhs_val;
-    }
-    __syncwarp();
+    process_chunk<T, DIM, SRC, REC>(p, st, rbc, rec_, h, rpl, rpe, bulk);
   }
   if (bulk && lane == 0) bulk_wait_all();
 }
