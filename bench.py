@@ -533,6 +533,7 @@ def assembly_only(args):
     wf.use_records = args.kernel == "records"
     wf.use_slices = args.slices
     wf.use_streams = args.streams
+    wf.use_fused = args.fused
     if args.slice_shift:
         wf.min_slice_shift = args.slice_shift
     if args.record_quarters:
@@ -877,6 +878,7 @@ def run_ours(args):
     wf.use_records = args.kernel == "records"
     wf.use_slices = args.slices
     wf.use_streams = args.streams
+    wf.use_fused = args.fused
     if args.slice_shift:
         wf.min_slice_shift = args.slice_shift
     if args.record_quarters:
@@ -1145,6 +1147,8 @@ def main():
     ap.add_argument("--slice-shift", type=int, default=0, help="cells per slice = 2^shift (default: the library's)")
     ap.add_argument("--record-quarters", type=int, default=0,
                     help="quarters of the blocks forming records in the overlapped assembly (default: the library's)")
+    ap.add_argument("--fused", type=int, default=0,
+                    help="1: FP64 tetrahedra through the fused persistent launch (record and row tiles from a plan)")
     ap.add_argument("--streams", type=int, default=0,
                     help="K > 0: the headline's two passes over K cell slices on two streams")
     ap.add_argument("--mlp-rows", type=int, default=3_200_000,

@@ -124,6 +124,10 @@ _SIGS = {
     "nfem_darcy_ring_bytes": ([_I, _I, C.POINTER(_SZ)], _I),
     "nfem_darcy_rt1p0_assemble_sliced": ([_I, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _I, _P, _I, _P, _P, _P,
                                           C.POINTER(DarcySlices), _P, _P, _I, _P, _SZ, _P, _P], _I),
+    "nfem_darcy_fused_plan_bytes": ([_I64, _I64, C.POINTER(_SZ)], _I),
+    "nfem_darcy_fused_plan": ([_P, _I64, _I64, _I, _P, _SZ, _P], _I),
+    "nfem_darcy_rt1p0_assemble_fused": ([_I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _I, _P, _I, _P, _P, _P, _P, _SZ,
+                                         _P, _P, _I, _P, _SZ, _P, _P], _I),
     "nfem_pattern_darcy_chunks": ([_P, _I64, _I, _I64, _I64, _P, _P, _P], _I),
     "nfem_copy_bytes": ([_P, _P, _SZ, _P], _I),
     "nfem_spmv": ([_I, _I64, _P, _P, _P, _P, _P, _P], _I),

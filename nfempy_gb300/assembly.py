@@ -432,6 +432,12 @@ class LaplaceDualWeakForm(WeakForm):
     use_streams = 0
     min_slice_shift = 17
     record_quarters = {torch.float64: 2, torch.float32: 1}
+    # FP64 tetrahedra: one persistent launch taking record tiles and row
+    # tiles from a plan (nfem_darcy_rt1p0_assemble_fused), bitwise the values
+    # of the two passes; fused_lead record tiles run ahead of the rows (0:
+    # the library's choice)
+    use_fused = False
+    fused_lead = 0
 
     def _check_space(self):
         sp = self.space
@@ -520,6 +526,17 @@ class LaplaceDualWeakForm(WeakForm):
                 _lib.call("nfem_darcy_workspace_bytes", sp.dim, vt, sp.n_cells, _lib.C.byref(nb))
                 self._cache[key] = torch.empty(max(int(nb.value), 16), dtype=torch.uint8, device=sp.device)
             ws = self._cache[key]
+            p_base = sp.field_offsets["p"]
+            if (self.use_fused and sp.dim == 3 and dtype == torch.float64 and not self.use_streams
+                    and p_base + sp.n_cells == jacobian.n_rows):
+                plan = self._fused_plan(jacobian, stream)
+                _lib.call("nfem_darcy_rt1p0_assemble_fused", sp.n_cells, jacobian.n_rows, _lib.ptr(sp.points),
+                          _lib.ptr(split), _lib.ptr(sp.cells), p_base, _lib.ptr(sp.rt_sign_mask), _lib.ptr(kt),
+                          _lib.ptr(st), mode, _lib.C.cast(qw, _lib.C.c_void_p), len(wts), _lib.ptr(jacobian.pairs),
+                          _lib.ptr(jacobian.pair_codes), _lib.ptr(jacobian.row_ptr), _lib.ptr(plan), plan.numel(),
+                          _lib.ptr(jacobian.values), _lib.ptr(residual), int(accumulate), _lib.ptr(ws), ws.numel(),
+                          _lib.ptr(jacobian.status), _lib.stream_ptr(stream))
+                return
             if self.use_streams and getattr(jacobian, "chunk_rows_host", None) is not None:
                 return self._assemble_two_streams(jacobian, residual, accumulate, stream, kt, st, mode, qw, len(wts),
                                                   split, ws, vt)
@@ -573,6 +590,22 @@ class LaplaceDualWeakForm(WeakForm):
                       p_base + min((k + 1) * S, T), _lib.ptr(jacobian.status), _lib.stream_ptr(side))
         events[K].record(side)
         main.wait_event(events[K])
+
+    def _fused_plan(self, jacobian, stream=None):
+        """Work plan of the fused FP64 assembly (nfem_darcy_fused_plan), built
+        once per matrix pattern; `fused_lead` record tiles run ahead of the
+        rows (0: the library's choice)."""
+        key = ("fused", id(jacobian.pairs), int(self.fused_lead))
+        if key not in self._cache:
+            sp = self.space
+            p_base = sp.field_offsets["p"]
+            nb = _lib.C.c_size_t(0)
+            _lib.call("nfem_darcy_fused_plan_bytes", sp.n_cells, p_base, _lib.C.byref(nb))
+            plan = torch.zeros(max(int(nb.value), 16), dtype=torch.uint8, device=sp.device)
+            _lib.call("nfem_darcy_fused_plan", _lib.ptr(jacobian.pairs), sp.n_cells, p_base, int(self.fused_lead),
+                      _lib.ptr(plan), plan.numel(), _lib.stream_ptr(stream))
+            self._cache[key] = plan
+        return self._cache[key]
 
     def _slice_plan(self, jacobian, dtype, vt):
         """(nfem_darcy_slices, ring workspace) of the overlapped assembly,

@@ -31,6 +31,7 @@
 // workspace a cell pass first evaluates each cell's metric terms once, and
 // the row pass reads those records instead of the vertices (two-pass form).
 #include <algorithm>
+#include <vector>
 
 #include "df64.cuh"
 #include "nfem_common.cuh"
@@ -2029,6 +2030,262 @@ extern "C" int nfem_darcy_l2_error(int dim, int64_t n_cells, const double* point
   if (dim == 3) darcy_l2_kernel<3><<<nb, 256, 0, stream>>>(p);
   else darcy_l2_kernel<2><<<nb, 256, 0, stream>>>(p);
   l2_final<<<1, 32, 0, stream>>>(p.partial, nb, errors);
+  NFEM_CHECK_LAUNCH();
+  return NFEM_OK;
+}
+
+namespace nfem {
+
+// ------------------------------------------------------------------ fused
+// One persistent launch of the two-pass FP64 assembly of tetrahedra, the
+// cell pass and the row pass side by side on every SM.  The blocks take
+// work items in the order of a schedule built once per pattern
+// (nfem_darcy_fused_plan): record tiles of 256 consecutive cells and row
+// tiles of 256 consecutive flux rows, each row tile placed after the record
+// tiles of every cell its rows touch plus a lead.
+//   record tile: each thread forms one cell's record and pressure row; then
+//                one thread publishes the tile's flag (release).
+//   row tile:    the threads wait (acquire, bounded) for the flags of the
+//                record tiles [lo, hi] its rows touch, then each warp writes
+//                one 32-row chunk, reading the records through L2 only.
+// Records are read back shortly after they are written, from L2, instead
+// of after the whole cell pass.  Every record tile a row tile waits for was
+// taken earlier by a block that is running and waits for nothing, so the
+// waits end; one that still runs out of polls sets NFEM_ERR_TIMEOUT and the
+// block goes on (its values are then not valid).
+constexpr int kFusedThreads = 256;
+constexpr int kFusedTile = 256;  // cells of a record tile = rows of a row tile
+constexpr int kFusedWarps = kFusedThreads / 32;
+constexpr uint32_t kFusedPolls = 1u << 22;
+static_assert(kFusedTile == kFusedWarps * 32, "one 32-row chunk per warp");
+#ifndef NFEM_FUSED_MIN_BLOCKS
+#define NFEM_FUSED_MIN_BLOCKS 4
+#endif
+
+// Plan layout (int32 words): [0] items, [1] record tiles, [2] row tiles,
+// [3] 0; then lo, hi of each row tile; then the schedule (item >= 0: record
+// tile; item < 0: row tile ~item); then, 16-byte aligned, the words zeroed
+// before each launch: the work counter and one flag per record tile.
+struct FusedLayout {
+  int64_t rec_tiles, row_tiles, items, sync_word, words;
+};
+static FusedLayout fused_layout(int64_t n_cells, int64_t p_base) {
+  FusedLayout L;
+  L.rec_tiles = ceil_div(n_cells, int64_t(kFusedTile));
+  L.row_tiles = ceil_div(p_base, int64_t(kFusedTile));
+  L.items = L.rec_tiles + L.row_tiles;
+  L.sync_word = (4 + 2 * L.row_tiles + L.items + 3) & ~int64_t(3);
+  L.words = L.sync_word + 1 + L.rec_tiles;
+  return L;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* ptr) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(uint32_t* ptr, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(ptr), "r"(v) : "memory");
+}
+
+template <int SRC>
+__global__ void __launch_bounds__(kFusedThreads, NFEM_FUSED_MIN_BLOCKS)
+    darcy_fused_kernel(const DarcyParams p, const int32_t* __restrict__ plan, int32_t* sync) {
+  __shared__ __align__(16) double stage[kFusedWarps][32 * kDarcyMaxRow];
+  __shared__ int item_s[2];
+  const int n_items = plan[0];
+  const int32_t* lohi = plan + 4;
+  const int32_t* sched = lohi + 2 * plan[2];
+  uint32_t* flags = reinterpret_cast<uint32_t*>(sync + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int4* __restrict__ cv4 = reinterpret_cast<const int4*>(p.cv);
+  const bool bulk = NFEM_DARCY_BULK && !p.accumulate && (reinterpret_cast<uintptr_t>(p.values) & 15) == 0;
+  auto rp_at = [&](int64_t r, int64_t e) { return __ldg(p.row_ptr + (r < e ? r : e)); };
+  for (int k = 0;; ++k) {
+    if (threadIdx.x == 0) item_s[k & 1] = atomicAdd(sync, 1);
+    __syncthreads();
+    const int q = item_s[k & 1];
+    if (q >= n_items) break;
+    const int it = __ldg(sched + q);
+    if (it >= 0) {
+      const int64_t c = int64_t(it) * kFusedTile + threadIdx.x;
+      if (c < p.n_cells) record_df_cell<SRC>(p, c, __ldg(cv4 + c));
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        st_release_gpu(flags + it, 1u);
+      }
+    } else {
+      const int j = ~it;
+      const int lo = __ldg(lohi + 2 * j), hi = __ldg(lohi + 2 * j + 1);
+      for (int t = lo + int(threadIdx.x); t <= hi; t += kFusedThreads) {
+        uint32_t polls = 0;
+        while (ld_acquire_gpu(flags + t) == 0u) {
+          if (++polls >= kFusedPolls) {
+            set_status(p.status, NFEM_ERR_TIMEOUT);
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+      __threadfence();
+      __syncthreads();
+      const int64_t rb = p.row_f0 + (int64_t(j) * kFusedWarps + warp) * 32;
+      if (rb < p.row_f1) {
+        if (bulk) {  // the staging buffer is free once the last bulk store has read it
+          if (lane == 0) bulk_wait_read();
+          __syncwarp();
+        }
+        const int64_t re = p.row_f1;
+        const RowHead h = load_head(p, rb + lane, re);
+        process_chunk<double, 3, NFEM_COEF_NONE, true, true>(p, stage[warp], rb, re, h, rp_at(rb + lane, re),
+                                                             rp_at(rb + 32, re), bulk);
+      }
+    }
+  }
+  if (bulk && lane == 0) bulk_wait_all();
+}
+
+// lo, hi of every row tile: the record tiles of the cells its rows touch
+__global__ void fused_tile_range_kernel(const int2* __restrict__ pairs, int64_t p_base, int32_t* __restrict__ lohi) {
+  __shared__ int s_lo, s_hi;
+  if (threadIdx.x == 0) {
+    s_lo = INT32_MAX;
+    s_hi = -1;
+  }
+  __syncthreads();
+  const int64_t r = int64_t(blockIdx.x) * kFusedTile + threadIdx.x;
+  int lo = INT32_MAX, hi = -1;
+  if (r < p_base) {
+    const int2 pr = pairs[r];
+    if (pr.x >= 0) {
+      const int t = pr.x / 5 / kFusedTile;
+      lo = min(lo, t);
+      hi = max(hi, t);
+    }
+    if (pr.y >= 0) {
+      const int t = pr.y / 5 / kFusedTile;
+      lo = min(lo, t);
+      hi = max(hi, t);
+    }
+  }
+  if (hi >= 0) {
+    atomicMin(&s_lo, lo);
+    atomicMax(&s_hi, hi);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    lohi[2 * blockIdx.x] = s_hi >= 0 ? s_lo : 0;
+    lohi[2 * blockIdx.x + 1] = s_hi;
+  }
+}
+
+template <int SRC>
+static int fused_resident_blocks() {
+  static int n = 0;
+  if (!n) n = resident_blocks(darcy_fused_kernel<SRC>, kFusedThreads);
+  return n;
+}
+
+}  // namespace nfem
+
+extern "C" int nfem_darcy_fused_plan_bytes(int64_t n_cells, int64_t p_base, size_t* bytes) {
+  if (!bytes || n_cells < 0 || p_base < 0) return NFEM_ERR_INVALID_ARG;
+  if (n_cells > int64_t(INT32_MAX) / 5) return NFEM_ERR_OVERFLOW;
+  *bytes = size_t(fused_layout(n_cells, p_base).words) * sizeof(int32_t);
+  return NFEM_OK;
+}
+
+extern "C" int nfem_darcy_fused_plan(const int32_t* row_pairs, int64_t n_cells, int64_t p_base, int lead_tiles,
+                                     void* plan, size_t plan_bytes, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  size_t need = 0;
+  const int rc = nfem_darcy_fused_plan_bytes(n_cells, p_base, &need);
+  if (rc) return rc;
+  if (!plan || plan_bytes < need || (reinterpret_cast<uintptr_t>(plan) & 15) || lead_tiles < 0 ||
+      (p_base > 0 && !row_pairs) || (reinterpret_cast<uintptr_t>(row_pairs) & 7))
+    return NFEM_ERR_INVALID_ARG;
+  const FusedLayout L = fused_layout(n_cells, p_base);
+  int32_t* d = static_cast<int32_t*>(plan);
+  std::vector<int32_t> h(size_t(L.sync_word), 0);
+  if (L.row_tiles > 0) {
+    fused_tile_range_kernel<<<unsigned(L.row_tiles), kFusedTile, 0, stream>>>(
+        reinterpret_cast<const int2*>(row_pairs), p_base, d + 4);
+    NFEM_CHECK_LAUNCH();
+    NFEM_TRY_CUDA(cudaMemcpyAsync(h.data() + 4, d + 4, size_t(2 * L.row_tiles) * sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, stream));
+    NFEM_TRY_CUDA(cudaStreamSynchronize(stream));
+  }
+  // every row tile after the record tiles it touches plus the lead
+  // default lead: half the blocks the GPU holds at once, so a row tile's
+  // record tiles were taken well before it and have finished
+  const int lead = lead_tiles > 0 ? lead_tiles
+                                  : std::max(1, grid_for(int64_t(1) << 40, 1, fused_resident_blocks<NFEM_COEF_CELL>()) / 2);
+  int32_t* sched = h.data() + 4 + 2 * L.row_tiles;
+  int64_t q = 0, next_rec = 0;
+  for (int64_t j = 0; j < L.row_tiles; ++j) {
+    const int64_t hi = h[4 + 2 * j + 1];
+    if (hi >= L.rec_tiles || h[4 + 2 * j] < 0) return NFEM_ERR_PATTERN;
+    const int64_t upto = std::min<int64_t>(L.rec_tiles - 1, hi + lead);
+    while (next_rec <= upto) sched[q++] = int32_t(next_rec++);
+    sched[q++] = ~int32_t(j);
+  }
+  while (next_rec < L.rec_tiles) sched[q++] = int32_t(next_rec++);
+  h[0] = int32_t(L.items);
+  h[1] = int32_t(L.rec_tiles);
+  h[2] = int32_t(L.row_tiles);
+  NFEM_TRY_CUDA(cudaMemcpyAsync(d, h.data(), size_t(L.sync_word) * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+  NFEM_TRY_CUDA(cudaStreamSynchronize(stream));
+  return NFEM_OK;
+}
+
+extern "C" int nfem_darcy_rt1p0_assemble_fused(int64_t n_cells, int64_t n_rows, const double* points,
+                                               const void* point_records, const int32_t* cell_vertices,
+                                               int64_t p_base, const uint8_t* sign_mask, const void* kappa,
+                                               const void* source, int source_mode, const double* qweights, int n_qp,
+                                               const int32_t* row_pairs, const uint32_t* pair_codes,
+                                               const int32_t* row_ptr, void* plan, size_t plan_bytes, void* values,
+                                               void* rhs, int accumulate, void* workspace, size_t workspace_bytes,
+                                               int32_t* dev_status, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n_cells < 0 || n_rows < 0 || p_base < 0 || p_base + n_cells != n_rows) return NFEM_ERR_INVALID_ARG;
+  if (n_rows == 0) return NFEM_OK;
+  size_t need = 0;
+  int rc = nfem_darcy_fused_plan_bytes(n_cells, p_base, &need);
+  if (rc) return rc;
+  if (!plan || plan_bytes < need || (reinterpret_cast<uintptr_t>(plan) & 15)) return NFEM_ERR_INVALID_ARG;
+  DarcyParams p;
+  rc = darcy_build(p, 3, NFEM_F64, n_cells, n_rows, points, static_cast<const float*>(point_records), cell_vertices,
+                   nullptr, p_base, sign_mask, kappa, source, source_mode, qweights, n_qp, row_pairs, pair_codes,
+                   row_ptr, nullptr, values, rhs, accumulate, workspace, workspace_bytes, dev_status);
+  if (rc) return rc;
+  if (!p.rec) return NFEM_ERR_WORKSPACE;
+  const FusedLayout L = fused_layout(n_cells, p_base);
+  int32_t* words = static_cast<int32_t*>(plan);
+  p.prow = 1;
+  p.row_f0 = 0;
+  p.row_f1 = p_base;
+  p.row_q0 = p.row_q1 = 0;
+  NFEM_TRY_CUDA(cudaMemsetAsync(words + L.sync_word, 0, size_t(1 + L.rec_tiles) * sizeof(int32_t), stream));
+  int per_sm = 0;
+  switch (source_mode) {
+    case NFEM_COEF_NONE: per_sm = fused_resident_blocks<NFEM_COEF_NONE>(); break;
+    case NFEM_COEF_CELL: per_sm = fused_resident_blocks<NFEM_COEF_CELL>(); break;
+    case NFEM_COEF_QPOINT: per_sm = fused_resident_blocks<NFEM_COEF_QPOINT>(); break;
+    default: return NFEM_ERR_INVALID_ARG;
+  }
+  const int grid = grid_for(L.items * int64_t(kFusedThreads), kFusedThreads, per_sm);
+  switch (source_mode) {
+    case NFEM_COEF_NONE:
+      darcy_fused_kernel<NFEM_COEF_NONE><<<grid, kFusedThreads, 0, stream>>>(p, words, words + L.sync_word);
+      break;
+    case NFEM_COEF_CELL:
+      darcy_fused_kernel<NFEM_COEF_CELL><<<grid, kFusedThreads, 0, stream>>>(p, words, words + L.sync_word);
+      break;
+    default:
+      darcy_fused_kernel<NFEM_COEF_QPOINT><<<grid, kFusedThreads, 0, stream>>>(p, words, words + L.sync_word);
+      break;
+  }
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }

@@ -390,3 +390,38 @@ def test_darcy_f64_lattice_records(cuda_lib, name, qpoint):
     assert ((res - res_df).abs().max() / res_df.abs().max()).item() <= 1e-13
     if name == "cube6":  # no lattice cell: the same double-float records
         assert torch.equal(A.values, A_df.values)
+
+
+@pytest.mark.parametrize("name", ["cube16", "moved16", "mixed8", "cube6"])
+@pytest.mark.parametrize("qpoint,accumulate,lead", [(False, False, 0), (True, False, 0), (False, True, 0),
+                                                    (False, False, 1), (False, False, 3)])
+def test_darcy_fused_equals_two_pass(cuda_lib, name, qpoint, accumulate, lead):
+    """The fused FP64 assembly (one persistent launch, record tiles and row
+    tiles from a plan, row tiles waiting on their record tiles' flags) writes
+    bitwise the values and residual of the two passes in turn: the same
+    record and row arithmetic, only scheduled differently.  A lead of 1 or 3
+    record tiles makes the row tiles wait on records still being formed."""
+    m = _lattice_meshes()[name]
+    T = m["blocks"][-1][1].shape[0]
+    rng = np.random.default_rng(T + 1)
+    kappa = np.exp(rng.normal(0.0, 2.0, T))
+    f_cell = rng.normal(0.0, 1.0, T)
+    rhs = f2d if qpoint else f_cell
+    sp = product_space(m, DARCY)
+    out = []
+    for fused in (False, True):
+        A = nf.CSRMatrix(sp, dtype=torch.float64)
+        res = torch.zeros(A.n_rows, dtype=torch.float64, device="cuda")
+        wf = nf.LaplaceDualWeakForm(sp)
+        wf.use_records = True
+        wf.use_fused = fused
+        wf.fused_lead = lead
+        wf.functions = {"kappa": kappa, "rhs": rhs}
+        wf.assemble(A, res)
+        if accumulate:  # a second pass adds the same element data again
+            wf.assemble(A, res, accumulate=True)
+        torch.cuda.synchronize()
+        A.check_status(f"fused={fused}")
+        out.append((A.values.clone(), res.clone()))
+    assert torch.equal(out[0][0], out[1][0])
+    assert torch.equal(out[0][1], out[1][1])
