@@ -388,22 +388,22 @@ int nfem_darcy_rt1p0_assemble_sliced(int value_type, int64_t n_cells, int64_t n_
  * reference interface, LaplaceDualWeakForm.evaluate_form
  * src/weak_forms/laplace_dual_weak_form.py:10-86 with the scatter of
  * src/assembly/ScatterFormData.py:5-25; bitwise the values of the two-pass
- * form): one persistent launch whose blocks take record tiles (256 cells:
- * records and pressure rows) and row tiles (256 flux rows) in the order of
- * a plan, each row tile after the record tiles of the cells it touches, so
- * records are read back from L2 soon after they are written.  A row tile
- * waits (bounded) for its record tiles' flags; a wait that runs out sets
- * NFEM_ERR_TIMEOUT.
+ * form): one persistent cooperative launch whose warps take record chunks
+ * (32 cells: records and pressure rows) and row chunks (32 flux rows) in
+ * the order of a plan, each row chunk after the record chunks of the cells
+ * it touches, so records are read back from L2 soon after they are
+ * written.  A row chunk waits (bounded) for its record chunks' flags; a
+ * wait that runs out sets NFEM_ERR_TIMEOUT.
  * nfem_darcy_fused_plan builds the plan once per pattern (it reads
- * row_pairs, synchronises `stream` and copies a few words per tile to the
- * host); lead_tiles > 0 sets how many record tiles run ahead of the rows
- * (0: half the blocks the GPU holds at once).  The plan also holds the
- * work counter and the tile flags that each assembly zeroes, so one plan
- * serves one assembly at a time.  Requires n_rows = p_base + n_cells and
+ * row_pairs, synchronises `stream` and copies one word per row chunk to the
+ * host); lead_chunks > 0 sets how many record chunks run ahead of the rows
+ * (0: half the warps the GPU holds at once).  The plan also holds the
+ * chunk flags that each assembly zeroes, so one plan serves one assembly
+ * at a time.  Requires n_rows = p_base + n_cells and
  * the record workspace of nfem_darcy_workspace_bytes(3, NFEM_F64, ...);
  * point_records may carry nfem_points_fixed64 records or be NULL. */
 int nfem_darcy_fused_plan_bytes(int64_t n_cells, int64_t p_base, size_t* bytes);
-int nfem_darcy_fused_plan(const int32_t* row_pairs, int64_t n_cells, int64_t p_base, int lead_tiles,
+int nfem_darcy_fused_plan(const int32_t* row_pairs, int64_t n_cells, int64_t p_base, int lead_chunks,
                           void* plan, size_t plan_bytes, void* stream);
 int nfem_darcy_rt1p0_assemble_fused(int64_t n_cells, int64_t n_rows, const double* points,
                                     const void* point_records, const int32_t* cell_vertices,

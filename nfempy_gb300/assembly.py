@@ -432,10 +432,11 @@ class LaplaceDualWeakForm(WeakForm):
     use_streams = 0
     min_slice_shift = 17
     record_quarters = {torch.float64: 2, torch.float32: 1}
-    # FP64 tetrahedra: one persistent launch taking record tiles and row
-    # tiles from a plan (nfem_darcy_rt1p0_assemble_fused), bitwise the values
-    # of the two passes; fused_lead record tiles run ahead of the rows (0:
-    # the library's choice)
+    # FP64 tetrahedra: one persistent launch whose warps take 32-cell record
+    # chunks and 32-row row chunks from a plan
+    # (nfem_darcy_rt1p0_assemble_fused), bitwise the values of the two
+    # passes; fused_lead record chunks run ahead of the rows (0: the
+    # library's choice)
     use_fused = False
     fused_lead = 0
 
@@ -593,7 +594,7 @@ class LaplaceDualWeakForm(WeakForm):
 
     def _fused_plan(self, jacobian, stream=None):
         """Work plan of the fused FP64 assembly (nfem_darcy_fused_plan), built
-        once per matrix pattern; `fused_lead` record tiles run ahead of the
+        once per matrix pattern; `fused_lead` record chunks run ahead of the
         rows (0: the library's choice)."""
         key = ("fused", id(jacobian.pairs), int(self.fused_lead))
         if key not in self._cache:

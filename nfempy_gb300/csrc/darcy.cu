@@ -1509,7 +1509,6 @@ static int launch_darcy_sliced(DarcyParams p, int shift, const int64_t* flux_beg
   const int64_t S = int64_t(1) << shift, T_ = p.n_cells, K = ceil_div(T_, S);
   int grid = grid_for(int64_t(1) << 40, 1, per_sm);
   grid = grid < 4 ? 4 : grid & ~3;
-  const int64_t p_base = p.row_q0;
   p.prow = 1;  // the cell blocks write the pressure rows of their cells
   for (int64_t l = 0; l <= K; ++l) {
     const int64_t k = l - 1;  // slice whose rows this launch writes
@@ -1795,7 +1794,6 @@ extern "C" int nfem_darcy_rt1p0_assemble_sliced(int value_type, int64_t n_cells,
   p.rec = ring;
   p.rp_off = int64_t(kFinalWords) * (int64_t(3) << shift);
   p.ring_shift = shift;
-  p.row_q0 = p_base;  // the launch loop takes p_base from here
   if (value_type == NFEM_F64) {
     switch (source_mode) {
       case NFEM_COEF_NONE: return launch_darcy_sliced<double, NFEM_COEF_NONE>(p, shift, F, q, stream);
@@ -2038,44 +2036,45 @@ namespace nfem {
 
 // ------------------------------------------------------------------ fused
 // One persistent launch of the two-pass FP64 assembly of tetrahedra, the
-// cell pass and the row pass side by side on every SM.  The blocks take
-// work items in the order of a schedule built once per pattern
-// (nfem_darcy_fused_plan): record tiles of 256 consecutive cells and row
-// tiles of 256 consecutive flux rows, each row tile placed after the record
-// tiles of every cell its rows touch plus a lead.
-//   record tile: each thread forms one cell's record and pressure row; then
-//                one thread publishes the tile's flag (release).
-//   row tile:    the threads wait (acquire, bounded) for the flags of the
-//                record tiles [lo, hi] its rows touch, then each warp writes
-//                one 32-row chunk, reading the records through L2 only.
-// Records are read back shortly after they are written, from L2, instead
-// of after the whole cell pass.  Every record tile a row tile waits for was
-// taken earlier by a block that is running and waits for nothing, so the
-// waits end; one that still runs out of polls sets NFEM_ERR_TIMEOUT and the
-// block goes on (its values are then not valid).
+// cell pass and the row pass side by side on every SM.  The work items are
+// record chunks (32 consecutive cells: their records and pressure rows) and
+// row chunks (32 consecutive flux rows), in the order of a schedule built
+// once per pattern (nfem_darcy_fused_plan) that puts every row chunk after
+// the record chunks of the cells its rows touch, plus a lead.  Warp w of
+// the W resident warps takes items w, w + W, w + 2W, ... in turn:
+//   record chunk: each lane forms one cell's record and pressure row; after
+//                 a warp barrier lane 0 publishes the chunk's flag (release);
+//   row chunk:    each lane waits (acquire, bounded) for the flags of the
+//                 record chunks of its row's cells, then the warp writes the
+//                 rows, reading the records through L2 only.
+// Records are read back shortly after they are written, from L2, instead of
+// after the whole cell pass, and no block-wide barrier couples the warps.
+// The launch is cooperative, so all W warps are resident; an item waits only
+// for items earlier in the schedule, each taken by a running warp whose own
+// waits point further back, so every wait ends.  One that still runs out of
+// polls sets NFEM_ERR_TIMEOUT and the warp goes on (its values are then not
+// valid).
 constexpr int kFusedThreads = 256;
-constexpr int kFusedTile = 256;  // cells of a record tile = rows of a row tile
 constexpr int kFusedWarps = kFusedThreads / 32;
 constexpr uint32_t kFusedPolls = 1u << 22;
-static_assert(kFusedTile == kFusedWarps * 32, "one 32-row chunk per warp");
 #ifndef NFEM_FUSED_MIN_BLOCKS
 #define NFEM_FUSED_MIN_BLOCKS 4
 #endif
 
-// Plan layout (int32 words): [0] items, [1] record tiles, [2] row tiles,
-// [3] 0; then lo, hi of each row tile; then the schedule (item >= 0: record
-// tile; item < 0: row tile ~item); then, 16-byte aligned, the words zeroed
-// before each launch: the work counter and one flag per record tile.
+// Plan layout (int32 words): [0] items, [1] record chunks, [2] row chunks,
+// [3] 0; then the last record chunk each row chunk touches; then the
+// schedule (item >= 0: record chunk; item < 0: row chunk ~item); then,
+// 16-byte aligned, one flag per record chunk, zeroed before each launch.
 struct FusedLayout {
-  int64_t rec_tiles, row_tiles, items, sync_word, words;
+  int64_t rec_chunks, row_chunks, items, sync_word, words;
 };
 static FusedLayout fused_layout(int64_t n_cells, int64_t p_base) {
   FusedLayout L;
-  L.rec_tiles = ceil_div(n_cells, int64_t(kFusedTile));
-  L.row_tiles = ceil_div(p_base, int64_t(kFusedTile));
-  L.items = L.rec_tiles + L.row_tiles;
-  L.sync_word = (4 + 2 * L.row_tiles + L.items + 3) & ~int64_t(3);
-  L.words = L.sync_word + 1 + L.rec_tiles;
+  L.rec_chunks = ceil_div(n_cells, int64_t(32));
+  L.row_chunks = ceil_div(p_base, int64_t(32));
+  L.items = L.rec_chunks + L.row_chunks;
+  L.sync_word = (4 + L.row_chunks + L.items + 3) & ~int64_t(3);
+  L.words = L.sync_word + L.rec_chunks;
   return L;
 }
 
@@ -2087,97 +2086,78 @@ __device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* ptr) {
 __device__ __forceinline__ void st_release_gpu(uint32_t* ptr, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(ptr), "r"(v) : "memory");
 }
+__device__ __forceinline__ void wait_flag(const DarcyParams& p, const uint32_t* flag) {
+  uint32_t polls = 0;
+  while (ld_acquire_gpu(flag) == 0u) {
+    if (++polls >= kFusedPolls) {
+      set_status(p.status, NFEM_ERR_TIMEOUT);
+      return;
+    }
+    __nanosleep(32);
+  }
+}
 
 template <int SRC>
 __global__ void __launch_bounds__(kFusedThreads, NFEM_FUSED_MIN_BLOCKS)
-    darcy_fused_kernel(const DarcyParams p, const int32_t* __restrict__ plan, int32_t* sync) {
+    darcy_fused_kernel(const DarcyParams p, const int32_t* __restrict__ plan, uint32_t* flags) {
   __shared__ __align__(16) double stage[kFusedWarps][32 * kDarcyMaxRow];
-  __shared__ int item_s[2];
-  const int n_items = plan[0];
-  const int32_t* lohi = plan + 4;
-  const int32_t* sched = lohi + 2 * plan[2];
-  uint32_t* flags = reinterpret_cast<uint32_t*>(sync + 1);
+  const int64_t n_items = plan[0];
+  const int32_t* sched = plan + 4 + plan[2];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t W = int64_t(gridDim.x) * kFusedWarps;
   const int4* __restrict__ cv4 = reinterpret_cast<const int4*>(p.cv);
   const bool bulk = NFEM_DARCY_BULK && !p.accumulate && (reinterpret_cast<uintptr_t>(p.values) & 15) == 0;
+  double* st = stage[warp];
   auto rp_at = [&](int64_t r, int64_t e) { return __ldg(p.row_ptr + (r < e ? r : e)); };
-  for (int k = 0;; ++k) {
-    if (threadIdx.x == 0) item_s[k & 1] = atomicAdd(sync, 1);
-    __syncthreads();
-    const int q = item_s[k & 1];
-    if (q >= n_items) break;
+  for (int64_t q = int64_t(blockIdx.x) * kFusedWarps + warp; q < n_items; q += W) {
     const int it = __ldg(sched + q);
     if (it >= 0) {
-      const int64_t c = int64_t(it) * kFusedTile + threadIdx.x;
+      const int64_t c = int64_t(it) * 32 + lane;
       if (c < p.n_cells) record_df_cell<SRC>(p, c, __ldg(cv4 + c));
-      __syncthreads();
-      if (threadIdx.x == 0) {
+      __syncwarp();
+      if (lane == 0) {
         __threadfence();
         st_release_gpu(flags + it, 1u);
       }
     } else {
-      const int j = ~it;
-      const int lo = __ldg(lohi + 2 * j), hi = __ldg(lohi + 2 * j + 1);
-      for (int t = lo + int(threadIdx.x); t <= hi; t += kFusedThreads) {
-        uint32_t polls = 0;
-        while (ld_acquire_gpu(flags + t) == 0u) {
-          if (++polls >= kFusedPolls) {
-            set_status(p.status, NFEM_ERR_TIMEOUT);
-            break;
-          }
-          __nanosleep(64);
-        }
+      const int64_t rb = p.row_f0 + int64_t(~it) * 32, re = p.row_f1;
+      const RowHead h = load_head(p, rb + lane, re);
+      const int32_t rpl = rp_at(rb + lane, re), rpe = rp_at(rb + 32, re);
+      // (a cell beyond the plan's record chunks means the pattern is not the
+      // one the plan was built from)
+      const int32_t n_rec = plan[1];
+      const int occ[2] = {h.pr.x, h.pr.y};
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        if (occ[t] < 0) continue;
+        const int32_t k = occ[t] / 5 / 32;
+        if (k < n_rec)
+          wait_flag(p, flags + k);
+        else
+          set_status(p.status, NFEM_ERR_PATTERN);
       }
-      __threadfence();
-      __syncthreads();
-      const int64_t rb = p.row_f0 + (int64_t(j) * kFusedWarps + warp) * 32;
-      if (rb < p.row_f1) {
-        if (bulk) {  // the staging buffer is free once the last bulk store has read it
-          if (lane == 0) bulk_wait_read();
-          __syncwarp();
-        }
-        const int64_t re = p.row_f1;
-        const RowHead h = load_head(p, rb + lane, re);
-        process_chunk<double, 3, NFEM_COEF_NONE, true, true>(p, stage[warp], rb, re, h, rp_at(rb + lane, re),
-                                                             rp_at(rb + 32, re), bulk);
+      if (bulk) {  // the staging buffer is free once the last bulk store has read it
+        if (lane == 0) bulk_wait_read();
       }
+      __syncwarp();
+      process_chunk<double, 3, NFEM_COEF_NONE, true, true>(p, st, rb, re, h, rpl, rpe, bulk);
     }
   }
   if (bulk && lane == 0) bulk_wait_all();
 }
 
-// lo, hi of every row tile: the record tiles of the cells its rows touch
-__global__ void fused_tile_range_kernel(const int2* __restrict__ pairs, int64_t p_base, int32_t* __restrict__ lohi) {
-  __shared__ int s_lo, s_hi;
-  if (threadIdx.x == 0) {
-    s_lo = INT32_MAX;
-    s_hi = -1;
-  }
-  __syncthreads();
-  const int64_t r = int64_t(blockIdx.x) * kFusedTile + threadIdx.x;
-  int lo = INT32_MAX, hi = -1;
+// The last record chunk that each row chunk's rows touch (-1: none).
+__global__ void fused_chunk_range_kernel(const int2* __restrict__ pairs, int64_t p_base, int64_t n_row_chunks,
+                                         int32_t* __restrict__ hi_out) {
+  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  int hi = -1;
   if (r < p_base) {
     const int2 pr = pairs[r];
-    if (pr.x >= 0) {
-      const int t = pr.x / 5 / kFusedTile;
-      lo = min(lo, t);
-      hi = max(hi, t);
-    }
-    if (pr.y >= 0) {
-      const int t = pr.y / 5 / kFusedTile;
-      lo = min(lo, t);
-      hi = max(hi, t);
-    }
+    if (pr.x >= 0) hi = max(hi, pr.x / 5 / 32);
+    if (pr.y >= 0) hi = max(hi, pr.y / 5 / 32);
   }
-  if (hi >= 0) {
-    atomicMin(&s_lo, lo);
-    atomicMax(&s_hi, hi);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    lohi[2 * blockIdx.x] = s_hi >= 0 ? s_lo : 0;
-    lohi[2 * blockIdx.x + 1] = s_hi;
-  }
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  if ((threadIdx.x & 31) == 0 && (r >> 5) < n_row_chunks) hi_out[r >> 5] = hi;
 }
 
 template <int SRC>
@@ -2185,6 +2165,16 @@ static int fused_resident_blocks() {
   static int n = 0;
   if (!n) n = resident_blocks(darcy_fused_kernel<SRC>, kFusedThreads);
   return n;
+}
+
+template <int SRC>
+static int launch_fused(const DarcyParams& p, const int32_t* plan, uint32_t* flags, int64_t items,
+                        cudaStream_t stream) {
+  const int grid = grid_for(items * 32, kFusedThreads, fused_resident_blocks<SRC>());
+  void* args[] = {const_cast<DarcyParams*>(&p), const_cast<int32_t**>(&plan), &flags};
+  NFEM_TRY_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(darcy_fused_kernel<SRC>), dim3(grid),
+                                            dim3(kFusedThreads), args, 0, stream));
+  return NFEM_OK;
 }
 
 }  // namespace nfem
@@ -2196,44 +2186,44 @@ extern "C" int nfem_darcy_fused_plan_bytes(int64_t n_cells, int64_t p_base, size
   return NFEM_OK;
 }
 
-extern "C" int nfem_darcy_fused_plan(const int32_t* row_pairs, int64_t n_cells, int64_t p_base, int lead_tiles,
+extern "C" int nfem_darcy_fused_plan(const int32_t* row_pairs, int64_t n_cells, int64_t p_base, int lead_chunks,
                                      void* plan, size_t plan_bytes, void* stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;
   size_t need = 0;
   const int rc = nfem_darcy_fused_plan_bytes(n_cells, p_base, &need);
   if (rc) return rc;
-  if (!plan || plan_bytes < need || (reinterpret_cast<uintptr_t>(plan) & 15) || lead_tiles < 0 ||
+  if (!plan || plan_bytes < need || (reinterpret_cast<uintptr_t>(plan) & 15) || lead_chunks < 0 ||
       (p_base > 0 && !row_pairs) || (reinterpret_cast<uintptr_t>(row_pairs) & 7))
     return NFEM_ERR_INVALID_ARG;
   const FusedLayout L = fused_layout(n_cells, p_base);
   int32_t* d = static_cast<int32_t*>(plan);
   std::vector<int32_t> h(size_t(L.sync_word), 0);
-  if (L.row_tiles > 0) {
-    fused_tile_range_kernel<<<unsigned(L.row_tiles), kFusedTile, 0, stream>>>(
-        reinterpret_cast<const int2*>(row_pairs), p_base, d + 4);
+  if (L.row_chunks > 0) {
+    fused_chunk_range_kernel<<<unsigned(ceil_div(L.row_chunks * 32, int64_t(256))), 256, 0, stream>>>(
+        reinterpret_cast<const int2*>(row_pairs), p_base, L.row_chunks, d + 4);
     NFEM_CHECK_LAUNCH();
-    NFEM_TRY_CUDA(cudaMemcpyAsync(h.data() + 4, d + 4, size_t(2 * L.row_tiles) * sizeof(int32_t),
+    NFEM_TRY_CUDA(cudaMemcpyAsync(h.data() + 4, d + 4, size_t(L.row_chunks) * sizeof(int32_t),
                                   cudaMemcpyDeviceToHost, stream));
     NFEM_TRY_CUDA(cudaStreamSynchronize(stream));
   }
-  // every row tile after the record tiles it touches plus the lead
-  // default lead: half the blocks the GPU holds at once, so a row tile's
-  // record tiles were taken well before it and have finished
-  const int lead = lead_tiles > 0 ? lead_tiles
-                                  : std::max(1, grid_for(int64_t(1) << 40, 1, fused_resident_blocks<NFEM_COEF_CELL>()) / 2);
-  int32_t* sched = h.data() + 4 + 2 * L.row_tiles;
+  // every row chunk after the record chunks it touches plus the lead
+  // (default: half the warps the GPU holds at once, so the record chunks a
+  // row chunk needs were taken about one round of all warps earlier)
+  const int64_t warps = int64_t(grid_for(int64_t(1) << 40, 1, fused_resident_blocks<NFEM_COEF_CELL>())) * kFusedWarps;
+  const int64_t lead = lead_chunks > 0 ? lead_chunks : std::max<int64_t>(1, warps / 2);
+  int32_t* sched = h.data() + 4 + L.row_chunks;
   int64_t q = 0, next_rec = 0;
-  for (int64_t j = 0; j < L.row_tiles; ++j) {
-    const int64_t hi = h[4 + 2 * j + 1];
-    if (hi >= L.rec_tiles || h[4 + 2 * j] < 0) return NFEM_ERR_PATTERN;
-    const int64_t upto = std::min<int64_t>(L.rec_tiles - 1, hi + lead);
+  for (int64_t j = 0; j < L.row_chunks; ++j) {
+    const int64_t hi = h[4 + j];
+    if (hi >= L.rec_chunks) return NFEM_ERR_PATTERN;
+    const int64_t upto = std::min<int64_t>(L.rec_chunks - 1, hi + lead);
     while (next_rec <= upto) sched[q++] = int32_t(next_rec++);
     sched[q++] = ~int32_t(j);
   }
-  while (next_rec < L.rec_tiles) sched[q++] = int32_t(next_rec++);
+  while (next_rec < L.rec_chunks) sched[q++] = int32_t(next_rec++);
   h[0] = int32_t(L.items);
-  h[1] = int32_t(L.rec_tiles);
-  h[2] = int32_t(L.row_tiles);
+  h[1] = int32_t(L.rec_chunks);
+  h[2] = int32_t(L.row_chunks);
   NFEM_TRY_CUDA(cudaMemcpyAsync(d, h.data(), size_t(L.sync_word) * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
   NFEM_TRY_CUDA(cudaStreamSynchronize(stream));
   return NFEM_OK;
@@ -2266,26 +2256,15 @@ extern "C" int nfem_darcy_rt1p0_assemble_fused(int64_t n_cells, int64_t n_rows, 
   p.row_f0 = 0;
   p.row_f1 = p_base;
   p.row_q0 = p.row_q1 = 0;
-  NFEM_TRY_CUDA(cudaMemsetAsync(words + L.sync_word, 0, size_t(1 + L.rec_tiles) * sizeof(int32_t), stream));
-  int per_sm = 0;
+  uint32_t* flags = reinterpret_cast<uint32_t*>(words + L.sync_word);
+  NFEM_TRY_CUDA(cudaMemsetAsync(flags, 0, size_t(L.rec_chunks) * sizeof(uint32_t), stream));
   switch (source_mode) {
-    case NFEM_COEF_NONE: per_sm = fused_resident_blocks<NFEM_COEF_NONE>(); break;
-    case NFEM_COEF_CELL: per_sm = fused_resident_blocks<NFEM_COEF_CELL>(); break;
-    case NFEM_COEF_QPOINT: per_sm = fused_resident_blocks<NFEM_COEF_QPOINT>(); break;
+    case NFEM_COEF_NONE: rc = launch_fused<NFEM_COEF_NONE>(p, words, flags, L.items, stream); break;
+    case NFEM_COEF_CELL: rc = launch_fused<NFEM_COEF_CELL>(p, words, flags, L.items, stream); break;
+    case NFEM_COEF_QPOINT: rc = launch_fused<NFEM_COEF_QPOINT>(p, words, flags, L.items, stream); break;
     default: return NFEM_ERR_INVALID_ARG;
   }
-  const int grid = grid_for(L.items * int64_t(kFusedThreads), kFusedThreads, per_sm);
-  switch (source_mode) {
-    case NFEM_COEF_NONE:
-      darcy_fused_kernel<NFEM_COEF_NONE><<<grid, kFusedThreads, 0, stream>>>(p, words, words + L.sync_word);
-      break;
-    case NFEM_COEF_CELL:
-      darcy_fused_kernel<NFEM_COEF_CELL><<<grid, kFusedThreads, 0, stream>>>(p, words, words + L.sync_word);
-      break;
-    default:
-      darcy_fused_kernel<NFEM_COEF_QPOINT><<<grid, kFusedThreads, 0, stream>>>(p, words, words + L.sync_word);
-      break;
-  }
+  if (rc) return rc;
   NFEM_CHECK_LAUNCH();
   return NFEM_OK;
 }

@@ -396,11 +396,12 @@ def test_darcy_f64_lattice_records(cuda_lib, name, qpoint):
 @pytest.mark.parametrize("qpoint,accumulate,lead", [(False, False, 0), (True, False, 0), (False, True, 0),
                                                     (False, False, 1), (False, False, 3)])
 def test_darcy_fused_equals_two_pass(cuda_lib, name, qpoint, accumulate, lead):
-    """The fused FP64 assembly (one persistent launch, record tiles and row
-    tiles from a plan, row tiles waiting on their record tiles' flags) writes
-    bitwise the values and residual of the two passes in turn: the same
-    record and row arithmetic, only scheduled differently.  A lead of 1 or 3
-    record tiles makes the row tiles wait on records still being formed."""
+    """The fused FP64 assembly (one persistent launch, record chunks and row
+    chunks from a plan, row chunks waiting on their record chunks' flags)
+    writes bitwise the values and residual of the two passes in turn: the
+    same record and row arithmetic, only scheduled differently.  A lead of 1
+    or 3 record chunks makes the row chunks wait on records still being
+    formed."""
     m = _lattice_meshes()[name]
     T = m["blocks"][-1][1].shape[0]
     rng = np.random.default_rng(T + 1)
