@@ -1155,7 +1155,8 @@ __device__ __forceinline__ void rows_body(const DarcyParams& p, T* st, int64_t r
 }
 
 template <typename T, int DIM, int SRC, bool REC = false>
-__global__ void __launch_bounds__(32 * kDarcyWarps, sizeof(T) == 4 ? NFEM_DARCY_MIN_BLOCKS : 1)
+__global__ void __launch_bounds__(32 * kDarcyWarps,
+                                  (sizeof(T) == 4 || (REC && DIM == 3)) ? NFEM_DARCY_MIN_BLOCKS : 1)
     darcy_rows_kernel(const DarcyParams p) {
   __shared__ __align__(16) T stage[kDarcyWarps][32 * kDarcyMaxRow];
   rows_body<T, DIM, SRC, REC>(p, stage[threadIdx.x >> 5], blockIdx.x, gridDim.x);
