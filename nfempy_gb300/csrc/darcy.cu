@@ -575,9 +575,11 @@ constexpr int kFinalWords = 10;
 //   U_ab = T120_ab * V * 2^(shift - k - e_kappa - e_det)
 // with kappa = m_kappa 2^e_kappa, |det| = m_det 2^e_det (m in [1, 2)) and
 // V = 1 / (30 m_kappa m_det) in double-float, turned into the 64-bit
-// fixed-point factor vq = V 2^68, normalised to [2^63, 2^64).  Each FP64
-// word is then one 32 x 64-bit high product packed into FP64 bits (within
-// one ulp of T120_ab V).  The same quantities as the double-float path,
+// FP64 factor vs = V 2^(shift - k - e_kappa - e_det).  Each FP64 word is
+// then the exact integer T120_ab (converted by bits) times vs: one FP64
+// multiply, within one ulp of T120_ab vs (the FP64 pipe runs these beside
+// the integer work; forming the product in 64-bit integer arithmetic took
+// about a third more instructions per cell).  The same quantities as the double-float path,
 // with fewer roundings and a fraction of its instructions.  (Keeping the
 // integers in the record and forming the words in the row pass instead
 // measured slower: the row pass needs 16 words per cell against 10 here,
@@ -628,12 +630,12 @@ __device__ __forceinline__ bool lattice_record(const DarcyParams& p, int64_t c, 
   const dfloat mdet = df_from_i64(static_cast<int64_t>(adet), e_det);
   const dfloat mkap = df_from_double(__longlong_as_double(static_cast<long long>((kb & 0xFFFFFFFFFFFFFull) |
                                                                                   (1023ull << 52))));
-  const uint64_t vq0 = df_to_u64_scaled(df_recip(df_mul_f(df_mul(mkap, mdet), 30.f)), 68);
-  const int lzv = df_clz64(vq0);
-  const uint64_t vq = vq0 << (lzv & 63);
-  const int ex = shift - k - e_kap - e_det - 68 - lzv;
-  if (adet != 0 && (ex < -1080 || ex > 920)) return false;
+  // V 2^ex as one FP64 number (V in (1/120, 1/30]); every word T120 V 2^ex
+  // with |T120| < 2^31 then stays a normal FP64 number
+  const int ex = shift - k - e_kap - e_det;
+  if (adet != 0 && (ex < -1010 || ex > 990)) return false;
   if (adet == 0) set_status(p.status, NFEM_ERR_DEGENERATE);
+  const double vs = df_to_double_scaled(df_recip(df_mul_f(df_mul(mkap, mdet), 30.f)), ex);
   const int32_t R[3] = {G[0][0] + G[0][1] + G[0][2], G[0][1] + G[1][1] + G[1][2], G[0][2] + G[1][2] + G[2][2]};
   const int32_t S = G[0][0] + G[1][1] + G[2][2] + R[0] + R[1] + R[2];
   // T120 in record order, converted and stored two words at a time
@@ -641,7 +643,8 @@ __device__ __forceinline__ bool lattice_record(const DarcyParams& p, int64_t c, 
     if (a == 0) return b == 0 ? S : S - 5 * R[b - 1];
     return S - 5 * (R[a - 1] + R[b - 1]) + 20 * G[a - 1][b - 1];
   };
-  auto word = [&](int a, int b) { return df_i32_times_q63(t120(a, b), vq, ex); };
+  // the exact integer as FP64 (by bits), times vs: one FP64 multiply per word
+  auto word = [&](int a, int b) { return df_i32_to_double(t120(a, b)) * vs; };
   const int64_t slot = rec_index(p, c);
   double2* o = reinterpret_cast<double2*>(static_cast<double*>(p.rec) + slot * kFinalWords);
   o[0] = make_double2(word(0, 0), word(0, 1));

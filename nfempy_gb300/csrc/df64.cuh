@@ -340,6 +340,15 @@ DF_HD double df_i32_times_q63(int32_t t, uint64_t vq, int e) {
   return t == 0 ? 0.0 : df_double(bits | (t < 0 ? 0x8000000000000000ull : 0ull));
 }
 
+// A 32-bit integer as FP64, exactly, by bits (no conversion instruction).
+DF_HD double df_i32_to_double(int32_t t) {
+  if (t == 0) return 0.0;
+  const uint32_t a = t < 0 ? 0u - static_cast<uint32_t>(t) : static_cast<uint32_t>(t);
+  const int lz = df_clz32(a);
+  const uint64_t frac = static_cast<uint64_t>(a << lz << 1) << 20;  // bits below the leading one
+  return df_double((t < 0 ? 0x8000000000000000ull : 0ull) | (static_cast<uint64_t>(1023 + 31 - lz) << 52) | frac);
+}
+
 // x 2^e as FP64 for a normalised double-float x (df_to_double, then the
 // exponent moved on the bits): results beyond the FP64 range become +-inf,
 // results below the normal range +-0 (no FP64 instruction).

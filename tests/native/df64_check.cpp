@@ -17,6 +17,7 @@ int main() {
   auto rnd = [&]() { return std::ldexp(u(g), ex(g)); };
   long double e_split = 0, e_pack = 0, e_add = 0, e_mul = 0, e_rec = 0, e_dot = 0, e_round = 0, e_i64 = 0;
   long double e_q64 = 0, e_prod = 0, e_scaled = 0;
+  bool i32_exact = true;
   std::uniform_int_distribution<int> tb(1, 31), eo(-1080, 920);
   std::uniform_int_distribution<int64_t> iq(-(int64_t(1) << 62), int64_t(1) << 62);
   std::uniform_int_distribution<int> sh(0, 120);
@@ -71,6 +72,11 @@ int main() {
       if (std::fabs(es) > 1e-300L && std::fabs(es) < 1e300L)
         e_scaled = std::fmax(e_scaled, std::fabs(((long double)rs - es) / es));
     }
+    // 32-bit integers to FP64 by bits: exact
+    {
+      const int32_t t = static_cast<int32_t>(g()) >> (it % 31);
+      if (nfem::df_i32_to_double(t) != static_cast<double>(t)) i32_exact = false;
+    }
     // packing of a normalised pair whose hi is a power of two and lo points below it
     dfloat q = nfem::quick_two_sum(std::ldexp(1.0f, ex(g)), -std::ldexp((float)std::fabs(u(g)), -30 + ex(g)));
     double qd = nfem::df_to_double(q);
@@ -79,5 +85,7 @@ int main() {
   std::printf("split %.9Le\nround %.9Le\npack %.9Le\nadd %.9Le\nmul %.9Le\nrecip %.9Le\ndot %.9Le\ni64 %.9Le\n",
               e_split, e_round, e_pack, e_add, e_mul, e_rec, e_dot, e_i64);
   std::printf("q64 %.9Le\nprod %.9Le\nscaled %.9Le\n", e_q64, e_prod, e_scaled);
+  std::printf("i32 %d\n", (i32_exact && nfem::df_i32_to_double(INT32_MIN) == -2147483648.0 &&
+                           nfem::df_i32_to_double(0) == 0.0 && nfem::df_i32_to_double(-1) == -1.0) ? 0 : 1);
   return 0;
 }

@@ -5,7 +5,8 @@ double-float split within 2^-48, 64-bit fixed-point integers within
 add / multiply / reciprocal / 3-term dot products within 2^-44 (operand
 splits included); for the lattice records, the 64-bit fixed-point factor
 within 2^-60, integer x fixed-point products packed into FP64 within one
-ulp (2^-52) and the scaled packing to half an ulp.  No GPU needed."""
+ulp (2^-52), the scaled packing to half an ulp and 32-bit integers to
+FP64 exactly.  No GPU needed."""
 import os
 import shutil
 import subprocess
@@ -29,5 +30,6 @@ def test_df64_routines_against_long_double():
     assert err["split"] <= 2.0 ** -48 and err["i64"] <= 2.0 ** -47
     assert err["round"] <= 2.0 ** -53 and err["pack"] <= 2.0 ** -53
     assert err["q64"] <= 2.0 ** -60 and err["prod"] <= 2.0 ** -52 and err["scaled"] <= 2.0 ** -53
+    assert err["i32"] == 0  # 32-bit integers to FP64 by bits, exactly
     for k in ("add", "mul", "recip", "dot"):
         assert err[k] <= 2.0 ** -44, (k, err[k])
