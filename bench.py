@@ -851,6 +851,36 @@ def batch2d_bench(args):
 
 
 # ------------------------------------------------------------------ GPU path
+def bind_host_near_gpu(dev):
+    """Keeps this process's host threads, and so the pinned buffers they
+    allocate for the end-to-end copies, on the NUMA node the GPU hangs off
+    when sysfs names one (a buffer on the far socket's memory crosses the
+    CPU-to-CPU link on every copy).  Returns what was done, or None."""
+    import torch
+    try:
+        pr = torch.cuda.get_device_properties(dev)
+        bdf = f"{pr.pci_domain_id:04x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0"
+        with open(f"/sys/bus/pci/devices/{bdf}/numa_node") as fh:
+            node = int(fh.read().strip())
+        if node < 0:
+            return None
+        with open(f"/sys/devices/system/node/node{node}/cpulist") as fh:
+            spec = fh.read().strip()
+        cpus = set()
+        for part in spec.split(","):
+            if "-" in part:
+                lo, hi = part.split("-")
+                cpus.update(range(int(lo), int(hi) + 1))
+            elif part:
+                cpus.add(int(part))
+        if not cpus:
+            return None
+        os.sched_setaffinity(0, cpus)
+        return {"numa_node": node, "cpus": len(cpus)}
+    except (OSError, ValueError, AttributeError):
+        return None
+
+
 def run_ours(args):
     rank, world, local = env_rank()
     cpu_prob = cpu_vec = cpu_solve = None
@@ -862,6 +892,7 @@ def run_ours(args):
     import numpy as np
     import torch
     torch.cuda.set_device(local)
+    host_affinity = bind_host_near_gpu(local)
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -1089,7 +1120,7 @@ def run_ours(args):
         "config": {"workload": f"darcy3d_rt1p0_cube{N_SIDE}x6", "n_cells": T, "n_points": V, "n_dof": n_dof,
                    "nnz": A.nnz, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "flushed before every timed step (256 MB write, outside the step events)",
-                   "bracket_ms_incl_flush": bracket_ms, "kernel": kernels},
+                   "bracket_ms_incl_flush": bracket_ms, "kernel": kernels, "host_affinity": host_affinity},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes": alg, "peak_source": peak_kind},
