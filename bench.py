@@ -782,13 +782,13 @@ def batch2d_bench(args):
     ach = alg / (ms * 1e-3) / 1e9
     out = {"metric": "DoF/s assembled", "value": sp.n_dof / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
            "problems": len(sides), "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz,
-           "kernel": "darcy_rows_kernel (one pass: triangles, FP32)",
+           "kernel": "darcy_records_kernel + darcy_rows_kernel (two passes: triangles, FP32)",
            "graph_replay_ms_per_step": graph_ms,
            "autotuned": {"config": best, "ms_per_step": tuned_ms, "candidates": len(tried),
                          "value": sp.n_dof / (tuned_ms * 1e-3), "cache": autotune.cache_path()},
            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                         "algorithmic_bytes": alg, "peak_source": kind,
-                        "traffic": profiled_traffic("darcy_rows_f32_batch512.txt")}}
+                        "traffic": profiled_traffic("darcy_records_rows_f32_batch512.txt")}}
     if not args.no_solve:
         # every problem at once: two-level FGMRES on the block-diagonal union,
         # aggregates of about s x s squares inside each problem (none spans

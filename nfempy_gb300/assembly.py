@@ -406,11 +406,11 @@ class LaplaceDualWeakForm(WeakForm):
     use_records: the row-owner kernel reads per-cell metric records from a
     first cell pass (True) instead of evaluating each (row, cell) incidence
     from the vertices (False); the values agree to rounding.  None (default)
-    takes the two passes for tetrahedra and for FP64, one pass for FP32
-    triangles, from measurements: 64^3 x 6 tets FP32 0.096 ms against
-    0.101 ms, FP64 0.50 ms against 1.12 ms (the geometry is evaluated once
-    per cell instead of once per incidence); the 512-problem triangle batch
-    FP32 0.280 ms against 0.250 ms (a triangle's geometry is cheap).
+    takes the two passes, from measurements: 64^3 x 6 tets FP32 0.096 ms
+    against 0.101 ms, FP64 0.50 ms against 1.12 ms (the geometry is
+    evaluated once per cell instead of once per incidence); the 512-problem
+    triangle batch FP32 0.245 ms against 0.291 ms once the cell pass writes
+    the pressure rows (before that, 0.280 against 0.250 ms).
     """
 
     cell_form = True
@@ -521,7 +521,7 @@ class LaplaceDualWeakForm(WeakForm):
         ws = None
         records = self.use_records
         if records is None:
-            records = sp.dim == 3 or dtype == torch.float64
+            records = True
         if records and not self.use_chunks:
             key = ("records", dtype)
             if key not in self._cache:
