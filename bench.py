@@ -746,7 +746,8 @@ def cosserat_bench(args):
 def batch2d_bench(args):
     """512 independent 2-D mixed Darcy problems (n_i ~ U{8..128} squares per
     side, 2 n_i^2 triangles, log K_i GRF with correlation length 0.1 and
-    sigma 1, f = 1) assembled in one launch over their disjoint union, FP32."""
+    sigma 1, f = 1) assembled together over their disjoint union (one cell pass,
+    one row pass), FP32."""
     import numpy as np
     import torch
     import nfempy_gb300 as nf

@@ -111,7 +111,7 @@ def union(meshes_list):
     first, so first-appearance numbering gives each mesh a contiguous range
     of every entity block and the assembled system is block diagonal up to
     that interleaving of blocks.  Used for batches of independent problems
-    assembled in one launch."""
+    assembled together (one cell pass and one row pass over all of them)."""
     dim = meshes_list[0]["dim"]
     pts, off = [], 0
     by_type = {}

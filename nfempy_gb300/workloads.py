@@ -5,7 +5,7 @@ darcy3d(n): unit cube, n^3 hexahedra x 6 Kuhn tetrahedra, RT1 x P0,
   sampled at cell centroids), source f = 1 per cell.  n = 64 gives
   1,572,864 tets, 4,743,168 DoF, nnz 36,200,448.
 darcy2d_batch(n_problems): a batch of independent 2-D mixed Darcy
-  problems assembled in one launch as one disjoint-union mesh: problem i is
+  problems assembled together as one disjoint-union mesh: problem i is
   the unit square with n_i x n_i squares x 2 triangles, n_i ~ U{8..128},
   log K_i a Gaussian random field (correlation length 0.1, sigma 1.0,
   seed + i) at the cell centroids, f = 1.  512 problems give about 15 M DoF.
