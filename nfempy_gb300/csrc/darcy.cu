@@ -148,9 +148,7 @@ __device__ __forceinline__ void cell_edges<double, 2>(const DarcyParams& p, int3
 // of the metric, the determinant and the element row then carries an exact
 // power of s, folded in once per incidence (element_row), which gives the
 // same rounded values as scaling each edge component.
-template <>
-__device__ __forceinline__ void cell_edges<float, 3>(const DarcyParams& p, int32_t c, float (&J)[3][3]) {
-  const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+__device__ __forceinline__ void cell_edges_of(const DarcyParams& p, const int4 v, float (&J)[3][3]) {
   const float4 r0 = packed_point(p.split, v.x), r1 = packed_point(p.split, v.y), r2 = packed_point(p.split, v.z),
                r3 = packed_point(p.split, v.w);
 #pragma unroll
@@ -159,6 +157,10 @@ __device__ __forceinline__ void cell_edges<float, 3>(const DarcyParams& p, int32
     J[1][d] = packed_diff(r2, r0, d, 1.f);
     J[2][d] = packed_diff(r3, r0, d, 1.f);
   }
+}
+template <>
+__device__ __forceinline__ void cell_edges<float, 3>(const DarcyParams& p, int32_t c, float (&J)[3][3]) {
+  cell_edges_of(p, __ldg(reinterpret_cast<const int4*>(p.cv) + c), J);
 }
 
 template <>
@@ -212,9 +214,10 @@ struct Incidence {
   uint32_t m;
 };
 
+// vpre: the cell's vertex ids already loaded (FP32 tetrahedra), or NULL
 template <typename T, int DIM, int SRC>
 __device__ __forceinline__ void load_incidence(const DarcyParams& p, int32_t c, bool need_geo,
-                                               Incidence<T, DIM>& x) {
+                                               Incidence<T, DIM>& x, const int4* vpre = nullptr) {
   const T* kappa = static_cast<const T*>(p.kappa);
   const T* src = static_cast<const T*>(p.source);
   x.m = __ldg(p.sign + c);
@@ -231,7 +234,14 @@ __device__ __forceinline__ void load_incidence(const DarcyParams& p, int32_t c, 
   check_positive(p.status, x.kap);
   check_finite(p.status, x.src);
   if (need_geo) {
-    cell_edges<T, DIM>(p, c, x.J);
+    if constexpr (sizeof(T) == 4 && DIM == 3) {
+      if (vpre)
+        cell_edges_of(p, *vpre, x.J);
+      else
+        cell_edges<T, DIM>(p, c, x.J);
+    } else {
+      cell_edges<T, DIM>(p, c, x.J);
+    }
   } else {
 #pragma unroll
     for (int i = 0; i < DIM; ++i)
@@ -527,11 +537,25 @@ __device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, co
 template <typename T, int DIM, int SRC>
 __device__ __forceinline__ void records_cells(const DarcyParams& p, int64_t t, int64_t nt) {
   const T u = edge_unit<T>(p);
-  for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
-    const PRowIn prow = load_prow(p, c);
-    Incidence<T, DIM> x;
-    load_incidence<T, DIM, SRC>(p, int32_t(c), true, x);
-    write_record<T, DIM, SRC>(p, c, x, u, prow);
+  if constexpr (sizeof(T) == 4 && DIM == 3) {
+    // the next cell's vertex ids one iteration ahead (as in the FP64 pass)
+    const int4* __restrict__ cv4 = reinterpret_cast<const int4*>(p.cv);
+    int4 v_next = p.cell_begin + t < p.cell_end ? __ldg(cv4 + p.cell_begin + t) : make_int4(0, 0, 0, 0);
+    for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
+      const int4 v = v_next;
+      if (c + nt < p.cell_end) v_next = __ldg(cv4 + c + nt);
+      const PRowIn prow = load_prow(p, c);
+      Incidence<T, DIM> x;
+      load_incidence<T, DIM, SRC>(p, int32_t(c), true, x, &v);
+      write_record<T, DIM, SRC>(p, c, x, u, prow);
+    }
+  } else {
+    for (int64_t c = p.cell_begin + t; c < p.cell_end; c += nt) {
+      const PRowIn prow = load_prow(p, c);
+      Incidence<T, DIM> x;
+      load_incidence<T, DIM, SRC>(p, int32_t(c), true, x);
+      write_record<T, DIM, SRC>(p, c, x, u, prow);
+    }
   }
 }
 
