@@ -16,10 +16,10 @@ def test_algorithmic_bytes_of_the_headline_workload():
 
 
 def test_profiled_traffic_is_read_from_the_summaries():
-    assert bench.profiled_traffic("darcy_records_rows_f32_cube64.txt") == 308_403_712
+    assert bench.profiled_traffic("darcy_records_rows_f32_cube64.txt") == 305_379_840
     assert bench.profiled_traffic("darcy_rows_f32_cube64.txt") == 314_387_200
     assert bench.profiled_traffic("elasticity_rows_f32_cube40.txt") == 711_353_344
-    assert bench.profiled_traffic("darcy_records_rows_f64_cube64.txt") == 625_478_400
+    assert bench.profiled_traffic("darcy_records_rows_f64_cube64.txt") == 625_029_632
     assert bench.profiled_traffic("darcy_records_rows_f32_batch512.txt") == 1_143_034_624
     assert bench.profiled_traffic("no_such_summary.txt") is None
 
