@@ -635,10 +635,6 @@ def elasticity_bench(args):
     ms = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
     A.check_status("elasticity bench")
     from nfempy_gb300 import autotune
-    autotune.set_knobs({"elas_rows": 4})  # images filled by shared-memory atomic adds, for comparison
-    ms_atomics = _time_assembly(lambda: wf.assemble(A, res, coefficients=coefs), args.steps, args.warmup)
-    autotune.reset_knobs()
-    A.check_status("elasticity bench, shared atomics")
     best, best_ms, tried = autotune.tune(f"elasticity_p2_f32_cells{sp.n_cells}",
                                          lambda: wf.assemble(A, res, coefficients=coefs),
                                          autotune.elasticity_candidates(), reps=max(3, args.steps // 4))
@@ -651,7 +647,6 @@ def elasticity_bench(args):
     ach = alg / (ms * 1e-3) / 1e9
     out = {"metric": "DoF/s assembled", "value": sp.n_dof / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
            "n_cells": T, "n_dof": sp.n_dof, "nnz": A.nnz, "kernel": "elasticity_rows_kernel",
-           "ms_per_step_shared_atomics": ms_atomics,
            "autotuned": {"config": best, "ms_per_step": tuned_ms, "candidates": len(tried)},
            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                         "algorithmic_bytes": alg, "peak_source": kind,

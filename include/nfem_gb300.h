@@ -70,10 +70,8 @@ const char* nfem_status_string(int status);
  *                                        accumulation by warp shuffles, 3
  *                                        (elasticity) registers for rows of at
  *                                        most 32 node columns and images for
- *                                        longer rows, 4 (elasticity) images
- *                                        with shared-memory atomic adds (not
- *                                        bitwise reproducible); 0 the built-in
- *                                        choice (shared-memory images)
+ *                                        longer rows; 0 the built-in choice
+ *                                        (shared-memory images)
  *   NFEM_KNOB_COARSE_TC                  trailing updates of the dense coarse
  *                                        inverse: 0 tensor cores (3xTF32) from
  *                                        512 aggregates on, 1 CUDA cores, 2

@@ -118,8 +118,7 @@ def darcy_candidates(dim):
 
 def elasticity_candidates():
     return ([{"form": {}, "knobs": {"elas_rows": 2}}, {"form": {}, "knobs": {"elas_rows": 3}}]
-            + [{"form": {}, "knobs": {"elas_rows": 1, "elas_warps": w}} for w in (2, 4, 8)]
-            + [{"form": {}, "knobs": {"elas_rows": 4, "elas_warps": w}} for w in (4, 8)])
+            + [{"form": {}, "knobs": {"elas_rows": 1, "elas_warps": w}} for w in (2, 4, 8)])
 
 
 def darcy_key(space, dtype):

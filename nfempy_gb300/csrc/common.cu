@@ -356,7 +356,7 @@ extern "C" int nfem_knob_set(int key, int value) {
       if (value != 0 && value != 2 && value != 4 && value != 8) return NFEM_ERR_INVALID_ARG;
       break;
     case NFEM_KNOB_ELAS_ROWS:
-      if (value < 0 || value > 4) return NFEM_ERR_INVALID_ARG;
+      if (value < 0 || value > 3) return NFEM_ERR_INVALID_ARG;
       break;
     case NFEM_KNOB_COARSE_TC:
       if (value < 0 || value > 2) return NFEM_ERR_INVALID_ARG;

@@ -69,11 +69,6 @@ struct ElasParams {
   // 2 degree > 32 only (the split form: register rows for the short edge
   // rows, shared-memory images for the long vertex rows)
   int deg_filter;
-  // 1: the three groups add their blocks into the one image at once with
-  // shared-memory atomic adds (a column two cells of the batch share then
-  // takes the two adds in the hardware's order); 0: in turn, plain
-  // read-modify-writes, bitwise deterministic
-  int atomic_rmw;
   int64_t n_cells;
   void* geom;  // [n_cells][12]: J^-1 (row-major, 9), lambda |det J|, mu |det J|, |det J|
   int64_t row0;  // first row of the space (dof_shift)
@@ -280,18 +275,7 @@ __global__ void __launch_bounds__(32 * WARPS) elasticity_rows_kernel(const ElasP
       }
       // add the 3 x 3 block at the node column: three images take every
       // group at once; one image takes the groups in turn (two cells of the
-      // node may share a column), the whole warp stepping together, or all
-      // groups at once through shared-memory atomics
-      if (kElasImages == 1 && p.atomic_rmw) {
-        if (act) {
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) atomicAdd(wimg + (i * deg + pos) * 4 + j, K[i][j]);
-        }
-        __syncwarp();
-        continue;
-      }
+      // node may share a column), the whole warp stepping together
 #pragma unroll
       for (int gg = 0; gg < (kElasImages == 1 ? 3 : 1); ++gg) {
         if (act && (kElasImages == 3 || g == gg)) {
@@ -663,7 +647,6 @@ extern "C" int nfem_elasticity_p2_assemble(int value_type, int64_t n_cells, int6
   p.deg_max = max_node_degree > 0 ? max_node_degree : kElasDegMax;
   if (p.deg_max > 255) return NFEM_ERR_UNSUPPORTED;  // node codes are bytes
   p.deg_filter = 0;
-  p.atomic_rmw = knob(NFEM_KNOB_ELAS_ROWS) == 4;
   if (knob(NFEM_KNOB_ELAS_ROWS) == 3 && p.deg_max <= 96) {
     // split: rows of at most 32 node columns in registers, longer rows in images
     p.deg_filter = 2;
