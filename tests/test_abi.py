@@ -112,11 +112,24 @@ def test_new_workspace_queries_and_argument_checks(lib_path):
     args = [0] * 26
     assert lib.nfem_darcy_rt1p0_assemble(4, 1, *args[2:]) == 1
     assert lib.nfem_darcy_rt1p0_assemble(3, 9, *args[2:]) == 1
-    # record workspace of the two-pass form: 8 FP32 words per cell, 12 / 8 FP64 words (3-D / 2-D)
+    # record workspace of the two-pass form: 8 FP32 words per cell, 11 / 8 FP64 words (3-D / 2-D)
     assert lib.nfem_darcy_workspace_bytes(3, _lib.NFEM_F32, 1000, ctypes.byref(b)) == 0 and b.value == 32000
     assert lib.nfem_darcy_workspace_bytes(3, _lib.NFEM_F64, 1000, ctypes.byref(b)) == 0 and b.value == 88000
     assert lib.nfem_darcy_workspace_bytes(2, _lib.NFEM_F64, 1000, ctypes.byref(b)) == 0 and b.value == 64000
     assert lib.nfem_darcy_workspace_bytes(4, _lib.NFEM_F32, 10, ctypes.byref(b)) == 1
+    # fused FP64 form: plan size (header, one word per 32-row chunk, the schedule, one flag
+    # per 32-cell chunk), and its checks before any device work
+    T, p_base = 1000, 2100
+    rec_chunks, row_chunks = -(-T // 32), -(-p_base // 32)
+    sync_word = (4 + row_chunks + rec_chunks + row_chunks + 3) // 4 * 4
+    assert lib.nfem_darcy_fused_plan_bytes(T, p_base, ctypes.byref(b)) == 0
+    assert b.value == 4 * (sync_word + rec_chunks)
+    assert lib.nfem_darcy_fused_plan_bytes(-1, p_base, ctypes.byref(b)) == 1
+    assert _lib.STATUS_NAMES[lib.nfem_darcy_fused_plan_bytes(2 ** 31, p_base, ctypes.byref(b))] == "NFEM_ERR_OVERFLOW"
+    assert lib.nfem_darcy_fused_plan(None, T, p_base, 0, None, 0, None) == 1             # no plan buffer
+    assert lib.nfem_darcy_fused_plan(dummy, T, p_base, -1, dummy, b.value, None) == 1    # negative lead
+    fused = [0] * 24
+    assert lib.nfem_darcy_rt1p0_assemble_fused(T, T + p_base + 1, *fused[2:]) == 1       # n_rows != p_base + T
 
 
 def test_two_level_ap_queries_and_argument_checks(lib_path):
