@@ -379,11 +379,6 @@ def solve_bench(args, A, wf, coefs, res, stream):
     t_struct = time.perf_counter() - t0
     ksp = KrylovSolver(A64, pc="two_level", A32_values=A.values, restart=args.tl_restart, two_level=tl)
     out["two_level_classical"] = _timed_solve(ksp, b, args, stream, two_level=True)
-    # the same solver again (setup and solve; the restart-cycle graph, captured
-    # during the first solve, is replayed): a sequence of solves on one pattern
-    again = _timed_solve(ksp, b, args, stream, two_level=True)
-    out["two_level_classical"]["repeat"] = {k: again[k] for k in ("setup_ms", "solve_ms", "time_to_solve_ms",
-                                                                  "inner_iterations", "final_relres_fp64")}
     out["two_level_classical"]["host_structure_s"] = t_struct
     out["two_level_classical"]["host_structure_first_call_s"] = t_first
     out["two_level_classical"]["aggregates"] = tl.n_agg
