@@ -2419,19 +2419,25 @@ extern "C" int nfem_solve_ir_fgmres(const nfem_csr* A64, const nfem_csr* A32, co
       scale_by_inv_w<<<gv, B, 0, s>>>(n, w.V, w.scal + 2, w.V, weighted ? pc->winvsqrt : nullptr, w.t32, nullptr);
       init_cycle<<<1, 128, 0, s>>>(w.g, m, w.scal + 2, w.gate);
       NFEM_CHECK_LAUNCH();
-      if (graphs && cycle_graph.exec == nullptr && !first_solve_cycle) {
-        // second cycle onwards: the m steps as one CUDA graph, captured once
-        // on a private stream (the caller's may be the legacy stream) and
-        // replayed on `s` every cycle; the launch sequence is fixed (the
-        // gate ends a converged cycle's work on the device)
-        NFEM_RC(cycle_graph.capture([&](cudaStream_t cs_) {
+      // Second cycle onwards: the m steps as one CUDA graph, captured once on
+      // a private stream (the caller's may be the legacy stream) and
+      // replayed on `s` every cycle; the launch sequence is fixed (the gate
+      // ends a converged cycle's work on the device).  Large systems capture
+      // it right after launching the first cycle, so the host's capture and
+      // instantiation overlap that cycle on the GPU; small ones at the second
+      // cycle, so a solve of one cycle captures nothing.
+      auto capture = [&]() {
+        return cycle_graph.capture([&](cudaStream_t cs_) {
           return arnoldi_steps(pc, A32, n, ld, m, ldh, w, weighted, gv, cs_);
-        }));
-      }
+        });
+      };
+      const bool early_capture = n >= (int64_t(1) << 20);
+      if (graphs && cycle_graph.exec == nullptr && !first_solve_cycle && !early_capture) NFEM_RC(capture());
       if (cycle_graph.exec) {
         NFEM_TRY_CUDA(cudaGraphLaunch(cycle_graph.exec, s));
       } else {
         NFEM_RC(arnoldi_steps(pc, A32, n, ld, m, ldh, w, weighted, gv, s));
+        if (graphs && early_capture && cycle_graph.exec == nullptr) NFEM_RC(capture());
       }
       first_solve_cycle = false;
       // one synchronisation per cycle: residual estimates of every step
