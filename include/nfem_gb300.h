@@ -324,7 +324,11 @@ int nfem_darcy_rt1p0_assemble(int dim, int value_type, int64_t n_cells, int64_t 
  * 11 words) and the row pass reads them in place of the vertices; the
  * values agree with the one pass to rounding (the same expressions, fused
  * alike or not).  The cell pass also writes each cell's pressure row
- * (row p_base + c).  NULL: one pass that evaluates every (row, cell) incidence from the
+ * (row p_base + c).  FP32 cells of poor shape quality (|det J| below 0.1
+ * times the product of their edge lengths from vertex 0) are finished by a
+ * second launch that takes |det J| in FP64 from `points` (or from the
+ * fixed-point records when `points` is NULL); the FP32 workspace holds
+ * their list (4 bytes per cell and 16).  NULL: one pass that evaluates every (row, cell) incidence from the
  * vertices.  The workspace is 16-byte aligned, of at least this size. */
 int nfem_darcy_workspace_bytes(int dim, int value_type, int64_t n_cells, size_t* bytes);
 

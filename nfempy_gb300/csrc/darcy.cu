@@ -82,6 +82,7 @@ struct DarcyParams {
   int lattice;           // FP64 tetrahedra: exact integer records for lattice cells (lattice_record)
   int prow;              // the cell pass writes each cell's pressure row (pressure_row); the row pass skips them
   int64_t rp_off;        // FP64 tetrahedra: r_p of record slot s at ((double*)rec)[rp_off + s]
+  int32_t* bad;          // FP32 records: [0] count, [4 ..] cells left to darcy_refine_kernel (NULL: none)
   // Work ranges of one launch: the cell pass covers cells [cell_begin,
   // cell_end); the row pass covers the rows [row_f0, row_f1) and then
   // [row_q0, row_q1) (flux rows and pressure rows of one cell slice, or all
@@ -212,7 +213,75 @@ struct Incidence {
   T kap;
   T src;
   uint32_t m;
+  int32_t c;  // the cell (for the FP64 |det J| of badly shaped cells)
 };
+
+// Badly shaped cells in FP32.  |det J| from FP32 edges carries a relative
+// error of a few ulps divided by the cell's shape quality
+//   q = |det J| / (|e_0| ... |e_{DIM-1}|)   (q^2 for the 2-D sqrt form),
+// which reaches 1e-5 near q ~ 1e-2 (flat or needle cells in general
+// orientation).  In the two-pass assembly the cell pass leaves cells with
+// q < 0.1 to a follow-up launch over their list (darcy_refine_kernel),
+// which takes their |det J| in FP64: from the FP64 points when the caller
+// passed them (exactly rounded edge differences), else from the 32-bit
+// fixed-point records (exact integer differences); their records and
+// pressure rows are then formed as for any other cell.  The opt-in one-pass,
+// cell-chunk and sliced forms keep FP32.  In edge units, like abs_det.
+constexpr float kSliverQ = 0.1f;
+
+template <int DIM>
+__device__ __noinline__ float refine_det(const DarcyParams& p, int32_t c) {
+  int vs[DIM + 1];
+  if constexpr (DIM == 3) {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+    vs[0] = v.x;
+    vs[1] = v.y;
+    vs[2] = v.z;
+    vs[3] = v.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) vs[k] = __ldg(p.cv + int64_t(c) * 3 + k);
+  }
+  double e[DIM][3];
+  double unit = 1.0;  // edge units per FP64 coordinate unit
+  if (p.points) {
+    unit = 1.0 / double(packed_lo_scale(p.split));
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        e[k][d] = __ldg(p.points + int64_t(vs[k + 1]) * 3 + d) - __ldg(p.points + int64_t(vs[0]) * 3 + d);
+  } else {
+    const float4 r0 = packed_point(p.split, vs[0]);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      const float4 r = packed_point(p.split, vs[k + 1]);
+      e[k][0] = double(int64_t(__float_as_int(r.x)) - __float_as_int(r0.x));
+      e[k][1] = double(int64_t(__float_as_int(r.y)) - __float_as_int(r0.y));
+      e[k][2] = double(int64_t(__float_as_int(r.z)) - __float_as_int(r0.z));
+    }
+  }
+  double det;
+  if constexpr (DIM == 3) {
+    det = e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) - e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
+          e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
+    det *= unit * unit * unit;
+  } else {
+    const double x = e[0][1] * e[1][2] - e[0][2] * e[1][1], y = e[0][2] * e[1][0] - e[0][0] * e[1][2],
+                 z = e[0][0] * e[1][1] - e[0][1] * e[1][0];
+    det = sqrt(x * x + y * y + z * z) * unit * unit;
+  }
+  return float(det < 0.0 ? -det : det);
+}
+
+// The cell's shape quality q from its FP32 metric, by reciprocal square
+// roots (the edge units put |e|^6 beyond the FP32 range)
+template <int DIM>
+__device__ __forceinline__ float shape_quality(float det, const float (&G)[DIM][DIM]) {
+  float q = det * rsqrtf(G[0][0]) * rsqrtf(G[1][1]);
+  if constexpr (DIM == 3) q *= rsqrtf(G[2][2]);
+  return q;
+}
 
 // vpre: the cell's vertex ids already loaded (FP32 tetrahedra), or NULL
 template <typename T, int DIM, int SRC>
@@ -221,6 +290,7 @@ __device__ __forceinline__ void load_incidence(const DarcyParams& p, int32_t c, 
   const T* kappa = static_cast<const T*>(p.kappa);
   const T* src = static_cast<const T*>(p.source);
   x.m = __ldg(p.sign + c);
+  x.c = c;
   x.kap = __ldg(kappa + c);
   x.src = T(0);
   if constexpr (SRC == NFEM_COEF_CELL) x.src = __ldg(src + c);
@@ -464,10 +534,11 @@ __device__ __forceinline__ void pressure_row(const DarcyParams& p, int64_t c, T 
 }
 
 // Record of cell c from its loaded incidence (see the layout above), and
-// its pressure row when p.prow is set.
+// its pressure row when p.prow is set.  det_in > 0: |det J| (edge units)
+// already formed in FP64 by the follow-up launch of badly shaped cells.
 template <typename T, int DIM, int SRC>
 __device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, const Incidence<T, DIM>& x, T u,
-                                             const PRowIn& prow) {
+                                             const PRowIn& prow, T det_in = T(0)) {
   using L = RecLayout<T, DIM>;
   constexpr int NW = L::n;
   using C = DarcyConst<T, DIM>;
@@ -477,7 +548,18 @@ __device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, co
   for (int i = 0; i < DIM; ++i)
 #pragma unroll
     for (int j = 0; j < DIM; ++j) G[i][j] = x.J[i][0] * x.J[j][0] + x.J[i][1] * x.J[j][1] + x.J[i][2] * x.J[j][2];
-  const T det = abs_det<T, DIM>(x.J, G);
+  T det = det_in;
+  if (!(det > T(0))) {
+    det = abs_det<T, DIM>(x.J, G);
+    if constexpr (sizeof(T) == 4) {
+      if (p.bad && det > T(0) && shape_quality<DIM>(det, G) < kSliverQ) {
+        // left to darcy_refine_kernel (FP64 |det J|): no record, no pressure row here
+        const int32_t k = atomicAdd(p.bad, 1);
+        p.bad[4 + k] = int32_t(c);
+        return;
+      }
+    }
+  }
   if (!(det > T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
   const T det_true = DIM == 3 ? det * (u * u * u) : det * (u * u);
   const T scale = T(C::kappa2) * recip(x.kap * (DIM == 3 ? det * u : det));
@@ -562,6 +644,22 @@ __device__ __forceinline__ void records_cells(const DarcyParams& p, int64_t t, i
 template <typename T, int DIM, int SRC>
 __global__ void __launch_bounds__(512) darcy_records_kernel(const DarcyParams p) {
   records_cells<T, DIM, SRC>(p, blockIdx.x * int64_t(blockDim.x) + threadIdx.x, int64_t(gridDim.x) * blockDim.x);
+}
+
+// The FP32 cells the cell pass left (shape quality below kSliverQ): |det J|
+// in FP64, then the record and pressure row as in the cell pass.  The count
+// is read on the device, so the launch needs no host round trip.
+template <int DIM, int SRC>
+__global__ void darcy_refine_kernel(const DarcyParams p) {
+  const int32_t n = p.bad[0];
+  const float u = edge_unit<float>(p);
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int32_t c = p.bad[4 + i];
+    const PRowIn prow = load_prow(p, c);
+    Incidence<float, DIM> x;
+    load_incidence<float, DIM, SRC>(p, c, true, x);
+    write_record<float, DIM, SRC>(p, c, x, u, prow, refine_det<DIM>(p, c));
+  }
 }
 
 // ------------------------------------------------------------------ FP64 tetrahedra
@@ -1477,7 +1575,13 @@ static void launch_cell_pass(const DarcyParams& p, cudaStream_t stream) {
     static int per_sm[4] = {0, 0, 0, 0};  // blocks of 64, 128, 256, 512 threads
     const int slot = cb == 512 ? 3 : (cb == 256 ? 2 : (cb == 128 ? 1 : 0));
     if (!per_sm[slot]) per_sm[slot] = resident_blocks(darcy_records_kernel<T, DIM, SRC>, cb);
+    if constexpr (sizeof(T) == 4) {
+      if (p.bad) cudaMemsetAsync(p.bad, 0, sizeof(int32_t), stream);
+    }
     darcy_records_kernel<T, DIM, SRC><<<grid_for(nc, cb, per_sm[slot]), cb, 0, stream>>>(p);
+    if constexpr (sizeof(T) == 4) {
+      if (p.bad) darcy_refine_kernel<DIM, SRC><<<grid_for(nc, 128, 1), 128, 0, stream>>>(p);
+    }
   }
 }
 
@@ -1605,8 +1709,11 @@ using namespace nfem;
 extern "C" int nfem_darcy_workspace_bytes(int dim, int value_type, int64_t n_cells, size_t* bytes) {
   if (!bytes || (dim != 2 && dim != 3) || (value_type != NFEM_F64 && value_type != NFEM_F32) || n_cells < 0)
     return NFEM_ERR_INVALID_ARG;
-  // FP32: 8 words per cell; FP64: 10 + 1 (tetrahedra: the words, then r_p) or 8 (triangles)
-  *bytes = value_type == NFEM_F64 ? size_t(n_cells) * (dim == 3 ? 11 : 8) * 8 : size_t(n_cells) * 8 * 4;
+  // FP32: 8 words per cell, then the list of badly shaped cells (a count
+  // and one index per cell); FP64: 10 + 1 (tetrahedra: the words, then r_p)
+  // or 8 (triangles)
+  *bytes = value_type == NFEM_F64 ? size_t(n_cells) * (dim == 3 ? 11 : 8) * 8
+                                  : size_t(n_cells) * 8 * 4 + (size_t(n_cells) + 4) * 4;
   return NFEM_OK;
 }
 
@@ -1654,6 +1761,7 @@ static int darcy_build(DarcyParams& p, int dim, int value_type, int64_t n_cells,
   for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
   p.rec = nullptr;
   p.rp_off = 0;
+  p.bad = nullptr;
   p.fixed = nullptr;
   p.lattice = knob(NFEM_KNOB_DARCY_F64_RECORDS) == 0;
   p.prow = 0;
@@ -1674,6 +1782,7 @@ static int darcy_build(DarcyParams& p, int dim, int value_type, int64_t n_cells,
       return NFEM_ERR_WORKSPACE;
     p.rec = workspace;
     p.rp_off = kFinalWords * n_cells;
+    if (value_type == NFEM_F32) p.bad = reinterpret_cast<int32_t*>(static_cast<float*>(workspace) + int64_t(n_cells) * 8);
   }
   return NFEM_OK;
 }
@@ -1820,6 +1929,7 @@ extern "C" int nfem_darcy_rt1p0_assemble_sliced(int value_type, int64_t n_cells,
   p.n_qp = source_mode == NFEM_COEF_QPOINT ? n_qp : 0;
   for (int i = 0; i < 32; ++i) p.qw[i] = (i < p.n_qp) ? qweights[i] : 0.0;
   p.rec = ring;
+  p.bad = nullptr;  // the overlapped form keeps FP32 |det J| for every cell
   p.rp_off = int64_t(kFinalWords) * (int64_t(3) << shift);
   p.ring_shift = shift;
   if (value_type == NFEM_F64) {

@@ -116,6 +116,56 @@ __device__ __forceinline__ void tet_edges<float>(const ElasParams& p, int32_t c,
   }
 }
 
+// J^-1 (row-major, g[0..8]) and det J of the edge matrix J (columns = edges)
+template <typename T>
+__device__ __forceinline__ T inverse_det(const T (&J)[3][3], T (&g)[12]) {
+  const T c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  const T c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  const T c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  const T det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+  const T id = T(1) / det;
+  g[0] = c00 * id;
+  g[3] = c01 * id;
+  g[6] = c02 * id;
+  g[1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+  g[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+  g[7] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+  g[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+  g[5] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+  g[8] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+  return det;
+}
+
+// Badly shaped cells in FP32: det J and J^-1 from FP32 edges carry a
+// relative error of a few ulps over the shape quality q = |det J| /
+// (|e_0| |e_1| |e_2|); cells with q < 0.1 take both in FP64, from the FP64
+// points when the caller passed them, else from the fixed-point records'
+// exact integer differences, rounded to FP32 once at the end.
+constexpr float kElasSliverQ = 0.1f;
+
+__device__ __noinline__ float refine_inverse(const ElasParams& p, int32_t c, float (&gf)[12]) {
+  double J[3][3];
+  if (p.points) {
+    tet_edges<double>(p, c, J);
+  } else {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+    const double s = double(packed_lo_scale(p.split));
+    const float4 r0 = packed_point(p.split, v.x);
+    const float4 r[3] = {packed_point(p.split, v.y), packed_point(p.split, v.z), packed_point(p.split, v.w)};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      J[0][k] = double(int64_t(__float_as_int(r[k].x)) - __float_as_int(r0.x)) * s;
+      J[1][k] = double(int64_t(__float_as_int(r[k].y)) - __float_as_int(r0.y)) * s;
+      J[2][k] = double(int64_t(__float_as_int(r[k].z)) - __float_as_int(r0.z)) * s;
+    }
+  }
+  double g[12];
+  const double det = inverse_det<double>(J, g);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) gf[k] = float(g[k]);
+  return float(det);
+}
+
 // Per-cell geometry, once per cell (every cell is read by the rows of its
 // ten nodes): J^-1, lambda |det J|, mu |det J|, |det J|.
 template <typename T>
@@ -127,23 +177,17 @@ __global__ void elas_geom_kernel(const ElasParams p) {
        c += int64_t(gridDim.x) * blockDim.x) {
     T J[3][3];
     tet_edges<T>(p, int32_t(c), J);
-    const T c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-    const T c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-    const T c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-    const T det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-    if (!(det != T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
-    const T id = T(1) / det;
-    const T adet = det < T(0) ? -det : det;
     T g[12];
-    g[0] = c00 * id;
-    g[3] = c01 * id;
-    g[6] = c02 * id;
-    g[1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-    g[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-    g[7] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-    g[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-    g[5] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-    g[8] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+    T det = inverse_det<T>(J, g);
+    if constexpr (sizeof(T) == 4) {
+      const T n0 = J[0][0] * J[0][0] + J[1][0] * J[1][0] + J[2][0] * J[2][0];
+      const T n1 = J[0][1] * J[0][1] + J[1][1] * J[1][1] + J[2][1] * J[2][1];
+      const T n2 = J[0][2] * J[0][2] + J[1][2] * J[1][2] + J[2][2] * J[2][2];
+      const T q = (det < T(0) ? -det : det) * rsqrtf(n0) * rsqrtf(n1) * rsqrtf(n2);
+      if (q < T(kElasSliverQ)) det = refine_inverse(p, int32_t(c), g);
+    }
+    if (!(det != T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
+    const T adet = det < T(0) ? -det : det;
     const T lam_c = __ldg(lam + c), mu_c = __ldg(mu + c);
     check_finite(p.status, lam_c);
     check_positive(p.status, mu_c);

@@ -112,8 +112,9 @@ def test_new_workspace_queries_and_argument_checks(lib_path):
     args = [0] * 26
     assert lib.nfem_darcy_rt1p0_assemble(4, 1, *args[2:]) == 1
     assert lib.nfem_darcy_rt1p0_assemble(3, 9, *args[2:]) == 1
-    # record workspace of the two-pass form: 8 FP32 words per cell, 11 / 8 FP64 words (3-D / 2-D)
-    assert lib.nfem_darcy_workspace_bytes(3, _lib.NFEM_F32, 1000, ctypes.byref(b)) == 0 and b.value == 32000
+    # record workspace of the two-pass form: 8 FP32 words per cell and the list of badly shaped
+    # cells (a count, one index per cell), 11 / 8 FP64 words (3-D / 2-D)
+    assert lib.nfem_darcy_workspace_bytes(3, _lib.NFEM_F32, 1000, ctypes.byref(b)) == 0 and b.value == 32000 + 4016
     assert lib.nfem_darcy_workspace_bytes(3, _lib.NFEM_F64, 1000, ctypes.byref(b)) == 0 and b.value == 88000
     assert lib.nfem_darcy_workspace_bytes(2, _lib.NFEM_F64, 1000, ctypes.byref(b)) == 0 and b.value == 64000
     assert lib.nfem_darcy_workspace_bytes(4, _lib.NFEM_F32, 10, ctypes.byref(b)) == 1

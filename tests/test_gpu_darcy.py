@@ -426,3 +426,48 @@ def test_darcy_fused_equals_two_pass(cuda_lib, name, qpoint, accumulate, lead):
         out.append((A.values.clone(), res.clone()))
     assert torch.equal(out[0][0], out[1][0])
     assert torch.equal(out[0][1], out[1][1])
+
+
+def _badly_shaped(gen, n, flat):
+    """A mesh of flat cells in general orientation: cube(n) squeezed by
+    `flat` along z and rotated (tetrahedra of shape quality ~ flat), or
+    square(n) squeezed along y and turned in its plane (triangles with
+    angles ~ flat)."""
+    m = getattr(mesh_gen, gen)(n)
+    pts = m["points"].copy()
+    if gen == "cube":
+        pts[:, 2] *= flat
+        a, b, c = 0.3, 0.7, 1.1
+        Rx = np.array([[1, 0, 0], [0, np.cos(a), -np.sin(a)], [0, np.sin(a), np.cos(a)]])
+        Ry = np.array([[np.cos(b), 0, np.sin(b)], [0, 1, 0], [-np.sin(b), 0, np.cos(b)]])
+        Rz = np.array([[np.cos(c), -np.sin(c), 0], [np.sin(c), np.cos(c), 0], [0, 0, 1]])
+        pts = pts @ (Rz @ Ry @ Rx).T
+    else:
+        pts[:, 1] *= flat
+        t = 0.6
+        xy = pts[:, :2] @ np.array([[np.cos(t), -np.sin(t)], [np.sin(t), np.cos(t)]]).T
+        pts = np.column_stack([xy, pts[:, 2]])
+    return dict(m, points=pts)
+
+
+@pytest.mark.parametrize("gen,n,flat", [("cube", 3, 1 / 512), ("cube", 4, 1 / 4096), ("square", 6, 1 / 512)])
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
+def test_darcy_badly_shaped_cells(cuda_lib, gen, n, flat, dtype, tol):
+    """Flat cells in general orientation (shape quality q ~ 1e-3 .. 1e-4),
+    where |det J| from FP32 edges would be off by a few ulps / q: the FP32
+    cell pass leaves them to the follow-up launch, which takes |det J| in
+    FP64 from the points; FP64 runs its double-float records.  Both against
+    the FP64 oracle at their usual tolerance."""
+    m = _badly_shaped(gen, n, flat)
+    T = m["blocks"][-1][1].shape[0]
+    rng = np.random.default_rng(T + 7)
+    kappa = np.exp(rng.normal(0.0, 1.0, T))
+    f_cell = rng.normal(0.0, 1.0, T)
+    sp, A, res = assemble_gpu(m, kappa, f_cell, dtype, use_slices=False)
+    A.check_status("badly shaped")
+    Ao, ro, *_ = darcy_oracle(m, kappa, f_cell=f_cell)
+    Ag = A.to_scipy()
+    np.testing.assert_array_equal(Ag.indptr, Ao.indptr)
+    assert row_scaled_err(Ag, Ao) <= tol
+    rg = res.double().cpu().numpy()
+    assert np.abs(rg - ro).max() <= tol * np.abs(ro).max()

@@ -47,8 +47,8 @@ def test_elasticity_matches_oracle(cuda_lib, dtype, tol, n, rows):
         autotune.reset_knobs()
 
 
-def _check_elasticity(dtype, tol, n):
-    m = mesh_gen.cube(n)
+def _check_elasticity(dtype, tol, n, mesh=None):
+    m = mesh_gen.cube(n) if mesh is None else mesh
     T = m["blocks"][-1][1].shape[0]
     rng = np.random.default_rng(n)
     lam = np.exp(rng.normal(0, 0.5, T))
@@ -70,6 +70,16 @@ def _check_elasticity(dtype, tol, n):
     assert row_scaled_err(Ag, Ao) <= tol
     rg = res.double().cpu().numpy()
     assert np.abs(rg - ro).max() <= tol * np.abs(ro).max()
+
+
+@pytest.mark.parametrize("flat", [1 / 512, 1 / 4096])
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
+def test_elasticity_badly_shaped_cells(cuda_lib, flat, dtype, tol):
+    """Flat tetrahedra in general orientation (shape quality ~ flat): the
+    FP32 geometry pass takes J^-1 and det J of such cells in FP64 from the
+    points.  Against the FP64 oracle at the usual tolerance."""
+    from tests.test_gpu_darcy import _badly_shaped
+    _check_elasticity(dtype, tol, 2, mesh=_badly_shaped("cube", 2, flat))
 
 
 def test_elasticity_penalty_matches_oracle(cuda_lib):
