@@ -201,7 +201,13 @@ __device__ __forceinline__ T abs_det(const T (&J)[DIM][3], const T (&G)[DIM][DIM
           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
     return d < T(0) ? -d : d;
   } else {
-    return sqrt(G[0][0] * G[1][1] - G[0][1] * G[0][1]);
+    // |e_0 x e_1| from the edges (not sqrt(G00 G11 - G01^2), whose
+    // difference loses a relative eps / q^2 on thin triangles against
+    // eps / q here)
+    (void)G;
+    const T x = J[0][1] * J[1][2] - J[0][2] * J[1][1], y = J[0][2] * J[1][0] - J[0][0] * J[1][2],
+            z = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    return sqrt(x * x + y * y + z * z);
   }
 }
 
@@ -272,6 +278,24 @@ __device__ __noinline__ float refine_det(const DarcyParams& p, int32_t c) {
     det = sqrt(x * x + y * y + z * z) * unit * unit;
   }
   return float(det < 0.0 ? -det : det);
+}
+
+// |det J| of tetrahedron c in FP64 from the FP64 points (exactly rounded
+// edge differences, hardware FP64 arithmetic): the FP64 path's badly shaped
+// cells, where double-float cancellation in the triple product would exceed
+// FP64's own error (a few ulps over q, like the reference's QR).
+__device__ __noinline__ double refine_det64(const DarcyParams& p, int64_t c) {
+  const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+  const int vs[4] = {v.x, v.y, v.z, v.w};
+  double e[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      e[k][d] = __ldg(p.points + int64_t(vs[k + 1]) * 3 + d) - __ldg(p.points + int64_t(vs[0]) * 3 + d);
+  const double det = e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) -
+                     e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) + e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
+  return det < 0.0 ? -det : det;
 }
 
 // The cell's shape quality q from its FP32 metric, by reciprocal square
@@ -860,7 +884,11 @@ __device__ __forceinline__ void record_df_cell(const DarcyParams& p, int64_t c, 
     cr[1] = df_dot<2>(a1, b1, pm);
     cr[2] = df_dot<2>(a2, b2, pm);
   }
-  const dfloat det = df_abs(df_dot<3>(E[0], cr, one));
+  dfloat det = df_abs(df_dot<3>(E[0], cr, one));
+  // a badly shaped cell: |det J| in FP64 from the points (df_dot's error
+  // over the shape quality would exceed FP64's own)
+  if (det.hi > 0.f && det.hi * rsqrtf(G[0][0].hi) * rsqrtf(G[1][1].hi) * rsqrtf(G[2][2].hi) < kSliverQ)
+    det = df_from_double(refine_det64(p, c));
   if (!(det.hi > 0.f)) set_status(p.status, NFEM_ERR_DEGENERATE);
   // row sums R_i, S = tr G + sum G
   dfloat R[3];
