@@ -33,11 +33,19 @@ def cell_jacobians(X):
     """Vectorised affine Jacobians: X [T, d+1, 3] -> J [T, 3, d], |det| [T], J+ [T, d, 3].
 
     Same quantities as evaluate_mapping (constant over the cell for affine
-    simplices); |det| = sqrt(det(J^T J)), J+ = (J^T J)^-1 J^T, which equal the
-    QR forms above for full-rank J.
+    simplices), formed as stably as the QR forms above: for tetrahedra
+    |det| = |det J| (LU) and J+ = J^-1; for triangles in R^3 |det| =
+    |J[:, 0] x J[:, 1]| and J+ = (J^T J)^-1 J^T.  (|det| = sqrt(det(J^T J))
+    would lose a relative eps / q^2 on cells of shape quality q, the QR form
+    and these eps / q.)
     """
     J = np.transpose(X[:, 1:, :] - X[:, :1, :], (0, 2, 1))
-    G = np.einsum("tgi,tgj->tij", J, J)
-    det = np.sqrt(np.linalg.det(G))
-    pinv = np.linalg.solve(G, np.transpose(J, (0, 2, 1)))
+    if J.shape[2] == 3:
+        det = np.abs(np.linalg.det(J))
+        pinv = np.linalg.inv(J)
+    else:
+        G = np.einsum("tgi,tgj->tij", J, J)
+        det = np.linalg.norm(np.cross(J[:, :, 0], J[:, :, 1]), axis=1) if J.shape[2] == 2 else np.sqrt(
+            np.linalg.det(G))
+        pinv = np.linalg.solve(G, np.transpose(J, (0, 2, 1)))
     return J, det, pinv
