@@ -226,14 +226,18 @@ struct Incidence {
 // error of a few ulps divided by the cell's shape quality
 //   q = |det J| / (|e_0| ... |e_{DIM-1}|)   (q^2 for the 2-D sqrt form),
 // which reaches 1e-5 near q ~ 1e-2 (flat or needle cells in general
-// orientation).  In the two-pass assembly the cell pass leaves cells with
-// q < 0.1 to a follow-up launch over their list (darcy_refine_kernel),
+// orientation); and an edge shorter than 2^20 units of the fixed-point
+// records carries a relative error above 2^-21 from their rounding, which
+// |det J| inherits in proportion.  In the two-pass assembly the cell pass
+// leaves cells with q < 0.1 or an edge below 2^20 units to a follow-up
+// launch over their list (darcy_refine_kernel),
 // which takes their |det J| in FP64: from the FP64 points when the caller
 // passed them (exactly rounded edge differences), else from the 32-bit
 // fixed-point records (exact integer differences); their records and
 // pressure rows are then formed as for any other cell.  The opt-in one-pass,
 // cell-chunk and sliced forms keep FP32.  In edge units, like abs_det.
 constexpr float kSliverQ = 0.1f;
+constexpr float kShortEdge2 = 1099511627776.0f;  // (2^20 edge units)^2
 
 template <int DIM>
 __device__ __noinline__ float refine_det(const DarcyParams& p, int32_t c) {
@@ -576,7 +580,9 @@ __device__ __forceinline__ void write_record(const DarcyParams& p, int64_t c, co
   if (!(det > T(0))) {
     det = abs_det<T, DIM>(x.J, G);
     if constexpr (sizeof(T) == 4) {
-      if (p.bad && det > T(0) && shape_quality<DIM>(det, G) < kSliverQ) {
+      T g_min = G[0][0] < G[1][1] ? G[0][0] : G[1][1];
+      if constexpr (DIM == 3) g_min = g_min < G[2][2] ? g_min : G[2][2];
+      if (p.bad && det > T(0) && (shape_quality<DIM>(det, G) < kSliverQ || g_min < kShortEdge2)) {
         // left to darcy_refine_kernel (FP64 |det J|): no record, no pressure row here
         const int32_t k = atomicAdd(p.bad, 1);
         p.bad[4 + k] = int32_t(c);

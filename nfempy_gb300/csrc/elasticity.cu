@@ -138,7 +138,9 @@ __device__ __forceinline__ T inverse_det(const T (&J)[3][3], T (&g)[12]) {
 
 // Badly shaped cells in FP32: det J and J^-1 from FP32 edges carry a
 // relative error of a few ulps over the shape quality q = |det J| /
-// (|e_0| |e_1| |e_2|); cells with q < 0.1 take both in FP64, from the FP64
+// (|e_0| |e_1| |e_2|), and an edge shorter than 2^20 units of the
+// fixed-point records a relative error above 2^-21 from their rounding;
+// cells with q < 0.1 or such an edge take both in FP64, from the FP64
 // points when the caller passed them, else from the fixed-point records'
 // exact integer differences, rounded to FP32 once at the end.
 constexpr float kElasSliverQ = 0.1f;
@@ -184,7 +186,9 @@ __global__ void elas_geom_kernel(const ElasParams p) {
       const T n1 = J[0][1] * J[0][1] + J[1][1] * J[1][1] + J[2][1] * J[2][1];
       const T n2 = J[0][2] * J[0][2] + J[1][2] * J[1][2] + J[2][2] * J[2][2];
       const T q = (det < T(0) ? -det : det) * rsqrtf(n0) * rsqrtf(n1) * rsqrtf(n2);
-      if (q < T(kElasSliverQ)) det = refine_inverse(p, int32_t(c), g);
+      const float s = packed_lo_scale(p.split) * 1048576.0f;  // 2^20 units
+      const T n_min = fminf(n0, fminf(n1, n2));
+      if (q < T(kElasSliverQ) || n_min < s * s) det = refine_inverse(p, int32_t(c), g);
     }
     if (!(det != T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
     const T adet = det < T(0) ? -det : det;
