@@ -120,6 +120,44 @@ __device__ __forceinline__ void cos_edges<float>(const CosParams& p, int32_t c, 
   }
 }
 
+template <typename T>
+__device__ __forceinline__ T cos_det(const T (&J)[3][3]) {
+  return J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+}
+
+// Badly shaped cells in FP32: det J from FP32 edges carries a relative error
+// of a few ulps over the shape quality q = |det J| / (|e_0| |e_1| |e_2|), and
+// an edge shorter than 2^20 units of the fixed-point records a relative error
+// above 2^-21 from their rounding; cells with q < 0.1 or such an edge take J
+// and det J in FP64, from the FP64 points when the caller passed them, else
+// from the fixed-point records' exact integer differences, rounded to FP32
+// once at the end.
+constexpr float kCosSliverQ = 0.1f;
+
+__device__ __noinline__ float cos_refine(const CosParams& p, int32_t c, float (&Jf)[3][3]) {
+  double J[3][3];
+  if (p.points) {
+    cos_edges<double>(p, c, J);
+  } else {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(p.cv) + c);
+    const double s = double(packed_lo_scale(p.split));
+    const float4 r0 = packed_point(p.split, v.x);
+    const float4 r[3] = {packed_point(p.split, v.y), packed_point(p.split, v.z), packed_point(p.split, v.w)};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      J[0][k] = double(int64_t(__float_as_int(r[k].x)) - __float_as_int(r0.x)) * s;
+      J[1][k] = double(int64_t(__float_as_int(r[k].y)) - __float_as_int(r0.y)) * s;
+      J[2][k] = double(int64_t(__float_as_int(r[k].z)) - __float_as_int(r0.z)) * s;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) Jf[i][k] = float(J[i][k]);
+  return float(cos_det<double>(J));
+}
+
 // Per-cell geometry once per cell (each cell is read by the rows of its ten
 // nodes): J, |det J| and the orientation mask.
 template <typename T>
@@ -129,8 +167,15 @@ __global__ void cos_geom_kernel(const CosParams p) {
        c += int64_t(gridDim.x) * blockDim.x) {
     T J[3][3];
     cos_edges<T>(p, int32_t(c), J);
-    const T det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                  J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    T det = cos_det<T>(J);
+    if constexpr (sizeof(T) == 4) {
+      const T n0 = J[0][0] * J[0][0] + J[1][0] * J[1][0] + J[2][0] * J[2][0];
+      const T n1 = J[0][1] * J[0][1] + J[1][1] * J[1][1] + J[2][1] * J[2][1];
+      const T n2 = J[0][2] * J[0][2] + J[1][2] * J[1][2] + J[2][2] * J[2][2];
+      const T q = (det < T(0) ? -det : det) * rsqrtf(n0) * rsqrtf(n1) * rsqrtf(n2);
+      const float s = packed_lo_scale(p.split) * 1048576.0f;  // 2^20 units
+      if (q < T(kCosSliverQ) || fminf(n0, fminf(n1, n2)) < s * s) det = cos_refine(p, int32_t(c), J);
+    }
     if (!(det != T(0))) set_status(p.status, NFEM_ERR_DEGENERATE);
     T g[12];
 #pragma unroll

@@ -37,8 +37,8 @@ def test_cosserat_matches_oracle(cuda_lib, dtype, tol, n, rows):
         autotune.reset_knobs()
 
 
-def _check_cosserat(dtype, tol, n):
-    m = mesh_gen.cube(n)
+def _check_cosserat(dtype, tol, n, mesh=None):
+    m = mesh_gen.cube(n) if mesh is None else mesh
     sp = product_space(m, FIELDS)
     topo = topology.Topology(m)
     cd, nd = topology.cell_dofs(topo, [topology.FieldSpec(*f) for f in FIELDS])
@@ -68,6 +68,24 @@ def _check_cosserat(dtype, tol, n):
     assert row_scaled_err(Ag, Ao) <= tol
     rg = res.double().cpu().numpy()
     assert np.abs(rg - ro).max() <= tol * np.abs(ro).max()
+
+
+@pytest.mark.parametrize("flat", [1 / 512, 1 / 4096])
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
+def test_cosserat_badly_shaped_cells(cuda_lib, flat, dtype, tol):
+    """Flat tetrahedra in general orientation (shape quality ~ flat): the
+    FP32 geometry pass takes J and det J of such cells in FP64 from the
+    points.  Against the FP64 oracle at the usual tolerance, except that FP64
+    is held to max(1e-12, 10 ulp / q_min): the oracle's own det J is only
+    that accurate there."""
+    from tests.test_gpu_darcy import _badly_shaped
+    m = _badly_shaped("cube", 2, flat)
+    E = m["points"][m["blocks"][-1][1]]
+    E = E[:, 1:] - E[:, :1]
+    q = np.abs(np.linalg.det(E)) / np.prod(np.linalg.norm(E, axis=2), axis=1)
+    if dtype == torch.float64:
+        tol = max(tol, 10 * 2.0 ** -53 / q.min())
+    _check_cosserat(dtype, tol, 2, mesh=m)
 
 
 @pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
